@@ -1,0 +1,348 @@
+// Test infrastructure only (oracle): a driver that links the reference's own
+// compiled classes (XSLAE / XOperator / XSpace / XSpaceModel / XGrid /
+// XSeparator / XImmersedBoundary / XProblem) and runs them on inputs written
+// by tests/golden/make_golden.py, so that golden vectors come from the
+// reference itself rather than from a restatement.
+//
+// Usage: ref_driver <task> <input.bin> <output.bin>
+//   task = matvec | solve | thomas | ib | poisson
+//
+// File format (both directions): a sequence of records
+//   char name[32]; char kind ('d' double / 'i' int32); int64 count; data[count]
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <map>
+#include <string>
+#include <vector>
+#include <stdexcept>
+
+#include "XSLAE.h"
+#include "XOperator.h"
+#include "XSpace.h"
+#include "XSpaceModel.h"
+#include "XGrid.h"
+#include "XSeparator.h"
+#include "XMask.h"
+#include "XProblem.h"
+#include "XImmersedBoundary.h"
+
+struct Rec { char kind; std::vector<double> d; std::vector<int> i; };
+typedef std::map<std::string, Rec> Bag;
+
+static Bag read_bag(const char* path) {
+  Bag bag;
+  FILE* f = fopen(path, "rb");
+  if (!f) throw std::runtime_error("cannot open input");
+  char name[33];
+  while (fread(name, 1, 32, f) == 32) {
+    name[32] = 0;
+    char kind; long long n;
+    if (fread(&kind, 1, 1, f) != 1 || fread(&n, 8, 1, f) != 1) throw std::runtime_error("bad record");
+    Rec r; r.kind = kind;
+    if (kind == 'd') { r.d.resize(n); if (n && fread(r.d.data(), 8, n, f) != (size_t)n) throw std::runtime_error("short d"); }
+    else { r.i.resize(n); if (n && fread(r.i.data(), 4, n, f) != (size_t)n) throw std::runtime_error("short i"); }
+    bag[std::string(name)] = r;
+  }
+  fclose(f);
+  return bag;
+}
+
+struct Writer {
+  FILE* f;
+  explicit Writer(const char* p) { f = fopen(p, "wb"); if (!f) throw std::runtime_error("cannot open output"); }
+  ~Writer() { fclose(f); }
+  void hdr(const char* name, char kind, long long n) {
+    char b[32]; memset(b, 0, 32); strncpy(b, name, 31);
+    fwrite(b, 1, 32, f); fwrite(&kind, 1, 1, f); fwrite(&n, 8, 1, f);
+  }
+  void d(const char* name, const std::vector<double>& v) { hdr(name, 'd', v.size()); if (!v.empty()) fwrite(v.data(), 8, v.size(), f); }
+  void i(const char* name, const std::vector<int>& v) { hdr(name, 'i', v.size()); if (!v.empty()) fwrite(v.data(), 4, v.size(), f); }
+  void s(const char* name, double x) { d(name, std::vector<double>(1, x)); }
+  void n(const char* name, int x) { i(name, std::vector<int>(1, x)); }
+};
+
+static const std::vector<double>& D(Bag& b, const char* k) {
+  Bag::iterator it = b.find(k);
+  if (it == b.end()) { fprintf(stderr, "missing %s\n", k); throw std::runtime_error("missing record"); }
+  return it->second.d;
+}
+static const std::vector<int>& I(Bag& b, const char* k) {
+  Bag::iterator it = b.find(k);
+  if (it == b.end()) { fprintf(stderr, "missing %s\n", k); throw std::runtime_error("missing record"); }
+  return it->second.i;
+}
+
+// ---------------------------------------------------------------------------
+// Grid + space model exactly as XProblem.cpp:3989-4049 (BuildLocalGrid) and
+// XProblem.cpp:4116-4207 (LocalPrepareVariables) build them.
+struct Setup {
+  int n1, n2, n3;
+  T3dNormalGrid* grid;
+  int model;
+  std::vector<double> hx, hy, hz;
+};
+
+static Setup build(Bag& b, int modelName) {
+  Setup s;
+  const std::vector<int>& dims = I(b, "dims");
+  s.n1 = dims[0]; s.n2 = dims[1]; s.n3 = dims[2];
+  const std::vector<double>& X = D(b, "x_nodes");
+  const std::vector<double>& Y = D(b, "y_nodes");
+  const std::vector<double>& Z = D(b, "z_nodes");
+  TSeparator* sep1 = new TRandomSeparator(s.n1, X.data());
+  TSeparator* sep2 = new TRandomSeparator(s.n2, Y.data());
+  TSeparator* sep3 = new TRandomSeparator(s.n3, Z.data());
+  const std::vector<int>& codes = I(b, "codes");
+  const std::vector<double>& nrm = D(b, "normals");
+  T3dNumberMask& mask = *(new T3dNumberMask(s.n1, s.n2, s.n3));
+  T3dVector**** normals = new T3dVector***[s.n1];
+  for (int i = 0; i < s.n1; i++) {
+    normals[i] = new T3dVector**[s.n2];
+    for (int j = 0; j < s.n2; j++) {
+      normals[i][j] = new T3dVector*[s.n3];
+      for (int k = 0; k < s.n3; k++) {
+        size_t c = ((size_t)i * s.n2 + j) * s.n3 + k;
+        mask[i][j][k] = codes[c];
+        T3dVector* nv = NULL;
+        if (nrm[3 * c] != 0 || nrm[3 * c + 1] != 0 || nrm[3 * c + 2] != 0) {
+          nv = new T3dVector; nv->X = nrm[3 * c]; nv->Y = nrm[3 * c + 1]; nv->Z = nrm[3 * c + 2];
+        }
+        normals[i][j][k] = nv;
+      }
+    }
+  }
+  s.grid = new T3dNormalGrid(sep1, sep2, sep3, mask, normals);
+  for (int q = 0; q < s.n1 - 1; q++) s.hx.push_back(s.grid->GetSeparator1().Separation[q]);
+  for (int q = 0; q < s.n2 - 1; q++) s.hy.push_back(s.grid->GetSeparator2().Separation[q]);
+  for (int q = 0; q < s.n3 - 1; q++) s.hz.push_back(s.grid->GetSeparator3().Separation[q]);
+
+  // Space mask: grid codes -> {0,1} as XProblem.cpp:4155-4182.
+  T3dNumberMask& spaceMask = s.grid->GetMask().Copy();
+  for (int i = 0; i < s.n1; i++)
+    for (int j = 0; j < s.n2; j++)
+      for (int k = 0; k < s.n3; k++) {
+        int m = spaceMask[i][j][k];
+        if (m == TActualPoint || m == TFictivePoint) spaceMask[i][j][k] = m;
+        else if (m == TDefinedBorderPoint || m == TEquationBorderPoint) spaceMask[i][j][k] = TFictivePoint;
+        else spaceMask[i][j][k] = TActualPoint;
+      }
+  TMask** masks = new TMask*[1];
+  masks[0] = &spaceMask;
+  TRnRelease3dSpaceModel* model = new TRnRelease3dSpaceModel(1, masks);
+  TRnSpace::AddModel(modelName, model, false);
+  s.model = modelName;
+  return s;
+}
+
+static TRnRelease3dSpace& vec_from(Setup& s, const std::vector<double>& v) {
+  TRnRelease3dSpace& x = *(new TRnRelease3dSpace(s.model));
+  for (int i = 0; i < s.n1; i++)
+    for (int j = 0; j < s.n2; j++)
+      for (int k = 0; k < s.n3; k++) x[i][j][k] = v[((size_t)i * s.n2 + j) * s.n3 + k];
+  return x;
+}
+static std::vector<double> vec_to(Setup& s, TRnRelease3dSpace& x) {
+  std::vector<double> v((size_t)s.n1 * s.n2 * s.n3);
+  for (int i = 0; i < s.n1; i++)
+    for (int j = 0; j < s.n2; j++)
+      for (int k = 0; k < s.n3; k++) v[((size_t)i * s.n2 + j) * s.n3 + k] = x[i][j][k];
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+static void task_matvec(Bag& b, Writer& w) {
+  Setup s = build(b, 11);
+  w.d("hx", s.hx); w.d("hy", s.hy); w.d("hz", s.hz);
+  TRnRelease3dSpace& x = vec_from(s, D(b, "x"));
+  TRnRelease3dSpace& sv = vec_from(s, D(b, "s"));
+  TRnRelease3dSpace& rho = vec_from(s, D(b, "density"));
+  TNodesGrid** grids = new TNodesGrid*[1]; grids[0] = s.grid;
+  T3dLaplaceOperator& A = *(new T3dLaplaceOperator(s.model, 1, grids));
+  T3dVariableDivergentedOperator& V = *(new T3dVariableDivergentedOperator(s.model, 1, grids));
+  V.withDensity(rho);
+  const std::vector<double>& yinit = D(b, "y_init");
+
+  // a6 / a10: y |= A(x), A(x)+s, A(x)-s (inactive cells keep y_init)
+  { TRnRelease3dSpace& y = vec_from(s, yinit); y |= ((TRnLinearOperator&)A)(x); w.d("lap_y", vec_to(s, y)); delete &y; }
+  { TRnRelease3dSpace& y = vec_from(s, yinit); y |= ((TRnLinearOperator&)A)(x) + sv; w.d("lap_y_plus", vec_to(s, y)); delete &y; }
+  { TRnRelease3dSpace& y = vec_from(s, yinit); y |= ((TRnLinearOperator&)A)(x) - sv; w.d("lap_y_minus", vec_to(s, y)); delete &y; }
+  // a7
+  // (only on grids whose PreNormal rows lie off the box faces: on the faces
+  // the reference's PreNormal branch reads outside its separation and density
+  // arrays, XOperator.cpp:2104-2130, 2211-2213)
+  if (b.count("vardiv")) { TRnRelease3dSpace& y = vec_from(s, yinit); y |= ((TRnLinearOperator&)V)(x); w.d("vd_y", vec_to(s, y)); delete &y; }
+  // a11: masked linear combinations
+  double p1 = D(b, "p1")[0], p2 = D(b, "p2")[0];
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z |= p1 * x + p2 * sv; w.d("lc_p1x_p2s", vec_to(s, z)); delete &z; }
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z |= x - sv; w.d("lc_x_minus_s", vec_to(s, z)); delete &z; }
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z |= x + p2 * sv; w.d("lc_x_p2s", vec_to(s, z)); delete &z; }
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z |= p1 * x; w.d("lc_p1x", vec_to(s, z)); delete &z; }
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z |= 0; w.d("lc_zero", vec_to(s, z)); delete &z; }
+  { TRnRelease3dSpace& z = vec_from(s, yinit); z.Assign(x); w.d("assign_x", vec_to(s, z)); delete &z; }
+  // a12: reductions
+  w.s("dot_xs", (x, sv));
+  w.s("norm_x", x.Norma(0));
+  w.s("dot_x_As", (x, ((TRnLinearOperator&)A)(sv)));
+  { int idx = -7; double m = x.GetAbsMaxElement(idx); w.s("absmax_x", m); w.n("absmax_x_index", idx); }
+  { int idx = -7; double m = sv.GetAbsMaxElement(idx); w.s("absmax_s", m); w.n("absmax_s_index", idx); }
+  { int idx = -7; double m = x.GetAbsMinElement(idx); w.s("absmin_x", m); w.n("absmin_x_index", idx); }
+  // a14: Rn numbering
+  int R = x.EndIndex;
+  w.n("end_index", R);
+  std::vector<int> fwd; fwd.reserve(3 * R);
+  std::vector<double> rn_vals; rn_vals.reserve(R);
+  for (int rn = 1; rn <= R; rn++) rn_vals.push_back(((TRnSpace&)x)[rn]);
+  w.d("x_by_rn", rn_vals);
+  delete &V; delete &A; delete &x; delete &sv; delete &rho;
+}
+
+// ---------------------------------------------------------------------------
+// Krylov solves through the reference TSLAE (XSLAE.cpp). op = 0 Laplace,
+// 1 variable-density; method = 0 CG, 1 BiCGStab, 2 MinRes.
+static void task_solve(Bag& b, Writer& w) {
+  Setup s = build(b, 21);
+  TNodesGrid** grids = new TNodesGrid*[1]; grids[0] = s.grid;
+  int op = I(b, "op")[0], method = I(b, "method")[0];
+  TRnRelease3dSpace& x = vec_from(s, D(b, "x0"));
+  TRnRelease3dSpace& rhs = vec_from(s, D(b, "b"));
+  T3dLaplaceOperator* A;
+  if (op == 0) A = new T3dLaplaceOperator(s.model, 1, grids);
+  else {
+    T3dVariableDivergentedOperator* V = new T3dVariableDivergentedOperator(s.model, 1, grids);
+    TRnRelease3dSpace& rho = vec_from(s, D(b, "density"));
+    V->withDensity(rho);
+    A = V;
+  }
+  TSLAE* slae = new TSLAE(*A, x, rhs);
+  if (method == 0) slae->SolveByConjugateGradients();
+  else if (method == 1) slae->SolveByBiConjugateGradientsStab();
+  else slae->SolveByMinimalResiduals();
+  TRnRelease3dSpace& res = dynamic_cast<TRnRelease3dSpace&>(const_cast<TRnSpace&>((const TRnSpace&)slae->Result));
+  w.d("result", vec_to(s, res));
+  // The residual the reference's own stopping rule sees, recomputed here.
+  TRnRelease3dSpace& r = *(new TRnRelease3dSpace(s.model));
+  r |= ((TRnLinearOperator&)*A)(res) - rhs;
+  w.s("resid_l2", r.Norma(0));
+  w.s("resid_inf", r.GetAbsMaxElement());
+}
+
+// ---------------------------------------------------------------------------
+// a5: TSLAE::SolveByScalarRunning on a batch of lines.
+static void task_thomas(Bag& b, Writer& w) {
+  int nl = I(b, "nlines")[0], M = I(b, "M")[0];
+  std::vector<double> u = D(b, "u");
+  const std::vector<double>& a = D(b, "a"), &bb = D(b, "b"), &c = D(b, "c"), &f = D(b, "f");
+  for (int l = 0; l < nl; l++) {
+    size_t o = (size_t)l * (M + 1);
+    TSLAE::SolveByScalarRunning(M, &u[o], &a[o], &bb[o], &c[o], &f[o]);
+  }
+  w.d("u", u);
+}
+
+// ---------------------------------------------------------------------------
+// a17-a19: the reference's IB driver methods, reached through a subclass that
+// only widens access.  No Initialize(): the boundary is assembled here.
+class IBProbe : public TImmersedBoundaryProblem {
+ public:
+  IBProbe(double tEnd, double tau) : TImmersedBoundaryProblem(tEnd, tau, 100.0, 1.0) {
+    fTimeSeparator = new TUniformSeparator(0, tEnd, tau);  // as THydrodynamicsProblem::Initialize
+  }
+  double step() { return fTimeSeparator->SeparationValue; }
+  virtual TMaskGenerator* CreateStatement() { return NULL; }
+  void setBoundary(TImmersedBoundary* bnd) { fBoundary = bnd; }
+  void interp(TRnRelease3dSpace& v, T3dNormalGrid* g, int axis) { Interpolate(v, g, axis, 1); }
+  void update(int axis) { UpdateBoundaryPosition(axis, 1); }
+  void forces(int axis) { ComputeBoundaryForces(axis, 1); }
+  void spread(TRnRelease3dSpace& f, T3dNormalGrid& gc, T3dNormalGrid* g, int axis) { SpreadForce(f, gc, g, axis, 1); }
+  ~IBProbe() {}
+};
+
+class ProbeBoundary : public TImmersedBoundary {
+ public:
+  double area;
+  double GetArea() { return area; }
+  double GetYCenter() { return 0; }
+  double GetZCenter() { return 0; }
+};
+
+static void task_ib(Bag& b, Writer& w) {
+  Setup s = build(b, 31);
+  double tau = D(b, "tau")[0];
+  IBProbe* P = new IBProbe(1000 * tau, tau);
+  const std::vector<double>& pos = D(b, "pos");      // 3*n
+  const std::vector<double>& ref = D(b, "ref");      // 3*n
+  const std::vector<int>& kind = I(b, "kind");       // 0 elastic, 1 target, 2 fixed-elastic, 3 plain
+  const std::vector<int>& nxt = I(b, "next");        // -1 none
+  const std::vector<int>& prv = I(b, "prev");
+  const std::vector<double>& d0 = D(b, "dist0");
+  const std::vector<double>& curv0 = D(b, "curv0");  // 3*n
+  const std::vector<double>& kst = D(b, "node_stiff");
+  const std::vector<double>& prm = D(b, "params");   // stiffness, stretching, bending, area
+  int n = (int)kind.size();
+  ProbeBoundary* B = new ProbeBoundary();
+  B->stiffness = prm[0]; B->stretchingStiffness = prm[1]; B->bendingStiffness = prm[2]; B->area = prm[3];
+  B->nodesCount = n;
+  B->nodes = new TNode*[n];
+  for (int q = 0; q < n; q++) {
+    TNode* nd;
+    if (kind[q] == 0) nd = new TElasticNode();
+    else if (kind[q] == 1) nd = new TTargetNode();
+    else if (kind[q] == 2) nd = new TFixedElasticNode();
+    else nd = new TNode();
+    nd->x = pos[3 * q]; nd->y = pos[3 * q + 1]; nd->z = pos[3 * q + 2];
+    nd->xRef = ref[3 * q]; nd->yRef = ref[3 * q + 1]; nd->zRef = ref[3 * q + 2];
+    nd->TNode::type = ELASTIC_NODE;  // never FIXED here: the mask side effect is not part of the arithmetic
+    nd->stretchingStiffness = kst[q];
+    nd->boundary = B;
+    nd->neighbors.initialDistanceNext = d0[q];
+    nd->neighbors.initialCurvatures[OX] = curv0[3 * q];
+    nd->neighbors.initialCurvatures[OY] = curv0[3 * q + 1];
+    nd->neighbors.initialCurvatures[OZ] = curv0[3 * q + 2];
+    B->nodes[q] = nd;
+  }
+  for (int q = 0; q < n; q++) {
+    B->nodes[q]->neighbors.next = nxt[q] >= 0 ? B->nodes[nxt[q]] : NULL;
+    B->nodes[q]->neighbors.prev = prv[q] >= 0 ? B->nodes[prv[q]] : NULL;
+  }
+  P->setBoundary(B);
+  w.s("tau_eff", P->step());
+  TRnRelease3dSpace& vel = vec_from(s, D(b, "velocity"));
+  int axis = I(b, "axis")[0];
+  // GetForce order (XProblem.cpp:8350-8353): interpolate, move, forces, spread.
+  P->interp(vel, s.grid, axis);
+  std::vector<double> vout(n);
+  for (int q = 0; q < n; q++) vout[q] = axis == 1 ? B->nodes[q]->xVel : axis == 2 ? B->nodes[q]->yVel : B->nodes[q]->zVel;
+  w.d("node_vel", vout);
+  P->update(axis);
+  std::vector<double> pout(3 * n);
+  for (int q = 0; q < n; q++) { pout[3 * q] = B->nodes[q]->x; pout[3 * q + 1] = B->nodes[q]->y; pout[3 * q + 2] = B->nodes[q]->z; }
+  w.d("pos_after", pout);
+  P->forces(axis);
+  std::vector<double> fout(n);
+  for (int q = 0; q < n; q++) fout[q] = axis == 1 ? B->nodes[q]->xForce : axis == 2 ? B->nodes[q]->yForce : B->nodes[q]->zForce;
+  w.d("node_force", fout);
+  TRnRelease3dSpace& force = *(new TRnRelease3dSpace(s.model));
+  P->spread(force, *s.grid, s.grid, axis);
+  w.d("force_box", vec_to(s, force));
+}
+
+int main(int argc, char** argv) {
+  if (argc != 4) { fprintf(stderr, "usage: ref_driver task in out\n"); return 2; }
+  try {
+    Bag b = read_bag(argv[2]);
+    Writer w(argv[3]);
+    std::string t = argv[1];
+    if (t == "matvec") task_matvec(b, w);
+    else if (t == "solve") task_solve(b, w);
+    else if (t == "thomas") task_thomas(b, w);
+    else if (t == "ib") task_ib(b, w);
+    else { fprintf(stderr, "unknown task\n"); return 2; }
+  } catch (const char* e) {
+    fprintf(stderr, "reference threw: %s\n", e); return 3;
+  } catch (std::exception& e) {
+    fprintf(stderr, "driver error: %s\n", e.what()); return 4;
+  }
+  return 0;
+}

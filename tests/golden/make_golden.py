@@ -1,0 +1,236 @@
+"""Regenerate the golden fixtures in this folder from the reference itself.
+
+Test infrastructure only.  Builds oracle/_ref/ref_driver (the reference's own
+XSLAE/XOperator/XSpace/... sources compiled in place by oracle/Makefile), feeds
+it seeded inputs and stores inputs + outputs as .npz files here.  Needs the
+reference tree (REF, default /root/reference); the fixtures it writes are what
+the tests read, so the tests themselves never need the reference.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.bagio import read_bag, write_bag  # noqa: E402
+from xflow_gb300 import workloads as wl  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def run(task, rec):
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        write_bag(fin, rec)
+        if os.environ.get("XF_KEEP_INPUT"):
+            write_bag(os.environ["XF_KEEP_INPUT"], rec)
+        p = subprocess.run([DRIVER, task, fin, fout], capture_output=True, text=True, timeout=300)
+        if p.returncode != 0:
+            return None, p.stderr.strip()
+        return read_bag(fout), None
+
+
+def grid_rec(codes, nrm, nodes):
+    n1, n2, n3 = codes.shape
+    return {
+        "dims": np.array([n1, n2, n3], np.int32),
+        "x_nodes": nodes[0], "y_nodes": nodes[1], "z_nodes": nodes[2],
+        "codes": codes.astype(np.int32).ravel(),
+        "normals": nrm.reshape(-1),
+    }
+
+
+def matvec_case(name, codes, nrm, nodes, seed, vardiv=False):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = codes.shape
+    x = rng.standard_normal(shape)
+    s = rng.standard_normal(shape)
+    # A tie for the abs-max: the first cell in i->j->k order must win.
+    act = np.argwhere(wl.space_mask(codes) == 1)
+    a, b = act[len(act) // 3], act[2 * len(act) // 3]
+    x[tuple(a)], x[tuple(b)] = -7.5, 7.5
+    rho = rng.uniform(0.5, 2.0, shape)
+    y0 = rng.standard_normal(shape)
+    rec = grid_rec(codes, nrm, nodes)
+    rec.update({"x": x.ravel(), "s": s.ravel(), "density": rho.ravel(), "y_init": y0.ravel(),
+                "p1": np.array([0.75]), "p2": np.array([-1.25])})
+    if vardiv:
+        rec["vardiv"] = np.array([1], np.int32)
+    out, err = run("matvec", rec)
+    if out is None:
+        raise RuntimeError(f"{name}: {err}")
+    inv = np.zeros(codes.size, np.int32)
+    sm = wl.space_mask(codes).ravel().astype(bool)
+    inv[sm] = np.arange(1, sm.sum() + 1)
+    save = dict(codes=codes, normals=nrm, x_nodes=nodes[0], y_nodes=nodes[1], z_nodes=nodes[2],
+                x=x, s=s, density=rho, y_init=y0, p1=0.75, p2=-1.25)
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, f"matvec_{name}.npz"), **save)
+    print(f"matvec_{name}: end_index={out['end_index'][0]} absmax={out['absmax_x'][0]} idx={out['absmax_x_index'][0]}")
+
+
+def error_case(name, codes, nrm, nodes):
+    """Inputs the reference rejects with a throw (bad codes / normals)."""
+    shape = codes.shape
+    rec = grid_rec(codes, nrm, nodes)
+    z = np.zeros(shape).ravel()
+    rec.update({"x": z, "s": z, "density": z + 1, "y_init": z, "p1": np.array([1.0]), "p2": np.array([1.0])})
+    out, err = run("matvec", rec)
+    return err
+
+
+def solve_case(name, codes, nrm, nodes, op, method, b, x0, rho=None):
+    rec = grid_rec(codes, nrm, nodes)
+    rec.update({"op": np.array([op], np.int32), "method": np.array([method], np.int32),
+                "x0": x0.ravel(), "b": b.ravel()})
+    if rho is not None:
+        rec["density"] = rho.ravel()
+    out, err = run("solve", rec)
+    if out is None:
+        raise RuntimeError(f"{name}: {err}")
+    save = dict(codes=codes, normals=nrm, x_nodes=nodes[0], y_nodes=nodes[1], z_nodes=nodes[2],
+                op=op, method=method, b=b, x0=x0)
+    if rho is not None:
+        save["density"] = rho
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **save)
+    print(f"solve_{name}: resid_l2={out['resid_l2'][0]:.3e} resid_inf={out['resid_inf'][0]:.3e}")
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True,
+                   stdout=subprocess.DEVNULL)
+    rng = np.random.Generator(np.random.PCG64(2024))
+
+    # --- operator / vector-algebra / numbering fixtures ---------------------
+    for name, shape, seed in (("mixed_a", (12, 11, 10), 11), ("mixed_b", (17, 9, 14), 12)):
+        codes, nrm = wl.mixed_grid(*shape, seed=seed)
+        nodes = [wl.random_nodes(n, rng) for n in shape]
+        matvec_case(name, codes, nrm, nodes, seed + 100)
+    for name, shape, seed in (("vardiv_a", (11, 12, 13), 21), ("vardiv_b", (9, 16, 10), 22)):
+        codes, nrm = wl.mixed_grid(*shape, seed=seed, face_prenormal=False, interior_rows=12)
+        nodes = [wl.random_nodes(n, rng) for n in shape]
+        matvec_case(name, codes, nrm, nodes, seed + 100, vardiv=True)
+    codes, nrm = wl.poisson_cube(10, 10, 10)
+    nodes = [wl.uniform_nodes(-1 / 16, 1 + 1 / 16, 1 / 8)[0]] * 3
+    matvec_case("poisson_cube", codes, nrm, nodes, 7)
+
+    # --- inputs the reference rejects ----------------------------------------
+    errs = {}
+    codes, nrm = wl.mixed_grid(8, 8, 8, seed=5)
+    nodes = [wl.random_nodes(8, rng) for _ in range(3)]
+    c2 = codes.copy(); c2[3, 3, 3] = wl.NORMAL
+    errs["normal_code_active"] = (c2, nrm)
+    c2 = codes.copy(); c2[4, 4, 4] = 2
+    errs["unknown_code"] = (c2, nrm)
+    c2 = codes.copy(); n2 = nrm.copy()
+    face = np.argwhere(codes[0] == wl.PREDEFINED)
+    if len(face):
+        j, k = face[0]
+        n2[0, j, k] = (-1.0, 0.5, 0.0)
+        errs["predefined_oblique_normal"] = (c2, n2)
+    face = np.argwhere(codes[0] == wl.PRENORMAL)
+    if len(face):
+        j, k = face[0]
+        n2 = nrm.copy(); n2[0, j, k] = 0.0
+        errs["prenormal_no_normal"] = (c2, n2)
+    rec = {}
+    for name, (c, n) in errs.items():
+        err = error_case(name, c, n, nodes)
+        rec[name + "_codes"] = c
+        rec[name + "_normals"] = n
+        rec[name + "_threw"] = err is not None
+        print(f"error case {name}: {err}")
+    rec["x_nodes"], rec["y_nodes"], rec["z_nodes"] = nodes
+    np.savez_compressed(os.path.join(HERE, "errors.npz"), **rec)
+
+    # --- solver fixtures -------------------------------------------------------
+    # SPD system: uniform Neumann box with one Defined (pinned) cell holding 0.
+    # (Non-uniform spacings make the flux-form operator nonsymmetric.)
+    shape = (11, 10, 9)
+    codes, nrm = wl.neumann_box(*shape)
+    codes[5, 5, 4] = wl.DEFINED
+    nodes = [wl.uniform_nodes(-0.05, 1.05, 0.1)[0][:n] for n in shape]
+    b = np.where(codes == wl.ACTUAL, rng.standard_normal(shape), 0.0)
+    x0 = np.zeros(shape)
+    solve_case("cg_spd", codes, nrm, nodes, 0, 0, b, x0)
+    solve_case("minres_spd", codes, nrm, nodes, 0, 2, b, x0)
+    # Time-loop style nonsymmetric system (Dirichlet semi-sum rows) by BiCGStab,
+    # warm-started from a nonzero x0.
+    codes, nrm = wl.poisson_cube(10, 9, 11)
+    nodes = [wl.random_nodes(n, rng) for n in codes.shape]
+    sm = wl.space_mask(codes).astype(bool)
+    b = np.where(sm, rng.standard_normal(codes.shape), 0.0)
+    x0 = np.where(sm, 0.1 * rng.standard_normal(codes.shape), 0.0)
+    solve_case("bicgstab_cube", codes, nrm, nodes, 0, 1, b, x0)
+    # Variable density: PreNormal rows off the faces (see matvec fixtures).
+    codes, nrm = wl.mixed_grid(10, 9, 11, seed=31, face_prenormal=False)
+    nodes = [wl.random_nodes(n, rng) for n in codes.shape]
+    sm = wl.space_mask(codes).astype(bool)
+    b = np.where(sm, rng.standard_normal(codes.shape), 0.0)
+    x0 = np.where(sm, 0.1 * rng.standard_normal(codes.shape), 0.0)
+    rho = rng.uniform(0.8, 1.25, codes.shape)
+    solve_case("bicgstab_vardiv", codes, nrm, nodes, 1, 1, b, x0, rho)
+
+    # --- Thomas lines (TSLAE::SolveByScalarRunning) ---------------------------
+    nl, M = 7, 12
+    a = rng.uniform(-1, 0, (nl, M + 1))
+    c = rng.uniform(-1, 0, (nl, M + 1))
+    bb = 2.5 + rng.uniform(0, 1, (nl, M + 1))
+    f = rng.standard_normal((nl, M + 1))
+    u = rng.standard_normal((nl, M + 1))
+    out, err = run("thomas", {"nlines": np.array([nl], np.int32), "M": np.array([M], np.int32),
+                              "u": u, "a": a, "b": bb, "c": c, "f": f})
+    if out is None:
+        raise RuntimeError(err)
+    np.savez_compressed(os.path.join(HERE, "thomas.npz"), u0=u, a=a, b=bb, c=c, f=f,
+                        M=M, ref_u=out["u"].reshape(nl, M + 1))
+    print("thomas ok")
+
+    # --- immersed boundary (interpolate, move, forces, spread) ----------------
+    n = 20
+    shape = (n, n, n)
+    hx = 1.0 / (n - 2)
+    nodes1 = np.array([i * hx for i in range(n)])
+    codes, nrm = wl.neumann_box(*shape)
+    nn = 14
+    th = np.linspace(0, 2 * np.pi, nn, endpoint=False)
+    pos = np.stack([0.5 + 0.2 * np.cos(th), 0.5 + 0.2 * np.sin(th), 0.45 + 0.05 * np.sin(2 * th)], 1)
+    pos += 0.01 * rng.standard_normal(pos.shape)
+    ref = pos + 0.02 * rng.standard_normal(pos.shape)
+    kind = np.array([(0, 1, 2, 3)[q % 4] for q in range(nn)], np.int32)
+    nxt = np.array([(q + 1) if q < nn - 1 else -1 for q in range(nn)], np.int32)
+    prv = np.array([(q - 1) if q > 0 else -1 for q in range(nn)], np.int32)
+    d0 = np.array([np.linalg.norm(pos[q] - pos[nxt[q]]) * 0.9 if nxt[q] >= 0 else 0.0 for q in range(nn)])
+    curv0 = 0.01 * rng.standard_normal((nn, 3))
+    kst = rng.uniform(50, 150, nn)
+    params = np.array([30.0, 1000.0, 5.0, 4 * np.pi * 0.04 / nn])
+    vel = rng.standard_normal(shape)
+    tau = 1e-3
+    for axis in (1, 2, 3):
+        rec = grid_rec(codes, nrm, [nodes1] * 3)
+        rec.update({"tau": np.array([tau]), "pos": pos.ravel(), "ref": ref.ravel(), "kind": kind,
+                    "next": nxt, "prev": prv, "dist0": d0, "curv0": curv0.ravel(), "node_stiff": kst,
+                    "params": params, "velocity": vel.ravel(), "axis": np.array([axis], np.int32)})
+        out, err = run("ib", rec)
+        if out is None:
+            raise RuntimeError(err)
+        np.savez_compressed(os.path.join(HERE, f"ib_axis{axis}.npz"), codes=codes, nodes=nodes1, tau=tau,
+                            pos=pos, ref=ref, kind=kind, next=nxt, prev=prv, dist0=d0, curv0=curv0,
+                            node_stiff=kst, params=params, velocity=vel, axis=axis,
+                            **{"ref_" + k: v for k, v in out.items()})
+        print(f"ib axis {axis}: max|vel|={np.abs(out['node_vel']).max():.3e} "
+              f"max|F|={np.abs(out['node_force']).max():.3e} sum f={out['force_box'].sum():.3e}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+"""Synthetic grids and right-hand sides for the pressure-projection path.
+
+Every array follows the reference's box convention: a grid of N intervals per
+axis has N+1 nodes, arrays are indexed [i][j][k] with k fastest (C order), and
+the integer mask holds the reference's point codes
+  0 Fictive, 1 Actual (XMask.h:6-7), 3 Defined, 4 PreDefined, 5 Normal,
+  6 PreNormal, 7 Equation, 8 PreEquation (XOperator.h:13-18).
+Normals are float64 (n1, n2, n3, 3); all-zero means "no normal" (NULL in the
+reference's T3dVector**** table, XGrid.h:279-299).
+
+Inputs are made on the host with numpy's PCG64 so that the oracle and the GPU
+see bit-identical data.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+FICTIVE, ACTUAL, DEFINED, PREDEFINED, NORMAL, PRENORMAL, EQUATION, PREEQUATION = 0, 1, 3, 4, 5, 6, 7, 8
+
+
+def uniform_nodes(start: float, end: float, h: float):
+    """Node coordinates and separations of TUniformSeparator (XSeparator.cpp:25-64):
+    the step is shrunk so that the interval divides evenly."""
+    res = (end - start) / h
+    ipart = math.floor(res)
+    n = int(ipart)
+    if abs(res - ipart) > 1e-11:
+        n += 1
+    step = (end - start) / float(n)
+    dims = np.empty(n + 1)
+    dims[0] = start
+    for i in range(1, n):
+        dims[i] = dims[i - 1] + step
+    dims[n] = end
+    sep = np.full(n, step)
+    return dims, sep
+
+
+def space_mask(codes: np.ndarray) -> np.ndarray:
+    """Grid codes -> space mask {0,1} as XProblem.cpp:4155-4182."""
+    act = np.isin(codes, (ACTUAL, PREDEFINED, NORMAL, PRENORMAL, PREEQUATION))
+    return act.astype(np.uint8)
+
+
+def neumann_box(n1: int, n2: int, n3: int):
+    """Interior Actual, ghost layer Fictive (homogeneous Neumann walls)."""
+    codes = np.zeros((n1, n2, n3), np.int32)
+    codes[1:-1, 1:-1, 1:-1] = ACTUAL
+    return codes, np.zeros((n1, n2, n3, 3))
+
+
+def poisson_cube(n1: int, n2: int, n3: int):
+    """Mask codes and normals of the reference's verification grid
+    (T3dPoissonProblem, XProblem.cpp:431-519): PreDefined rows on the z faces
+    (PreNormal on their rim), PreNormal on the x and y faces."""
+    N, L, M = n1 - 1, n2 - 1, n3 - 1
+    codes = np.zeros((n1, n2, n3), np.int32)
+    nrm = np.zeros((n1, n2, n3, 3))
+    for i in range(n1):
+        for j in range(n2):
+            for k in range(n3):
+                if i not in (0, N) and j not in (0, L) and k not in (0, M):
+                    codes[i, j, k] = ACTUAL
+                    continue
+                inner_ij = i not in (0, N) and j not in (0, L)
+                if inner_ij and k in (0, M):
+                    rim = i in (1, N - 1) or j in (1, L - 1)
+                    codes[i, j, k] = PRENORMAL if rim else PREDEFINED
+                    nrm[i, j, k] = (0, 0, -1 if k == 0 else 1)
+                elif i in (0, N) and j not in (0, L) and k not in (0, M):
+                    codes[i, j, k] = PRENORMAL
+                    nrm[i, j, k] = (-1 if i == 0 else 1, 0, 0)
+                elif j in (0, L) and i not in (0, N) and k not in (0, M):
+                    codes[i, j, k] = PRENORMAL
+                    nrm[i, j, k] = (0, -1 if j == 0 else 1, 0)
+    return codes, nrm
+
+
+def mixed_grid(n1: int, n2: int, n3: int, seed: int, oblique: bool = True,
+               face_prenormal: bool = True, interior_rows: int = 0):
+    """A small grid that exercises every operator branch: Fictive holes,
+    inactive Defined/Equation cells read by Actual neighbours, PreDefined
+    (Dirichlet semi-sum) rows and PreNormal rows with axis and oblique outward
+    normals on the faces.  `face_prenormal=False` keeps PreNormal rows off the
+    box faces; `interior_rows` turns that many interior Actual cells into
+    PreDefined/PreNormal rows (the variable-density operator is only defined
+    for PreNormal rows away from the box faces)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    codes = np.zeros((n1, n2, n3), np.int32)
+    nrm = np.zeros((n1, n2, n3, 3))
+    codes[1:-1, 1:-1, 1:-1] = ACTUAL
+    inner = np.argwhere(codes == ACTUAL)
+    pick = rng.choice(len(inner), size=max(3, len(inner) // 12), replace=False)
+    for q, p in enumerate(pick):
+        codes[tuple(inner[p])] = (FICTIVE, DEFINED, EQUATION)[q % 3]
+    dims = (n1, n2, n3)
+    for i in range(n1):
+        for j in range(n2):
+            for k in range(n3):
+                idx = (i, j, k)
+                ext = [a for a in range(3) if idx[a] in (0, dims[a] - 1)]
+                if len(ext) != 1:
+                    continue
+                a = ext[0]
+                out = -1.0 if idx[a] == 0 else 1.0
+                u = rng.random()
+                if u < 0.25:
+                    codes[idx] = FICTIVE
+                elif u < 0.5:
+                    codes[idx] = PREDEFINED
+                    nrm[idx][a] = out
+                elif u < 0.85 and face_prenormal:
+                    codes[idx] = PRENORMAL
+                    nrm[idx][a] = out
+                    if oblique and rng.random() < 0.5:
+                        for b in range(3):
+                            if b != a:
+                                nrm[idx][b] = rng.choice((-1.0, 1.0)) * rng.uniform(0.1, 0.6)
+                elif u < 0.93:
+                    codes[idx] = DEFINED
+                else:
+                    codes[idx] = EQUATION
+    if interior_rows:
+        inner = np.argwhere(codes[1:-1, 1:-1, 1:-1] == ACTUAL) + 1
+        pick = rng.choice(len(inner), size=interior_rows, replace=False)
+        for q, p in enumerate(pick):
+            idx = tuple(inner[p])
+            a = q % 3
+            if q % 2 == 0:
+                codes[idx] = PREDEFINED
+                nrm[idx][a] = rng.choice((-1.0, 1.0))
+            else:
+                codes[idx] = PRENORMAL
+                nrm[idx] = rng.uniform(-1, 1, 3)
+                nrm[idx][a] = rng.choice((-1.0, 1.0))
+    return codes, nrm
+
+
+def random_nodes(n: int, rng, start: float = 0.0) -> np.ndarray:
+    """n node coordinates with random positive spacings (TRandomSeparator input)."""
+    h = rng.uniform(0.5, 1.5, size=n - 1) / (n - 1)
+    return start + np.concatenate([[0.0], np.cumsum(h)])
+
+
+def spheres_grid(n: int, nspheres: int, rmin: float, rmax: float, seed: int):
+    """Unit cube, n cells per axis, cell-centred with one ghost layer
+    (nodes -h/2 .. 1+h/2 as XProblem.cpp:392-394), Fictive ghost layer
+    (homogeneous Neumann walls) and `nspheres` non-overlapping spheres with
+    radii U[rmin, rmax] masked Fictive.  Active cells left with no open face
+    are made Fictive so that every active row couples to the rest."""
+    h = 1.0 / n
+    nodes, sep = uniform_nodes(-h / 2, 1 + h / 2, h)
+    nb = len(nodes)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres, radii = [], []
+    tries = 0
+    while len(centres) < nspheres:
+        tries += 1
+        if tries > 100000:
+            raise RuntimeError("sphere packing failed")
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(r, 1 - r, size=3)
+        if all(np.linalg.norm(c - c2) > r + r2 for c2, r2 in zip(centres, radii)):
+            centres.append(c)
+            radii.append(r)
+    codes = np.zeros((nb, nb, nb), np.int32)
+    codes[1:-1, 1:-1, 1:-1] = ACTUAL
+    x = nodes
+    for c, r in zip(centres, radii):
+        lo = np.searchsorted(x, c - r - h)
+        hi = np.searchsorted(x, c + r + h) + 1
+        sl = tuple(slice(max(1, lo[a]), min(nb - 1, hi[a])) for a in range(3))
+        X, Y, Z = np.meshgrid(x[sl[0]], x[sl[1]], x[sl[2]], indexing="ij")
+        inside = (X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2 < r * r
+        sub = codes[sl]
+        sub[inside] = FICTIVE
+    _drop_isolated(codes)
+    return codes, np.zeros((nb, nb, nb, 3)), nodes, sep, (np.array(centres), np.array(radii))
+
+
+def _drop_isolated(codes: np.ndarray) -> None:
+    act = codes == ACTUAL
+    nonfict = codes != FICTIVE
+    opened = np.zeros_like(act)
+    for a in range(3):
+        for s in (-1, 1):
+            opened[1:-1, 1:-1, 1:-1] |= np.roll(nonfict, -s, axis=a)[1:-1, 1:-1, 1:-1]
+    codes[act & ~opened] = FICTIVE
+
+
+def divergence_rhs(codes: np.ndarray, sep, seed: int) -> np.ndarray:
+    """b = -(div u) of an i.i.d. N(0,1) staggered velocity field on Actual cells
+    (the pressure right-hand side of XProblem.cpp:5474-5512 with rho = 1 and
+    tau = 1), zero elsewhere, projected to zero mean over active cells."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n1, n2, n3 = codes.shape
+    hx, hy, hz = sep
+    b = np.zeros(codes.shape)
+    u = rng.standard_normal((n1, n2, n3))
+    v = rng.standard_normal((n1, n2, n3))
+    w = rng.standard_normal((n1, n2, n3))
+    div = np.zeros(codes.shape)
+    div[1:, :, :] += (u[1:] - u[:-1]) / np.asarray(hx)[:, None, None]
+    div[:, 1:, :] += (v[:, 1:] - v[:, :-1]) / np.asarray(hy)[None, :, None]
+    div[:, :, 1:] += (w[:, :, 1:] - w[:, :, :-1]) / np.asarray(hz)[None, None, :]
+    act = codes == ACTUAL
+    b[act] = -div[act]
+    sm = space_mask(codes).astype(bool)
+    b[sm] -= b[sm].mean()
+    return b
