@@ -1,0 +1,204 @@
+"""Test infrastructure only: ctypes front of oracle/liboracle.so, the CPU
+restatement of the reference arithmetic (oracle/xf_oracle.c).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
+checker.  The product never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+LAPLACE, VARDIV = 0, 1
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        d, i32, i64, u8 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_uint8)
+        L.xfo_rn_map.restype = C.c_int64
+        L.xfo_dot.restype = C.c_double
+        L.xfo_norm.restype = C.c_double
+        L.xfo_absmax.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("resid", C.c_double), ("status", C.c_int)]
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def set_threads(n):
+    lib().xfo_set_threads(int(n))
+
+
+def space_mask(codes):
+    codes = np.ascontiguousarray(codes, dtype=np.int32)
+    out = np.empty(codes.shape, np.uint8)
+    lib().xfo_space_mask(_p(codes, C.c_int32), C.c_int64(codes.size), _p(out, C.c_uint8))
+    return out
+
+
+def rn_map(smask):
+    smask = np.ascontiguousarray(smask, dtype=np.uint8)
+    n1, n2, n3 = smask.shape
+    inv = np.zeros(smask.shape, np.int32)
+    cnt = int(smask.sum())
+    fwd = np.zeros((cnt, 3), np.int32)
+    r = lib().xfo_rn_map(_p(smask, C.c_uint8), n1, n2, n3, _p(inv, C.c_int32), _p(fwd, C.c_int32))
+    return int(r), inv, fwd
+
+
+def validate(op, codes, normals):
+    codes = np.ascontiguousarray(codes, dtype=np.int32)
+    normals = f64(normals)
+    bad = C.c_int64(-1)
+    st = lib().xfo_validate(op, _p(codes, C.c_int32), _p(normals, C.c_double), *codes.shape, C.byref(bad))
+    return st, bad.value
+
+
+class Grid:
+    """Codes, normals, separations (and density) of one box."""
+
+    def __init__(self, codes, normals, hx, hy, hz, density=None):
+        self.codes = np.ascontiguousarray(codes, dtype=np.int32)
+        self.normals = f64(normals)
+        self.hx, self.hy, self.hz = f64(hx), f64(hy), f64(hz)
+        self.density = f64(density) if density is not None else np.ones(self.codes.shape)
+        self.shape = self.codes.shape
+        self.smask = space_mask(self.codes)
+
+    def args(self):
+        return (_p(self.codes, C.c_int32), _p(self.normals, C.c_double), _p(self.hx, C.c_double),
+                _p(self.hy, C.c_double), _p(self.hz, C.c_double), _p(self.density, C.c_double), *self.shape)
+
+
+def apply(op, g, x, s=None, sign=0, y_init=None):
+    x = f64(x)
+    y = f64(y_init).copy() if y_init is not None else np.zeros(g.shape)
+    s_ = f64(s) if s is not None else np.zeros(g.shape)
+    st = lib().xfo_apply(op, *g.args(), _p(x, C.c_double), _p(s_, C.c_double), sign, _p(y, C.c_double))
+    if st != 0:
+        raise ValueError(f"oracle apply rejected the grid (status {st})")
+    return y
+
+
+def lincomb(p1, s1, p2, s2, smask, z_init):
+    z = f64(z_init).copy()
+    s1 = f64(s1)
+    s2k = f64(s2) if s2 is not None else None
+    lib().xfo_lincomb(C.c_double(p1), _p(s1, C.c_double), C.c_double(p2),
+                      _p(s2k, C.c_double) if s2k is not None else None,
+                      _p(np.ascontiguousarray(smask, np.uint8), C.c_uint8), C.c_int64(z.size), _p(z, C.c_double))
+    return z
+
+
+def dot(a, b, smask):
+    a, b = f64(a), f64(b)
+    m = np.ascontiguousarray(smask, np.uint8)
+    return lib().xfo_dot(_p(a, C.c_double), _p(b, C.c_double), _p(m, C.c_uint8), C.c_int64(a.size))
+
+
+def norm(a, smask):
+    a = f64(a)
+    m = np.ascontiguousarray(smask, np.uint8)
+    return lib().xfo_norm(_p(a, C.c_double), _p(m, C.c_uint8), C.c_int64(a.size))
+
+
+def absmax(a, smask, inv):
+    a = f64(a)
+    m = np.ascontiguousarray(smask, np.uint8)
+    inv = np.ascontiguousarray(inv, np.int32)
+    idx = C.c_int32(0)
+    v = lib().xfo_absmax(_p(a, C.c_double), _p(m, C.c_uint8), _p(inv, C.c_int32), C.c_int64(a.size), C.byref(idx))
+    return v, idx.value
+
+
+def _solve(fn, op, g, x0, b, tol, maxit):
+    x0, b = f64(x0), f64(b)
+    res = np.zeros(g.shape)
+    st = Stats()
+    rc = fn(op, *g.args(), _p(x0, C.c_double), _p(b, C.c_double), C.c_double(tol), int(maxit),
+            _p(res, C.c_double), C.byref(st))
+    if rc != 0:
+        raise ValueError(f"oracle solver rejected the grid (status {rc})")
+    return res, st
+
+
+def cg_reference(op, g, x0, b, eps=0.0, maxit=0):
+    return _solve(lib().xfo_cg_reference, op, g, x0, b, eps, maxit)
+
+
+def bicgstab_reference(op, g, x0, b, eps=0.0, maxit=0):
+    return _solve(lib().xfo_bicgstab_reference, op, g, x0, b, eps, maxit)
+
+
+def minres_reference(op, g, x0, b, eps=0.0, maxit=0):
+    return _solve(lib().xfo_minres_reference, op, g, x0, b, eps, maxit)
+
+
+def cg_plain(op, g, x0, b, rtol, maxit=0):
+    return _solve(lib().xfo_cg_plain, op, g, x0, b, rtol, maxit)
+
+
+def thomas(M, u, a, b, c, f):
+    u = f64(u).copy()
+    lib().xfo_thomas(int(M), _p(u, C.c_double), _p(f64(a), C.c_double), _p(f64(b), C.c_double),
+                     _p(f64(c), C.c_double), _p(f64(f), C.c_double))
+    return u
+
+
+def ib_interpolate(vel, h0, axis, pos):
+    vel, h0, pos = f64(vel), f64(h0), f64(pos)
+    out = np.zeros(len(pos))
+    lib().xfo_ib_interpolate(_p(vel, C.c_double), *vel.shape, _p(h0, C.c_double), int(axis), len(pos),
+                             _p(pos, C.c_double), _p(out, C.c_double))
+    return out
+
+
+def ib_update(axis, tau, node_vel, pos):
+    pos = f64(pos).copy()
+    lib().xfo_ib_update(len(pos), int(axis), C.c_double(tau), _p(f64(node_vel), C.c_double), _p(pos, C.c_double))
+    return pos
+
+
+def ib_forces(axis, pos, ref, kind, nxt, prv, dist0, curv0, node_stiff, params):
+    n = len(kind)
+    out = np.zeros(n)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)  # noqa: E731
+    kind, nxt, prv = i32(kind), i32(nxt), i32(prv)
+    lib().xfo_ib_forces(n, int(axis), _p(f64(pos), C.c_double), _p(f64(ref), C.c_double), _p(kind, C.c_int32),
+                        _p(nxt, C.c_int32), _p(prv, C.c_int32), _p(f64(dist0), C.c_double),
+                        _p(f64(curv0), C.c_double), _p(f64(node_stiff), C.c_double), _p(f64(params), C.c_double),
+                        _p(out, C.c_double))
+    return out
+
+
+def ib_spread(shape, h0, axis, pos, force, fbox=None):
+    fbox = np.zeros(shape) if fbox is None else f64(fbox).copy()
+    pos, h0 = f64(pos), f64(h0)
+    lib().xfo_ib_spread(_p(fbox, C.c_double), *shape, _p(h0, C.c_double), int(axis), len(pos),
+                        _p(pos, C.c_double), _p(f64(force), C.c_double))
+    return fbox

@@ -1,0 +1,664 @@
+/* Test infrastructure only: CPU restatement of the reference's pressure-path
+ * arithmetic.  See xf_oracle.h.  Parity of this restatement is pinned by
+ * tests/test_oracle_golden.py against fixtures produced by the reference's
+ * own compiled classes (tests/golden/make_golden.py).
+ *
+ * With xfo_set_threads(1) every loop runs in the reference's i->j->k order
+ * with the reference's operation order (bit-exact operator and vector
+ * algebra).  More threads parallelise the cell loops for the timed CPU
+ * baseline; reductions then sum per-thread partials (not bit-exact).
+ */
+#define _GNU_SOURCE
+#include "xf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 1;
+void xfo_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int xfo_get_threads(void) { return g_threads; }
+
+enum { FICT = 0, ACT = 1, DEF = 3, PREDEF = 4, NORM = 5, PRENORM = 6, EQU = 7, PREEQU = 8 };
+
+/* XProblem.cpp:4155-4182: grid codes -> space mask. */
+void xfo_space_mask(const int32_t* codes, int64_t ncell, uint8_t* smask) {
+  for (int64_t c = 0; c < ncell; c++) {
+    int m = codes[c];
+    smask[c] = (m == ACT || m == PREDEF || m == NORM || m == PRENORM || m == PREEQU) ? 1 : 0;
+  }
+}
+
+/* XSpaceModel.cpp:383-406: Rn numbering, 1-based, i->j->k order. */
+int64_t xfo_rn_map(const uint8_t* smask, int n1, int n2, int n3, int32_t* inv_box, int32_t* fwd_ijk) {
+  int64_t num = 0;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        int64_t c = ((int64_t)i * n2 + j) * n3 + k;
+        if (smask[c] > 0) {
+          num++;
+          if (inv_box) inv_box[c] = (int32_t)num;
+          if (fwd_ijk) { fwd_ijk[3 * (num - 1)] = i; fwd_ijk[3 * (num - 1) + 1] = j; fwd_ijk[3 * (num - 1) + 2] = k; }
+        } else if (inv_box) {
+          inv_box[c] = 0;
+        }
+      }
+  return num;
+}
+
+/* Every check the reference makes while evaluating an active row
+ * (XOperator.cpp:971-1123, 1933-2227), plus index-range checks for reads the
+ * reference would make outside its arrays.  Returns XFO_ERR_MASK and the first
+ * offending cell. */
+int xfo_validate(int op, const int32_t* codes, const double* normals, int n1, int n2, int n3, int64_t* bad) {
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        int64_t c = ((int64_t)i * n2 + j) * n3 + k;
+        int m = codes[c];
+        int known = (m == FICT || m == ACT || m == DEF || m == PREDEF || m == NORM || m == PRENORM || m == EQU || m == PREEQU);
+        int interior = i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2 && k >= 1 && k <= n3 - 2;
+        int ok = 1;
+        if (!known) ok = 0;
+        else if (m == NORM || m == PREEQU) ok = 0;
+        else if (m == ACT) ok = interior;
+        else if (m == PREDEF || m == PRENORM) {
+          double nx = normals[3 * c], ny = normals[3 * c + 1], nz = normals[3 * c + 2];
+          if (nx == 0 && ny == 0 && nz == 0) ok = 0;
+          else if (m == PREDEF) {
+            if (nx != 0) ok = (ny == 0 && nz == 0 && fabs(nx) == 1);
+            else if (ny != 0) ok = (nx == 0 && nz == 0 && fabs(ny) == 1);
+            else ok = (nx == 0 && ny == 0 && fabs(nz) == 1);
+            if (ok) {
+              int di = nx > 0 ? -1 : nx < 0 ? 1 : 0, dj = ny > 0 ? -1 : ny < 0 ? 1 : 0, dk = nz > 0 ? -1 : nz < 0 ? 1 : 0;
+              ok = i + di >= 0 && i + di < n1 && j + dj >= 0 && j + dj < n2 && k + dk >= 0 && k + dk < n3;
+            }
+          } else {
+            int lo_i = nx > 0 ? -1 : 0, hi_i = nx < 0 ? 1 : 0;
+            int lo_j = ny > 0 ? -1 : 0, hi_j = ny < 0 ? 1 : 0;
+            int lo_k = nz > 0 ? -1 : 0, hi_k = nz < 0 ? 1 : 0;
+            ok = i + lo_i >= 0 && i + hi_i < n1 && j + lo_j >= 0 && j + hi_j < n2 && k + lo_k >= 0 && k + hi_k < n3;
+            if (op == XFO_OP_VARDIV) ok = ok && interior;
+          }
+        }
+        if (!ok) { if (bad) *bad = c; return XFO_ERR_MASK; }
+      }
+  return XFO_OK;
+}
+
+typedef struct {
+  int n1, n2, n3;
+  int64_t s1, s2;
+  const int32_t* codes;
+  const double* nrm;
+  const double *hx, *hy, *hz, *rho;
+} xfo_grid;
+
+/* T3dLaplaceOperator::operator(), XOperator.cpp:938-1129 (Actual, PreDefined,
+ * PreNormal branches). */
+static double lap_row(const xfo_grid* g, const double* f, int i, int j, int k) {
+  const int64_t s1 = g->s1, s2 = g->s2;
+  const int64_t c = i * s1 + j * s2 + k;
+  const int m = g->codes[c];
+  const int32_t* mask = g->codes;
+  if (m == ACT) {
+    double hx_2X = (g->hx[i - 1] + g->hx[i]) / 2;
+    double hx_2Y = (g->hy[j - 1] + g->hy[j]) / 2;
+    double hx_2Z = (g->hz[k - 1] + g->hz[k]) / 2;
+    double f_i_1 = (f[c] - f[c - s1]) / (g->hx[i - 1]);
+    double f_i = (f[c + s1] - f[c]) / (g->hx[i]);
+    double f_j_1 = (f[c] - f[c - s2]) / (g->hy[j - 1]);
+    double f_j = (f[c + s2] - f[c]) / (g->hy[j]);
+    double f_k_1 = (f[c] - f[c - 1]) / (g->hz[k - 1]);
+    double f_k = (f[c + 1] - f[c]) / (g->hz[k]);
+    if (mask[c - s1] == FICT) f_i_1 = 0;
+    if (mask[c + s1] == FICT) f_i = 0;
+    if (mask[c - s2] == FICT) f_j_1 = 0;
+    if (mask[c + s2] == FICT) f_j = 0;
+    if (mask[c - 1] == FICT) f_k_1 = 0;
+    if (mask[c + 1] == FICT) f_k = 0;
+    return -((f_i - f_i_1) / hx_2X + (f_j - f_j_1) / hx_2Y + (f_k - f_k_1) / hx_2Z);
+  }
+  const double nx = g->nrm[3 * c], ny = g->nrm[3 * c + 1], nz = g->nrm[3 * c + 2];
+  if (m == PREDEF) {
+    double semiSum = 0;
+    if (nx > 0) semiSum = (f[c] + f[c - s1]) / 2;
+    else if (nx < 0) semiSum = (f[c + s1] + f[c]) / 2;
+    if (ny > 0) semiSum = (f[c] + f[c - s2]) / 2;
+    else if (ny < 0) semiSum = (f[c + s2] + f[c]) / 2;
+    if (nz > 0) semiSum = (f[c] + f[c - 1]) / 2;
+    else if (nz < 0) semiSum = (f[c + 1] + f[c]) / 2;
+    return semiSum;
+  }
+  /* PreNormal */
+  int sI = 0, sI1 = 0, sJ = 0, sJ1 = 0, sK = 0, sK1 = 0;
+  double hxl = 1, hyl = 1, hzl = 1;
+  if (nx > 0) { sI = 0; sI1 = -1; hxl = g->hx[i - 1]; } else if (nx < 0) { sI = 1; sI1 = 0; hxl = g->hx[i]; }
+  if (ny > 0) { sJ = 0; sJ1 = -1; hyl = g->hy[j - 1]; } else if (ny < 0) { sJ = 1; sJ1 = 0; hyl = g->hy[j]; }
+  if (nz > 0) { sK = 0; sK1 = -1; hzl = g->hz[k - 1]; } else if (nz < 0) { sK = 1; sK1 = 0; hzl = g->hz[k]; }
+#define F(a, b, d) f[(int64_t)(i + (a)) * s1 + (int64_t)(j + (b)) * s2 + (k + (d))]
+  double fl = (F(sI, 0, 0) + F(sI, sJ, 0) + F(sI, 0, sK) + F(sI, sJ, sK)) / 4;
+  double fl_1 = (F(sI1, 0, 0) + F(sI1, sJ, 0) + F(sI1, 0, sK) + F(sI1, sJ, sK)) / 4;
+  double dfx = (fl - fl_1) / hxl;
+  fl = (F(0, sJ, 0) + F(sI, sJ, 0) + F(0, sJ, sK) + F(sI, sJ, sK)) / 4;
+  fl_1 = (F(0, sJ1, 0) + F(sI, sJ1, 0) + F(0, sJ1, sK) + F(sI, sJ1, sK)) / 4;
+  double dfy = (fl - fl_1) / hyl;
+  fl = (F(0, 0, sK) + F(sI, 0, sK) + F(0, sJ, sK) + F(sI, sJ, sK)) / 4;
+  fl_1 = (F(0, 0, sK1) + F(sI, 0, sK1) + F(0, sJ, sK1) + F(sI, sJ, sK1)) / 4;
+  double dfz = (fl - fl_1) / hzl;
+#undef F
+  if (g->rho == NULL) return dfx * nx + dfy * ny + dfz * nz;
+  /* T3dVariableDivergentedOperator PreNormal tail, XOperator.cpp:2211-2221,
+   * including its precedence (rho[i+1] - rho[i]/h). */
+  const double* rho = g->rho;
+  double d_x = rho[c + s1] - rho[c] / (g->hx[i - 1]);
+  double d_y = rho[c + s2] - rho[c] / (g->hy[j - 1]);
+  double d_z = rho[c + 1] - rho[c] / (g->hz[k - 1]);
+  double laplace_p = dfx * nx + dfy * ny + dfz * nz;
+  double divergence_density = d_x + d_y + d_z;
+  return rho[c] * laplace_p - divergence_density * f[c];
+}
+
+/* T3dVariableDivergentedOperator::operator() Actual branch, XOperator.cpp:1933-2026. */
+static double vardiv_actual(const xfo_grid* g, const double* f, int i, int j, int k) {
+  const int64_t s1 = g->s1, s2 = g->s2;
+  const int64_t c = i * s1 + j * s2 + k;
+  const int32_t* mask = g->codes;
+  const double* rho = g->rho;
+  double h_1X = g->hx[i - 1], hX = g->hx[i];
+  double h_1Y = g->hy[j - 1], hY = g->hy[j];
+  double h_1Z = g->hz[k - 1], hZ = g->hz[k];
+  double hx_2X = (g->hx[i - 1] + g->hx[i]) / 2;
+  double hx_2Y = (g->hy[j - 1] + g->hy[j]) / 2;
+  double hx_2Z = (g->hz[k - 1] + g->hz[k]) / 2;
+  double f_i_1 = rho[c - s1] * (f[c] - f[c - s1]) / (h_1X);
+  double f_i = rho[c + s1] * (f[c + s1] - f[c]) / (hX);
+  double f_j_1 = rho[c - s2] * (f[c] - f[c - s2]) / (h_1Y);
+  double f_j = rho[c + s2] * (f[c + s2] - f[c]) / (hY);
+  double f_k_1 = rho[c - 1] * (f[c] - f[c - 1]) / (h_1Z);
+  double f_k = rho[c + 1] * (f[c + 1] - f[c]) / (hZ);
+  double d_i = (rho[c + s1] - rho[c]) / (h_1X);
+  double d_j = (rho[c + s2] - rho[c]) / (h_1Y);
+  double d_k = (rho[c + 1] - rho[c]) / (h_1Z);
+  if (mask[c - s1] == FICT) f_i_1 = 0;
+  if (mask[c + s1] == FICT) { f_i = 0; d_i = 0; }
+  if (mask[c - s2] == FICT) f_j_1 = 0;
+  if (mask[c + s2] == FICT) { f_j = 0; d_j = 0; }
+  if (mask[c - 1] == FICT) f_k_1 = 0;
+  if (mask[c + 1] == FICT) { f_k = 0; d_k = 0; }
+  double laplace_p = ((f_i - f_i_1) / hx_2X + (f_j - f_j_1) / hx_2Y + (f_k - f_k_1) / hx_2Z);
+  double divergence_density = d_i + d_j + d_k;
+  return -(rho[c] * laplace_p - divergence_density * f[c]);
+}
+
+static double row(int op, const xfo_grid* g, const double* f, int i, int j, int k) {
+  int64_t c = i * g->s1 + j * g->s2 + k;
+  if (op == XFO_OP_VARDIV && g->codes[c] == ACT) return vardiv_actual(g, f, i, j, k);
+  return lap_row(g, f, i, j, k);
+}
+
+static int active(const int32_t* codes, int64_t c) {
+  int m = codes[c];
+  return m == ACT || m == PREDEF || m == NORM || m == PRENORM || m == PREEQU;
+}
+
+/* TRnRelease3dSpace::LocalReleaseAssignSpeedLinearCombination(op),
+ * XSpace.cpp:3013-3217: y = A x (+/- s) on cells with space mask > 0. */
+int xfo_apply(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+              const double* hz, const double* density, int n1, int n2, int n3, const double* x,
+              const double* s, int sign, double* y) {
+  int64_t bad;
+  if (xfo_validate(op, codes, normals, n1, n2, n3, &bad) != XFO_OK) return XFO_ERR_MASK;
+  xfo_grid g = {n1, n2, n3, (int64_t)n2 * n3, n3, codes, normals, hx, hy, hz, op == XFO_OP_VARDIV ? density : NULL};
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        int64_t c = ((int64_t)i * n2 + j) * n3 + k;
+        if (!active(codes, c)) continue;
+        double v = row(op, &g, x, i, j, k);
+        if (sign > 0) v = v + s[c];
+        else if (sign < 0) v = v - s[c];
+        y[c] = v;
+      }
+  return XFO_OK;
+}
+
+/* XSpace.cpp:2489-3010: z = p1*s1 + p2*s2 on active cells. */
+void xfo_lincomb(double p1, const double* s1, double p2, const double* s2, const uint8_t* smask, int64_t n,
+                 double* z) {
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+  for (int64_t c = 0; c < n; c++)
+    if (smask[c] > 0) {
+      double a = s1 ? p1 * s1[c] : 0.0;
+      z[c] = s2 ? a + p2 * s2[c] : a;
+    }
+}
+
+/* XSpace.cpp:3261-3342 (sequential accumulation). */
+double xfo_dot(const double* a, const double* b, const uint8_t* smask, int64_t n) {
+  double res = 0;
+  if (g_threads == 1) {
+    for (int64_t c = 0; c < n; c++)
+      if (smask[c] > 0) res = res + a[c] * b[c];
+    return res;
+  }
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : res)
+  for (int64_t c = 0; c < n; c++)
+    if (smask[c] > 0) res = res + a[c] * b[c];
+  return res;
+}
+
+/* XSpace.cpp:3219-3259 + 1205-1217: sqrtl of the masked sum of squares. */
+double xfo_norm(const double* a, const uint8_t* smask, int64_t n) {
+  double res = 0;
+  for (int64_t c = 0; c < n; c++)
+    if (smask[c] > 0) res = res + a[c] * a[c];
+  return (double)sqrtl(res);
+}
+
+/* XSpace.cpp:3428-3487 (type 1): first strict maximum of |a| in i->j->k order;
+ * Rn index 1 when nothing beats 0. */
+double xfo_absmax(const double* a, const uint8_t* smask, const int32_t* inv, int64_t n, int32_t* rn) {
+  double res = 0;
+  int32_t idx = 1;
+  for (int64_t c = 0; c < n; c++)
+    if (smask[c] > 0) {
+      double v = fabs(a[c]);
+      if (v > res) { res = v; idx = inv[c]; }
+    }
+  if (rn) *rn = idx;
+  return res;
+}
+
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int op;
+  xfo_grid g;
+  uint8_t* smask;
+  int64_t n;
+} sys_t;
+
+static int sys_init(sys_t* S, int op, const int32_t* codes, const double* normals, const double* hx,
+                    const double* hy, const double* hz, const double* density, int n1, int n2, int n3) {
+  int64_t bad;
+  if (xfo_validate(op, codes, normals, n1, n2, n3, &bad) != XFO_OK) return XFO_ERR_MASK;
+  S->op = op;
+  xfo_grid g = {n1, n2, n3, (int64_t)n2 * n3, n3, codes, normals, hx, hy, hz, op == XFO_OP_VARDIV ? density : NULL};
+  S->g = g;
+  S->n = (int64_t)n1 * n2 * n3;
+  S->smask = (uint8_t*)malloc(S->n);
+  xfo_space_mask(codes, S->n, S->smask);
+  return XFO_OK;
+}
+
+static void apply(sys_t* S, const double* x, const double* s, int sign, double* y) {
+  xfo_grid* g = &S->g;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+  for (int i = 0; i < g->n1; i++)
+    for (int j = 0; j < g->n2; j++)
+      for (int k = 0; k < g->n3; k++) {
+        int64_t c = ((int64_t)i * g->n2 + j) * g->n3 + k;
+        if (!S->smask[c]) continue;
+        double v = row(S->op, g, x, i, j, k);
+        if (sign > 0) v = v + s[c];
+        else if (sign < 0) v = v - s[c];
+        y[c] = v;
+      }
+}
+
+/* (A x, y) through LocalReleaseInnerproduct(op), XSpace.cpp:3344-3419. */
+static double dot_op(sys_t* S, const double* x, const double* y) {
+  xfo_grid* g = &S->g;
+  double res = 0;
+  if (g_threads == 1) {
+    for (int i = 0; i < g->n1; i++)
+      for (int j = 0; j < g->n2; j++)
+        for (int k = 0; k < g->n3; k++) {
+          int64_t c = ((int64_t)i * g->n2 + j) * g->n3 + k;
+          if (S->smask[c]) res = res + y[c] * row(S->op, g, x, i, j, k);
+        }
+    return res;
+  }
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : res)
+  for (int i = 0; i < g->n1; i++)
+    for (int j = 0; j < g->n2; j++)
+      for (int k = 0; k < g->n3; k++) {
+        int64_t c = ((int64_t)i * g->n2 + j) * g->n3 + k;
+        if (S->smask[c]) res = res + y[c] * row(S->op, g, x, i, j, k);
+      }
+  return res;
+}
+
+static double* zeros(int64_t n) { return (double*)calloc((size_t)n, sizeof(double)); }
+static double* copyv(const double* a, int64_t n) {
+  double* p = (double*)malloc((size_t)n * sizeof(double));
+  memcpy(p, a, (size_t)n * sizeof(double));
+  return p;
+}
+static void massign(double* dst, const double* src, const uint8_t* m, int64_t n) {
+  for (int64_t c = 0; c < n; c++)
+    if (m[c]) dst[c] = src[c];
+}
+
+/* TSLAE::SolveByConjugateGradients, XSLAE.cpp:56-157 (three-term form, true
+ * residual every iteration, ||r||_2 <= eps absolute). */
+int xfo_cg_reference(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                     const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
+                     const double* b, double eps, int maxit, double* result, xfo_stats* st) {
+  sys_t S;
+  if (sys_init(&S, op, codes, normals, hx, hy, hz, density, n1, n2, n3)) return XFO_ERR_MASK;
+  const int64_t n = S.n;
+  const uint8_t* m = S.smask;
+  if (eps <= 0) eps = 1e-5;
+  memcpy(result, x0, (size_t)n * sizeof(double));
+  for (int64_t c = 0; c < n; c++) if (m[c]) result[c] = 0; /* *fResult |= 0 */
+  double* xk_1 = copyv(x0, n);
+  double* rk_1 = zeros(n);
+  apply(&S, xk_1, b, -1, rk_1);
+  double rk_1Xrk_1 = xfo_dot(rk_1, rk_1, m, n);
+  massign(result, xk_1, m, n);
+  st->iterations = 0; st->status = 0; st->resid = sqrt(rk_1Xrk_1);
+  if (rk_1Xrk_1 != 0) {
+    double tauk = rk_1Xrk_1 / dot_op(&S, rk_1, rk_1);
+    double* xk = copyv(x0, n);
+    xfo_lincomb(1.0, xk_1, -tauk, rk_1, m, n, xk);
+    double* rk = zeros(n);
+    apply(&S, xk, b, -1, rk);
+    double rkXrk = xfo_dot(rk, rk, m, n);
+    massign(result, xk, m, n);
+    if (rkXrk != 0) {
+      double alfak = 1;
+      int it = 0;
+      double epsCur = (double)sqrtl(rkXrk);
+      while (epsCur > eps) {
+        if (maxit > 0 && it >= maxit) { st->status = 13; break; }
+        it++;
+        double tauk1 = rkXrk / dot_op(&S, rk, rk);
+        double alfak1 = 1 - (1 / alfak) * (tauk1 / tauk) * (rkXrk / rk_1Xrk_1);
+        alfak1 = 1 / alfak1;
+        xfo_lincomb(alfak1, xk, (1 - alfak1), xk_1, m, n, result);
+        xfo_lincomb(1.0, result, -(tauk1 * alfak1), rk, m, n, result);
+        massign(xk_1, xk, m, n);
+        massign(rk_1, rk, m, n);
+        rk_1Xrk_1 = rkXrk;
+        tauk = tauk1;
+        alfak = alfak1;
+        massign(xk, result, m, n);
+        apply(&S, xk, b, -1, rk);
+        rkXrk = xfo_dot(rk, rk, m, n);
+        epsCur = (double)sqrtl(rkXrk);
+      }
+      st->iterations = it;
+      st->resid = epsCur;
+    }
+    free(xk); free(rk);
+  }
+  free(xk_1); free(rk_1); free(S.smask);
+  return XFO_OK;
+}
+
+/* TSLAE::SolveByBiConjugateGradientsStab, XSLAE.cpp:667-768 (warm start,
+ * ||r||_inf <= eps). */
+int xfo_bicgstab_reference(int op, const int32_t* codes, const double* normals, const double* hx,
+                           const double* hy, const double* hz, const double* density, int n1, int n2, int n3,
+                           const double* x0, const double* b, double eps, int maxit, double* result,
+                           xfo_stats* st) {
+  sys_t S;
+  if (sys_init(&S, op, codes, normals, hx, hy, hz, density, n1, n2, n3)) return XFO_ERR_MASK;
+  const int64_t n = S.n;
+  const uint8_t* m = S.smask;
+  if (eps <= 0) eps = 1e-5;
+  int32_t idx;
+  int32_t* inv = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+  xfo_rn_map(m, n1, n2, n3, inv, NULL);
+  memcpy(result, x0, (size_t)n * sizeof(double));
+  for (int64_t c = 0; c < n; c++) if (m[c]) result[c] = 0;
+  double* Un = copyv(x0, n);
+  double *tmp1 = zeros(n), *tmp2 = zeros(n), *Rn = zeros(n), *sRn = zeros(n);
+  double *Pn = zeros(n), *Pn1 = zeros(n), *Vn = zeros(n), *Sn = zeros(n), *Tn = zeros(n);
+  apply(&S, Un, NULL, 0, Rn);
+  xfo_lincomb(1.0, b, -1.0, Rn, m, n, Rn);
+  massign(sRn, Rn, m, n);
+  double pn = 1., an = 1., bn = 1., wn = 1., pn1;
+  int it = 0;
+  double norm = xfo_absmax(Rn, m, inv, n, &idx);
+  st->status = 0;
+  while (norm > eps) {
+    if (maxit > 0 && it >= maxit) { st->status = 13; break; }
+    it++;
+    pn1 = xfo_dot(sRn, Rn, m, n);
+    bn = (pn1 / pn) * (an / wn);
+    xfo_lincomb(wn, Vn, 0, NULL, m, n, Pn1);
+    xfo_lincomb(1.0, Pn, -1.0, Pn1, m, n, Pn1);
+    xfo_lincomb(bn, Pn1, 0, NULL, m, n, Pn1);
+    xfo_lincomb(1.0, Rn, 1.0, Pn1, m, n, Pn1);
+    apply(&S, Pn1, NULL, 0, Vn);
+    an = pn1 / xfo_dot(sRn, Vn, m, n);
+    xfo_lincomb(an, Vn, 0, NULL, m, n, Sn);
+    xfo_lincomb(1.0, Rn, -1.0, Sn, m, n, Sn);
+    apply(&S, Sn, NULL, 0, Tn);
+    wn = xfo_dot(Tn, Sn, m, n) / xfo_dot(Tn, Tn, m, n);
+    xfo_lincomb(an, Pn1, 0, NULL, m, n, tmp1);
+    xfo_lincomb(1.0, tmp1, wn, Sn, m, n, tmp2);
+    xfo_lincomb(1.0, Un, 1.0, tmp2, m, n, Un);
+    xfo_lincomb(wn, Tn, 0, NULL, m, n, Rn);
+    xfo_lincomb(1.0, Sn, -1.0, Rn, m, n, Rn);
+    pn = pn1;
+    massign(Pn, Pn1, m, n);
+    norm = xfo_absmax(Rn, m, inv, n, &idx);
+  }
+  massign(result, Un, m, n);
+  st->iterations = it;
+  st->resid = norm;
+  free(Un); free(tmp1); free(tmp2); free(Rn); free(sRn); free(Pn); free(Pn1); free(Vn); free(Sn); free(Tn);
+  free(inv); free(S.smask);
+  return XFO_OK;
+}
+
+/* TSLAE::SolveByMinimalResiduals, XSLAE.cpp:350-414 (||r||_2 <= eps). */
+int xfo_minres_reference(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                         const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
+                         const double* b, double eps, int maxit, double* result, xfo_stats* st) {
+  sys_t S;
+  if (sys_init(&S, op, codes, normals, hx, hy, hz, density, n1, n2, n3)) return XFO_ERR_MASK;
+  const int64_t n = S.n;
+  const uint8_t* m = S.smask;
+  if (eps <= 0) eps = 1e-7;
+  memcpy(result, x0, (size_t)n * sizeof(double));
+  for (int64_t c = 0; c < n; c++) if (m[c]) result[c] = 0;
+  double* xk = copyv(x0, n);
+  double *rk = zeros(n), *Ark = zeros(n);
+  apply(&S, xk, b, -1, rk);
+  double rkXrk = xfo_dot(rk, rk, m, n);
+  massign(result, xk, m, n);
+  int it = 0;
+  double epsCur = sqrt(rkXrk);
+  st->status = 0;
+  if (rkXrk != 0) {
+    epsCur = (double)sqrtl(rkXrk);
+    while (epsCur > eps) {
+      if (maxit > 0 && it >= maxit) { st->status = 13; break; }
+      it++;
+      apply(&S, rk, NULL, 0, Ark);
+      double alfa = (-1) * xfo_dot(Ark, rk, m, n) / xfo_dot(Ark, Ark, m, n);
+      xfo_lincomb(1.0, xk, alfa, rk, m, n, xk);
+      apply(&S, xk, b, -1, rk);
+      rkXrk = xfo_dot(rk, rk, m, n);
+      epsCur = (double)sqrtl(rkXrk);
+    }
+  }
+  massign(result, xk, m, n);
+  st->iterations = it;
+  st->resid = epsCur;
+  free(xk); free(rk); free(Ark); free(S.smask);
+  return XFO_OK;
+}
+
+/* Plain Hestenes-Stiefel CG with a relative-residual stop: the FP64 CPU
+ * counterpart of the GPU judge (not a reference routine; the reference's CG
+ * is the three-term form above). */
+int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                 const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
+                 const double* b, double rtol, int maxit, double* result, xfo_stats* st) {
+  sys_t S;
+  if (sys_init(&S, op, codes, normals, hx, hy, hz, density, n1, n2, n3)) return XFO_ERR_MASK;
+  const int64_t n = S.n;
+  const uint8_t* m = S.smask;
+  memcpy(result, x0, (size_t)n * sizeof(double));
+  double *r = zeros(n), *p = zeros(n), *q = zeros(n);
+  apply(&S, result, b, -1, r); /* r = A x - b */
+  xfo_lincomb(-1.0, r, 0, NULL, m, n, r);
+  double bb = xfo_dot(b, b, m, n);
+  double rr = xfo_dot(r, r, m, n);
+  massign(p, r, m, n);
+  int it = 0;
+  st->status = 0;
+  double thr = rtol * rtol * bb;
+  while (rr > thr) {
+    if (maxit > 0 && it >= maxit) { st->status = 13; break; }
+    it++;
+    apply(&S, p, NULL, 0, q);
+    double alpha = rr / xfo_dot(p, q, m, n);
+    double rr_new = 0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : rr_new) if (g_threads > 1)
+    for (int64_t c = 0; c < n; c++)
+      if (m[c]) {
+        result[c] += alpha * p[c];
+        r[c] -= alpha * q[c];
+        rr_new += r[c] * r[c];
+      }
+    double beta = rr_new / rr;
+    rr = rr_new;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+    for (int64_t c = 0; c < n; c++)
+      if (m[c]) p[c] = r[c] + beta * p[c];
+  }
+  st->iterations = it;
+  st->resid = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  free(r); free(p); free(q); free(S.smask);
+  return XFO_OK;
+}
+
+/* TSLAE::SolveByScalarRunning, XSLAE.cpp:416-445. */
+void xfo_thomas(int M, double* u, const double* a, const double* b, const double* c, const double* f) {
+  double* A = (double*)malloc(sizeof(double) * (M + 1));
+  double* B = (double*)malloc(sizeof(double) * (M + 1));
+  A[0] = 0;
+  B[0] = u[0];
+  A[M] = B[M] = 0;
+  for (int m = 1; m < M; m++) {
+    A[m] = (-c[m]) / (a[m] * A[m - 1] + b[m]);
+    B[m] = (f[m] - a[m] * B[m - 1]) / (a[m] * A[m - 1] + b[m]);
+  }
+  for (int m = M - 1; m > 0; m--) u[m] = A[m] * u[m + 1] + B[m];
+  free(A);
+  free(B);
+}
+
+/* ------------------------------------------------------------------------ */
+#define IB_RANGE 3
+
+/* TImmersedBoundaryProblem::Index(grid, coord, type, axis, 3, 3), XProblem.cpp:8931-8967. */
+static int ib_index(double coord, double step, int nend, int type, int axis) {
+  int index = (int)floor((coord + (type != axis ? 0.5 * step : 0)) / step);
+  if (index > (nend - 1) - IB_RANGE) index = (nend - 1) - IB_RANGE;
+  if (index < IB_RANGE) index = IB_RANGE;
+  return index;
+}
+/* Coord(grid, index, type, axis), XProblem.cpp:8988-9006. */
+static double ib_coord(int index, double step, int type, int axis) {
+  return index * step - (type != axis ? 0.5 * step : 0);
+}
+/* OptimalDirichlet, XProblem.cpp:9008-9032 (cosine delta). */
+static double ib_delta(double distance, double h) {
+  if (distance < 2 * h) return 1.0 / (4 * h) * (1 + cos(M_PI * distance / (2 * h)));
+  return 0;
+}
+
+/* TImmersedBoundaryProblem::Interpolate, XProblem.cpp:8620-8791. h0 holds
+ * Separation[0] of the three separators; the box has n-1 intervals per axis. */
+void xfo_ib_interpolate(const double* vel, int n1, int n2, int n3, const double* h0, int axis, int nn,
+                        const double* pos, double* node_vel) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const double cb = h0[axis - 1] * h0[axis - 1] * h0[axis - 1];
+  for (int q = 0; q < nn; q++) {
+    double px = pos[3 * q], py = pos[3 * q + 1], pz = pos[3 * q + 2];
+    int xi = ib_index(px, h0[0], n1 - 1, 1, axis);
+    int yi = ib_index(py, h0[1], n2 - 1, 2, axis);
+    int zi = ib_index(pz, h0[2], n3 - 1, 3, axis);
+    double acc = 0;
+    for (int i = xi - IB_RANGE; i <= xi + IB_RANGE; ++i)
+      for (int j = yi - IB_RANGE; j <= yi + IB_RANGE; ++j)
+        for (int k = zi - IB_RANGE; k <= zi + IB_RANGE; ++k) {
+          double wx = ib_delta(fabs(px - ib_coord(i, h0[0], 1, axis)), h0[0]);
+          double wy = ib_delta(fabs(py - ib_coord(j, h0[1], 2, axis)), h0[1]);
+          double wz = ib_delta(fabs(pz - ib_coord(k, h0[2], 3, axis)), h0[2]);
+          acc += (vel[i * s1 + j * s2 + k] * wx * wy * wz) * cb;
+        }
+    node_vel[q] = acc;
+  }
+}
+
+/* UpdateBoundaryPosition, XProblem.cpp:8858-8894. */
+void xfo_ib_update(int nn, int axis, double tau, const double* node_vel, double* pos) {
+  for (int q = 0; q < nn; q++) pos[3 * q + axis - 1] += node_vel[q] * tau;
+}
+
+/* ComputeBoundaryForces, XProblem.cpp:8436-8547, with the node laws of
+ * XImmersedBoundary.cpp:654-757.  params = {stiffness, stretchingStiffness,
+ * bendingStiffness, area}.  Runs in node order (the reference's loop with one
+ * thread; with several it races on neighbours' forces). */
+void xfo_ib_forces(int nn, int axis, const double* pos, const double* ref, const int32_t* kind,
+                   const int32_t* next, const int32_t* prev, const double* dist0, const double* curv0,
+                   const double* node_stiff, const double* params, double* force) {
+  const int a = axis - 1;
+  const double stiffness = params[0], kst = params[1], kbend = params[2], area = params[3];
+  for (int q = 0; q < nn; q++) force[q] = 0;
+  for (int q = 0; q < nn; q++) {
+    double sf = 0, bf = 0, tf = 0;
+    int nx = next[q], pv = prev[q];
+    int kd = kind[q];
+    if ((kd == 0 || kd == 2 || kd == 4) && nx >= 0) {
+      double DX = pos[3 * q] - pos[3 * nx], DY = pos[3 * q + 1] - pos[3 * nx + 1], DZ = pos[3 * q + 2] - pos[3 * nx + 2];
+      double distance = sqrt(DX * DX + DY * DY + DZ * DZ);
+      double distance_axis = pos[3 * q + a] - pos[3 * nx + a];
+      double k = kd == 2 ? node_stiff[q] : kst;
+      sf = k * (distance - dist0[q]) * distance_axis / distance;
+    }
+    if (kd == 0 && nx >= 0 && pv >= 0) {
+      double curv = pos[3 * nx + a] - 2 * pos[3 * q + a] + pos[3 * pv + a];
+      bf = kbend * (curv0[3 * q + a] - curv);
+    }
+    if (kd == 1 || kd == 4) tf = stiffness * (pos[3 * q + a] - ref[3 * q + a]);
+    if (kd == 2) tf = node_stiff[q] * (pos[3 * q + a] - ref[3 * q + a]);
+    force[q] += -(sf + 2 * bf + tf) * area;
+    if (nx >= 0) force[nx] += (sf + bf) * area;
+    if (pv >= 0) force[pv] += bf * area;
+  }
+}
+
+/* SpreadForce, XProblem.cpp:8550-8617 (arithmetic only; the FIXED-node mask
+ * rewrite is not part of it). fbox must already hold the zeroed force. */
+void xfo_ib_spread(double* fbox, int n1, int n2, int n3, const double* h0, int axis, int nn, const double* pos,
+                   const double* force) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  for (int q = 0; q < nn; q++) {
+    double px = pos[3 * q], py = pos[3 * q + 1], pz = pos[3 * q + 2];
+    int xi = ib_index(px, h0[0], n1 - 1, 1, axis);
+    int yi = ib_index(py, h0[1], n2 - 1, 2, axis);
+    int zi = ib_index(pz, h0[2], n3 - 1, 3, axis);
+    for (int i = xi - IB_RANGE; i <= xi + IB_RANGE; ++i)
+      for (int j = yi - IB_RANGE; j <= yi + IB_RANGE; ++j)
+        for (int k = zi - IB_RANGE; k <= zi + IB_RANGE; ++k) {
+          double wx = ib_delta(fabs(px - ib_coord(i, h0[0], 1, axis)), h0[0]);
+          double wy = ib_delta(fabs(py - ib_coord(j, h0[1], 2, axis)), h0[1]);
+          double wz = ib_delta(fabs(pz - ib_coord(k, h0[2], 3, axis)), h0[2]);
+          fbox[i * s1 + j * s2 + k] += (force[q] * wx * wy * wz);
+        }
+  }
+}

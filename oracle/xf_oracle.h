@@ -1,0 +1,82 @@
+/* Test infrastructure only: CPU restatement of the reference algorithms on the
+ * pressure-projection path.  Used by tests/ (as the checker), by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline / reference arm.
+ * Nothing in the product links this library.
+ *
+ * Layout: every box is (n1, n2, n3) float64 in C order (k fastest), exactly the
+ * reference's double*** [i][j][k] flattened.  Codes are int32 point codes
+ * (XMask.h:6-7, XGrid.h:11, XOperator.h:13-18); normals are 3 float64 per cell,
+ * all-zero meaning "no normal".  Each routine cites the reference lines it
+ * restates; with threads == 1 every loop runs in the reference's order.
+ */
+#ifndef XF_ORACLE_H
+#define XF_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { XFO_OK = 0, XFO_ERR_MASK = 3, XFO_ERR_ARG = 1 };
+enum { XFO_OP_LAPLACE = 0, XFO_OP_VARDIV = 1 };
+
+void xfo_set_threads(int n);
+int xfo_get_threads(void);
+
+void xfo_space_mask(const int32_t* codes, int64_t ncell, uint8_t* smask);
+int64_t xfo_rn_map(const uint8_t* smask, int n1, int n2, int n3, int32_t* inv_box, int32_t* fwd_ijk);
+int xfo_validate(int op, const int32_t* codes, const double* normals, int n1, int n2, int n3, int64_t* bad_cell);
+
+/* y = A x (sign 0), A x + s (sign +1), A x - s (sign -1) on active cells. */
+int xfo_apply(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+              const double* hz, const double* density, int n1, int n2, int n3, const double* x,
+              const double* s, int sign, double* y);
+
+void xfo_lincomb(double p1, const double* s1, double p2, const double* s2, const uint8_t* smask,
+                 int64_t ncell, double* z);
+double xfo_dot(const double* a, const double* b, const uint8_t* smask, int64_t ncell);
+double xfo_norm(const double* a, const uint8_t* smask, int64_t ncell);
+double xfo_absmax(const double* a, const uint8_t* smask, const int32_t* inv_box, int64_t ncell, int32_t* rn_index);
+
+typedef struct {
+  int iterations;
+  double resid;      /* the quantity the stopping rule tested last */
+  int status;        /* 0 converged, 13 iteration cap hit */
+} xfo_stats;
+
+/* Reference solvers, same arithmetic sequence as XSLAE.cpp; maxit caps the
+ * loop (the reference has none), eps as the reference hard-codes when <= 0. */
+int xfo_cg_reference(int op, const int32_t* codes, const double* normals, const double* hx,
+                     const double* hy, const double* hz, const double* density, int n1, int n2, int n3,
+                     const double* x0, const double* b, double eps, int maxit, double* result, xfo_stats* st);
+int xfo_bicgstab_reference(int op, const int32_t* codes, const double* normals, const double* hx,
+                           const double* hy, const double* hz, const double* density, int n1, int n2,
+                           int n3, const double* x0, const double* b, double eps, int maxit, double* result,
+                           xfo_stats* st);
+int xfo_minres_reference(int op, const int32_t* codes, const double* normals, const double* hx,
+                         const double* hy, const double* hz, const double* density, int n1, int n2, int n3,
+                         const double* x0, const double* b, double eps, int maxit, double* result,
+                         xfo_stats* st);
+/* Plain Hestenes-Stiefel CG to ||b - A x||_2 <= rtol ||b||_2 (the FP64 judge). */
+int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                 const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
+                 const double* b, double rtol, int maxit, double* result, xfo_stats* st);
+
+void xfo_thomas(int M, double* u, const double* a, const double* b, const double* c, const double* f);
+
+/* Immersed boundary (XProblem.cpp:8436-9046, XImmersedBoundary.cpp:654-759).
+ * Nodes: pos/ref 3 per node; kind 0 elastic, 1 target, 2 fixed-elastic,
+ * 3 plain, 4 fixed-stretching; next/prev -1 for none. axis 1..3. */
+void xfo_ib_interpolate(const double* vel, int n1, int n2, int n3, const double* h0, int axis, int nn,
+                        const double* pos, double* node_vel);
+void xfo_ib_update(int nn, int axis, double tau, const double* node_vel, double* pos);
+void xfo_ib_forces(int nn, int axis, const double* pos, const double* ref, const int32_t* kind,
+                   const int32_t* next, const int32_t* prev, const double* dist0, const double* curv0,
+                   const double* node_stiff, const double* params, double* force);
+void xfo_ib_spread(double* fbox, int n1, int n2, int n3, const double* h0, int axis, int nn, const double* pos,
+                   const double* force);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -31,7 +31,10 @@ def run(task, rec):
         write_bag(fin, rec)
         if os.environ.get("XF_KEEP_INPUT"):
             write_bag(os.environ["XF_KEEP_INPUT"], rec)
-        p = subprocess.run([DRIVER, task, fin, fout], capture_output=True, text=True, timeout=300)
+        # One OpenMP thread: ComputeBoundaryForces (XProblem.cpp:8541-8544) races
+        # on neighbours' forces when run with more.
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        p = subprocess.run([DRIVER, task, fin, fout], capture_output=True, text=True, timeout=300, env=env)
         if p.returncode != 0:
             return None, p.stderr.strip()
         return read_bag(fout), None
