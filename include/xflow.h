@@ -1,0 +1,190 @@
+/* xflow_gb300: GB300-native (sm_103a) pressure-projection path of xFlow.
+ *
+ * C ABI only: plain pointers, sizes and status codes; no C++ types and no
+ * exceptions cross it.  One context owns one CUDA stream on one device and is
+ * not thread-safe.  Every call returns XF_OK (0) or an XF_* status; on error
+ * xf_last_error() holds a one-line reason.
+ *
+ * Data convention (identical to the reference): a grid of N x L x M intervals
+ * has a box of n1 = N+1, n2 = L+1, n3 = M+1 cells, stored C-order with k
+ * fastest, exactly the reference's double*** [i][j][k] flattened.  Point codes
+ * are the reference's (XMask.h:6-7, XGrid.h:11, XOperator.h:13-18):
+ *   0 Fictive, 1 Actual, 3 Defined, 4 PreDefined, 5 Normal, 6 PreNormal,
+ *   7 Equation, 8 PreEquation.
+ * Rn indices are 1-based in i->j->k order (XSpaceModel.cpp:383-406).
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef XFLOW_H
+#define XFLOW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  XF_OK = 0,
+  XF_ERR_ARG = 1,        /* bad argument (null pointer, size mismatch)        */
+  XF_ERR_CUDA = 2,       /* CUDA runtime error                                 */
+  XF_ERR_MASK = 3,       /* a row the reference throws on (XOperator.cpp:1037, */
+                         /* 1043-1055, 1075-1080, 1122) or would read outside  */
+                         /* its arrays                                         */
+  XF_ERR_NOMEM = 4,
+  XF_ERR_STATE = 5,      /* object used with the wrong grid / dtype            */
+  XF_ERR_UNSUPPORTED = 6,
+  XF_STALL = 10,         /* solver made no progress                            */
+  XF_DIVERGED = 11,
+  XF_NAN = 12,
+  XF_MAXIT = 13,         /* iteration cap reached (the reference has none)     */
+  XF_BREAKDOWN = 14      /* zero denominator (XSLAE.cpp:274-275)               */
+};
+
+enum { XF_F64 = 0, XF_F32 = 1 };
+
+/* Operators (XOperator.h:292-319, 410-423). */
+enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1 };
+
+/* xf_matvec flags */
+enum {
+  XF_EXACT = 1,          /* FP64 only: the reference's operation order, bit-exact */
+  XF_ZERO_INACTIVE = 2   /* write 0 to inactive cells instead of leaving them   */
+};
+
+typedef struct xf_ctx xf_ctx;
+typedef struct xf_grid xf_grid;
+typedef struct xf_vec xf_vec;
+typedef struct xf_op xf_op;
+
+/* ---- context ------------------------------------------------------------- */
+int xf_create(int device, xf_ctx** out);
+int xf_destroy(xf_ctx* ctx);
+const char* xf_last_error(const xf_ctx* ctx);
+const char* xf_status_string(int status);
+int xf_synchronize(xf_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work against it. */
+void* xf_stream(xf_ctx* ctx);
+
+/* ---- grid: T3dNormalGrid + TRnRelease3dSpaceModel ------------------------- */
+/* Replaces T3dNormalGrid(sep1, sep2, sep3, mask, normals) (XGrid.h:282) and
+ * TRnRelease3dSpaceModel(1, masks) (XSpaceModel.h:499-533, built as
+ * XProblem.cpp:4116-4207 does).  codes: n1*n2*n3 int32; hx: n1-1 separations
+ * (TSeparator::Separation), hy: n2-1, hz: n3-1; normals: 3 doubles per cell or
+ * NULL, all-zero meaning no normal.  Host pointers. */
+int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t* codes, const double* hx,
+                   const double* hy, const double* hz, const double* normals, xf_grid** out);
+int xf_grid_destroy(xf_grid* g);
+/* TRnSpaceModel::EndIndex (XSpaceModel.h:50-54): number of active cells. */
+int xf_grid_end_index(const xf_grid* g, int64_t* end_index);
+/* Rn numbering (XSpaceModel.cpp:383-406), computed on the GPU: inv_box gets
+ * the 1-based Rn index of each cell (0 when inactive), fwd_ijk 3 ints (i,j,k)
+ * per Rn index.  Host pointers, either may be NULL. */
+int xf_grid_rn_map(const xf_grid* g, int32_t* inv_box, int32_t* fwd_ijk);
+/* Space mask 0/1 per cell (XProblem.cpp:4155-4182).  Host pointer. */
+int xf_grid_space_mask(const xf_grid* g, uint8_t* smask_box);
+/* Validity of the grid for an operator: XF_OK or XF_ERR_MASK with the first
+ * offending cell (flat index) in bad_cell. */
+int xf_grid_check(const xf_grid* g, int op, int64_t* bad_cell);
+
+/* ---- vectors: TRnRelease3dSpace ------------------------------------------ */
+/* Replaces TRnRelease3dSpace(model) (XSpace.h:595-633): a device box of the
+ * grid's shape, zero-filled like TRnRelease3dData (XSpace.cpp:2213-2225). */
+int xf_vec_create(xf_grid* g, int dtype, xf_vec** out);
+int xf_vec_destroy(xf_vec* v);
+int xf_vec_upload(xf_vec* v, const double* host_box);        /* whole box      */
+int xf_vec_download(const xf_vec* v, double* host_box);      /* whole box      */
+/* TSpace::Assign (XSpace.cpp:2343-2361): whole-box copy (dtypes may differ). */
+int xf_vec_assign(xf_vec* dst, const xf_vec* src);
+/* x |= c on active cells (XSpace.cpp:2424-2487 for c = 0). */
+int xf_vec_fill(xf_vec* v, double c);
+/* Raw device pointer of the box (double* or float*). */
+void* xf_vec_data(xf_vec* v);
+
+/* ---- operators ----------------------------------------------------------- */
+/* T3dLaplaceOperator (XOperator.cpp:809-1129) or
+ * T3dVariableDivergentedOperator (XOperator.cpp:1901-2293). */
+int xf_op_create(xf_grid* g, int kind, xf_op** out);
+int xf_op_destroy(xf_op* op);
+/* T3dVariableDivergentedOperator::withDensity (XOperator.cpp:2235-2268):
+ * copies the density box (host pointer, n1*n2*n3 doubles). */
+int xf_op_set_density(xf_op* op, const double* host_density_box);
+
+/* y |= A(x) + sign*s  (sign 0, +1, -1; s may be NULL for sign 0), on active
+ * cells: TRnRelease3dSpace::LocalReleaseAssignSpeedLinearCombination(op)
+ * (XSpace.cpp:3013-3217).  Inactive cells of y are left as they are, or set
+ * to 0 with XF_ZERO_INACTIVE.  With opt_dot non-NULL also returns (w, y) over
+ * active cells for w = opt_w (or x when opt_w is NULL) in FP64. */
+int xf_matvec(xf_op* op, const xf_vec* x, xf_vec* y, const xf_vec* s, int sign, int flags,
+              const xf_vec* opt_w, double* opt_dot);
+
+/* ---- vector algebra: TRnRelease3dSpace masked loops ---------------------- */
+/* z |= p1*s1 + p2*s2 on active cells (XSpace.cpp:2489-3010); s2 may be NULL. */
+int xf_lincomb(double p1, const xf_vec* s1, double p2, const xf_vec* s2, xf_vec* z);
+/* (a, b) over active cells, FP64 (XSpace.cpp:3261-3342). */
+int xf_dot(const xf_vec* a, const xf_vec* b, double* out);
+/* TNormalizedSpace::Norma: sqrt of the masked sum of squares
+ * (XSpace.cpp:3219-3259, 1205-1217). */
+int xf_norm(const xf_vec* a, double* out);
+/* (x, A y) (XSpace.cpp:3344-3419). */
+int xf_dot_op(xf_op* op, const xf_vec* x, const xf_vec* y, double* out);
+/* GetAbsMaxElement(index) (XSpace.cpp:3428-3487, type 1): the first strict
+ * maximum of |a| in i->j->k order and its Rn index (1 when all are 0). */
+int xf_absmax(const xf_vec* a, double* out, int64_t* rn_index);
+
+/* ---- solvers: TSLAE ------------------------------------------------------- */
+enum {
+  XF_CG = 0,             /* Hestenes-Stiefel CG, relative tolerance (FP64 judge)   */
+  XF_CG_REFERENCE = 1,   /* TSLAE::SolveByConjugateGradients, XSLAE.cpp:56-157     */
+  XF_BICGSTAB = 2,       /* TSLAE::SolveByBiConjugateGradientsStab, :667-768       */
+  XF_MINRES = 3,         /* TSLAE::SolveByMinimalResiduals, :350-414               */
+  XF_BICG = 4,           /* TSLAE::SolveByBiConjugateGradients, :159-348           */
+  XF_FCG = 5             /* flexible CG with a preconditioner                      */
+};
+enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
+enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2 };
+
+typedef struct {
+  int method;            /* XF_CG ...                                              */
+  int precision;         /* XF_PREC_FP64 or XF_PREC_MIXED (CG only)                */
+  int precond;           /* XF_PRECOND_*                                           */
+  int maxit;             /* iteration cap; 0 = 100000                              */
+  double rtol;           /* relative tolerance on ||b - A x||_2 / ||b||_2 (XF_CG,  */
+                         /* XF_FCG, mixed); <= 0 means 1e-8                        */
+  double atol;           /* absolute tolerance of the reference-semantics methods; */
+                         /* <= 0 means the reference's hard-coded value            */
+  int replace_every;     /* mixed: true-residual replacement period (50)           */
+  int check_every;       /* host polls the device convergence flag every this     */
+                         /* many iterations (16)                                   */
+  int exact;             /* reference-semantics methods: use XF_EXACT matvecs      */
+  int reserved[7];
+} xf_solve_opts;
+
+typedef struct {
+  int status;            /* XF_OK or XF_MAXIT / XF_BREAKDOWN / XF_NAN / XF_STALL   */
+  int iterations;        /* inner (Krylov) iterations                              */
+  int replacements;      /* mixed: true-residual replacements done                 */
+  int fallbacks;         /* FCG: times it fell back to plain CG                    */
+  double rel_resid;      /* final true ||b - A x||_2 / ||b||_2, FP64               */
+  double abs_resid;      /* final value the method's own stopping rule tested      */
+  double ms;             /* device time of the solve                               */
+  double reserved[4];
+} xf_solve_stats;
+
+void xf_solve_opts_default(xf_solve_opts* o);
+/* TSLAE(A, x, b) + SolveBy*() + Result (XSLAE.h:12-35): x holds the initial
+ * guess on entry (warm start as TSLAE::UpdateP, XSLAE.cpp:37-40) and the
+ * result on exit.  x and b are FP64 vectors of op's grid. */
+int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, xf_solve_stats* stats);
+/* The same with host boxes (upload b and x, solve, download x): the call a
+ * host-resident caller such as the reference's time loop makes. */
+int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
+                  xf_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XFLOW_H */

@@ -1,0 +1,257 @@
+"""xflow_gb300: GB300-native pressure-projection path of xFlow.
+
+Python front of the C ABI (include/xflow.h).  The objects mirror the
+reference's surface: Grid ~ T3dNormalGrid + TRnRelease3dSpaceModel,
+Vec ~ TRnRelease3dSpace, Operator ~ T3dLaplaceOperator /
+T3dVariableDivergentedOperator, SLAE ~ TSLAE (XSLAE.h:9-48).  Every call runs
+on the GPU through libxflow.so; a missing library raises, nothing falls back
+to the CPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import (XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_MINRES,  # noqa: F401
+                   XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_ZERO_INACTIVE, XFError)
+
+
+def _check(ctx_handle, st):
+    if st != capi.XF_OK:
+        msg = capi.lib().xf_last_error(ctx_handle) if ctx_handle else b""
+        raise XFError(st, (msg or capi.lib().xf_status_string(st)).decode())
+
+
+class Context:
+    def __init__(self, device=0):
+        L = capi.lib()
+        h = C.c_void_p()
+        st = L.xf_create(device, C.byref(h))
+        if st != capi.XF_OK:
+            raise XFError(st, "xf_create failed (no CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            capi.lib().xf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        _check(self.h, capi.lib().xf_synchronize(self.h))
+
+
+class Grid:
+    """Box of point codes with separations and normals (reference layout)."""
+
+    def __init__(self, ctx, codes, hx, hy, hz, normals=None):
+        self.ctx = ctx
+        self.codes = np.ascontiguousarray(codes, dtype=np.int32)
+        self.shape = self.codes.shape
+        hx, hy, hz = (np.ascontiguousarray(a, dtype=np.float64) for a in (hx, hy, hz))
+        nrm = np.ascontiguousarray(normals, dtype=np.float64) if normals is not None else None
+        h = C.c_void_p()
+        _check(ctx.h, capi.lib().xf_grid_create(ctx.h, *self.shape, capi._ptr(self.codes), capi._ptr(hx),
+                                                capi._ptr(hy), capi._ptr(hz), capi._ptr(nrm), C.byref(h)))
+        self.h = h
+        self._keep = (hx, hy, hz)
+
+    @property
+    def end_index(self):
+        e = C.c_int64()
+        _check(self.ctx.h, capi.lib().xf_grid_end_index(self.h, C.byref(e)))
+        return e.value
+
+    def rn_map(self):
+        inv = np.zeros(self.shape, np.int32)
+        fwd = np.zeros((self.end_index, 3), np.int32)
+        _check(self.ctx.h, capi.lib().xf_grid_rn_map(self.h, capi._ptr(inv), capi._ptr(fwd)))
+        return inv, fwd
+
+    def space_mask(self):
+        m = np.zeros(self.shape, np.uint8)
+        _check(self.ctx.h, capi.lib().xf_grid_space_mask(self.h, capi._ptr(m)))
+        return m
+
+    def check(self, op):
+        bad = C.c_int64(-1)
+        st = capi.lib().xf_grid_check(self.h, op, C.byref(bad))
+        return st, bad.value
+
+    def vec(self, data=None, dtype=XF_F64):
+        v = Vec(self, dtype)
+        if data is not None:
+            v.upload(data)
+        return v
+
+    def close(self):
+        if self.h:
+            capi.lib().xf_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Vec:
+    def __init__(self, grid, dtype=XF_F64):
+        self.grid, self.dtype = grid, dtype
+        h = C.c_void_p()
+        _check(grid.ctx.h, capi.lib().xf_vec_create(grid.h, dtype, C.byref(h)))
+        self.h = h
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == int(np.prod(self.grid.shape))
+        _check(self.grid.ctx.h, capi.lib().xf_vec_upload(self.h, capi._ptr(a)))
+        return self
+
+    def download(self):
+        out = np.empty(self.grid.shape, np.float64)
+        _check(self.grid.ctx.h, capi.lib().xf_vec_download(self.h, capi._ptr(out)))
+        return out
+
+    def assign(self, other):
+        _check(self.grid.ctx.h, capi.lib().xf_vec_assign(self.h, other.h))
+        return self
+
+    def fill(self, c):
+        _check(self.grid.ctx.h, capi.lib().xf_vec_fill(self.h, float(c)))
+        return self
+
+    def dot(self, other):
+        out = C.c_double()
+        _check(self.grid.ctx.h, capi.lib().xf_dot(self.h, other.h, C.byref(out)))
+        return out.value
+
+    def norm(self):
+        out = C.c_double()
+        _check(self.grid.ctx.h, capi.lib().xf_norm(self.h, C.byref(out)))
+        return out.value
+
+    def absmax(self):
+        out, idx = C.c_double(), C.c_int64()
+        _check(self.grid.ctx.h, capi.lib().xf_absmax(self.h, C.byref(out), C.byref(idx)))
+        return out.value, idx.value
+
+    def lincomb(self, p1, s1, p2=0.0, s2=None):
+        _check(self.grid.ctx.h, capi.lib().xf_lincomb(float(p1), s1.h, float(p2), s2.h if s2 is not None else None,
+                                                      self.h))
+        return self
+
+    def close(self):
+        if self.h:
+            capi.lib().xf_vec_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Operator:
+    def __init__(self, grid, kind=XF_OP_LAPLACE, density=None):
+        self.grid, self.kind = grid, kind
+        h = C.c_void_p()
+        _check(grid.ctx.h, capi.lib().xf_op_create(grid.h, kind, C.byref(h)))
+        self.h = h
+        if density is not None:
+            self.set_density(density)
+
+    def set_density(self, rho):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        _check(self.grid.ctx.h, capi.lib().xf_op_set_density(self.h, capi._ptr(rho)))
+
+    def apply(self, x, y, s=None, sign=0, flags=0, w=None, want_dot=False):
+        d = C.c_double()
+        _check(self.grid.ctx.h, capi.lib().xf_matvec(self.h, x.h, y.h, s.h if s is not None else None, sign, flags,
+                                                     w.h if w is not None else None,
+                                                     C.byref(d) if want_dot else None))
+        return d.value if want_dot else None
+
+    def dot_op(self, x, y):
+        out = C.c_double()
+        _check(self.grid.ctx.h, capi.lib().xf_dot_op(self.h, x.h, y.h, C.byref(out)))
+        return out.value
+
+    def close(self):
+        if self.h:
+            capi.lib().xf_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_opts(method=XF_CG, precision=XF_PREC_FP64, rtol=1e-8, atol=0.0, maxit=100000, replace_every=50,
+               check_every=16, exact=False):
+    o = capi.SolveOpts()
+    capi.lib().xf_solve_opts_default(C.byref(o))
+    o.method, o.precision, o.rtol, o.atol, o.maxit = method, precision, rtol, atol, maxit
+    o.replace_every, o.check_every, o.exact = replace_every, check_every, int(exact)
+    return o
+
+
+def solve(op, x, b, **kw):
+    """Solve A x = b in place (x holds the initial guess); returns the stats."""
+    o = solve_opts(**kw)
+    st = capi.SolveStats()
+    _check(op.grid.ctx.h, capi.lib().xf_solve(op.h, C.byref(o), x.h, b.h, C.byref(st)))
+    return st
+
+
+def solve_host(op, x_host, b_host, **kw):
+    """Host-buffer solve (upload, solve, download inside one C-ABI call)."""
+    o = solve_opts(**kw)
+    st = capi.SolveStats()
+    _check(op.grid.ctx.h, capi.lib().xf_solve_host(op.h, C.byref(o), capi._ptr(x_host), capi._ptr(b_host),
+                                                   C.byref(st)))
+    return st
+
+
+class SLAE:
+    """TSLAE (XSLAE.h:9-48): holds A, x, b; SolveBy*() writes Result.
+
+    Unlike the reference, the operands stay owned by the caller."""
+
+    def __init__(self, A, x, b):
+        self.A, self.x, self.b = A, x, b
+        self.stats = None
+
+    def UpdateP(self, p):      # XSLAE.cpp:37-40
+        self.x.assign(p)
+
+    def UpdateRP(self, rp):    # XSLAE.cpp:43-46
+        self.b.assign(rp)
+
+    def _run(self, method, **kw):
+        self.stats = solve(self.A, self.x, self.b, method=method, **kw)
+        if self.stats.status != capi.XF_OK:
+            raise XFError(self.stats.status, capi.lib().xf_status_string(self.stats.status).decode())
+        return self.stats
+
+    def SolveByConjugateGradients(self, **kw):
+        return self._run(XF_CG_REFERENCE, **kw)
+
+    def SolveByBiConjugateGradientsStab(self, **kw):
+        return self._run(XF_BICGSTAB, **kw)
+
+    def SolveByMinimalResiduals(self, **kw):
+        return self._run(XF_MINRES, **kw)
+
+    @property
+    def Result(self):
+        return self.x

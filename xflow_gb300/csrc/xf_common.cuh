@@ -1,0 +1,148 @@
+// Internal definitions shared by the xflow_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/xflow.h"
+
+// ---------------------------------------------------------------------------
+// Cell kind byte: bits 0..5 = neighbour in direction (-x,+x,-y,+y,-z,+z) is
+// not Fictive (flux open, XOperator.cpp:1003-1008); bits 6..7 = row kind.
+enum : uint8_t {
+  K_MX = 1, K_PX = 2, K_MY = 4, K_PY = 8, K_MZ = 16, K_PZ = 32,
+  K_ROW_SHIFT = 6,
+  ROW_NONE = 0, ROW_ACTUAL = 1, ROW_PREDEF = 2, ROW_PRENORM = 3
+};
+__host__ __device__ inline int row_of(uint8_t k) { return k >> K_ROW_SHIFT; }
+
+// Fixed reduction geometry: deterministic partial sums (one per block, then a
+// fixed-order final pass by the last block to finish).
+constexpr int RED_THREADS = 256;
+constexpr int RED_MAX_BLOCKS = 1216;  // 152 SMs x 8
+constexpr int NUM_SLOTS = 16;         // independent reductions in flight
+
+// Device-resident scratch of a context.
+struct DevScratch {
+  double partials[NUM_SLOTS][RED_MAX_BLOCKS];
+  unsigned int tickets[NUM_SLOTS];
+  double scalars[256];
+  long long iscalars[64];
+};
+
+struct xf_ctx {
+  int device;
+  int sm_count;
+  cudaStream_t stream;
+  DevScratch* scratch;       // device
+  double* host_scalars;      // pinned, 256 doubles
+  cudaEvent_t ev0, ev1;
+  char err[512];
+};
+
+struct xf_grid {
+  xf_ctx* ctx;
+  int n1, n2, n3;
+  int64_t ncell, s1, s2;
+  int64_t end_index;
+  uint8_t* kind;             // device, per cell
+  uint8_t* smask;            // device, per cell (0/1)
+  int32_t* inv;              // device, Rn index per cell (0 inactive)
+  int32_t* brow_of;          // device, per cell: index into brow arrays or -1
+  int64_t nbrow;             // PreDefined + PreNormal rows
+  double* brow_nrm;          // device, 3 per boundary row
+  double *hx, *hy, *hz;      // device separations (n-1 each)
+  float *fhx, *fhy, *fhz;
+  // fast-path coefficients per index: c?m[i] = 1/(h[i-1]*hh[i]), c?p[i] = 1/(h[i]*hh[i]),
+  // hh[i] = (h[i-1]+h[i])/2; rh = 1/h; rhh = 1/hh
+  double *cxm, *cxp, *cym, *cyp, *czm, *czp;
+  float *fxm, *fxp, *fym, *fyp, *fzm, *fzp;
+  double *rhx, *rhy, *rhz, *rhhx, *rhhy, *rhhz;
+  float *frhx, *frhy, *frhz, *frhhx, *frhhy, *frhhz;
+  int lap_status, vardiv_status;
+  int64_t lap_bad, vardiv_bad;
+};
+
+struct xf_vec {
+  xf_grid* g;
+  int dtype;
+  void* data;
+};
+
+struct xf_op {
+  xf_grid* g;
+  int kind;
+  double* rho;     // device density box (VARDIV)
+  float* rho32;
+  int rho_set;
+};
+
+// ---------------------------------------------------------------------------
+int xf_fail(xf_ctx* ctx, int status, const char* fmt, ...);
+#define XF_CUDA(ctx, call)                                                              \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return xf_fail((ctx), XF_ERR_CUDA, "%s: %s (%s:%d)", #call,  \
+                                          cudaGetErrorString(e_), __FILE__, __LINE__);   \
+  } while (0)
+
+inline int grid_blocks(const xf_ctx* ctx, int64_t n, int threads, int per_sm = 8) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)ctx->sm_count * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+inline int red_blocks(const xf_ctx* ctx, int64_t n) {
+  int b = grid_blocks(ctx, n, RED_THREADS, 8);
+  return b > RED_MAX_BLOCKS ? RED_MAX_BLOCKS : b;
+}
+
+// ---------------------------------------------------------------------------
+// Block reduction helpers (FP64).
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block; result valid in thread 0.  sh must hold 32 doubles.
+__device__ inline double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  return v;
+}
+
+// Publishes this block's partial of `nval` sums into slot partials and returns
+// true in the last block to arrive (all partials visible).  `flag` is shared.
+template <int NV>
+__device__ inline bool publish_partials(DevScratch* S, int slot0, const double (&v)[NV], double* sh, bool* flag) {
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    double s = block_sum(v[q], sh);
+    if (threadIdx.x == 0) S->partials[slot0 + q][blockIdx.x] = s;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned int t = atomicAdd(&S->tickets[slot0], 1u);
+    *flag = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  return *flag;
+}
+
+// In the last block: fixed-order sum of the published partials of slot.
+__device__ inline double finish_partials(DevScratch* S, int slot, double* sh) {
+  __threadfence();
+  double v = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(&S->partials[slot][b]);
+  return block_sum(v, sh);
+}

@@ -1,0 +1,584 @@
+// Krylov solvers of TSLAE (XSLAE.cpp) on the GPU.
+//
+//  XF_CG            Hestenes-Stiefel CG, relative tolerance; FP64, or mixed
+//                   (FP32 matvec / vectors, FP64 dots and scalars, true FP64
+//                   residual replacement every `replace_every` iterations and
+//                   at convergence - reliable updates).
+//  XF_CG_REFERENCE  TSLAE::SolveByConjugateGradients (three-term form).
+//  XF_BICGSTAB      TSLAE::SolveByBiConjugateGradientsStab.
+//  XF_MINRES        TSLAE::SolveByMinimalResiduals.
+//
+// Every iteration is a short chain of kernels whose scalar recurrences run on
+// the device (xf_control.cuh); chunks of iterations are captured in a CUDA
+// graph and the host only polls the device "done" flag between chunks.
+#include <math.h>
+
+#include <functional>
+#include <vector>
+
+#include "xf_control.cuh"
+#include "xf_stencil.cuh"
+
+void xf_mv64(const xf_op* op, const MvReq<double>& q);
+void xf_mv32(const xf_op* op, const MvReq<float>& q);
+int xf_op_ready(const xf_op* op);
+
+#define GUARD_DONE(S) \
+  if ((S)->iscalars[I_DONE]) return;
+
+// ---------------------------------------------------------------------------
+// x += alpha p; r -= alpha q; (r, r) -> SL_B; control CTL_CG_BETA.  Unmasked:
+// the solver keeps p, q, r at zero on inactive cells.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                                                       const T* __restrict__ q, int64_t n, DevScratch* S) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  GUARD_DONE(S);
+  const T alpha = (T)S->scalars[D_ALPHA];
+  double acc = 0.0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    x[c] = x[c] + alpha * p[c];
+    T rv = r[c] - alpha * q[c];
+    r[c] = rv;
+    acc += (double)rv * (double)rv;
+  }
+  double v[1] = {acc};
+  if (publish_partials<1>(S, SL_B, v, sh, &last)) {
+    double t = finish_partials(S, SL_B, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_B] = t;
+      S->tickets[SL_B] = 0;
+      control_step(S, CTL_CG_BETA);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, int64_t n, DevScratch* S) {
+  GUARD_DONE(S);
+  const T beta = (T)S->scalars[D_BETA];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    p[c] = r[c] + beta * p[c];
+}
+
+// Mixed: fold the FP32 correction into the FP64 iterate (x += e; e = 0).
+__global__ void k_fold(double* __restrict__ x, float* __restrict__ e, int64_t n, DevScratch* S, int gated) {
+  if (gated && (S->iscalars[I_DONE] || !S->iscalars[I_NEEDREP])) return;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    x[c] += (double)e[c];
+    e[c] = 0.f;
+  }
+}
+
+// Masked FP64 dot with a control step.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_dot_ctl(const T* __restrict__ a, const T* __restrict__ b,
+                                                         const uint8_t* __restrict__ m, int64_t n, DevScratch* S,
+                                                         int slot, int ctl, int guard) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (guard && S->iscalars[I_DONE]) return;
+  double acc = 0.0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    if (m[c]) acc += (double)a[c] * (double)b[c];
+  double v[1] = {acc};
+  if (publish_partials<1>(S, slot, v, sh, &last)) {
+    double t = finish_partials(S, slot, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[slot] = t;
+      S->tickets[slot] = 0;
+      control_step(S, ctl);
+    }
+  }
+}
+
+// ---- reference-semantics helpers (masked, device scalars) -------------------
+// z = a - d[ci] * s   (TSLAE CG start: xk |= xk_1 - tauk*rk_1)
+__global__ void k_axmy_dev(double* __restrict__ z, const double* __restrict__ a, const double* __restrict__ s,
+                           const uint8_t* __restrict__ m, int64_t n, DevScratch* S, int ci) {
+  GUARD_DONE(S);
+  const double c1 = S->scalars[ci];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) z[i] = a[i] - c1 * s[i];
+}
+
+// XSLAE.cpp:124-134: result = alfak1*xk + (1-alfak1)*xk_1; result -= (tauk1*alfak1)*rk;
+// xk_1 = xk; xk = result.
+__global__ void k_rcg_update(double* __restrict__ xk, double* __restrict__ xk_1, const double* __restrict__ rk,
+                             const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+  GUARD_DONE(S);
+  const double c1 = S->scalars[D_C1], c2 = S->scalars[D_C2], c3 = S->scalars[D_C3];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!m[i]) continue;
+    double res = c1 * xk[i] + c2 * xk_1[i];
+    res = res - c3 * rk[i];
+    xk_1[i] = xk[i];
+    xk[i] = res;
+  }
+}
+
+// XSLAE.cpp:723-727: Pn1 = Rn + bn*(Pn - wn*Vn), in the reference's steps.
+__global__ void k_bcgs_p(double* __restrict__ Pn1, const double* __restrict__ Rn, const double* __restrict__ Pn,
+                         const double* __restrict__ Vn, const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+  GUARD_DONE(S);
+  const double wn = S->scalars[D_WN], bn = S->scalars[D_BN];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!m[i]) continue;
+    double t = wn * Vn[i];
+    t = Pn[i] - t;
+    t = bn * t;
+    Pn1[i] = Rn[i] + t;
+  }
+}
+
+// XSLAE.cpp:732-733: Sn = Rn - an*Vn.
+__global__ void k_bcgs_s(double* __restrict__ Sn, const double* __restrict__ Rn, const double* __restrict__ Vn,
+                         const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+  GUARD_DONE(S);
+  const double an = S->scalars[D_AN];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) Sn[i] = Rn[i] - an * Vn[i];
+}
+
+__device__ __forceinline__ double max_nan_skip(double a, double b) { return b > a ? b : a; }
+__device__ double block_max(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max_nan_skip(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max_nan_skip(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// XSLAE.cpp:738-749: Un += an*Pn1 + wn*Sn; Rn = Sn - wn*Tn; Pn = Pn1; then
+// ||Rn||_inf (NaN never wins, XSpace.cpp:3455-3463) with control `ctl`.
+__global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ Un, double* __restrict__ Rn,
+                                                          double* __restrict__ Pn, const double* __restrict__ Pn1,
+                                                          const double* __restrict__ Sn, const double* __restrict__ Tn,
+                                                          const uint8_t* __restrict__ m, int64_t n, DevScratch* S,
+                                                          int update, int ctl) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (update) GUARD_DONE(S);
+  const double an = S->scalars[D_AN], wn = S->scalars[D_WN];
+  double best = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!m[i]) continue;
+    double r;
+    if (update) {
+      double tmp1 = an * Pn1[i];
+      double tmp2 = tmp1 + wn * Sn[i];
+      Un[i] = Un[i] + tmp2;
+      double t = wn * Tn[i];
+      r = Sn[i] - t;
+      Rn[i] = r;
+      Pn[i] = Pn1[i];
+    } else {
+      r = Rn[i];
+    }
+    best = max_nan_skip(best, fabs(r));
+  }
+  double bm = block_max(best, sh);
+  if (threadIdx.x == 0) {
+    S->partials[SL_D][blockIdx.x] = bm;
+    __threadfence();
+    unsigned int t = atomicAdd(&S->tickets[SL_D], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double q = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) q = max_nan_skip(q, __ldcg(&S->partials[SL_D][b]));
+  q = block_max(q, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[SL_D] = q;
+    S->tickets[SL_D] = 0;
+    control_step(S, ctl);
+  }
+}
+
+// XSLAE.cpp:387: xk = xk + alfa*rk.
+__global__ void k_mr_x(double* __restrict__ xk, const double* __restrict__ rk, const uint8_t* __restrict__ m, int64_t n,
+                       DevScratch* S) {
+  GUARD_DONE(S);
+  const double alfa = S->scalars[D_ALFA];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) xk[i] = xk[i] + alfa * rk[i];
+}
+
+__global__ void k_reset_state(DevScratch* S, double rtol2, double eps, long long maxit, long long repevery, long long mixed) {
+  for (int q = 0; q < 8; q++) S->iscalars[q] = 0;
+  S->iscalars[I_STATUS] = XF_OK;
+  S->iscalars[I_MAXIT] = maxit;
+  S->iscalars[I_REPEVERY] = repevery;
+  S->iscalars[I_MIXED] = mixed;
+  S->scalars[D_RTOL2] = rtol2;
+  S->scalars[D_EPS] = eps;
+  for (int q = 0; q < NUM_SLOTS; q++) S->tickets[q] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Device buffers owned for the duration of one solve.
+struct Bufs {
+  xf_ctx* ctx;
+  std::vector<void*> ptrs;
+  explicit Bufs(xf_ctx* c) : ctx(c) {}
+  template <typename T>
+  T* get(int64_t n, bool zero = true) {
+    void* p = nullptr;
+    if (cudaMallocAsync(&p, n * sizeof(T), ctx->stream) != cudaSuccess) return nullptr;
+    if (zero) cudaMemsetAsync(p, 0, n * sizeof(T), ctx->stream);
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+  ~Bufs() {
+    for (void* p : ptrs) cudaFreeAsync(p, ctx->stream);
+  }
+};
+
+struct HostState { long long done, status, it, repl, kernels; };
+
+static int read_state(xf_ctx* ctx, HostState* hs) {
+  long long tmp[4];
+  XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch->iscalars, 4 * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  memcpy(tmp, ctx->host_scalars, sizeof(tmp));
+  hs->done = tmp[0]; hs->status = tmp[1]; hs->it = tmp[2]; hs->repl = tmp[3];
+  return XF_OK;
+}
+
+// Runs `iter` (which enqueues one iteration) until the device flags done:
+// chunks of `chunk` iterations are captured once into a CUDA graph; the state
+// of chunk k is read while chunk k+1 is already queued.
+static int run_loop(xf_ctx* ctx, const std::function<void()>& iter, int chunk, int maxit, HostState* hs) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  XF_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (int c = 0; c < chunk; c++) iter();
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+  if (ce != cudaSuccess) return xf_fail(ctx, XF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return xf_fail(ctx, XF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+  }
+  long long* hbuf = (long long*)(ctx->host_scalars + 128);  // two 4-entry state slots
+  cudaEvent_t ev[2];
+  cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  const int max_chunks = maxit / chunk + 3;
+  int st = XF_OK;
+  int launched = 0;
+  size_t nodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &nodes);
+  bool done = false;
+  // keep two chunks in flight
+  for (int k = 0; k < max_chunks && !done; k++) {
+    ce = cudaGraphLaunch(exec, ctx->stream);
+    if (ce != cudaSuccess) { st = xf_fail(ctx, XF_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce)); break; }
+    cudaMemcpyAsync(hbuf + 4 * (k & 1), ctx->scratch->iscalars, 4 * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaEventRecord(ev[k & 1], ctx->stream);
+    launched++;
+    if (k >= 1) {
+      cudaEventSynchronize(ev[(k - 1) & 1]);
+      if (hbuf[4 * ((k - 1) & 1)]) done = true;
+    }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  if (st) return st;
+  XF_CUDA(ctx, cudaGetLastError());
+  long long kernels = hs->kernels + (long long)launched * (long long)nodes;
+  int rs = read_state(ctx, hs);
+  hs->kernels = kernels;
+  return rs;
+}
+
+static double read_scalar(xf_ctx* ctx, int idx) {
+  cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->scalars[idx], 8, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return ctx->host_scalars[0];
+}
+
+// True relative residual ||b - A x||_2 / ||b||_2 in FP64 (fast rows).
+static int true_residual(const xf_op* op, const double* x, const double* b, double* tmp, double* rel, double* bbout) {
+  xf_ctx* ctx = op->g->ctx;
+  DevScratch* S = ctx->scratch;
+  k_dot_ctl<double><<<red_blocks(ctx, op->g->ncell), RED_THREADS, 0, ctx->stream>>>(b, b, op->g->smask, op->g->ncell, S, SL_B, CTL_NONE, 0);
+  MvReq<double> q;
+  q.x = x; q.y = tmp; q.s = b; q.sign = -1; q.neg = 1; q.zero_inactive = 1; q.dot_self = 1; q.slot = SL_C;
+  xf_mv64(op, q);
+  XF_CUDA(ctx, cudaGetLastError());
+  double bb = read_scalar(ctx, SL_B), rr = read_scalar(ctx, SL_C + 1);
+  *rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  if (bbout) *bbout = bb;
+  return XF_OK;
+}
+
+// ---------------------------------------------------------------------------
+static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec* bv, xf_solve_stats* st) {
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  DevScratch* S = ctx->scratch;
+  const int64_t n = g->ncell;
+  const bool mixed = o.precision == XF_PREC_MIXED;
+  double* x = (double*)xv->data;
+  const double* b = (const double*)bv->data;
+  Bufs B(ctx);
+  const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
+  int total_it = 0, total_repl = 0;
+  HostState hs = {0, 0, 0, 0, 0};
+  double rel = 0;
+  double *r = nullptr, *p = nullptr, *q = nullptr;
+  float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  if (!mixed) {
+    r = B.get<double>(n); p = B.get<double>(n); q = B.get<double>(n);
+    if (!r || !p || !q) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
+  } else {
+    e32 = B.get<float>(n); r32 = B.get<float>(n); p32 = B.get<float>(n); q32 = B.get<float>(n);
+    if (!e32 || !r32 || !p32 || !q32) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
+  }
+  double* tmp = B.get<double>(n, false);
+  if (!tmp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate residual");
+  for (int attempt = 0; attempt < 3; attempt++) {
+    k_reset_state<<<1, 1, 0, ctx->stream>>>(S, o.rtol * o.rtol, 0.0, o.maxit - total_it, o.replace_every, mixed ? 1 : 0);
+    k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(b, b, g->smask, n, S, SL_B, CTL_NONE, 0);
+    std::function<void()> iter;
+    if (!mixed) {
+      MvReq<double> m0;
+      m0.x = x; m0.y = r; m0.s = b; m0.sign = -1; m0.neg = 1; m0.zero_inactive = 1; m0.dot_self = 1; m0.slot = SL_A;
+      m0.ctl = CTL_CG_INIT;
+      xf_mv64(op, m0);
+      XF_CUDA(ctx, cudaMemcpyAsync(p, r, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+      iter = [=]() {
+        MvReq<double> m1;
+        m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
+        xf_mv64(op, m1);
+        k_cg_xr<double><<<rb, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
+        k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S);
+      };
+    } else {
+      float *e = e32, *r = r32, *p = p32, *q = q32;
+      XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
+      MvReq<double> m0;
+      m0.x = x; m0.y32 = r; m0.s = b; m0.sign = -1; m0.neg = 1; m0.zero_inactive = 1; m0.dot_self = 1; m0.slot = SL_A;
+      m0.ctl = CTL_CG_INIT;
+      xf_mv64(op, m0);
+      XF_CUDA(ctx, cudaMemcpyAsync(p, r, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+      iter = [=]() {
+        MvReq<float> m1;
+        m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
+        xf_mv32(op, m1);
+        k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S);
+        k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 1);
+        MvReq<double> m2;
+        m2.x = x; m2.y32 = r; m2.s = b; m2.sign = -1; m2.neg = 1; m2.zero_inactive = 1; m2.dot_self = 1;
+        m2.slot = SL_C; m2.ctl = CTL_MIXED_REPL; m2.gate = 1;
+        xf_mv64(op, m2);
+        k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S);
+      };
+    }
+    XF_CUDA(ctx, cudaGetLastError());
+    int chunk = o.check_every > 0 ? o.check_every : 16;
+    int rc = run_loop(ctx, iter, chunk, o.maxit - total_it, &hs);
+    if (rc) return rc;
+    total_it += (int)hs.it;
+    total_repl += (int)hs.repl;
+    hs.kernels += 3 + (mixed ? 1 : 0) + 2;
+    if (mixed) {
+      // fold any correction left behind by an early stop (no-op otherwise)
+      k_fold<<<eb, 256, 0, ctx->stream>>>(x, e32, n, S, 0);
+    }
+    int r2 = true_residual(op, x, b, tmp, &rel, nullptr);
+    if (r2) return r2;
+    // The recursive residual can drift from the true one: restart from the
+    // current iterate until the true residual meets the tolerance.
+    if (hs.status != XF_OK || rel <= o.rtol || total_it >= o.maxit) break;
+  }
+  st->status = (int)hs.status;
+  if (st->status == XF_OK && rel > o.rtol) st->status = total_it >= o.maxit ? XF_MAXIT : XF_STALL;
+  st->iterations = total_it;
+  st->replacements = total_repl;
+  st->reserved[0] = (double)hs.kernels;
+  st->rel_resid = rel;
+  st->abs_resid = rel;
+  return XF_OK;
+}
+
+static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec* bv, xf_solve_stats* st) {
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  DevScratch* S = ctx->scratch;
+  const int64_t n = g->ncell;
+  const uint8_t* m = g->smask;
+  double* x = (double*)xv->data;
+  const double* b = (const double*)bv->data;
+  const bool exact = o.exact != 0;
+  Bufs B(ctx);
+  const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
+  std::function<void()> iter;
+  HostState hs = {0, 0, 0, 0, 0};
+  double eps = o.atol;
+  if (o.method == XF_CG_REFERENCE) {
+    if (eps <= 0) eps = 1e-5;   // XSLAE.cpp:64
+    k_reset_state<<<1, 1, 0, ctx->stream>>>(S, 0.0, eps, o.maxit, 1, 0);
+    // xk_1 = copy(x) (whole box); rk_1 = A(xk_1) - b; (rk_1, rk_1)
+    double* xk_1 = B.get<double>(n, false);
+    double* rk = B.get<double>(n);
+    if (!xk_1 || !rk) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    XF_CUDA(ctx, cudaMemcpyAsync(xk_1, x, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    MvReq<double> q0;
+    q0.x = xk_1; q0.y = rk; q0.s = b; q0.sign = -1; q0.dot_self = 1; q0.exact = exact; q0.slot = SL_A; q0.ctl = CTL_RCG_INIT;
+    xf_mv64(op, q0);
+    // tauk = (rk_1,rk_1) / (A rk_1, rk_1)
+    MvReq<double> q1;
+    q1.x = rk; q1.w = rk; q1.exact = exact; q1.slot = SL_A; q1.ctl = CTL_RCG_TAU0;
+    xf_mv64(op, q1);
+    // xk = xk_1 - tauk*rk_1 (x already equals xk_1 on every cell)
+    k_axmy_dev<<<eb, 256, 0, ctx->stream>>>(x, xk_1, rk, m, n, S, D_TAUK);
+    // rk = A(xk) - b
+    MvReq<double> q2;
+    q2.x = x; q2.y = rk; q2.s = b; q2.sign = -1; q2.dot_self = 1; q2.exact = exact; q2.slot = SL_A; q2.ctl = CTL_RCG_RES0;
+    xf_mv64(op, q2);
+    iter = [=]() {
+      MvReq<double> a;
+      a.x = rk; a.w = rk; a.exact = exact; a.slot = SL_A; a.ctl = CTL_RCG_TAU;
+      xf_mv64(op, a);
+      k_rcg_update<<<eb, 256, 0, ctx->stream>>>(x, xk_1, rk, m, n, S);
+      MvReq<double> c;
+      c.x = x; c.y = rk; c.s = b; c.sign = -1; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_RCG_RES;
+      xf_mv64(op, c);
+    };
+  } else if (o.method == XF_BICGSTAB) {
+    if (eps <= 0) eps = 1e-5;   // XSLAE.cpp:669
+    k_reset_state<<<1, 1, 0, ctx->stream>>>(S, 0.0, eps, o.maxit, 1, 0);
+    double *Rn = B.get<double>(n), *sRn = B.get<double>(n), *Pn = B.get<double>(n), *Pn1 = B.get<double>(n);
+    double *Vn = B.get<double>(n), *Sn = B.get<double>(n), *Tn = B.get<double>(n);
+    if (!Rn || !sRn || !Pn || !Pn1 || !Vn || !Sn || !Tn) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    // Rn = b - A(Un)
+    MvReq<double> q0;
+    q0.x = x; q0.y = Rn; q0.s = b; q0.sign = -1; q0.neg = 1; q0.exact = exact;
+    xf_mv64(op, q0);
+    XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
+    iter = [=]() {
+      k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(sRn, Rn, m, n, S, SL_A, CTL_BCGS_PN1, 1);
+      k_bcgs_p<<<eb, 256, 0, ctx->stream>>>(Pn1, Rn, Pn, Vn, m, n, S);
+      MvReq<double> a;
+      a.x = Pn1; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
+      xf_mv64(op, a);
+      k_bcgs_s<<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
+      MvReq<double> c;
+      c.x = Sn; c.y = Tn; c.w = Sn; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_BCGS_WN;
+      xf_mv64(op, c);
+      k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 1, CTL_BCGS_END);
+    };
+  } else if (o.method == XF_MINRES) {
+    if (eps <= 0) eps = 1e-7;   // XSLAE.cpp:358
+    k_reset_state<<<1, 1, 0, ctx->stream>>>(S, 0.0, eps, o.maxit, 1, 0);
+    double *rk = B.get<double>(n), *Ark = B.get<double>(n);
+    if (!rk || !Ark) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    MvReq<double> q0;
+    q0.x = x; q0.y = rk; q0.s = b; q0.sign = -1; q0.dot_self = 1; q0.exact = exact; q0.slot = SL_A; q0.ctl = CTL_MR_INIT;
+    xf_mv64(op, q0);
+    iter = [=]() {
+      MvReq<double> a;
+      a.x = rk; a.y = Ark; a.w = rk; a.dot_self = 1; a.exact = exact; a.slot = SL_A; a.ctl = CTL_MR_ALFA;
+      xf_mv64(op, a);
+      k_mr_x<<<eb, 256, 0, ctx->stream>>>(x, rk, m, n, S);
+      MvReq<double> c;
+      c.x = x; c.y = rk; c.s = b; c.sign = -1; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_MR_RES;
+      xf_mv64(op, c);
+    };
+  } else {
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: method %d not available", o.method);
+  }
+  XF_CUDA(ctx, cudaGetLastError());
+  int chunk = o.check_every > 0 ? o.check_every : 16;
+  int rc = run_loop(ctx, iter, chunk, o.maxit, &hs);
+  if (rc) return rc;
+  double* tmp = B.get<double>(n, false);
+  if (!tmp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+  double own = o.method == XF_BICGSTAB ? read_scalar(ctx, D_NORM) : read_scalar(ctx, D_EPSCUR);
+  double rel = 0;
+  int r2 = true_residual(op, x, b, tmp, &rel, nullptr);
+  if (r2) return r2;
+  st->status = (int)hs.status;
+  st->iterations = (int)hs.it;
+  st->rel_resid = rel;
+  st->abs_resid = own;
+  st->reserved[0] = (double)(hs.kernels + 6);
+  return XF_OK;
+}
+
+extern "C" void xf_solve_opts_default(xf_solve_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->method = XF_CG;
+  o->precision = XF_PREC_FP64;
+  o->precond = XF_PRECOND_NONE;
+  o->maxit = 100000;
+  o->rtol = 1e-8;
+  o->atol = 0.0;
+  o->replace_every = 50;
+  o->check_every = 16;
+  o->exact = 0;
+}
+
+extern "C" int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, xf_solve_stats* stats) {
+  if (!op || !x || !b || !stats) return XF_ERR_ARG;
+  xf_ctx* ctx = op->g->ctx;
+  if (x->g != op->g || b->g != op->g) return xf_fail(ctx, XF_ERR_STATE, "xf_solve: vectors of another grid");
+  if (x->dtype != XF_F64 || b->dtype != XF_F64) return xf_fail(ctx, XF_ERR_STATE, "xf_solve: x and b must be FP64");
+  int st;
+  if ((st = xf_op_ready(op))) return st;
+  xf_solve_opts o;
+  if (opts) o = *opts;
+  else xf_solve_opts_default(&o);
+  if (o.maxit <= 0) o.maxit = 100000;
+  if (o.rtol <= 0) o.rtol = 1e-8;
+  if (o.replace_every <= 0) o.replace_every = 50;
+  if (o.check_every <= 0) o.check_every = 16;
+  memset(stats, 0, sizeof(*stats));
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  if (o.method == XF_CG) st = solve_cg(op, o, x, b, stats);
+  else if (o.method == XF_CG_REFERENCE || o.method == XF_BICGSTAB || o.method == XF_MINRES) st = solve_reference(op, o, x, b, stats);
+  else st = xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: method %d not available", o.method);
+  if (st) {
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+  }
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  XF_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  stats->ms = ms;
+  return XF_OK;
+}
+
+extern "C" int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
+                             xf_solve_stats* stats) {
+  if (!op || !host_x || !host_b) return XF_ERR_ARG;
+  xf_vec *x = nullptr, *b = nullptr;
+  int st = xf_vec_create(op->g, XF_F64, &x);
+  if (st) return st;
+  st = xf_vec_create(op->g, XF_F64, &b);
+  if (st) { xf_vec_destroy(x); return st; }
+  if (!(st = xf_vec_upload(x, host_x)) && !(st = xf_vec_upload(b, host_b)) && !(st = xf_solve(op, opts, x, b, stats)))
+    st = xf_vec_download(x, host_x);
+  xf_vec_destroy(x);
+  xf_vec_destroy(b);
+  return st;
+}
