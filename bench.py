@@ -196,9 +196,13 @@ def main():
     ap.add_argument("--impl", default="xflow", choices=["xflow", "reference"])
     ap.add_argument("--size", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="a few launches of each hot kernel on the full grid (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.kernels_only:
+        return kernels_only(args)
 
     import xflow_gb300 as xf
 
@@ -339,6 +343,30 @@ def main():
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def kernels_only(args):
+    """Three launches of the FP32 and FP64 stencils and 32 iterations of the
+    mixed and FP64 CG on the full workload: a bounded command for ncu."""
+    import xflow_gb300 as xf
+
+    codes, sep, b = workload(args.size)
+    ctx = xf.Context(0)
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    A = xf.Operator(g, xf.XF_OP_LAPLACE)
+    rng = np.random.Generator(np.random.PCG64(1))
+    xh = rng.standard_normal(g.shape)
+    for dt in (xf.XF_F32, xf.XF_F64):
+        p, q = g.vec(xh, dt), g.vec(None, dt)
+        for _ in range(3):
+            A.apply(p, q, flags=xf.XF_ZERO_INACTIVE)
+    bv = g.vec(b)
+    for prec in (xf.XF_PREC_MIXED, xf.XF_PREC_FP64):
+        x = g.vec(np.zeros(g.shape))
+        st = xf.solve(A, x, bv, method=xf.XF_CG, precision=prec, rtol=RTOL, maxit=32)
+        print(f"precision {prec}: {st.iterations} iterations, {st.ms:.2f} ms, status {st.status}")
+    ctx.synchronize()
     return 0
 
 

@@ -8,6 +8,7 @@ on the GPU through libxflow.so; a missing library raises, nothing falls back
 to the CPU.
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -22,10 +23,28 @@ def _check(ctx_handle, st):
         raise XFError(st, (msg or capi.lib().xf_status_string(st)).decode())
 
 
-class Context:
+class _Owned:
+    """A handle whose children are released before it (objects may be
+    collected in any order, so a child whose parent is gone is skipped)."""
+
+    h = None
+
+    def _init_children(self):
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, child):
+        self._children.add(child)
+
+    def _close_children(self):
+        for ch in list(getattr(self, "_children", ())):
+            ch.close()
+
+
+class Context(_Owned):
     def __init__(self, device=0):
         L = capi.lib()
         h = C.c_void_p()
+        self._init_children()
         st = L.xf_create(device, C.byref(h))
         if st != capi.XF_OK:
             raise XFError(st, "xf_create failed (no CUDA device?)")
@@ -33,6 +52,7 @@ class Context:
 
     def close(self):
         if self.h:
+            self._close_children()
             capi.lib().xf_destroy(self.h)
             self.h = None
 
@@ -46,11 +66,12 @@ class Context:
         _check(self.h, capi.lib().xf_synchronize(self.h))
 
 
-class Grid:
+class Grid(_Owned):
     """Box of point codes with separations and normals (reference layout)."""
 
     def __init__(self, ctx, codes, hx, hy, hz, normals=None):
         self.ctx = ctx
+        self._init_children()
         self.codes = np.ascontiguousarray(codes, dtype=np.int32)
         self.shape = self.codes.shape
         hx, hy, hz = (np.ascontiguousarray(a, dtype=np.float64) for a in (hx, hy, hz))
@@ -60,6 +81,7 @@ class Grid:
                                                 capi._ptr(hy), capi._ptr(hz), capi._ptr(nrm), C.byref(h)))
         self.h = h
         self._keep = (hx, hy, hz)
+        ctx._adopt(self)
 
     @property
     def end_index(self):
@@ -91,7 +113,9 @@ class Grid:
 
     def close(self):
         if self.h:
-            capi.lib().xf_grid_destroy(self.h)
+            self._close_children()
+            if self.ctx.h:
+                capi.lib().xf_grid_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -101,12 +125,13 @@ class Grid:
             pass
 
 
-class Vec:
+class Vec(_Owned):
     def __init__(self, grid, dtype=XF_F64):
         self.grid, self.dtype = grid, dtype
         h = C.c_void_p()
         _check(grid.ctx.h, capi.lib().xf_vec_create(grid.h, dtype, C.byref(h)))
         self.h = h
+        grid._adopt(self)
 
     def upload(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
@@ -149,7 +174,8 @@ class Vec:
 
     def close(self):
         if self.h:
-            capi.lib().xf_vec_destroy(self.h)
+            if self.grid.h and self.grid.ctx.h:
+                capi.lib().xf_vec_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -159,12 +185,13 @@ class Vec:
             pass
 
 
-class Operator:
+class Operator(_Owned):
     def __init__(self, grid, kind=XF_OP_LAPLACE, density=None):
         self.grid, self.kind = grid, kind
         h = C.c_void_p()
         _check(grid.ctx.h, capi.lib().xf_op_create(grid.h, kind, C.byref(h)))
         self.h = h
+        grid._adopt(self)
         if density is not None:
             self.set_density(density)
 
@@ -186,7 +213,8 @@ class Operator:
 
     def close(self):
         if self.h:
-            capi.lib().xf_op_destroy(self.h)
+            if self.grid.h and self.grid.ctx.h:
+                capi.lib().xf_op_destroy(self.h)
             self.h = None
 
     def __del__(self):

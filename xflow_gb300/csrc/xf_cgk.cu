@@ -1,0 +1,193 @@
+// The CG iteration's stencil: q = A p for the Laplace operator on the fast
+// path, fused with (p, q) and the CTL_CG_ALPHA control step.
+//
+// Plane march as in xf_stencil.cu, but with a compile-time epilogue and, when
+// the row length allows it, two consecutive cells per thread (8- or 16-byte
+// vector loads along k), which halves the index and load instructions per
+// cell.  FP64 rows use the precomputed diagonal: one DMUL and six DFMA.
+#include "xf_control.cuh"
+#include "xf_stencil.cuh"
+
+template <typename T> struct V2;
+template <> struct V2<float> { typedef float2 type; };
+template <> struct V2<double> { typedef double2 type; };
+
+constexpr int CGK_THREADS = 256;
+
+// PreDefined / PreNormal rows (rare: a branch that is warp-uniform off the
+// boundary).
+template <typename T>
+__device__ __forceinline__ T slow_row(const StencilGrid<T>& g, const T* __restrict__ x, int i, int j, int k, int c, uint8_t kb) {
+  return apply_row<T, XF_OP_LAPLACE, false>(g, x, i, j, k, c, kb);
+}
+
+template <typename T>
+struct CgqArgs {
+  StencilGrid<T> g;
+  const T* __restrict__ x;
+  T* __restrict__ y;
+  const double* __restrict__ diag;
+  DevScratch* S;
+  int chunk;
+};
+
+template <typename T, bool USE_D>
+__device__ __forceinline__ T lap_fast(uint8_t kb, T cxm, T cxp, T cym, T cyp, T czm, T czp, T d, T xm, T xc, T xp,
+                                      T xjm, T xjp, T xkm, T xkp) {
+  if (USE_D) {
+    const T kpx = (kb & K_PX) ? cxp : T(0), kmx = (kb & K_MX) ? cxm : T(0);
+    const T kpy = (kb & K_PY) ? cyp : T(0), kmy = (kb & K_MY) ? cym : T(0);
+    const T kpz = (kb & K_PZ) ? czp : T(0), kmz = (kb & K_MZ) ? czm : T(0);
+    T s = kpx * xp;
+    s = fma(kmx, xm, s);
+    s = fma(kpy, xjp, s);
+    s = fma(kmy, xjm, s);
+    s = fma(kpz, xkp, s);
+    s = fma(kmz, xkm, s);
+    return fma(d, xc, -s);
+  } else {
+    const T tpx = (kb & K_PX) ? cxp * (xp - xc) : T(0);
+    const T tmx = (kb & K_MX) ? cxm * (xc - xm) : T(0);
+    const T tpy = (kb & K_PY) ? cyp * (xjp - xc) : T(0);
+    const T tmy = (kb & K_MY) ? cym * (xc - xjm) : T(0);
+    const T tpz = (kb & K_PZ) ? czp * (xkp - xc) : T(0);
+    const T tmz = (kb & K_MZ) ? czm * (xc - xkm) : T(0);
+    return -(((tpx - tmx) + (tpy - tmy)) + (tpz - tmz));
+  }
+}
+
+// Two cells (k0, k0+1) per thread; needs n3 even (then P is even and every
+// cell pair is 2*sizeof(T)-aligned and inside one k-row).
+template <typename T, bool USE_D>
+__global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q2(CgqArgs<T> a) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  typedef typename V2<T>::type VT;
+  const StencilGrid<T>& g = a.g;
+  const int P = g.n2 * g.n3;
+  const int p0 = 2 * (blockIdx.x * CGK_THREADS + threadIdx.x);
+  const int i0 = blockIdx.y * a.chunk, i1 = min(g.n1, i0 + a.chunk);
+  DotAcc<T> acc;
+  if (p0 < P) {
+    const int j = p0 / g.n3, k0 = p0 - j * g.n3;
+    const int ojm = j > 0 ? -g.n3 : 0, ojp = j < g.n2 - 1 ? g.n3 : 0;
+    const int okm = k0 > 0 ? -1 : 0, okp = k0 + 1 < g.n3 - 1 ? 2 : 1;
+    const T cym = g.cym[j], cyp = g.cyp[j];
+    const T czm0 = g.czm[k0], czp0 = g.czp[k0], czm1 = g.czm[k0 + 1], czp1 = g.czp[k0 + 1];
+    const T* __restrict__ x = a.x;
+    int c = i0 * P + p0;
+    const VT zero = {T(0), T(0)};
+    VT xm = i0 > 0 ? *reinterpret_cast<const VT*>(x + c - P) : zero;
+    VT xc = *reinterpret_cast<const VT*>(x + c);
+    VT xp = i0 + 1 < g.n1 ? *reinterpret_cast<const VT*>(x + c + P) : zero;
+    uchar2 kc = *reinterpret_cast<const uchar2*>(g.kind + c);
+    for (int i = i0; i < i1; i++, c += P) {
+      const VT xpp = i + 2 < g.n1 ? *reinterpret_cast<const VT*>(x + c + 2 * P) : zero;
+      const uchar2 kn = i + 1 < g.n1 ? *reinterpret_cast<const uchar2*>(g.kind + c + P) : make_uchar2(0, 0);
+      const VT xjm = *reinterpret_cast<const VT*>(x + c + ojm);
+      const VT xjp = *reinterpret_cast<const VT*>(x + c + ojp);
+      const T xkm = x[c + okm], xkp = x[c + okp];
+      const T cxm = g.cxm[i], cxp = g.cxp[i];
+      T d0 = 0, d1 = 0;
+      if (USE_D) {
+        const VT dd = *reinterpret_cast<const VT*>(a.diag + c);
+        d0 = dd.x; d1 = dd.y;
+      }
+      VT out;
+      out.x = lap_fast<T, USE_D>(kc.x, cxm, cxp, cym, cyp, czm0, czp0, d0, xm.x, xc.x, xp.x, xjm.x, xjp.x, xkm, xc.y);
+      out.y = lap_fast<T, USE_D>(kc.y, cxm, cxp, cym, cyp, czm1, czp1, d1, xm.y, xc.y, xp.y, xjm.y, xjp.y, xc.x, xkp);
+      const int r0 = row_of(kc.x), r1 = row_of(kc.y);
+      if (r0 > ROW_ACTUAL) out.x = slow_row<T>(g, x, i, j, k0, c, kc.x);
+      if (r1 > ROW_ACTUAL) out.y = slow_row<T>(g, x, i, j, k0 + 1, c + 1, kc.y);
+      if (r0 == ROW_NONE) out.x = T(0);
+      if (r1 == ROW_NONE) out.y = T(0);
+      acc.add(xc.x, out.x);
+      acc.add(xc.y, out.y);
+      *reinterpret_cast<VT*>(a.y + c) = out;
+      xm = xc; xc = xp; xp = xpp; kc = kn;
+    }
+  }
+  double vals[1] = {acc.value()};
+  if (publish_partials<1>(S, SL_A, vals, sh, &last)) {
+    double t = finish_partials(S, SL_A, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_A] = t;
+      S->tickets[SL_A] = 0;
+      control_step(S, CTL_CG_ALPHA);
+    }
+  }
+}
+
+// One cell per thread (any n3).
+template <typename T, bool USE_D>
+__global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q1(CgqArgs<T> a) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  const StencilGrid<T>& g = a.g;
+  const int P = g.n2 * g.n3;
+  const int p = blockIdx.x * CGK_THREADS + threadIdx.x;
+  const int i0 = blockIdx.y * a.chunk, i1 = min(g.n1, i0 + a.chunk);
+  DotAcc<T> acc;
+  if (p < P) {
+    const int j = p / g.n3, k = p - j * g.n3;
+    const int ojm = j > 0 ? -g.n3 : 0, ojp = j < g.n2 - 1 ? g.n3 : 0;
+    const int okm = k > 0 ? -1 : 0, okp = k < g.n3 - 1 ? 1 : 0;
+    const T cym = g.cym[j], cyp = g.cyp[j], czm = g.czm[k], czp = g.czp[k];
+    const T* __restrict__ x = a.x;
+    int c = i0 * P + p;
+    T xm = i0 > 0 ? x[c - P] : T(0);
+    T xc = x[c];
+    T xp = i0 + 1 < g.n1 ? x[c + P] : T(0);
+    uint8_t kc = g.kind[c];
+    for (int i = i0; i < i1; i++, c += P) {
+      const T xpp = i + 2 < g.n1 ? x[c + 2 * P] : T(0);
+      const uint8_t kn = i + 1 < g.n1 ? g.kind[c + P] : (uint8_t)0;
+      const T xjm = x[c + ojm], xjp = x[c + ojp], xkm = x[c + okm], xkp = x[c + okp];
+      const T d = USE_D ? (T)a.diag[c] : T(0);
+      T v = lap_fast<T, USE_D>(kc, g.cxm[i], g.cxp[i], cym, cyp, czm, czp, d, xm, xc, xp, xjm, xjp, xkm, xkp);
+      const int r = row_of(kc);
+      if (r > ROW_ACTUAL) v = slow_row<T>(g, x, i, j, k, c, kc);
+      if (r == ROW_NONE) v = T(0);
+      acc.add(xc, v);
+      a.y[c] = v;
+      xm = xc; xc = xp; xp = xpp; kc = kn;
+    }
+  }
+  double vals[1] = {acc.value()};
+  if (publish_partials<1>(S, SL_A, vals, sh, &last)) {
+    double t = finish_partials(S, SL_A, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_A] = t;
+      S->tickets[SL_A] = 0;
+      control_step(S, CTL_CG_ALPHA);
+    }
+  }
+}
+
+template <typename T>
+static void launch_cg_q(const xf_op* op, const T* x, T* y) {
+  const xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  CgqArgs<T> a;
+  a.g = make_stencil_grid<T>(g, nullptr);
+  a.x = x; a.y = y; a.diag = g->diag; a.S = ctx->scratch;
+  const int P = g->n2 * g->n3;
+  const bool two = (g->n3 % 2) == 0;
+  const int per = two ? 2 : 1;
+  const int bx = (P / per + CGK_THREADS - 1) / CGK_THREADS;
+  int chunk = 16;
+  while ((int64_t)bx * ((g->n1 + chunk - 1) / chunk) > RED_MAX_BLOCKS) chunk *= 2;
+  a.chunk = chunk;
+  dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
+  constexpr bool D = std::is_same<T, double>::value;
+  if (two) k_cg_q2<T, D><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
+  else k_cg_q1<T, D><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
+}
+
+// q = A p with (p, q) -> SL_A and the CG alpha step.  Laplace operators only.
+void xf_cg_q64(const xf_op* op, const double* p, double* q) { launch_cg_q<double>(op, p, q); }
+void xf_cg_q32(const xf_op* op, const float* p, float* q) { launch_cg_q<float>(op, p, q); }

@@ -21,7 +21,7 @@ __host__ __device__ inline int row_of(uint8_t k) { return k >> K_ROW_SHIFT; }
 // Fixed reduction geometry: deterministic partial sums (one per block, then a
 // fixed-order final pass by the last block to finish).
 constexpr int RED_THREADS = 256;
-constexpr int RED_MAX_BLOCKS = 1216;  // 152 SMs x 8
+constexpr int RED_MAX_BLOCKS = 8192;  // partials per slot (stencil grids can be 2-D)
 constexpr int NUM_SLOTS = 16;         // independent reductions in flight
 
 // Device-resident scratch of a context.
@@ -61,6 +61,7 @@ struct xf_grid {
   float *fxm, *fxp, *fym, *fyp, *fzm, *fzp;
   double *rhx, *rhy, *rhz, *rhhx, *rhhy, *rhhz;
   float *frhx, *frhy, *frhz, *frhhx, *frhhy, *frhhz;
+  double* diag;              // device, per cell: diagonal of the Laplace Actual row (fast FP64)
   int lap_status, vardiv_status;
   int64_t lap_bad, vardiv_bad;
 };
@@ -99,8 +100,38 @@ inline int red_blocks(const xf_ctx* ctx, int64_t n) {
   int b = grid_blocks(ctx, n, RED_THREADS, 8);
   return b > RED_MAX_BLOCKS ? RED_MAX_BLOCKS : b;
 }
+__device__ __forceinline__ int lin_block() { return blockIdx.y * gridDim.x + blockIdx.x; }
+__device__ __forceinline__ int num_blocks() { return gridDim.x * gridDim.y; }
 
 // ---------------------------------------------------------------------------
+// Per-thread dot accumulators.  FP64 data: plain FP64 FMA.  FP32 data: the
+// product a*b is split exactly into hi + lo with one FMA (TwoProduct) and
+// summed in float-float (TwoSum), so the per-thread partial carries ~44 bits
+// without touching the FP64 pipe (1/58 of the FP32 rate on GB300); partials
+// are combined in FP64 across threads and blocks.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float s = hi + p;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (p - bp);
+    hi = s;
+    lo = lo + (err + e);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // Block reduction helpers (FP64).
 __device__ inline double warp_sum(double v) {
 #pragma unroll
@@ -128,12 +159,12 @@ __device__ inline bool publish_partials(DevScratch* S, int slot0, const double (
 #pragma unroll
   for (int q = 0; q < NV; q++) {
     double s = block_sum(v[q], sh);
-    if (threadIdx.x == 0) S->partials[slot0 + q][blockIdx.x] = s;
+    if (threadIdx.x == 0) S->partials[slot0 + q][lin_block()] = s;
   }
   if (threadIdx.x == 0) {
     __threadfence();
     unsigned int t = atomicAdd(&S->tickets[slot0], 1u);
-    *flag = (t == gridDim.x - 1);
+    *flag = (t == (unsigned)num_blocks() - 1);
   }
   __syncthreads();
   return *flag;
@@ -143,6 +174,7 @@ __device__ inline bool publish_partials(DevScratch* S, int slot0, const double (
 __device__ inline double finish_partials(DevScratch* S, int slot, double* sh) {
   __threadfence();
   double v = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(&S->partials[slot][b]);
+  const int nb = num_blocks();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += __ldcg(&S->partials[slot][b]);
   return block_sum(v, sh);
 }

@@ -18,7 +18,9 @@ enum {
   D_ALFA = 60, D_RR64
 };
 // integer scalars
-enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED };
+// I_PAUSE: the mixed CG's inner recursion has met the tolerance (or the cap)
+// and waits for the true-residual replacement at the end of its chunk.
+enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED, I_PAUSE };
 
 enum {
   CTL_NONE = 0,
@@ -78,7 +80,8 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       d[D_BETA] = rn / d[D_RR];
       d[D_RR] = rn;
       if (I[I_MIXED]) {
-        if (rn <= d[D_THR] || (I[I_IT] % I[I_REPEVERY]) == 0 || I[I_IT] >= I[I_MAXIT]) I[I_NEEDREP] = 1;
+        // the replacement at the end of the chunk confirms or resumes
+        if (rn <= d[D_THR] || I[I_IT] >= I[I_MAXIT]) I[I_PAUSE] = 1;
       } else {
         if (rn <= d[D_THR]) finish(S, XF_OK);
         else if (I[I_IT] >= I[I_MAXIT]) finish(S, XF_MAXIT);
@@ -89,6 +92,7 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       double r64 = d[SL_C + 1];
       I[I_REPL] += 1;
       I[I_NEEDREP] = 0;
+      I[I_PAUSE] = 0;
       d[D_RR64] = r64;
       if (isnan(r64)) finish(S, XF_NAN);
       else if (r64 <= d[D_THR]) finish(S, XF_OK);

@@ -318,11 +318,30 @@ static int build_coeffs(xf_grid* g, const double* h, int n, double** cm, double*
   return XF_OK;
 }
 
+// Diagonal of each Laplace Actual row in coefficient form: the sum of the
+// open faces' coefficients (0 for every other row).
+__global__ void k_diag(const uint8_t* __restrict__ kind, const double* __restrict__ cxm, const double* __restrict__ cxp,
+                       const double* __restrict__ cym, const double* __restrict__ cyp, const double* __restrict__ czm,
+                       const double* __restrict__ czp, int n1, int n2, int n3, double* __restrict__ diag) {
+  const int64_t n = (int64_t)n1 * n2 * n3, s1 = (int64_t)n2 * n3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t kb = kind[c];
+    double d = 0.0;
+    if (row_of(kb) == ROW_ACTUAL) {
+      const int i = (int)(c / s1), j = (int)((c / n3) % n2), k = (int)(c % n3);
+      d = (((kb & K_PX) ? cxp[i] : 0.0) + ((kb & K_MX) ? cxm[i] : 0.0)) +
+          (((kb & K_PY) ? cyp[j] : 0.0) + ((kb & K_MY) ? cym[j] : 0.0)) +
+          (((kb & K_PZ) ? czp[k] : 0.0) + ((kb & K_MZ) ? czm[k] : 0.0));
+    }
+    diag[c] = d;
+  }
+}
+
 extern "C" int xf_grid_destroy(xf_grid* g) {
   if (!g) return XF_ERR_ARG;
   cudaSetDevice(g->ctx->device);
   cudaStreamSynchronize(g->ctx->stream);
-  void* ptrs[] = {g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
+  void* ptrs[] = {g->diag, g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
                   g->cxm, g->cxp, g->cym, g->cyp, g->czm, g->czp, g->fxm, g->fxp, g->fym, g->fyp, g->fzm, g->fzp,
                   g->rhx, g->rhy, g->rhz, g->rhhx, g->rhhy, g->rhhz, g->frhx, g->frhy, g->frhz, g->frhhx, g->frhhy, g->frhhz};
   for (void* p : ptrs)
@@ -395,6 +414,10 @@ extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t
         (st = build_coeffs(g, hz, n3, &g->czm, &g->czp, &g->fzm, &g->fzp, &g->rhz, &g->rhhz, &g->frhz, &g->frhhz)))
       goto fail;
   }
+  G_TRY(cudaMalloc(&g->diag, n * sizeof(double)));
+  k_diag<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g->kind, g->cxm, g->cxp, g->cym, g->cyp, g->czm, g->czp,
+                                                             n1, n2, n3, g->diag);
+  G_TRY(cudaGetLastError());
   G_TRY(cudaStreamSynchronize(ctx->stream));
 #undef G_TRY
   cleanup();

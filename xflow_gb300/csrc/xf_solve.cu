@@ -12,6 +12,7 @@
 // the device (xf_control.cuh); chunks of iterations are captured in a CUDA
 // graph and the host only polls the device "done" flag between chunks.
 #include <math.h>
+#include <stdlib.h>
 
 #include <functional>
 #include <vector>
@@ -21,6 +22,8 @@
 
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
 void xf_mv32(const xf_op* op, const MvReq<float>& q);
+void xf_cg_q64(const xf_op* op, const double* p, double* q);
+void xf_cg_q32(const xf_op* op, const float* p, float* q);
 int xf_op_ready(const xf_op* op);
 
 #define GUARD_DONE(S) \
@@ -29,21 +32,46 @@ int xf_op_ready(const xf_op* op);
 // ---------------------------------------------------------------------------
 // x += alpha p; r -= alpha q; (r, r) -> SL_B; control CTL_CG_BETA.  Unmasked:
 // the solver keeps p, q, r at zero on inactive cells.
+// 16-byte vector view of T (cudaMalloc'd boxes are 256-byte aligned).
+template <typename T> struct V16;
+template <> struct V16<float> { typedef float4 type; };
+template <> struct V16<double> { typedef double2 type; };
+
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                                                        const T* __restrict__ q, int64_t n, DevScratch* S) {
   __shared__ double sh[32];
   __shared__ bool last;
-  GUARD_DONE(S);
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  typedef typename V16<T>::type VT;
+  constexpr int L = 16 / sizeof(T);
   const T alpha = (T)S->scalars[D_ALPHA];
-  double acc = 0.0;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-    x[c] = x[c] + alpha * p[c];
-    T rv = r[c] - alpha * q[c];
-    r[c] = rv;
-    acc += (double)rv * (double)rv;
+  DotAcc<T> acc;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nv = n / L;
+  for (int64_t v = tid; v < nv; v += stride) {
+    VT xv = reinterpret_cast<const VT*>(x)[v], rv = reinterpret_cast<const VT*>(r)[v];
+    const VT pv = reinterpret_cast<const VT*>(p)[v], qv = reinterpret_cast<const VT*>(q)[v];
+    T* xa = reinterpret_cast<T*>(&xv);
+    T* ra = reinterpret_cast<T*>(&rv);
+    const T* pa = reinterpret_cast<const T*>(&pv);
+    const T* qa = reinterpret_cast<const T*>(&qv);
+#pragma unroll
+    for (int l = 0; l < L; l++) {
+      xa[l] = fma(alpha, pa[l], xa[l]);
+      ra[l] = fma(-alpha, qa[l], ra[l]);
+      acc.add(ra[l], ra[l]);
+    }
+    reinterpret_cast<VT*>(x)[v] = xv;
+    reinterpret_cast<VT*>(r)[v] = rv;
   }
-  double v[1] = {acc};
+  for (int64_t c = nv * L + tid; c < n; c += stride) {
+    x[c] = fma(alpha, p[c], x[c]);
+    T rv = fma(-alpha, q[c], r[c]);
+    r[c] = rv;
+    acc.add(rv, rv);
+  }
+  double v[1] = {acc.value()};
   if (publish_partials<1>(S, SL_B, v, sh, &last)) {
     double t = finish_partials(S, SL_B, sh);
     if (threadIdx.x == 0) {
@@ -54,18 +82,43 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __r
   }
 }
 
+// p = r + beta p.  `after_replace`: the step that follows a true-residual
+// replacement runs even while the inner recursion is paused.
 template <typename T>
-__global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, int64_t n, DevScratch* S) {
-  GUARD_DONE(S);
+__global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, int64_t n, DevScratch* S, int after_replace) {
+  if (S->iscalars[I_DONE] || (!after_replace && S->iscalars[I_PAUSE])) return;
+  typedef typename V16<T>::type VT;
+  constexpr int L = 16 / sizeof(T);
   const T beta = (T)S->scalars[D_BETA];
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
-    p[c] = r[c] + beta * p[c];
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nv = n / L;
+  for (int64_t v = tid; v < nv; v += stride) {
+    VT pv = reinterpret_cast<const VT*>(p)[v];
+    const VT rv = reinterpret_cast<const VT*>(r)[v];
+    T* pa = reinterpret_cast<T*>(&pv);
+    const T* ra = reinterpret_cast<const T*>(&rv);
+#pragma unroll
+    for (int l = 0; l < L; l++) pa[l] = fma(beta, pa[l], ra[l]);
+    reinterpret_cast<VT*>(p)[v] = pv;
+  }
+  for (int64_t c = nv * L + tid; c < n; c += stride) p[c] = fma(beta, p[c], r[c]);
 }
 
 // Mixed: fold the FP32 correction into the FP64 iterate (x += e; e = 0).
-__global__ void k_fold(double* __restrict__ x, float* __restrict__ e, int64_t n, DevScratch* S, int gated) {
-  if (gated && (S->iscalars[I_DONE] || !S->iscalars[I_NEEDREP])) return;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+// mode 0: always; mode 2: unless the solve is done.
+__global__ void k_fold(double* __restrict__ x, float* __restrict__ e, int64_t n, DevScratch* S, int mode) {
+  if (mode == 2 && S->iscalars[I_DONE]) return;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nv = n / 2;
+  for (int64_t v = tid; v < nv; v += stride) {
+    double2 xv = reinterpret_cast<const double2*>(x)[v];
+    const float2 ev = reinterpret_cast<const float2*>(e)[v];
+    xv.x += (double)ev.x;
+    xv.y += (double)ev.y;
+    reinterpret_cast<double2*>(x)[v] = xv;
+    reinterpret_cast<float2*>(e)[v] = make_float2(0.f, 0.f);
+  }
+  for (int64_t c = nv * 2 + tid; c < n; c += stride) {
     x[c] += (double)e[c];
     e[c] = 0.f;
   }
@@ -215,7 +268,7 @@ __global__ void k_mr_x(double* __restrict__ xk, const double* __restrict__ rk, c
 }
 
 __global__ void k_reset_state(DevScratch* S, double rtol2, double eps, long long maxit, long long repevery, long long mixed) {
-  for (int q = 0; q < 8; q++) S->iscalars[q] = 0;
+  for (int q = 0; q < 16; q++) S->iscalars[q] = 0;
   S->iscalars[I_STATUS] = XF_OK;
   S->iscalars[I_MAXIT] = maxit;
   S->iscalars[I_REPEVERY] = repevery;
@@ -258,11 +311,27 @@ static int read_state(xf_ctx* ctx, HostState* hs) {
 // Runs `iter` (which enqueues one iteration) until the device flags done:
 // chunks of `chunk` iterations are captured once into a CUDA graph; the state
 // of chunk k is read while chunk k+1 is already queued.
-static int run_loop(xf_ctx* ctx, const std::function<void()>& iter, int chunk, int maxit, HostState* hs) {
+static int run_loop_direct(xf_ctx* ctx, const std::function<void(int)>& iter, int chunk, int maxit, HostState* hs) {
+  const int max_chunks = maxit / chunk + 3;
+  long long kernels = hs->kernels;
+  for (int k = 0; k < max_chunks; k++) {
+    for (int c = 0; c < chunk; c++) iter(c);
+    int st = read_state(ctx, hs);
+    if (st) return st;
+    if (hs->done) break;
+  }
+  hs->kernels = kernels;
+  return XF_OK;
+}
+
+static int run_loop(xf_ctx* ctx, const std::function<void(int)>& iter, int chunk, int maxit, HostState* hs) {
+  // XF_NO_GRAPH=1: enqueue the same kernels without graph capture (diagnostics).
+  static const bool no_graph = getenv("XF_NO_GRAPH") && getenv("XF_NO_GRAPH")[0] == '1';
+  if (no_graph) return run_loop_direct(ctx, iter, chunk, maxit, hs);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   XF_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (int c = 0; c < chunk; c++) iter();
+  for (int c = 0; c < chunk; c++) iter(c);
   cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
   if (ce != cudaSuccess) return xf_fail(ctx, XF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
   ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -354,21 +423,30 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   for (int attempt = 0; attempt < 3; attempt++) {
     k_reset_state<<<1, 1, 0, ctx->stream>>>(S, o.rtol * o.rtol, 0.0, o.maxit - total_it, o.replace_every, mixed ? 1 : 0);
     k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(b, b, g->smask, n, S, SL_B, CTL_NONE, 0);
-    std::function<void()> iter;
+    std::function<void(int)> iter;
+    int chunk = o.check_every > 0 ? o.check_every : 16;
+    const bool lap = op->kind == XF_OP_LAPLACE;
     if (!mixed) {
       MvReq<double> m0;
       m0.x = x; m0.y = r; m0.s = b; m0.sign = -1; m0.neg = 1; m0.zero_inactive = 1; m0.dot_self = 1; m0.slot = SL_A;
       m0.ctl = CTL_CG_INIT;
       xf_mv64(op, m0);
       XF_CUDA(ctx, cudaMemcpyAsync(p, r, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-      iter = [=]() {
-        MvReq<double> m1;
-        m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
-        xf_mv64(op, m1);
+      iter = [=](int) {
+        if (lap) {
+          xf_cg_q64(op, p, q);
+        } else {
+          MvReq<double> m1;
+          m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
+          xf_mv64(op, m1);
+        }
         k_cg_xr<double><<<rb, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
-        k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S);
+        k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0);
       };
     } else {
+      // One graph chunk = `replace_every` iterations; its last iteration folds
+      // the FP32 correction into x and replaces r by the true FP64 residual.
+      chunk = o.replace_every;
       float *e = e32, *r = r32, *p = p32, *q = q32;
       XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
       MvReq<double> m0;
@@ -376,21 +454,27 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       m0.ctl = CTL_CG_INIT;
       xf_mv64(op, m0);
       XF_CUDA(ctx, cudaMemcpyAsync(p, r, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-      iter = [=]() {
-        MvReq<float> m1;
-        m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
-        xf_mv32(op, m1);
+      const int last = chunk - 1;
+      iter = [=](int c) {
+        if (lap) {
+          xf_cg_q32(op, p, q);
+        } else {
+          MvReq<float> m1;
+          m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
+          xf_mv32(op, m1);
+        }
         k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S);
-        k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 1);
-        MvReq<double> m2;
-        m2.x = x; m2.y32 = r; m2.s = b; m2.sign = -1; m2.neg = 1; m2.zero_inactive = 1; m2.dot_self = 1;
-        m2.slot = SL_C; m2.ctl = CTL_MIXED_REPL; m2.gate = 1;
-        xf_mv64(op, m2);
-        k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S);
+        if (c == last) {
+          k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
+          MvReq<double> m2;
+          m2.x = x; m2.y32 = r; m2.s = b; m2.sign = -1; m2.neg = 1; m2.zero_inactive = 1; m2.dot_self = 1;
+          m2.slot = SL_C; m2.ctl = CTL_MIXED_REPL;
+          xf_mv64(op, m2);
+        }
+        k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, c == last ? 1 : 0);
       };
     }
     XF_CUDA(ctx, cudaGetLastError());
-    int chunk = o.check_every > 0 ? o.check_every : 16;
     int rc = run_loop(ctx, iter, chunk, o.maxit - total_it, &hs);
     if (rc) return rc;
     total_it += (int)hs.it;
@@ -427,7 +511,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
   const bool exact = o.exact != 0;
   Bufs B(ctx);
   const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
-  std::function<void()> iter;
+  std::function<void(int)> iter;
   HostState hs = {0, 0, 0, 0, 0};
   double eps = o.atol;
   if (o.method == XF_CG_REFERENCE) {
@@ -451,7 +535,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     MvReq<double> q2;
     q2.x = x; q2.y = rk; q2.s = b; q2.sign = -1; q2.dot_self = 1; q2.exact = exact; q2.slot = SL_A; q2.ctl = CTL_RCG_RES0;
     xf_mv64(op, q2);
-    iter = [=]() {
+    iter = [=](int) {
       MvReq<double> a;
       a.x = rk; a.w = rk; a.exact = exact; a.slot = SL_A; a.ctl = CTL_RCG_TAU;
       xf_mv64(op, a);
@@ -472,7 +556,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     xf_mv64(op, q0);
     XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
-    iter = [=]() {
+    iter = [=](int) {
       k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(sRn, Rn, m, n, S, SL_A, CTL_BCGS_PN1, 1);
       k_bcgs_p<<<eb, 256, 0, ctx->stream>>>(Pn1, Rn, Pn, Vn, m, n, S);
       MvReq<double> a;
@@ -492,7 +576,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     MvReq<double> q0;
     q0.x = x; q0.y = rk; q0.s = b; q0.sign = -1; q0.dot_self = 1; q0.exact = exact; q0.slot = SL_A; q0.ctl = CTL_MR_INIT;
     xf_mv64(op, q0);
-    iter = [=]() {
+    iter = [=](int) {
       MvReq<double> a;
       a.x = rk; a.y = Ark; a.w = rk; a.dot_self = 1; a.exact = exact; a.slot = SL_A; a.ctl = CTL_MR_ALFA;
       xf_mv64(op, a);

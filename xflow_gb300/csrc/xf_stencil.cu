@@ -1,6 +1,15 @@
 // Operators (T3dLaplaceOperator, T3dVariableDivergentedOperator) and the
 // masked matvec y |= A(x) (+/- s) of TRnRelease3dSpace::
 // LocalReleaseAssignSpeedLinearCombination(op) (XSpace.cpp:3013-3217).
+//
+// Kernel layout (plane march): a thread owns one (j, k) column of the box and
+// walks a chunk of i-planes, keeping x[i-1], x[i], x[i+1] in registers and
+// prefetching plane i+2 while it computes plane i.  Consecutive threads own
+// consecutive k, so every plane access is coalesced; the j+-1 / k+-1
+// neighbours are re-reads of lines the neighbouring threads just fetched (L1/L2).
+#include <type_traits>
+
+#include "xf_control.cuh"
 #include "xf_stencil.cuh"
 
 template <>
@@ -26,11 +35,11 @@ StencilGrid<float> make_stencil_grid<float>(const xf_grid* g, const float* rho) 
   return s;
 }
 
-#include "xf_control.cuh"
+constexpr int MV_THREADS = 256;
 
 // y |= A(x) + sign*s (negated when neg), written to y (T) and/or y32 (float);
-// fused FP64 dots (w, v) -> slot_w and (v, v) -> slot_self; the last block
-// to finish runs the solver control step `ctl`.
+// fused FP64 dots (w, v) -> slot_w and (v, v) -> slot_w+1; the last block to
+// finish runs the solver control step `ctl`.
 template <typename T>
 struct MatvecArgs {
   StencilGrid<T> g;
@@ -39,55 +48,102 @@ struct MatvecArgs {
   float* __restrict__ y32;
   const T* __restrict__ s;
   const T* __restrict__ w;
+  const double* __restrict__ diag;
   int sign, neg, zero_inactive, dot_w, dot_self;
-  int slot_w, slot_self, ctl, gate;
+  int slot_w, ctl, gate, chunk;
   DevScratch* S;
 };
 
-// One warp per k-row (i, j): 32 consecutive cells per step, coalesced.
-template <typename T, int OP, bool EXACT>
-__global__ void __launch_bounds__(256) k_matvec(MatvecArgs<T> a) {
+// Laplace Actual row on register-resident x[i-1], x[i], x[i+1].
+template <typename T, bool USE_D>
+__device__ __forceinline__ T march_lap(const StencilGrid<T>& g, const MatvecArgs<T>& a, int c, int i, uint8_t kb,
+                                       T xm, T xc, T xp, T xjm, T xjp, T xkm, T xkp, T cym, T cyp, T czm, T czp) {
+  const T cxm = g.cxm[i], cxp = g.cxp[i];
+  if (USE_D) {
+    // FP64: y = D x_c - sum_n c_n x_n  (one DMUL and six DFMA per row)
+    const T kpx = (kb & K_PX) ? cxp : T(0), kmx = (kb & K_MX) ? cxm : T(0);
+    const T kpy = (kb & K_PY) ? cyp : T(0), kmy = (kb & K_MY) ? cym : T(0);
+    const T kpz = (kb & K_PZ) ? czp : T(0), kmz = (kb & K_MZ) ? czm : T(0);
+    T acc = (T)a.diag[c] * xc;
+    acc = fma(-kpx, xp, acc);
+    acc = fma(-kmx, xm, acc);
+    acc = fma(-kpy, xjp, acc);
+    acc = fma(-kmy, xjm, acc);
+    acc = fma(-kpz, xkp, acc);
+    acc = fma(-kmz, xkm, acc);
+    return acc;
+  } else {
+    // FP32: the reference's difference form, c * (x_n - x_c)
+    const T tpx = (kb & K_PX) ? cxp * (xp - xc) : T(0);
+    const T tmx = (kb & K_MX) ? cxm * (xc - xm) : T(0);
+    const T tpy = (kb & K_PY) ? cyp * (xjp - xc) : T(0);
+    const T tmy = (kb & K_MY) ? cym * (xc - xjm) : T(0);
+    const T tpz = (kb & K_PZ) ? czp * (xkp - xc) : T(0);
+    const T tmz = (kb & K_MZ) ? czm * (xc - xkm) : T(0);
+    return -(((tpx - tmx) + (tpy - tmy)) + (tpz - tmz));
+  }
+}
+
+template <typename T, int OP, bool EXACT, bool USE_D>
+__global__ void __launch_bounds__(MV_THREADS) k_matvec(MatvecArgs<T> a) {
   __shared__ double sh[32];
   __shared__ bool last;
   // Solver kernels turn into no-ops once the solve is done (or, when gated,
   // while no true-residual replacement is pending).
   if (a.ctl != CTL_NONE && (a.S->iscalars[I_DONE] || (a.gate && !a.S->iscalars[I_NEEDREP]))) return;
   const StencilGrid<T>& g = a.g;
-  const int lane = threadIdx.x & 31;
-  const int warps = blockDim.x >> 5;
-  const int nrows = g.n1 * g.n2;
-  double dw = 0.0, ds = 0.0;
-  for (int r = blockIdx.x * warps + (threadIdx.x >> 5); r < nrows; r += gridDim.x * warps) {
-    const int i = r / g.n2, j = r - i * g.n2;
-    const int base = r * g.n3;
-    for (int k = lane; k < g.n3; k += 32) {
-      const int c = base + k;
-      const uint8_t kb = g.kind[c];
-      if (row_of(kb) == ROW_NONE) {
+  const int P = g.n2 * g.n3;
+  const int p = blockIdx.x * MV_THREADS + threadIdx.x;
+  const int i0 = blockIdx.y * a.chunk;
+  const int i1 = min(g.n1, i0 + a.chunk);
+  DotAcc<T> dw, ds;
+  if (p < P) {
+    const int j = p / g.n3, k = p - j * g.n3;
+    // side offsets clamped to stay inside the box (only used by interior rows)
+    const int okm = k > 0 ? -1 : 0, okp = k < g.n3 - 1 ? 1 : 0;
+    const int ojm = j > 0 ? -g.n3 : 0, ojp = j < g.n2 - 1 ? g.n3 : 0;
+    const bool fast = (OP == XF_OP_LAPLACE) && !EXACT;
+    T cym = 0, cyp = 0, czm = 0, czp = 0;
+    if (fast) { cym = g.cym[j]; cyp = g.cyp[j]; czm = g.czm[k]; czp = g.czp[k]; }
+    const T* __restrict__ x = a.x;
+    int c = i0 * P + p;
+    T xm = i0 > 0 ? x[c - P] : T(0);
+    T xc = x[c];
+    T xp = i0 + 1 < g.n1 ? x[c + P] : T(0);
+    uint8_t kc = g.kind[c];
+    for (int i = i0; i < i1; i++, c += P) {
+      const T xpp = i + 2 < g.n1 ? x[c + 2 * P] : T(0);
+      const uint8_t kn = i + 1 < g.n1 ? g.kind[c + P] : (uint8_t)0;
+      const T xjm = x[c + ojm], xjp = x[c + ojp], xkm = x[c + okm], xkp = x[c + okp];
+      const int row = row_of(kc);
+      if (row == ROW_NONE) {
         if (a.zero_inactive) {
           if (a.y) a.y[c] = T(0);
           if (a.y32) a.y32[c] = 0.f;
         }
-        continue;
+      } else {
+        T v;
+        if (fast && row == ROW_ACTUAL) v = march_lap<T, USE_D>(g, a, c, i, kc, xm, xc, xp, xjm, xjp, xkm, xkp, cym, cyp, czm, czp);
+        else v = apply_row<T, OP, EXACT>(g, x, i, j, k, c, kc);
+        if (a.sign > 0) v = v + a.s[c];
+        else if (a.sign < 0) v = v - a.s[c];
+        if (a.neg) v = -v;
+        if (a.dot_w) dw.add(a.w[c], v);
+        if (a.dot_self) ds.add(v, v);
+        if (a.y) a.y[c] = v;
+        if (a.y32) a.y32[c] = (float)v;
       }
-      T v = apply_row<T, OP, EXACT>(g, a.x, i, j, k, c, kb);
-      if (a.sign > 0) v = v + a.s[c];
-      else if (a.sign < 0) v = v - a.s[c];
-      if (a.neg) v = -v;
-      if (a.dot_w) dw += (double)a.w[c] * (double)v;
-      if (a.dot_self) ds += (double)v * (double)v;
-      if (a.y) a.y[c] = v;
-      if (a.y32) a.y32[c] = (float)v;
+      xm = xc; xc = xp; xp = xpp; kc = kn;
     }
   }
   if (a.dot_w || a.dot_self || a.ctl != CTL_NONE) {
-    double vals[2] = {dw, ds};
+    double vals[2] = {dw.value(), ds.value()};
     if (publish_partials<2>(a.S, a.slot_w, vals, sh, &last)) {
       double tw = finish_partials(a.S, a.slot_w, sh);
       double ts = finish_partials(a.S, a.slot_w + 1, sh);
       if (threadIdx.x == 0) {
         if (a.dot_w) a.S->scalars[a.slot_w] = tw;
-        if (a.dot_self) a.S->scalars[a.slot_self] = ts;
+        if (a.dot_self) a.S->scalars[a.slot_w + 1] = ts;
         a.S->tickets[a.slot_w] = 0;
         control_step(a.S, a.ctl);
       }
@@ -101,21 +157,27 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   xf_ctx* ctx = g->ctx;
   MatvecArgs<T> a;
   a.g = make_stencil_grid<T>(g, rho);
-  a.x = q.x; a.y = q.y; a.y32 = q.y32; a.s = q.s; a.w = q.w;
+  a.x = q.x; a.y = q.y; a.y32 = q.y32; a.s = q.s; a.w = q.w; a.diag = g->diag;
   a.sign = q.sign; a.neg = q.neg; a.zero_inactive = q.zero_inactive;
   a.dot_w = q.w != nullptr; a.dot_self = q.dot_self;
-  // two consecutive partial slots: slot_w and slot_w+1 (self)
-  a.slot_w = q.slot; a.slot_self = q.slot + 1; a.ctl = q.ctl; a.gate = q.gate;
+  a.slot_w = q.slot; a.ctl = q.ctl; a.gate = q.gate;
   a.S = ctx->scratch;
-  const int64_t rows = (int64_t)g->n1 * g->n2;
-  int blocks = grid_blocks(ctx, rows * 32, 256, 8);
-  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  const int P = g->n2 * g->n3;
+  const int bx = (P + MV_THREADS - 1) / MV_THREADS;
+  // plane chunk: ~16 planes per block, fewer chunks if the partial-sum table
+  // would overflow
+  int chunk = 16;
+  while ((int64_t)bx * ((g->n1 + chunk - 1) / chunk) > RED_MAX_BLOCKS) chunk *= 2;
+  a.chunk = chunk;
+  dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
+  const bool use_d = std::is_same<T, double>::value && op->kind == XF_OP_LAPLACE && !q.exact;
   if (op->kind == XF_OP_LAPLACE) {
-    if (q.exact) k_matvec<T, XF_OP_LAPLACE, true><<<blocks, 256, 0, ctx->stream>>>(a);
-    else k_matvec<T, XF_OP_LAPLACE, false><<<blocks, 256, 0, ctx->stream>>>(a);
+    if (q.exact) k_matvec<T, XF_OP_LAPLACE, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    else if (use_d) k_matvec<T, XF_OP_LAPLACE, false, true><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    else k_matvec<T, XF_OP_LAPLACE, false, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
   } else {
-    if (q.exact) k_matvec<T, XF_OP_VARDIV, true><<<blocks, 256, 0, ctx->stream>>>(a);
-    else k_matvec<T, XF_OP_VARDIV, false><<<blocks, 256, 0, ctx->stream>>>(a);
+    if (q.exact) k_matvec<T, XF_OP_VARDIV, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    else k_matvec<T, XF_OP_VARDIV, false, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
   }
 }
 
