@@ -202,8 +202,9 @@ def spheres_case(n, nsph, seed):
 
 
 @pytest.mark.parametrize("precision", [xf.XF_PREC_FP64, xf.XF_PREC_MIXED])
-def test_plain_cg_matches_oracle_cg(ctx, precision):
-    codes, nrm, sep, b = spheres_case(40, 6, 5)
+@pytest.mark.parametrize("n", [40, 25])   # box 42^2 planes take the staged fused path, 27^2 the generic one
+def test_plain_cg_matches_oracle_cg(ctx, precision, n):
+    codes, nrm, sep, b = spheres_case(n, 6, 5)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
     A = xf.Operator(g)
     x, bv = g.vec(np.zeros(g.shape)), g.vec(b)

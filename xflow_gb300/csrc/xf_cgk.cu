@@ -1,10 +1,16 @@
-// The CG iteration's stencil: q = A p for the Laplace operator on the fast
-// path, fused with (p, q) and the CTL_CG_ALPHA control step.
+// Stencil kernels of the CG iterations (Laplace operator, fast rows).
 //
-// Plane march as in xf_stencil.cu, but with a compile-time epilogue and, when
-// the row length allows it, two consecutive cells per thread (8- or 16-byte
-// vector loads along k), which halves the index and load instructions per
-// cell.  FP64 rows use the precomputed diagonal: one DMUL and six DFMA.
+//  q-mode:   q = A p, (p, q) -> SL_A, control CTL_CG_ALPHA (FP32 or FP64).
+//  res-mode: r32 = float(b - A x) in FP64 with (r, r) -> slot+1 and a control
+//            step: the mixed solver's start and its true-residual replacements.
+//
+// Plane march: a thread owns a (j, k) column (two consecutive cells when the
+// row length is even: 8/16-byte vector loads along k) and walks i with
+// x[i-1], x[i], x[i+1] in registers, prefetching plane i+2.  FP64 rows use the
+// precomputed diagonal: one DMUL and six DFMA per cell, the FP64 issue rate
+// being the bound on GB300.
+#include <type_traits>
+
 #include "xf_control.cuh"
 #include "xf_stencil.cuh"
 
@@ -14,22 +20,25 @@ template <> struct V2<double> { typedef double2 type; };
 
 constexpr int CGK_THREADS = 256;
 
-// PreDefined / PreNormal rows (rare: a branch that is warp-uniform off the
-// boundary).
-template <typename T>
-__device__ __forceinline__ T slow_row(const StencilGrid<T>& g, const T* __restrict__ x, int i, int j, int k, int c, uint8_t kb) {
-  return apply_row<T, XF_OP_LAPLACE, false>(g, x, i, j, k, c, kb);
-}
-
 template <typename T>
 struct CgqArgs {
   StencilGrid<T> g;
   const T* __restrict__ x;
   T* __restrict__ y;
   const double* __restrict__ diag;
+  const T* __restrict__ b;     // res-mode right-hand side
+  float* __restrict__ y32;     // res-mode output
   DevScratch* S;
-  int chunk;
+  int chunk, slot, ctl;
 };
+
+// PreDefined / PreNormal rows (rare: a branch that is warp-uniform off the
+// boundary).
+template <typename T>
+__device__ __forceinline__ T slow_row(const StencilGrid<T>& g, const T* __restrict__ x, int i, int j, int k, int c,
+                                      uint8_t kb) {
+  return apply_row<T, XF_OP_LAPLACE, false>(g, x, i, j, k, c, kb);
+}
 
 template <typename T, bool USE_D>
 __device__ __forceinline__ T lap_fast(uint8_t kb, T cxm, T cxp, T cym, T cyp, T czm, T czp, T d, T xm, T xc, T xp,
@@ -56,14 +65,38 @@ __device__ __forceinline__ T lap_fast(uint8_t kb, T cxm, T cxp, T cym, T cyp, T 
   }
 }
 
+// Publishes the block's dot (into SL_A, or slot+1 in res-mode under slot's
+// ticket) and, in the last block, totals it and runs the control step.
+template <typename T, bool RES>
+__device__ __forceinline__ void finish_cg_kernel(DevScratch* S, const CgqArgs<T>& a, const DotAcc<T>& acc, double* sh,
+                                                 bool* last) {
+  const int slot = RES ? a.slot + 1 : SL_A;
+  const int ticket = RES ? a.slot : SL_A;
+  double s = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0) {
+    S->partials[slot][lin_block()] = s;
+    __threadfence();
+    unsigned int t = atomicAdd(&S->tickets[ticket], 1u);
+    *last = (t == (unsigned)num_blocks() - 1);
+  }
+  __syncthreads();
+  if (!*last) return;
+  double tot = finish_partials(S, slot, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[slot] = tot;
+    S->tickets[ticket] = 0;
+    control_step(S, RES ? a.ctl : CTL_CG_ALPHA);
+  }
+}
+
 // Two cells (k0, k0+1) per thread; needs n3 even (then P is even and every
 // cell pair is 2*sizeof(T)-aligned and inside one k-row).
-template <typename T, bool USE_D>
+template <typename T, bool USE_D, bool RES>
 __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q2(CgqArgs<T> a) {
   __shared__ double sh[32];
   __shared__ bool last;
   DevScratch* S = a.S;
-  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  if (S->iscalars[I_DONE] || (!RES && S->iscalars[I_PAUSE])) return;
   typedef typename V2<T>::type VT;
   const StencilGrid<T>& g = a.g;
   const int P = g.n2 * g.n3;
@@ -101,32 +134,35 @@ __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q2(CgqArgs<T> a) {
       const int r0 = row_of(kc.x), r1 = row_of(kc.y);
       if (r0 > ROW_ACTUAL) out.x = slow_row<T>(g, x, i, j, k0, c, kc.x);
       if (r1 > ROW_ACTUAL) out.y = slow_row<T>(g, x, i, j, k0 + 1, c + 1, kc.y);
+      if (RES) {
+        const VT bb = *reinterpret_cast<const VT*>(a.b + c);
+        out.x = bb.x - out.x;
+        out.y = bb.y - out.y;
+      }
       if (r0 == ROW_NONE) out.x = T(0);
       if (r1 == ROW_NONE) out.y = T(0);
-      acc.add(xc.x, out.x);
-      acc.add(xc.y, out.y);
-      *reinterpret_cast<VT*>(a.y + c) = out;
+      if (RES) {
+        acc.add(out.x, out.x);
+        acc.add(out.y, out.y);
+        *reinterpret_cast<float2*>(a.y32 + c) = make_float2((float)out.x, (float)out.y);
+      } else {
+        acc.add(xc.x, out.x);
+        acc.add(xc.y, out.y);
+        *reinterpret_cast<VT*>(a.y + c) = out;
+      }
       xm = xc; xc = xp; xp = xpp; kc = kn;
     }
   }
-  double vals[1] = {acc.value()};
-  if (publish_partials<1>(S, SL_A, vals, sh, &last)) {
-    double t = finish_partials(S, SL_A, sh);
-    if (threadIdx.x == 0) {
-      S->scalars[SL_A] = t;
-      S->tickets[SL_A] = 0;
-      control_step(S, CTL_CG_ALPHA);
-    }
-  }
+  finish_cg_kernel<T, RES>(S, a, acc, sh, &last);
 }
 
 // One cell per thread (any n3).
-template <typename T, bool USE_D>
+template <typename T, bool USE_D, bool RES>
 __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q1(CgqArgs<T> a) {
   __shared__ double sh[32];
   __shared__ bool last;
   DevScratch* S = a.S;
-  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  if (S->iscalars[I_DONE] || (!RES && S->iscalars[I_PAUSE])) return;
   const StencilGrid<T>& g = a.g;
   const int P = g.n2 * g.n3;
   const int p = blockIdx.x * CGK_THREADS + threadIdx.x;
@@ -151,30 +187,28 @@ __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q1(CgqArgs<T> a) {
       T v = lap_fast<T, USE_D>(kc, g.cxm[i], g.cxp[i], cym, cyp, czm, czp, d, xm, xc, xp, xjm, xjp, xkm, xkp);
       const int r = row_of(kc);
       if (r > ROW_ACTUAL) v = slow_row<T>(g, x, i, j, k, c, kc);
+      if (RES) v = a.b[c] - v;
       if (r == ROW_NONE) v = T(0);
-      acc.add(xc, v);
-      a.y[c] = v;
+      if (RES) {
+        acc.add(v, v);
+        a.y32[c] = (float)v;
+      } else {
+        acc.add(xc, v);
+        a.y[c] = v;
+      }
       xm = xc; xc = xp; xp = xpp; kc = kn;
     }
   }
-  double vals[1] = {acc.value()};
-  if (publish_partials<1>(S, SL_A, vals, sh, &last)) {
-    double t = finish_partials(S, SL_A, sh);
-    if (threadIdx.x == 0) {
-      S->scalars[SL_A] = t;
-      S->tickets[SL_A] = 0;
-      control_step(S, CTL_CG_ALPHA);
-    }
-  }
+  finish_cg_kernel<T, RES>(S, a, acc, sh, &last);
 }
 
-template <typename T>
-static void launch_cg_q(const xf_op* op, const T* x, T* y) {
+template <typename T, bool RES>
+static void launch_cg_q(const xf_op* op, const T* x, T* y, const T* b, float* y32, int slot, int ctl) {
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
   CgqArgs<T> a;
   a.g = make_stencil_grid<T>(g, nullptr);
-  a.x = x; a.y = y; a.diag = g->diag; a.S = ctx->scratch;
+  a.x = x; a.y = y; a.b = b; a.y32 = y32; a.diag = g->diag; a.S = ctx->scratch; a.slot = slot; a.ctl = ctl;
   const int P = g->n2 * g->n3;
   const bool two = (g->n3 % 2) == 0;
   const int per = two ? 2 : 1;
@@ -184,10 +218,18 @@ static void launch_cg_q(const xf_op* op, const T* x, T* y) {
   a.chunk = chunk;
   dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
   constexpr bool D = std::is_same<T, double>::value;
-  if (two) k_cg_q2<T, D><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
-  else k_cg_q1<T, D><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
+  if (two) k_cg_q2<T, D, RES><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
+  else k_cg_q1<T, D, RES><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
 }
 
 // q = A p with (p, q) -> SL_A and the CG alpha step.  Laplace operators only.
-void xf_cg_q64(const xf_op* op, const double* p, double* q) { launch_cg_q<double>(op, p, q); }
-void xf_cg_q32(const xf_op* op, const float* p, float* q) { launch_cg_q<float>(op, p, q); }
+void xf_cg_q64(const xf_op* op, const double* p, double* q) {
+  launch_cg_q<double, false>(op, p, q, nullptr, nullptr, SL_A, CTL_CG_ALPHA);
+}
+void xf_cg_q32(const xf_op* op, const float* p, float* q) {
+  launch_cg_q<float, false>(op, p, q, nullptr, nullptr, SL_A, CTL_CG_ALPHA);
+}
+// r32 = float(b - A x) in FP64, (r, r) -> scalars[slot + 1], then control `ctl`.
+void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl) {
+  launch_cg_q<double, true>(op, x, nullptr, b, r32, slot, ctl);
+}

@@ -62,6 +62,8 @@ struct xf_grid {
   double *rhx, *rhy, *rhz, *rhhx, *rhhy, *rhhz;
   float *frhx, *frhy, *frhz, *frhhx, *frhhy, *frhhz;
   double* diag;              // device, per cell: diagonal of the Laplace Actual row (fast FP64)
+  int uniform;               // every separation of each axis is equal: coefficients are per-axis constants
+  double ucx, ucy, ucz;      // then 1/h^2 per axis (== c?m[i] == c?p[i] for every interior index)
   int lap_status, vardiv_status;
   int64_t lap_bad, vardiv_bad;
 };

@@ -20,11 +20,13 @@ enum {
 // integer scalars
 // I_PAUSE: the mixed CG's inner recursion has met the tolerance (or the cap)
 // and waits for the true-residual replacement at the end of its chunk.
-enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED, I_PAUSE };
+// I_PBUF: which of the two direction buffers holds the current p (fused FP32
+// iteration).  I_ERR: a bounded wait in a staged kernel ran out.
+enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED, I_PAUSE, I_PBUF, I_ERR };
 
 enum {
   CTL_NONE = 0,
-  CTL_CG_INIT, CTL_CG_ALPHA, CTL_CG_BETA, CTL_MIXED_REPL,
+  CTL_CG_INIT, CTL_CG_ALPHA, CTL_CG_BETA, CTL_MIXED_REPL, CTL_CG_BETA_FLIP,
   CTL_RCG_INIT, CTL_RCG_TAU0, CTL_RCG_RES0, CTL_RCG_TAU, CTL_RCG_RES,
   CTL_BCGS_NORM0, CTL_BCGS_PN1, CTL_BCGS_AN, CTL_BCGS_WN, CTL_BCGS_END,
   CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES
@@ -60,7 +62,8 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       double rr = d[SL_A + 1], bb = d[SL_B];
       d[D_RR] = rr; d[D_RR_PREV] = rr; d[D_BB] = bb; d[D_THR] = d[D_RTOL2] * bb;
       d[D_RR64] = rr;
-      I[I_IT] = 0; I[I_REPL] = 0; I[I_NEEDREP] = 0; I[I_DONE] = 0; I[I_STATUS] = XF_OK;
+      d[D_BETA] = 0.0;   // the fused iteration forms p = r + beta p from p = 0
+      I[I_IT] = 0; I[I_REPL] = 0; I[I_NEEDREP] = 0; I[I_DONE] = 0; I[I_STATUS] = XF_OK; I[I_PBUF] = 0;
       if (isnan(rr)) finish(S, XF_NAN);
       else if (rr <= d[D_THR]) finish(S, XF_OK);
       break;
@@ -72,6 +75,9 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       else d[D_ALPHA] = d[D_RR] / pq;
       break;
     }
+    case CTL_CG_BETA_FLIP:  // fused iteration: the new p now lives in the other buffer
+      I[I_PBUF] ^= 1;
+      // fall through
     case CTL_CG_BETA: {  // SL_B: r.r after the update
       double rn = d[SL_B];
       I[I_IT] += 1;

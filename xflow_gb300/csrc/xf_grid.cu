@@ -414,6 +414,17 @@ extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t
         (st = build_coeffs(g, hz, n3, &g->czm, &g->czp, &g->fzm, &g->fzp, &g->rhz, &g->rhhz, &g->frhz, &g->frhhz)))
       goto fail;
   }
+  {
+    // Uniform axes: c?m[i] = c?p[i] = 1/(h*h) for every interior index, bit for
+    // bit the table value (1/(h*((h+h)/2)) == 1/(h*h) exactly).
+    auto uni = [](const double* h, int n, double* c) {
+      for (int i = 1; i < n - 1; i++)
+        if (h[i] != h[0]) return false;
+      *c = 1.0 / (h[0] * ((h[0] + h[0]) / 2));
+      return true;
+    };
+    g->uniform = uni(hx, n1, &g->ucx) && uni(hy, n2, &g->ucy) && uni(hz, n3, &g->ucz);
+  }
   G_TRY(cudaMalloc(&g->diag, n * sizeof(double)));
   k_diag<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g->kind, g->cxm, g->cxp, g->cym, g->cyp, g->czm, g->czp,
                                                              n1, n2, n3, g->diag);

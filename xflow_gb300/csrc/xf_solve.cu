@@ -24,6 +24,10 @@ void xf_mv64(const xf_op* op, const MvReq<double>& q);
 void xf_mv32(const xf_op* op, const MvReq<float>& q);
 void xf_cg_q64(const xf_op* op, const double* p, double* q);
 void xf_cg_q32(const xf_op* op, const float* p, float* q);
+void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
+bool xf_cgf_supported(const xf_grid* g);
+int xf_cgf_prepare(xf_ctx* ctx, const xf_grid* g);
+void xf_cgf_iteration(const xf_op* op, float* r, float* e, float* p0, float* p1);
 int xf_op_ready(const xf_op* op);
 
 #define GUARD_DONE(S) \
@@ -442,6 +446,28 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         }
         k_cg_xr<double><<<rb, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
         k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0);
+      };
+    } else if (lap && xf_cgf_supported(g) && getenv("XF_FUSED") && getenv("XF_FUSED")[0] == '1') {
+      // (opt-in: measured slower than the three-kernel iteration so far)
+      // Staged fused iteration: K1 (p = r + beta p, (p, A p)) and K2 (A p
+      // recomputed, e += alpha p, r -= alpha A p, (r, r)); p ping-pongs
+      // between p32 and q32.  One graph chunk = `replace_every` iterations
+      // ending with the FP64 fold and true-residual replacement.
+      chunk = o.replace_every;
+      int rcp = xf_cgf_prepare(ctx, g);
+      if (rcp) return rcp;
+      float *e = e32, *r = r32, *pa = p32, *pb = q32;
+      XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
+      xf_cg_res64(op, x, b, r, SL_A, CTL_CG_INIT);
+      const int last = chunk - 1;
+      iter = [=](int c) {
+        xf_cgf_iteration(op, r, e, pa, pb);
+        if (c == last) {
+          k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
+          xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
+        }
       };
     } else {
       // One graph chunk = `replace_every` iterations; its last iteration folds

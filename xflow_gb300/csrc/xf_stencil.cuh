@@ -86,21 +86,23 @@ __device__ __forceinline__ T exact_vd_actual(const StencilGrid<T>& g, const T* _
 }
 
 // PreDefined (semi-sum, XOperator.cpp:1034-1069) and PreNormal
-// (XOperator.cpp:1070-1119; variable-density tail :2210-2221) rows.
-template <typename T, bool VARDIV>
-__device__ __forceinline__ T boundary_row(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k,
-                                          int c, int row) {
+// (XOperator.cpp:1070-1119; variable-density tail :2210-2221) rows.  `F`
+// returns the argument at offset (di, dj, dk) from the row's cell, so the same
+// formulas serve global-memory and shared-memory-staged callers.
+template <typename T, bool VARDIV, class F>
+__device__ __forceinline__ T boundary_row_acc(const StencilGrid<T>& g, const F& FF, int i, int j, int k, int c,
+                                              int row) {
   const int s1 = g.s1, s2 = g.s2;
   const int b = g.brow_of[c];
   const double nxd = g.brow_nrm[3 * b], nyd = g.brow_nrm[3 * b + 1], nzd = g.brow_nrm[3 * b + 2];
   if (row == ROW_PREDEF) {
     T semiSum = 0;
-    if (nxd > 0) semiSum = (f[c] + f[c - s1]) / T(2);
-    else if (nxd < 0) semiSum = (f[c + s1] + f[c]) / T(2);
-    if (nyd > 0) semiSum = (f[c] + f[c - s2]) / T(2);
-    else if (nyd < 0) semiSum = (f[c + s2] + f[c]) / T(2);
-    if (nzd > 0) semiSum = (f[c] + f[c - 1]) / T(2);
-    else if (nzd < 0) semiSum = (f[c + 1] + f[c]) / T(2);
+    if (nxd > 0) semiSum = (FF(0, 0, 0) + FF(-1, 0, 0)) / T(2);
+    else if (nxd < 0) semiSum = (FF(1, 0, 0) + FF(0, 0, 0)) / T(2);
+    if (nyd > 0) semiSum = (FF(0, 0, 0) + FF(0, -1, 0)) / T(2);
+    else if (nyd < 0) semiSum = (FF(0, 1, 0) + FF(0, 0, 0)) / T(2);
+    if (nzd > 0) semiSum = (FF(0, 0, 0) + FF(0, 0, -1)) / T(2);
+    else if (nzd < 0) semiSum = (FF(0, 0, 1) + FF(0, 0, 0)) / T(2);
     return semiSum;
   }
   const T nx = (T)nxd, ny = (T)nyd, nz = (T)nzd;
@@ -109,7 +111,6 @@ __device__ __forceinline__ T boundary_row(const StencilGrid<T>& g, const T* __re
   if (nxd > 0) { sI = 0; sI1 = -1; hxl = g.hx[i - 1]; } else if (nxd < 0) { sI = 1; sI1 = 0; hxl = g.hx[i]; }
   if (nyd > 0) { sJ = 0; sJ1 = -1; hyl = g.hy[j - 1]; } else if (nyd < 0) { sJ = 1; sJ1 = 0; hyl = g.hy[j]; }
   if (nzd > 0) { sK = 0; sK1 = -1; hzl = g.hz[k - 1]; } else if (nzd < 0) { sK = 1; sK1 = 0; hzl = g.hz[k]; }
-#define FF(a, bb, d) f[c + (a) * s1 + (bb) * s2 + (d)]
   T fl = (FF(sI, 0, 0) + FF(sI, sJ, 0) + FF(sI, 0, sK) + FF(sI, sJ, sK)) / T(4);
   T fl_1 = (FF(sI1, 0, 0) + FF(sI1, sJ, 0) + FF(sI1, 0, sK) + FF(sI1, sJ, sK)) / T(4);
   T dfx = (fl - fl_1) / hxl;
@@ -119,7 +120,6 @@ __device__ __forceinline__ T boundary_row(const StencilGrid<T>& g, const T* __re
   fl = (FF(0, 0, sK) + FF(sI, 0, sK) + FF(0, sJ, sK) + FF(sI, sJ, sK)) / T(4);
   fl_1 = (FF(0, 0, sK1) + FF(sI, 0, sK1) + FF(0, sJ, sK1) + FF(sI, sJ, sK1)) / T(4);
   T dfz = (fl - fl_1) / hzl;
-#undef FF
   if (!VARDIV) return dfx * nx + dfy * ny + dfz * nz;
   const T* __restrict__ rho = g.rho;
   T d_x = rho[c + s1] - rho[c] / (g.hx[i - 1]);
@@ -127,7 +127,21 @@ __device__ __forceinline__ T boundary_row(const StencilGrid<T>& g, const T* __re
   T d_z = rho[c + 1] - rho[c] / (g.hz[k - 1]);
   T laplace_p = dfx * nx + dfy * ny + dfz * nz;
   T divergence_density = d_x + d_y + d_z;
-  return rho[c] * laplace_p - divergence_density * f[c];
+  return rho[c] * laplace_p - divergence_density * FF(0, 0, 0);
+}
+
+template <typename T>
+struct GlobalAcc {
+  const T* __restrict__ f;
+  int c, s1, s2;
+  __device__ __forceinline__ T operator()(int a, int b, int d) const { return f[c + a * s1 + b * s2 + d]; }
+};
+
+template <typename T, bool VARDIV>
+__device__ __forceinline__ T boundary_row(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k,
+                                          int c, int row) {
+  GlobalAcc<T> acc{f, c, g.s1, g.s2};
+  return boundary_row_acc<T, VARDIV>(g, acc, i, j, k, c, row);
 }
 
 template <typename T>
