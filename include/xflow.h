@@ -184,6 +184,25 @@ int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, x
 int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                   xf_solve_stats* stats);
 
+/* ---- allocation-free inner product --------------------------------------- */
+/* No counterpart in the reference (which has no device memory at all).
+ * The masked FP64 dot of xf_dot, sum over c < n with d_mask[c] != 0 (d_mask
+ * may be NULL: every element) of d_a[c]*d_b[c], written to *d_out, for
+ * callers that cannot allocate device memory: code running during a CUDA
+ * graph capture, in a host callback, or under a memory budget that forbids
+ * allocation once a time loop is running.  All pointers are caller-owned
+ * device memory; the call is asynchronous on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream) and allocates nothing: its scratch is a
+ * 64 KiB file-scope device array that every device loading the library keeps
+ * until exit.  n beyond XF_NOALLOC_MAX_ELEMS returns XF_ERR_ARG.  Calls share
+ * that scratch, so calls that overlap on the GPU race; calls ordered on one
+ * stream do not.  The first call on a device resolves the scratch address
+ * (cudaGetSymbolAddress, that device current): make it before any stream
+ * capture. */
+#define XF_NOALLOC_MAX_ELEMS (8192LL * 256LL * 16LL)
+int xf_dot_noalloc(const double* d_a, const double* d_b, const uint8_t* d_mask, int64_t n, double* d_out,
+                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif
