@@ -184,6 +184,15 @@ int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, x
 int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                   xf_solve_stats* stats);
 
+/* ---- measurement ---------------------------------------------------------- */
+/* No counterpart in the reference (a profiling helper).  Times each kernel of
+ * one CG iteration on op's grid alone, `reps` launches each, with CUDA events
+ * on the context stream, and writes the average ms per launch: [0] FP32
+ * stencil q = A p with (p,q), [1] FP32 x/r update with (r,r), [2] FP32
+ * direction update, [3] FP64 true residual r32 = b - A x, [4] FP64 stencil.
+ * Laplace operators only. */
+int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
+
 /* ---- allocation-free inner product --------------------------------------- */
 /* No counterpart in the reference (which has no device memory at all).
  * The masked FP64 dot of xf_dot, sum over c < n with d_mask[c] != 0 (d_mask

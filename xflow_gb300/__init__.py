@@ -241,6 +241,16 @@ def solve(op, x, b, **kw):
     return st
 
 
+CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "stencil_f64")
+
+
+def profile_cg_kernels(op, reps=20):
+    """Average ms per launch of each CG-iteration kernel, timed alone."""
+    out = (C.c_double * 5)()
+    _check(op.grid.ctx.h, capi.lib().xf_profile_cg_kernels(op.h, int(reps), out))
+    return dict(zip(CG_KERNELS, list(out)))
+
+
 def solve_host(op, x_host, b_host, **kw):
     """Host-buffer solve (upload, solve, download inside one C-ABI call)."""
     o = solve_opts(**kw)

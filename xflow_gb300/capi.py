@@ -26,7 +26,7 @@ EXPORTS = [
     "xf_grid_check", "xf_vec_create", "xf_vec_destroy", "xf_vec_upload", "xf_vec_download", "xf_vec_assign",
     "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_matvec",
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
-    "xf_solve_host", "xf_dot_noalloc",
+    "xf_solve_host", "xf_profile_cg_kernels", "xf_dot_noalloc",
 ]
 
 
@@ -87,6 +87,7 @@ def lib():
         L.xf_solve.argtypes = [vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
         L.xf_solve_host.argtypes = [vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
         L.xf_dot_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
+        L.xf_profile_cg_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 

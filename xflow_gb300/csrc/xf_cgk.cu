@@ -9,6 +9,8 @@
 // x[i-1], x[i], x[i+1] in registers, prefetching plane i+2.  FP64 rows use the
 // precomputed diagonal: one DMUL and six DFMA per cell, the FP64 issue rate
 // being the bound on GB300.
+#include <stdlib.h>
+
 #include <type_traits>
 
 #include "xf_control.cuh"
@@ -72,15 +74,7 @@ __device__ __forceinline__ void finish_cg_kernel(DevScratch* S, const CgqArgs<T>
                                                  bool* last) {
   const int slot = RES ? a.slot + 1 : SL_A;
   const int ticket = RES ? a.slot : SL_A;
-  double s = block_sum(acc.value(), sh);
-  if (threadIdx.x == 0) {
-    S->partials[slot][lin_block()] = s;
-    __threadfence();
-    unsigned int t = atomicAdd(&S->tickets[ticket], 1u);
-    *last = (t == (unsigned)num_blocks() - 1);
-  }
-  __syncthreads();
-  if (!*last) return;
+  if (!publish_acc<T>(S, slot, ticket, acc, sh, last)) return;
   double tot = finish_partials(S, slot, sh);
   if (threadIdx.x == 0) {
     S->scalars[slot] = tot;
@@ -202,6 +196,95 @@ __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q1(CgqArgs<T> a) {
   finish_cg_kernel<T, RES>(S, a, acc, sh, &last);
 }
 
+// FP32 q = A p, software-pipelined plane march for uniform grids: two cells
+// per thread; the centre column is loaded three planes ahead, the j+-1 / k+-1
+// neighbours and the kind bytes of the next plane one step ahead, so no load
+// is consumed in the step that issues it.  Per-axis constant coefficients.
+struct Side2 { float2 jm, jp; float km, kp; };
+
+// Read-only loads go through the non-coherent path explicitly (__ldg): the
+// pointers travel in a parameter struct, where __restrict__ does not reach
+// the compiler.
+__device__ __forceinline__ Side2 load_side2(const float* __restrict__ x, int c, int ojm, int ojp, int okm, int okp) {
+  Side2 s;
+  s.jm = __ldg(reinterpret_cast<const float2*>(x + c + ojm));
+  s.jp = __ldg(reinterpret_cast<const float2*>(x + c + ojp));
+  s.km = __ldg(x + c + okm);
+  s.kp = __ldg(x + c + okp);
+  return s;
+}
+
+// Actual rows use A p = D p_c - (cx (p_i+1 + p_i-1) + cy (..) + cz (..)): the
+// CG direction is zero on every inactive cell, so a closed (Fictive) face's
+// neighbour term vanishes by itself and only the diagonal D depends on the
+// open faces; D comes from a 64-entry table indexed by the face bits.
+// BROWS: the grid has PreDefined/PreNormal rows.  Without them the (never
+// taken) boundary-row branch is compiled out: its mere presence costs ~15% here.
+// Prefetch addresses are clamped to the box instead of bounds-checked: a
+// clamped (out-of-box) plane only ever feeds rows on the box faces, which are
+// never Actual rows, so its values are never used.
+template <bool BROWS>
+__global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q2u(CgqArgs<float> a, float cx, float cy, float cz) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  __shared__ float dtab[64];
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x;
+    dtab[b] = cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
+              cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
+  }
+  __syncthreads();
+  const StencilGrid<float>& g = a.g;
+  const int n1 = g.n1, n3 = g.n3;
+  const int P = g.n2 * n3;
+  const int p0 = 2 * (blockIdx.x * CGK_THREADS + threadIdx.x);
+  const int i0 = blockIdx.y * a.chunk, i1 = min(n1, i0 + a.chunk);
+  DotAcc<float> acc;
+  if (p0 < P) {
+    const int j = p0 / n3, k0 = p0 - j * n3;
+    const int ojm = j > 0 ? -n3 : 0, ojp = j < g.n2 - 1 ? n3 : 0;
+    const int okm = k0 > 0 ? -1 : 0, okp = k0 + 1 < n3 - 1 ? 2 : 1;
+    const float* __restrict__ x = a.x;
+    const int last_plane = n1 - 1;
+    auto ld = [&](int i) -> float2 {
+      const int ic = min(max(i, 0), last_plane);
+      return __ldg(reinterpret_cast<const float2*>(x + ic * P + p0));
+    };
+    auto ldk = [&](int i) -> uchar2 {
+      return __ldg(reinterpret_cast<const uchar2*>(g.kind + min(i, last_plane) * P + p0));
+    };
+    float2 xm = ld(i0 - 1), xc = ld(i0), xp = ld(i0 + 1), xpp = ld(i0 + 2);
+    uchar2 kc = ldk(i0), kn = ldk(i0 + 1);
+    Side2 sc = load_side2(x, i0 * P + p0, ojm, ojp, okm, okp);
+    for (int i = i0; i < i1; i++) {
+      const int c = i * P + p0;
+      // loads for later steps, in flight during this step's arithmetic
+      const float2 x3 = ld(i + 3);
+      const uchar2 kn2 = ldk(i + 2);
+      const Side2 sn = load_side2(x, min(i + 1, last_plane) * P + p0, ojm, ojp, okm, okp);
+      float2 out;
+      out.x = fmaf(dtab[kc.x & 63], xc.x, -fmaf(cx, xp.x + xm.x, fmaf(cy, sc.jp.x + sc.jm.x, cz * (xc.y + sc.km))));
+      out.y = fmaf(dtab[kc.y & 63], xc.y, -fmaf(cx, xp.y + xm.y, fmaf(cy, sc.jp.y + sc.jm.y, cz * (sc.kp + xc.x))));
+      const int r0 = row_of(kc.x), r1 = row_of(kc.y);
+      if (BROWS) {
+        if (r0 > ROW_ACTUAL) out.x = slow_row<float>(g, x, i, j, k0, c, kc.x);
+        if (r1 > ROW_ACTUAL) out.y = slow_row<float>(g, x, i, j, k0 + 1, c + 1, kc.y);
+      }
+      if (r0 == ROW_NONE) out.x = 0.f;
+      if (r1 == ROW_NONE) out.y = 0.f;
+      acc.add(xc.x, out.x);
+      acc.add(xc.y, out.y);
+      *reinterpret_cast<float2*>(a.y + c) = out;
+      xm = xc; xc = xp; xp = xpp; xpp = x3;
+      kc = kn; kn = kn2;
+      sc = sn;
+    }
+  }
+  finish_cg_kernel<float, false>(S, a, acc, sh, &last);
+}
+
 template <typename T, bool RES>
 static void launch_cg_q(const xf_op* op, const T* x, T* y, const T* b, float* y32, int slot, int ctl) {
   const xf_grid* g = op->g;
@@ -218,6 +301,13 @@ static void launch_cg_q(const xf_op* op, const T* x, T* y, const T* b, float* y3
   a.chunk = chunk;
   dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
   constexpr bool D = std::is_same<T, double>::value;
+  if constexpr (!D && !RES) {
+    if (two && g->uniform && !(getenv("XF_Q2_PLAIN") && getenv("XF_Q2_PLAIN")[0] == '1')) {
+      if (g->nbrow > 0) k_cg_q2u<true><<<grid, CGK_THREADS, 0, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
+      else k_cg_q2u<false><<<grid, CGK_THREADS, 0, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
+      return;
+    }
+  }
   if (two) k_cg_q2<T, D, RES><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
   else k_cg_q1<T, D, RES><<<grid, CGK_THREADS, 0, ctx->stream>>>(a);
 }

@@ -134,6 +134,37 @@ struct DotAcc<float> {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// Sum of the block's accumulators, valid in thread 0.  FP32 accumulators are
+// reduced across each warp in float-float (FP32 pipe) and reach FP64 once per
+// warp, so the epilogue issues ~1/32 of the FP64 instructions of a per-thread
+// conversion.
+__device__ inline double warp_sum(double v);
+template <typename T>
+__device__ inline double block_sum_acc(const DotAcc<T>& acc, double* sh);
+template <>
+__device__ inline double block_sum_acc<double>(const DotAcc<double>& acc, double* sh);
+template <>
+__device__ inline double block_sum_acc<float>(const DotAcc<float>& acc, double* sh) {
+  float hi = acc.hi, lo = acc.lo;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float s = hi + bh;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (bh - bp);
+    hi = s;
+    lo = lo + (bl + err);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = (double)hi + (double)lo;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  double v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  return v;
+}
+
 // Block reduction helpers (FP64).
 __device__ inline double warp_sum(double v) {
 #pragma unroll
@@ -152,6 +183,26 @@ __device__ inline double block_sum(double v, double* sh) {
   v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
   if (w == 0) v = warp_sum(v);
   return v;
+}
+
+template <>
+__device__ inline double block_sum_acc<double>(const DotAcc<double>& acc, double* sh) {
+  return block_sum(acc.value(), sh);
+}
+
+// Publishes one accumulator into partials[slot] under tickets[ticket]; true in
+// the last block to arrive.
+template <typename T>
+__device__ inline bool publish_acc(DevScratch* S, int slot, int ticket, const DotAcc<T>& acc, double* sh, bool* flag) {
+  const double s = block_sum_acc<T>(acc, sh);
+  if (threadIdx.x == 0) {
+    S->partials[slot][lin_block()] = s;
+    __threadfence();
+    unsigned int t = atomicAdd(&S->tickets[ticket], 1u);
+    *flag = (t == (unsigned)num_blocks() - 1);
+  }
+  __syncthreads();
+  return *flag;
 }
 
 // Publishes this block's partial of `nval` sums into slot partials and returns

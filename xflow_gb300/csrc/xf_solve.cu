@@ -75,8 +75,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __r
     r[c] = rv;
     acc.add(rv, rv);
   }
-  double v[1] = {acc.value()};
-  if (publish_partials<1>(S, SL_B, v, sh, &last)) {
+  if (publish_acc<T>(S, SL_B, SL_B, acc, sh, &last)) {
     double t = finish_partials(S, SL_B, sh);
     if (threadIdx.x == 0) {
       S->scalars[SL_B] = t;
@@ -492,10 +491,14 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S);
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
-          MvReq<double> m2;
-          m2.x = x; m2.y32 = r; m2.s = b; m2.sign = -1; m2.neg = 1; m2.zero_inactive = 1; m2.dot_self = 1;
-          m2.slot = SL_C; m2.ctl = CTL_MIXED_REPL;
-          xf_mv64(op, m2);
+          if (lap) {
+            xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
+          } else {
+            MvReq<double> m2;
+            m2.x = x; m2.y32 = r; m2.s = b; m2.sign = -1; m2.neg = 1; m2.zero_inactive = 1; m2.dot_self = 1;
+            m2.slot = SL_C; m2.ctl = CTL_MIXED_REPL;
+            xf_mv64(op, m2);
+          }
         }
         k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, c == last ? 1 : 0);
       };
@@ -629,6 +632,52 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
   st->rel_resid = rel;
   st->abs_resid = own;
   st->reserved[0] = (double)(hs.kernels + 6);
+  return XF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel timing of one CG iteration, each kernel alone (CUDA events on the
+// context stream around every launch; the solver state is reset between
+// launches so no control step turns the next launch into a no-op).
+extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
+  if (!op || !ms_out || reps <= 0) return XF_ERR_ARG;
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  if (op->kind != XF_OP_LAPLACE) return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_profile_cg_kernels: Laplace operators only");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  DevScratch* S = ctx->scratch;
+  const int64_t n = g->ncell;
+  const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
+  Bufs B(ctx);
+  float *e = B.get<float>(n), *r = B.get<float>(n), *p = B.get<float>(n), *q = B.get<float>(n);
+  double *x = B.get<double>(n), *b = B.get<double>(n), *p64 = B.get<double>(n), *q64 = B.get<double>(n);
+  if (!e || !r || !p || !q || !x || !b || !p64 || !q64) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  auto time = [&](const std::function<void()>& f) -> double {
+    double tot = 0;
+    for (int k = 0; k < reps + 2; k++) {
+      k_reset_state<<<1, 1, 0, ctx->stream>>>(S, 0.0, 0.0, 1ll << 40, 1ll << 40, 1);
+      cudaEventRecord(t0, ctx->stream);
+      f();
+      cudaEventRecord(t1, ctx->stream);
+      cudaEventSynchronize(t1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (k >= 2) tot += ms;
+    }
+    return tot / reps;
+  };
+  ms_out[0] = time([&] { xf_cg_q32(op, p, q); });
+  ms_out[1] = time([&] { k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S); });
+  ms_out[2] = time([&] { k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0); });
+  ms_out[3] = time([&] { xf_cg_res64(op, x, b, r, SL_C, CTL_NONE); });
+  ms_out[4] = time([&] { xf_cg_q64(op, p64, q64); });
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  XF_CUDA(ctx, cudaGetLastError());
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return XF_OK;
 }
 
