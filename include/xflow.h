@@ -189,8 +189,10 @@ int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const do
  * one CG iteration on op's grid alone, `reps` launches each, with CUDA events
  * on the context stream, and writes the average ms per launch: [0] FP32
  * stencil q = A p with (p,q), [1] FP32 x/r update with (r,r), [2] FP32
- * direction update, [3] FP64 true residual r32 = b - A x, [4] FP64 stencil.
- * Laplace operators only. */
+ * direction update, [3] FP64 true residual r32 = b - A x, [4] FP64 stencil,
+ * [5] FP32 stencil with the direction update fused in (p' = r + beta p,
+ * q = A p', (p', q)), or -1 where the grid does not take that path.
+ * ms_out holds 6 doubles.  Laplace operators only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
 /* ---- allocation-free inner product --------------------------------------- */

@@ -202,7 +202,7 @@ def spheres_case(n, nsph, seed):
 
 
 @pytest.mark.parametrize("precision", [xf.XF_PREC_FP64, xf.XF_PREC_MIXED])
-@pytest.mark.parametrize("n", [40, 25])   # box 42^2 planes take the staged fused path, 27^2 the generic one
+@pytest.mark.parametrize("n", [40, 25])   # box 42 (even rows): fused direction update; box 27: three-kernel path
 def test_plain_cg_matches_oracle_cg(ctx, precision, n):
     codes, nrm, sep, b = spheres_case(n, 6, 5)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
@@ -255,12 +255,37 @@ def test_solve_host_roundtrip(ctx):
     assert np.linalg.norm(r[sm]) / np.linalg.norm(b[sm]) <= 1.01e-8
 
 
-def test_maxit_status(ctx):
+@pytest.mark.parametrize("precision", [xf.XF_PREC_FP64, xf.XF_PREC_MIXED])
+def test_maxit_status(ctx, precision):
     codes, nrm, sep, b = spheres_case(32, 4, 11)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
     A = xf.Operator(g)
-    st = xf.solve(A, g.vec(np.zeros(g.shape)), g.vec(b), method=xf.XF_CG, rtol=1e-12, maxit=5)
+    st = xf.solve(A, g.vec(np.zeros(g.shape)), g.vec(b), method=xf.XF_CG, precision=precision, rtol=1e-12,
+                  maxit=5)
     assert st.status == capi.XF_MAXIT and st.iterations == 5
+
+
+def test_fused_direction_update_matches_three_kernel_path(ctx, monkeypatch):
+    """The mixed CG's fused iteration (p' = r + beta p inside the stencil, p
+    ping-ponging between two buffers) against the three-kernel iteration on the
+    same system: same iteration count within 2, same solution within the
+    solve's own accuracy."""
+    codes, nrm, sep, b = spheres_case(48, 8, 21)
+    g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
+    A = xf.Operator(g)
+    bv = g.vec(b)
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("XF_PQ_FUSE", mode)
+        x = g.vec(np.zeros(g.shape))
+        st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=1e-9)
+        assert st.status == capi.XF_OK and st.rel_resid <= 1e-9
+        out[mode] = (st, x.download())
+    (s1, x1), (s0, x0) = out["1"], out["0"]
+    assert abs(s1.iterations - s0.iterations) <= 2, (s1.iterations, s0.iterations)
+    sm = codes != 0
+    d = (x1 - x1[sm].mean()) - (x0 - x0[sm].mean())
+    assert np.abs(d[sm]).max() <= 1e-6 * np.abs(x0[sm] - x0[sm].mean()).max()
 
 
 def test_nan_rhs_reports_nan(ctx):

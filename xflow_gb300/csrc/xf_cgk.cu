@@ -285,6 +285,161 @@ __global__ void __launch_bounds__(CGK_THREADS, 4) k_cg_q2u(CgqArgs<float> a, flo
   finish_cg_kernel<float, false>(S, a, acc, sh, &last);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 direction update fused into the stencil, for uniform grids without
+// PreDefined/PreNormal rows:
+//     p' = r + beta p   (every cell; r and p are zero off the active set),
+//     q  = A p',  (p', q) -> SL_A, control CTL_CG_ALPHA_FLIP.
+// p' is formed on the fly wherever the stencil needs it (the centre column
+// and its four side neighbours), so p' must not overwrite p while other
+// threads still read p: the direction ping-pongs between two buffers and the
+// device flag I_PBUF names the one holding the current p (flipped by the
+// control step once every block has read it).
+// The grid is one wave of resident blocks; each block walks work items
+// (plane chunk, column group) round-robin, plane-chunk major so that blocks
+// on neighbouring column groups march the same planes at the same time (their
+// shared halo rows stay in L2), and publishes its dot once.
+struct PqArgs {
+  StencilGrid<float> g;
+  const float* r;
+  float* pb0;
+  float* pb1;
+  float* q;
+  DevScratch* S;
+  int chunk, nchunk, bx;
+};
+
+struct SideRaw { float2 rjm, rjp, pjm, pjp; float rkm, rkp, pkm, pkp; };
+
+__device__ __forceinline__ SideRaw load_side_raw(const float* __restrict__ r, const float* __restrict__ p, int c,
+                                                 int ojm, int ojp, int okm, int okp) {
+  SideRaw s;
+  s.rjm = __ldg(reinterpret_cast<const float2*>(r + c + ojm));
+  s.rjp = __ldg(reinterpret_cast<const float2*>(r + c + ojp));
+  s.pjm = __ldg(reinterpret_cast<const float2*>(p + c + ojm));
+  s.pjp = __ldg(reinterpret_cast<const float2*>(p + c + ojp));
+  s.rkm = __ldg(r + c + okm);
+  s.rkp = __ldg(r + c + okp);
+  s.pkm = __ldg(p + c + okm);
+  s.pkp = __ldg(p + c + okp);
+  return s;
+}
+
+__device__ __forceinline__ float2 dir2(float beta, float2 r, float2 p) {
+  return make_float2(fmaf(beta, p.x, r.x), fmaf(beta, p.y, r.y));
+}
+
+__device__ __forceinline__ Side2 dir_side(float beta, const SideRaw& s) {
+  Side2 o;
+  o.jm = dir2(beta, s.rjm, s.pjm);
+  o.jp = dir2(beta, s.rjp, s.pjp);
+  o.km = fmaf(beta, s.pkm, s.rkm);
+  o.kp = fmaf(beta, s.pkp, s.rkp);
+  return o;
+}
+
+__global__ void __launch_bounds__(CGK_THREADS, 3) k_cg_pq2u(PqArgs a, float cx, float cy, float cz) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  __shared__ float dtab[64];
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  const float beta = (float)S->scalars[D_BETA];
+  const int sel = (int)S->iscalars[I_PBUF];
+  const float* __restrict__ po = sel ? a.pb1 : a.pb0;
+  float* __restrict__ pn = sel ? a.pb0 : a.pb1;
+  const float* __restrict__ r = a.r;
+  float* __restrict__ q = a.q;
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x;
+    dtab[b] = cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
+              cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
+  }
+  __syncthreads();
+  const StencilGrid<float>& g = a.g;
+  const int n1 = g.n1, n3 = g.n3;
+  const int P = g.n2 * n3;
+  const int last_plane = n1 - 1;
+  const int items = a.nchunk * a.bx;
+  DotAcc<float> acc;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int ic = item / a.bx, gx = item - ic * a.bx;
+    const int p0 = 2 * (gx * CGK_THREADS + threadIdx.x);
+    if (p0 >= P) continue;
+    const int i0 = ic * a.chunk, i1 = min(n1, i0 + a.chunk);
+    const int j = p0 / n3, k0 = p0 - j * n3;
+    const int ojm = j > 0 ? -n3 : 0, ojp = j < g.n2 - 1 ? n3 : 0;
+    const int okm = k0 > 0 ? -1 : 0, okp = k0 + 1 < n3 - 1 ? 2 : 1;
+    // Plane addresses clamped to the box: a clamped plane only feeds rows on
+    // the box faces, which are never Actual rows (their outputs are zeroed).
+    auto pl = [&](int i) { return min(max(i, 0), last_plane) * P + p0; };
+    auto ldr = [&](int i) { return __ldg(reinterpret_cast<const float2*>(r + pl(i))); };
+    auto ldp = [&](int i) { return __ldg(reinterpret_cast<const float2*>(po + pl(i))); };
+    auto ldk = [&](int i) { return __ldg(reinterpret_cast<const uchar2*>(g.kind + pl(i))); };
+    float2 xm = dir2(beta, ldr(i0 - 1), ldp(i0 - 1));
+    float2 xc = dir2(beta, ldr(i0), ldp(i0));
+    float2 xp = dir2(beta, ldr(i0 + 1), ldp(i0 + 1));
+    float2 r2 = ldr(i0 + 2), p2 = ldp(i0 + 2);
+    uchar2 kc = ldk(i0), kn = ldk(i0 + 1);
+    Side2 sc = dir_side(beta, load_side_raw(r, po, pl(i0), ojm, ojp, okm, okp));
+    for (int i = i0; i < i1; i++) {
+      const int c = i * P + p0;
+      // loads for later steps, in flight during this step's arithmetic
+      const float2 r3 = ldr(i + 3), p3 = ldp(i + 3);
+      const uchar2 kn2 = ldk(i + 2);
+      const SideRaw sn = load_side_raw(r, po, pl(i + 1), ojm, ojp, okm, okp);
+      float2 out;
+      out.x = fmaf(dtab[kc.x & 63], xc.x, -fmaf(cx, xp.x + xm.x, fmaf(cy, sc.jp.x + sc.jm.x, cz * (xc.y + sc.km))));
+      out.y = fmaf(dtab[kc.y & 63], xc.y, -fmaf(cx, xp.y + xm.y, fmaf(cy, sc.jp.y + sc.jm.y, cz * (sc.kp + xc.x))));
+      if (row_of(kc.x) == ROW_NONE) out.x = 0.f;
+      if (row_of(kc.y) == ROW_NONE) out.y = 0.f;
+      acc.add(xc.x, out.x);
+      acc.add(xc.y, out.y);
+      *reinterpret_cast<float2*>(pn + c) = xc;
+      *reinterpret_cast<float2*>(q + c) = out;
+      xm = xc; xc = xp; xp = dir2(beta, r2, p2);
+      r2 = r3; p2 = p3;
+      kc = kn; kn = kn2;
+      sc = dir_side(beta, sn);
+    }
+  }
+  if (!publish_acc<float>(S, SL_A, SL_A, acc, sh, &last)) return;
+  double tot = finish_partials(S, SL_A, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[SL_A] = tot;
+    S->tickets[SL_A] = 0;
+    control_step(S, CTL_CG_ALPHA_FLIP);
+  }
+}
+
+bool xf_cg_pq_supported(const xf_grid* g) {
+  return g->uniform && g->nbrow == 0 && (g->n3 % 2) == 0 && g->n1 >= 2;
+}
+
+// p' = r + beta p (p in pb[I_PBUF]), q = A p', (p', q), alpha, flip.
+void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
+  const xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  static int resident = 0;   // blocks per SM at this kernel's launch bounds
+  if (!resident) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_cg_pq2u, CGK_THREADS, 0) != cudaSuccess ||
+        resident < 1)
+      resident = 1;
+  }
+  PqArgs a;
+  a.g = make_stencil_grid<float>(g, nullptr);
+  a.r = r; a.pb0 = pb0; a.pb1 = pb1; a.q = q; a.S = ctx->scratch;
+  const int P = g->n2 * g->n3;
+  a.bx = (P / 2 + CGK_THREADS - 1) / CGK_THREADS;
+  a.chunk = 8;
+  a.nchunk = (g->n1 + a.chunk - 1) / a.chunk;
+  int64_t items = (int64_t)a.bx * a.nchunk;
+  int64_t blocks = (int64_t)ctx->sm_count * resident;
+  if (blocks > items) blocks = items;
+  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  k_cg_pq2u<<<(int)blocks, CGK_THREADS, 0, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
+}
+
 template <typename T, bool RES>
 static void launch_cg_q(const xf_op* op, const T* x, T* y, const T* b, float* y32, int slot, int ctl) {
   const xf_grid* g = op->g;

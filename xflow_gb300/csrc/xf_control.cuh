@@ -26,7 +26,7 @@ enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIX
 
 enum {
   CTL_NONE = 0,
-  CTL_CG_INIT, CTL_CG_ALPHA, CTL_CG_BETA, CTL_MIXED_REPL, CTL_CG_BETA_FLIP,
+  CTL_CG_INIT, CTL_CG_ALPHA, CTL_CG_BETA, CTL_MIXED_REPL, CTL_CG_BETA_FLIP, CTL_CG_ALPHA_FLIP,
   CTL_RCG_INIT, CTL_RCG_TAU0, CTL_RCG_RES0, CTL_RCG_TAU, CTL_RCG_RES,
   CTL_BCGS_NORM0, CTL_BCGS_PN1, CTL_BCGS_AN, CTL_BCGS_WN, CTL_BCGS_END,
   CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES
@@ -68,6 +68,9 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       else if (rr <= d[D_THR]) finish(S, XF_OK);
       break;
     }
+    case CTL_CG_ALPHA_FLIP:  // fused direction update: the new p lives in the other buffer
+      I[I_PBUF] ^= 1;
+      // fall through
     case CTL_CG_ALPHA: {  // SL_A: p.q
       double pq = d[SL_A];
       if (isnan(pq)) finish(S, XF_NAN);

@@ -25,6 +25,8 @@ void xf_mv32(const xf_op* op, const MvReq<float>& q);
 void xf_cg_q64(const xf_op* op, const double* p, double* q);
 void xf_cg_q32(const xf_op* op, const float* p, float* q);
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
+bool xf_cg_pq_supported(const xf_grid* g);
+void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q);
 bool xf_cgf_supported(const xf_grid* g);
 int xf_cgf_prepare(xf_ctx* ctx, const xf_grid* g);
 void xf_cgf_iteration(const xf_op* op, float* r, float* e, float* p0, float* p1);
@@ -43,10 +45,13 @@ template <> struct V16<double> { typedef double2 type; };
 
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-                                                       const T* __restrict__ q, int64_t n, DevScratch* S) {
+                                                       const T* __restrict__ q, int64_t n, DevScratch* S,
+                                                       const T* __restrict__ p_alt = nullptr) {
   __shared__ double sh[32];
   __shared__ bool last;
   if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  // fused direction update: p ping-pongs and I_PBUF names the current buffer
+  if (p_alt && S->iscalars[I_PBUF]) p = p_alt;
   typedef typename V16<T>::type VT;
   constexpr int L = 16 / sizeof(T);
   const T alpha = (T)S->scalars[D_ALPHA];
@@ -413,13 +418,17 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   HostState hs = {0, 0, 0, 0, 0};
   double rel = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr;
-  float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr;
   if (!mixed) {
     r = B.get<double>(n); p = B.get<double>(n); q = B.get<double>(n);
     if (!r || !p || !q) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
   } else {
     e32 = B.get<float>(n); r32 = B.get<float>(n); p32 = B.get<float>(n); q32 = B.get<float>(n);
     if (!e32 || !r32 || !p32 || !q32) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
+    if (op->kind == XF_OP_LAPLACE && xf_cg_pq_supported(g)) {
+      p32b = B.get<float>(n);
+      if (!p32b) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
+    }
   }
   double* tmp = B.get<double>(n, false);
   if (!tmp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate residual");
@@ -463,6 +472,29 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       const int last = chunk - 1;
       iter = [=](int c) {
         xf_cgf_iteration(op, r, e, pa, pb);
+        if (c == last) {
+          k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
+          xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
+        }
+      };
+    } else if (lap && p32b && !(getenv("XF_PQ_FUSE") && getenv("XF_PQ_FUSE")[0] == '0')) {
+      // Two kernels per iteration: K1 forms p' = r + beta p inside the
+      // stencil (q = A p', (p', q), alpha; p ping-pongs between p32 and a
+      // second buffer), K2 updates e and r with (r, r) and beta.  One graph
+      // chunk = `replace_every` iterations; its last iteration folds the FP32
+      // correction into x and replaces r by the true FP64 residual, whose
+      // beta the next K1 uses.
+      chunk = o.replace_every;
+      float *e = e32, *r = r32, *pa = p32, *q = q32;
+      float* pb = p32b;
+      XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
+      xf_cg_res64(op, x, b, r, SL_A, CTL_CG_INIT);
+      const int last = chunk - 1;
+      iter = [=](int c) {
+        xf_cg_pq32(op, r, pa, pb, q);
+        k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, pa, q, n, S, pb);
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
           xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
@@ -674,6 +706,12 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
   ms_out[2] = time([&] { k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0); });
   ms_out[3] = time([&] { xf_cg_res64(op, x, b, r, SL_C, CTL_NONE); });
   ms_out[4] = time([&] { xf_cg_q64(op, p64, q64); });
+  ms_out[5] = -1.0;
+  if (xf_cg_pq_supported(g)) {
+    float* p2 = B.get<float>(n);
+    if (!p2) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
+    ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
+  }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   XF_CUDA(ctx, cudaGetLastError());
