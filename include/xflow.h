@@ -36,6 +36,8 @@ enum {
   XF_ERR_NOMEM = 4,
   XF_ERR_STATE = 5,      /* object used with the wrong grid / dtype            */
   XF_ERR_UNSUPPORTED = 6,
+  XF_ERR_CHECK = 7,      /* a border-condition consistency check of the        */
+                         /* reference failed (XProblem.cpp:5690-5694, 5747-5752) */
   XF_STALL = 10,         /* solver made no progress                            */
   XF_DIVERGED = 11,
   XF_NAN = 12,
@@ -183,6 +185,81 @@ int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, x
  * host-resident caller such as the reference's time loop makes. */
 int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                   xf_solve_stats* stats);
+
+/* ---- time-step passes around the pressure solve --------------------------- */
+/* TVPProblem::SolveBySplitting (XProblem.cpp:5474-5829).  Staggered boxes as
+ * the reference's grids (XStatement.h:127-135): for a pressure grid gp of
+ * n1 x n2 x n3, u lives on an (n1-1) x n2 x n3 grid, v on n1 x (n2-1) x n3 and
+ * w on n1 x n2 x (n3-1); each is an FP64 xf_vec of its own xf_grid, whose
+ * point codes and separations (hxU, hyV, hzW) the passes read.  density is an
+ * FP64 pressure box (NULL: 1 everywhere); border boxes hold the boundary
+ * values the reference's GetBorderCondition* return (NULL: 0).  Results are
+ * bit-identical to the reference's loops.  A cell the reference throws on
+ * returns XF_ERR_MASK (or XF_ERR_CHECK for its value checks), naming the first
+ * such cell in its loop order. */
+/* Pressure right-hand side (XProblem.cpp:5474-5512): Fictive 0; Actual
+ * -(rho^2 du/dx + dv/dy + dw/dz) / tau; PreDefined the border value. */
+int xf_pressure_rhs(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, const xf_vec* density,
+                    double tau, const xf_vec* border, xf_vec* rhs);
+/* Velocity correction of component `axis` (XProblem.cpp:5598-5777):
+ * vel = vel_prev - tau dp/dx_axis / rho on Actual/Normal/Equation cells, the
+ * border value on Defined cells, then PreDefined cells mirror their single
+ * Actual neighbour (2 * border - vel[neighbour]).  p is the pressure box. */
+int xf_velocity_correct(int axis, const xf_vec* vel_prev, const xf_vec* p, const xf_vec* density, double tau,
+                        const xf_vec* border, xf_vec* vel);
+/* Control balance (XProblem.cpp:5782-5829): the first strict maximum of
+ * |div u| over Actual pressure cells in i->j->k order, and its (i, j, k)
+ * (-1s when no cell beats 0). */
+int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, double* value,
+                      int32_t* ijk);
+
+/* ---- tridiagonal lines ---------------------------------------------------- */
+/* Replaces TSLAE::SolveByScalarRunning(M, u, a, b, c, f) (XSLAE.h:23,
+ * XSLAE.cpp:416-445), called once per grid line by the ADI sweeps
+ * (XProblem.cpp:1369, 2049, 2734, 3427): here every line of a sweep in one
+ * call.  Solves a[m] u[m-1] + b[m] u[m] + c[m] u[m+1] = f[m], m = 1..M-1, with
+ * u[0] and u[M] given (and kept), for nl1 * nl2 lines; element m of line
+ * (l1, l2) of every array is at offset l1*ls1 + l2*ls2 + m*ms.  All arrays are
+ * FP64 device memory (e.g. xf_vec_data of boxes).  The reference's recurrences
+ * and operation order: bit-identical results.  Asynchronous on the context
+ * stream; uses a context workspace of M * nl1 * nl2 doubles. */
+int xf_thomas_lines(xf_ctx* ctx, int M, int nl1, int nl2, int64_t ls1, int64_t ls2, int64_t ms, double* u,
+                    const double* a, const double* b, const double* c, const double* f);
+
+/* ---- immersed boundary ---------------------------------------------------- */
+/* Replaces the marker side of TImmersedBoundaryProblem (XProblem.h:1060-1112):
+ * ComputeBoundaryForces, SpreadForce, Interpolate, UpdateBoundaryPosition
+ * (XProblem.cpp:8436-8894) over the TImmersedBoundary node list.  Nodes are
+ * created once from host arrays and stay on the device:
+ *   pos, ref     3 doubles per node (x, y, z; ref = the target-node anchor)
+ *   kind         node law (XImmersedBoundary.h / .cpp:654-759), XF_IB_* below
+ *   next, prev   neighbour node index or -1 (TNode::neighbors)
+ *   dist0        initial distance to next; curv0 3 per node (initialCurvatures)
+ *   node_stiff   per-node stiffness (fixed-elastic nodes)
+ *   params       {stiffness, stretchingStiffness, bendingStiffness, area}
+ * Boxes (velocity, force) are FP64 xf_vec of the staggered grid of `axis`
+ * (1 = x, 2 = y, 3 = z); h0 holds the three uniform spacings.  Forces sum in
+ * the reference's serial node order (bit-identical); spreading adds markers'
+ * contributions with atomics (last-bit order effects). */
+enum { XF_IB_ELASTIC = 0, XF_IB_TARGET = 1, XF_IB_FIXED_ELASTIC = 2, XF_IB_PLAIN = 3, XF_IB_FIXED_STRETCHING = 4 };
+enum { XF_IB_POS = 0, XF_IB_VEL = 1, XF_IB_FORCE = 2 };   /* fields: 3 * nn doubles each */
+typedef struct xf_ib xf_ib;
+int xf_ib_create(xf_ctx* ctx, int nn, const double* pos, const double* ref, const int32_t* kind, const int32_t* next,
+                 const int32_t* prev, const double* dist0, const double* curv0, const double* node_stiff,
+                 const double* params, xf_ib** out);
+int xf_ib_destroy(xf_ib* ib);
+/* POS: x,y,z per node; VEL and FORCE: the x array, then y, then z (nn each). */
+int xf_ib_download(const xf_ib* ib, int field, double* host);
+int xf_ib_upload(xf_ib* ib, int field, const double* host);
+/* Interpolate (XProblem.cpp:8620-8791): node velocity[axis] from the box. */
+int xf_ib_interpolate(xf_ib* ib, const xf_vec* velocity, const double* h0, int axis);
+/* UpdateBoundaryPosition (XProblem.cpp:8858-8894): pos[axis] += vel[axis] * tau. */
+int xf_ib_update_position(xf_ib* ib, int axis, double tau);
+/* ComputeBoundaryForces (XProblem.cpp:8436-8547): force[axis] from positions. */
+int xf_ib_compute_forces(xf_ib* ib, int axis);
+/* SpreadForce (XProblem.cpp:8550-8617, arithmetic): zero the box, then add
+ * every node's force[axis] times its 7^3 cosine-delta weights. */
+int xf_ib_spread(xf_ib* ib, xf_vec* force, const double* h0, int axis);
 
 /* ---- measurement ---------------------------------------------------------- */
 /* No counterpart in the reference (a profiling helper).  Times each kernel of

@@ -34,6 +34,7 @@ def lib():
         L.xfo_dot.restype = C.c_double
         L.xfo_norm.restype = C.c_double
         L.xfo_absmax.restype = C.c_double
+        L.xfo_divergence_max.restype = C.c_double
         _lib = L
     return _lib
 
@@ -202,3 +203,37 @@ def ib_spread(shape, h0, axis, pos, force, fbox=None):
     lib().xfo_ib_spread(_p(fbox, C.c_double), *shape, _p(h0, C.c_double), int(axis), len(pos),
                         _p(pos, C.c_double), _p(f64(force), C.c_double))
     return fbox
+
+
+# Time-step passes (XProblem.cpp:5474-5829)
+def pressure_rhs(codes, u, v, w, hxU, hyV, hzW, tau, density=None, border=None):
+    codes = np.ascontiguousarray(codes, np.int32)
+    rhs = np.zeros(codes.shape)
+    bad = C.c_int64(-1)
+    st = lib().xfo_pressure_rhs(_p(codes, C.c_int32), *codes.shape, _p(f64(u), C.c_double), _p(f64(v), C.c_double),
+                                _p(f64(w), C.c_double), _p(f64(hxU), C.c_double), _p(f64(hyV), C.c_double),
+                                _p(f64(hzW), C.c_double), _p(f64(density), C.c_double) if density is not None else None,
+                                C.c_double(tau), _p(f64(border), C.c_double) if border is not None else None,
+                                _p(rhs, C.c_double), C.byref(bad))
+    return rhs, st, bad.value
+
+
+def velocity_correct(axis, codes, prev, p, hP, tau, density=None, border=None, cur=None):
+    codes = np.ascontiguousarray(codes, np.int32)
+    cur = np.zeros(codes.shape) if cur is None else f64(cur).copy()
+    bad = C.c_int64(-1)
+    st = lib().xfo_velocity_correct(int(axis), _p(codes, C.c_int32), *codes.shape, _p(f64(prev), C.c_double),
+                                    _p(f64(p), C.c_double), _p(f64(hP), C.c_double),
+                                    _p(f64(density), C.c_double) if density is not None else None, C.c_double(tau),
+                                    _p(f64(border), C.c_double) if border is not None else None,
+                                    _p(cur, C.c_double), C.byref(bad))
+    return cur, st, bad.value
+
+
+def divergence_max(codes, u, v, w, hxU, hyV, hzW):
+    codes = np.ascontiguousarray(codes, np.int32)
+    ijk = np.zeros(3, np.int32)
+    val = lib().xfo_divergence_max(_p(codes, C.c_int32), *codes.shape, _p(f64(u), C.c_double),
+                                   _p(f64(v), C.c_double), _p(f64(w), C.c_double), _p(f64(hxU), C.c_double),
+                                   _p(f64(hyV), C.c_double), _p(f64(hzW), C.c_double), _p(ijk, C.c_int32))
+    return val, tuple(int(t) for t in ijk)

@@ -662,3 +662,133 @@ void xfo_ib_spread(double* fbox, int n1, int n2, int n3, const double* h0, int a
         }
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Pressure right-hand side, XProblem.cpp:5474-5512.  Point codes as XMask.h:
+ * 0 Fictive, 1 Actual, 3 Defined, 4 PreDefined, 5 Normal, 6 PreNormal,
+ * 7 Equation, 8 PreEquation.  An Actual cell on the box face would read
+ * outside the velocity boxes in the reference: reported as XFO_ERR_MASK. */
+int xfo_pressure_rhs(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                     const double* w, const double* hxU, const double* hyV, const double* hzW, const double* density,
+                     double tau, const double* border, double* rhs, int64_t* bad) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int64_t sv1 = (int64_t)(n2 - 1) * n3, sw1 = (int64_t)n2 * (n3 - 1), sw2 = n3 - 1;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t c = i * s1 + j * s2 + k;
+        const int mijk = codes[c];
+        if (mijk == 0) {
+          rhs[c] = 0;
+        } else if (mijk == 1) {
+          if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
+            *bad = c;
+            return XFO_ERR_MASK;
+          }
+          double u_i_1 = u[(i - 1) * s1 + j * s2 + k], u_i = u[i * s1 + j * s2 + k];
+          double v_j_1 = v[i * sv1 + (j - 1) * s2 + k], v_j = v[i * sv1 + j * s2 + k];
+          double w_k_1 = w[i * sw1 + j * sw2 + k - 1], w_k = w[i * sw1 + j * sw2 + k];
+          double d = density ? density[c] : 1.0;
+          double div_ = d * d * ((u_i - u_i_1) / hxU[i - 1]) + ((v_j - v_j_1) / hyV[j - 1]) +
+                        ((w_k - w_k_1) / hzW[k - 1]);
+          rhs[c] = -(div_ / tau);
+        } else if (mijk == 4) {
+          rhs[c] = border ? border[c] : 0.0;
+        } else {   /* not implemented for this border type / unknown code: the reference throws */
+          *bad = c;
+          return XFO_ERR_MASK;
+        }
+      }
+  return XFO_OK;
+}
+
+/* Velocity correction of one component, XProblem.cpp:5598-5777: pass 1 over
+ * every cell but PreDefined, pass 2 over PreDefined cells. */
+int xfo_velocity_correct(int axis, const int32_t* codes, int b1, int b2, int b3, const double* prev, const double* p,
+                         const double* hP, const double* density, double tau, const double* border, double* cur,
+                         int64_t* bad) {
+  const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
+  const int p2 = axis == 2 ? b2 + 1 : b2, p3 = axis == 3 ? b3 + 1 : b3;
+  const int64_t ps1 = (int64_t)p2 * p3, ps2 = p3;
+  for (int pass = 1; pass < 3; pass++)
+    for (int i = 0; i < b1; i++)
+      for (int j = 0; j < b2; j++)
+        for (int k = 0; k < b3; k++) {
+          const int64_t c = i * s1 + j * s2 + k;
+          const int mijk = codes[c];
+          if (pass == 1 && mijk == 4) continue;
+          if (pass == 2 && mijk != 4) continue;
+          if (mijk == 0) {
+            cur[c] = 0;
+          } else if (mijk == 1 || mijk == 5 || mijk == 7) {
+            const int64_t cp = i * ps1 + j * ps2 + k;
+            double gradP;
+            if (axis == 1) gradP = (p[cp + ps1] - p[cp]) / hP[i];
+            else if (axis == 2) gradP = (p[cp + ps2] - p[cp]) / hP[j];
+            else gradP = (p[cp + 1] - p[cp]) / hP[k];
+            cur[c] = prev[c] - tau * gradP / (density ? density[cp] : 1.0);
+          } else if (mijk == 3) {
+            double defVal = border ? border[c] : 0.0;
+            if (prev[c] != defVal) {
+              *bad = c;
+              return XFO_ERR_CHECK;
+            }
+            cur[c] = defVal;
+          } else if (mijk == 4) {
+            double defVal = border ? border[c] : 0.0;
+            int64_t nb = -1;
+            int count = 0;
+            for (int dir = 1; dir < 4; dir++)
+              for (int sign = 0; sign < 2; sign++) {
+                int shift = -1 + sign * 2;
+                int ii = i, jj = j, kk = k;
+                if (dir == 1) ii = i + shift;
+                else if (dir == 2) jj = j + shift;
+                else kk = k + shift;
+                if (ii >= 0 && ii < b1 && jj >= 0 && jj < b2 && kk >= 0 && kk < b3 &&
+                    codes[ii * s1 + jj * s2 + kk] == 1) {
+                  nb = ii * s1 + jj * s2 + kk;
+                  count++;
+                }
+              }
+            if (count != 1) {
+              *bad = c;
+              return XFO_ERR_MASK;
+            }
+            double check = fabs(prev[c] - (2 * defVal - prev[nb]));
+            if (check > 1e-10) {
+              *bad = c;
+              return XFO_ERR_CHECK;
+            }
+            cur[c] = 2 * defVal - cur[nb];
+          } else {
+            *bad = c;
+            return XFO_ERR_MASK;
+          }
+        }
+  return XFO_OK;
+}
+
+/* Control balance, XProblem.cpp:5782-5829. */
+double xfo_divergence_max(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                          const double* w, const double* hxU, const double* hyV, const double* hzW, int32_t* ijk) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int64_t sv1 = (int64_t)(n2 - 1) * n3, sw1 = (int64_t)n2 * (n3 - 1), sw2 = n3 - 1;
+  double divMaxValue = 0;
+  ijk[0] = ijk[1] = ijk[2] = -1;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        if (codes[i * s1 + j * s2 + k] != 1) continue;
+        double div = ((u[i * s1 + j * s2 + k] - u[(i - 1) * s1 + j * s2 + k]) / hxU[i - 1]) +
+                     ((v[i * sv1 + j * s2 + k] - v[i * sv1 + (j - 1) * s2 + k]) / hyV[j - 1]) +
+                     ((w[i * sw1 + j * sw2 + k] - w[i * sw1 + j * sw2 + k - 1]) / hzW[k - 1]);
+        if (fabs(div) > divMaxValue) {
+          divMaxValue = fabs(div);
+          ijk[0] = i;
+          ijk[1] = j;
+          ijk[2] = k;
+        }
+      }
+  return divMaxValue;
+}

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-enum { XFO_OK = 0, XFO_ERR_MASK = 3, XFO_ERR_ARG = 1 };
+enum { XFO_OK = 0, XFO_ERR_MASK = 3, XFO_ERR_ARG = 1, XFO_ERR_CHECK = 7 };
 enum { XFO_OP_LAPLACE = 0, XFO_OP_VARDIV = 1 };
 
 void xfo_set_threads(int n);
@@ -75,6 +75,22 @@ void xfo_ib_forces(int nn, int axis, const double* pos, const double* ref, const
                    const double* node_stiff, const double* params, double* force);
 void xfo_ib_spread(double* fbox, int n1, int n2, int n3, const double* h0, int axis, int nn, const double* pos,
                    const double* force);
+
+/* Time-step passes of TVPProblem::SolveBySplitting.  Staggered boxes: u is
+ * (n1-1) x n2 x n3, v n1 x (n2-1) x n3, w n1 x n2 x (n3-1) for a pressure box
+ * n1 x n2 x n3; hxU/hyV/hzW are the separations of the u/v/w grids along their
+ * own axis.  density may be NULL (1); border NULL (0).  Return 0, or the
+ * reference's throw as XFO_ERR_MASK / XFO_ERR_CHECK with its cell in *bad. */
+int xfo_pressure_rhs(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                     const double* w, const double* hxU, const double* hyV, const double* hzW, const double* density,
+                     double tau, const double* border, double* rhs, int64_t* bad);
+/* vel box b1 x b2 x b3 with codes; p box one layer longer along axis; hP the
+ * pressure separations along axis. */
+int xfo_velocity_correct(int axis, const int32_t* codes, int b1, int b2, int b3, const double* prev, const double* p,
+                         const double* hP, const double* density, double tau, const double* border, double* cur,
+                         int64_t* bad);
+double xfo_divergence_max(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                          const double* w, const double* hxU, const double* hyV, const double* hzW, int32_t* ijk);
 
 #ifdef __cplusplus
 }

@@ -13,8 +13,9 @@ import weakref
 import numpy as np
 
 from . import capi
-from .capi import (XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_MINRES,  # noqa: F401
-                   XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_ZERO_INACTIVE, XFError)
+from .capi import (XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE,  # noqa: F401
+                   XF_IB_POS, XF_IB_VEL, XF_MINRES, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED,
+                   XF_ZERO_INACTIVE, XFError)
 
 
 def _check(ctx_handle, st):
@@ -294,3 +295,105 @@ class SLAE:
     @property
     def Result(self):
         return self.x
+
+
+# ---------------------------------------------------------------------------
+# Time-step passes around the pressure solve (XProblem.cpp:5474-5829)
+def _h(v):
+    return v.h if v is not None else None
+
+
+def pressure_rhs(gp, u, v, w, tau, rhs, density=None, border=None):
+    """rhs |= the reference's pressure right-hand side (XProblem.cpp:5474-5512)."""
+    _check(gp.ctx.h, capi.lib().xf_pressure_rhs(gp.h, u.h, v.h, w.h, _h(density), float(tau), _h(border), rhs.h))
+    return rhs
+
+
+def velocity_correct(axis, vel_prev, p, tau, vel, density=None, border=None):
+    """vel |= the projected velocity component `axis` (XProblem.cpp:5598-5777)."""
+    _check(vel.grid.ctx.h, capi.lib().xf_velocity_correct(int(axis), vel_prev.h, p.h, _h(density), float(tau),
+                                                          _h(border), vel.h))
+    return vel
+
+
+def divergence_max(gp, u, v, w):
+    """(max |div u| over Actual cells, (i, j, k)) as the control balance (XProblem.cpp:5782-5829)."""
+    val = C.c_double()
+    ijk = np.zeros(3, np.int32)
+    _check(gp.ctx.h, capi.lib().xf_divergence_max(gp.h, u.h, v.h, w.h, C.byref(val), capi._ptr(ijk)))
+    return val.value, tuple(int(t) for t in ijk)
+
+
+# ---------------------------------------------------------------------------
+def thomas_lines(ctx, M, u, a, b, c, f, nl1, nl2, ls1, ls2, ms):
+    """TSLAE::SolveByScalarRunning over nl1*nl2 lines at once (XSLAE.cpp:416-445).
+    u, a, b, c, f are FP64 Vecs (or raw device pointers); element m of line
+    (l1, l2) sits at l1*ls1 + l2*ls2 + m*ms.  Asynchronous on the context stream."""
+    def ptr(v):
+        return capi.lib().xf_vec_data(v.h) if isinstance(v, Vec) else v
+    _check(ctx.h, capi.lib().xf_thomas_lines(ctx.h, int(M), int(nl1), int(nl2), int(ls1), int(ls2), int(ms),
+                                             ptr(u), ptr(a), ptr(b), ptr(c), ptr(f)))
+
+
+def box_lines(shape, axis):
+    """(M, nl1, nl2, ls1, ls2, ms) of the lines of a C-order box along axis 1..3."""
+    n1, n2, n3 = shape
+    s1, s2 = n2 * n3, n3
+    if axis == 1:
+        return n1 - 1, n2, n3, s2, 1, s1
+    if axis == 2:
+        return n2 - 1, n1, n3, s1, 1, s2
+    return n3 - 1, n1, n2, s1, s2, 1
+
+
+class Markers(_Owned):
+    """Immersed-boundary node list on the device (TImmersedBoundary nodes and
+    the marker side of TImmersedBoundaryProblem, XProblem.cpp:8436-8894)."""
+
+    def __init__(self, ctx, pos, ref, kind, nxt, prv, dist0, curv0, node_stiff, params):
+        self.ctx = ctx
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        pos, ref, curv0 = f64(pos).reshape(-1, 3), f64(ref).reshape(-1, 3), f64(curv0).reshape(-1, 3)
+        self.nn = len(pos)
+        keep = (pos, ref, i32(kind), i32(nxt), i32(prv), f64(dist0), curv0, f64(node_stiff), f64(params))
+        h = C.c_void_p()
+        _check(ctx.h, capi.lib().xf_ib_create(ctx.h, self.nn, *[capi._ptr(a) for a in keep], C.byref(h)))
+        self.h = h
+        ctx._adopt(self)
+
+    def get(self, field):
+        out = np.empty(3 * self.nn, np.float64)
+        _check(self.ctx.h, capi.lib().xf_ib_download(self.h, field, capi._ptr(out)))
+        return out.reshape(self.nn, 3) if field == XF_IB_POS else out.reshape(3, self.nn)
+
+    def set(self, field, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        assert a.size == 3 * self.nn
+        _check(self.ctx.h, capi.lib().xf_ib_upload(self.h, field, capi._ptr(a)))
+
+    def interpolate(self, velocity, h0, axis):
+        h0 = np.ascontiguousarray(h0, dtype=np.float64)
+        _check(self.ctx.h, capi.lib().xf_ib_interpolate(self.h, velocity.h, capi._ptr(h0), int(axis)))
+
+    def update_position(self, axis, tau):
+        _check(self.ctx.h, capi.lib().xf_ib_update_position(self.h, int(axis), float(tau)))
+
+    def compute_forces(self, axis):
+        _check(self.ctx.h, capi.lib().xf_ib_compute_forces(self.h, int(axis)))
+
+    def spread(self, force, h0, axis):
+        h0 = np.ascontiguousarray(h0, dtype=np.float64)
+        _check(self.ctx.h, capi.lib().xf_ib_spread(self.h, force.h, capi._ptr(h0), int(axis)))
+
+    def close(self):
+        if self.h:
+            if self.ctx.h:
+                capi.lib().xf_ib_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

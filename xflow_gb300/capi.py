@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libxflow.so")
 
 XF_OK, XF_ERR_ARG, XF_ERR_CUDA, XF_ERR_MASK, XF_ERR_NOMEM, XF_ERR_STATE, XF_ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5, 6
+XF_ERR_CHECK = 7
 XF_STALL, XF_DIVERGED, XF_NAN, XF_MAXIT, XF_BREAKDOWN = 10, 11, 12, 13, 14
 XF_F64, XF_F32 = 0, 1
 XF_OP_LAPLACE, XF_OP_VARDIV = 0, 1
@@ -18,6 +19,8 @@ XF_EXACT, XF_ZERO_INACTIVE = 1, 2
 XF_CG, XF_CG_REFERENCE, XF_BICGSTAB, XF_MINRES, XF_BICG, XF_FCG = 0, 1, 2, 3, 4, 5
 XF_PREC_FP64, XF_PREC_MIXED = 0, 1
 XF_PRECOND_NONE, XF_PRECOND_JACOBI, XF_PRECOND_UNET = 0, 1, 2
+XF_IB_ELASTIC, XF_IB_TARGET, XF_IB_FIXED_ELASTIC, XF_IB_PLAIN, XF_IB_FIXED_STRETCHING = 0, 1, 2, 3, 4
+XF_IB_POS, XF_IB_VEL, XF_IB_FORCE = 0, 1, 2
 
 # Every symbol include/xflow.h declares (checked by tests/test_abi.py).
 EXPORTS = [
@@ -26,7 +29,9 @@ EXPORTS = [
     "xf_grid_check", "xf_vec_create", "xf_vec_destroy", "xf_vec_upload", "xf_vec_download", "xf_vec_assign",
     "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_matvec",
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
-    "xf_solve_host", "xf_profile_cg_kernels", "xf_dot_noalloc",
+    "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
+    "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
+    "xf_profile_cg_kernels", "xf_dot_noalloc",
 ]
 
 
@@ -88,6 +93,19 @@ def lib():
         L.xf_solve_host.argtypes = [vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
         L.xf_dot_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
         L.xf_profile_cg_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        L.xf_pressure_rhs.argtypes = [vp, vp, vp, vp, vp, C.c_double, vp, vp]
+        L.xf_velocity_correct.argtypes = [C.c_int, vp, vp, vp, C.c_double, vp, vp]
+        L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]
+        L.xf_thomas_lines.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64,
+                                      vp, vp, vp, vp, vp]
+        L.xf_ib_create.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
+        L.xf_ib_destroy.argtypes = [vp]
+        L.xf_ib_download.argtypes = [vp, C.c_int, vp]
+        L.xf_ib_upload.argtypes = [vp, C.c_int, vp]
+        L.xf_ib_interpolate.argtypes = [vp, vp, vp, C.c_int]
+        L.xf_ib_update_position.argtypes = [vp, C.c_int, C.c_double]
+        L.xf_ib_compute_forces.argtypes = [vp, C.c_int]
+        L.xf_ib_spread.argtypes = [vp, vp, vp, C.c_int]
         _lib = L
     return _lib
 

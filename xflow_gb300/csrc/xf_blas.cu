@@ -37,39 +37,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(const T* __restrict__ a, co
   }
 }
 
-// First strict maximum of |a| in flat order: (value, cell) pairs combine by
-// larger value, then smaller cell.
-struct AbsMax { double v; long long c; };
-__device__ __forceinline__ AbsMax am_combine(AbsMax x, AbsMax y) {
-  if (y.c < 0) return x;
-  if (x.c < 0) return y;
-  if (y.v > x.v || (y.v == x.v && y.c < x.c)) return y;
-  return x;
-}
-__device__ __forceinline__ AbsMax am_warp(AbsMax a) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    AbsMax b;
-    b.v = __shfl_xor_sync(0xffffffffu, a.v, o);
-    b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
-    a = am_combine(a, b);
-  }
-  return a;
-}
-__device__ AbsMax am_block(AbsMax a, AbsMax* sh) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  a = am_warp(a);
-  __syncthreads();
-  if (lane == 0) sh[w] = a;
-  __syncthreads();
-  const int nw = (blockDim.x + 31) >> 5;
-  AbsMax r;
-  r.v = 0; r.c = -1;
-  if (threadIdx.x < nw) r = sh[threadIdx.x];
-  if (w == 0) r = am_warp(r);
-  return r;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_absmax(const T* __restrict__ a, const uint8_t* __restrict__ m,
                                                         const int32_t* __restrict__ inv, int64_t n, DevScratch* S,

@@ -39,14 +39,20 @@ struct xf_ctx {
   DevScratch* scratch;       // device
   double* host_scalars;      // pinned, 256 doubles
   cudaEvent_t ev0, ev1;
+  void* work = nullptr;       // device workspace of line solvers (grows, freed by xf_destroy)
+  size_t work_bytes = 0;
   char err[512];
 };
+
+// Device workspace of at least `bytes` (nullptr when it cannot grow).
+void* xf_ctx_work(xf_ctx* ctx, size_t bytes);
 
 struct xf_grid {
   xf_ctx* ctx;
   int n1, n2, n3;
   int64_t ncell, s1, s2;
   int64_t end_index;
+  uint8_t* code;             // device, per cell: the reference point code (0..8)
   uint8_t* kind;             // device, per cell
   uint8_t* smask;            // device, per cell (0/1)
   int32_t* inv;              // device, Rn index per cell (0 inactive)
@@ -163,6 +169,39 @@ __device__ inline double block_sum_acc<float>(const DotAcc<float>& acc, double* 
   double v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
   if (w == 0) v = warp_sum(v);
   return v;
+}
+
+// First strict maximum of |a| in flat order: (value, cell) pairs combine by
+// larger value, then smaller cell.
+struct AbsMax { double v; long long c; };
+__device__ __forceinline__ AbsMax am_combine(AbsMax x, AbsMax y) {
+  if (y.c < 0) return x;
+  if (x.c < 0) return y;
+  if (y.v > x.v || (y.v == x.v && y.c < x.c)) return y;
+  return x;
+}
+__device__ __forceinline__ AbsMax am_warp(AbsMax a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    AbsMax b;
+    b.v = __shfl_xor_sync(0xffffffffu, a.v, o);
+    b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
+    a = am_combine(a, b);
+  }
+  return a;
+}
+__device__ inline AbsMax am_block(AbsMax a, AbsMax* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  a = am_warp(a);
+  __syncthreads();
+  if (lane == 0) sh[w] = a;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  AbsMax r;
+  r.v = 0; r.c = -1;
+  if (threadIdx.x < nw) r = sh[threadIdx.x];
+  if (w == 0) r = am_warp(r);
+  return r;
 }
 
 // Block reduction helpers (FP64).

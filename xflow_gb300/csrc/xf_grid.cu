@@ -27,6 +27,7 @@ extern "C" const char* xf_status_string(int s) {
     case XF_ERR_NOMEM: return "out of device memory";
     case XF_ERR_STATE: return "object mismatch";
     case XF_ERR_UNSUPPORTED: return "unsupported combination";
+    case XF_ERR_CHECK: return "border-condition check failed";
     case XF_STALL: return "solver stalled";
     case XF_DIVERGED: return "solver diverged";
     case XF_NAN: return "NaN in solver";
@@ -60,11 +61,29 @@ extern "C" int xf_create(int device, xf_ctx** out) {
   return XF_OK;
 }
 
+void* xf_ctx_work(xf_ctx* ctx, size_t bytes) {
+  if (ctx->work_bytes >= bytes) return ctx->work;
+  if (ctx->work) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->work);
+  }
+  ctx->work = nullptr;
+  ctx->work_bytes = 0;
+  if (cudaMalloc(&ctx->work, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->work = nullptr;
+    return nullptr;
+  }
+  ctx->work_bytes = bytes;
+  return ctx->work;
+}
+
 extern "C" int xf_destroy(xf_ctx* ctx) {
   if (!ctx) return XF_ERR_ARG;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->scratch);
+  if (ctx->work) cudaFree(ctx->work);
   cudaFreeHost(ctx->host_scalars);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
@@ -341,13 +360,21 @@ extern "C" int xf_grid_destroy(xf_grid* g) {
   if (!g) return XF_ERR_ARG;
   cudaSetDevice(g->ctx->device);
   cudaStreamSynchronize(g->ctx->stream);
-  void* ptrs[] = {g->diag, g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
+  void* ptrs[] = {g->diag, g->code, g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
                   g->cxm, g->cxp, g->cym, g->cyp, g->czm, g->czp, g->fxm, g->fxp, g->fym, g->fyp, g->fzm, g->fzp,
                   g->rhx, g->rhy, g->rhz, g->rhhx, g->rhhy, g->rhhz, g->frhx, g->frhy, g->frhz, g->frhhx, g->frhhy, g->frhhz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete g;
   return XF_OK;
+}
+
+// Point codes as bytes (codes outside 0..255 become 255: an unknown code).
+__global__ void k_code_bytes(const int32_t* __restrict__ codes, int64_t n, uint8_t* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t m = codes[c];
+    out[c] = (m >= 0 && m < 255) ? (uint8_t)m : (uint8_t)255;
+  }
 }
 
 extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t* codes, const double* hx,
@@ -390,6 +417,9 @@ extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t
   G_TRY(cudaMalloc(&d_bad, 2 * sizeof(unsigned long long)));
   G_TRY(cudaMemcpyAsync(d_bad, h_bad, sizeof(h_bad), cudaMemcpyHostToDevice, ctx->stream));
   k_classify<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(d_codes, d_nrm, n1, n2, n3, g->kind, g->smask, d_isb, d_bad);
+  G_TRY(cudaGetLastError());
+  G_TRY(cudaMalloc(&g->code, n));
+  k_code_bytes<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(d_codes, n, g->code);
   G_TRY(cudaGetLastError());
   G_TRY(cudaMemcpyAsync(h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost, ctx->stream));
   if ((st = scan_number(ctx, g->smask, n, g->inv, 1, 0, &g->end_index)) != XF_OK) goto fail;

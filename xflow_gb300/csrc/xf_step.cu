@@ -1,0 +1,358 @@
+// The time-step passes on either side of the pressure solve
+// (TVPProblem::SolveBySplitting):
+//
+//  xf_pressure_rhs      right-hand side of the pressure equation,
+//                       XProblem.cpp:5474-5512;
+//  xf_velocity_correct  projection of one staggered velocity component,
+//                       XProblem.cpp:5598-5777;
+//  xf_divergence_max    the "control balance" check, XProblem.cpp:5782-5829.
+//
+// Staggered boxes follow the reference's grids (XStatement.h:127-135): with the
+// pressure box n1 x n2 x n3, the u box is (n1-1) x n2 x n3, v is n1 x (n2-1) x n3
+// and w is n1 x n2 x (n3-1), all C order; each velocity box's own grid carries
+// the separations the reference reads (hxU, hyV, hzW).  One thread per cell, the
+// reference's expressions and operation order (FP64, no contraction): results
+// are bit-identical to its loops.
+//
+// The reference throws at the first offending cell of its loop; here every
+// offending cell reports its index to a per-kind minimum (atomicMin) in the
+// context scratch, and the host turns the first one in the reference's loop
+// order into the status and message.
+#include <math.h>
+
+#include "xf_common.cuh"
+
+enum { PC_FICTIVE = 0, PC_ACTUAL = 1, PC_DEFINED = 3, PC_PREDEFINED = 4, PC_NORMAL = 5, PC_PRENORMAL = 6,
+       PC_EQUATION = 7, PC_PREEQUATION = 8 };
+
+// Error kinds, each the minimum offending cell in iscalars[CHK0 + kind].
+enum { CHK0 = 48, E_RANGE = 0, E_NOTIMPL_P, E_UNKNOWN, E_DEFINED, E_PREDEF_NONE, E_PREDEF_MANY, E_PREDEF_VALUE,
+       E_NOTIMPL_V, E_COUNT };
+constexpr long long NO_CELL = 0x7f7f7f7f7f7f7f7fLL;   // cudaMemset byte 0x7f
+constexpr int SL_STEP = 8;                              // reduction slot of xf_divergence_max (and SL_STEP + 1)
+
+__device__ __forceinline__ void report(DevScratch* S, int kind, long long cell) {
+  atomicMin(&S->iscalars[CHK0 + kind], cell);
+}
+
+__global__ void k_pressure_rhs(const uint8_t* __restrict__ code, int n1, int n2, int n3, const double* __restrict__ u,
+                               const double* __restrict__ v, const double* __restrict__ w,
+                               const double* __restrict__ hxU, const double* __restrict__ hyV,
+                               const double* __restrict__ hzW, const double* __restrict__ rho, double tau,
+                               const double* __restrict__ border, double* __restrict__ rhs, DevScratch* S) {
+  const int64_t n = (int64_t)n1 * n2 * n3;
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int64_t sv1 = (int64_t)(n2 - 1) * n3, sw1 = (int64_t)n2 * (n3 - 1), sw2 = n3 - 1;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int m = code[c];
+    if (m == PC_FICTIVE) {
+      rhs[c] = 0;
+    } else if (m == PC_ACTUAL) {
+      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
+        report(S, E_RANGE, c);   // the reference would read outside the velocity boxes
+        continue;
+      }
+      const int64_t cu = i * s1 + j * s2 + k;            // u box: (n1-1) x n2 x n3
+      const int64_t cv = i * sv1 + j * s2 + k;           // v box: n1 x (n2-1) x n3
+      const int64_t cw = i * sw1 + j * sw2 + k;          // w box: n1 x n2 x (n3-1)
+      const double u_i_1 = u[cu - s1], u_i = u[cu];
+      const double v_j_1 = v[cv - s2], v_j = v[cv];
+      const double w_k_1 = w[cw - 1], w_k = w[cw];
+      const double d = rho ? rho[c] : 1.0;
+      const double div_ = d * d * ((u_i - u_i_1) / hxU[i - 1]) + ((v_j - v_j_1) / hyV[j - 1]) +
+                          ((w_k - w_k_1) / hzW[k - 1]);
+      rhs[c] = -(div_ / tau);
+    } else if (m == PC_PREDEFINED) {
+      rhs[c] = border ? border[c] : 0.0;
+    } else if (m == PC_PRENORMAL || m == PC_DEFINED || m == PC_NORMAL || m == PC_EQUATION || m == PC_PREEQUATION) {
+      report(S, E_NOTIMPL_P, c);
+    } else {
+      report(S, E_UNKNOWN, c);
+    }
+  }
+}
+
+// Velocity correction, pass 1 (every cell but PreDefined ones): axis 1..3;
+// the velocity box is b1 x b2 x b3, the pressure box has one more layer along
+// the axis.
+__global__ void k_vel_pass1(int axis, const uint8_t* __restrict__ code, int b1, int b2, int b3,
+                            const double* __restrict__ prev, double* __restrict__ cur, const double* __restrict__ p,
+                            const double* __restrict__ hP, const double* __restrict__ rho, double tau,
+                            const double* __restrict__ border, DevScratch* S) {
+  const int64_t n = (int64_t)b1 * b2 * b3;
+  const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
+  const int p2 = axis == 2 ? b2 + 1 : b2, p3 = axis == 3 ? b3 + 1 : b3;
+  const int64_t ps1 = (int64_t)p2 * p3, ps2 = p3;
+  const int64_t pstep = axis == 1 ? ps1 : axis == 2 ? ps2 : 1;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int m = code[c];
+    if (m == PC_PREDEFINED) continue;
+    if (m == PC_FICTIVE) {
+      cur[c] = 0;
+    } else if (m == PC_ACTUAL || m == PC_NORMAL || m == PC_EQUATION) {
+      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      const int64_t cp = i * ps1 + j * ps2 + k;
+      const double h = axis == 1 ? hP[i] : axis == 2 ? hP[j] : hP[k];
+      const double gradP = (p[cp + pstep] - p[cp]) / h;
+      cur[c] = prev[c] - tau * gradP / (rho ? rho[cp] : 1.0);
+    } else if (m == PC_DEFINED) {
+      const double defVal = border ? border[c] : 0.0;
+      if (prev[c] != defVal) report(S, E_DEFINED, c);
+      cur[c] = defVal;
+    } else if (m == PC_PRENORMAL || m == PC_PREEQUATION) {
+      report(S, E_NOTIMPL_V, c);
+    } else {
+      report(S, E_UNKNOWN, c);
+    }
+  }
+}
+
+// Pass 2: PreDefined cells mirror their single Actual neighbour about the
+// border value.
+__global__ void k_vel_pass2(const uint8_t* __restrict__ code, int b1, int b2, int b3, const double* __restrict__ prev,
+                            double* __restrict__ cur, const double* __restrict__ border, DevScratch* S) {
+  const int64_t n = (int64_t)b1 * b2 * b3;
+  const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (code[c] != PC_PREDEFINED) continue;
+    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    const double defVal = border ? border[c] : 0.0;
+    int64_t nb = -1;
+    int count = 0;
+    for (int dir = 1; dir < 4; dir++)
+      for (int sign = 0; sign < 2; sign++) {
+        const int shift = -1 + sign * 2;
+        const int ii = dir == 1 ? i + shift : i, jj = dir == 2 ? j + shift : j, kk = dir == 3 ? k + shift : k;
+        if (ii >= 0 && ii < b1 && jj >= 0 && jj < b2 && kk >= 0 && kk < b3) {
+          const int64_t q = ii * s1 + jj * s2 + kk;
+          if (code[q] == PC_ACTUAL) {
+            nb = q;
+            count++;
+          }
+        }
+      }
+    if (count <= 0) { report(S, E_PREDEF_NONE, c); continue; }
+    if (count > 1) { report(S, E_PREDEF_MANY, c); continue; }
+    const double check = fabs(prev[c] - (2 * defVal - prev[nb]));
+    if (check > 1e-10) report(S, E_PREDEF_VALUE, c);
+    cur[c] = 2 * defVal - cur[nb];
+  }
+}
+
+// Control balance: first strict maximum of |div u| over Actual pressure cells.
+__global__ void __launch_bounds__(RED_THREADS) k_div_max(const uint8_t* __restrict__ code, int n1, int n2, int n3,
+                                                         const double* __restrict__ u, const double* __restrict__ v,
+                                                         const double* __restrict__ w, const double* __restrict__ hxU,
+                                                         const double* __restrict__ hyV,
+                                                         const double* __restrict__ hzW, DevScratch* S, int slot) {
+  __shared__ AbsMax sh[32];
+  __shared__ bool last;
+  const int64_t n = (int64_t)n1 * n2 * n3;
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int64_t sv1 = (int64_t)(n2 - 1) * n3, sw1 = (int64_t)n2 * (n3 - 1), sw2 = n3 - 1;
+  AbsMax best;
+  best.v = 0.0;
+  best.c = -1;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (code[c] != PC_ACTUAL) continue;
+    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
+      report(S, E_RANGE, c);   // the reference would read outside the velocity boxes
+      continue;
+    }
+    const int64_t cu = i * s1 + j * s2 + k, cv = i * sv1 + j * s2 + k, cw = i * sw1 + j * sw2 + k;
+    const double div = ((u[cu] - u[cu - s1]) / hxU[i - 1]) + ((v[cv] - v[cv - s2]) / hyV[j - 1]) +
+                       ((w[cw] - w[cw - 1]) / hzW[k - 1]);
+    const double a = fabs(div);
+    if (a > best.v) { best.v = a; best.c = c; }   // NaN never wins, as in the reference
+  }
+  AbsMax r = am_block(best, sh);
+  if (threadIdx.x == 0) {
+    S->partials[slot][blockIdx.x] = r.v;
+    S->partials[slot + 1][blockIdx.x] = (double)r.c;
+    __threadfence();
+    unsigned int t = atomicAdd(&S->tickets[slot], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  AbsMax q;
+  q.v = 0.0;
+  q.c = -1;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    AbsMax x;
+    x.v = __ldcg(&S->partials[slot][b]);
+    x.c = (long long)__ldcg(&S->partials[slot + 1][b]);
+    q = am_combine(q, x);
+  }
+  q = am_block(q, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[slot] = q.c >= 0 ? q.v : 0.0;
+    S->scalars[slot + 1] = (double)q.c;
+    S->tickets[slot] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+static bool is_f64(const xf_vec* v) { return v && v->dtype == XF_F64; }
+
+static int check_staggered(xf_ctx* ctx, const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w,
+                           const char* who) {
+  if (!is_f64(u) || !is_f64(v) || !is_f64(w)) return xf_fail(ctx, XF_ERR_ARG, "%s: u, v, w must be FP64 boxes", who);
+  const xf_grid *gu = u->g, *gv = v->g, *gw = w->g;
+  if (gu->ctx != ctx || gv->ctx != ctx || gw->ctx != ctx)
+    return xf_fail(ctx, XF_ERR_ARG, "%s: boxes of another context", who);
+  if (gu->n1 != gp->n1 - 1 || gu->n2 != gp->n2 || gu->n3 != gp->n3 || gv->n1 != gp->n1 || gv->n2 != gp->n2 - 1 ||
+      gv->n3 != gp->n3 || gw->n1 != gp->n1 || gw->n2 != gp->n2 || gw->n3 != gp->n3 - 1)
+    return xf_fail(ctx, XF_ERR_ARG,
+                   "%s: staggered boxes must be (n1-1,n2,n3), (n1,n2-1,n3), (n1,n2,n3-1) for a %dx%dx%d pressure box",
+                   who, gp->n1, gp->n2, gp->n3);
+  return XF_OK;
+}
+
+static int clear_checks(xf_ctx* ctx) {
+  XF_CUDA(ctx, cudaMemsetAsync(&ctx->scratch->iscalars[CHK0], 0x7f, E_COUNT * sizeof(long long), ctx->stream));
+  return XF_OK;
+}
+
+static int read_checks(xf_ctx* ctx, long long* out) {
+  XF_CUDA(ctx, cudaGetLastError());
+  XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->iscalars[CHK0], E_COUNT * sizeof(long long),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  memcpy(out, ctx->host_scalars, E_COUNT * sizeof(long long));
+  return XF_OK;
+}
+
+// The first offending cell (in flat order) among `kinds`, or -1.
+static int first_error(const long long* chk, const int* kinds, int nk, long long* cell) {
+  int best = -1;
+  *cell = NO_CELL;
+  for (int t = 0; t < nk; t++)
+    if (chk[kinds[t]] < *cell) {
+      *cell = chk[kinds[t]];
+      best = kinds[t];
+    }
+  return best;
+}
+
+static const char* check_message(int kind) {
+  switch (kind) {
+    case E_RANGE: return "an Actual pressure cell on the box face (the reference reads outside the velocity boxes)";
+    case E_NOTIMPL_P: return "Method is not implemented for this border point type of pressure";
+    case E_UNKNOWN: return "Unknown point mask type";
+    case E_DEFINED: return "Defined border condition checking error";
+    case E_PREDEF_NONE: return "PreDefined border condition checking error - actual values count <= 0";
+    case E_PREDEF_MANY: return "PreDefined border condition checking error - actual values count > 1";
+    case E_PREDEF_VALUE: return "PreDefined border condition checking error - value incorrect";
+    case E_NOTIMPL_V: return "Method is not implemented for this point border type of velocity";
+    default: return "unknown";
+  }
+}
+
+static int fail_at(xf_ctx* ctx, const xf_grid* g, int kind, long long cell, const char* who) {
+  const int i = (int)(cell / g->s1), j = (int)((cell - i * g->s1) / g->s2), k = (int)(cell % g->s2);
+  const int st = (kind == E_DEFINED || kind == E_PREDEF_VALUE) ? XF_ERR_CHECK : XF_ERR_MASK;
+  return xf_fail(ctx, st, "%s: %s at (%d, %d, %d)", who, check_message(kind), i, j, k);
+}
+
+static int same_box(const xf_vec* a, const xf_grid* g) {
+  return a->g->n1 == g->n1 && a->g->n2 == g->n2 && a->g->n3 == g->n3;
+}
+
+extern "C" int xf_pressure_rhs(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w,
+                               const xf_vec* density, double tau, const xf_vec* border, xf_vec* rhs) {
+  if (!gp || !rhs) return XF_ERR_ARG;
+  xf_ctx* ctx = gp->ctx;
+  int st;
+  if ((st = check_staggered(ctx, gp, u, v, w, "xf_pressure_rhs"))) return st;
+  if (!is_f64(rhs) || !same_box(rhs, gp) || (density && (!is_f64(density) || !same_box(density, gp))) ||
+      (border && (!is_f64(border) || !same_box(border, gp))))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_pressure_rhs: rhs, density and border must be FP64 pressure boxes");
+  if (!(tau != 0)) return xf_fail(ctx, XF_ERR_ARG, "xf_pressure_rhs: tau must be nonzero");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((st = clear_checks(ctx))) return st;
+  k_pressure_rhs<<<grid_blocks(ctx, gp->ncell, 256), 256, 0, ctx->stream>>>(
+      gp->code, gp->n1, gp->n2, gp->n3, (const double*)u->data, (const double*)v->data, (const double*)w->data,
+      u->g->hx, v->g->hy, w->g->hz, density ? (const double*)density->data : nullptr, tau,
+      border ? (const double*)border->data : nullptr, (double*)rhs->data, ctx->scratch);
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int kinds[] = {E_RANGE, E_NOTIMPL_P, E_UNKNOWN};
+  const int bad = first_error(chk, kinds, 3, &cell);
+  if (bad >= 0) return fail_at(ctx, gp, bad, cell, "xf_pressure_rhs");
+  return XF_OK;
+}
+
+extern "C" int xf_velocity_correct(int axis, const xf_vec* vel_prev, const xf_vec* p, const xf_vec* density, double tau,
+                                   const xf_vec* border, xf_vec* vel) {
+  if (!vel_prev || !p || !vel) return XF_ERR_ARG;
+  xf_ctx* ctx = vel->g->ctx;
+  const xf_grid* gv = vel->g;
+  const xf_grid* gp = p->g;
+  if (axis < 1 || axis > 3) return xf_fail(ctx, XF_ERR_ARG, "xf_velocity_correct: axis must be 1, 2 or 3");
+  if (!is_f64(vel_prev) || !is_f64(p) || !is_f64(vel) || !same_box(vel_prev, gv) ||
+      (border && (!is_f64(border) || !same_box(border, gv))) ||
+      (density && (!is_f64(density) || !same_box(density, gp))))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_velocity_correct: FP64 boxes of matching shapes expected");
+  if (gp->n1 != gv->n1 + (axis == 1) || gp->n2 != gv->n2 + (axis == 2) || gp->n3 != gv->n3 + (axis == 3))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_velocity_correct: the pressure box must have one more layer along axis %d",
+                   axis);
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  int st;
+  if ((st = clear_checks(ctx))) return st;
+  const double* hP = axis == 1 ? gp->hx : axis == 2 ? gp->hy : gp->hz;
+  const int bl = grid_blocks(ctx, gv->ncell, 256);
+  const double* bd = border ? (const double*)border->data : nullptr;
+  k_vel_pass1<<<bl, 256, 0, ctx->stream>>>(axis, gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
+                                           (double*)vel->data, (const double*)p->data, hP,
+                                           density ? (const double*)density->data : nullptr, tau, bd, ctx->scratch);
+  k_vel_pass2<<<bl, 256, 0, ctx->stream>>>(gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
+                                           (double*)vel->data, bd, ctx->scratch);
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int pass1[] = {E_DEFINED, E_NOTIMPL_V, E_UNKNOWN};
+  const int pass2[] = {E_PREDEF_NONE, E_PREDEF_MANY, E_PREDEF_VALUE};
+  int bad = first_error(chk, pass1, 3, &cell);
+  if (bad < 0) bad = first_error(chk, pass2, 3, &cell);
+  if (bad >= 0) return fail_at(ctx, gv, bad, cell, "xf_velocity_correct");
+  return XF_OK;
+}
+
+extern "C" int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, double* value,
+                                 int32_t* ijk) {
+  if (!gp || !value) return XF_ERR_ARG;
+  xf_ctx* ctx = gp->ctx;
+  int st;
+  if ((st = check_staggered(ctx, gp, u, v, w, "xf_divergence_max"))) return st;
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((st = clear_checks(ctx))) return st;
+  const int bl = red_blocks(ctx, gp->ncell);
+  k_div_max<<<bl, RED_THREADS, 0, ctx->stream>>>(gp->code, gp->n1, gp->n2, gp->n3, (const double*)u->data,
+                                                 (const double*)v->data, (const double*)w->data, u->g->hx, v->g->hy,
+                                                 w->g->hz, ctx->scratch, SL_STEP);
+  XF_CUDA(ctx, cudaGetLastError());
+  XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->scalars[SL_STEP], 2 * sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const double val = ctx->host_scalars[0];
+  const long long c = (long long)ctx->host_scalars[1];
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int kinds[] = {E_RANGE};
+  const int bad = first_error(chk, kinds, 1, &cell);
+  if (bad >= 0) return fail_at(ctx, gp, bad, cell, "xf_divergence_max");
+  *value = val;
+  if (ijk) {
+    if (c < 0) {
+      ijk[0] = ijk[1] = ijk[2] = -1;
+    } else {
+      ijk[0] = (int32_t)(c / gp->s1);
+      ijk[1] = (int32_t)((c - ijk[0] * gp->s1) / gp->s2);
+      ijk[2] = (int32_t)(c % gp->s2);
+    }
+  }
+  return XF_OK;
+}
