@@ -47,8 +47,9 @@ enum {
 
 enum { XF_F64 = 0, XF_F32 = 1 };
 
-/* Operators (XOperator.h:292-319, 410-423). */
-enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1 };
+/* Operators (XOperator.h:292-319, 410-423; XF_OP_PACK: T1dPackOperator,
+ * XOperator.h:320-378, made by xf_pack_create). */
+enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1, XF_OP_PACK = 2 };
 
 /* xf_matvec flags */
 enum {
@@ -115,6 +116,27 @@ int xf_op_destroy(xf_op* op);
  * copies the density box (host pointer, n1*n2*n3 doubles). */
 int xf_op_set_density(xf_op* op, const double* host_density_box);
 
+/* Packed operator: replaces T1dPackOperator(model, A, &null) (XOperator.cpp:
+ * 1135-1350) built from A (Laplace or variable-density, density set).  Rows
+ * and columns are the Rn indices of A's grid; row i holds the nonzero A[i][c]
+ * for c over the cell and its space neighbours at i-1, i+1, j-1, j+1, k-1, k+1
+ * (the activity table, XOperator.cpp:837-936), in that order; the transposed
+ * storage likewise per column.  Values are A's own FP64 arithmetic, bit for
+ * bit.  The result is an xf_op of kind XF_OP_PACK over the same grid: xf_matvec
+ * applies the row dot in storage order (XOperator.cpp:1550-1571, FP64 only),
+ * xf_solve accepts it with every FP64 method, and XF_BICG requires it.  A zero
+ * row or column returns XF_ERR_MASK (the reference throws, :1233, :1316). */
+int xf_pack_create(xf_op* a, xf_op** out);
+/* T1dPackOperator::operator~ (XOperator.h:330): switch between A and A^T.
+ * Other operators return XF_ERR_UNSUPPORTED (the reference throws,
+ * XOperator.h:302). */
+int xf_op_transpose(xf_op* op);
+/* Rows (= EndIndex) and nonzeros of the row and column storages. */
+int xf_pack_size(const xf_op* pack, int64_t* rows, int64_t* nnz, int64_t* nnz_t);
+/* The row (transpose = 0) or column (1) storage as 0-based CSR over Rn: ptr
+ * rows+1 entries, cols/vals nnz entries.  Host pointers. */
+int xf_pack_download(const xf_op* pack, int transpose, int32_t* ptr, int32_t* cols, double* vals);
+
 /* y |= A(x) + sign*s  (sign 0, +1, -1; s may be NULL for sign 0), on active
  * cells: TRnRelease3dSpace::LocalReleaseAssignSpeedLinearCombination(op)
  * (XSpace.cpp:3013-3217).  Inactive cells of y are left as they are, or set
@@ -143,7 +165,8 @@ enum {
   XF_CG_REFERENCE = 1,   /* TSLAE::SolveByConjugateGradients, XSLAE.cpp:56-157     */
   XF_BICGSTAB = 2,       /* TSLAE::SolveByBiConjugateGradientsStab, :667-768       */
   XF_MINRES = 3,         /* TSLAE::SolveByMinimalResiduals, :350-414               */
-  XF_BICG = 4,           /* TSLAE::SolveByBiConjugateGradients, :159-348           */
+  XF_BICG = 4,           /* TSLAE::SolveByBiConjugateGradients, :159-348 (packed   */
+                         /* operators only: it needs A^T)                        */
   XF_FCG = 5             /* flexible CG with a preconditioner                      */
 };
 enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };

@@ -35,6 +35,10 @@ def lib():
         L.xfo_norm.restype = C.c_double
         L.xfo_absmax.restype = C.c_double
         L.xfo_divergence_max.restype = C.c_double
+        L.xfo_pack_build.restype = C.c_int64
+        L.xfo_pack_apply.argtypes = [C.c_int64] + [C.c_void_p] * 5
+        L.xfo_bicg_reference.argtypes = [C.c_int64] + [C.c_void_p] * 7 + [C.c_double, C.c_int, C.c_void_p,
+                                                                          C.c_void_p]
         _lib = L
     return _lib
 
@@ -237,3 +241,42 @@ def divergence_max(codes, u, v, w, hxU, hyV, hzW):
                                    _p(f64(v), C.c_double), _p(f64(w), C.c_double), _p(f64(hxU), C.c_double),
                                    _p(f64(hyV), C.c_double), _p(f64(hzW), C.c_double), _p(ijk, C.c_int32))
     return val, tuple(int(t) for t in ijk)
+
+
+# T1dPackOperator and the reference BiCG (XOperator.cpp:1135-1571, XSLAE.cpp:159-348)
+class Pack:
+    def __init__(self, a_ptr, a_cols, a_vals, t_ptr, t_cols, t_vals):
+        self.a = (np.ascontiguousarray(a_ptr, np.int32), np.ascontiguousarray(a_cols, np.int32), f64(a_vals))
+        self.t = (np.ascontiguousarray(t_ptr, np.int32), np.ascontiguousarray(t_cols, np.int32), f64(t_vals))
+        self.rows = len(self.a[0]) - 1
+
+
+def pack_build(op, g):
+    R = int(g.smask.sum())
+    a_ptr, t_ptr = np.zeros(R + 1, np.int32), np.zeros(R + 1, np.int32)
+    a_cols, t_cols = np.zeros(7 * R, np.int32), np.zeros(7 * R, np.int32)
+    a_vals, t_vals = np.zeros(7 * R), np.zeros(7 * R)
+    nnz = lib().xfo_pack_build(op, *g.args(), _p(a_ptr, C.c_int32), _p(a_cols, C.c_int32),
+                               _p(a_vals, C.c_double), _p(t_ptr, C.c_int32), _p(t_cols, C.c_int32),
+                               _p(t_vals, C.c_double))
+    if nnz < 0:
+        raise ValueError("the operator rejects this grid")
+    return Pack(a_ptr, a_cols[:nnz], a_vals[:nnz], t_ptr, t_cols[:nnz], t_vals[:nnz])
+
+
+def pack_apply(pk, x, transpose=False):
+    ptr, cols, vals = pk.t if transpose else pk.a
+    y = np.zeros(pk.rows)
+    lib().xfo_pack_apply(pk.rows, _p(ptr, C.c_int32), _p(cols, C.c_int32), _p(vals, C.c_double),
+                         _p(f64(x), C.c_double), _p(y, C.c_double))
+    return y
+
+
+def bicg_reference(pk, b, eps=0.0, maxit=0):
+    out = np.zeros(pk.rows)
+    st = Stats()
+    rc = lib().xfo_bicg_reference(pk.rows, *[_p(a, C.c_int32 if a.dtype == np.int32 else C.c_double)
+                                             for a in pk.a + pk.t],
+                                  _p(f64(b), C.c_double), C.c_double(eps), int(maxit), _p(out, C.c_double),
+                                  C.byref(st))
+    return out, st, rc

@@ -5,7 +5,7 @@
 // reference itself rather than from a restatement.
 //
 // Usage: ref_driver <task> <input.bin> <output.bin>
-//   task = matvec | solve | thomas | ib | poisson
+//   task = matvec | solve | thomas | ib | pack
 //
 // File format (both directions): a sequence of records
 //   char name[32]; char kind ('d' double / 'i' int32); int64 count; data[count]
@@ -229,6 +229,75 @@ static void task_solve(Bag& b, Writer& w) {
 }
 
 // ---------------------------------------------------------------------------
+// a8/a9/a2: T1dPackOperator built from the Laplace operator exactly as
+// XProblem.cpp:700-760 does (Rn space model of all-Actual points, NULL
+// transform vector), its row and column storages, A x and A^T x on a seeded x,
+// and TSLAE::SolveByBiConjugateGradients on the packed system.
+class PackProbe : public T1dPackOperator {
+ public:
+  PackProbe(int model, const TRnLinearOperator& A, double** v)
+      : TRnLinearOperator(model), T1dPackOperator(model, A, v) {}  // virtual base first
+  void dump(Writer& w, bool transpose) {
+    int n = transpose ? fRowsCountT : fRowsCount;
+    int* cnt = transpose ? fRowsElementsCountT : fRowsElementsCount;
+    double** m = transpose ? fMatrixPackT : fMatrixPack;
+    int** c = transpose ? fColumnsT : fColumns;
+    std::vector<int> ptr(1, 0), cols;
+    std::vector<double> vals;
+    for (int r = 0; r < n; r++) {
+      for (int q = 0; q < cnt[r]; q++) { cols.push_back(c[r][q]); vals.push_back(m[r][q]); }
+      ptr.push_back((int)cols.size());
+    }
+    w.i(transpose ? "t_ptr" : "a_ptr", ptr);
+    w.i(transpose ? "t_cols" : "a_cols", cols);
+    w.d(transpose ? "t_vals" : "a_vals", vals);
+  }
+};
+
+static void task_pack(Bag& b, Writer& w) {
+  Setup s = build(b, 31);
+  TNodesGrid** grids = new TNodesGrid*[1]; grids[0] = s.grid;
+  T3dLaplaceOperator& A = *(new T3dLaplaceOperator(s.model, 1, grids));
+  TRnRelease3dSpace& probe = vec_from(s, D(b, "x"));
+  int RN = probe.EndIndex;
+  T1dNumberMask& maskRn = *(new T1dNumberMask(RN));
+  for (int rn = 0; rn < RN; rn++) maskRn[rn] = TActualPoint;
+  TMask** masksRn = new TMask*[1];
+  masksRn[0] = &maskRn;
+  TRnRelease1dSpaceModel& modelRn = *(new TRnRelease1dSpaceModel(1, masksRn));
+  const int nameRn = 777;
+  TRnSpace::AddModel(nameRn, &modelRn, false);
+  double* nullVector = NULL;
+  PackProbe& P = *(new PackProbe(nameRn, A, &nullVector));
+  P.dump(w, false);
+  P.dump(w, true);
+  TRnRelease1dSpace& x = *(new TRnRelease1dSpace(nameRn));
+  TRnRelease1dSpace& y = *(new TRnRelease1dSpace(nameRn));
+  const std::vector<double>& xr = D(b, "x_rn");
+  for (int rn = 0; rn < RN; rn++) x[rn] = xr[rn];
+  y |= ((TRnLinearOperator&)P)(x);
+  std::vector<double> out(RN);
+  for (int rn = 0; rn < RN; rn++) out[rn] = y[rn];
+  w.d("ax", out);
+  ~P;
+  y |= ((TRnLinearOperator&)P)(x);
+  for (int rn = 0; rn < RN; rn++) out[rn] = y[rn];
+  w.d("atx", out);
+  ~P;
+  if (b.count("b_rn")) {
+    TRnRelease1dSpace& rhs = *(new TRnRelease1dSpace(nameRn));
+    TRnRelease1dSpace& x0 = *(new TRnRelease1dSpace(nameRn));
+    const std::vector<double>& br = D(b, "b_rn");
+    for (int rn = 0; rn < RN; rn++) { rhs[rn] = br[rn]; x0[rn] = 0; }
+    TSLAE* slae = new TSLAE(P, x0, rhs);
+    slae->SolveByBiConjugateGradients();
+    TRnRelease1dSpace& res = dynamic_cast<TRnRelease1dSpace&>(const_cast<TRnSpace&>((const TRnSpace&)slae->Result));
+    for (int rn = 0; rn < RN; rn++) out[rn] = res[rn];
+    w.d("bicg_x", out);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // a5: TSLAE::SolveByScalarRunning on a batch of lines.
 static void task_thomas(Bag& b, Writer& w) {
   int nl = I(b, "nlines")[0], M = I(b, "M")[0];
@@ -338,6 +407,7 @@ int main(int argc, char** argv) {
     else if (t == "solve") task_solve(b, w);
     else if (t == "thomas") task_thomas(b, w);
     else if (t == "ib") task_ib(b, w);
+    else if (t == "pack") task_pack(b, w);
     else { fprintf(stderr, "unknown task\n"); return 2; }
   } catch (const char* e) {
     fprintf(stderr, "reference threw: %s\n", e); return 3;

@@ -792,3 +792,156 @@ double xfo_divergence_max(const int32_t* codes, int n1, int n2, int n3, const do
       }
   return divMaxValue;
 }
+
+/* ------------------------------------------------------------------------ */
+/* T1dPackOperator (XOperator.cpp:1135-1350) over the Rn space of the
+ * operator's grid.  Column j of A is A(e_j) evaluated by the operator itself
+ * (xfo_apply), read on the rows of j's activity-table entry (the cell, then
+ * its space neighbours at i-1, i+1, j-1, j+1, k-1, k+1:
+ * T3dLaplaceOperator::ConstructActivityTables, XOperator.cpp:837-936) and kept
+ * where nonzero; that is the transposed storage.  Row i of the original
+ * storage looks its entries up in the columns of i's activity-table entry, in
+ * that order (:1290-1322).  ptr has R+1 entries, cols/vals up to 7R; returns
+ * nnz, or -1 on a grid the operator rejects. */
+static int pack_pattern(const uint8_t* sm, const int32_t* inv, int n1, int n2, int n3, int i, int j, int k,
+                        int32_t* out) {
+  const int di[7] = {0, -1, 1, 0, 0, 0, 0}, dj[7] = {0, 0, 0, -1, 1, 0, 0}, dk[7] = {0, 0, 0, 0, 0, -1, 1};
+  int cnt = 0;
+  for (int s = 0; s < 7; s++) {
+    int a = i + di[s], b = j + dj[s], c = k + dk[s];
+    if (a < 0 || a >= n1 || b < 0 || b >= n2 || c < 0 || c >= n3) continue;
+    int64_t q = ((int64_t)a * n2 + b) * n3 + c;
+    if (sm[q]) out[cnt++] = inv[q] - 1;
+  }
+  return cnt;
+}
+
+int64_t xfo_pack_build(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                       const double* hz, const double* density, int n1, int n2, int n3, int32_t* a_ptr,
+                       int32_t* a_cols, double* a_vals, int32_t* t_ptr, int32_t* t_cols, double* t_vals) {
+  const int64_t n = (int64_t)n1 * n2 * n3;
+  uint8_t* sm = (uint8_t*)malloc((size_t)n);
+  xfo_space_mask(codes, n, sm);
+  int32_t* inv = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+  int32_t* fwd = (int32_t*)malloc((size_t)n * 3 * sizeof(int32_t));
+  const int64_t R = xfo_rn_map(sm, n1, n2, n3, inv, fwd);
+  double* e = (double*)calloc((size_t)n, sizeof(double));
+  double* y = (double*)calloc((size_t)n, sizeof(double));
+  int32_t pat[7];
+  int64_t nnz = 0;
+  t_ptr[0] = 0;
+  for (int64_t col = 0; col < R; col++) {
+    const int i = fwd[3 * col], j = fwd[3 * col + 1], k = fwd[3 * col + 2];
+    const int64_t c = ((int64_t)i * n2 + j) * n3 + k;
+    e[c] = 1;
+    if (xfo_apply(op, codes, normals, hx, hy, hz, density, n1, n2, n3, e, NULL, 0, y) != XFO_OK) {
+      nnz = -1;
+      break;
+    }
+    e[c] = 0;
+    const int cnt = pack_pattern(sm, inv, n1, n2, n3, i, j, k, pat);
+    for (int s = 0; s < cnt; s++) {
+      const int row = pat[s];
+      const int64_t rc = ((int64_t)fwd[3 * row] * n2 + fwd[3 * row + 1]) * n3 + fwd[3 * row + 2];
+      if (y[rc] != 0) {
+        t_cols[nnz] = row;
+        t_vals[nnz] = y[rc];
+        nnz++;
+      }
+    }
+    t_ptr[col + 1] = (int32_t)nnz;
+  }
+  if (nnz >= 0) {
+    int64_t m = 0;
+    a_ptr[0] = 0;
+    for (int64_t row = 0; row < R; row++) {
+      const int cnt = pack_pattern(sm, inv, n1, n2, n3, fwd[3 * row], fwd[3 * row + 1], fwd[3 * row + 2], pat);
+      for (int s = 0; s < cnt; s++) {
+        const int col = pat[s];
+        double value = 0;
+        for (int q = t_ptr[col]; q < t_ptr[col + 1]; q++)
+          if (t_cols[q] == row) { value = t_vals[q]; break; }
+        if (value != 0) {
+          a_cols[m] = col;
+          a_vals[m] = value;
+          m++;
+        }
+      }
+      a_ptr[row + 1] = (int32_t)m;
+    }
+  }
+  free(sm); free(inv); free(fwd); free(e); free(y);
+  return nnz;
+}
+
+/* T1dPackOperator::operator() (XOperator.cpp:1550-1571): the row dot in
+ * storage order. */
+void xfo_pack_apply(int64_t R, const int32_t* ptr, const int32_t* cols, const double* vals, const double* x,
+                    double* y) {
+  for (int64_t r = 0; r < R; r++) {
+    double res = 0;
+    for (int q = ptr[r]; q < ptr[r + 1]; q++) res = res + (vals[q]) * (x[cols[q]]);
+    y[r] = res;
+  }
+}
+
+static double dot1(const double* a, const double* b, int64_t R) {
+  double res = 0;
+  for (int64_t i = 0; i < R; i++) res = res + a[i] * b[i];
+  return res;
+}
+
+/* TSLAE::SolveByBiConjugateGradients (XSLAE.cpp:159-348) on a packed system:
+ * x starts at 0 whatever x0 holds (:171); stop when ||r||_2 <= eps (1e-8 when
+ * eps <= 0, :166); a zero beta numerator or denominator is the reference's
+ * throw (XFO_ERR_CHECK here, :274-275). */
+int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, const double* a_vals,
+                       const int32_t* t_ptr, const int32_t* t_cols, const double* t_vals, const double* b, double eps,
+                       int maxit, double* result, xfo_stats* st) {
+  if (eps <= 0) eps = 1e-8;
+  double *xk = zeros(R), *xk_new = zeros(R), *rk = zeros(R), *rt = zeros(R), *rk_new = zeros(R);
+  double *rt_new = zeros(R), *pk = zeros(R), *pt = zeros(R), *pk_new = zeros(R), *pt_new = zeros(R);
+  double* Ap = zeros(R);
+  int status = XFO_OK;
+  xfo_pack_apply(R, a_ptr, a_cols, a_vals, xk, rk);
+  for (int64_t i = 0; i < R; i++) rk[i] = rk[i] - b[i];        /* rk |= A(xk) - b */
+  for (int64_t i = 0; i < R; i++) rt[i] = (-1) * rk[i];        /* rt |= (-1)*rk   */
+  for (int64_t i = 0; i < R; i++) rk[i] = rt[i];
+  memcpy(pk, rk, (size_t)R * 8);
+  memcpy(pt, rt, (size_t)R * 8);
+  double rkXrk = dot1(rk, rk, R);
+  double epsCur = sqrt(rkXrk);
+  int it = 0;
+  st->status = 0;
+  while (epsCur > eps) {
+    if (maxit > 0 && it >= maxit) { st->status = 13; break; }
+    ++it;
+    double alpha1 = dot1(rk, rt, R);
+    xfo_pack_apply(R, a_ptr, a_cols, a_vals, pk, Ap);
+    double alpha2 = dot1(Ap, pt, R);
+    double alpha = alpha1 / alpha2;
+    for (int64_t i = 0; i < R; i++) xk_new[i] = xk[i] + alpha * pk[i];
+    for (int64_t i = 0; i < R; i++) rk_new[i] = (-alpha) * Ap[i] + rk[i];
+    xfo_pack_apply(R, t_ptr, t_cols, t_vals, pt, rt_new);
+    for (int64_t i = 0; i < R; i++) rt_new[i] = (-alpha) * rt_new[i] + rt[i];
+    double beta1 = dot1(rk_new, rt_new, R);
+    double beta2 = dot1(rk, rt, R);
+    if (beta1 == 0 || beta2 == 0) { status = XFO_ERR_CHECK; break; }
+    double beta = beta1 / beta2;
+    for (int64_t i = 0; i < R; i++) pk_new[i] = rk_new[i] + beta * pk[i];
+    for (int64_t i = 0; i < R; i++) pt_new[i] = rt_new[i] + beta * pt[i];
+    memcpy(xk, xk_new, (size_t)R * 8);
+    memcpy(rk, rk_new, (size_t)R * 8);
+    memcpy(rt, rt_new, (size_t)R * 8);
+    memcpy(pk, pk_new, (size_t)R * 8);
+    memcpy(pt, pt_new, (size_t)R * 8);
+    rkXrk = dot1(rk, rk, R);
+    epsCur = sqrt(rkXrk);
+  }
+  memcpy(result, xk, (size_t)R * 8);
+  st->iterations = it;
+  st->resid = epsCur;
+  free(xk); free(xk_new); free(rk); free(rt); free(rk_new); free(rt_new); free(pk); free(pt); free(pk_new);
+  free(pt_new); free(Ap);
+  return status;
+}

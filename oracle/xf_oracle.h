@@ -92,6 +92,18 @@ int xfo_velocity_correct(int axis, const int32_t* codes, int b1, int b2, int b3,
 double xfo_divergence_max(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
                           const double* w, const double* hxU, const double* hyV, const double* hzW, int32_t* ijk);
 
+/* T1dPackOperator (XOperator.cpp:1135-1350): original (a_*) and transposed
+ * (t_*) storages over Rn (0-based rows/cols); arrays of R+1 / 7R entries.
+ * Returns nnz or -1. */
+int64_t xfo_pack_build(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                       const double* hz, const double* density, int n1, int n2, int n3, int32_t* a_ptr,
+                       int32_t* a_cols, double* a_vals, int32_t* t_ptr, int32_t* t_cols, double* t_vals);
+void xfo_pack_apply(int64_t R, const int32_t* ptr, const int32_t* cols, const double* vals, const double* x,
+                    double* y);
+int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, const double* a_vals,
+                       const int32_t* t_ptr, const int32_t* t_cols, const double* t_vals, const double* b, double eps,
+                       int maxit, double* result, xfo_stats* st);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,7 +6,7 @@ it seeded inputs and stores inputs + outputs as .npz files here.  Needs the
 reference tree (REF, default /root/reference); the fixtures it writes are what
 the tests read, so the tests themselves never need the reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [pack]
 """
 import os
 import subprocess
@@ -107,6 +107,41 @@ def solve_case(name, codes, nrm, nodes, op, method, b, x0, rho=None):
         save["ref_" + k] = v
     np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **save)
     print(f"solve_{name}: resid_l2={out['resid_l2'][0]:.3e} resid_inf={out['resid_inf'][0]:.3e}")
+
+
+def pack_case(name, codes, nrm, nodes, seed, bicg):
+    """T1dPackOperator from the Laplace operator: both storages, A x, A^T x and,
+    when `bicg`, TSLAE::SolveByBiConjugateGradients on the packed system."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sm = wl.space_mask(codes).astype(bool)
+    R = int(sm.sum())
+    rec = grid_rec(codes, nrm, nodes)
+    rec["x"] = np.zeros(codes.size)
+    x_rn = rng.standard_normal(R)
+    rec["x_rn"] = x_rn
+    b_rn = rng.standard_normal(R)
+    if bicg:
+        rec["b_rn"] = b_rn
+    out, err = run("pack", rec)
+    if out is None:
+        raise RuntimeError(f"{name}: {err}")
+    save = dict(codes=codes, normals=nrm, x_nodes=nodes[0], y_nodes=nodes[1], z_nodes=nodes[2], x_rn=x_rn)
+    if bicg:
+        save["b_rn"] = b_rn
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, f"pack_{name}.npz"), **save)
+    print(f"pack_{name}: rows={R} nnz={len(out['a_vals'])}" + (" bicg ok" if bicg else ""))
+
+
+def pack_fixtures():
+    rng = np.random.Generator(np.random.PCG64(4040))
+    codes, nrm = wl.mixed_grid(12, 11, 10, seed=41)
+    nodes = [wl.random_nodes(n, rng) for n in codes.shape]
+    pack_case("mixed", codes, nrm, nodes, 42, bicg=False)
+    codes, nrm = wl.poisson_cube(9, 8, 10)
+    nodes = [wl.random_nodes(n, rng) for n in codes.shape]
+    pack_case("cube", codes, nrm, nodes, 43, bicg=True)
 
 
 def main():
@@ -236,4 +271,9 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # `make_golden.py pack` regenerates only the pack-operator fixtures
+    if sys.argv[1:] == ["pack"]:
+        pack_fixtures()
+    else:
+        main()
+        pack_fixtures()

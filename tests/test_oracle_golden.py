@@ -144,3 +144,23 @@ def test_immersed_boundary_steps(axis):
     np.testing.assert_array_equal(F, f["ref_node_force"])
     box = O.ib_spread(f["codes"].shape, h0, axis, pos2, F)
     np.testing.assert_array_equal(box.ravel(), f["ref_force_box"])
+
+
+@pytest.mark.parametrize("name", golden_names("pack_"))
+def test_pack_operator_and_bicg(name):
+    """T1dPackOperator storages, A x / A^T x and the reference BiCG (the
+    reference's own outputs) against the oracle's restatement: bit-exact."""
+    f = golden(name)
+    hx, hy, hz = seps(f)
+    g = O.Grid(f["codes"], f["normals"], hx, hy, hz)
+    pk = O.pack_build(O.LAPLACE, g)
+    for side, key in ((pk.a, "a"), (pk.t, "t")):
+        np.testing.assert_array_equal(side[0], f[f"ref_{key}_ptr"])
+        np.testing.assert_array_equal(side[1], f[f"ref_{key}_cols"])
+        np.testing.assert_array_equal(side[2], f[f"ref_{key}_vals"])
+    np.testing.assert_array_equal(O.pack_apply(pk, f["x_rn"]), f["ref_ax"])
+    np.testing.assert_array_equal(O.pack_apply(pk, f["x_rn"], transpose=True), f["ref_atx"])
+    if "b_rn" in f:
+        x, st, rc = O.bicg_reference(pk, f["b_rn"])
+        assert rc == 0 and st.status == 0
+        np.testing.assert_array_equal(x, f["ref_bicg_x"])

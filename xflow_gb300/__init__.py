@@ -13,7 +13,7 @@ import weakref
 import numpy as np
 
 from . import capi
-from .capi import (XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE,  # noqa: F401
+from .capi import (XF_BICG, XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE,  # noqa: F401
                    XF_IB_POS, XF_IB_VEL, XF_MINRES, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED,
                    XF_ZERO_INACTIVE, XFError)
 
@@ -223,6 +223,35 @@ class Operator(_Owned):
             self.close()
         except Exception:
             pass
+
+
+class PackedOperator(Operator):
+    """T1dPackOperator (XOperator.cpp:1135-1571) built on the GPU from `op`."""
+
+    def __init__(self, op):
+        self.grid, self.kind = op.grid, capi.XF_OP_PACK
+        h = C.c_void_p()
+        _check(op.grid.ctx.h, capi.lib().xf_pack_create(op.h, C.byref(h)))
+        self.h = h
+        op.grid._adopt(self)
+
+    def transpose(self):
+        """operator~ (XOperator.h:330): apply A^T from now on (again: A)."""
+        _check(self.grid.ctx.h, capi.lib().xf_op_transpose(self.h))
+        return self
+
+    def size(self):
+        r, a, t = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(self.grid.ctx.h, capi.lib().xf_pack_size(self.h, C.byref(r), C.byref(a), C.byref(t)))
+        return r.value, a.value, t.value
+
+    def csr(self, transpose=False):
+        rows, nnz, nnz_t = self.size()
+        m = nnz_t if transpose else nnz
+        ptr, cols, vals = np.zeros(rows + 1, np.int32), np.zeros(m, np.int32), np.zeros(m)
+        _check(self.grid.ctx.h, capi.lib().xf_pack_download(self.h, int(transpose), capi._ptr(ptr), capi._ptr(cols),
+                                                            capi._ptr(vals)))
+        return ptr, cols, vals
 
 
 def solve_opts(method=XF_CG, precision=XF_PREC_FP64, rtol=1e-8, atol=0.0, maxit=100000, replace_every=50,

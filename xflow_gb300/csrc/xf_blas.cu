@@ -189,6 +189,8 @@ extern "C" int xf_dot_op(xf_op* op, const xf_vec* x, const xf_vec* y, double* ou
   if (x->g != op->g) return xf_fail(op->g->ctx, XF_ERR_STATE, "xf_dot_op: vectors of another grid");
   if ((st = xf_op_ready(op))) return st;
   xf_ctx* ctx = op->g->ctx;
+  if (op->kind == XF_OP_PACK && x->dtype != XF_F64)
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_dot_op: packed operators are FP64");
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   void* tmp = nullptr;
   const size_t es = x->dtype == XF_F64 ? 8 : 4;

@@ -80,12 +80,15 @@ struct xf_vec {
   void* data;
 };
 
+struct PackData;   // packed operator storage (xf_pack.cu)
 struct xf_op {
   xf_grid* g;
   int kind;
   double* rho;     // device density box (VARDIV)
   float* rho32;
   int rho_set;
+  PackData* pack = nullptr;   // XF_OP_PACK
+  int transposed = 0;         // XF_OP_PACK: applies A^T (T1dPackOperator::operator~)
 };
 
 // ---------------------------------------------------------------------------

@@ -15,7 +15,7 @@ enum {
   D_RR = 32, D_RR_PREV, D_ALPHA, D_BETA, D_BB, D_THR, D_RTOL2, D_EPS,
   D_TAUK = 40, D_TAUK1, D_ALFAK, D_ALFAK1, D_RK1RK1, D_RKRK, D_EPSCUR, D_C1, D_C2, D_C3,
   D_PN = 52, D_PN1, D_AN, D_BN, D_WN, D_NORM,
-  D_ALFA = 60, D_RR64
+  D_ALFA = 60, D_RR64, D_BCG_A1
 };
 // integer scalars
 // I_PAUSE: the mixed CG's inner recursion has met the tolerance (or the cap)
@@ -29,7 +29,8 @@ enum {
   CTL_CG_INIT, CTL_CG_ALPHA, CTL_CG_BETA, CTL_MIXED_REPL, CTL_CG_BETA_FLIP, CTL_CG_ALPHA_FLIP,
   CTL_RCG_INIT, CTL_RCG_TAU0, CTL_RCG_RES0, CTL_RCG_TAU, CTL_RCG_RES,
   CTL_BCGS_NORM0, CTL_BCGS_PN1, CTL_BCGS_AN, CTL_BCGS_WN, CTL_BCGS_END,
-  CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES
+  CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES,
+  CTL_BICG_INIT, CTL_BICG_ALPHA, CTL_BICG_BETA
 };
 
 template <typename T>
@@ -44,6 +45,8 @@ struct MvReq {
   int slot = SL_A;
   int ctl = CTL_NONE;
   int gate = 0;   // 1: run only while a true-residual replacement is pending
+  int transpose = 0;   // packed operators: apply the other side (A^T when op applies A)
+  int guard = 0;       // packed operators: skip once the solve is done (implied by ctl)
 };
 
 __device__ inline void finish(DevScratch* S, long long status) {
@@ -211,6 +214,31 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       d[D_EPSCUR] = sqrt(v);
       if (isnan(v)) finish(S, XF_NAN);
       else if (d[D_EPSCUR] <= d[D_EPS]) finish(S, XF_OK);
+      else if (I[I_IT] >= I[I_MAXIT]) finish(S, XF_MAXIT);
+      break;
+    }
+    // ---- TSLAE::SolveByBiConjugateGradients (XSLAE.cpp:159-348) -----------
+    case CTL_BICG_INIT: {  // SL_D: (rk, rk)
+      double v = d[SL_D];
+      d[D_EPSCUR] = sqrt(v);
+      I[I_IT] = 0; I[I_DONE] = 0; I[I_STATUS] = XF_OK;
+      if (isnan(v)) finish(S, XF_NAN);
+      else if (!(d[D_EPSCUR] > d[D_EPS])) finish(S, XF_OK);
+      break;
+    }
+    case CTL_BICG_ALPHA: {  // SL_B: alpha1 = (rk, rt); SL_A: alpha2 = (A pk, pt)
+      I[I_IT] += 1;
+      d[D_BCG_A1] = d[SL_B];
+      d[D_ALPHA] = d[SL_B] / d[SL_A];
+      break;
+    }
+    case CTL_BICG_BETA: {  // SL_C: beta1 = (rk', rt'); SL_C+1: (rk', rk')
+      double beta1 = d[SL_C], beta2 = d[D_BCG_A1], rr = d[SL_C + 1];
+      if (beta1 == 0 || beta2 == 0) { finish(S, XF_BREAKDOWN); break; }   // the reference throws (:274-275)
+      d[D_BETA] = beta1 / beta2;
+      d[D_EPSCUR] = sqrt(rr);
+      if (isnan(rr) || isnan(d[D_BETA])) finish(S, XF_NAN);
+      else if (!(d[D_EPSCUR] > d[D_EPS])) finish(S, XF_OK);
       else if (I[I_IT] >= I[I_MAXIT]) finish(S, XF_MAXIT);
       break;
     }

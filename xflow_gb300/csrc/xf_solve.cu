@@ -275,6 +275,67 @@ __global__ void k_mr_x(double* __restrict__ xk, const double* __restrict__ rk, c
     if (m[i]) xk[i] = xk[i] + alfa * rk[i];
 }
 
+// ---- TSLAE::SolveByBiConjugateGradients (XSLAE.cpp:159-348) -------------
+// Start (:169-189): xk = 0 whatever x held, rk = A(0) - b = -b, rt = -rk = b,
+// rk = rt, pk = rk, pt = rt; everything off the active set stays as it is.
+__global__ void k_bicg_init(double* __restrict__ x, double* __restrict__ rk, double* __restrict__ rt,
+                            double* __restrict__ pk, double* __restrict__ pt, const double* __restrict__ b,
+                            const uint8_t* __restrict__ m, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) {
+      const double r = (0.0 - b[i]) * (-1);
+      x[i] = 0;
+      rk[i] = r; rt[i] = r; pk[i] = r; pt[i] = r;
+    }
+}
+
+// :237-251: xk += alpha pk; rk = (-alpha) A pk + rk; rt = (-alpha) A^T pt + rt;
+// then (rk, rt) -> SL_C and (rk, rk) -> SL_C+1 with the beta step.
+__global__ void __launch_bounds__(RED_THREADS) k_bicg_update(double* __restrict__ x, double* __restrict__ rk,
+                                                             double* __restrict__ rt, const double* __restrict__ pk,
+                                                             const double* __restrict__ Ap,
+                                                             const double* __restrict__ Atp,
+                                                             const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  GUARD_DONE(S);
+  const double alpha = S->scalars[D_ALPHA];
+  DotAcc<double> a1, a2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) {
+      x[i] = x[i] + alpha * pk[i];
+      const double r = (-alpha) * Ap[i] + rk[i];
+      const double t = (-alpha) * Atp[i] + rt[i];
+      rk[i] = r;
+      rt[i] = t;
+      a1.add(r, t);
+      a2.add(r, r);
+    }
+  double v[2] = {a1.value(), a2.value()};
+  if (publish_partials<2>(S, SL_C, v, sh, &last)) {
+    double t1 = finish_partials(S, SL_C, sh);
+    double t2 = finish_partials(S, SL_C + 1, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_C] = t1;
+      S->scalars[SL_C + 1] = t2;
+      S->tickets[SL_C] = 0;
+      control_step(S, CTL_BICG_BETA);
+    }
+  }
+}
+
+// :282-291: pk = rk + beta pk; pt = rt + beta pt.
+__global__ void k_bicg_p(double* __restrict__ pk, double* __restrict__ pt, const double* __restrict__ rk,
+                         const double* __restrict__ rt, const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+  GUARD_DONE(S);
+  const double beta = S->scalars[D_BETA];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (m[i]) {
+      pk[i] = rk[i] + beta * pk[i];
+      pt[i] = rt[i] + beta * pt[i];
+    }
+}
+
 __global__ void k_reset_state(DevScratch* S, double rtol2, double eps, long long maxit, long long repevery, long long mixed) {
   for (int q = 0; q < 16; q++) S->iscalars[q] = 0;
   S->iscalars[I_STATUS] = XF_OK;
@@ -646,6 +707,29 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
       c.x = x; c.y = rk; c.s = b; c.sign = -1; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_MR_RES;
       xf_mv64(op, c);
     };
+  } else if (o.method == XF_BICG) {
+    // A^T exists for packed operators only (T3dLaplaceOperator::operator~
+    // throws, XOperator.h:302).
+    if (op->kind != XF_OP_PACK)
+      return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: BiCG needs a packed operator (xf_pack_create) for A^T");
+    if (eps <= 0) eps = 1e-8;   // XSLAE.cpp:166
+    k_reset_state<<<1, 1, 0, ctx->stream>>>(S, 0.0, eps, o.maxit, 1, 0);
+    double *rk = B.get<double>(n), *rt = B.get<double>(n), *pk = B.get<double>(n), *pt = B.get<double>(n);
+    double *Ap = B.get<double>(n), *Atp = B.get<double>(n);
+    if (!rk || !rt || !pk || !pt || !Ap || !Atp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    k_bicg_init<<<eb, 256, 0, ctx->stream>>>(x, rk, rt, pk, pt, b, m, n);
+    k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(rk, rk, m, n, S, SL_D, CTL_BICG_INIT, 0);
+    iter = [=](int) {
+      k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(rk, rt, m, n, S, SL_B, CTL_NONE, 1);
+      MvReq<double> a;
+      a.x = pk; a.y = Ap; a.w = pt; a.slot = SL_A; a.ctl = CTL_BICG_ALPHA;
+      xf_mv64(op, a);
+      MvReq<double> t;
+      t.x = pt; t.y = Atp; t.transpose = 1; t.guard = 1;
+      xf_mv64(op, t);
+      k_bicg_update<<<rb, RED_THREADS, 0, ctx->stream>>>(x, rk, rt, pk, Ap, Atp, m, n, S);
+      k_bicg_p<<<eb, 256, 0, ctx->stream>>>(pk, pt, rk, rt, m, n, S);
+    };
   } else {
     return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: method %d not available", o.method);
   }
@@ -750,8 +834,11 @@ extern "C" int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const x
   memset(stats, 0, sizeof(*stats));
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   XF_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  if (op->kind == XF_OP_PACK && (o.precision != XF_PREC_FP64 || (o.method == XF_CG && o.exact)))
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: packed operators solve in FP64");
   if (o.method == XF_CG) st = solve_cg(op, o, x, b, stats);
-  else if (o.method == XF_CG_REFERENCE || o.method == XF_BICGSTAB || o.method == XF_MINRES) st = solve_reference(op, o, x, b, stats);
+  else if (o.method == XF_CG_REFERENCE || o.method == XF_BICGSTAB || o.method == XF_MINRES || o.method == XF_BICG)
+    st = solve_reference(op, o, x, b, stats);
   else st = xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: method %d not available", o.method);
   if (st) {
     cudaStreamSynchronize(ctx->stream);

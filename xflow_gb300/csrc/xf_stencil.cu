@@ -181,7 +181,14 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   }
 }
 
-void xf_mv64(const xf_op* op, const MvReq<double>& q) { launch_matvec<double>(op, op->rho, q); }
+void xf_pack_mv64(const xf_op* op, const MvReq<double>& q);
+void xf_pack_free(PackData* P);
+
+void xf_mv64(const xf_op* op, const MvReq<double>& q) {
+  if (op->kind == XF_OP_PACK) xf_pack_mv64(op, q);
+  else launch_matvec<double>(op, op->rho, q);
+}
+// (packed operators are FP64 only: the callers refuse FP32 with them)
 void xf_mv32(const xf_op* op, const MvReq<float>& q) { launch_matvec<float>(op, op->rho32, q); }
 
 // Used by the C-ABI helpers: plain apply with an optional dot into slot.
@@ -235,6 +242,7 @@ extern "C" int xf_op_destroy(xf_op* op) {
   cudaStreamSynchronize(op->g->ctx->stream);
   if (op->rho) cudaFree(op->rho);
   if (op->rho32) cudaFree(op->rho32);
+  if (op->pack) xf_pack_free(op->pack);
   delete op;
   return XF_OK;
 }
@@ -281,6 +289,8 @@ extern "C" int xf_matvec(xf_op* op, const xf_vec* x, xf_vec* y, const xf_vec* s,
     return xf_fail(ctx, XF_ERR_STATE, "xf_matvec: mixed dtypes");
   const bool exact = (flags & XF_EXACT) != 0;
   if (exact && x->dtype != XF_F64) return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_matvec: XF_EXACT needs FP64 vectors");
+  if (op->kind == XF_OP_PACK && x->dtype != XF_F64)
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_matvec: packed operators are FP64");
   const xf_vec* w = opt_dot ? (opt_w ? opt_w : x) : nullptr;
   if (w && (st = check_vec(op, w, "xf_matvec w"))) return st;
   if (w && w->dtype != x->dtype) return xf_fail(ctx, XF_ERR_STATE, "xf_matvec: dot partner dtype");
