@@ -321,6 +321,16 @@ class SLAE:
     def SolveByMinimalResiduals(self, **kw):
         return self._run(XF_MINRES, **kw)
 
+    def SolveByBiConjugateGradients(self, **kw):
+        """Needs A packed (PackedOperator): the reference's BiCG applies A^T."""
+        return self._run(XF_BICG, **kw)
+
+    @staticmethod
+    def SolveByScalarRunning(ctx, M, u, a, b, c, f, lines=(1, 1, 0, 0), ms=1):
+        """TSLAE::SolveByScalarRunning for a batch of lines (see thomas_lines)."""
+        nl1, nl2, ls1, ls2 = lines
+        thomas_lines(ctx, M, u, a, b, c, f, nl1, nl2, ls1, ls2, ms)
+
     @property
     def Result(self):
         return self.x
