@@ -275,7 +275,7 @@ def main():
     # compulsory bytes per box cell: pq_fused_f32 reads r, p, kind and writes
     # p', q (17 B); the others as in their kernels' comments
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
-           "pq_fused_f32": 17}
+           "pq_fused_f32": 17, "pq_march_f32": 17}
     if "pq_fused_f32" in kms:   # the solver's path on this grid: 2 kernels per iteration
         per_iter = {"pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
     else:

@@ -291,8 +291,10 @@ int xf_ib_spread(xf_ib* ib, xf_vec* force, const double* h0, int axis);
  * stencil q = A p with (p,q), [1] FP32 x/r update with (r,r), [2] FP32
  * direction update, [3] FP64 true residual r32 = b - A x, [4] FP64 stencil,
  * [5] FP32 stencil with the direction update fused in (p' = r + beta p,
- * q = A p', (p', q)), or -1 where the grid does not take that path.
- * ms_out holds 6 doubles.  Laplace operators only. */
+ * q = A p', (p', q)) as the solver launches it, or -1 where the grid does not
+ * take that path; [6] the same step by the register plane march where [5] is
+ * the shared-memory tiled kernel, else -1.
+ * ms_out holds 7 doubles.  Laplace operators only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
 /* ---- allocation-free inner product --------------------------------------- */

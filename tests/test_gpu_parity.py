@@ -265,27 +265,34 @@ def test_maxit_status(ctx, precision):
     assert st.status == capi.XF_MAXIT and st.iterations == 5
 
 
-def test_fused_direction_update_matches_three_kernel_path(ctx, monkeypatch):
+# box 50: register march; box 66 (P % 8 == 4: a half 8-cell group ends the
+# plane) and box 72 (3 tiles, the last one partial): shared-memory tile
+@pytest.mark.parametrize("n", [48, 64, 70])
+def test_fused_direction_update_matches_three_kernel_path(ctx, monkeypatch, n):
     """The mixed CG's fused iteration (p' = r + beta p inside the stencil, p
-    ping-ponging between two buffers) against the three-kernel iteration on the
-    same system: same iteration count within 2, same solution within the
+    ping-ponging between two buffers), by the tiled kernel where the plane
+    allows it and by the register march, against the three-kernel iteration on
+    the same system: same iteration count within 2, same solution within the
     solve's own accuracy."""
-    codes, nrm, sep, b = spheres_case(48, 8, 21)
+    codes, nrm, sep, b = spheres_case(n, 8, 21)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
     A = xf.Operator(g)
     bv = g.vec(b)
     out = {}
-    for mode in ("1", "0"):
-        monkeypatch.setenv("XF_PQ_FUSE", mode)
+    for fuse, pqt in (("1", "1"), ("1", "0"), ("0", "1")):
+        monkeypatch.setenv("XF_PQ_FUSE", fuse)
+        monkeypatch.setenv("XF_PQT", pqt)
         x = g.vec(np.zeros(g.shape))
         st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=1e-9)
         assert st.status == capi.XF_OK and st.rel_resid <= 1e-9
-        out[mode] = (st, x.download())
-    (s1, x1), (s0, x0) = out["1"], out["0"]
-    assert abs(s1.iterations - s0.iterations) <= 2, (s1.iterations, s0.iterations)
+        out[fuse + pqt] = (st, x.download())
+    s0, x0 = out["01"]
     sm = codes != 0
-    d = (x1 - x1[sm].mean()) - (x0 - x0[sm].mean())
-    assert np.abs(d[sm]).max() <= 1e-6 * np.abs(x0[sm] - x0[sm].mean()).max()
+    for key in ("11", "10"):
+        s1, x1 = out[key]
+        assert abs(s1.iterations - s0.iterations) <= 2, (key, s1.iterations, s0.iterations)
+        d = (x1 - x1[sm].mean()) - (x0 - x0[sm].mean())
+        assert np.abs(d[sm]).max() <= 1e-6 * np.abs(x0[sm] - x0[sm].mean()).max()
 
 
 def test_nan_rhs_reports_nan(ctx):

@@ -412,14 +412,246 @@ __global__ void __launch_bounds__(CGK_THREADS, 3) k_cg_pq2u(PqArgs a, float cx, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same fused step with the plane staged in shared memory.  A block owns a
+// tile of PQT_V * 256 consecutive cells of the flattened (j, k) plane (8 per
+// thread, two 16-byte vectors per field) and marches along i.  Per plane it
+// forms p' = r + beta p once: its own cells in registers (x-neighbours stay in
+// registers across the march) and a halo of n3 + 1 cells on either side, then
+// writes the plane's p' tile to shared memory, from where the j+-1 and k+-1
+// neighbours are read.  The raw r and p of plane i+2 (own cells) and of the
+// halo of plane i+1 are in flight while plane i is computed.  Shared memory is
+// double-buffered: one barrier per plane.
+// Layout of a buffer: [pad | left halo (H) | own tile | right halo (H)], with
+// H = n3 + 1 and the own tile at a 16-byte aligned offset.
+constexpr int PQT_V = 8;
+constexpr int PQT_TILE = CGK_THREADS * PQT_V;
+
+struct PqtArgs {
+  StencilGrid<float> g;
+  const float* r;
+  float* pb0;
+  float* pb1;
+  float* q;
+  DevScratch* S;
+  int chunk, nchunk, tiles;   // work items: nchunk plane chunks x tiles per plane
+  int H, off, stride;         // halo width, own-tile offset, floats per buffer
+};
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__global__ void __launch_bounds__(CGK_THREADS, 2) k_cg_pqt(PqtArgs a, float cx, float cy, float cz) {
+  extern __shared__ float4 smem4[];
+  float* sbuf = reinterpret_cast<float*>(smem4);
+  __shared__ double sh[32];
+  __shared__ bool last;
+  __shared__ float dtab[64];
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  const float beta = (float)S->scalars[D_BETA];
+  const int sel = (int)S->iscalars[I_PBUF];
+  const float* __restrict__ po = sel ? a.pb1 : a.pb0;
+  float* __restrict__ pn = sel ? a.pb0 : a.pb1;
+  const float* __restrict__ r = a.r;
+  float* __restrict__ q = a.q;
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x;
+    dtab[b] = cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
+              cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
+  }
+  const StencilGrid<float>& g = a.g;
+  const int n1 = g.n1, n3 = g.n3;
+  const int P = g.n2 * n3;
+  const int last_plane = n1 - 1;
+  const int H = a.H, OFF = a.off;
+  const int nhalo = 2 * H;                    // halo cells per plane
+  const int items = a.nchunk * a.tiles;
+  DotAcc<float> acc;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int ic = item / a.tiles, tile = item - ic * a.tiles;
+    const int base = tile * PQT_TILE;
+    const int t0 = base + threadIdx.x * PQT_V;   // first own plane cell
+    // P is a multiple of 4: the low four cells are valid or none, and so are the high four
+    const bool own = t0 < P, own_hi = t0 + 4 < P;
+    const int i0 = ic * a.chunk, i1 = min(n1, i0 + a.chunk);
+    auto pl = [&](int i) { return min(max(i, 0), last_plane) * P; };
+    // own raw loads (8 cells: two float4 of r and of p)
+    auto ld_own = [&](int i, float4& r0, float4& r1, float4& p0, float4& p1) {
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      const int c = pl(i) + t0;
+      r0 = own ? ldg4(r + c) : z;
+      p0 = own ? ldg4(po + c) : z;
+      r1 = own_hi ? ldg4(r + c + 4) : z;
+      p1 = own_hi ? ldg4(po + c + 4) : z;
+    };
+    auto dir4 = [&](float4 rr, float4 pp) {
+      return make_float4(fmaf(beta, pp.x, rr.x), fmaf(beta, pp.y, rr.y), fmaf(beta, pp.z, rr.z), fmaf(beta, pp.w, rr.w));
+    };
+    // halo: up to HPT cells per thread, plane positions base-H.. and base+TILE..
+    constexpr int HPT = 4;   // covers 2H <= 4 * 256, i.e. n3 <= 511 (checked on the host)
+    auto halo_pos = [&](int h) { return h < H ? base - H + h : base + PQT_TILE + (h - H); };
+    float hr[HPT], hp[HPT];
+    auto ld_halo = [&](int i) {
+      const int pi = pl(i);
+#pragma unroll
+      for (int u = 0; u < HPT; u++) {
+        const int h = threadIdx.x + u * CGK_THREADS;
+        const int x = halo_pos(h);
+        const bool ok = h < nhalo && x >= 0 && x < P;
+        hr[u] = ok ? __ldg(r + pi + x) : 0.f;
+        hp[u] = ok ? __ldg(po + pi + x) : 0.f;
+      }
+    };
+    float4 xm0, xm1, xc0, xc1, xp0, xp1;
+    float4 r2a, r2b, p2a, p2b;
+    {
+      float4 a0, a1, b0, b1;
+      ld_own(i0 - 1, a0, a1, b0, b1);
+      xm0 = dir4(a0, b0); xm1 = dir4(a1, b1);
+      ld_own(i0, a0, a1, b0, b1);
+      xc0 = dir4(a0, b0); xc1 = dir4(a1, b1);
+      ld_own(i0 + 1, a0, a1, b0, b1);
+      xp0 = dir4(a0, b0); xp1 = dir4(a1, b1);
+      ld_own(i0 + 2, r2a, r2b, p2a, p2b);
+    }
+    ld_halo(i0);
+    auto ld_kind = [&](int i) {
+      const uint32_t* kp = reinterpret_cast<const uint32_t*>(g.kind + pl(i) + t0);
+      return make_uint2(own ? __ldg(kp) : 0u, own_hi ? __ldg(kp + 1) : 0u);
+    };
+    uint2 kc = ld_kind(i0);
+    for (int i = i0; i < i1; i++) {
+      float* buf = sbuf + (i & 1) * a.stride;
+      // p' of plane i into shared memory: own tile and halo
+      *reinterpret_cast<float4*>(buf + OFF + threadIdx.x * PQT_V) = xc0;
+      *reinterpret_cast<float4*>(buf + OFF + threadIdx.x * PQT_V + 4) = xc1;
+#pragma unroll
+      for (int u = 0; u < HPT; u++) {
+        const int h = threadIdx.x + u * CGK_THREADS;
+        if (h < nhalo) buf[h < H ? OFF - H + h : OFF + PQT_TILE + (h - H)] = fmaf(beta, hp[u], hr[u]);
+      }
+      // loads for later planes, in flight during this plane's arithmetic
+      float4 r3a, r3b, p3a, p3b;
+      ld_own(i + 3, r3a, r3b, p3a, p3b);
+      ld_halo(i + 1);
+      const uint2 kn = ld_kind(i + 1);
+      __syncthreads();
+      if (own) {
+        const float* s0 = buf + OFF + threadIdx.x * PQT_V;
+        float c[8] = {xc0.x, xc0.y, xc0.z, xc0.w, xc1.x, xc1.y, xc1.z, xc1.w};
+        const float m[8] = {xm0.x, xm0.y, xm0.z, xm0.w, xm1.x, xm1.y, xm1.z, xm1.w};
+        const float pp[8] = {xp0.x, xp0.y, xp0.z, xp0.w, xp1.x, xp1.y, xp1.z, xp1.w};
+        float jm[8], jp[8];
+#pragma unroll
+        for (int v = 0; v < 8; v += 2) {
+          const float2 a2 = *reinterpret_cast<const float2*>(s0 + v - n3);
+          const float2 b2 = *reinterpret_cast<const float2*>(s0 + v + n3);
+          jm[v] = a2.x; jm[v + 1] = a2.y; jp[v] = b2.x; jp[v + 1] = b2.y;
+        }
+        const float km0 = s0[-1], kp7 = s0[8];
+        const uint32_t kw[2] = {kc.x, kc.y};
+        float out[8];
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+          const uint32_t kb = (kw[v >> 2] >> (8 * (v & 3))) & 0xffu;
+          const float km = v == 0 ? km0 : c[v - 1];
+          const float kp = v == 7 ? kp7 : c[v + 1];
+          float o = fmaf(dtab[kb & 63], c[v], -fmaf(cx, pp[v] + m[v], fmaf(cy, jp[v] + jm[v], cz * (kp + km))));
+          if ((kb >> K_ROW_SHIFT) == ROW_NONE) o = 0.f;
+          out[v] = o;
+          acc.add(c[v], o);
+        }
+        const int cg = i * P + t0;
+        *reinterpret_cast<float4*>(pn + cg) = xc0;
+        *reinterpret_cast<float4*>(q + cg) = make_float4(out[0], out[1], out[2], out[3]);
+        if (own_hi) {
+          *reinterpret_cast<float4*>(pn + cg + 4) = xc1;
+          *reinterpret_cast<float4*>(q + cg + 4) = make_float4(out[4], out[5], out[6], out[7]);
+        }
+      }
+      xm0 = xc0; xm1 = xc1; xc0 = xp0; xc1 = xp1;
+      xp0 = dir4(r2a, p2a); xp1 = dir4(r2b, p2b);
+      r2a = r3a; r2b = r3b; p2a = p3a; p2b = p3b;
+      kc = kn;
+    }
+    __syncthreads();   // the next item rewrites both buffers
+  }
+  if (!publish_acc<float>(S, SL_A, SL_A, acc, sh, &last)) return;
+  double tot = finish_partials(S, SL_A, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[SL_A] = tot;
+    S->tickets[SL_A] = 0;
+    control_step(S, CTL_CG_ALPHA_FLIP);
+  }
+}
+
+// The tiled kernel needs P to be a multiple of 4 (16-byte own vectors in
+// every plane), n3 even (8-byte aligned j+-1 reads from shared memory) and
+// 2 (n3 + 1) <= 4 * 256 halo cells.
+static bool pqt_supported(const xf_grid* g) {
+  const int64_t P = (int64_t)g->n2 * g->n3;
+  return (P % 4) == 0 && (g->n3 % 2) == 0 && 2 * (g->n3 + 1) <= 4 * CGK_THREADS && g->n3 >= 2 && g->n2 >= 2;
+}
+
 bool xf_cg_pq_supported(const xf_grid* g) {
   return g->uniform && g->nbrow == 0 && (g->n3 % 2) == 0 && g->n1 >= 2;
 }
 
-// p' = r + beta p (p in pb[I_PBUF]), q = A p', (p', q), alpha, flip.
-void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
+static void launch_pqt(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
+  PqtArgs a;
+  a.g = make_stencil_grid<float>(g, nullptr);
+  a.r = r; a.pb0 = pb0; a.pb1 = pb1; a.q = q; a.S = ctx->scratch;
+  const int P = g->n2 * g->n3;
+  a.H = g->n3 + 1;
+  a.off = (a.H + 3) & ~3;
+  a.stride = (a.off + PQT_TILE + a.H + 3) & ~3;
+  a.tiles = (P + PQT_TILE - 1) / PQT_TILE;
+  const size_t smem = 2 * (size_t)a.stride * sizeof(float);
+  static int resident = 0;   // blocks per SM at this kernel's launch bounds and shared memory
+  static size_t resident_smem = 0;
+  if (!resident || resident_smem != smem) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_cg_pqt, CGK_THREADS, smem) != cudaSuccess ||
+        resident < 1)
+      resident = 1;
+    resident_smem = smem;
+  }
+  const int64_t B = (int64_t)ctx->sm_count * resident;
+  // plane chunk: the length whose last wave wastes least (cost ~ waves x
+  // (chunk + 2 start-up planes))
+  int best = 8;
+  double best_cost = 1e30;
+  for (int L = 4; L <= 32; L++) {
+    const int64_t items = (int64_t)a.tiles * ((g->n1 + L - 1) / L);
+    const double cost = (double)((items + B - 1) / B) * (L + 2);
+    if (cost < best_cost) { best_cost = cost; best = L; }
+  }
+  a.chunk = best;
+  a.nchunk = (g->n1 + a.chunk - 1) / a.chunk;
+  int64_t blocks = B, items = (int64_t)a.tiles * a.nchunk;
+  if (blocks > items) blocks = items;
+  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  k_cg_pqt<<<(int)blocks, CGK_THREADS, smem, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
+}
+
+// p' = r + beta p (p in pb[I_PBUF]), q = A p', (p', q), alpha, flip: the
+// shared-memory tiled kernel where the plane allows it, else the register
+// march.  variant: 0 automatic, 1 register march, 2 tiled.
+void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
+void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
+  const char* env = getenv("XF_PQT");   // "0": the register march even where the tile fits
+  xf_cg_pq32_variant(op, r, pb0, pb1, q, (env && env[0] == '0') ? 1 : 0);
+}
+bool xf_cg_pqt_supported(const xf_grid* g) { return pqt_supported(g); }
+
+void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant) {
+  const xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  if (variant != 1 && pqt_supported(g)) {
+    launch_pqt(op, r, pb0, pb1, q);
+    return;
+  }
   static int resident = 0;   // blocks per SM at this kernel's launch bounds
   if (!resident) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_cg_pq2u, CGK_THREADS, 0) != cudaSuccess ||

@@ -27,6 +27,8 @@ void xf_cg_q32(const xf_op* op, const float* p, float* q);
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
 bool xf_cg_pq_supported(const xf_grid* g);
 void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q);
+void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
+bool xf_cg_pqt_supported(const xf_grid* g);
 bool xf_cgf_supported(const xf_grid* g);
 int xf_cgf_prepare(xf_ctx* ctx, const xf_grid* g);
 void xf_cgf_iteration(const xf_op* op, float* r, float* e, float* p0, float* p1);
@@ -88,6 +90,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __r
       control_step(S, CTL_CG_BETA);
     }
   }
+}
+
+// One wave of resident blocks for the x/r update (its grid-stride loop then
+// has no partial second wave), capped by the reduction table.
+template <typename T>
+static int xr_blocks(xf_ctx* ctx, int64_t n) {
+  static int per_sm[2] = {0, 0};
+  int& r = per_sm[sizeof(T) == 8];
+  if (!r && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_cg_xr<T>, RED_THREADS, 0) != cudaSuccess || r < 1))
+    r = 1;
+  int64_t b = (int64_t)ctx->sm_count * r;
+  const int64_t need = (n + RED_THREADS - 1) / RED_THREADS;
+  if (b > need) b = need;
+  if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
+  return (int)(b < 1 ? 1 : b);
 }
 
 // p = r + beta p.  `after_replace`: the step that follows a true-residual
@@ -475,6 +492,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   const double* b = (const double*)bv->data;
   Bufs B(ctx);
   const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
+  const int xb32 = xr_blocks<float>(ctx, n), xb64 = xr_blocks<double>(ctx, n);
   int total_it = 0, total_repl = 0;
   HostState hs = {0, 0, 0, 0, 0};
   double rel = 0;
@@ -513,7 +531,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
           m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
           xf_mv64(op, m1);
         }
-        k_cg_xr<double><<<rb, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
+        k_cg_xr<double><<<xb64, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
         k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0);
       };
     } else if (lap && xf_cgf_supported(g) && getenv("XF_FUSED") && getenv("XF_FUSED")[0] == '1') {
@@ -555,7 +573,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       const int last = chunk - 1;
       iter = [=](int c) {
         xf_cg_pq32(op, r, pa, pb, q);
-        k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, pa, q, n, S, pb);
+        k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, r, pa, q, n, S, pb);
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
           xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
@@ -581,7 +599,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
           m1.x = p; m1.y = q; m1.w = p; m1.zero_inactive = 1; m1.slot = SL_A; m1.ctl = CTL_CG_ALPHA;
           xf_mv32(op, m1);
         }
-        k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S);
+        k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S);
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
           if (lap) {
@@ -786,15 +804,17 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     return tot / reps;
   };
   ms_out[0] = time([&] { xf_cg_q32(op, p, q); });
-  ms_out[1] = time([&] { k_cg_xr<float><<<rb, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S); });
+  const int xb32 = xr_blocks<float>(ctx, n);
+  ms_out[1] = time([&] { k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, r, p, q, n, S); });
   ms_out[2] = time([&] { k_cg_p<float><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0); });
   ms_out[3] = time([&] { xf_cg_res64(op, x, b, r, SL_C, CTL_NONE); });
   ms_out[4] = time([&] { xf_cg_q64(op, p64, q64); });
-  ms_out[5] = -1.0;
+  ms_out[5] = ms_out[6] = -1.0;
   if (xf_cg_pq_supported(g)) {
     float* p2 = B.get<float>(n);
     if (!p2) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
     ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
+    if (xf_cg_pqt_supported(g)) ms_out[6] = time([&] { xf_cg_pq32_variant(op, r, p, p2, q, 1); });
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
