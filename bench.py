@@ -196,6 +196,8 @@ def main():
     ap.add_argument("--impl", default="xflow", choices=["xflow", "reference"])
     ap.add_argument("--size", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rows", action="store_true",
+                    help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="a few launches of each hot kernel on the full grid (for ncu captures)")
     args = ap.parse_args()
@@ -203,6 +205,8 @@ def main():
         return reference_arm(args)
     if args.kernels_only:
         return kernels_only(args)
+    if args.rows:
+        return rows(args)
 
     import xflow_gb300 as xf
 
@@ -370,6 +374,116 @@ def kernels_only(args):
         st = xf.solve(A, x, bv, method=xf.XF_CG, precision=prec, rtol=RTOL, maxit=32)
         print(f"precision {prec}: {st.iterations} iterations, {st.ms:.2f} ms, status {st.status}")
     ctx.synchronize()
+    return 0
+
+
+def rows(args):
+    """Time the other rows of the path at their configurations' sizes, each
+    call end to end on the device (CUDA events on the context stream around
+    `reps` calls; the calls that check the reference's throw conditions read a
+    few bytes back inside the timed region):
+      channel 256x64x64 (the immersed-body config): pressure RHS, velocity
+        correction (u), control balance, IB interpolate / forces / spread with
+        an icosphere of 2562 markers, Thomas lines along x;
+      512x128x128 (the full time loop config): pressure RHS, velocity
+        correction, control balance;
+      256^3 spheres Poisson system: packed-operator build and its SpMV.
+    Prints one JSON line per row with ms per call and algorithmic GB/s."""
+    import torch
+
+    import xflow_gb300 as xf
+    from xflow_gb300 import workloads as wl_step
+
+    ctx = xf.Context(0)
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    peak, _ = peaks()
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = []
+
+    def report(row, config, ms, nbytes=None, **extra):
+        d = {"row": row, "config": config, "ms": ms}
+        if nbytes:
+            d.update({"alg_bytes": nbytes, "GB_s": nbytes / (ms * 1e-3) / 1e9, "frac_of_measured_hbm":
+                      nbytes / (ms * 1e-3) / 1e9 / peak})
+        d.update(extra)
+        out.append(d)
+        print(json.dumps(d), flush=True)
+
+    # --- time-step passes at the two channel sizes ---------------------------
+    for (n1, n2, n3), name in (((257, 65, 65), "channel 256x64x64"), ((513, 129, 129), "channel 512x128x128")):
+        cs = wl_step.staggered_channel(n1, n2, n3, seed=7)
+        gp = xf.Grid(ctx, cs["pc"], *cs["hP"])
+        gu, gv, gw = (xf.Grid(ctx, cs[c], *cs[h]) for c, h in (("uc", "hU"), ("vc", "hV"), ("wc", "hW")))
+        u, v, w = gu.vec(cs["u"]), gv.vec(cs["v"]), gw.vec(cs["w"])
+        rho, pb, rhs = gp.vec(cs["density"]), gp.vec(cs["p_border"]), gp.vec(None)
+        p = gp.vec(cs["p"])
+        ub, un = gu.vec(cs["u_border"]), gu.vec(None)
+        npc, nuc = int(np.prod(gp.shape)), int(np.prod(gu.shape))
+        ms = timed(lambda: xf.pressure_rhs(gp, u, v, w, cs["tau"], rhs, density=rho, border=pb))
+        report("a20 pressure RHS (XProblem.cpp:5474-5512)", name, ms, npc * (1 + 8 + 8 + 8 + 8 + 8 + 8))
+        ms = timed(lambda: xf.velocity_correct(1, u, p, cs["tau"], un, density=rho, border=ub))
+        report("velocity correction u (XProblem.cpp:5598-5777)", name, ms, nuc * (1 + 8 + 8 + 8 + 8 + 8))
+        ms = timed(lambda: xf.divergence_max(gp, u, v, w))
+        report("control balance (XProblem.cpp:5782-5829)", name, ms, npc * (1 + 8 + 8 + 8))
+        if n1 == 257:
+            # Thomas lines along x of the u box: (n2 * n3) lines of n1-2 unknowns
+            M, nl1, nl2, ls1, ls2, ms_ = xf.box_lines(gu.shape, 1)
+            rng = np.random.Generator(np.random.PCG64(3))
+            a = gu.vec(rng.uniform(-1, 0, gu.shape))
+            c = gu.vec(rng.uniform(-1, 0, gu.shape))
+            bb = gu.vec(2.5 + rng.uniform(0, 1, gu.shape))
+            f = gu.vec(rng.standard_normal(gu.shape))
+            uu = gu.vec(rng.standard_normal(gu.shape))
+            ms = timed(lambda: xf.thomas_lines(ctx, M, uu, a, bb, c, f, nl1, nl2, ls1, ls2, ms_))
+            report("a5 Thomas lines along x (XSLAE.cpp:416-445)", name + f", {nl1 * nl2} lines of {M + 1}", ms,
+                   nuc * 8 * 6 + nuc * 8 * 2)
+            # IB: icosphere r = 0.15 at (1, .5, .5), subdivision 4 (2562 vertices)
+            from xflow_gb300 import workloads as wl
+
+            verts = wl.icosphere(4) * 0.15 + np.array([1.0, 0.5, 0.5])
+            nn = len(verts)
+            nxt = np.roll(np.arange(nn), -1).astype(np.int32)
+            prv = np.roll(np.arange(nn), 1).astype(np.int32)
+            mk = xf.Markers(ctx, verts, verts, np.full(nn, xf.capi.XF_IB_TARGET, np.int32), nxt, prv,
+                            np.zeros(nn), np.zeros((nn, 3)), np.ones(nn), np.array([1.0, 1.0, 1.0, 1e-4]))
+            h0 = np.array([1 / 64] * 3)
+            ms = timed(lambda: mk.interpolate(u, h0, 1))
+            report("a17 IB interpolate (XProblem.cpp:8620-8791)", name + f", {nn} markers", ms)
+            ms = timed(lambda: mk.compute_forces(1))
+            report("a18 IB forces (XProblem.cpp:8436-8547)", name + f", {nn} markers", ms)
+            ms = timed(lambda: mk.spread(un, h0, 1))
+            report("a19 IB spread (XProblem.cpp:8550-8617)", name + f", {nn} markers", ms)
+        for o in (u, v, w, rho, pb, rhs, p, ub, un):
+            o.close()
+        for gg in (gp, gu, gv, gw):
+            gg.close()
+
+    # --- packed operator at 256^3 ----------------------------------------------
+    codes, sep, b = workload(args.size)
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    A = xf.Operator(g, xf.XF_OP_LAPLACE)
+    t0 = time.perf_counter()
+    P = xf.PackedOperator(A)
+    ctx.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    rows_, nnz, _ = P.size()
+    x, y = g.vec(b), g.vec(None)
+    ms = timed(lambda: P.apply(x, y))
+    ncell = int(np.prod(g.shape))
+    report("a9 packed operator SpMV (XOperator.cpp:1550-1571)", f"256^3 spheres, {rows_} rows, {nnz} nonzeros", ms,
+           ncell * 1 + rows_ * (4 + 8 + 1) + nnz * (8 + 4) + rows_ * 8 * 2, build_ms=build_ms)
     return 0
 
 

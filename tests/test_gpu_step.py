@@ -9,7 +9,7 @@ import pytest
 
 import xflow_gb300 as xf
 from oracle import oracle as O
-from tests import step_cases
+from xflow_gb300 import workloads as wl_step
 from xflow_gb300 import capi
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +32,7 @@ def grids(ctx, cs):
 
 @pytest.mark.parametrize("with_density", [False, True])
 def test_pressure_rhs_matches_oracle(ctx, with_density):
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     gp, gu, gv, gw = grids(ctx, cs)
     dens = cs["density"] if with_density else None
     rhs = gp.vec(np.full(gp.shape, 9.0))
@@ -46,7 +46,7 @@ def test_pressure_rhs_matches_oracle(ctx, with_density):
 
 @pytest.mark.parametrize("axis", [1, 2, 3])
 def test_velocity_correct_matches_oracle(ctx, axis):
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     gp, gu, gv, gw = grids(ctx, cs)
     g, codes, prev = [(gu, cs["uc"], cs["u"]), (gv, cs["vc"], cs["v"]), (gw, cs["wc"], cs["w"])][axis - 1]
     border = cs["u_border"] if axis == 1 else np.zeros(codes.shape)
@@ -60,7 +60,7 @@ def test_velocity_correct_matches_oracle(ctx, axis):
 
 
 def test_divergence_max_matches_oracle(ctx):
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     gp, gu, gv, gw = grids(ctx, cs)
     got, ijk = xf.divergence_max(gp, gu.vec(cs["u"]), gv.vec(cs["v"]), gw.vec(cs["w"]))
     want, wijk = O.divergence_max(cs["pc"], cs["u"], cs["v"], cs["w"], cs["hU"][0], cs["hV"][1], cs["hW"][2])
@@ -71,7 +71,7 @@ def test_divergence_max_matches_oracle(ctx):
 
 
 def test_step_errors_match_reference_throws(ctx):
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     gp, gu, gv, gw = grids(ctx, cs)
     # a Defined inflow value that differs from the border value
     u = cs["u"].copy()

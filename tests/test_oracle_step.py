@@ -6,7 +6,7 @@ evaluates the same FP64 operations in the same order per element."""
 import numpy as np
 
 from oracle import oracle as O
-from tests import step_cases
+from xflow_gb300 import workloads as wl_step
 
 
 def np_rhs(cs, dens, border):
@@ -23,7 +23,7 @@ def np_rhs(cs, dens, border):
 
 
 def test_pressure_rhs_restatements_agree():
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     for dens in (None, cs["density"]):
         got, st, _ = O.pressure_rhs(cs["pc"], cs["u"], cs["v"], cs["w"], cs["hU"][0], cs["hV"][1], cs["hW"][2],
                                     cs["tau"], density=dens, border=cs["p_border"])
@@ -32,7 +32,7 @@ def test_pressure_rhs_restatements_agree():
 
 
 def test_velocity_correct_restatements_agree():
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     uc, u, p, tau, rho, b = cs["uc"], cs["u"], cs["p"], cs["tau"], cs["density"], cs["u_border"]
     got, st, _ = O.velocity_correct(1, uc, u, p, cs["hP"][0], tau, density=rho, border=b)
     assert st == 0
@@ -46,7 +46,7 @@ def test_velocity_correct_restatements_agree():
 
 
 def test_divergence_max_restatements_agree():
-    cs = step_cases.channel()
+    cs = wl_step.staggered_channel()
     u, v, w = cs["u"], cs["v"], cs["w"]
     val, ijk = O.divergence_max(cs["pc"], u, v, w, cs["hU"][0], cs["hV"][1], cs["hW"][2])
     i, j, k = np.nonzero(cs["pc"] == 1)   # C order: np.nonzero walks i -> j -> k

@@ -210,3 +210,101 @@ def divergence_rhs(codes: np.ndarray, sep, seed: int) -> np.ndarray:
     sm = space_mask(codes).astype(bool)
     b[sm] -= b[sm].mean()
     return b
+
+
+# ---------------------------------------------------------------------------
+U_IN = 1.25   # inflow velocity of the staggered channel case
+
+
+def _stag_seps(rng, n):
+    return rng.uniform(0.8, 1.2, n - 1) / (n - 1)
+
+
+def staggered_channel(n1=14, n2=11, n3=12, seed=3):
+    """Staggered channel case for the time-step passes around the pressure
+    solve (TVPProblem::SolveBySplitting, XProblem.cpp:5474-5829).
+
+    Pressure box n1 x n2 x n3 with a Fictive ghost layer, Actual interior, a
+    masked (Fictive) sphere, and PreDefined cells on the outlet face; u box
+    (n1-1) x n2 x n3 with a Defined inflow face (border value U_IN) and a
+    PreDefined outflow face whose values mirror the interior as the
+    reference's check demands; v and w boxes with Fictive ghosts.  Separations
+    are seeded and non-uniform so that every index of hxU/hyV/hzW and
+    hxP/hyP/hzP is exercised."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    hP = [_stag_seps(rng, n) for n in (n1, n2, n3)]
+    ii, jj, kk = np.meshgrid(np.arange(n1), np.arange(n2), np.arange(n3), indexing="ij")
+    sphere = (ii - n1 / 2) ** 2 + (jj - n2 / 2) ** 2 + (kk - n3 / 2) ** 2 < (min(n1, n2, n3) / 5) ** 2
+
+    pc = np.zeros((n1, n2, n3), np.int32)
+    pc[1:-1, 1:-1, 1:-1] = 1
+    pc[-1, 1:-1, 1:-1] = 4            # outlet: PreDefined pressure
+    pc[sphere] = 0
+
+    uc = np.zeros((n1 - 1, n2, n3), np.int32)
+    uc[1:-1, 1:-1, 1:-1] = 1
+    uc[0, 1:-1, 1:-1] = 3             # inflow: Defined
+    uc[-1, 1:-1, 1:-1] = 4            # outflow: PreDefined (one Actual neighbour, i-1)
+    uc[sphere[:-1]] = 0
+    vc = np.zeros((n1, n2 - 1, n3), np.int32)
+    vc[1:-1, 1:-1, 1:-1] = 1
+    vc[sphere[:, :-1]] = 0
+    wc = np.zeros((n1, n2, n3 - 1), np.int32)
+    wc[1:-1, 1:-1, 1:-1] = 1
+    wc[sphere[:, :, :-1]] = 0
+    # a PreDefined u cell next to the sphere could see no Actual neighbour:
+    # keep the outflow face clear of it
+    uc[-1][uc[-2] != 1] = 0
+
+    # separations of the staggered grids: u nodes sit between p nodes along x
+    hU = [np.full(n1 - 2, 0.0), hP[1], hP[2]]
+    hU[0] = 0.5 * (hP[0][:-1] + hP[0][1:])
+    hV = [hP[0], 0.5 * (hP[1][:-1] + hP[1][1:]), hP[2]]
+    hW = [hP[0], hP[1], 0.5 * (hP[2][:-1] + hP[2][1:])]
+
+    u = rng.standard_normal(uc.shape)
+    v = rng.standard_normal(vc.shape)
+    w = rng.standard_normal(wc.shape)
+    u_border = np.zeros(uc.shape)
+    u_border[uc == 3] = U_IN
+    u_border[uc == 4] = rng.uniform(0.5, 1.5, int((uc == 4).sum()))
+    u[uc == 3] = U_IN
+    # PreDefined previous values satisfy |prev - (2 b - prev[i-1])| <= 1e-10
+    face = uc[-1] == 4
+    u[-1][face] = 2 * u_border[-1][face] - u[-2][face]
+    density = rng.uniform(0.5, 2.0, pc.shape)
+    p_border = np.where(pc == 4, rng.standard_normal(pc.shape), 0.0)
+    p = rng.standard_normal(pc.shape)
+    return dict(pc=pc, uc=uc, vc=vc, wc=wc, hP=hP, hU=hU, hV=hV, hW=hW, u=u, v=v, w=w, u_border=u_border,
+                density=density, p_border=p_border, p=p, tau=1e-3)
+
+
+def icosphere(subdiv: int) -> np.ndarray:
+    """Unit icosphere vertices: the icosahedron's 12 vertices, each triangle
+    split in four `subdiv` times with midpoints pushed to the sphere
+    (10 * 4**subdiv + 2 vertices: 2562 at subdivision 4, the immersed-body
+    config's marker set)."""
+    t = (1.0 + 5 ** 0.5) / 2
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(p, float) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts)
