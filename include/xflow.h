@@ -48,8 +48,13 @@ enum {
 enum { XF_F64 = 0, XF_F32 = 1 };
 
 /* Operators (XOperator.h:292-319, 410-423; XF_OP_PACK: T1dPackOperator,
- * XOperator.h:320-378, made by xf_pack_create). */
-enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1, XF_OP_PACK = 2 };
+ * XOperator.h:320-378, made by xf_pack_create; XF_OP_ADVDIFF: the implicit
+ * advection-diffusion operator of the momentum / transport equations, set up
+ * by xf_op_set_advection). */
+enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1, XF_OP_PACK = 2, XF_OP_ADVDIFF = 3 };
+/* xf_op_set_advection flags (THydrodynamicsProblem's flagConvective and
+ * flagDiffusion, XProblem.cpp:1236-1238) */
+enum { XF_ADV_CONVECTIVE = 1, XF_ADV_DIFFUSIVE = 2 };
 
 /* xf_matvec flags */
 enum {
@@ -115,6 +120,26 @@ int xf_op_destroy(xf_op* op);
 /* T3dVariableDivergentedOperator::withDensity (XOperator.cpp:2235-2268):
  * copies the density box (host pointer, n1*n2*n3 doubles). */
 int xf_op_set_density(xf_op* op, const double* host_density_box);
+
+/* Coefficients of an XF_OP_ADVDIFF operator.  Replaces the ADI line systems of
+ * the transfer / momentum equations (THydrodynamicsProblem, XProblem.cpp:
+ * 1236-1238 and the same coefficients at :3199-3218), which the reference
+ * solves direction by direction with TSLAE::SolveByScalarRunning, by one
+ * implicit 7-point operator: the sum over the three directions of the
+ * reference's line coefficients.  On Actual cells, with per direction
+ * h_1 = h[m-1], h = h[m], hx2 = h_1 + h, hxhxh = h_1 h (h_1 + h) / 2 and the
+ * advecting velocity component vd at the cell,
+ *   A_d = conv 0.5 (-vd / hx2) + diff 0.5 (-D h / hxhxh)      (f[m-1])
+ *   B_d = diff 0.5 D hx2 / hxhxh                              (f[m])
+ *   C_d = conv 0.5 (vd / hx2) + diff 0.5 (-D h_1 / hxhxh)     (f[m+1])
+ *   (A f)_c = (1/tau) f_c + sum_d (A_d f[m-1] + B_d f_c + C_d f[m+1]),
+ * in that evaluation order.  PreDefined and PreNormal rows are the Laplace
+ * operator's (semi-sum, normal derivative).  u, v, w are FP64 boxes of the
+ * operator's grid (NULL: 0), copied into the operator; flags are
+ * XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE.  Nonsymmetric: solve it with
+ * XF_BICGSTAB, XF_MINRES, or XF_BICG on its packed form. */
+int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, const xf_vec* w, double tau,
+                        double diff_coef, int flags);
 
 /* Packed operator: replaces T1dPackOperator(model, A, &null) (XOperator.cpp:
  * 1135-1350) built from A (Laplace or variable-density, density set).  Rows

@@ -280,3 +280,15 @@ def bicg_reference(pk, b, eps=0.0, maxit=0):
                                   _p(f64(b), C.c_double), C.c_double(eps), int(maxit), _p(out, C.c_double),
                                   C.byref(st))
     return out, st, rc
+
+
+def apply_advdiff(g, x, u, v, w, tau, D, flags=3):
+    """Implicit advection-diffusion operator on the oracle grid g (XProblem.cpp:1236-1238 summed over x, y, z)."""
+    y = np.zeros(g.shape)
+    p = lambda a: _p(f64(a), C.c_double) if a is not None else None  # noqa: E731
+    st = lib().xfo_apply_advdiff(_p(g.codes, C.c_int32), _p(g.normals, C.c_double), _p(g.hx, C.c_double),
+                                 _p(g.hy, C.c_double), _p(g.hz, C.c_double), p(u), p(v), p(w), C.c_double(tau),
+                                 C.c_double(D), int(flags), *g.shape, _p(f64(x), C.c_double), _p(y, C.c_double))
+    if st != 0:
+        raise ValueError("oracle advection-diffusion rejected the grid")
+    return y

@@ -945,3 +945,48 @@ int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, c
   free(pt_new); free(Ap);
   return status;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Implicit advection-diffusion operator of the momentum / transport
+ * equations: on Actual cells the sum over x, y, z of the reference's ADI line
+ * coefficients (THydrodynamicsProblem, XProblem.cpp:1236-1238), after
+ * (1/tau) f_c, in the reference's operation order; PreDefined / PreNormal rows
+ * as the Laplace operator's.  vel[d] is the advecting component along d at the
+ * cell; flags bit 0 convective, bit 1 diffusive. */
+static double ad_dir(const double* h, int m, double vd, double D, double conv, double diff, double fm, double fc,
+                     double fp) {
+  double h_1 = h[m - 1], hh = h[m];
+  double hx2 = h[m - 1] + h[m];
+  double hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / 2;
+  double A = conv * (0.5 * (-vd / hx2)) + diff * (0.5 * (-(D)*hh / hxhxh));
+  double B = diff * (0.5 * (D)*hx2 / hxhxh);
+  double C = conv * (0.5 * (vd / hx2)) + diff * (0.5 * (-(D)*h_1 / hxhxh));
+  return A * fm + B * fc + C * fp;
+}
+
+int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                      const double* hz, const double* u, const double* v, const double* w, double tau, double D,
+                      int flags, int n1, int n2, int n3, const double* x, double* y) {
+  int64_t bad;
+  if (xfo_validate(XFO_OP_LAPLACE, codes, normals, n1, n2, n3, &bad) != XFO_OK) return XFO_ERR_MASK;
+  xfo_grid g = {n1, n2, n3, (int64_t)n2 * n3, n3, codes, normals, hx, hy, hz, NULL};
+  const double conv = (flags & 1) ? 1.0 : 0.0, diff = (flags & 2) ? 1.0 : 0.0, itau = 1 / tau;
+  const int64_t s1 = g.s1, s2 = g.s2;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        int64_t c = ((int64_t)i * n2 + j) * n3 + k;
+        if (!active(codes, c)) continue;
+        if (codes[c] != ACT) {
+          y[c] = lap_row(&g, x, i, j, k);
+          continue;
+        }
+        const double fc = x[c];
+        double res = itau * fc;
+        res = res + ad_dir(hx, i, u ? u[c] : 0.0, D, conv, diff, x[c - s1], fc, x[c + s1]);
+        res = res + ad_dir(hy, j, v ? v[c] : 0.0, D, conv, diff, x[c - s2], fc, x[c + s2]);
+        res = res + ad_dir(hz, k, w ? w[c] : 0.0, D, conv, diff, x[c - 1], fc, x[c + 1]);
+        y[c] = res;
+      }
+  return XFO_OK;
+}

@@ -104,6 +104,13 @@ int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, c
                        const int32_t* t_ptr, const int32_t* t_cols, const double* t_vals, const double* b, double eps,
                        int maxit, double* result, xfo_stats* st);
 
+/* Implicit advection-diffusion operator (momentum / transport): y = A x on
+ * active cells; the reference's ADI line coefficients summed over the three
+ * directions (XProblem.cpp:1236-1238).  flags: 1 convective, 2 diffusive. */
+int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
+                      const double* hz, const double* u, const double* v, const double* w, double tau, double D,
+                      int flags, int n1, int n2, int n3, const double* x, double* y);
+
 #ifdef __cplusplus
 }
 #endif

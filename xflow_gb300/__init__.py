@@ -13,9 +13,10 @@ import weakref
 import numpy as np
 
 from . import capi
-from .capi import (XF_BICG, XF_BICGSTAB, XF_CG, XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE,  # noqa: F401
-                   XF_IB_POS, XF_IB_VEL, XF_MINRES, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED,
-                   XF_ZERO_INACTIVE, XFError)
+from .capi import (XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE, XF_BICG, XF_BICGSTAB, XF_CG,  # noqa: F401
+                   XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE, XF_IB_POS, XF_IB_VEL, XF_MINRES,
+                   XF_OP_ADVDIFF, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_ZERO_INACTIVE,
+                   XFError)
 
 
 def _check(ctx_handle, st):
@@ -199,6 +200,11 @@ class Operator(_Owned):
     def set_density(self, rho):
         rho = np.ascontiguousarray(rho, dtype=np.float64)
         _check(self.grid.ctx.h, capi.lib().xf_op_set_density(self.h, capi._ptr(rho)))
+
+    def set_advection(self, u, v, w, tau, diff_coef, flags=XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE):
+        """XF_OP_ADVDIFF coefficients: advecting velocity Vecs (or None), tau, D, flags."""
+        hh = [x.h if x is not None else None for x in (u, v, w)]
+        _check(self.grid.ctx.h, capi.lib().xf_op_set_advection(self.h, *hh, float(tau), float(diff_coef), int(flags)))
 
     def apply(self, x, y, s=None, sign=0, flags=0, w=None, want_dot=False):
         d = C.c_double()

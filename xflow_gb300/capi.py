@@ -14,7 +14,8 @@ XF_OK, XF_ERR_ARG, XF_ERR_CUDA, XF_ERR_MASK, XF_ERR_NOMEM, XF_ERR_STATE, XF_ERR_
 XF_ERR_CHECK = 7
 XF_STALL, XF_DIVERGED, XF_NAN, XF_MAXIT, XF_BREAKDOWN = 10, 11, 12, 13, 14
 XF_F64, XF_F32 = 0, 1
-XF_OP_LAPLACE, XF_OP_VARDIV, XF_OP_PACK = 0, 1, 2
+XF_OP_LAPLACE, XF_OP_VARDIV, XF_OP_PACK, XF_OP_ADVDIFF = 0, 1, 2, 3
+XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE = 1, 2
 XF_EXACT, XF_ZERO_INACTIVE = 1, 2
 XF_CG, XF_CG_REFERENCE, XF_BICGSTAB, XF_MINRES, XF_BICG, XF_FCG = 0, 1, 2, 3, 4, 5
 XF_PREC_FP64, XF_PREC_MIXED = 0, 1
@@ -27,7 +28,7 @@ EXPORTS = [
     "xf_create", "xf_destroy", "xf_last_error", "xf_status_string", "xf_synchronize", "xf_stream",
     "xf_grid_create", "xf_grid_destroy", "xf_grid_end_index", "xf_grid_rn_map", "xf_grid_space_mask",
     "xf_grid_check", "xf_vec_create", "xf_vec_destroy", "xf_vec_upload", "xf_vec_download", "xf_vec_assign",
-    "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_pack_create", "xf_op_transpose",
+    "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_op_set_advection", "xf_pack_create", "xf_op_transpose",
     "xf_pack_size", "xf_pack_download", "xf_matvec",
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
     "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
@@ -83,6 +84,7 @@ def lib():
         L.xf_op_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
         L.xf_op_destroy.argtypes = [vp]
         L.xf_op_set_density.argtypes = [vp, vp]
+        L.xf_op_set_advection.argtypes = [vp, vp, vp, vp, C.c_double, C.c_double, C.c_int]
         L.xf_pack_create.argtypes = [vp, C.POINTER(vp)]
         L.xf_op_transpose.argtypes = [vp]
         L.xf_pack_size.argtypes = [vp, i64p, i64p, i64p]

@@ -89,6 +89,11 @@ struct xf_op {
   int rho_set;
   PackData* pack = nullptr;   // XF_OP_PACK
   int transposed = 0;         // XF_OP_PACK: applies A^T (T1dPackOperator::operator~)
+  // XF_OP_ADVDIFF: advecting velocity boxes (FP64 and FP32 copies) and coefficients
+  double* adv64[3] = {nullptr, nullptr, nullptr};
+  float* adv32[3] = {nullptr, nullptr, nullptr};
+  double ad_tau = 1, ad_D = 0;
+  int ad_flags = 0, adv_set = 0;
 };
 
 // ---------------------------------------------------------------------------

@@ -203,8 +203,8 @@ extern "C" int xf_pack_create(xf_op* src, xf_op** out) {
   xf_grid* g = src->g;
   xf_ctx* ctx = g->ctx;
   if (src->kind == XF_OP_PACK) return xf_fail(ctx, XF_ERR_ARG, "xf_pack_create: the operator is already packed");
-  if (src->kind == XF_OP_VARDIV && !src->rho_set)
-    return xf_fail(ctx, XF_ERR_STATE, "xf_pack_create: set the density first");
+  if ((src->kind == XF_OP_VARDIV && !src->rho_set) || (src->kind == XF_OP_ADVDIFF && !src->adv_set))
+    return xf_fail(ctx, XF_ERR_STATE, "xf_pack_create: set the operator's coefficients first");
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   const int64_t R = g->end_index, n = g->ncell;
   if (R <= 0) return xf_fail(ctx, XF_ERR_ARG, "xf_pack_create: the grid has no active cells");

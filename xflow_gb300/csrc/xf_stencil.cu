@@ -171,6 +171,18 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   a.chunk = chunk;
   dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
   const bool use_d = std::is_same<T, double>::value && op->kind == XF_OP_LAPLACE && !q.exact;
+  if (op->kind == XF_OP_ADVDIFF) {
+    constexpr bool D64 = std::is_same<T, double>::value;
+    a.g.adv0 = D64 ? (const T*)op->adv64[0] : (const T*)op->adv32[0];
+    a.g.adv1 = D64 ? (const T*)op->adv64[1] : (const T*)op->adv32[1];
+    a.g.adv2 = D64 ? (const T*)op->adv64[2] : (const T*)op->adv32[2];
+    a.g.ad_itau = (T)(1 / op->ad_tau);
+    a.g.ad_D = (T)op->ad_D;
+    a.g.ad_conv = (op->ad_flags & XF_ADV_CONVECTIVE) ? T(1) : T(0);
+    a.g.ad_diff = (op->ad_flags & XF_ADV_DIFFUSIVE) ? T(1) : T(0);
+    k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    return;
+  }
   if (op->kind == XF_OP_LAPLACE) {
     if (q.exact) k_matvec<T, XF_OP_LAPLACE, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     else if (use_d) k_matvec<T, XF_OP_LAPLACE, false, true><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
@@ -207,7 +219,7 @@ void xf_apply_f32(const xf_op* op, const float* x, float* y, const float* s, int
 
 // ---------------------------------------------------------------------------
 extern "C" int xf_op_create(xf_grid* g, int kind, xf_op** out) {
-  if (!g || !out || (kind != XF_OP_LAPLACE && kind != XF_OP_VARDIV))
+  if (!g || !out || (kind != XF_OP_LAPLACE && kind != XF_OP_VARDIV && kind != XF_OP_ADVDIFF))
     return xf_fail(g ? g->ctx : nullptr, XF_ERR_ARG, "xf_op_create: bad arguments");
   *out = nullptr;
   int64_t bad = -1;
@@ -242,6 +254,10 @@ extern "C" int xf_op_destroy(xf_op* op) {
   cudaStreamSynchronize(op->g->ctx->stream);
   if (op->rho) cudaFree(op->rho);
   if (op->rho32) cudaFree(op->rho32);
+  for (int d = 0; d < 3; d++) {
+    if (op->adv64[d]) cudaFree(op->adv64[d]);
+    if (op->adv32[d]) cudaFree(op->adv32[d]);
+  }
   if (op->pack) xf_pack_free(op->pack);
   delete op;
   return XF_OK;
@@ -264,7 +280,40 @@ extern "C" int xf_op_set_density(xf_op* op, const double* host_rho) {
   return XF_OK;
 }
 
+extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, const xf_vec* w, double tau,
+                                   double diff_coef, int flags) {
+  if (!op) return XF_ERR_ARG;
+  xf_ctx* ctx = op->g->ctx;
+  if (op->kind != XF_OP_ADVDIFF) return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_advection: not an advection-diffusion operator");
+  if (!(tau != 0) || (flags & ~(XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE)))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_op_set_advection: tau must be nonzero and flags XF_ADV_*");
+  const xf_vec* vel[3] = {u, v, w};
+  for (int d = 0; d < 3; d++)
+    if (vel[d] && (vel[d]->g != op->g || vel[d]->dtype != XF_F64))
+      return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_advection: velocities must be FP64 boxes of the operator's grid");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int64_t n = op->g->ncell;
+  for (int d = 0; d < 3; d++) {
+    if (!op->adv64[d] && (cudaMalloc(&op->adv64[d], n * 8) != cudaSuccess ||
+                          cudaMalloc(&op->adv32[d], n * 4) != cudaSuccess)) {
+      cudaGetLastError();
+      return xf_fail(ctx, XF_ERR_NOMEM, "xf_op_set_advection: allocation");
+    }
+    if (vel[d]) XF_CUDA(ctx, cudaMemcpyAsync(op->adv64[d], vel[d]->data, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    else XF_CUDA(ctx, cudaMemsetAsync(op->adv64[d], 0, n * 8, ctx->stream));
+    k_d2f<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(op->adv64[d], op->adv32[d], n);
+  }
+  XF_CUDA(ctx, cudaGetLastError());
+  op->ad_tau = tau;
+  op->ad_D = diff_coef;
+  op->ad_flags = flags;
+  op->adv_set = 1;
+  return XF_OK;
+}
+
 int xf_op_ready(const xf_op* op) {
+  if (op->kind == XF_OP_ADVDIFF && !op->adv_set)
+    return xf_fail(op->g->ctx, XF_ERR_STATE, "advection-diffusion operator used before xf_op_set_advection");
   if (op->kind == XF_OP_VARDIV && !op->rho_set)
     return xf_fail(op->g->ctx, XF_ERR_STATE, "variable-density operator used before xf_op_set_density");
   return XF_OK;

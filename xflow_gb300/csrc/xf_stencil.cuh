@@ -24,6 +24,9 @@ struct StencilGrid {
   const T* __restrict__ rhx; const T* __restrict__ rhy; const T* __restrict__ rhz;
   const T* __restrict__ rhhx; const T* __restrict__ rhhy; const T* __restrict__ rhhz;
   const T* __restrict__ rho;  // density box (VARDIV) or null
+  // ADVDIFF: advecting velocity per direction, 1/tau, D and the two flags as 0/1
+  const T* __restrict__ adv0; const T* __restrict__ adv1; const T* __restrict__ adv2;
+  T ad_itau, ad_D, ad_conv, ad_diff;
   int n1, n2, n3;
   int s1, s2;
 };
@@ -183,12 +186,39 @@ __device__ __forceinline__ T fast_vd_actual(const StencilGrid<T>& g, const T* __
   return -(rc * lap - (d_i + d_j + d_k) * fc);
 }
 
+// Advection-diffusion Actual row: per direction the reference's ADI line
+// coefficients (XProblem.cpp:1236-1238) in its operation order, summed over
+// x, y, z after (1/tau) f_c.  Neighbour values are read as they are (the
+// solver keeps inactive cells at 0).
+template <typename T>
+__device__ __forceinline__ T ad_dir(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T fm, T fc, T fp) {
+  const T h_1 = h[m - 1], hh = h[m];
+  const T hx2 = h[m - 1] + h[m];
+  const T hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / T(2);
+  const T A = conv * (T(0.5) * (-vd / hx2)) + diff * (T(0.5) * (-(D)*hh / hxhxh));
+  const T B = diff * (T(0.5) * (D)*hx2 / hxhxh);
+  const T C = conv * (T(0.5) * (vd / hx2)) + diff * (T(0.5) * (-(D)*h_1 / hxhxh));
+  return A * fm + B * fc + C * fp;
+}
+
+template <typename T>
+__device__ __forceinline__ T ad_actual(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c) {
+  const int s1 = g.s1, s2 = g.s2;
+  const T fc = f[c];
+  T res = g.ad_itau * fc;
+  res = res + ad_dir<T>(g.hx, i, g.adv0[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
+  res = res + ad_dir<T>(g.hy, j, g.adv1[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
+  res = res + ad_dir<T>(g.hz, k, g.adv2[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
+  return res;
+}
+
 // One row of A applied to f at cell c of kind kb (row != ROW_NONE).
 template <typename T, int OP, bool EXACT>
 __device__ __forceinline__ T apply_row(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c,
                                        uint8_t kb) {
   const int row = row_of(kb);
   if (row == ROW_ACTUAL) {
+    if (OP == XF_OP_ADVDIFF) return ad_actual<T>(g, f, i, j, k, c);
     if (OP == XF_OP_LAPLACE) return EXACT ? exact_lap_actual<T>(g, f, i, j, k, c, kb) : fast_lap_actual<T>(g, f, i, j, k, c, kb);
     return EXACT ? exact_vd_actual<T>(g, f, i, j, k, c, kb) : fast_vd_actual<T>(g, f, i, j, k, c, kb);
   }
