@@ -309,6 +309,17 @@ int xf_ib_compute_forces(xf_ib* ib, int axis);
  * every node's force[axis] times its 7^3 cosine-delta weights. */
 int xf_ib_spread(xf_ib* ib, xf_vec* force, const double* h0, int axis);
 
+/* ---- learned preconditioner: tensor-core building blocks ------------------ */
+/* No counterpart in the reference (it has no learned component).  One
+ * 128 x N x K tile on the 5th-generation tensor cores (tcgen05, FP32
+ * accumulation in tensor memory): D = A B^T with A 128 x K and B N x K BF16
+ * (raw 16-bit patterns, K contiguous), D 128 x N FP32, all host pointers;
+ * 16 <= N, K <= 256, multiples of 16.  variant 0 is the operand layout the
+ * convolution kernels use; variant 1 swaps the two core-matrix strides of the
+ * shared-memory descriptors (a layout check). */
+int xf_tc_gemm_bf16(xf_ctx* ctx, int N, int K, const uint16_t* host_a, const uint16_t* host_b, float* host_d,
+                    int variant);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* No counterpart in the reference (a profiling helper).  Times each kernel of
  * one CG iteration on op's grid alone, `reps` launches each, with CUDA events
