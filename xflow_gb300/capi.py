@@ -33,7 +33,7 @@ EXPORTS = [
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
     "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
     "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
-    "xf_tc_gemm_bf16", "xf_profile_cg_kernels", "xf_dot_noalloc",
+    "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_profile_cg_kernels", "xf_dot_noalloc",
 ]
 
 
@@ -101,6 +101,9 @@ def lib():
         L.xf_dot_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
         L.xf_profile_cg_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.xf_tc_gemm_bf16.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, C.c_int]
+        L.xf_conv3d_bf16.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp,
+                                     C.c_int, C.c_int, C.c_int, C.c_int]
+        L.xf_conv_status.argtypes = [vp]
         L.xf_pressure_rhs.argtypes = [vp, vp, vp, vp, vp, C.c_double, vp, vp]
         L.xf_velocity_correct.argtypes = [C.c_int, vp, vp, vp, C.c_double, vp, vp]
         L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]

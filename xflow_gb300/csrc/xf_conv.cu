@@ -120,3 +120,186 @@ extern "C" int xf_tc_gemm_bf16(xf_ctx* ctx, int N, int K, const uint16_t* host_a
   if (herr) return xf_fail(ctx, XF_ERR_CUDA, "xf_tc_gemm_bf16: the MMA completion wait ran out");
   return XF_OK;
 }
+
+// ---------------------------------------------------------------------------
+// 3x3x3 convolution as an implicit GEMM on the tensor cores.
+//
+// Activations are channels-last BF16 boxes of the level's grid (the box with
+// its ghost layer, cell c = (i n2 + j) n3 + k, Ci channels per cell, row pitch
+// `ld` channels), allocated with a zero margin of XF_CONV_MARGIN(n2, n3) rows
+// before cell 0 and after the last cell, so every tap of every tile reads
+// inside the allocation.  Ghost and inactive cells hold 0 in every activation
+// (the epilogue multiplies by the level's mask), which makes the ghost layer
+// the zero padding of the convolution, also across the flattened row ends.
+//
+// A tile is 128 consecutive cells.  For tap t at offset o_t the A operand is
+// the contiguous block of rows c0 + o_t .. c0 + o_t + 127 (128 x Ci), the B
+// operand W[t] (Co x Ci); the 27 taps x Ci/16 MMAs accumulate in tensor
+// memory (128 lanes x Co FP32 columns).  Operand stages rotate through
+// XF_CONV_STAGES shared-memory buffers; a stage is refilled only after the
+// tensor core has signalled (mbarrier) that the MMAs reading it are done.
+// Epilogue: + bias, ReLU (optional), x mask, BF16 or FP32 store of the first
+// `out_ch` channels at row pitch out_ld.
+constexpr int CONV_STAGES = 3;
+
+struct ConvArgs {
+  const uint16_t* in;   // cell 0, channel 0 of the input slice
+  int in_ld, Ci;
+  const uint16_t* W;    // [27][Co][Ci]
+  const float* bias;    // [Co] or null
+  int Co;
+  const uint8_t* mask;  // [ncell]
+  int n2, n3;
+  int64_t ncell;
+  uint16_t* out16;      // cell 0, first output channel (BF16), or null
+  float* out32;         // or FP32
+  int out_ld, out_ch, relu;
+  int* err;
+};
+
+__global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t mbar[CONV_STAGES];
+  __shared__ uint32_t tmem_base;
+  const int Ci = a.Ci, Co = a.Co;
+  const int stage_a = TC_M * Ci * 2, stage_b = Co * Ci * 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = tmem_cols(Co);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+  if (threadIdx.x == 0)
+    for (int s = 0; s < CONV_STAGES; s++) tc::mbar_init(&mbar[s], 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = tmem_base;
+  const uint32_t idesc = tc::idesc_bf16_f32(TC_M, Co);
+  const uint32_t lbo = 128, sbo = (uint32_t)(Ci / 8) * 128;
+  const int64_t P = (int64_t)a.n2 * a.n3;
+  uint32_t issued[CONV_STAGES] = {0, 0, 0}, waited[CONV_STAGES] = {0, 0, 0};
+  bool ok = true;
+  auto drain = [&](int s) {   // wait for the stage's outstanding commit (at most one)
+    if (waited[s] < issued[s]) {
+      const bool w = tc::mbar_wait(&mbar[s], (issued[s] - 1) & 1);
+      if (!w) ok = false;
+      waited[s] = issued[s];
+    }
+  };
+  const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int64_t c0 = tile * TC_M;
+    for (int t = 0; t < 27; t++) {
+      const int s = t % CONV_STAGES;
+      drain(s);
+      const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
+      const int64_t off = di * P + dj * (int64_t)a.n3 + dk;
+      uint8_t* sA = smem + s * (stage_a + stage_b);
+      uint8_t* sB = sA + stage_a;
+      stage_kmajor(sA, a.in + (c0 + off) * a.in_ld, TC_M, Ci, a.in_ld);
+      stage_kmajor(sB, a.W + (int64_t)t * Co * Ci, Co, Ci, Ci);
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        for (int k = 0; k < Ci / 16; k++) {
+          const uint64_t ad = tc::smem_desc(tc::smem_addr(sA + k * 256), lbo, sbo);
+          const uint64_t bd = tc::smem_desc(tc::smem_addr(sB + k * 256), lbo, sbo);
+          tc::mma_bf16(tbase, ad, bd, idesc, t > 0 || k > 0);
+        }
+        tc::mma_commit(&mbar[s]);
+      }
+      issued[s]++;
+    }
+    for (int s = 0; s < CONV_STAGES; s++) drain(s);
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    tc::fence_after_sync();
+    // epilogue: warp w owns rows 32w .. 32w+31 (TMEM lanes)
+    const int64_t c = c0 + warp * 32 + lane;
+    const bool live = c < a.ncell;
+    const float m = live ? (float)a.mask[c] : 0.f;
+    for (int co = 0; co < Co; co += 8) {
+      float v[8];
+      tc::tmem_ld8(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)co, v);
+      if (!live || co >= a.out_ch) continue;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float x = v[q] + (a.bias ? a.bias[co + q] : 0.f);
+        if (a.relu) x = fmaxf(x, 0.f);
+        v[q] = x * m;
+      }
+      if (a.out16) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+          pk[q] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(a.out16 + c * a.out_ld + co) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      } else {
+        const int nq = min(8, a.out_ch - co);
+        for (int q = 0; q < nq; q++) a.out32[c * a.out_ld + co + q] = v[q];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();   // TMEM is read before the next tile's first MMA overwrites it
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+    for (int s = 0; s < CONV_STAGES; s++)
+      if (waited[s] < issued[s]) tc::mbar_wait(&mbar[s], (issued[s] - 1) & 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, ncols);
+}
+
+// Error flag of the convolutions: a slot of the context scratch, cleared by
+// xf_conv_status.
+constexpr int I_CONV_ERR = 60;
+static int* conv_err_flag(xf_ctx* ctx) { return reinterpret_cast<int*>(&ctx->scratch->iscalars[I_CONV_ERR]); }
+
+extern "C" int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci,
+                              const void* weights, const float* bias, int co, const uint8_t* mask, void* out,
+                              int out_ld, int out_ch, int out_fp32, int relu) {
+  if (!ctx || !in || !weights || !mask || !out) return XF_ERR_ARG;
+  if (ci < 16 || ci > 128 || ci % 16 || co < 16 || co > 128 || co % 16 || out_ch < 1 || out_ch > co ||
+      in_ld < ci || in_ld % 8 || out_ld < out_ch || (!out_fp32 && (out_ld % 8 || out_ch % 8)) || n1 < 3 || n2 < 3 ||
+      n3 < 3)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: channel counts / pitches out of range");
+  if (((uintptr_t)in | (uintptr_t)weights | (uintptr_t)out) & 15)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: pointers must be 16-byte aligned");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  int* err = conv_err_flag(ctx);
+  ConvArgs a;
+  a.in = (const uint16_t*)in; a.in_ld = in_ld; a.Ci = ci;
+  a.W = (const uint16_t*)weights; a.bias = bias; a.Co = co;
+  a.mask = mask; a.n2 = n2; a.n3 = n3; a.ncell = (int64_t)n1 * n2 * n3;
+  a.out16 = out_fp32 ? nullptr : (uint16_t*)out;
+  a.out32 = out_fp32 ? (float*)out : nullptr;
+  a.out_ld = out_ld; a.out_ch = out_ch; a.relu = relu; a.err = err;
+  const size_t smem = (size_t)CONV_STAGES * (TC_M * ci * 2 + co * ci * 2);
+  XF_CUDA(ctx, cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  XF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc, 128, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
+  int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+  if (blocks > ntiles) blocks = ntiles;
+  k_conv3_tc<<<(int)blocks, 128, smem, ctx->stream>>>(a);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// Reads and clears the error flag of the convolutions since the last call
+// (synchronises the stream).
+extern "C" int xf_conv_status(xf_ctx* ctx) {
+  if (!ctx) return XF_ERR_ARG;
+  int* err = conv_err_flag(ctx);
+  int h = 0;
+  XF_CUDA(ctx, cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  XF_CUDA(ctx, cudaMemsetAsync(err, 0, 4, ctx->stream));
+  if (h) return xf_fail(ctx, XF_ERR_CUDA, "convolution: a tensor-core completion wait ran out");
+  return XF_OK;
+}
