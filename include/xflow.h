@@ -339,6 +339,45 @@ int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
                    int relu);
 int xf_conv_status(xf_ctx* ctx);
 
+/* The learned preconditioner: a 3-level 3-D U-Net (16/32/64 channels, 3x3x3
+ * convolutions on the tensor cores, ReLU, BF16 weights and activations, FP32
+ * accumulation, about 0.35 M parameters) over the grid's box; level l+1
+ * halves the interior, so the interior dimensions must be multiples of 4.
+ * Parameters are one FP32 array, per layer W[27][co][ci] then b[co], layers
+ * enc0a (ci padded 1 -> 16), enc0b, enc1a, enc1b, mid_a, mid_b, dec1a (96 in),
+ * dec1b, dec0a (48 in), dec0b, out (co padded 1 -> 16; padding forced to 0).
+ * No counterpart in the reference. */
+typedef struct xf_unet xf_unet;
+int xf_unet_create(const xf_grid* g, xf_unet** out);
+int xf_unet_destroy(xf_unet* u);
+int xf_unet_param_count(const xf_unet* u, int64_t* n);
+int xf_unet_set_params(xf_unet* u, const float* host_params);   /* also restarts Adam */
+int xf_unet_get_params(xf_unet* u, float* host_params);
+int xf_unet_get_grads(xf_unet* u, float* host_grads);
+/* z = U-Net(r / rms(r)) on the active cells (FP64 boxes of the grid). */
+int xf_unet_apply(xf_unet* u, const xf_vec* r, xf_vec* z);
+/* One training step on the pair (r, e), e the error of an iterate and r its
+ * residual (A e = r).  With op (the symmetric stencil operator of the grid)
+ * the loss is one minus the A-norm cosine of the output z and the error,
+ * 1 - (z, r) / sqrt((z, A z) (e, r)), what preconditioned CG convergence
+ * depends on; without, the mean over active cells of (z - e / rms e)^2.
+ * Writes the loss, accumulates fresh gradients (backward pass: the
+ * tensor-core convolution with flipped weights for the input gradients, FP32
+ * reductions for the weight gradients) and with apply_update takes an Adam
+ * step (lr, beta 0.9 / 0.999). */
+int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, const xf_vec* e, double lr, int apply_update,
+                       double* loss);
+/* Flexible CG, truncated FCG(m): each preconditioned residual is
+ * A-orthogonalised against the last m directions (m = opts->reserved[0],
+ * 1..8, default 8), robust to a preconditioner that varies between
+ * applications.  Preconditioner opts->precond: XF_PRECOND_UNET (u),
+ * XF_PRECOND_JACOBI (Laplace diagonal) or none; FP64; stops on the true
+ * relative residual (opts->rtol).  Plain CG is the fallback (counted in
+ * stats->fallbacks): per iteration when z is no descent direction, for good
+ * when the residual stalls. */
+int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b,
+                 xf_solve_stats* stats);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* No counterpart in the reference (a profiling helper).  Times each kernel of
  * one CG iteration on op's grid alone, `reps` launches each, with CUDA events

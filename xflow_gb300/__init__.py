@@ -443,3 +443,115 @@ class Markers(_Owned):
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Learned preconditioner (no counterpart in the reference)
+UNET_LAYERS = (("enc0a", 16, 16), ("enc0b", 16, 16), ("enc1a", 16, 32), ("enc1b", 32, 32), ("mid_a", 32, 64),
+               ("mid_b", 64, 64), ("dec1a", 96, 32), ("dec1b", 32, 32), ("dec0a", 48, 16), ("dec0b", 16, 16),
+               ("out", 16, 16))
+
+
+def unet_init_params(seed=0):
+    """He-normal weights over each layer's real fan-in (input 1 channel for
+    enc0a, output 1 channel for out), zero biases; the padding stays 0."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    parts = []
+    for name, ci, co in UNET_LAYERS:
+        ci_real = 1 if name == "enc0a" else ci
+        w = rng.standard_normal((27, co, ci)) * np.sqrt(2.0 / (27 * ci_real))
+        if name == "enc0a":
+            w[:, :, 1:] = 0
+        if name == "out":
+            w[:, 1:, :] = 0
+            w *= np.sqrt(0.5)   # no ReLU after the output layer
+        parts += [w.ravel(), np.zeros(co)]
+    return np.concatenate(parts).astype(np.float32)
+
+
+class UNet(_Owned):
+    """3-level 3-D U-Net preconditioner on a grid (interior dims multiple of 4)."""
+
+    def __init__(self, grid, params=None, seed=0):
+        self.grid = grid
+        h = C.c_void_p()
+        _check(grid.ctx.h, capi.lib().xf_unet_create(grid.h, C.byref(h)))
+        self.h = h
+        grid._adopt(self)
+        n = C.c_int64()
+        _check(grid.ctx.h, capi.lib().xf_unet_param_count(self.h, C.byref(n)))
+        self.nparams = n.value
+        self.set_params(unet_init_params(seed) if params is None else params)
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.nparams
+        _check(self.grid.ctx.h, capi.lib().xf_unet_set_params(self.h, capi._ptr(p)))
+
+    def params(self):
+        p = np.zeros(self.nparams, np.float32)
+        _check(self.grid.ctx.h, capi.lib().xf_unet_get_params(self.h, capi._ptr(p)))
+        return p
+
+    def grads(self):
+        p = np.zeros(self.nparams, np.float32)
+        _check(self.grid.ctx.h, capi.lib().xf_unet_get_grads(self.h, capi._ptr(p)))
+        return p
+
+    def apply(self, r, z):
+        _check(self.grid.ctx.h, capi.lib().xf_unet_apply(self.h, r.h, z.h))
+        return z
+
+    def train_step(self, r, e, lr=1e-3, update=True, op=None):
+        """One step on (r, e); with op one minus the A-norm cosine of output and error,
+        else the MSE against e / rms e."""
+        loss = C.c_double()
+        _check(self.grid.ctx.h, capi.lib().xf_unet_train_step(self.h, op.h if op is not None else None, r.h, e.h,
+                                                              float(lr), int(update), C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if self.h:
+            if self.grid.h and self.grid.ctx.h:
+                capi.lib().xf_unet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_fcg(op, x, b, unet=None, precond=None, rtol=1e-8, maxit=100000, window=8):
+    """Flexible CG, FCG(window), with the U-Net (default when given), Jacobi or no preconditioner."""
+    o = solve_opts(method=capi.XF_FCG, rtol=rtol, maxit=maxit)
+    o.reserved[0] = int(window)
+    o.precond = precond if precond is not None else (capi.XF_PRECOND_UNET if unet is not None else
+                                                     capi.XF_PRECOND_NONE)
+    st = capi.SolveStats()
+    _check(op.grid.ctx.h, capi.lib().xf_solve_fcg(op.h, unet.h if unet is not None else None, C.byref(o), x.h, b.h,
+                                                  C.byref(st)))
+    return st
+
+
+def harvest_pairs(op, b, iters, xstar=None):
+    """(residual, error) pairs from plain FP64 CG's own iterates on A x = b:
+    for each k in `iters`, x_k = CG after k iterations from 0, r_k = b - A x_k,
+    e_k = x* - x_k with x* the converged (1e-10) solution.  Returns lists of
+    device Vecs (r_k, e_k)."""
+    g = op.grid
+    if xstar is None:
+        xstar = g.vec(np.zeros(g.shape))
+        solve(op, xstar, b, method=XF_CG, rtol=1e-10)
+    rs, es = [], []
+    for k in iters:
+        xk = g.vec(np.zeros(g.shape))
+        solve(op, xk, b, method=XF_CG, rtol=1e-30, maxit=int(k))
+        ax = g.vec(None)
+        op.apply(xk, ax, flags=XF_ZERO_INACTIVE)
+        r = g.vec(None).lincomb(1.0, b, -1.0, ax)
+        e = g.vec(None).lincomb(1.0, xstar, -1.0, xk)
+        rs.append(r)
+        es.append(e)
+    return rs, es

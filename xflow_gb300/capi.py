@@ -33,7 +33,9 @@ EXPORTS = [
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
     "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
     "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
-    "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_profile_cg_kernels", "xf_dot_noalloc",
+    "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
+    "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
+    "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_dot_noalloc",
 ]
 
 
@@ -104,6 +106,15 @@ def lib():
         L.xf_conv3d_bf16.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp,
                                      C.c_int, C.c_int, C.c_int, C.c_int]
         L.xf_conv_status.argtypes = [vp]
+        L.xf_unet_create.argtypes = [vp, C.POINTER(vp)]
+        L.xf_unet_destroy.argtypes = [vp]
+        L.xf_unet_param_count.argtypes = [vp, i64p]
+        L.xf_unet_set_params.argtypes = [vp, vp]
+        L.xf_unet_get_params.argtypes = [vp, vp]
+        L.xf_unet_get_grads.argtypes = [vp, vp]
+        L.xf_unet_apply.argtypes = [vp, vp, vp]
+        L.xf_unet_train_step.argtypes = [vp, vp, vp, vp, C.c_double, C.c_int, C.POINTER(C.c_double)]
+        L.xf_solve_fcg.argtypes = [vp, vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
         L.xf_pressure_rhs.argtypes = [vp, vp, vp, vp, vp, C.c_double, vp, vp]
         L.xf_velocity_correct.argtypes = [C.c_int, vp, vp, vp, C.c_double, vp, vp]
         L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]

@@ -154,6 +154,8 @@ struct ConvArgs {
   uint16_t* out16;      // cell 0, first output channel (BF16), or null
   float* out32;         // or FP32
   int out_ld, out_ch, relu;
+  const uint16_t* gate;   // optional: zero the outputs where gate[c * gate_ld + ch] <= 0 (ReLU backward)
+  int gate_ld;
   int* err;
 };
 
@@ -222,10 +224,13 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
       float v[8];
       tc::tmem_ld8(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)co, v);
       if (!live || co >= a.out_ch) continue;
+      uint16_t gt[8];
+      if (a.gate) *reinterpret_cast<uint4*>(gt) = *reinterpret_cast<const uint4*>(a.gate + c * a.gate_ld + co);
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         float x = v[q] + (a.bias ? a.bias[co + q] : 0.f);
         if (a.relu) x = fmaxf(x, 0.f);
+        if (a.gate && ((gt[q] & 0x8000u) || !(gt[q] & 0x7FFFu))) x = 0.f;   // gate value <= 0
         v[q] = x * m;
       }
       if (a.out16) {
@@ -259,19 +264,13 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
 constexpr int I_CONV_ERR = 60;
 static int* conv_err_flag(xf_ctx* ctx) { return reinterpret_cast<int*>(&ctx->scratch->iscalars[I_CONV_ERR]); }
 
-extern "C" int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci,
-                              const void* weights, const float* bias, int co, const uint8_t* mask, void* out,
-                              int out_ld, int out_ch, int out_fp32, int relu) {
-  if (!ctx || !in || !weights || !mask || !out) return XF_ERR_ARG;
-  if (ci < 16 || ci > 128 || ci % 16 || co < 16 || co > 128 || co % 16 || out_ch < 1 || out_ch > co ||
-      in_ld < ci || in_ld % 8 || out_ld < out_ch || (!out_fp32 && (out_ld % 8 || out_ch % 8)) || n1 < 3 || n2 < 3 ||
-      n3 < 3)
-    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: channel counts / pitches out of range");
-  if (((uintptr_t)in | (uintptr_t)weights | (uintptr_t)out) & 15)
-    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: pointers must be 16-byte aligned");
-  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+// Launch on the context stream (arguments checked by the caller).
+int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci, const void* weights,
+                   const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
+                   int relu, const void* gate, int gate_ld) {
   int* err = conv_err_flag(ctx);
   ConvArgs a;
+  a.gate = (const uint16_t*)gate; a.gate_ld = gate_ld;
   a.in = (const uint16_t*)in; a.in_ld = in_ld; a.Ci = ci;
   a.W = (const uint16_t*)weights; a.bias = bias; a.Co = co;
   a.mask = mask; a.n2 = n2; a.n3 = n3; a.ncell = (int64_t)n1 * n2 * n3;
@@ -289,6 +288,21 @@ extern "C" int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* i
   k_conv3_tc<<<(int)blocks, 128, smem, ctx->stream>>>(a);
   XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
+}
+
+extern "C" int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci,
+                              const void* weights, const float* bias, int co, const uint8_t* mask, void* out,
+                              int out_ld, int out_ch, int out_fp32, int relu) {
+  if (!ctx || !in || !weights || !mask || !out) return XF_ERR_ARG;
+  if (ci < 16 || ci > 128 || ci % 16 || co < 16 || co > 128 || co % 16 || out_ch < 1 || out_ch > co ||
+      in_ld < ci || in_ld % 8 || out_ld < out_ch || (!out_fp32 && (out_ld % 8 || out_ch % 8)) || n1 < 3 || n2 < 3 ||
+      n3 < 3)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: channel counts / pitches out of range");
+  if (((uintptr_t)in | (uintptr_t)weights | (uintptr_t)out) & 15)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_conv3d_bf16: pointers must be 16-byte aligned");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  return xf_conv_launch(ctx, n1, n2, n3, in, in_ld, ci, weights, bias, co, mask, out, out_ld, out_ch, out_fp32, relu,
+                        nullptr, 0);
 }
 
 // Reads and clears the error flag of the convolutions since the last call

@@ -1,0 +1,919 @@
+// Learned preconditioner: a 3-level 3-D U-Net (16/32/64 channels, 3x3x3
+// convolutions, ReLU, BF16 weights and activations, FP32 accumulation) run
+// by the tensor-core convolution of xf_conv.cu, trained on (residual, error)
+// pairs by this file's own backward pass, and applied inside a flexible CG.
+// No counterpart in the reference (it has no learned component).
+//
+// Levels: the grid's box (ghost layer included) is level 0; level l+1 halves
+// the interior ((n-2)/2 + 2 per axis, interior divisible by 4), its cell
+// (I,J,K) covering the fine interior cells 2I-1..2I (per axis).  Masks: level
+// 0 = the grid's space mask, level l+1 = any child active.
+//
+// Network (channels):
+//   enc0a 1->16, enc0b 16->16 (skip S0) | pool | enc1a 16->32, enc1b 32->32
+//   (skip S1) | pool | mid_a 32->64, mid_b 64->64 | up -> [64 | S1] ->
+//   dec1a 96->32, dec1b 32->32 | up -> [32 | S0] -> dec0a 48->16,
+//   dec0b 16->16, out 16->1 (no ReLU).
+// The skips are written by their encoder convolutions straight into the
+// channel slices of the decoder inputs (no concatenation copies).  The input
+// channel is padded to 16 and the output to 16 (the padding weights stay 0).
+// Input r is divided by its RMS over the active cells; the output is the
+// preconditioned direction (its scale is irrelevant to the flexible CG).
+#include <math.h>
+
+#include <vector>
+
+#include "xf_control.cuh"
+
+int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci, const void* weights,
+                   const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
+                   int relu, const void* gate, int gate_ld);
+void xf_mv64(const xf_op* op, const MvReq<double>& q);
+void xf_dot_async(const xf_grid* g, int dtype, const void* a, const void* b, int slot);
+int xf_op_ready(const xf_op* op);
+
+namespace {
+
+struct Level {
+  int n1, n2, n3;
+  int64_t n, margin;
+  uint8_t* mask = nullptr;
+  int64_t active = 0;
+};
+
+// channels-last BF16 activation box with its zero margins
+struct Act {
+  uint16_t* base = nullptr;
+  int C = 0, level = 0;
+  int64_t rows = 0;
+  uint16_t* p0(const Level* L) const { return base + L[level].margin * C; }
+};
+
+enum { ENC0A, ENC0B, ENC1A, ENC1B, MIDA, MIDB, DEC1A, DEC1B, DEC0A, DEC0B, OUTL, NLAYER };
+const int LCI[NLAYER] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16, 16};
+const int LCO[NLAYER] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16, 16};
+const int LLEV[NLAYER] = {0, 0, 1, 1, 2, 2, 1, 1, 0, 0, 0};
+const int LRELU[NLAYER] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0};
+
+struct Layer {
+  int ci, co;
+  int64_t nw;                 // 27 * co * ci
+  float* w = nullptr;         // FP32 master [27][co][ci]
+  float* b = nullptr;         // [co]
+  uint16_t* w16 = nullptr;    // BF16 [27][co][ci]
+  uint16_t* wt16 = nullptr;   // BF16 flipped transpose [27][ci][co]: w16[26-t][co][ci]
+  float *gw = nullptr, *gb = nullptr;                  // gradients
+  float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;   // Adam moments
+};
+
+}  // namespace
+
+struct xf_unet {
+  xf_ctx* ctx;
+  const xf_grid* g;
+  Level L[3];
+  Layer ly[NLAYER];
+  // forward activations
+  Act X0, A0, CAT0, D0a, D0b;       // level 0 (CAT0 = [up 32 | S0 16])
+  Act P1, A1, CAT1, D1a, D1b;       // level 1 (CAT1 = [up 64 | S1 32])
+  Act P2, M2a, M2b;                 // level 2
+  float* zout = nullptr;            // level-0 box, FP32, 1 channel
+  // backward buffers (gradients w.r.t. pre-activations, BF16)
+  Act G0_16a, G0_16b, G0_48, G1_32a, G1_32b, G1_96, G2_64a, G2_64b, G1_16, G2_32;
+  float* gsum = nullptr;            // FP32 [level-0 cells x 16]: S0 gradient accumulator
+  float* gsum1 = nullptr;           // FP32 [level-1 cells x 32]: S1 gradient accumulator
+  double* red = nullptr;            // device reductions: [0] sum r^2, [1] sum e^2, [2] loss
+  double* zd = nullptr;             // level-0 box, FP64: the output (A-norm loss)
+  double* az = nullptr;             // A zd
+  int step = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Coarse mask: any active child.
+__global__ void k_mask_pool(const uint8_t* __restrict__ fine, int f2, int f3, uint8_t* __restrict__ coarse, int c1,
+                            int c2, int c3) {
+  const int64_t n = (int64_t)c1 * c2 * c3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int I = (int)(c / ((int64_t)c2 * c3)), J = (int)((c / c3) % c2), K = (int)(c % c3);
+    uint8_t m = 0;
+    if (I >= 1 && I <= c1 - 2 && J >= 1 && J <= c2 - 2 && K >= 1 && K <= c3 - 2)
+      for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+          for (int d = 0; d < 2; d++)
+            m |= fine[((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)];
+    coarse[c] = m ? 1 : 0;
+  }
+}
+
+__device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+__device__ __forceinline__ uint16_t f2bf(float x) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7F800000u) == 0x7F800000u) return (uint16_t)(u >> 16);   // inf / nan
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+// Average of the 8 children (inactive children hold 0), times the coarse mask.
+// src: fine slice (pointer at cell 0, pitch sld), dst: coarse (pitch dld), C channels.
+__global__ void k_pool(const uint16_t* __restrict__ src, int sld, int f2, int f3, uint16_t* __restrict__ dst,
+                       int dld, const uint8_t* __restrict__ cmask, int c1, int c2, int c3, int C) {
+  const int64_t n = (int64_t)c1 * c2 * c3 * C;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = u / C;
+    const int ch = (int)(u - c * C);
+    const int I = (int)(c / ((int64_t)c2 * c3)), J = (int)((c / c3) % c2), K = (int)(c % c3);
+    float s = 0.f;
+    if (cmask[c])
+      for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+          for (int d = 0; d < 2; d++)
+            s += bf2f(src[(((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * sld + ch]);
+    dst[c * dld + ch] = f2bf(s * 0.125f);
+  }
+}
+
+// Pooling backward: every active fine child receives 1/8 of its parent's
+// gradient, added to an FP32 accumulator (pitch ald).
+__global__ void k_pool_bwd(const uint16_t* __restrict__ gcoarse, int gld, int c2, int c3,
+                           const uint8_t* __restrict__ fmask, int f1, int f2, int f3, float* __restrict__ acc,
+                           int ald, int C) {
+  const int64_t n = (int64_t)f1 * f2 * f3 * C;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = u / C;
+    const int ch = (int)(u - c * C);
+    if (!fmask[c]) continue;
+    const int i = (int)(c / ((int64_t)f2 * f3)), j = (int)((c / f3) % f2), k = (int)(c % f3);
+    const int64_t pc = ((int64_t)(1 + (i - 1) / 2) * c2 + (1 + (j - 1) / 2)) * c3 + (1 + (k - 1) / 2);
+    acc[c * ald + ch] += 0.125f * bf2f(gcoarse[pc * gld + ch]);
+  }
+}
+
+// Nearest upsampling of a coarse slice into a fine slice, times the fine mask.
+__global__ void k_upsample(const uint16_t* __restrict__ src, int sld, int c2, int c3, uint16_t* __restrict__ dst,
+                           int dld, const uint8_t* __restrict__ fmask, int f1, int f2, int f3, int C) {
+  const int64_t n = (int64_t)f1 * f2 * f3 * C;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = u / C;
+    const int ch = (int)(u - c * C);
+    uint16_t v = 0;
+    if (fmask[c]) {
+      const int i = (int)(c / ((int64_t)f2 * f3)), j = (int)((c / f3) % f2), k = (int)(c % f3);
+      const int64_t pc = ((int64_t)(1 + (i - 1) / 2) * c2 + (1 + (j - 1) / 2)) * c3 + (1 + (k - 1) / 2);
+      v = src[pc * sld + ch];
+    }
+    dst[c * dld + ch] = v;
+  }
+}
+
+// Upsampling backward: a coarse cell's gradient is the sum over its 8
+// children; then x coarse mask and the coarse activation's ReLU gate.
+__global__ void k_upsample_bwd(const uint16_t* __restrict__ gfine, int gld, int f2, int f3,
+                               const uint16_t* __restrict__ gate, int gtld, const uint8_t* __restrict__ cmask,
+                               int c1, int c2, int c3, uint16_t* __restrict__ dst, int dld, int C) {
+  const int64_t n = (int64_t)c1 * c2 * c3 * C;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = u / C;
+    const int ch = (int)(u - c * C);
+    float s = 0.f;
+    if (cmask[c] && bf2f(gate[c * gtld + ch]) > 0.f) {
+      const int I = (int)(c / ((int64_t)c2 * c3)), J = (int)((c / c3) % c2), K = (int)(c % c3);
+      for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+          for (int d = 0; d < 2; d++)
+            s += bf2f(gfine[(((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * gld + ch]);
+    }
+    dst[c * dld + ch] = f2bf(s);
+  }
+}
+
+// Skip gradient: dPre = (skip part of the decoder's input gradient + pooled
+// path's accumulator) x mask x ReLU gate; the accumulator is cleared.
+__global__ void k_skip_grad(const uint16_t* __restrict__ gskip, int gld, float* __restrict__ acc, int ald,
+                            const uint16_t* __restrict__ gate, int gtld, const uint8_t* __restrict__ mask, int64_t ncell,
+                            uint16_t* __restrict__ dst, int dld, int C) {
+  const int64_t n = ncell * C;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = u / C;
+    const int ch = (int)(u - c * C);
+    float v = bf2f(gskip[c * gld + ch]) + acc[c * ald + ch];
+    acc[c * ald + ch] = 0.f;
+    if (!mask[c] || !(bf2f(gate[c * gtld + ch]) > 0.f)) v = 0.f;
+    dst[c * dld + ch] = f2bf(v);
+  }
+}
+
+// Sum of squares over the active cells (FP64 atomics into red[slot]).
+__global__ void k_sumsq(const double* __restrict__ x, const uint8_t* __restrict__ m, int64_t n, double* red, int slot) {
+  double s = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    if (m[c]) s += x[c] * x[c];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&red[slot], s);
+}
+
+// Level-0 input: channel 0 = r / rms(r) on active cells, channels 1..15 = 0.
+__global__ void k_unet_input(const double* __restrict__ r, const uint8_t* __restrict__ m, int64_t n,
+                             const double* __restrict__ red, double count, uint16_t* __restrict__ x0) {
+  const double ss = red[0];
+  const float inv = ss > 0 ? (float)(1.0 / sqrt(ss / count)) : 0.f;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    uint16_t v[16] = {0};
+    if (m[c]) v[0] = f2bf((float)r[c] * inv);
+    uint4* d = reinterpret_cast<uint4*>(x0 + c * 16);
+    d[0] = *reinterpret_cast<uint4*>(&v[0]);
+    d[1] = *reinterpret_cast<uint4*>(&v[8]);
+  }
+}
+
+// Loss (mean over active cells of (z - t)^2, t = e / rms(e)) and its
+// gradient as the output layer's 16-channel dPre (channel 0).
+__global__ void k_unet_loss(const float* __restrict__ z, const double* __restrict__ e, const uint8_t* __restrict__ m,
+                            int64_t n, double count, double* red, uint16_t* __restrict__ g16) {
+  const double ss = red[1];
+  const double inv = ss > 0 ? 1.0 / sqrt(ss / count) : 0.0;
+  double l = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    uint16_t v[16] = {0};
+    if (m[c]) {
+      const double d = (double)z[c] - e[c] * inv;
+      l += d * d;
+      v[0] = f2bf((float)(2.0 * d / count));
+    }
+    uint4* dst = reinterpret_cast<uint4*>(g16 + c * 16);
+    dst[0] = *reinterpret_cast<uint4*>(&v[0]);
+    dst[1] = *reinterpret_cast<uint4*>(&v[8]);
+  }
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&red[2], l / count);
+}
+
+// Weight gradient on the CUDA cores in FP32: gw[t][co][ci] += sum over cells
+// of g[c][co] * x[c + off_t][ci]; gb[co] += sum g[c][co] (tap 13 blocks).
+// Block = (tap, chunk of cells); the chunk's gradient and input rows are
+// staged in shared memory, each thread owns co*ci/256 (co, ci) pairs.
+constexpr int WG_CELLS = 64;
+__global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, int gld, const uint16_t* __restrict__ x,
+                                               int xld, int ci, int co, int n2, int n3, int64_t ncell, int chunk,
+                                               float* __restrict__ gw, float* __restrict__ gb) {
+  extern __shared__ float wsm[];
+  float* sg = wsm;                   // [WG_CELLS][co]
+  float* sx = wsm + WG_CELLS * co;   // [WG_CELLS][ci]
+  const int t = blockIdx.y;
+  const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
+  const int64_t off = di * (int64_t)n2 * n3 + dj * (int64_t)n3 + dk;
+  const int npair = co * ci;
+  const int per = (npair + 255) / 256;   // <= 24 (96 x 64 / 256)
+  float accv[24];
+  for (int q = 0; q < per; q++) accv[q] = 0.f;
+  float accb = 0.f;
+  const int64_t c_beg = (int64_t)blockIdx.x * chunk, c_end = min(ncell, c_beg + chunk);
+  for (int64_t cb = c_beg; cb < c_end; cb += WG_CELLS) {
+    const int nc = (int)min((int64_t)WG_CELLS, c_end - cb);
+    __syncthreads();
+    for (int u = threadIdx.x; u < WG_CELLS * co; u += 256) {
+      const int r = u / co, ch = u - r * co;
+      sg[u] = r < nc ? bf2f(g[(cb + r) * gld + ch]) : 0.f;
+    }
+    for (int u = threadIdx.x; u < WG_CELLS * ci; u += 256) {
+      const int r = u / ci, ch = u - r * ci;
+      sx[u] = r < nc ? bf2f(x[(cb + r + off) * xld + ch]) : 0.f;
+    }
+    __syncthreads();
+    for (int q = 0; q < per; q++) {
+      const int pr = threadIdx.x + q * 256;
+      if (pr >= npair) break;
+      const int o = pr / ci, i = pr - o * ci;
+      float s = 0.f;
+      for (int r = 0; r < WG_CELLS; r++) s = fmaf(sg[r * co + o], sx[r * ci + i], s);
+      accv[q] += s;
+    }
+    if (t == 13 && threadIdx.x < co)
+      for (int r = 0; r < WG_CELLS; r++) accb += sg[r * co + threadIdx.x];
+  }
+  for (int q = 0; q < per; q++) {
+    const int pr = threadIdx.x + q * 256;
+    if (pr < npair) atomicAdd(&gw[(int64_t)t * npair + pr], accv[q]);
+  }
+  if (t == 13 && threadIdx.x < co) atomicAdd(&gb[threadIdx.x], accb);
+}
+
+// Adam step on one layer (bias-corrected, step counts from 1), then the BF16
+// copies: w16[t][co][ci] and the flipped transpose wt16[26-t][ci][co].
+__global__ void k_adam(float* w, float* gwt, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
+                       float c1, float c2, int clear) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const float gr = gwt[u];
+    const float mm = b1 * m[u] + (1 - b1) * gr;
+    const float vv = b2 * v[u] + (1 - b2) * gr * gr;
+    m[u] = mm;
+    v[u] = vv;
+    w[u] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    if (clear) gwt[u] = 0.f;
+  }
+}
+
+__global__ void k_weights_bf16(const float* __restrict__ w, int co, int ci, uint16_t* __restrict__ w16,
+                               uint16_t* __restrict__ wt16) {
+  const int64_t n = (int64_t)27 * co * ci;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(u / ((int64_t)co * ci));
+    const int o = (int)((u / ci) % co), i = (int)(u % ci);
+    const uint16_t h = f2bf(w[u]);
+    w16[u] = h;
+    wt16[((int64_t)(26 - t) * ci + i) * co + o] = h;
+  }
+}
+
+// A-norm loss 1 - (z,r) / sqrt((z,Az)(e,r)) (one minus the A-norm cosine of
+// the output and the error; dots in scalars[10..12]) and its gradient
+// -(r - (z,r)/(z,Az) A z) / sqrt((z,Az)(e,r)) as the output layer's
+// 16-channel dPre (channel 0).
+__global__ void k_anorm_grad(const double* __restrict__ r, const double* __restrict__ az,
+                             const uint8_t* __restrict__ m, int64_t n, const DevScratch* __restrict__ S, double* red,
+                             uint16_t* __restrict__ g16) {
+  const double zr = S->scalars[10], zaz = S->scalars[11], er = S->scalars[12];
+  const bool ok = zaz > 0 && er > 0;
+  const double c1 = ok ? -1 / sqrt(zaz * er) : 0.0, c2 = ok ? zr / zaz : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) red[2] = ok ? 1 - zr / sqrt(zaz * er) : 1.0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    uint16_t v[16] = {0};
+    if (m[c]) v[0] = f2bf((float)(c1 * (r[c] - c2 * az[c])));
+    uint4* dst = reinterpret_cast<uint4*>(g16 + c * 16);
+    dst[0] = *reinterpret_cast<uint4*>(&v[0]);
+    dst[1] = *reinterpret_cast<uint4*>(&v[8]);
+  }
+}
+
+__global__ void k_f2d_mask(const float* __restrict__ z, const uint8_t* __restrict__ m, int64_t n,
+                           double* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = m[c] ? (double)z[c] : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+static int ublocks(xf_ctx* ctx, int64_t n) { return grid_blocks(ctx, n, 256); }
+
+static int act_alloc(xf_unet* u, Act& a, int level, int C) {
+  a.level = level;
+  a.C = C;
+  a.rows = u->L[level].n + 2 * u->L[level].margin;
+  if (cudaMalloc(&a.base, a.rows * C * 2) != cudaSuccess) {
+    cudaGetLastError();
+    a.base = nullptr;
+    return XF_ERR_NOMEM;
+  }
+  return cudaMemsetAsync(a.base, 0, a.rows * C * 2, u->ctx->stream) == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+}
+
+static void unet_free(xf_unet* u) {
+  Act* a[] = {&u->X0, &u->A0, &u->CAT0, &u->D0a, &u->D0b, &u->P1, &u->A1, &u->CAT1, &u->D1a, &u->D1b,
+              &u->P2, &u->M2a, &u->M2b, &u->G0_16a, &u->G0_16b, &u->G0_48, &u->G1_32a, &u->G1_32b,
+              &u->G1_96, &u->G2_64a, &u->G2_64b, &u->G1_16, &u->G2_32};
+  for (Act* x : a)
+    if (x->base) cudaFree(x->base);
+  for (int l = 1; l < 3; l++)
+    if (u->L[l].mask) cudaFree(u->L[l].mask);
+  for (Layer& y : u->ly) {
+    void* ps[] = {y.w, y.b, y.w16, y.wt16, y.gw, y.gb, y.mw, y.vw, y.mb, y.vb};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+  }
+  if (u->zout) cudaFree(u->zout);
+  if (u->gsum) cudaFree(u->gsum);
+  if (u->gsum1) cudaFree(u->gsum1);
+  if (u->red) cudaFree(u->red);
+  if (u->zd) cudaFree(u->zd);
+  if (u->az) cudaFree(u->az);
+  delete u;
+}
+
+extern "C" int xf_unet_destroy(xf_unet* u) {
+  if (!u) return XF_OK;
+  cudaSetDevice(u->ctx->device);
+  cudaStreamSynchronize(u->ctx->stream);
+  unet_free(u);
+  return XF_OK;
+}
+
+static int64_t count_active(xf_ctx* ctx, const uint8_t* mask, int64_t n) {
+  std::vector<uint8_t> h(n);
+  if (cudaMemcpy(h.data(), mask, n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  int64_t s = 0;
+  for (int64_t c = 0; c < n; c++) s += h[c] != 0;
+  return s;
+}
+
+extern "C" int xf_unet_create(const xf_grid* g, xf_unet** out) {
+  if (!g || !out) return XF_ERR_ARG;
+  *out = nullptr;
+  xf_ctx* ctx = g->ctx;
+  if ((g->n1 - 2) % 4 || (g->n2 - 2) % 4 || (g->n3 - 2) % 4 || g->n1 < 10 || g->n2 < 10 || g->n3 < 10)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_unet_create: interior dimensions must be multiples of 4 (>= 8)");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  xf_unet* u = new xf_unet();
+  u->ctx = ctx;
+  u->g = g;
+  int dims[3] = {g->n1, g->n2, g->n3};
+  for (int l = 0; l < 3; l++) {
+    Level& L = u->L[l];
+    L.n1 = dims[0]; L.n2 = dims[1]; L.n3 = dims[2];
+    L.n = (int64_t)L.n1 * L.n2 * L.n3;
+    L.margin = XF_CONV_MARGIN(L.n2, L.n3);
+    for (int a = 0; a < 3; a++) dims[a] = (dims[a] - 2) / 2 + 2;
+  }
+  u->L[0].mask = g->smask;
+  int st = XF_OK;
+  for (int l = 1; l < 3 && !st; l++) {
+    if (cudaMalloc(&u->L[l].mask, u->L[l].n) != cudaSuccess) st = XF_ERR_NOMEM;
+    else
+      k_mask_pool<<<ublocks(ctx, u->L[l].n), 256, 0, ctx->stream>>>(u->L[l - 1].mask, u->L[l - 1].n2, u->L[l - 1].n3,
+                                                                   u->L[l].mask, u->L[l].n1, u->L[l].n2, u->L[l].n3);
+  }
+  struct { Act* a; int level, C; } acts[] = {
+      {&u->X0, 0, 16}, {&u->A0, 0, 16}, {&u->CAT0, 0, 48}, {&u->D0a, 0, 16}, {&u->D0b, 0, 16},
+      {&u->P1, 1, 16}, {&u->A1, 1, 32}, {&u->CAT1, 1, 96}, {&u->D1a, 1, 32}, {&u->D1b, 1, 32},
+      {&u->P2, 2, 32}, {&u->M2a, 2, 64}, {&u->M2b, 2, 64},
+      {&u->G0_16a, 0, 16}, {&u->G0_16b, 0, 16}, {&u->G0_48, 0, 48}, {&u->G1_32a, 1, 32}, {&u->G1_32b, 1, 32},
+      {&u->G1_96, 1, 96}, {&u->G2_64a, 2, 64}, {&u->G2_64b, 2, 64}, {&u->G1_16, 1, 16}, {&u->G2_32, 2, 32}};
+  for (auto& e : acts)
+    if (!st) st = act_alloc(u, *e.a, e.level, e.C);
+  for (int k = 0; k < NLAYER && !st; k++) {
+    Layer& y = u->ly[k];
+    y.ci = LCI[k]; y.co = LCO[k];
+    y.nw = (int64_t)27 * y.co * y.ci;
+    float** f32[] = {&y.w, &y.gw, &y.mw, &y.vw};
+    for (float** p : f32)
+      if (!st && cudaMalloc(p, y.nw * 4) != cudaSuccess) st = XF_ERR_NOMEM;
+    float** fb[] = {&y.b, &y.gb, &y.mb, &y.vb};
+    for (float** p : fb)
+      if (!st && cudaMalloc(p, y.co * 4) != cudaSuccess) st = XF_ERR_NOMEM;
+    if (!st && (cudaMalloc(&y.w16, y.nw * 2) != cudaSuccess || cudaMalloc(&y.wt16, y.nw * 2) != cudaSuccess))
+      st = XF_ERR_NOMEM;
+    if (!st) {
+      cudaMemsetAsync(y.w, 0, y.nw * 4, ctx->stream); cudaMemsetAsync(y.gw, 0, y.nw * 4, ctx->stream);
+      cudaMemsetAsync(y.mw, 0, y.nw * 4, ctx->stream); cudaMemsetAsync(y.vw, 0, y.nw * 4, ctx->stream);
+      cudaMemsetAsync(y.b, 0, y.co * 4, ctx->stream); cudaMemsetAsync(y.gb, 0, y.co * 4, ctx->stream);
+      cudaMemsetAsync(y.mb, 0, y.co * 4, ctx->stream); cudaMemsetAsync(y.vb, 0, y.co * 4, ctx->stream);
+      cudaMemsetAsync(y.w16, 0, y.nw * 2, ctx->stream); cudaMemsetAsync(y.wt16, 0, y.nw * 2, ctx->stream);
+    }
+  }
+  if (!st && (cudaMalloc(&u->zout, u->L[0].n * 4) != cudaSuccess ||
+              cudaMalloc(&u->gsum, u->L[0].n * 16 * 4) != cudaSuccess ||
+              cudaMalloc(&u->gsum1, u->L[1].n * 32 * 4) != cudaSuccess || cudaMalloc(&u->red, 8 * 8) != cudaSuccess ||
+              cudaMalloc(&u->zd, u->L[0].n * 8) != cudaSuccess || cudaMalloc(&u->az, u->L[0].n * 8) != cudaSuccess))
+    st = XF_ERR_NOMEM;
+  if (!st) {
+    cudaMemsetAsync(u->zout, 0, u->L[0].n * 4, ctx->stream);
+    cudaMemsetAsync(u->gsum, 0, u->L[0].n * 16 * 4, ctx->stream);
+    cudaMemsetAsync(u->gsum1, 0, u->L[1].n * 32 * 4, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) st = XF_ERR_CUDA;
+  }
+  for (int l = 0; l < 3 && !st; l++) {
+    u->L[l].active = count_active(ctx, u->L[l].mask, u->L[l].n);
+    if (u->L[l].active < 0) st = XF_ERR_CUDA;
+  }
+  if (st) {
+    cudaGetLastError();
+    cudaStreamSynchronize(ctx->stream);
+    unet_free(u);
+    return xf_fail(ctx, st, "xf_unet_create: device allocation / set-up failed");
+  }
+  *out = u;
+  return XF_OK;
+}
+
+extern "C" int xf_unet_param_count(const xf_unet* u, int64_t* n) {
+  if (!u || !n) return XF_ERR_ARG;
+  int64_t s = 0;
+  for (const Layer& y : u->ly) s += y.nw + y.co;
+  *n = s;
+  return XF_OK;
+}
+
+// Parameters as one FP32 array: per layer W[27][co][ci] then b[co], layers in
+// network order.  Padding weights (input channels 1..15 of the first layer,
+// output channels 1..15 of the last) are forced to 0.
+static int params_io(xf_unet* u, float* host, int which, bool upload) {
+  xf_ctx* ctx = u->ctx;
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int64_t o = 0;
+  for (int k = 0; k < NLAYER; k++) {
+    Layer& y = u->ly[k];
+    float* w = which == 0 ? y.w : y.gw;
+    float* b = which == 0 ? y.b : y.gb;
+    if (upload) {
+      std::vector<float> hw(host + o, host + o + y.nw), hb(host + o + y.nw, host + o + y.nw + y.co);
+      for (int t = 0; t < 27; t++)
+        for (int co = 0; co < y.co; co++)
+          for (int ci = 0; ci < y.ci; ci++)
+            if ((k == ENC0A && ci > 0) || (k == OUTL && co > 0)) hw[((size_t)t * y.co + co) * y.ci + ci] = 0.f;
+      if (k == OUTL)
+        for (int co = 1; co < y.co; co++) hb[co] = 0.f;
+      XF_CUDA(ctx, cudaMemcpy(w, hw.data(), y.nw * 4, cudaMemcpyHostToDevice));
+      XF_CUDA(ctx, cudaMemcpy(b, hb.data(), y.co * 4, cudaMemcpyHostToDevice));
+      if (which == 0)
+        k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, ctx->stream>>>(y.w, y.co, y.ci, y.w16, y.wt16);
+    } else {
+      XF_CUDA(ctx, cudaMemcpy(host + o, w, y.nw * 4, cudaMemcpyDeviceToHost));
+      XF_CUDA(ctx, cudaMemcpy(host + o + y.nw, b, y.co * 4, cudaMemcpyDeviceToHost));
+    }
+    o += y.nw + y.co;
+  }
+  XF_CUDA(ctx, cudaGetLastError());
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return XF_OK;
+}
+
+extern "C" int xf_unet_set_params(xf_unet* u, const float* host) {
+  if (!u || !host) return XF_ERR_ARG;
+  u->step = 0;
+  for (Layer& y : u->ly) {   // a new parameter set restarts Adam
+    cudaMemsetAsync(y.mw, 0, y.nw * 4, u->ctx->stream); cudaMemsetAsync(y.vw, 0, y.nw * 4, u->ctx->stream);
+    cudaMemsetAsync(y.mb, 0, y.co * 4, u->ctx->stream); cudaMemsetAsync(y.vb, 0, y.co * 4, u->ctx->stream);
+  }
+  return params_io(u, const_cast<float*>(host), 0, true);
+}
+extern "C" int xf_unet_get_params(xf_unet* u, float* host) {
+  if (!u || !host) return XF_ERR_ARG;
+  return params_io(u, host, 0, false);
+}
+extern "C" int xf_unet_get_grads(xf_unet* u, float* host) {
+  if (!u || !host) return XF_ERR_ARG;
+  return params_io(u, host, 1, false);
+}
+
+// ---------------------------------------------------------------------------
+// Forward pass on the residual box r (FP64, the grid's layout); the output
+// (FP32, level-0 box) lands in u->zout.
+static int conv(xf_unet* u, int k, const Act& in, int in_off, void* out, int out_ld, int out_ch, int out_fp32) {
+  const Layer& y = u->ly[k];
+  const Level& L = u->L[LLEV[k]];
+  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, in.p0(u->L) + in_off, in.C, y.ci, y.w16, y.b, y.co, L.mask, out,
+                        out_ld, out_ch, out_fp32, LRELU[k], nullptr, 0);
+}
+// Input gradient of layer k from its pre-activation gradient g: the convolution
+// with the flipped transposed weights, x mask, x the ReLU gate of `gate` (the
+// input activation) when given.
+static int dgrad(xf_unet* u, int k, const Act& g, void* out, int out_ld, const Act* gate, int gate_off) {
+  const Layer& y = u->ly[k];
+  const Level& L = u->L[LLEV[k]];
+  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, g.p0(u->L), g.C, y.co, y.wt16, nullptr, y.ci, L.mask, out, out_ld,
+                        y.ci, 0, 0, gate ? (const void*)(gate->p0(u->L) + gate_off) : nullptr, gate ? gate->C : 0);
+}
+static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_off) {
+  const Layer& y = u->ly[k];
+  const Level& L = u->L[LLEV[k]];
+  const int chunk = 4096;
+  dim3 grid((unsigned)((L.n + chunk - 1) / chunk), 27);
+  const size_t smem = (size_t)WG_CELLS * (y.co + y.ci) * 4;
+  k_wgrad<<<grid, 256, smem, u->ctx->stream>>>(g.p0(u->L), g.C, x.p0(u->L) + x_off, x.C, y.ci, y.co, L.n2, L.n3, L.n,
+                                                 chunk, y.gw, y.gb);
+}
+
+static int forward(xf_unet* u, const double* r) {
+  xf_ctx* ctx = u->ctx;
+  cudaStream_t s = ctx->stream;
+  const Level* L = u->L;
+  int st;
+  XF_CUDA(ctx, cudaMemsetAsync(u->red, 0, 8 * 8, s));
+  k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0);
+  k_unet_input<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, (double)L[0].active,
+                                                    u->X0.p0(L));
+  if ((st = conv(u, ENC0A, u->X0, 0, u->A0.p0(L), 16, 16, 0))) return st;
+  if ((st = conv(u, ENC0B, u->A0, 0, u->CAT0.p0(L) + 32, 48, 16, 0))) return st;   // S0
+  k_pool<<<ublocks(ctx, L[1].n * 16), 256, 0, s>>>(u->CAT0.p0(L) + 32, 48, L[0].n2, L[0].n3, u->P1.p0(L), 16,
+                                                   L[1].mask, L[1].n1, L[1].n2, L[1].n3, 16);
+  if ((st = conv(u, ENC1A, u->P1, 0, u->A1.p0(L), 32, 32, 0))) return st;
+  if ((st = conv(u, ENC1B, u->A1, 0, u->CAT1.p0(L) + 64, 96, 32, 0))) return st;   // S1
+  k_pool<<<ublocks(ctx, L[2].n * 32), 256, 0, s>>>(u->CAT1.p0(L) + 64, 96, L[1].n2, L[1].n3, u->P2.p0(L), 32,
+                                                   L[2].mask, L[2].n1, L[2].n2, L[2].n3, 32);
+  if ((st = conv(u, MIDA, u->P2, 0, u->M2a.p0(L), 64, 64, 0))) return st;
+  if ((st = conv(u, MIDB, u->M2a, 0, u->M2b.p0(L), 64, 64, 0))) return st;
+  k_upsample<<<ublocks(ctx, L[1].n * 64), 256, 0, s>>>(u->M2b.p0(L), 64, L[2].n2, L[2].n3, u->CAT1.p0(L), 96,
+                                                       L[1].mask, L[1].n1, L[1].n2, L[1].n3, 64);
+  if ((st = conv(u, DEC1A, u->CAT1, 0, u->D1a.p0(L), 32, 32, 0))) return st;
+  if ((st = conv(u, DEC1B, u->D1a, 0, u->D1b.p0(L), 32, 32, 0))) return st;
+  k_upsample<<<ublocks(ctx, L[0].n * 32), 256, 0, s>>>(u->D1b.p0(L), 32, L[1].n2, L[1].n3, u->CAT0.p0(L), 48,
+                                                       L[0].mask, L[0].n1, L[0].n2, L[0].n3, 32);
+  if ((st = conv(u, DEC0A, u->CAT0, 0, u->D0a.p0(L), 16, 16, 0))) return st;
+  if ((st = conv(u, DEC0B, u->D0a, 0, u->D0b.p0(L), 16, 16, 0))) return st;
+  if ((st = conv(u, OUTL, u->D0b, 0, u->zout, 1, 1, 1))) return st;
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// Backward pass from the loss against the target e (FP64 box): weight and
+// bias gradients accumulate into gw / gb.
+static int backward(xf_unet* u, const double* r, const double* e, const xf_op* op) {
+  xf_ctx* ctx = u->ctx;
+  cudaStream_t s = ctx->stream;
+  const Level* L = u->L;
+  int st;
+  if (op) {   // A-norm loss
+    k_f2d_mask<<<ublocks(ctx, L[0].n), 256, 0, s>>>(u->zout, L[0].mask, L[0].n, u->zd);
+    MvReq<double> m;
+    m.x = u->zd; m.y = u->az; m.zero_inactive = 1;
+    xf_mv64(op, m);
+    xf_dot_async(u->g, XF_F64, u->zd, r, 10);
+    xf_dot_async(u->g, XF_F64, u->zd, u->az, 11);
+    xf_dot_async(u->g, XF_F64, e, r, 12);
+    k_anorm_grad<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, u->az, L[0].mask, L[0].n, ctx->scratch, u->red,
+                                                      u->G0_16a.p0(L));
+  } else {
+    k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1);
+    k_unet_loss<<<ublocks(ctx, L[0].n), 256, 0, s>>>(u->zout, e, L[0].mask, L[0].n, (double)L[0].active, u->red,
+                                                     u->G0_16a.p0(L));
+  }
+  // out, dec0b, dec0a
+  wgrad(u, OUTL, u->G0_16a, u->D0b, 0);
+  if ((st = dgrad(u, OUTL, u->G0_16a, u->G0_16b.p0(L), 16, &u->D0b, 0))) return st;
+  wgrad(u, DEC0B, u->G0_16b, u->D0a, 0);
+  if ((st = dgrad(u, DEC0B, u->G0_16b, u->G0_16a.p0(L), 16, &u->D0a, 0))) return st;
+  wgrad(u, DEC0A, u->G0_16a, u->CAT0, 0);
+  if ((st = dgrad(u, DEC0A, u->G0_16a, u->G0_48.p0(L), 48, nullptr, 0))) return st;
+  // up(D1b) part -> dec1b's pre-activation gradient
+  k_upsample_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G0_48.p0(L), 48, L[0].n2, L[0].n3, u->D1b.p0(L), 32,
+                                                           L[1].mask, L[1].n1, L[1].n2, L[1].n3, u->G1_32a.p0(L), 32,
+                                                           32);
+  wgrad(u, DEC1B, u->G1_32a, u->D1a, 0);
+  if ((st = dgrad(u, DEC1B, u->G1_32a, u->G1_32b.p0(L), 32, &u->D1a, 0))) return st;
+  wgrad(u, DEC1A, u->G1_32b, u->CAT1, 0);
+  if ((st = dgrad(u, DEC1A, u->G1_32b, u->G1_96.p0(L), 96, nullptr, 0))) return st;
+  // up(M2b) part -> mid_b
+  k_upsample_bwd<<<ublocks(ctx, L[2].n * 64), 256, 0, s>>>(u->G1_96.p0(L), 96, L[1].n2, L[1].n3, u->M2b.p0(L), 64,
+                                                           L[2].mask, L[2].n1, L[2].n2, L[2].n3, u->G2_64a.p0(L), 64,
+                                                           64);
+  wgrad(u, MIDB, u->G2_64a, u->M2a, 0);
+  if ((st = dgrad(u, MIDB, u->G2_64a, u->G2_64b.p0(L), 64, &u->M2a, 0))) return st;
+  wgrad(u, MIDA, u->G2_64b, u->P2, 0);
+  if ((st = dgrad(u, MIDA, u->G2_64b, u->G2_32.p0(L), 32, nullptr, 0))) return st;
+  k_pool_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G2_32.p0(L), 32, L[2].n2, L[2].n3, L[1].mask, L[1].n1,
+                                                       L[1].n2, L[1].n3, u->gsum1, 32, 32);
+  // S1 = enc1b output: skip gradient + pooled path
+  k_skip_grad<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G1_96.p0(L) + 64, 96, u->gsum1, 32, u->CAT1.p0(L) + 64,
+                                                        96, L[1].mask, L[1].n, u->G1_32a.p0(L), 32, 32);
+  wgrad(u, ENC1B, u->G1_32a, u->A1, 0);
+  if ((st = dgrad(u, ENC1B, u->G1_32a, u->G1_32b.p0(L), 32, &u->A1, 0))) return st;
+  wgrad(u, ENC1A, u->G1_32b, u->P1, 0);
+  if ((st = dgrad(u, ENC1A, u->G1_32b, u->G1_16.p0(L), 16, nullptr, 0))) return st;
+  k_pool_bwd<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G1_16.p0(L), 16, L[1].n2, L[1].n3, L[0].mask, L[0].n1,
+                                                       L[0].n2, L[0].n3, u->gsum, 16, 16);
+  k_skip_grad<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G0_48.p0(L) + 32, 48, u->gsum, 16, u->CAT0.p0(L) + 32,
+                                                        48, L[0].mask, L[0].n, u->G0_16a.p0(L), 16, 16);
+  wgrad(u, ENC0B, u->G0_16a, u->A0, 0);
+  if ((st = dgrad(u, ENC0B, u->G0_16a, u->G0_16b.p0(L), 16, &u->A0, 0))) return st;
+  wgrad(u, ENC0A, u->G0_16b, u->X0, 0);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+static int check_box(const xf_unet* u, const xf_vec* v, const char* who) {
+  if (!v || v->g != u->g || v->dtype != XF_F64)
+    return xf_fail(u->ctx, XF_ERR_STATE, "%s: FP64 boxes of the network's grid expected", who);
+  return XF_OK;
+}
+
+// z = U-Net(r), FP64 box (0 on inactive cells).
+int xf_unet_apply_dev(xf_unet* u, const double* r, double* z) {
+  int st = forward(u, r);
+  if (st) return st;
+  k_f2d_mask<<<ublocks(u->ctx, u->L[0].n), 256, 0, u->ctx->stream>>>(u->zout, u->L[0].mask, u->L[0].n, z);
+  XF_CUDA(u->ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+extern "C" int xf_unet_apply(xf_unet* u, const xf_vec* r, xf_vec* z) {
+  if (!u) return XF_ERR_ARG;
+  int st;
+  if ((st = check_box(u, r, "xf_unet_apply")) || (st = check_box(u, z, "xf_unet_apply"))) return st;
+  XF_CUDA(u->ctx, cudaSetDevice(u->ctx->device));
+  if ((st = xf_unet_apply_dev(u, (const double*)r->data, (double*)z->data))) return st;
+  return xf_conv_status(u->ctx);
+}
+
+extern "C" int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, const xf_vec* e, double lr,
+                                  int apply_update, double* loss) {
+  if (!u) return XF_ERR_ARG;
+  int st;
+  if ((st = check_box(u, r, "xf_unet_train_step")) || (st = check_box(u, e, "xf_unet_train_step"))) return st;
+  if (op && (op->g != u->g || op->kind == XF_OP_PACK))
+    return xf_fail(u->ctx, XF_ERR_ARG, "xf_unet_train_step: the operator must be a stencil operator of the network's grid");
+  if (op && (st = xf_op_ready(op))) return st;
+  xf_ctx* ctx = u->ctx;
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  for (Layer& y : u->ly) {
+    XF_CUDA(ctx, cudaMemsetAsync(y.gw, 0, y.nw * 4, s));
+    XF_CUDA(ctx, cudaMemsetAsync(y.gb, 0, y.co * 4, s));
+  }
+  if ((st = forward(u, (const double*)r->data))) return st;
+  if ((st = backward(u, (const double*)r->data, (const double*)e->data, op))) return st;
+  if (apply_update) {
+    u->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)u->step), c2 = 1.f - powf(b2, (float)u->step);
+    for (Layer& y : u->ly) {
+      k_adam<<<ublocks(ctx, y.nw), 256, 0, s>>>(y.w, y.gw, y.mw, y.vw, y.nw, (float)lr, b1, b2, 1e-8f, c1, c2, 0);
+      k_adam<<<1, 256, 0, s>>>(y.b, y.gb, y.mb, y.vb, y.co, (float)lr, b1, b2, 1e-8f, c1, c2, 0);
+      k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, s>>>(y.w, y.co, y.ci, y.w16, y.wt16);
+    }
+  }
+  XF_CUDA(ctx, cudaGetLastError());
+  if (loss) {
+    XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, u->red + 2, 8, cudaMemcpyDeviceToHost, s));
+  }
+  if ((st = xf_conv_status(ctx))) return st;   // synchronises
+  if (loss) *loss = ctx->host_scalars[0];
+  return XF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Flexible CG, truncated FCG(m) (Notay's flexible CG): each new preconditioned
+// residual z = M(r) is A-orthogonalised against the last m search directions,
+//     p = z - sum_j ((z, A p_j) / (p_j, A p_j)) p_j,
+// which keeps the method robust to a preconditioner that varies from one
+// application to the next (a network), then x += alpha p, r -= alpha A p with
+// alpha = (p, r) / (p, A p).  FP64 vectors and dots.  Plain CG stays the
+// fallback and the judge: an iteration whose z is no descent direction
+// ((z, r) <= 0) uses z = r, and when the residual has not dropped by 10% over
+// 50 iterations the preconditioner is switched off for the rest of the solve
+// (both counted in stats->fallbacks).  The stop rule is the true relative
+// residual ||b - A x|| <= rtol ||b||.  m = opts->reserved[0] (1..8, default 8).
+__global__ void k_fcg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                             const double* __restrict__ q, double alpha, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    x[c] += alpha * p[c];
+    r[c] -= alpha * q[c];
+  }
+}
+__global__ void k_axpy_d(double* __restrict__ y, const double* __restrict__ x, double a, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    y[c] += a * x[c];
+}
+__global__ void k_jacobi(const double* __restrict__ r, const double* __restrict__ diag, const uint8_t* __restrict__ kind,
+                         int64_t n, double* __restrict__ z) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const double d = diag[c];
+    z[c] = (row_of(kind[c]) == ROW_ACTUAL && d > 0) ? r[c] / d : r[c];
+  }
+}
+
+// scalar slots: 0..7 (z, A p_j); 10 (z, r); 11 (r, r); 12 (p, r); 14/15 matvec dots
+enum { FS_ZR = 10, FS_RR = 11, FS_PR = 12, FS_PQ = 14 };
+
+static int read_n(xf_ctx* ctx, int first, int count, double* out) {
+  XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->scalars[first], count * 8, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int q = 0; q < count; q++) out[q] = ctx->host_scalars[q];
+  return XF_OK;
+}
+
+extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* xv, const xf_vec* bv,
+                            xf_solve_stats* st) {
+  if (!op || !xv || !bv || !st) return XF_ERR_ARG;
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  if (xv->g != g || bv->g != g || xv->dtype != XF_F64 || bv->dtype != XF_F64)
+    return xf_fail(ctx, XF_ERR_STATE, "xf_solve_fcg: x and b must be FP64 boxes of the operator's grid");
+  xf_solve_opts o;
+  if (opts) o = *opts;
+  else xf_solve_opts_default(&o);
+  if (o.maxit <= 0) o.maxit = 100000;
+  if (o.rtol <= 0) o.rtol = 1e-8;
+  const int m = o.reserved[0] > 0 ? (o.reserved[0] > 8 ? 8 : o.reserved[0]) : 8;
+  if (o.precond == XF_PRECOND_UNET && (!u || u->g != g))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_solve_fcg: XF_PRECOND_UNET needs a network built on the operator's grid");
+  if (o.precond == XF_PRECOND_JACOBI && op->kind != XF_OP_LAPLACE)
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve_fcg: Jacobi uses the Laplace diagonal");
+  int rc;
+  if ((rc = xf_op_ready(op))) return rc;
+  memset(st, 0, sizeof(*st));
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int64_t n = g->ncell;
+  std::vector<double*> bufs;
+  auto buf = [&]() -> double* {
+    double* p = nullptr;
+    if (cudaMalloc(&p, n * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    cudaMemsetAsync(p, 0, n * 8, ctx->stream);
+    bufs.push_back(p);
+    return p;
+  };
+  auto cleanup = [&]() {
+    for (double* p : bufs) cudaFree(p);
+  };
+  double *r = buf(), *z = buf(), *pn = buf(), *qn = buf();
+  double *P[8] = {nullptr}, *Q[8] = {nullptr};
+  bool okb = r && z && pn && qn;
+  for (int j = 0; j < m && okb; j++) okb = (P[j] = buf()) && (Q[j] = buf());
+  if (!okb) {
+    cleanup();
+    return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve_fcg: allocation");
+  }
+  double pq_win[8] = {0};
+  cudaStream_t s = ctx->stream;
+  const int eb = grid_blocks(ctx, n, 256);
+  double* x = (double*)xv->data;
+  const double* b = (const double*)bv->data;
+  int precond = o.precond;
+  auto fail = [&](int code, const char* msg) {
+    cleanup();
+    return xf_fail(ctx, code, "xf_solve_fcg: %s", msg);
+  };
+  auto apply_m = [&]() -> int {   // z = M r
+    if (precond == XF_PRECOND_UNET) return xf_unet_apply_dev(u, r, z);
+    if (precond == XF_PRECOND_JACOBI) {
+      k_jacobi<<<eb, 256, 0, s>>>(r, g->diag, g->kind, n, z);
+      return XF_OK;
+    }
+    return cudaMemcpyAsync(z, r, n * 8, cudaMemcpyDeviceToDevice, s) == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+  };
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  {
+    MvReq<double> mv;   // r = b - A x (zero off the active set)
+    mv.x = x; mv.y = r; mv.s = b; mv.sign = -1; mv.neg = 1; mv.zero_inactive = 1;
+    xf_mv64(op, mv);
+  }
+  xf_dot_async(g, XF_F64, b, b, FS_RR);
+  double bb;
+  if ((rc = read_n(ctx, FS_RR, 1, &bb))) return fail(rc, "scalar read");
+  const double thr = o.rtol * o.rtol * bb;
+  xf_dot_async(g, XF_F64, r, r, FS_RR);
+  double rr;
+  if ((rc = read_n(ctx, FS_RR, 1, &rr))) return fail(rc, "scalar read");
+  int it = 0, nwin = 0, head = 0, status = XF_OK;
+  double rr_mark = rr;
+  int mark_it = 0;
+  while (rr > thr) {
+    if (it >= o.maxit) { status = XF_MAXIT; break; }
+    if (std::isnan(rr)) { status = XF_NAN; break; }
+    it++;
+    if ((rc = apply_m())) return fail(rc, "preconditioner");
+    xf_dot_async(g, XF_F64, z, r, FS_ZR);
+    double zr;
+    if ((rc = read_n(ctx, FS_ZR, 1, &zr))) return fail(rc, "scalar read");
+    if (!(zr > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
+      st->fallbacks++;
+      XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 8, cudaMemcpyDeviceToDevice, s));
+    }
+    // p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j over the window
+    XF_CUDA(ctx, cudaMemcpyAsync(pn, z, n * 8, cudaMemcpyDeviceToDevice, s));
+    if (nwin > 0) {
+      for (int j = 0; j < nwin; j++) xf_dot_async(g, XF_F64, z, Q[j], j);
+      double zq[8];
+      if ((rc = read_n(ctx, 0, nwin, zq))) return fail(rc, "scalar read");
+      for (int j = 0; j < nwin; j++)
+        if (pq_win[j] > 0) k_axpy_d<<<eb, 256, 0, s>>>(pn, P[j], -zq[j] / pq_win[j], n);
+    }
+    MvReq<double> mv;   // q = A p, (p, q)
+    mv.x = pn; mv.y = qn; mv.w = pn; mv.zero_inactive = 1; mv.slot = FS_PQ;
+    xf_mv64(op, mv);
+    xf_dot_async(g, XF_F64, pn, r, FS_PR);
+    double pq, pr;
+    if ((rc = read_n(ctx, FS_PQ, 1, &pq)) || (rc = read_n(ctx, FS_PR, 1, &pr))) return fail(rc, "scalar read");
+    if (!(pq > 0)) { status = std::isnan(pq) ? XF_NAN : XF_BREAKDOWN; break; }
+    const double alpha = pr / pq;
+    k_fcg_update<<<eb, 256, 0, s>>>(x, r, pn, qn, alpha, n);
+    // the new direction joins the window (ring of m)
+    XF_CUDA(ctx, cudaMemcpyAsync(P[head], pn, n * 8, cudaMemcpyDeviceToDevice, s));
+    XF_CUDA(ctx, cudaMemcpyAsync(Q[head], qn, n * 8, cudaMemcpyDeviceToDevice, s));
+    pq_win[head] = pq;
+    head = (head + 1) % m;
+    if (nwin < m) nwin++;
+    xf_dot_async(g, XF_F64, r, r, FS_RR);
+    if ((rc = read_n(ctx, FS_RR, 1, &rr))) return fail(rc, "scalar read");
+    if (it - mark_it >= 50) {   // stall watch
+      if (precond != XF_PRECOND_NONE && !(rr < 0.81 * rr_mark)) {
+        precond = XF_PRECOND_NONE;
+        st->fallbacks++;
+      }
+      rr_mark = rr;
+      mark_it = it;
+    }
+  }
+  {
+    MvReq<double> mv;   // true residual
+    mv.x = x; mv.y = qn; mv.s = b; mv.sign = -1; mv.neg = 1; mv.zero_inactive = 1; mv.dot_self = 1; mv.slot = FS_PQ;
+    xf_mv64(op, mv);
+  }
+  double tr[2];
+  if ((rc = read_n(ctx, FS_PQ, 2, tr))) return fail(rc, "scalar read");
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+  XF_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  cleanup();
+  if (o.precond == XF_PRECOND_UNET && (rc = xf_conv_status(ctx))) return rc;
+  const double rel = bb > 0 ? sqrt(tr[1] / bb) : sqrt(tr[1]);
+  st->status = status == XF_OK && rel > o.rtol ? XF_STALL : status;
+  st->iterations = it;
+  st->rel_resid = rel;
+  st->abs_resid = sqrt(tr[1]);
+  st->ms = ms;
+  return XF_OK;
+}
