@@ -196,6 +196,10 @@ def main():
     ap.add_argument("--impl", default="xflow", choices=["xflow", "reference"])
     ap.add_argument("--size", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--learned", action="store_true",
+                    help="train the U-Net preconditioner and time it and its flexible CG at full size")
+    ap.add_argument("--learned-applies-only", action="store_true", help="with --learned: no solves")
+    ap.add_argument("--learned-max-its", type=int, default=0, help="with --learned: cap of the learned solve")
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV)")
     ap.add_argument("--kernels-only", action="store_true",
@@ -207,6 +211,8 @@ def main():
         return kernels_only(args)
     if args.rows:
         return rows(args)
+    if args.learned:
+        return learned(args)
 
     import xflow_gb300 as xf
 
@@ -484,6 +490,106 @@ def rows(args):
     ncell = int(np.prod(g.shape))
     report("a9 packed operator SpMV (XOperator.cpp:1550-1571)", f"256^3 spheres, {rows_} rows, {nnz} nonzeros", ms,
            ncell * 1 + rows_ * (4 + 8 + 1) + nnz * (8 + 4) + rows_ * 8 * 2, build_ms=build_ms)
+    return 0
+
+
+UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=(200, 201, 202), iters=(2, 5, 10, 20, 40, 80, 120, 160, 240),
+                  steps=600, lr=2e-3)
+
+
+def unet_flops(shape):
+    """Tensor-core FLOPs of one U-Net application on a box: executed (padded
+    channels) and useful (1 input and 1 output channel in the end layers)."""
+    import xflow_gb300 as xf
+
+    cells, dims = [], list(shape)
+    for _ in range(3):
+        cells.append(int(np.prod(dims)))
+        dims = [(d - 2) // 2 + 2 for d in dims]
+    lev = {"enc0a": 0, "enc0b": 0, "enc1a": 1, "enc1b": 1, "mid_a": 2, "mid_b": 2, "dec1a": 1, "dec1b": 1,
+           "dec0a": 0, "dec0b": 0, "out": 0}
+    ex = us = 0
+    for name, ci, co in xf.UNET_LAYERS:
+        n = cells[lev[name]]
+        ex += 2 * 27 * ci * co * n
+        us += 2 * 27 * (1 if name == "enc0a" else ci) * (1 if name == "out" else co) * n
+    return ex, us
+
+
+def learned(args):
+    """The learned preconditioner at the bench's 256^3 system: a U-Net trained
+    on the GPU (this library's forward/backward kernels, Adam, the A-norm
+    loss) on (residual, error) pairs harvested from plain CG's own iterates on
+    a 64^3 system of the same sphere family, then applied by flexible CG
+    FCG(8) at full size.  Prints one JSON line: training time and loss, the
+    U-Net application time and tensor FLOP rate, and the learned FCG solve
+    (iterations, ms, true residual) beside plain FP64 CG on the same system.
+    --learned-max-its caps the learned solve (0: to the tolerance)."""
+    import torch
+
+    import xflow_gb300 as xf
+    from xflow_gb300 import workloads as wl
+
+    ctx = xf.Context(0)
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    T = UNET_TRAIN
+    codes, nrm, _, sep, _ = wl.spheres_grid(T["n"], T["spheres"], 0.02, 0.06, T["seed"])
+    g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
+    A = xf.Operator(g)
+    net = xf.UNet(g, seed=1)
+    t0 = time.perf_counter()
+    rs, es = [], []
+    for s in T["rhs_seeds"]:
+        b = wl.divergence_rhs(codes, (sep,) * 3, s)
+        r_, e_ = xf.harvest_pairs(A, g.vec(b), iters=T["iters"])
+        rs += r_
+        es += e_
+    first = float(np.mean([net.train_step(r, e, update=False, op=A) for r, e in zip(rs, es)]))
+    t1 = time.perf_counter()
+    for step in range(T["steps"]):
+        q = step % len(rs)
+        net.train_step(rs[q], es[q], lr=T["lr"], op=A)
+    ctx.synchronize()
+    t2 = time.perf_counter()
+    last = float(np.mean([net.train_step(r, e, update=False, op=A) for r, e in zip(rs, es)]))
+    params = net.params()
+    codes2, sep2, b2 = workload(args.size)
+    g2 = xf.Grid(ctx, codes2, sep2, sep2, sep2, None)
+    A2 = xf.Operator(g2)
+    net2 = xf.UNet(g2, params)
+    bv = g2.vec(b2)
+    z = g2.vec(None)
+    for _ in range(2):
+        net2.apply(bv, z)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record(stream)
+    for _ in range(reps):
+        net2.apply(bv, z)
+    e1.record(stream)
+    e1.synchronize()
+    apply_ms = e0.elapsed_time(e1) / reps
+    ex, us = unet_flops(g2.shape)
+    line = {"mode": "learned preconditioner", "workload": f"{args.size}^3 spheres system (the bench's)",
+            "train": {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
+                      "steps": T["steps"], "lr": T["lr"], "s": t2 - t1, "harvest_s": t1 - t0,
+                      "anorm_loss_before": first, "anorm_loss_after": last},
+            "unet_apply_ms": apply_ms, "tensor_tflops_executed": ex / (apply_ms * 1e-3) / 1e12,
+            "tensor_tflops_useful": us / (apply_ms * 1e-3) / 1e12, "tflop_per_apply": ex / 1e12}
+    if not args.learned_applies_only:
+        maxit = args.learned_max_its if args.learned_max_its > 0 else 100000
+        x = g2.vec(np.zeros(g2.shape))
+        st = xf.solve_fcg(A2, x, bv, unet=net2, rtol=RTOL, maxit=maxit)
+        line["learned_fcg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid,
+                               "status": int(st.status), "fallbacks": st.fallbacks, "window": 8}
+        x = g2.vec(np.zeros(g2.shape))
+        st = xf.solve(A2, x, bv, method=xf.XF_CG, rtol=RTOL)
+        line["plain_fp64_cg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid}
+        x = g2.vec(np.zeros(g2.shape))
+        st = xf.solve(A2, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL)
+        line["mixed_fp32_cg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid}
+    print(json.dumps(line))
     return 0
 
 

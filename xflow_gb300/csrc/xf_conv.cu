@@ -279,8 +279,12 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
   a.out_ld = out_ld; a.out_ch = out_ch; a.relu = relu; a.err = err;
   const size_t smem = (size_t)CONV_STAGES * (TC_M * ci * 2 + co * ci * 2);
   XF_CUDA(ctx, cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  XF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc, 128, smem));
+  // Residency from the kernel's real limits: shared memory (227 KB per SM, with
+  // ~1 KB static and reserved per CTA), tensor-memory columns (512 per SM) and
+  // threads (2048 per SM).
+  int per_sm = (int)((227 * 1024) / (smem + 2048));
+  per_sm = min(per_sm, (int)(512 / tmem_cols(co)));
+  per_sm = min(per_sm, 16);
   if (per_sm < 1) per_sm = 1;
   const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
   int64_t blocks = (int64_t)ctx->sm_count * per_sm;

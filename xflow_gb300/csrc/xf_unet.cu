@@ -148,20 +148,22 @@ __global__ void k_pool_bwd(const uint16_t* __restrict__ gcoarse, int gld, int c2
   }
 }
 
-// Nearest upsampling of a coarse slice into a fine slice, times the fine mask.
+// Nearest upsampling of a coarse slice into a fine slice, times the fine mask;
+// 8 channels (16 bytes) per thread (C, pitches and slice offsets are multiples of 8).
 __global__ void k_upsample(const uint16_t* __restrict__ src, int sld, int c2, int c3, uint16_t* __restrict__ dst,
                            int dld, const uint8_t* __restrict__ fmask, int f1, int f2, int f3, int C) {
-  const int64_t n = (int64_t)f1 * f2 * f3 * C;
+  const int C8 = C / 8;
+  const int64_t n = (int64_t)f1 * f2 * f3 * C8;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = u / C;
-    const int ch = (int)(u - c * C);
-    uint16_t v = 0;
+    const int64_t c = u / C8;
+    const int ch = (int)(u - c * C8) * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
     if (fmask[c]) {
       const int i = (int)(c / ((int64_t)f2 * f3)), j = (int)((c / f3) % f2), k = (int)(c % f3);
       const int64_t pc = ((int64_t)(1 + (i - 1) / 2) * c2 + (1 + (j - 1) / 2)) * c3 + (1 + (k - 1) / 2);
-      v = src[pc * sld + ch];
+      v = *reinterpret_cast<const uint4*>(src + pc * sld + ch);
     }
-    dst[c * dld + ch] = v;
+    *reinterpret_cast<uint4*>(dst + c * dld + ch) = v;
   }
 }
 
@@ -591,11 +593,11 @@ static int forward(xf_unet* u, const double* r) {
                                                    L[2].mask, L[2].n1, L[2].n2, L[2].n3, 32);
   if ((st = conv(u, MIDA, u->P2, 0, u->M2a.p0(L), 64, 64, 0))) return st;
   if ((st = conv(u, MIDB, u->M2a, 0, u->M2b.p0(L), 64, 64, 0))) return st;
-  k_upsample<<<ublocks(ctx, L[1].n * 64), 256, 0, s>>>(u->M2b.p0(L), 64, L[2].n2, L[2].n3, u->CAT1.p0(L), 96,
+  k_upsample<<<ublocks(ctx, L[1].n * 8), 256, 0, s>>>(u->M2b.p0(L), 64, L[2].n2, L[2].n3, u->CAT1.p0(L), 96,
                                                        L[1].mask, L[1].n1, L[1].n2, L[1].n3, 64);
   if ((st = conv(u, DEC1A, u->CAT1, 0, u->D1a.p0(L), 32, 32, 0))) return st;
   if ((st = conv(u, DEC1B, u->D1a, 0, u->D1b.p0(L), 32, 32, 0))) return st;
-  k_upsample<<<ublocks(ctx, L[0].n * 32), 256, 0, s>>>(u->D1b.p0(L), 32, L[1].n2, L[1].n3, u->CAT0.p0(L), 48,
+  k_upsample<<<ublocks(ctx, L[0].n * 4), 256, 0, s>>>(u->D1b.p0(L), 32, L[1].n2, L[1].n3, u->CAT0.p0(L), 48,
                                                        L[0].mask, L[0].n1, L[0].n2, L[0].n3, 32);
   if ((st = conv(u, DEC0A, u->CAT0, 0, u->D0a.p0(L), 16, 16, 0))) return st;
   if ((st = conv(u, DEC0B, u->D0a, 0, u->D0b.p0(L), 16, 16, 0))) return st;
