@@ -201,7 +201,8 @@ def main():
     ap.add_argument("--learned-applies-only", action="store_true", help="with --learned: no solves")
     ap.add_argument("--learned-max-its", type=int, default=0, help="with --learned: cap of the learned solve")
     ap.add_argument("--rows", action="store_true",
-                    help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV)")
+                    help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
+    ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
     ap.add_argument("--kernels-only", action="store_true",
                     help="a few launches of each hot kernel on the full grid (for ncu captures)")
     args = ap.parse_args()
@@ -389,10 +390,11 @@ def rows(args):
     `reps` calls; the calls that check the reference's throw conditions read a
     few bytes back inside the timed region):
       channel 256x64x64 (the immersed-body config): pressure RHS, velocity
-        correction (u), control balance, IB interpolate / forces / spread with
-        an icosphere of 2562 markers, Thomas lines along x;
+        correction (u), control balance, momentum RHS (u), IB interpolate /
+        forces / spread with an icosphere of 2562 markers, Thomas lines along
+        x, the VTK volume (with the oracle's fprintf writer timed beside it);
       512x128x128 (the full time loop config): pressure RHS, velocity
-        correction, control balance;
+        correction, control balance, momentum RHS;
       256^3 spheres Poisson system: packed-operator build and its SpMV.
     Prints one JSON line per row with ms per call and algorithmic GB/s."""
     import torch
@@ -443,6 +445,12 @@ def rows(args):
         report("velocity correction u (XProblem.cpp:5598-5777)", name, ms, nuc * (1 + 8 + 8 + 8 + 8 + 8))
         ms = timed(lambda: xf.divergence_max(gp, u, v, w))
         report("control balance (XProblem.cpp:5782-5829)", name, ms, npc * (1 + 8 + 8 + 8))
+        vis = gp.vec(np.full(gp.shape, 0.01))
+        mom = tuple(gu.vec(None) for _ in range(5))
+        ms = timed(lambda: xf.momentum_rhs(1, gu, u, v, w, vis=vis, border=ub, out=mom))
+        # compulsory: code, u, v, w, vis, border in; uTr, vTr, wTr, visTr, rp out
+        report("momentum RHS u: staggered interpolation + viscous terms (XProblem.cpp:5088-5419)", name, ms,
+               nuc * (1 + 8 * 5 + 8 * 5))
         if n1 == 257:
             # Thomas lines along x of the u box: (n2 * n3) lines of n1-2 unknowns
             M, nl1, nl2, ls1, ls2, ms_ = xf.box_lines(gu.shape, 1)
@@ -471,6 +479,36 @@ def rows(args):
             report("a18 IB forces (XProblem.cpp:8436-8547)", name + f", {nn} markers", ms)
             ms = timed(lambda: mk.spread(un, h0, 1))
             report("a19 IB spread (XProblem.cpp:8550-8617)", name + f", {nn} markers", ms)
+        if n1 == 257:
+            # VTK volume of the step (node box one smaller than the pressure box)
+            node_codes = np.ascontiguousarray(cs["pc"][:-1, :-1, :-1])
+            xyz = [np.concatenate([[0.0], np.cumsum(h[:n - 2])]) for h, n in zip(cs["hP"], (n1, n2, n3))]
+            gn = xf.Grid(ctx, node_codes, *(np.diff(a) for a in xyz))
+            path = os.path.join(tempfile.gettempdir(), "xf_rows.vtk")
+            nbytes = [0]
+
+            def vtk():
+                nbytes[0] = xf.write_vtk(path, gn, *xyz, u, v, w, p, rho, rho, vis)
+
+            ms = timed(vtk, reps=3)
+            extra = {"file_bytes": nbytes[0], "text_MB_s": nbytes[0] / (ms * 1e-3) / 1e6}
+            if not args.rows_no_cpu:
+                from oracle import oracle as O   # the reference's writer loops through the C library's fprintf
+
+                t0 = time.perf_counter()
+                O.vtk_write(path + ".cpu", node_codes, *xyz, cs["u"], cs["v"], cs["w"], cs["pc"], cs["p"], cs["pc"],
+                            cs["density"], cs["pc"], cs["density"], np.full(gp.shape, 0.01))
+                extra["cpu_baseline_ms"] = (time.perf_counter() - t0) * 1e3
+                extra["cpu_baseline"] = "oracle restatement of the reference's VTK loops (fprintf), 1 thread"
+                extra["identical_to_cpu"] = open(path, "rb").read() == open(path + ".cpu", "rb").read()
+                os.remove(path + ".cpu")
+            report("VTK legacy ASCII volume (XProblem.cpp:6132-6345)", name + f", {int(np.prod(gn.shape))} nodes",
+                   ms, **extra)
+            os.remove(path)
+            gn.close()
+        vis.close()
+        for o in mom:
+            o.close()
         for o in (u, v, w, rho, pb, rhs, p, ub, un):
             o.close()
         for gg in (gp, gu, gv, gw):

@@ -140,6 +140,11 @@ int xf_op_set_density(xf_op* op, const double* host_density_box);
  * XF_BICGSTAB, XF_MINRES, or XF_BICG on its packed form. */
 int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, const xf_vec* w, double tau,
                         double diff_coef, int flags);
+/* Variable-viscosity form (the visTr overload of SolveTransferEquation__,
+ * XProblem.cpp:2784-3420, diffCoefVar[i][j][k] at :3204): d, an FP64 box of
+ * the operator's grid, is copied and replaces diff_coef cell by cell; NULL
+ * returns to the constant. */
+int xf_op_set_diffusion_field(xf_op* op, const xf_vec* d);
 
 /* Packed operator: replaces T1dPackOperator(model, A, &null) (XOperator.cpp:
  * 1135-1350) built from A (Laplace or variable-density, density set).  Rows
@@ -260,6 +265,54 @@ int xf_velocity_correct(int axis, const xf_vec* vel_prev, const xf_vec* p, const
  * (-1s when no cell beats 0). */
 int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, double* value,
                       int32_t* ijk);
+/* Momentum right-hand side of velocity equation `axis` (1 u, 2 v, 3 w),
+ * TVPProblem::SolveBySplitting XProblem.cpp:5088-5419, on the component's own
+ * grid (the grid of the five outputs, distinct FP64 vectors):
+ *  - Actual cells: the transfer velocities averaged onto the component's
+ *    nodes (4-point means of the other two components, :5108-5133), the face
+ *    viscosity (mean of the two pressure-box values of vis straddling the
+ *    node), rp = force (GetForce: the immersed-boundary forcing, NULL = 0),
+ *    then rp += dVis . (dVel + dU), central differences of those fields
+ *    (:5352-5419);
+ *  - Defined and PreDefined cells (and, for axis 1, Normal cells whose normal
+ *    is along x only): zero transfer fields, rp = border;
+ *  - Fictive cells: all zero.
+ * u_prev, v_prev, w_prev are the staggered boxes of the pressure box one layer
+ * longer than the component along `axis`; vis is that pressure box (NULL: 0);
+ * border and force are component boxes (NULL: 0).  Cells the reference throws
+ * on (Equation, PreNormal, PreEquation, other Normal cells, unknown codes, an
+ * Actual cell on the box face) return XF_ERR_MASK naming the first in its loop
+ * order.  Bit-identical to the reference's loops (FP64, no contraction). */
+int xf_momentum_rhs(int axis, const xf_vec* u_prev, const xf_vec* v_prev, const xf_vec* w_prev, const xf_vec* vis,
+                    const xf_vec* border, const xf_vec* force, xf_vec* u_tr, xf_vec* v_tr, xf_vec* w_tr,
+                    xf_vec* vis_tr, xf_vec* rp);
+
+/* ---- field output ----------------------------------------------------------- */
+/* VTK legacy ASCII volume of one time step, replacing the writer in
+ * TVPProblem::SolveBySplitting (XProblem.cpp:6132-6345), byte for byte:
+ * header, POINTS (node coordinates x[i], y[j], z[k] for node indices 1..N-1,
+ * 1..L-1, 1..M-1, k outermost), the velocity averaged from the staggered
+ * boxes onto the nodes (0 at Fictive nodes of `nodes`), then pressure,
+ * density, concentration and viscosity averaged over the 8 surrounding
+ * pressure-box cells (sum of all 8 over the count of non-Fictive ones in the
+ * field's own grid; viscosity counts with the concentration grid, as the
+ * reference does), every number as C's "%f" prints it.  nodes is the node
+ * grid, box (N+1) x (L+1) x (M+1); x, y, z host arrays of N+1, L+1, M+1
+ * coordinates; u, v, w the staggered boxes and p, density, conc, vis FP64
+ * vectors on their grids, box (N+2) x (L+2) x (M+2).  The text is formatted
+ * on the device and streamed to `path`; *bytes (optional) receives the file
+ * size.  Synchronous. */
+int xf_vtk_write(const char* path, const xf_grid* nodes, const double* x, const double* y, const double* z,
+                 const xf_vec* u, const xf_vec* v, const xf_vec* w, const xf_vec* p, const xf_vec* density,
+                 const xf_vec* conc, const xf_vec* vis, int64_t* bytes);
+/* "%f\n" of each of n host values, formatted on the device (the VTK
+ * writer's number formatting): *length receives the byte count; the text is
+ * stored into out when capacity allows (out may be NULL to query). */
+int xf_format_fixed6(xf_ctx* ctx, const double* values, int64_t n, char* out, int64_t capacity, int64_t* length);
+/* NPY file of a vector's box, shape (n1, n2, n3), '<f8' or '<f4', C order,
+ * with the header cnpy::npy_save writes (cnpy.h:66-112, 206-233; the time
+ * loop's NPY output, XProblem.cpp:6545-6590).  Synchronous. */
+int xf_npy_write(const char* path, const xf_vec* vec);
 
 /* ---- tridiagonal lines ---------------------------------------------------- */
 /* Replaces TSLAE::SolveByScalarRunning(M, u, a, b, c, f) (XSLAE.h:23,

@@ -16,6 +16,8 @@ LIB = os.path.join(HERE, "liboracle.so")
 LAPLACE, VARDIV = 0, 1
 
 
+XFO_OK, XFO_ERR_ARG, XFO_ERR_MASK, XFO_ERR_CHECK = 0, 1, 3, 7   # oracle status codes (xf_oracle.h)
+
 def build():
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
 
@@ -36,6 +38,8 @@ def lib():
         L.xfo_absmax.restype = C.c_double
         L.xfo_divergence_max.restype = C.c_double
         L.xfo_pack_build.restype = C.c_int64
+        L.xfo_format_fixed6.restype = C.c_int64
+        L.xfo_format_fixed6.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
         L.xfo_pack_apply.argtypes = [C.c_int64] + [C.c_void_p] * 5
         L.xfo_bicg_reference.argtypes = [C.c_int64] + [C.c_void_p] * 7 + [C.c_double, C.c_int, C.c_void_p,
                                                                           C.c_void_p]
@@ -234,6 +238,19 @@ def velocity_correct(axis, codes, prev, p, hP, tau, density=None, border=None, c
     return cur, st, bad.value
 
 
+def momentum_rhs(axis, codes, u, v, w, hx, hy, hz, vis=None, border=None, force=None, normals=None):
+    """Momentum right-hand side of velocity component `axis` on its own box (XProblem.cpp:5088-5419):
+    returns (uTr, vTr, wTr, visTr, rp), status, first throwing cell."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    out = [np.zeros(codes.shape) for _ in range(5)]
+    bad = C.c_int64(-1)
+    p = lambda a: _p(f64(a), C.c_double) if a is not None else None  # noqa: E731
+    st = lib().xfo_momentum_rhs(int(axis), _p(codes, C.c_int32), p(normals), *codes.shape, p(u), p(v), p(w), p(vis),
+                                p(hx), p(hy), p(hz), p(border), p(force), *(_p(o, C.c_double) for o in out),
+                                C.byref(bad))
+    return tuple(out), st, bad.value
+
+
 def divergence_max(codes, u, v, w, hxU, hyV, hzW):
     codes = np.ascontiguousarray(codes, np.int32)
     ijk = np.zeros(3, np.int32)
@@ -282,13 +299,37 @@ def bicg_reference(pk, b, eps=0.0, maxit=0):
     return out, st, rc
 
 
-def apply_advdiff(g, x, u, v, w, tau, D, flags=3):
-    """Implicit advection-diffusion operator on the oracle grid g (XProblem.cpp:1236-1238 summed over x, y, z)."""
+def apply_advdiff(g, x, u, v, w, tau, D, flags=3, Dfield=None):
+    """Implicit advection-diffusion operator on the oracle grid g (XProblem.cpp:1236-1238 summed over x, y, z);
+    Dfield: the per-cell diffusion coefficient of the variable-viscosity form (XProblem.cpp:3204)."""
     y = np.zeros(g.shape)
     p = lambda a: _p(f64(a), C.c_double) if a is not None else None  # noqa: E731
     st = lib().xfo_apply_advdiff(_p(g.codes, C.c_int32), _p(g.normals, C.c_double), _p(g.hx, C.c_double),
                                  _p(g.hy, C.c_double), _p(g.hz, C.c_double), p(u), p(v), p(w), C.c_double(tau),
-                                 C.c_double(D), int(flags), *g.shape, _p(f64(x), C.c_double), _p(y, C.c_double))
+                                 C.c_double(D), p(Dfield), int(flags), *g.shape, _p(f64(x), C.c_double),
+                                 _p(y, C.c_double))
     if st != 0:
         raise ValueError("oracle advection-diffusion rejected the grid")
     return y
+
+
+# Field output (XProblem.cpp:6132-6345)
+def vtk_write(path, node_codes, x, y, z, u, v, w, p_codes, p, d_codes, density, c_codes, conc, vis):
+    """The reference's VTK legacy ASCII volume written with its own format strings; node box shape (N+1, L+1, M+1)."""
+    N, L, M = (s_ - 1 for s_ in node_codes.shape)
+    i32 = lambda a: _p(np.ascontiguousarray(a, np.int32), C.c_int32)  # noqa: E731
+    d = lambda a: _p(f64(a), C.c_double)  # noqa: E731
+    keep = [np.ascontiguousarray(a, np.int32) for a in (node_codes, p_codes, d_codes, c_codes)]
+    st = lib().xfo_vtk_write(str(path).encode(), N, L, M, i32(keep[0]), d(x), d(y), d(z), d(u), d(v), d(w),
+                             i32(keep[1]), d(p), i32(keep[2]), d(density), i32(keep[3]), d(conc), d(vis))
+    if st != 0:
+        raise OSError("oracle VTK writer could not open " + str(path))
+
+
+def format_fixed6(values):
+    """b"".join(b"%f\n" % v): the C library's "%f" of each value."""
+    v = f64(values)
+    n = lib().xfo_format_fixed6(_p(v, C.c_double), v.size, None, 0)
+    buf = C.create_string_buffer(int(n))
+    lib().xfo_format_fixed6(_p(v, C.c_double), v.size, buf, n)
+    return buf.raw[:n]

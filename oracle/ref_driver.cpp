@@ -5,7 +5,8 @@
 // reference itself rather than from a restatement.
 //
 // Usage: ref_driver <task> <input.bin> <output.bin>
-//   task = matvec | solve | thomas | ib | pack
+//   task = matvec | solve | thomas | ib | pack | npy
+//   (npy writes <output.bin>.npy through the reference's cnpy::npy_save)
 //
 // File format (both directions): a sequence of records
 //   char name[32]; char kind ('d' double / 'i' int32); int64 count; data[count]
@@ -27,6 +28,7 @@
 #include "XMask.h"
 #include "XProblem.h"
 #include "XImmersedBoundary.h"
+#include "cnpy.h"
 
 struct Rec { char kind; std::vector<double> d; std::vector<int> i; };
 typedef std::map<std::string, Rec> Bag;
@@ -397,6 +399,14 @@ static void task_ib(Bag& b, Writer& w) {
   w.d("force_box", vec_to(s, force));
 }
 
+// cnpy::npy_save (cnpy.h:66-112) of "data" with shape "shape", as the time
+// loop's NPY output calls it (XProblem.cpp:6545-6590).
+static void task_npy(Bag& b, const char* out) {
+  const std::vector<int>& sh = b["shape"].i;
+  std::vector<unsigned int> shape(sh.begin(), sh.end());
+  cnpy::npy_save(std::string(out) + ".npy", b["data"].d.data(), shape.data(), (unsigned int)shape.size(), "w");
+}
+
 int main(int argc, char** argv) {
   if (argc != 4) { fprintf(stderr, "usage: ref_driver task in out\n"); return 2; }
   try {
@@ -408,6 +418,7 @@ int main(int argc, char** argv) {
     else if (t == "thomas") task_thomas(b, w);
     else if (t == "ib") task_ib(b, w);
     else if (t == "pack") task_pack(b, w);
+    else if (t == "npy") task_npy(b, argv[3]);
     else { fprintf(stderr, "unknown task\n"); return 2; }
   } catch (const char* e) {
     fprintf(stderr, "reference threw: %s\n", e); return 3;

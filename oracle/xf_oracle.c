@@ -13,6 +13,7 @@
 
 #include <math.h>
 #include <stdlib.h>
+#include <stdio.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -793,6 +794,114 @@ double xfo_divergence_max(const int32_t* codes, int n1, int n2, int n3, const do
   return divMaxValue;
 }
 
+/* Momentum right-hand side of velocity component `axis` (1 u, 2 v, 3 w) on
+ * its own b1 x b2 x b3 box, TVPProblem::SolveBySplitting, XProblem.cpp:
+ * 5088-5419.  Pass 1 (:5088-5305), per cell in i -> j -> k order: Fictive
+ * cells zero everything; Actual cells take the transfer velocities averaged
+ * onto the component's nodes (:5108-5133), the face viscosity (the mean of the
+ * two pressure-box values straddling the node) and rp = 0; Defined and
+ * PreDefined cells zero the transfer fields and take rp = border; Normal cells
+ * do the same for axis 1 with a normal along x only (:5157-5170) and throw
+ * otherwise; Equation, PreNormal, PreEquation and unknown codes throw.  Pass 2
+ * (:5310-5350): rp = force on Actual cells (GetForce; NULL is the base class's
+ * zero force).  Pass 3 (:5352-5419): on Actual cells rp += dVis . (dVel + dU),
+ * central differences over (h[m] + h[m-1]) of the pass-1 fields.  Boxes: u
+ * (n1-1) x n2 x n3, v n1 x (n2-1) x n3, w n1 x n2 x (n3-1), vis n1 x n2 x n3
+ * for the pressure box n1 x n2 x n3; hx/hy/hz are the component grid's
+ * separations.  Returns XFO_OK, or XFO_ERR_MASK with the first throwing cell
+ * (or an Actual cell on the box face, where the reference reads outside its
+ * arrays) in *bad. */
+int xfo_momentum_rhs(int axis, const int32_t* codes, const double* normals, int b1, int b2, int b3,
+                     const double* u, const double* v, const double* w, const double* vis, const double* hx,
+                     const double* hy, const double* hz, const double* border, const double* force, double* uTr,
+                     double* vTr, double* wTr, double* visTr, double* rp, int64_t* bad) {
+  if (axis < 1 || axis > 3) return XFO_ERR_ARG;
+  const int n2 = b2 + (axis == 2), n3 = b3 + (axis == 3);   /* the pressure box's last two extents */
+  const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
+  /* strides of the u, v, w and pressure boxes */
+  const int64_t us1 = (int64_t)n2 * n3, us2 = n3;
+  const int64_t vs1 = (int64_t)(n2 - 1) * n3, vs2 = n3;
+  const int64_t ws1 = (int64_t)n2 * (n3 - 1), ws2 = n3 - 1;
+  const int64_t ps1 = (int64_t)n2 * n3, ps2 = n3;
+#define U_(i, j, k) u[(int64_t)(i) * us1 + (int64_t)(j) * us2 + (k)]
+#define V_(i, j, k) v[(int64_t)(i) * vs1 + (int64_t)(j) * vs2 + (k)]
+#define W_(i, j, k) w[(int64_t)(i) * ws1 + (int64_t)(j) * ws2 + (k)]
+#define P_(i, j, k) vis[(int64_t)(i) * ps1 + (int64_t)(j) * ps2 + (k)]
+  for (int i = 0; i < b1; i++)
+    for (int j = 0; j < b2; j++)
+      for (int k = 0; k < b3; k++) {
+        const int64_t c = i * s1 + j * s2 + k;
+        const int mijk = codes[c];
+        if (mijk == 0) {
+          uTr[c] = 0; vTr[c] = 0; wTr[c] = 0; rp[c] = 0; visTr[c] = 0;
+        } else if (mijk == 1) {
+          if (i < 1 || i > b1 - 2 || j < 1 || j > b2 - 2 || k < 1 || k > b3 - 2) {
+            *bad = c;
+            return XFO_ERR_MASK;
+          }
+          if (axis == 1) {
+            uTr[c] = U_(i, j, k);
+            vTr[c] = (V_(i, j, k) + V_(i + 1, j, k) + V_(i, j - 1, k) + V_(i + 1, j - 1, k)) / 4;
+            wTr[c] = (W_(i, j, k) + W_(i + 1, j, k) + W_(i, j, k - 1) + W_(i + 1, j, k - 1)) / 4;
+            visTr[c] = vis ? (P_(i, j, k) + P_(i + 1, j, k)) / 2 : 0.0;
+          } else if (axis == 2) {
+            uTr[c] = (U_(i, j, k) + U_(i, j + 1, k) + U_(i - 1, j, k) + U_(i - 1, j + 1, k)) / 4;
+            vTr[c] = V_(i, j, k);
+            wTr[c] = (W_(i, j, k) + W_(i, j + 1, k) + W_(i, j, k - 1) + W_(i, j + 1, k - 1)) / 4;
+            visTr[c] = vis ? (P_(i, j, k) + P_(i, j + 1, k)) / 2 : 0.0;
+          } else {
+            uTr[c] = (U_(i, j, k) + U_(i, j, k + 1) + U_(i - 1, j, k) + U_(i - 1, j, k + 1)) / 4;
+            vTr[c] = (V_(i, j, k) + V_(i, j, k + 1) + V_(i, j - 1, k) + V_(i, j - 1, k + 1)) / 4;
+            wTr[c] = W_(i, j, k);
+            visTr[c] = vis ? (P_(i, j, k) + P_(i, j, k + 1)) / 2 : 0.0;
+          }
+          rp[c] = 0;
+        } else if (mijk == 3 || mijk == 4) {
+          uTr[c] = 0; vTr[c] = 0; wTr[c] = 0; visTr[c] = 0;
+          rp[c] = border ? border[c] : 0.0;
+        } else if (mijk == 5) {
+          const double nx = normals ? normals[3 * c] : 0.0, ny = normals ? normals[3 * c + 1] : 0.0,
+                       nz = normals ? normals[3 * c + 2] : 0.0;
+          uTr[c] = 0; vTr[c] = 0; wTr[c] = 0; visTr[c] = 0;
+          if (axis != 1 || nx == 0 || ny != 0 || nz != 0) {
+            *bad = c;
+            return XFO_ERR_MASK;
+          }
+          rp[c] = border ? border[c] : 0.0;
+        } else {   /* Equation, PreNormal, PreEquation: not implemented; else unknown */
+          *bad = c;
+          return XFO_ERR_MASK;
+        }
+      }
+#undef U_
+#undef V_
+#undef W_
+#undef P_
+  for (int64_t c = 0; c < (int64_t)b1 * b2 * b3; c++)
+    if (codes[c] == 1) rp[c] = force ? force[c] : 0.0;
+  for (int i = 0; i < b1; i++)
+    for (int j = 0; j < b2; j++)
+      for (int k = 0; k < b3; k++) {
+        const int64_t c = i * s1 + j * s2 + k;
+        if (codes[c] != 1) continue;
+        const double ddx = hx[i] + hx[i - 1], ddy = hy[j] + hy[j - 1], ddz = hz[k] + hz[k - 1];
+        const double dVisX = (visTr[c + s1] - visTr[c - s1]) / ddx;
+        const double dVisY = (visTr[c + s2] - visTr[c - s2]) / ddy;
+        const double dVisZ = (visTr[c + 1] - visTr[c - 1]) / ddz;
+        const int64_t st = axis == 1 ? s1 : axis == 2 ? s2 : 1;
+        const double dd = axis == 1 ? ddx : axis == 2 ? ddy : ddz;
+        const double dU = (uTr[c + st] - uTr[c - st]) / dd;
+        const double dV = (vTr[c + st] - vTr[c - st]) / dd;
+        const double dW = (wTr[c + st] - wTr[c - st]) / dd;
+        const double* velTr = axis == 1 ? uTr : axis == 2 ? vTr : wTr;
+        const double dVelX = (velTr[c + s1] - velTr[c - s1]) / ddx;
+        const double dVelY = (velTr[c + s2] - velTr[c - s2]) / ddy;
+        const double dVelZ = (velTr[c + 1] - velTr[c - 1]) / ddz;
+        rp[c] = rp[c] + (dVisX * (dVelX + dU) + dVisY * (dVelY + dV) + dVisZ * (dVelZ + dW));
+      }
+  return XFO_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* T1dPackOperator (XOperator.cpp:1135-1350) over the Rn space of the
  * operator's grid.  Column j of A is A(e_j) evaluated by the operator itself
@@ -966,7 +1075,7 @@ static double ad_dir(const double* h, int m, double vd, double D, double conv, d
 
 int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
                       const double* hz, const double* u, const double* v, const double* w, double tau, double D,
-                      int flags, int n1, int n2, int n3, const double* x, double* y) {
+                      const double* Dfield, int flags, int n1, int n2, int n3, const double* x, double* y) {
   int64_t bad;
   if (xfo_validate(XFO_OP_LAPLACE, codes, normals, n1, n2, n3, &bad) != XFO_OK) return XFO_ERR_MASK;
   xfo_grid g = {n1, n2, n3, (int64_t)n2 * n3, n3, codes, normals, hx, hy, hz, NULL};
@@ -982,11 +1091,100 @@ int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double*
           continue;
         }
         const double fc = x[c];
+        const double Dc = Dfield ? Dfield[c] : D;   /* diffCoefVar[i][j][k], XProblem.cpp:3204 */
         double res = itau * fc;
-        res = res + ad_dir(hx, i, u ? u[c] : 0.0, D, conv, diff, x[c - s1], fc, x[c + s1]);
-        res = res + ad_dir(hy, j, v ? v[c] : 0.0, D, conv, diff, x[c - s2], fc, x[c + s2]);
-        res = res + ad_dir(hz, k, w ? w[c] : 0.0, D, conv, diff, x[c - 1], fc, x[c + 1]);
+        res = res + ad_dir(hx, i, u ? u[c] : 0.0, Dc, conv, diff, x[c - s1], fc, x[c + s1]);
+        res = res + ad_dir(hy, j, v ? v[c] : 0.0, Dc, conv, diff, x[c - s2], fc, x[c + s2]);
+        res = res + ad_dir(hz, k, w ? w[c] : 0.0, Dc, conv, diff, x[c - 1], fc, x[c + 1]);
         y[c] = res;
       }
   return XFO_OK;
+}
+
+/* VTK legacy ASCII volume of one time step, XProblem.cpp:6132-6345, with the
+ * reference's format strings and loops (k outer, i inner over node indices
+ * 1..N-1 etc.).  Node box (N+1) x (L+1) x (M+1) with codes node_codes;
+ * staggered u (N+1)(L+2)(M+2), v (N+2)(L+1)(M+2), w (N+2)(L+2)(M+1);
+ * pressure-box fields p, density, conc, vis (N+2)(L+2)(M+2) with the
+ * pressure, density and concentration grids' codes (viscosity uses the
+ * concentration mask, :6331).  x, y, z: node coordinates.  Returns 0. */
+static double xfo_avg8(const int32_t* code, const double* f, int i, int j, int k, int64_t s1, int64_t s2) {
+  const int64_t c = i * s1 + j * s2 + k;
+  if (code[c] == 0) return 0;
+  const int64_t o1 = c + s1, o2 = c + s1 + s2, o3 = c + s1 + 1, o4 = c + s1 + s2 + 1, o5 = c, o6 = c + s2,
+                o7 = c + 1, o8 = c + s2 + 1;
+  int avr = (int)(code[o1] != 0) + (int)(code[o2] != 0) + (int)(code[o3] != 0) + (int)(code[o4] != 0) +
+            (int)(code[o5] != 0) + (int)(code[o6] != 0) + (int)(code[o7] != 0) + (int)(code[o8] != 0);
+  double p1 = f[o1], p2 = f[o2], p3 = f[o3], p4 = f[o4], p5 = f[o5], p6 = f[o6], p7 = f[o7], p8 = f[o8];
+  return (p1 + p2 + p3 + p4 + p5 + p6 + p7 + p8) / avr;
+}
+
+int xfo_vtk_write(const char* path, int N, int L, int M, const int32_t* node_codes, const double* x, const double* y,
+                  const double* z, const double* u, const double* v, const double* w, const int32_t* p_codes,
+                  const double* p, const int32_t* d_codes, const double* density, const int32_t* c_codes,
+                  const double* conc, const double* vis) {
+  FILE* f = fopen(path, "w");
+  if (!f) return XFO_ERR_ARG;
+  const int NML = (N - 1) * (L - 1) * (M - 1);
+  const int64_t nb2 = L + 1, nb3 = M + 1;
+  const int64_t us1 = (int64_t)(L + 2) * (M + 2), us2 = M + 2;
+  const int64_t vs1 = (int64_t)(L + 1) * (M + 2), vs2 = M + 2;
+  const int64_t ws1 = (int64_t)(L + 2) * (M + 1), ws2 = M + 1;
+  const int64_t ps1 = (int64_t)(L + 2) * (M + 2), ps2 = M + 2;
+  fprintf(f, "# vtk DataFile Version 3.0\n");
+  fprintf(f, "Flow\nASCII\n\n");
+  fprintf(f, "DATASET STRUCTURED_GRID\n");
+  fprintf(f, "DIMENSIONS %d %d %d\n", N - 1, L - 1, M - 1);
+  fprintf(f, "POINTS %d double\n", NML);
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) fprintf(f, "%f  %f  %f\n", x[i], y[j], z[k]);
+  fprintf(f, "POINT_DATA %d\n\nVECTORS Velocity double\n", NML);
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) {
+        double uu, vv, ww;
+        if (node_codes[(i * nb2 + j) * nb3 + k] == 0) {
+          uu = 0; vv = 0; ww = 0;
+        } else {
+          const int64_t cu = i * us1 + j * us2 + k, cv = i * vs1 + j * vs2 + k, cw = i * ws1 + j * ws2 + k;
+          uu = (u[cu] + u[cu + us2] + u[cu + 1] + u[cu + us2 + 1]) / 4;
+          vv = (v[cv] + v[cv + vs1] + v[cv + 1] + v[cv + vs1 + 1]) / 4;
+          ww = (w[cw] + w[cw + ws1] + w[cw + ws2] + w[cw + ws1 + ws2]) / 4;
+        }
+        fprintf(f, "%f ", uu);
+        fprintf(f, "%f ", vv);
+        fprintf(f, "%f\n ", ww);
+      }
+  fprintf(f, "\nSCALARS Pressure float\nLOOKUP_TABLE default\n");
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) fprintf(f, "%f\n ", xfo_avg8(p_codes, p, i, j, k, ps1, ps2));
+  fprintf(f, "\nSCALARS Density float\nLOOKUP_TABLE default\n");
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) fprintf(f, "%f\n", xfo_avg8(d_codes, density, i, j, k, ps1, ps2));
+  fprintf(f, "\nSCALARS Concentration float\nLOOKUP_TABLE default\n");
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) fprintf(f, "%f\n", xfo_avg8(c_codes, conc, i, j, k, ps1, ps2));
+  fprintf(f, "\nSCALARS Viscosity float\nLOOKUP_TABLE default\n");
+  for (int k = 1; k < M; k++)
+    for (int j = 1; j < L; j++)
+      for (int i = 1; i < N; i++) fprintf(f, "%f\n", xfo_avg8(c_codes, vis, i, j, k, ps1, ps2));
+  fclose(f);
+  return XFO_OK;
+}
+
+/* "%f\n" of each value, concatenated (the C library's formatting); returns
+ * the length, writing only when out has room for it. */
+int64_t xfo_format_fixed6(const double* values, int64_t n, char* out, int64_t capacity) {
+  int64_t len = 0;
+  char buf[400];
+  for (int64_t q = 0; q < n; q++) {
+    int m = snprintf(buf, sizeof(buf), "%f\n", values[q]);
+    if (out && len + m <= capacity) memcpy(out + len, buf, (size_t)m);
+    len += m;
+  }
+  return len;
 }

@@ -106,12 +106,35 @@ int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, c
 
 /* Implicit advection-diffusion operator (momentum / transport): y = A x on
  * active cells; the reference's ADI line coefficients summed over the three
- * directions (XProblem.cpp:1236-1238).  flags: 1 convective, 2 diffusive. */
+ * directions (XProblem.cpp:1236-1238).  flags: 1 convective, 2 diffusive.
+ * Dfield (NULL: the constant D) is the per-cell coefficient of the
+ * variable-viscosity form (diffCoefVar, XProblem.cpp:3204). */
 int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
                       const double* hz, const double* u, const double* v, const double* w, double tau, double D,
-                      int flags, int n1, int n2, int n3, const double* x, double* y);
+                      const double* Dfield, int flags, int n1, int n2, int n3, const double* x, double* y);
+
+/* Momentum right-hand side of one velocity component (XProblem.cpp:
+ * 5088-5419): transfer velocities, face viscosity and rp on the component's
+ * b1 x b2 x b3 box (axis 1 u, 2 v, 3 w).  u/v/w are the staggered boxes of the
+ * pressure box (b1 + (axis==1)) x (b2 + (axis==2)) x (b3 + (axis==3)), vis
+ * that pressure box (NULL: 0), border / force the component box (NULL: 0),
+ * normals 3 per component cell (NULL: 0).  XFO_ERR_MASK with the first
+ * throwing cell in *bad. */
+int xfo_momentum_rhs(int axis, const int32_t* codes, const double* normals, int b1, int b2, int b3,
+                     const double* u, const double* v, const double* w, const double* vis, const double* hx,
+                     const double* hy, const double* hz, const double* border, const double* force, double* uTr,
+                     double* vTr, double* wTr, double* visTr, double* rp, int64_t* bad);
 
 #ifdef __cplusplus
 }
 #endif
+
+/* VTK legacy ASCII volume (XProblem.cpp:6132-6345) written with the
+ * reference's format strings; see xf_oracle.c for the box shapes. */
+int xfo_vtk_write(const char* path, int N, int L, int M, const int32_t* node_codes, const double* x, const double* y,
+                  const double* z, const double* u, const double* v, const double* w, const int32_t* p_codes,
+                  const double* p, const int32_t* d_codes, const double* density, const int32_t* c_codes,
+                  const double* conc, const double* vis);
+/* "%f\n" of each value (the C library's formatting); returns the length. */
+int64_t xfo_format_fixed6(const double* values, int64_t n, char* out, int64_t capacity);
 #endif

@@ -6,7 +6,7 @@ it seeded inputs and stores inputs + outputs as .npz files here.  Needs the
 reference tree (REF, default /root/reference); the fixtures it writes are what
 the tests read, so the tests themselves never need the reference.
 
-    python tests/golden/make_golden.py [pack]
+    python tests/golden/make_golden.py [pack | npy]
 """
 import os
 import subprocess
@@ -270,10 +270,31 @@ def main():
               f"max|F|={np.abs(out['node_force']).max():.3e} sum f={out['force_box'].sum():.3e}")
 
 
+def npy_fixtures():
+    """NPY files written by the reference's cnpy::npy_save (XProblem.cpp:6545-6590) for three box shapes
+    (header dicts of three lengths, so three different space paddings)."""
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True, stdout=subprocess.DEVNULL)
+    rng = np.random.Generator(np.random.PCG64(77))
+    for name, shape in (("npy_box_a", (5, 6, 7)), ("npy_box_b", (10, 2, 3)), ("npy_box_c", (130, 129, 3))):
+        data = rng.standard_normal(shape)
+        data[0, 0, :2] = (np.inf, -0.0)
+        with tempfile.TemporaryDirectory() as td:
+            fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+            write_bag(fin, {"shape": np.array(shape, np.int32), "data": data.ravel()})
+            subprocess.run([DRIVER, "npy", fin, fout], check=True, timeout=60)
+            with open(fout + ".npy", "rb") as f:
+                blob = f.read()
+        with open(os.path.join(HERE, name + ".npy"), "wb") as f:
+            f.write(blob)
+
+
 if __name__ == "__main__":
-    # `make_golden.py pack` regenerates only the pack-operator fixtures
+    # `make_golden.py pack` / `npy` regenerate only those fixtures
     if sys.argv[1:] == ["pack"]:
         pack_fixtures()
+    elif sys.argv[1:] == ["npy"]:
+        npy_fixtures()
     else:
         main()
         pack_fixtures()
+        npy_fixtures()

@@ -94,3 +94,109 @@ def test_step_errors_match_reference_throws(ctx):
     # mismatched staggered shapes are refused before any launch
     with pytest.raises(xf.XFError):
         xf.pressure_rhs(gp, gv.vec(cs["v"]), gv.vec(cs["v"]), gw.vec(cs["w"]), cs["tau"], gp.vec(None))
+
+
+def momentum_case(cs, seed=8):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vis = rng.uniform(0.01, 0.02, cs["pc"].shape)
+    comps = ((1, cs["uc"], cs["hU"]), (2, cs["vc"], cs["hV"]), (3, cs["wc"], cs["hW"]))
+    extra = {a: (rng.standard_normal(c.shape), rng.standard_normal(c.shape)) for a, c, _ in comps}
+    return vis, comps, extra
+
+
+@pytest.mark.parametrize("axis", [1, 2, 3])
+@pytest.mark.parametrize("with_force", [False, True])
+def test_momentum_rhs_matches_oracle(ctx, axis, with_force):
+    cs = wl_step.staggered_channel()
+    gp, gu, gv, gw = grids(ctx, cs)
+    vis, comps, extra = momentum_case(cs)
+    _, codes, hs = comps[axis - 1]
+    g = (gu, gv, gw)[axis - 1]
+    border, force = extra[axis]
+    force = force if with_force else None
+    out = xf.momentum_rhs(axis, g, gu.vec(cs["u"]), gv.vec(cs["v"]), gw.vec(cs["w"]), vis=gp.vec(vis),
+                          border=g.vec(border), force=g.vec(force) if force is not None else None)
+    want, st, _ = O.momentum_rhs(axis, codes, cs["u"], cs["v"], cs["w"], *hs, vis=vis, border=border, force=force)
+    assert st == 0
+    for name, o, w_ in zip(("uTr", "vTr", "wTr", "visTr", "rp"), out, want):
+        np.testing.assert_array_equal(o.download(), w_, err_msg=name)
+
+
+def test_momentum_rhs_normal_cells_and_throws(ctx):
+    cs = wl_step.staggered_channel()
+    gp, gu, gv, gw = grids(ctx, cs)
+    uc = cs["uc"].copy()
+    nrm = np.zeros(uc.shape + (3,))
+    cells = np.argwhere(uc == 4)[:3]
+    for c in cells:
+        uc[tuple(c)] = 5
+        nrm[tuple(c)] = (-1.0, 0.0, 0.0)
+    border = np.arange(uc.size, dtype=np.float64).reshape(uc.shape)
+    args = (gu.vec(cs["u"]), gv.vec(cs["v"]), gw.vec(cs["w"]))
+    gn = xf.Grid(ctx, uc, *cs["hU"], nrm)
+    out = xf.momentum_rhs(1, gn, *args, border=gn.vec(border))
+    want, st, _ = O.momentum_rhs(1, uc, cs["u"], cs["v"], cs["w"], *cs["hU"], border=border, normals=nrm)
+    assert st == 0
+    np.testing.assert_array_equal(out[4].download(), want[4])
+    # a normal with a y component: the reference's throw at the first such cell
+    nrm[tuple(cells[2])] = (-1.0, 0.25, 0.0)
+    nrm[tuple(cells[1])] = (-1.0, 0.0, 0.25)
+    gb = xf.Grid(ctx, uc, *cs["hU"], nrm)
+    with pytest.raises(xf.XFError) as e:
+        xf.momentum_rhs(1, gb, *args, border=gb.vec(border))
+    assert e.value.status == capi.XF_ERR_MASK and "(%d, %d, %d)" % tuple(int(t) for t in cells[1]) in str(e.value)
+    # Equation and PreNormal cells in the v equation
+    for code in (7, 6):
+        vc = cs["vc"].copy()
+        c = tuple(int(t) for t in np.argwhere(vc == 1)[7])
+        vc[c] = code
+        gx = xf.Grid(ctx, vc, *cs["hV"])
+        with pytest.raises(xf.XFError) as e:
+            xf.momentum_rhs(2, gx, *args)
+        assert e.value.status == capi.XF_ERR_MASK and "(%d, %d, %d)" % c in str(e.value)
+    # wrong staggered shapes are argument errors
+    with pytest.raises(xf.XFError) as e:
+        xf.momentum_rhs(2, gu, *args)
+    assert e.value.status == capi.XF_ERR_ARG
+
+
+def test_momentum_equation_variable_viscosity(ctx):
+    """The u equation end to end: rp from xf_momentum_rhs, the variable-viscosity advection-diffusion rows
+    (diffCoefVar = visTr) bit-exact against the oracle, and the implicit system (1/tau) u + ... = u_prev/tau + rp
+    solved by BiCGStab to its stop rule (max-norm of the true residual <= 1e-5, XSLAE.cpp:712)."""
+    cs = wl_step.staggered_channel()
+    gp, gu0, gv, gw = grids(ctx, cs)
+    vis, comps, extra = momentum_case(cs)
+    # the outflow face's PreDefined rows take the semi-sum with their inner neighbour: normal +x
+    nrm = np.zeros(cs["uc"].shape + (3,))
+    nrm[cs["uc"] == 4] = (1.0, 0.0, 0.0)
+    gu = xf.Grid(ctx, cs["uc"], *cs["hU"], nrm)
+    uTr, vTr, wTr, visTr, rp = xf.momentum_rhs(1, gu, gu0.vec(cs["u"]), gv.vec(cs["v"]), gw.vec(cs["w"]),
+                                               vis=gp.vec(vis), border=gu.vec(cs["u_border"]))
+    tau = cs["tau"]
+    A = xf.Operator(gu, xf.XF_OP_ADVDIFF)
+    A.set_advection(uTr, vTr, wTr, tau, 0.0, xf.XF_ADV_CONVECTIVE | xf.XF_ADV_DIFFUSIVE)
+    A.set_diffusion_field(visTr)
+    og = O.Grid(cs["uc"], nrm, *cs["hU"])
+    rng = np.random.Generator(np.random.PCG64(4))
+    x = rng.standard_normal(gu.shape)
+    y = gu.vec(None)
+    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    want = O.apply_advdiff(og, x, uTr.download(), vTr.download(), wTr.download(), tau, 0.0, 3,
+                           Dfield=visTr.download())
+    sm = og.smask.astype(bool)
+    np.testing.assert_array_equal(y.download()[sm], want[sm])
+    # the constant form differs once the field is set, and returns when it is cleared
+    A.set_diffusion_field(None)
+    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    np.testing.assert_array_equal(y.download()[sm], O.apply_advdiff(og, x, uTr.download(), vTr.download(),
+                                                                     wTr.download(), tau, 0.0, 3)[sm])
+    A.set_diffusion_field(visTr)
+    # right-hand side u_prev / tau + rp on Actual rows, the border rows' values elsewhere
+    b = np.where(cs["uc"] == 1, cs["u"] / tau + rp.download(), rp.download()) * sm
+    xv = gu.vec(cs["u"] * sm)
+    st = xf.solve(A, xv, gu.vec(b), method=xf.XF_BICGSTAB)
+    assert st.status == capi.XF_OK and st.iterations > 0
+    r = gu.vec(None)
+    A.apply(xv, r, flags=xf.XF_ZERO_INACTIVE)
+    assert np.abs(r.download()[sm] - b[sm]).max() <= 1e-5

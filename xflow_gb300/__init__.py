@@ -206,6 +206,11 @@ class Operator(_Owned):
         hh = [x.h if x is not None else None for x in (u, v, w)]
         _check(self.grid.ctx.h, capi.lib().xf_op_set_advection(self.h, *hh, float(tau), float(diff_coef), int(flags)))
 
+    def set_diffusion_field(self, d):
+        """XF_OP_ADVDIFF: per-cell diffusion coefficient Vec (the visTr form, XProblem.cpp:3204); None: the
+        constant again."""
+        _check(self.grid.ctx.h, capi.lib().xf_op_set_diffusion_field(self.h, _h(d)))
+
     def apply(self, x, y, s=None, sign=0, flags=0, w=None, want_dot=False):
         d = C.c_double()
         _check(self.grid.ctx.h, capi.lib().xf_matvec(self.h, x.h, y.h, s.h if s is not None else None, sign, flags,
@@ -368,6 +373,41 @@ def divergence_max(gp, u, v, w):
     ijk = np.zeros(3, np.int32)
     _check(gp.ctx.h, capi.lib().xf_divergence_max(gp.h, u.h, v.h, w.h, C.byref(val), capi._ptr(ijk)))
     return val.value, tuple(int(t) for t in ijk)
+
+
+def momentum_rhs(axis, gc, u_prev, v_prev, w_prev, vis=None, border=None, force=None, out=None):
+    """Momentum right-hand side of velocity equation `axis` on the component grid gc (XProblem.cpp:5088-5419):
+    returns the Vecs (uTr, vTr, wTr, visTr, rp), reusing `out` when given."""
+    out = out if out is not None else tuple(gc.vec(None) for _ in range(5))
+    _check(gc.ctx.h, capi.lib().xf_momentum_rhs(int(axis), u_prev.h, v_prev.h, w_prev.h, _h(vis), _h(border),
+                                                 _h(force), *(o.h for o in out)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Field output (XProblem.cpp:6132-6345, 6545-6590)
+def write_vtk(path, nodes, x, y, z, u, v, w, p, density, conc, vis):
+    """The time loop's VTK legacy ASCII volume, formatted on the device; returns the file size."""
+    xyz = [np.ascontiguousarray(a, np.float64) for a in (x, y, z)]
+    n = C.c_int64()
+    _check(nodes.ctx.h, capi.lib().xf_vtk_write(str(path).encode(), nodes.h, *(capi._ptr(a) for a in xyz), u.h, v.h,
+                                                 w.h, p.h, density.h, conc.h, vis.h, C.byref(n)))
+    return n.value
+
+
+def format_fixed6(ctx, values):
+    """b"".join(b"%f\\n" % v for v in values), formatted on the device."""
+    v = np.ascontiguousarray(values, np.float64).ravel()
+    n = C.c_int64()
+    _check(ctx.h, capi.lib().xf_format_fixed6(ctx.h, capi._ptr(v), v.size, None, 0, C.byref(n)))
+    buf = C.create_string_buffer(max(int(n.value), 1))
+    _check(ctx.h, capi.lib().xf_format_fixed6(ctx.h, capi._ptr(v), v.size, buf, n.value, C.byref(n)))
+    return buf.raw[:n.value]
+
+
+def write_npy(path, vec):
+    """NPY file of a Vec's box with cnpy's header."""
+    _check(vec.grid.ctx.h, capi.lib().xf_npy_write(str(path).encode(), vec.h))
 
 
 # ---------------------------------------------------------------------------

@@ -28,10 +28,10 @@ EXPORTS = [
     "xf_create", "xf_destroy", "xf_last_error", "xf_status_string", "xf_synchronize", "xf_stream",
     "xf_grid_create", "xf_grid_destroy", "xf_grid_end_index", "xf_grid_rn_map", "xf_grid_space_mask",
     "xf_grid_check", "xf_vec_create", "xf_vec_destroy", "xf_vec_upload", "xf_vec_download", "xf_vec_assign",
-    "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_op_set_advection", "xf_pack_create", "xf_op_transpose",
+    "xf_vec_fill", "xf_vec_data", "xf_op_create", "xf_op_destroy", "xf_op_set_density", "xf_op_set_advection", "xf_op_set_diffusion_field", "xf_pack_create", "xf_op_transpose",
     "xf_pack_size", "xf_pack_download", "xf_matvec",
     "xf_lincomb", "xf_dot", "xf_norm", "xf_dot_op", "xf_absmax", "xf_solve_opts_default", "xf_solve",
-    "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
+    "xf_solve_host", "xf_pressure_rhs", "xf_velocity_correct", "xf_divergence_max", "xf_momentum_rhs", "xf_vtk_write", "xf_format_fixed6", "xf_npy_write", "xf_thomas_lines", "xf_ib_create", "xf_ib_destroy", "xf_ib_download", "xf_ib_upload",
     "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
     "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
     "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
@@ -118,6 +118,11 @@ def lib():
         L.xf_pressure_rhs.argtypes = [vp, vp, vp, vp, vp, C.c_double, vp, vp]
         L.xf_velocity_correct.argtypes = [C.c_int, vp, vp, vp, C.c_double, vp, vp]
         L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]
+        L.xf_momentum_rhs.argtypes = [C.c_int] + [vp] * 11
+        L.xf_vtk_write.argtypes = [C.c_char_p] + [vp] * 12
+        L.xf_format_fixed6.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.POINTER(C.c_int64)]
+        L.xf_npy_write.argtypes = [C.c_char_p, vp]
+        L.xf_op_set_diffusion_field.argtypes = [vp, vp]
         L.xf_thomas_lines.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64,
                                       vp, vp, vp, vp, vp]
         L.xf_ib_create.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]

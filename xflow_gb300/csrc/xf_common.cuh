@@ -53,6 +53,7 @@ struct xf_grid {
   int64_t ncell, s1, s2;
   int64_t end_index;
   uint8_t* code;             // device, per cell: the reference point code (0..8)
+  uint8_t* nflag;            // device, per Normal (code 5) cell: bit 0/1/2 = normal x/y/z nonzero
   uint8_t* kind;             // device, per cell
   uint8_t* smask;            // device, per cell (0/1)
   int32_t* inv;              // device, Rn index per cell (0 inactive)
@@ -92,6 +93,9 @@ struct xf_op {
   // XF_OP_ADVDIFF: advecting velocity boxes (FP64 and FP32 copies) and coefficients
   double* adv64[3] = {nullptr, nullptr, nullptr};
   float* adv32[3] = {nullptr, nullptr, nullptr};
+  double* adD64 = nullptr;   // per-cell diffusion coefficient (null: the constant ad_D)
+  float* adD32 = nullptr;
+  int adD_set = 0;
   double ad_tau = 1, ad_D = 0;
   int ad_flags = 0, adv_set = 0;
 };

@@ -360,7 +360,7 @@ extern "C" int xf_grid_destroy(xf_grid* g) {
   if (!g) return XF_ERR_ARG;
   cudaSetDevice(g->ctx->device);
   cudaStreamSynchronize(g->ctx->stream);
-  void* ptrs[] = {g->diag, g->code, g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
+  void* ptrs[] = {g->diag, g->code, g->nflag, g->kind, g->smask, g->inv, g->brow_of, g->brow_nrm, g->hx, g->hy, g->hz, g->fhx, g->fhy, g->fhz,
                   g->cxm, g->cxp, g->cym, g->cyp, g->czm, g->czp, g->fxm, g->fxp, g->fym, g->fyp, g->fzm, g->fzp,
                   g->rhx, g->rhy, g->rhz, g->rhhx, g->rhhy, g->rhhz, g->frhx, g->frhy, g->frhz, g->frhhx, g->frhhy, g->frhhz};
   for (void* p : ptrs)
@@ -369,11 +369,16 @@ extern "C" int xf_grid_destroy(xf_grid* g) {
   return XF_OK;
 }
 
-// Point codes as bytes (codes outside 0..255 become 255: an unknown code).
-__global__ void k_code_bytes(const int32_t* __restrict__ codes, int64_t n, uint8_t* __restrict__ out) {
+// Point codes as bytes (codes outside 0..255 become 255: an unknown code), and
+// the nonzero components of Normal cells' normals.
+__global__ void k_code_bytes(const int32_t* __restrict__ codes, const double* __restrict__ nrm, int64_t n,
+                             uint8_t* __restrict__ out, uint8_t* __restrict__ nflag) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t m = codes[c];
     out[c] = (m >= 0 && m < 255) ? (uint8_t)m : (uint8_t)255;
+    uint8_t f = 0;
+    if (m == 5 && nrm) f = (nrm[3 * c] != 0 ? 1 : 0) | (nrm[3 * c + 1] != 0 ? 2 : 0) | (nrm[3 * c + 2] != 0 ? 4 : 0);
+    nflag[c] = f;
   }
 }
 
@@ -419,7 +424,8 @@ extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t
   k_classify<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(d_codes, d_nrm, n1, n2, n3, g->kind, g->smask, d_isb, d_bad);
   G_TRY(cudaGetLastError());
   G_TRY(cudaMalloc(&g->code, n));
-  k_code_bytes<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(d_codes, n, g->code);
+  G_TRY(cudaMalloc(&g->nflag, n));
+  k_code_bytes<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(d_codes, d_nrm, n, g->code, g->nflag);
   G_TRY(cudaGetLastError());
   G_TRY(cudaMemcpyAsync(h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost, ctx->stream));
   if ((st = scan_number(ctx, g->smask, n, g->inv, 1, 0, &g->end_index)) != XF_OK) goto fail;

@@ -178,6 +178,7 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
     a.g.adv2 = D64 ? (const T*)op->adv64[2] : (const T*)op->adv32[2];
     a.g.ad_itau = (T)(1 / op->ad_tau);
     a.g.ad_D = (T)op->ad_D;
+    a.g.adDf = !op->adD_set ? nullptr : D64 ? (const T*)op->adD64 : (const T*)op->adD32;
     a.g.ad_conv = (op->ad_flags & XF_ADV_CONVECTIVE) ? T(1) : T(0);
     a.g.ad_diff = (op->ad_flags & XF_ADV_DIFFUSIVE) ? T(1) : T(0);
     k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
@@ -258,6 +259,8 @@ extern "C" int xf_op_destroy(xf_op* op) {
     if (op->adv64[d]) cudaFree(op->adv64[d]);
     if (op->adv32[d]) cudaFree(op->adv32[d]);
   }
+  if (op->adD64) cudaFree(op->adD64);
+  if (op->adD32) cudaFree(op->adD32);
   if (op->pack) xf_pack_free(op->pack);
   delete op;
   return XF_OK;
@@ -308,6 +311,30 @@ extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, 
   op->ad_D = diff_coef;
   op->ad_flags = flags;
   op->adv_set = 1;
+  return XF_OK;
+}
+
+extern "C" int xf_op_set_diffusion_field(xf_op* op, const xf_vec* d) {
+  if (!op) return XF_ERR_ARG;
+  xf_ctx* ctx = op->g->ctx;
+  if (op->kind != XF_OP_ADVDIFF)
+    return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_diffusion_field: not an advection-diffusion operator");
+  if (!d) {
+    op->adD_set = 0;
+    return XF_OK;
+  }
+  if (d->g != op->g || d->dtype != XF_F64)
+    return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_diffusion_field: an FP64 box of the operator's grid expected");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int64_t n = op->g->ncell;
+  if (!op->adD64 && (cudaMalloc(&op->adD64, n * 8) != cudaSuccess || cudaMalloc(&op->adD32, n * 4) != cudaSuccess)) {
+    cudaGetLastError();
+    return xf_fail(ctx, XF_ERR_NOMEM, "xf_op_set_diffusion_field: allocation");
+  }
+  XF_CUDA(ctx, cudaMemcpyAsync(op->adD64, d->data, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  k_d2f<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(op->adD64, op->adD32, n);
+  XF_CUDA(ctx, cudaGetLastError());
+  op->adD_set = 1;
   return XF_OK;
 }
 

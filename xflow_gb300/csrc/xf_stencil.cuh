@@ -26,6 +26,7 @@ struct StencilGrid {
   const T* __restrict__ rho;  // density box (VARDIV) or null
   // ADVDIFF: advecting velocity per direction, 1/tau, D and the two flags as 0/1
   const T* __restrict__ adv0; const T* __restrict__ adv1; const T* __restrict__ adv2;
+  const T* __restrict__ adDf;   // per-cell D of the variable-viscosity form, or null
   T ad_itau, ad_D, ad_conv, ad_diff;
   int n1, n2, n3;
   int s1, s2;
@@ -205,10 +206,11 @@ template <typename T>
 __device__ __forceinline__ T ad_actual(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c) {
   const int s1 = g.s1, s2 = g.s2;
   const T fc = f[c];
+  const T D = g.adDf ? g.adDf[c] : g.ad_D;   // diffCoefVar[i][j][k] (XProblem.cpp:3204) or the constant
   T res = g.ad_itau * fc;
-  res = res + ad_dir<T>(g.hx, i, g.adv0[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
-  res = res + ad_dir<T>(g.hy, j, g.adv1[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
-  res = res + ad_dir<T>(g.hz, k, g.adv2[c], g.ad_D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
+  res = res + ad_dir<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
+  res = res + ad_dir<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
+  res = res + ad_dir<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
   return res;
 }
 

@@ -5,7 +5,9 @@
 //                       XProblem.cpp:5474-5512;
 //  xf_velocity_correct  projection of one staggered velocity component,
 //                       XProblem.cpp:5598-5777;
-//  xf_divergence_max    the "control balance" check, XProblem.cpp:5782-5829.
+//  xf_divergence_max    the "control balance" check, XProblem.cpp:5782-5829;
+//  xf_momentum_rhs      transfer velocities, face viscosity and right-hand
+//                       side of one velocity equation, XProblem.cpp:5088-5419.
 //
 // Staggered boxes follow the reference's grids (XStatement.h:127-135): with the
 // pressure box n1 x n2 x n3, the u box is (n1-1) x n2 x n3, v is n1 x (n2-1) x n3
@@ -27,7 +29,7 @@ enum { PC_FICTIVE = 0, PC_ACTUAL = 1, PC_DEFINED = 3, PC_PREDEFINED = 4, PC_NORM
 
 // Error kinds, each the minimum offending cell in iscalars[CHK0 + kind].
 enum { CHK0 = 48, E_RANGE = 0, E_NOTIMPL_P, E_UNKNOWN, E_DEFINED, E_PREDEF_NONE, E_PREDEF_MANY, E_PREDEF_VALUE,
-       E_NOTIMPL_V, E_COUNT };
+       E_NOTIMPL_V, E_NOTIMPL_EQ, E_COUNT };
 constexpr long long NO_CELL = 0x7f7f7f7f7f7f7f7fLL;   // cudaMemset byte 0x7f
 constexpr int SL_STEP = 8;                              // reduction slot of xf_divergence_max (and SL_STEP + 1)
 
@@ -195,6 +197,100 @@ __global__ void __launch_bounds__(RED_THREADS) k_div_max(const uint8_t* __restri
   }
 }
 
+// Momentum right-hand side, pass 1 (XProblem.cpp:5088-5305) with pass 2
+// (:5310-5350) folded in: every cell of the component box b1 x b2 x b3 of
+// velocity `axis`.  The staggered boxes have the pressure box's strides less
+// one layer along their own axis; vis is the pressure box.
+struct MomArgs {
+  int axis, b1, b2, b3;
+  const uint8_t* code;
+  const uint8_t* nflag;
+  const double *u, *v, *w, *vis, *border, *force;
+  const double *hx, *hy, *hz;
+  double *uTr, *vTr, *wTr, *visTr, *rp;
+  DevScratch* S;
+};
+
+__global__ void k_mom_transfer(MomArgs a) {
+  const int64_t n = (int64_t)a.b1 * a.b2 * a.b3;
+  const int64_t s1 = (int64_t)a.b2 * a.b3, s2 = a.b3;
+  const int n2 = a.b2 + (a.axis == 2), n3 = a.b3 + (a.axis == 3);
+  const int64_t us1 = (int64_t)n2 * n3, us2 = n3;
+  const int64_t vs1 = (int64_t)(n2 - 1) * n3, vs2 = n3;
+  const int64_t ws1 = (int64_t)n2 * (n3 - 1), ws2 = n3 - 1;
+  const int64_t ps1 = (int64_t)n2 * n3, ps2 = n3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int m = a.code[c];
+    double ut = 0, vt = 0, wt = 0, vist = 0, r = 0;
+    if (m == PC_FICTIVE) {
+    } else if (m == PC_ACTUAL) {
+      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      if (i < 1 || i > a.b1 - 2 || j < 1 || j > a.b2 - 2 || k < 1 || k > a.b3 - 2) {
+        report(a.S, E_RANGE, c);   // the reference would read outside the boxes
+        continue;
+      }
+      const int64_t cu = i * us1 + j * us2 + k, cv = i * vs1 + j * vs2 + k, cw = i * ws1 + j * ws2 + k;
+      const int64_t cp = i * ps1 + j * ps2 + k;
+      const double* u = a.u;
+      const double* v = a.v;
+      const double* w = a.w;
+      if (a.axis == 1) {
+        ut = u[cu];
+        vt = (v[cv] + v[cv + vs1] + v[cv - vs2] + v[cv + vs1 - vs2]) / 4;
+        wt = (w[cw] + w[cw + ws1] + w[cw - 1] + w[cw + ws1 - 1]) / 4;
+        if (a.vis) vist = (a.vis[cp] + a.vis[cp + ps1]) / 2;
+      } else if (a.axis == 2) {
+        ut = (u[cu] + u[cu + us2] + u[cu - us1] + u[cu - us1 + us2]) / 4;
+        vt = v[cv];
+        wt = (w[cw] + w[cw + ws2] + w[cw - 1] + w[cw + ws2 - 1]) / 4;
+        if (a.vis) vist = (a.vis[cp] + a.vis[cp + ps2]) / 2;
+      } else {
+        ut = (u[cu] + u[cu + 1] + u[cu - us1] + u[cu - us1 + 1]) / 4;
+        vt = (v[cv] + v[cv + 1] + v[cv - vs2] + v[cv - vs2 + 1]) / 4;
+        wt = w[cw];
+        if (a.vis) vist = (a.vis[cp] + a.vis[cp + 1]) / 2;
+      }
+      r = a.force ? a.force[c] : 0.0;   // GetForce replaces the Actual rows' zero
+    } else if (m == PC_DEFINED || m == PC_PREDEFINED) {
+      r = a.border ? a.border[c] : 0.0;
+    } else if (m == PC_NORMAL) {
+      if (a.axis != 1 || a.nflag[c] != 1) { report(a.S, E_NOTIMPL_EQ, c); continue; }
+      r = a.border ? a.border[c] : 0.0;
+    } else if (m == PC_EQUATION || m == PC_PRENORMAL || m == PC_PREEQUATION) {
+      report(a.S, E_NOTIMPL_V, c);
+      continue;
+    } else {
+      report(a.S, E_UNKNOWN, c);
+      continue;
+    }
+    a.uTr[c] = ut; a.vTr[c] = vt; a.wTr[c] = wt; a.visTr[c] = vist; a.rp[c] = r;
+  }
+}
+
+// Pass 3 (XProblem.cpp:5352-5419): rp += dVis . (dVel + dU) on Actual cells.
+__global__ void k_mom_viscous(MomArgs a) {
+  const int64_t n = (int64_t)a.b1 * a.b2 * a.b3;
+  const int64_t s1 = (int64_t)a.b2 * a.b3, s2 = a.b3;
+  const int64_t st = a.axis == 1 ? s1 : a.axis == 2 ? s2 : 1;
+  const double* velTr = a.axis == 1 ? a.uTr : a.axis == 2 ? a.vTr : a.wTr;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (a.code[c] != PC_ACTUAL) continue;
+    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    const double ddx = a.hx[i] + a.hx[i - 1], ddy = a.hy[j] + a.hy[j - 1], ddz = a.hz[k] + a.hz[k - 1];
+    const double dVisX = (a.visTr[c + s1] - a.visTr[c - s1]) / ddx;
+    const double dVisY = (a.visTr[c + s2] - a.visTr[c - s2]) / ddy;
+    const double dVisZ = (a.visTr[c + 1] - a.visTr[c - 1]) / ddz;
+    const double dd = a.axis == 1 ? ddx : a.axis == 2 ? ddy : ddz;
+    const double dU = (a.uTr[c + st] - a.uTr[c - st]) / dd;
+    const double dV = (a.vTr[c + st] - a.vTr[c - st]) / dd;
+    const double dW = (a.wTr[c + st] - a.wTr[c - st]) / dd;
+    const double dVelX = (velTr[c + s1] - velTr[c - s1]) / ddx;
+    const double dVelY = (velTr[c + s2] - velTr[c - s2]) / ddy;
+    const double dVelZ = (velTr[c + 1] - velTr[c - 1]) / ddz;
+    a.rp[c] = a.rp[c] + (dVisX * (dVelX + dU) + dVisY * (dVelY + dV) + dVisZ * (dVelZ + dW));
+  }
+}
+
 // ---------------------------------------------------------------------------
 static bool is_f64(const xf_vec* v) { return v && v->dtype == XF_F64; }
 
@@ -248,6 +344,9 @@ static const char* check_message(int kind) {
     case E_PREDEF_MANY: return "PreDefined border condition checking error - actual values count > 1";
     case E_PREDEF_VALUE: return "PreDefined border condition checking error - value incorrect";
     case E_NOTIMPL_V: return "Method is not implemented for this point border type of velocity";
+    case E_NOTIMPL_EQ:
+      return "Method is not implemented for this point border type of velocity and this equation number and this "
+             "normal vector";
     default: return "unknown";
   }
 }
@@ -354,5 +453,61 @@ extern "C" int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_ve
       ijk[2] = (int32_t)(c % gp->s2);
     }
   }
+  return XF_OK;
+}
+
+extern "C" int xf_momentum_rhs(int axis, const xf_vec* u_prev, const xf_vec* v_prev, const xf_vec* w_prev,
+                               const xf_vec* vis, const xf_vec* border, const xf_vec* force, xf_vec* u_tr,
+                               xf_vec* v_tr, xf_vec* w_tr, xf_vec* vis_tr, xf_vec* rp) {
+  if (!u_prev || !v_prev || !w_prev || !u_tr || !v_tr || !w_tr || !vis_tr || !rp) return XF_ERR_ARG;
+  const xf_grid* gc = rp->g;   // the component's grid
+  xf_ctx* ctx = gc->ctx;
+  if (axis < 1 || axis > 3) return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: axis must be 1, 2 or 3");
+  const xf_vec* outs[5] = {u_tr, v_tr, w_tr, vis_tr, rp};
+  for (const xf_vec* o : outs)
+    if (!is_f64(o) || o->g != gc)
+      return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: outputs must be FP64 vectors of the component's grid");
+  for (int q = 0; q < 5; q++)
+    for (int r = q + 1; r < 5; r++)
+      if (outs[q] == outs[r]) return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: outputs must be distinct");
+  if ((border && (!is_f64(border) || !same_box(border, gc))) || (force && (!is_f64(force) || !same_box(force, gc))))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: border and force must be FP64 component boxes");
+  const int n1 = gc->n1 + (axis == 1), n2 = gc->n2 + (axis == 2), n3 = gc->n3 + (axis == 3);
+  const xf_vec* vel[3] = {u_prev, v_prev, w_prev};
+  for (int d = 0; d < 3; d++) {
+    if (!is_f64(vel[d]) || vel[d]->g->ctx != ctx)
+      return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: u, v, w must be FP64 boxes of this context");
+    const xf_grid* g = vel[d]->g;
+    if (g->n1 != n1 - (d == 0) || g->n2 != n2 - (d == 1) || g->n3 != n3 - (d == 2))
+      return xf_fail(ctx, XF_ERR_ARG,
+                     "xf_momentum_rhs: staggered boxes must be (n1-1,n2,n3), (n1,n2-1,n3), (n1,n2,n3-1) for the "
+                     "%dx%dx%d pressure box of this component",
+                     n1, n2, n3);
+  }
+  if (vis && (!is_f64(vis) || vis->g->n1 != n1 || vis->g->n2 != n2 || vis->g->n3 != n3))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_momentum_rhs: vis must be an FP64 pressure box");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  int st;
+  if ((st = clear_checks(ctx))) return st;
+  MomArgs a;
+  a.axis = axis; a.b1 = gc->n1; a.b2 = gc->n2; a.b3 = gc->n3;
+  a.code = gc->code; a.nflag = gc->nflag;
+  a.u = (const double*)u_prev->data; a.v = (const double*)v_prev->data; a.w = (const double*)w_prev->data;
+  a.vis = vis ? (const double*)vis->data : nullptr;
+  a.border = border ? (const double*)border->data : nullptr;
+  a.force = force ? (const double*)force->data : nullptr;
+  a.hx = gc->hx; a.hy = gc->hy; a.hz = gc->hz;
+  a.uTr = (double*)u_tr->data; a.vTr = (double*)v_tr->data; a.wTr = (double*)w_tr->data;
+  a.visTr = (double*)vis_tr->data; a.rp = (double*)rp->data;
+  a.S = ctx->scratch;
+  const int bl = grid_blocks(ctx, gc->ncell, 256);
+  k_mom_transfer<<<bl, 256, 0, ctx->stream>>>(a);
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int kinds[] = {E_RANGE, E_NOTIMPL_V, E_NOTIMPL_EQ, E_UNKNOWN};
+  const int bad = first_error(chk, kinds, 4, &cell);
+  if (bad >= 0) return fail_at(ctx, gc, bad, cell, "xf_momentum_rhs");
+  k_mom_viscous<<<bl, 256, 0, ctx->stream>>>(a);
+  XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
 }
