@@ -265,30 +265,36 @@ def test_maxit_status(ctx, precision):
     assert st.status == capi.XF_MAXIT and st.iterations == 5
 
 
-# box 50: register march; box 66 (P % 8 == 4: a half 8-cell group ends the
-# plane) and box 72 (3 tiles, the last one partial): shared-memory tile
+# box 50, box 66 (P % 8 == 4: a half 8-cell group ends the plane) and box 72
+# (3 tiles of the staged kernels, the last one partial)
 @pytest.mark.parametrize("n", [48, 64, 70])
 def test_fused_direction_update_matches_three_kernel_path(ctx, monkeypatch, n):
     """The mixed CG's fused iteration (p' = r + beta p inside the stencil, p
-    ping-ponging between two buffers), by the tiled kernel where the plane
-    allows it and by the register march, against the three-kernel iteration on
-    the same system: same iteration count within 2, same solution within the
+    ping-ponging between two buffers), by the bulk-staged kernel, the tiled
+    kernel and the register march, against the three-kernel iteration on the
+    same system: same iteration count within 2, same solution within the
     solve's own accuracy."""
     codes, nrm, sep, b = spheres_case(n, 8, 21)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
     A = xf.Operator(g)
     bv = g.vec(b)
     out = {}
-    for fuse, pqt in (("1", "1"), ("1", "0"), ("0", "1")):
+    # "12b": the bulk-staged kernel on 3 blocks, several work items each (the cross-item load stream)
+    for fuse, pqt, cap in (("1", "2", None), ("1", "2", "3"), ("1", "1", None), ("1", "0", None), ("0", "1", None)):
         monkeypatch.setenv("XF_PQ_FUSE", fuse)
         monkeypatch.setenv("XF_PQT", pqt)
+        if cap:
+            monkeypatch.setenv("XF_PQB_BLOCKS", cap)
+        else:
+            monkeypatch.delenv("XF_PQB_BLOCKS", raising=False)
         x = g.vec(np.zeros(g.shape))
         st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=1e-9)
         assert st.status == capi.XF_OK and st.rel_resid <= 1e-9
-        out[fuse + pqt] = (st, x.download())
+        out[fuse + pqt + ("b" if cap else "")] = (st, x.download())
+    monkeypatch.delenv("XF_PQB_BLOCKS", raising=False)
     s0, x0 = out["01"]
     sm = codes != 0
-    for key in ("11", "10"):
+    for key in ("12", "12b", "11", "10"):
         s1, x1 = out[key]
         assert abs(s1.iterations - s0.iterations) <= 2, (key, s1.iterations, s0.iterations)
         d = (x1 - x1[sm].mean()) - (x0 - x0[sm].mean())

@@ -636,18 +636,28 @@ static void launch_pqt(const xf_op* op, const float* r, float* pb0, float* pb1, 
 }
 
 // p' = r + beta p (p in pb[I_PBUF]), q = A p', (p', q), alpha, flip: the
-// shared-memory tiled kernel where the plane allows it, else the register
-// march.  variant: 0 automatic, 1 register march, 2 tiled.
+// bulk-staged kernel (xf_cgb.cu) where the plane allows it, else the
+// shared-memory tiled kernel, else the register march.  variant: 0
+// automatic, 1 register march, 2 tiled, 3 bulk-staged.
+bool xf_cg_pqb_supported(const xf_grid* g);
+void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
-  const char* env = getenv("XF_PQT");   // "0": the register march even where the tile fits
-  xf_cg_pq32_variant(op, r, pb0, pb1, q, (env && env[0] == '0') ? 1 : 0);
+  // XF_PQT: "0" the register march, "1" the tiled kernel, "2" the bulk-staged
+  // kernel (each where the plane allows it); unset: automatic
+  const char* env = getenv("XF_PQT");
+  const int v = !env ? 0 : env[0] == '0' ? 1 : env[0] == '1' ? 2 : env[0] == '2' ? 3 : 0;
+  xf_cg_pq32_variant(op, r, pb0, pb1, q, v);
 }
 bool xf_cg_pqt_supported(const xf_grid* g) { return pqt_supported(g); }
 
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant) {
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
+  if ((variant == 0 || variant == 3) && xf_cg_pqb_supported(g)) {
+    xf_cg_pqb_launch(op, r, pb0, pb1, q);
+    return;
+  }
   if (variant != 1 && pqt_supported(g)) {
     launch_pqt(op, r, pb0, pb1, q);
     return;
