@@ -36,7 +36,6 @@ namespace {
 constexpr int PQB_THREADS = 256;
 constexpr int PQB_TILE = 8 * PQB_THREADS;   // 2048 plane cells per tile
 constexpr int PQB_HALF = PQB_TILE / 2;
-constexpr int PQB_NS = 2;                   // raw ring depth (planes in flight)
 constexpr int PQB_NP = 3;                   // p' plane ring: i-1, i, i+1
 
 struct PqbArgs {
@@ -57,7 +56,8 @@ __device__ __forceinline__ float4 fma4(float b, float4 p, float4 r) {
 }
 __device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
-__global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant__ PqbArgs a) {
+template <int PQB_NS>   // raw ring depth (planes in flight)
+__global__ void __launch_bounds__(PQB_THREADS, PQB_NS == 1 ? 4 : PQB_NS == 2 ? 3 : 2) k_cg_pqb(const __grid_constant__ PqbArgs a) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ double sh[32];
   __shared__ bool last;
@@ -88,23 +88,27 @@ __global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant
   __syncthreads();
 
   // The load stream: for each of this block's items, planes lo..hi (the
-  // chunk's planes and one on either side, inside the box).
-  auto item_range = [&](int item, int& base, int& i0, int& i1, int& lo, int& hi) {
+  // chunk's planes and one on either side, inside the box), upwards for even
+  // chunks and downwards for odd ones, so that the two blocks sharing a chunk
+  // boundary read its planes at about the same time (the second read hits L2).
+  auto item_range = [&](int item, int& base, int& i0, int& i1, int& lo, int& hi, int& dir) {
     const int ic = item / a.tiles;
     base = (item - ic * a.tiles) * PQB_TILE;
     i0 = ic * a.chunk;
     i1 = min(n1, i0 + a.chunk);
     lo = max(i0 - 1, 0);
     hi = min(i1, n1 - 1);
+    dir = (ic & 1) ? -1 : 1;
   };
   // producer state (thread 0 only)
-  int p_item = blockIdx.x, p_plane = 0, p_base = 0, p_hi = -1;
+  int p_item = blockIdx.x, p_plane = 0, p_base = 0, p_end = 0, p_dir = 1;
   long long issued = 0;
   auto p_start_item = [&]() {
     if (p_item < items) {
-      int i0, i1, lo;
-      item_range(p_item, p_base, i0, i1, lo, p_hi);
-      p_plane = lo;
+      int i0, i1, lo, hi;
+      item_range(p_item, p_base, i0, i1, lo, hi, p_dir);
+      p_plane = p_dir > 0 ? lo : hi;
+      p_end = p_dir > 0 ? hi : lo;
     }
   };
   auto issue_one = [&]() -> bool {
@@ -118,9 +122,11 @@ __global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant
     bulk_g2s(dst, r + c_lo, bytes, &mbar[s]);
     bulk_g2s(dst + RL, po + c_lo, bytes, &mbar[s]);
     issued++;
-    if (++p_plane > p_hi) {
+    if (p_plane == p_end) {
       p_item += gridDim.x;
       p_start_item();
+    } else {
+      p_plane += p_dir;
     }
     return true;
   };
@@ -144,24 +150,27 @@ __global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant
   long long waited = 0;       // loads thread 0 has seen land
   long long item_first = 0;   // stream index of the current item's first plane
   for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
-    int base, i0, i1, lo, hi;
-    item_range(item, base, i0, i1, lo, hi);
+    int base, i0, i1, lo, hi, dir;
+    item_range(item, base, i0, i1, lo, hi, dir);
     const int xa = base + 4 * threadIdx.x, xb = xa + PQB_HALF;   // this thread's two groups
     const bool va = xa < P, vb = xb < P;                         // P % 4 == 0: whole groups
     const int sa = HA + 4 * threadIdx.x, sb = sa + PQB_HALF;     // their region index
-    uchar4 ka = make_uchar4(0, 0, 0, 0), kb = ka;
-    if (va) ka = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)i0 * P + xa);
-    if (vb) kb = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)i0 * P + xb);
+    uchar4 ka = make_uchar4(0, 0, 0, 0), kb = ka;   // row kinds of the first plane computed
+    const int kfirst = dir > 0 ? i0 : i1 - 1;
+    if (va) ka = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)kfirst * P + xa);
+    if (vb) kb = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)kfirst * P + xb);
     bool wok = true;
     // own p'(i-1) in registers: the ring slot of plane i-1 is rewritten during
     // step i+1, possibly while a slower warp is still in step i
     float4 xma = make_float4(0.f, 0.f, 0.f, 0.f), xmb = xma;
-    // step i: p'(i+1) of the region into the p' ring, then q of plane i
-    for (int i = i0 - 2; i < i1; i++) {
-      const int j = i + 1;
+    // step i: p'(j) of the region into the p' ring, j = i + dir the next
+    // plane in march order, then q of plane i
+    const int first = dir > 0 ? i0 - 2 : i1 + 1, stop = dir > 0 ? i1 : i0 - 1;
+    for (int i = first; i != stop; i += dir) {
+      const int j = i + dir;
       const bool load = j >= lo && j <= hi;
       if (load) {
-        const long long L = item_first + (j - lo);
+        const long long L = item_first + (dir > 0 ? j - lo : hi - j);
         wok = mbar_wait_bounded(&mbar[L % PQB_NS], (uint32_t)((L / PQB_NS) & 1));
         if (wok) {
           waited = L + 1;
@@ -185,20 +194,20 @@ __global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant
       }
       // next plane's row kinds, in flight during this plane
       uchar4 kna = ka, knb = kb;
-      if (i >= i0 && i + 1 < i1) {
-        if (va) kna = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)(i + 1) * P + xa);
-        if (vb) knb = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)(i + 1) * P + xb);
+      if (i >= i0 && i < i1 && j >= i0 && j < i1) {
+        if (va) kna = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)j * P + xa);
+        if (vb) knb = *reinterpret_cast<const uchar4*>(a.kind + (int64_t)j * P + xb);
       }
       if (__syncthreads_or(!wok)) { ok = false; break; }
       if (load) release();   // plane j's slot is consumed
-      if (i == i0 - 1 && i >= 0) {   // p'(i0-1), written during the previous step
+      if (i == (dir > 0 ? i0 - 1 : i1) && i >= 0 && i < n1) {   // the plane before the chunk, written last step
         const float* pc = pring + (size_t)((i + PQB_NP) % PQB_NP) * RL;
         xma = lds4(pc + sa);
         xmb = lds4(pc + sb);
       }
-      if (i >= i0) {
+      if (i >= i0 && i < i1) {
         const float* pc = pring + (size_t)((i + PQB_NP) % PQB_NP) * RL;
-        const float* pp = pring + (size_t)((i + 1 + PQB_NP) % PQB_NP) * RL;
+        const float* pp = pring + (size_t)((j + PQB_NP) % PQB_NP) * RL;
         const float4 xca = lds4(pc + sa), xcb = lds4(pc + sb);
         // k-1 / k+1 of the group ends from the neighbouring lanes (lane 0 / 31 from shared memory)
         const float la = __shfl_up_sync(0xffffffffu, xca.w, 1), lb = __shfl_up_sync(0xffffffffu, xcb.w, 1);
@@ -269,7 +278,7 @@ __global__ void __launch_bounds__(PQB_THREADS, 3) k_cg_pqb(const __grid_constant
   }
 }
 
-size_t pqb_smem(int RL) { return 128 + (size_t)(PQB_NS * 2 + PQB_NP) * RL * sizeof(float); }
+size_t pqb_smem(int RL, int ns) { return 128 + (size_t)(ns * 2 + PQB_NP) * RL * sizeof(float); }
 
 }  // namespace
 
@@ -279,7 +288,7 @@ bool xf_cg_pqb_supported(const xf_grid* g) {
   const int64_t P = (int64_t)g->n2 * g->n3;
   if (P % 4 != 0 || g->n3 % 2 != 0 || g->n3 < 2 || g->n2 < 2 || P > (1 << 30)) return false;
   const int HA = (g->n3 + 1 + 3) & ~3;
-  return pqb_smem(PQB_TILE + 2 * HA) <= 227 * 1024 - 1024;
+  return pqb_smem(PQB_TILE + 2 * HA, 2) <= 227 * 1024 - 1024;
 }
 
 void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
@@ -293,15 +302,20 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
   a.RL = PQB_TILE + 2 * a.HA;
   a.tiles = (a.P + PQB_TILE - 1) / PQB_TILE;
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
-  const size_t smem = pqb_smem(a.RL);
-  static size_t attr_smem = 0;
-  if (attr_smem < smem) {
-    cudaFuncSetAttribute(k_cg_pqb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_smem = smem;
+  // ring depth 2 (3 blocks per SM); XF_PQB_NS = 1 or 4 selects the 1-deep ring
+  // (4 blocks per SM) or the 4-deep one (2 blocks per SM)
+  int ns = 2;
+  if (const char* env = getenv("XF_PQB_NS")) ns = env[0] == '1' ? 1 : (env[0] == '4' && pqb_smem(a.RL, 4) <= 112 * 1024) ? 4 : 2;
+  const size_t smem = pqb_smem(a.RL, ns);
+  static size_t attr_smem[5] = {0, 0, 0, 0, 0};
+  if (attr_smem[ns] < smem) {
+    cudaFuncSetAttribute(ns == 1 ? k_cg_pqb<1> : ns == 4 ? k_cg_pqb<4> : k_cg_pqb<2>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_smem[ns] = smem;
   }
   // resident blocks per SM from shared memory (1 KB reserved per block) and the launch bounds
   int resident = (int)((228 * 1024) / (smem + 1024 + 1024));
-  if (resident > 3) resident = 3;
+  if (resident > (ns == 1 ? 4 : 3)) resident = ns == 1 ? 4 : 3;
   if (resident < 1) resident = 1;
   const int64_t B = (int64_t)ctx->sm_count * resident;
   // plane chunk: the length whose last wave wastes least (cost ~ waves x (chunk + 1))
@@ -322,5 +336,10 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
     const long cap = strtol(env, nullptr, 10);
     if (cap >= 1 && cap < blocks) blocks = cap;
   }
-  k_cg_pqb<<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
+  if (ns == 1)
+    k_cg_pqb<1><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
+  else if (ns == 4)
+    k_cg_pqb<4><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
+  else
+    k_cg_pqb<2><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
 }
