@@ -6,6 +6,8 @@
 // its operand layout and descriptors are checked on their own.
 #include <cuda_bf16.h>
 
+#include <stdlib.h>
+
 #include "xf_common.cuh"
 #include "xf_tc.cuh"
 
@@ -259,6 +261,226 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
   if (warp == 0) tc::tmem_dealloc(tbase, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// The same convolution with the three k-taps of each (di, dj) stacked along N.
+//
+// A tcgen05.mma of M = 128, K = 16 costs about the same time for any N up to
+// 32 (about 39 cycles on GB300; 44 at N = 64, 60 at 128), so one MMA of
+// N = 3 Co replaces three of N = Co.  For slab (di, dj) the A operand is the
+// 128 rows X[c0 - 1 + di P + dj n3 + r], the B operand the taps (di, dj, -1),
+// (di, dj, 0), (di, dj, +1) stacked, [3 Co][Ci] (consecutive in the weight
+// layout [27][Co][Ci]); TMEM accumulates D_dk over the nine slabs, and the
+// epilogue applies the k shift on the output side:
+//     y[c0 + r - 1] = D_-1[r - 1] + D_0[r] + D_+1[r + 1],   r = 1 .. 126,
+// neighbouring TMEM rows coming from the neighbouring lanes (warp shuffles; a
+// shared-memory exchange across warps).  A tile therefore yields 126 cells;
+// the last tile starts at ncell - 126 (its overlap rewrites identical values)
+// so that every row read stays inside the zero margins.
+//
+// Operands (slab x channel chunk of KC <= 48 channels) are copied with
+// cp.async (16 bytes per copy) into a ring of ST_STAGES shared-memory stages;
+// a stage is refilled once the MMAs that read it two steps earlier have
+// committed to its mbarrier.  Requires 3 Co <= 256 (Co <= 80).
+constexpr int ST_STAGES = 4;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int KC>   // channels per pipeline step (16, 32 or 48)
+__global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t mbar[ST_STAGES];
+  __shared__ uint32_t tmem_base;
+  __shared__ float xch[2][4][80];   // per warp: lane 31's D_-1 row, lane 0's D_+1 row
+  constexpr int kg = KC / 8;        // 16-byte chunks per operand row
+  const int Ci = a.Ci, Co = a.Co, N3 = 3 * Co;
+  const int nk = Ci / KC;           // channel chunks per slab
+  const int units = 9 * nk;         // pipeline steps per tile
+  const int stage_a = 128 * KC * 2, stage_b = N3 * KC * 2, stage = stage_a + stage_b;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = tmem_cols(N3);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+  if (threadIdx.x == 0)
+    for (int s = 0; s < ST_STAGES; s++) tc::mbar_init(&mbar[s], 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = tmem_base;
+  const uint32_t idesc = tc::idesc_bf16_f32(128, N3);
+  const uint32_t lbo = 128, sbo = (uint32_t)kg * 128;
+  const int64_t P = (int64_t)a.n2 * a.n3;
+  const int64_t ntiles = (a.ncell + 125) / 126;
+  const int my_tiles = ntiles > blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  const int total = my_tiles * units;   // this CTA's pipeline steps
+  auto tile_start = [&](int k) {         // first output cell of this CTA's k-th tile
+    const int64_t st = ((int64_t)blockIdx.x + (int64_t)k * gridDim.x) * 126;
+    return st + 126 > a.ncell ? (a.ncell > 126 ? a.ncell - 126 : (int64_t)0) : st;
+  };
+  // This thread's A copy chunks, fixed for every step: rows r = v / kg, chunk
+  // q = v % kg for v = tid + 128 i (i < kg): shared offsets and global offsets
+  // relative to the step's first row.
+  uint32_t a_soff[kg];
+  int64_t a_goff[kg];
+#pragma unroll
+  for (int i = 0; i < kg; i++) {
+    const int v = threadIdx.x + 128 * i, r = v / kg, q = v - r * kg;
+    a_soff[i] = (uint32_t)((r >> 3) * kg * 128 + q * 128 + (r & 7) * 16);
+    a_goff[i] = (int64_t)r * a.in_ld + q * 8;
+  }
+  // producer counters of the step being issued: tile kp, slab sp, channel chunk cpk
+  int kp = 0, sp = 0, cpk = 0;
+  int64_t row_base = my_tiles ? tile_start(0) - 1 : 0;
+  auto issue = [&](int gp) {   // copies of step gp into stage gp % ST_STAGES (an empty group past the end)
+    if (gp < total) {
+      const int di = sp / 3 - 1, dj = sp % 3 - 1;
+      const int64_t row0 = row_base + di * P + dj * (int64_t)a.n3;
+      uint8_t* sA = smem + (gp % ST_STAGES) * stage;
+      uint8_t* sB = sA + stage_a;
+      const uint16_t* src_a = a.in + row0 * a.in_ld + cpk * KC;
+#pragma unroll
+      for (int i = 0; i < kg; i++) cp_async16(sA + a_soff[i], src_a + a_goff[i]);
+      const uint16_t* src_b = a.W + (int64_t)sp * N3 * Ci + cpk * KC;
+      for (int v = threadIdx.x; v < N3 * kg; v += 128) {
+        const int n = v / kg, q = v - n * kg;
+        cp_async16(sB + (n >> 3) * kg * 128 + q * 128 + (n & 7) * 16, src_b + (int64_t)n * Ci + q * 8);
+      }
+      // advance to the next step
+      if (++cpk == nk) {
+        cpk = 0;
+        if (++sp == 9) {
+          sp = 0;
+          if (++kp < my_tiles) row_base = tile_start(kp) - 1;
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  bool ok = true;
+  // Commits into stage st complete in order; step g is commit g / ST_STAGES of
+  // its stage.  seen[st] counts the ones observed, so a wait is idempotent and
+  // the barrier is never more than one phase ahead of it.
+  uint32_t seen[ST_STAGES] = {0, 0, 0, 0};
+  auto wait_stage = [&](int g) {   // MMAs of step g have finished
+    const int st = g % ST_STAGES;
+    const uint32_t idx = (uint32_t)(g / ST_STAGES);
+    while (ok && seen[st] <= idx) {
+      if (!tc::mbar_wait(&mbar[st], seen[st] & 1)) { ok = false; break; }
+      seen[st]++;
+    }
+  };
+  int64_t commits[ST_STAGES] = {0, 0, 0, 0};   // thread 0: commits issued per stage
+  issue(0);
+  issue(1);
+  int k = 0, u = 0;   // consumer: tile and step within it of step g
+  for (int g = 0; g < total && ok; g++) {
+    // refill the stage of step g - 2 (its MMAs committed two steps ago) with step g + 2
+    if (g >= 2) wait_stage(g - 2);
+    issue(g + 2);
+    cp_async_wait<2>();   // this thread's copies of step g have landed
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    tc::fence_after_sync();
+    if (threadIdx.x == 0) {
+      const uint8_t* sA = smem + (g % ST_STAGES) * stage;
+      const uint8_t* sB = sA + stage_a;
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; kk++) {
+        const uint64_t ad = tc::smem_desc(tc::smem_addr(sA + kk * 256), lbo, sbo);
+        const uint64_t bd = tc::smem_desc(tc::smem_addr(sB + kk * 256), lbo, sbo);
+        tc::mma_bf16(tbase, ad, bd, idesc, u > 0 || kk > 0);
+      }
+      tc::mma_commit(&mbar[g % ST_STAGES]);
+      commits[g % ST_STAGES]++;
+    }
+    if (++u != units) continue;
+    u = 0;
+    // ---- epilogue of the tile: the accumulator is complete once step g's MMAs are
+    wait_stage(g);
+    if (!__syncthreads_and(ok)) { ok = false; break; }
+    tc::fence_after_sync();
+    const int64_t c0 = tile_start(k++);
+    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
+    // pass 1: rows at the warp edges for the neighbouring warps
+    for (int co = 0; co < Co; co += 8) {
+      float dm[8], dp[8];
+      tc::tmem_ld8(trow + (uint32_t)co, dm);
+      tc::tmem_ld8(trow + (uint32_t)(2 * Co + co), dp);
+      if (lane == 31)
+        for (int q = 0; q < 8; q++) xch[0][warp][co + q] = dm[q];
+      if (lane == 0)
+        for (int q = 0; q < 8; q++) xch[1][warp][co + q] = dp[q];
+    }
+    __syncthreads();
+    const int r = warp * 32 + lane;
+    const int64_t c = c0 + r - 1;
+    const bool live = r >= 1 && r <= 126 && c < a.ncell;
+    const float m = live ? (float)a.mask[c] : 0.f;
+    for (int co = 0; co < Co; co += 8) {
+      float dm[8], d0[8], dp[8];
+      tc::tmem_ld8(trow + (uint32_t)co, dm);
+      tc::tmem_ld8(trow + (uint32_t)(Co + co), d0);
+      tc::tmem_ld8(trow + (uint32_t)(2 * Co + co), dp);
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float prev = __shfl_up_sync(0xffffffffu, dm[q], 1);
+        float next = __shfl_down_sync(0xffffffffu, dp[q], 1);
+        if (lane == 0) prev = warp > 0 ? xch[0][warp - 1][co + q] : 0.f;
+        if (lane == 31) next = warp < 3 ? xch[1][warp + 1][co + q] : 0.f;
+        v[q] = prev + d0[q] + next;
+      }
+      if (!live || co >= a.out_ch) continue;
+      uint16_t gt[8];
+      if (a.gate) *reinterpret_cast<uint4*>(gt) = *reinterpret_cast<const uint4*>(a.gate + c * a.gate_ld + co);
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float x = v[q] + (a.bias ? a.bias[co + q] : 0.f);
+        if (a.relu) x = fmaxf(x, 0.f);
+        if (a.gate && ((gt[q] & 0x8000u) || !(gt[q] & 0x7FFFu))) x = 0.f;   // gate value <= 0
+        v[q] = x * m;
+      }
+      if (a.out16) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+          pk[q] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(a.out16 + c * a.out_ld + co) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      } else {
+        const int nq = min(8, a.out_ch - co);
+        for (int q = 0; q < nq; q++) a.out32[c * a.out_ld + co + q] = v[q];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();   // TMEM and the exchange rows are read before the next tile reuses them
+  }
+  cp_async_wait<0>();   // no copy may land after the block leaves
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+  }
+  // every commit thread 0 issued has been observed (bounded waits) before TMEM is freed
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < ST_STAGES; st++) {
+      while ((int64_t)seen[st] < commits[st]) {
+        if (!tc::mbar_wait(&mbar[st], seen[st] & 1)) break;
+        seen[st]++;
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, ncols);
+}
+
 // Error flag of the convolutions: a slot of the context scratch, cleared by
 // xf_conv_status.
 constexpr int I_CONV_ERR = 60;
@@ -277,6 +499,24 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
   a.out16 = out_fp32 ? nullptr : (uint16_t*)out;
   a.out32 = out_fp32 ? (float*)out : nullptr;
   a.out_ld = out_ld; a.out_ch = out_ch; a.relu = relu; a.err = err;
+  const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
+  if (3 * co <= 256 && !(getenv("XF_CONV_TAPS") && getenv("XF_CONV_TAPS")[0] == '1')) {
+    // k-taps stacked along N (XF_CONV_TAPS=1 selects the per-tap kernel)
+    const int KC = ci == 16 ? 16 : ci == 48 ? 48 : ci % 32 == 0 ? 32 : 16;
+    auto kern = KC == 16 ? k_conv3_st<16> : KC == 32 ? k_conv3_st<32> : k_conv3_st<48>;
+    const size_t smem = (size_t)ST_STAGES * ((128 + 3 * co) * KC * 2);
+    XF_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = (int)((227 * 1024) / (smem + 3 * 1024 + 1024));
+    per_sm = min(per_sm, (int)(512 / tmem_cols(3 * co)));
+    per_sm = min(per_sm, 16);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t tiles = (a.ncell + 125) / 126;
+    int64_t blocks = (int64_t)ctx->sm_count * per_sm;
+    if (blocks > tiles) blocks = tiles;
+    kern<<<(int)blocks, 128, smem, ctx->stream>>>(a);
+    XF_CUDA(ctx, cudaGetLastError());
+    return XF_OK;
+  }
   const size_t smem = (size_t)CONV_STAGES * (TC_M * ci * 2 + co * ci * 2);
   XF_CUDA(ctx, cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // Residency from the kernel's real limits: shared memory (227 KB per SM, with
@@ -286,7 +526,6 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
   per_sm = min(per_sm, (int)(512 / tmem_cols(co)));
   per_sm = min(per_sm, 16);
   if (per_sm < 1) per_sm = 1;
-  const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
   int64_t blocks = (int64_t)ctx->sm_count * per_sm;
   if (blocks > ntiles) blocks = ntiles;
   k_conv3_tc<<<(int)blocks, 128, smem, ctx->stream>>>(a);
