@@ -200,7 +200,12 @@ enum {
   XF_FCG = 5             /* flexible CG with a preconditioner                      */
 };
 enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
-enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2 };
+/* XF_PRECOND_CHEB: XF_CG with XF_PREC_MIXED on a uniform Laplace grid without
+ * boundary rows, preconditioned by z = p(A) r, p the degree-2 polynomial of
+ * two Chebyshev-iteration steps over [lambda_max / ratio, lambda_max]
+ * (lambda_max the Gershgorin bound; ratio = opts.reserved[1], default 30),
+ * both stencil applications in one pass over memory. */
+enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3 };
 
 typedef struct {
   int method;            /* XF_CG ...                                              */

@@ -266,11 +266,16 @@ class PackedOperator(Operator):
 
 
 def solve_opts(method=XF_CG, precision=XF_PREC_FP64, rtol=1e-8, atol=0.0, maxit=100000, replace_every=50,
-               check_every=16, exact=False):
+               check_every=16, exact=False, precond=None, cheb_ratio=0):
+    """precond: capi.XF_PRECOND_CHEB with XF_CG and XF_PREC_MIXED for the polynomial preconditioner
+    (cheb_ratio: its lambda_max / lambda_min, 0 for the default)."""
     o = capi.SolveOpts()
     capi.lib().xf_solve_opts_default(C.byref(o))
     o.method, o.precision, o.rtol, o.atol, o.maxit = method, precision, rtol, atol, maxit
     o.replace_every, o.check_every, o.exact = replace_every, check_every, int(exact)
+    if precond is not None:
+        o.precond = precond
+    o.reserved[1] = int(cheb_ratio)
     return o
 
 

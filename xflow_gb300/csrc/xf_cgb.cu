@@ -49,6 +49,7 @@ struct PqbArgs {
   int HA, RL;                 // halo width (multiple of 4, >= n3 + 1), region length TILE + 2 HA
   int tiles, chunk, nchunk;   // work items: nchunk plane chunks x tiles
   float cx, cy, cz;
+  int ctl;                    // control step of the last block
 };
 
 __device__ __forceinline__ float4 fma4(float b, float4 p, float4 r) {
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(PQB_THREADS, PQB_NS == 1 ? 4 : PQB_NS == 2 ? 3
   if (threadIdx.x == 0) {
     S->scalars[SL_A] = tot;
     S->tickets[SL_A] = 0;
-    control_step(S, CTL_CG_ALPHA_FLIP);
+    control_step(S, a.ctl);
   }
 }
 
@@ -291,7 +292,7 @@ bool xf_cg_pqb_supported(const xf_grid* g) {
   return pqb_smem(PQB_TILE + 2 * HA, 2) <= 227 * 1024 - 1024;
 }
 
-void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
+void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int ctl) {
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
   PqbArgs a;
@@ -302,6 +303,7 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
   a.RL = PQB_TILE + 2 * a.HA;
   a.tiles = (a.P + PQB_TILE - 1) / PQB_TILE;
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
+  a.ctl = ctl;
   // ring depth 2 (3 blocks per SM); XF_PQB_NS = 1 or 4 selects the 1-deep ring
   // (4 blocks per SM) or the 4-deep one (2 blocks per SM)
   int ns = 2;

@@ -640,7 +640,7 @@ static void launch_pqt(const xf_op* op, const float* r, float* pb0, float* pb1, 
 // shared-memory tiled kernel, else the register march.  variant: 0
 // automatic, 1 register march, 2 tiled, 3 bulk-staged.
 bool xf_cg_pqb_supported(const xf_grid* g);
-void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q);
+void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int ctl = CTL_CG_ALPHA_FLIP);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q) {
   // XF_PQT: "0" the register march, "1" the tiled kernel, "2" the bulk-staged

@@ -1,0 +1,354 @@
+// K0 of the polynomially preconditioned mixed CG:
+//
+//   z = p(A) r,   (r, z) -> beta
+//
+// on uniform Laplace grids, p the degree-2 polynomial of two steps of the
+// Chebyshev iteration for A z = r over [lambda_max / ratio, lambda_max]
+// (positive on the spectrum, so p(A) is symmetric positive definite), in
+// Horner form
+//
+//   y1 = a1 r + a2 (A r),   z = a0 r + A y1,
+//
+// both stencil levels in one pass over memory.  A block owns a tile of
+// CP_TILE consecutive cells of the flattened (j, k) plane and marches a chunk
+// of i-planes.  The raw r of each plane (tile plus a halo of 2 HA cells,
+// HA >= n3 + 1, on either side) arrives by bulk asynchronous copy
+// (cp.async.bulk) into a CP_NS-deep ring; at step t the block
+//   - computes level 1 for plane t-1 over the tile plus one halo (y1 into a
+//     four-plane ring),
+//   - computes level 2 for plane t-3 on its own cells (z to global memory,
+//     the (r, z) partial),
+//   - loads the row kinds of plane t for the next step's level 1,
+// and synchronises once.  The stencil is the fast Laplace row of the CG
+// kernels (open-face diagonal, uniform coefficients); rows without an
+// equation give 0, so inactive cells keep z = 0.  Halo cells outside the box
+// hold stale values that only rows without an equation read.
+//
+// Every mbarrier wait is bounded; a wait that runs out records I_ERR, lets the
+// copies in flight land (bounded), ends the solve with XF_ERR_CUDA and leaves.
+#include <stdint.h>
+#include <stdlib.h>
+
+#include <vector>
+
+#include "xf_bulk.cuh"
+#include "xf_control.cuh"
+#include "xf_stencil.cuh"
+
+namespace {
+
+constexpr int CP_THREADS = 256;
+constexpr int CP_TILE = 8 * CP_THREADS;   // 2048 plane cells
+constexpr int CP_NS = 4;                  // raw ring: planes t-2, t-1, t and one in flight
+constexpr int CP_NY = 4;                  // y1 ring: planes t-4 .. t-1
+
+struct CpArgs {
+  const uint8_t* kind;
+  const float* r;
+  float* z;
+  DevScratch* S;
+  int n1, n3, P;
+  int HA, R0, R1;             // halo unit (multiple of 4), raw region TILE + 4 HA, level-1 region TILE + 2 HA
+  int tiles, chunk, nchunk;   // work items: nchunk plane chunks x tiles
+  float cx, cy, cz;           // uniform Laplace coefficients
+  float a0, a1, a2;           // Horner coefficients of p
+};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+// Fast Laplace row (uniform grid) of four consecutive cells whose centres are
+// c[0..3]: i-neighbours m, p; j-neighbours at -+n3 from s (shared memory,
+// 8-byte aligned); k-neighbours from s-1 and s+4.
+__device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, float4 m, float4 p, const float* s, int n3,
+                                     float cx, float cy, float cz, float out[4]) {
+  const float2 jm01 = *reinterpret_cast<const float2*>(s - n3), jm23 = *reinterpret_cast<const float2*>(s - n3 + 2);
+  const float2 jp01 = *reinterpret_cast<const float2*>(s + n3), jp23 = *reinterpret_cast<const float2*>(s + n3 + 2);
+  const float cc[4] = {c.x, c.y, c.z, c.w};
+  const float mm[4] = {m.x, m.y, m.z, m.w};
+  const float pp[4] = {p.x, p.y, p.z, p.w};
+  const float jm[4] = {jm01.x, jm01.y, jm23.x, jm23.y};
+  const float jp[4] = {jp01.x, jp01.y, jp23.x, jp23.y};
+  const float km[4] = {s[-1], cc[0], cc[1], cc[2]};
+  const float kp[4] = {cc[1], cc[2], cc[3], s[4]};
+  const uint8_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    float o = fmaf(dtab[kk[v] & 63], cc[v], -fmaf(cx, pp[v] + mm[v], fmaf(cy, jp[v] + jm[v], cz * (kp[v] + km[v]))));
+    if ((kk[v] >> K_ROW_SHIFT) == ROW_NONE) o = 0.f;
+    out[v] = o;
+  }
+}
+
+__global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constant__ CpArgs a) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ double sh[32];
+  __shared__ bool last;
+  __shared__ float dtab[64];
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  const int n1 = a.n1, n3 = a.n3, P = a.P, HA = a.HA, R0 = a.R0, R1 = a.R1;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
+  float* ring = reinterpret_cast<float*>(smem + 128);          // CP_NS x R0 raw r
+  float* yring = ring + (size_t)CP_NS * R0;                     // CP_NY x R1 level-1 planes
+  uint8_t* kbuf = reinterpret_cast<uint8_t*>(yring + (size_t)CP_NY * R1);   // 2 x R1 row kinds
+  const int64_t total = (int64_t)n1 * P;
+  const int items = a.nchunk * a.tiles;
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x;
+    dtab[b] = a.cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + a.cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
+              a.cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CP_NS; s++) mbar_init(&mbar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  auto item_range = [&](int item, int& base, int& i0, int& i1, int& lo, int& hi) {
+    const int ic = item / a.tiles;
+    base = (item - ic * a.tiles) * CP_TILE;
+    i0 = ic * a.chunk;
+    i1 = min(n1, i0 + a.chunk);
+    lo = max(i0 - 2, 0);
+    hi = min(i1 + 1, n1 - 1);
+  };
+  // producer (thread 0): the stream of raw planes over this block's items
+  int p_item = blockIdx.x, p_plane = 0, p_base = 0, p_hi = -1;
+  long long issued = 0;
+  auto p_start_item = [&]() {
+    if (p_item < items) {
+      int i0, i1, lo;
+      item_range(p_item, p_base, i0, i1, lo, p_hi);
+      p_plane = lo;
+    }
+  };
+  auto issue_one = [&]() -> bool {
+    if (p_item >= items) return false;
+    const int s = (int)(issued % CP_NS);
+    const int64_t reg_lo = (int64_t)p_plane * P + p_base - 2 * HA, reg_hi = reg_lo + R0;
+    const int64_t c_lo = reg_lo < 0 ? 0 : reg_lo, c_hi = reg_hi > total ? total : reg_hi;
+    const uint32_t bytes = (uint32_t)(c_hi - c_lo) * 4u;
+    mbar_expect_tx(&mbar[s], bytes);
+    bulk_g2s(ring + (size_t)s * R0 + (c_lo - reg_lo), a.r + c_lo, bytes, &mbar[s]);
+    issued++;
+    if (++p_plane > p_hi) {
+      p_item += gridDim.x;
+      p_start_item();
+    }
+    return true;
+  };
+  if (threadIdx.x == 0) {
+    p_start_item();
+    for (int s = 0; s < CP_NS; s++)
+      if (!issue_one()) break;
+  }
+  long long released = 0;
+  auto release = [&]() {
+    released++;
+    if (threadIdx.x == 0) {
+      fence_proxy_async();
+      while (issued < released + CP_NS && issue_one()) {
+      }
+    }
+  };
+
+  DotAcc<float> acc;
+  bool ok = true;
+  long long waited = 0;
+  long long item_first = 0;
+  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+    int base, i0, i1, lo, hi;
+    item_range(item, base, i0, i1, lo, hi);
+    const int l1lo = max(i0 - 1, 0), l1hi = min(i1, n1 - 1);   // planes of level 1
+    auto rslot = [&](int pl) {   // raw slot of a loaded plane (any slot for planes not loaded)
+      const int q = pl < lo ? lo : pl > hi ? hi : pl;
+      return ring + (size_t)((item_first + (q - lo)) % CP_NS) * R0;
+    };
+    auto yslot = [&](int pl) { return yring + (size_t)(((pl % CP_NY) + CP_NY) % CP_NY) * R1; };
+    // own cells of level 2: two groups of four at 4 t and TILE/2 + 4 t
+    const int xa = base + 4 * threadIdx.x, xb = xa + CP_TILE / 2;
+    const bool va = xa < P, vb = xb < P;
+    const int ya = HA + 4 * threadIdx.x, yb = ya + CP_TILE / 2;   // their index in the level-1 region
+    // level-2 inputs of the next plane, prefetched one step ahead
+    float4 rpa = make_float4(0.f, 0.f, 0.f, 0.f), rpb = rpa;
+    uchar4 kpa = make_uchar4(0, 0, 0, 0), kpb = kpa;
+    auto prefetch2 = [&](int pl) {
+      if (pl < i0 || pl >= i1) return;
+      const int64_t o = (int64_t)pl * P;
+      if (va) { rpa = __ldg(reinterpret_cast<const float4*>(a.r + o + xa)); kpa = *reinterpret_cast<const uchar4*>(a.kind + o + xa); }
+      if (vb) { rpb = __ldg(reinterpret_cast<const float4*>(a.r + o + xb)); kpb = *reinterpret_cast<const uchar4*>(a.kind + o + xb); }
+    };
+    // row kinds of a level-1 plane over the level-1 region (0 outside the box)
+    auto load_kinds = [&](int pl) {
+      uint8_t* kb = kbuf + (size_t)(pl & 1) * R1;
+      const int64_t x0 = (int64_t)pl * P + base - HA;   // multiple of 4
+      for (int w = threadIdx.x; w < R1 / 4; w += CP_THREADS) {
+        const int64_t x = x0 + 4 * w;
+        uint32_t v = 0;
+        if (x >= 0 && x + 4 <= total) v = __ldg(reinterpret_cast<const uint32_t*>(a.kind + x));
+        reinterpret_cast<uint32_t*>(kb)[w] = v;
+      }
+    };
+    long long rel_next = lo;   // next plane whose raw slot is released
+    bool wok = true;
+    for (int t = i0 - 2; t <= i1 + 2; t++) {
+      // (A) raw plane t has landed
+      if (t >= lo && t <= hi) {
+        const long long L = item_first + (t - lo);
+        wok = mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1)) && wok;
+        if (wok) waited = L + 1;
+      }
+      if (wok) {
+        // (B) level 1 for plane t-1: y1 = a1 r + a2 (A r) over the level-1 region
+        const int p1 = t - 1;
+        if (p1 >= l1lo && p1 <= l1hi) {
+          const float* Rc = rslot(p1);
+          const float* Rm = rslot(p1 - 1);
+          const float* Rp = rslot(p1 + 1);
+          const uint8_t* kb = kbuf + (size_t)(p1 & 1) * R1;
+          float* Y = yslot(p1);
+          for (int g = threadIdx.x; g < R1 / 4; g += CP_THREADS) {
+            const int s = HA + 4 * g;   // raw index of the group's first cell
+            const float4 c = ld4(Rc + s);
+            float ar[4];
+            lap4(dtab, *reinterpret_cast<const uchar4*>(kb + 4 * g), c, ld4(Rm + s), ld4(Rp + s), Rc + s, n3, a.cx,
+                 a.cy, a.cz, ar);
+            *reinterpret_cast<float4*>(Y + 4 * g) = make_float4(fmaf(a.a2, ar[0], a.a1 * c.x), fmaf(a.a2, ar[1], a.a1 * c.y),
+                                                                fmaf(a.a2, ar[2], a.a1 * c.z), fmaf(a.a2, ar[3], a.a1 * c.w));
+          }
+        }
+        // (C) level 2 for plane t-3: z = a0 r + A y1 on the own cells, (r, z)
+        const int p2 = t - 3;
+        if (p2 >= i0 && p2 < i1) {
+          const float* Yc = yslot(p2);
+          const float* Ym = yslot(p2 - 1);
+          const float* Yp = yslot(p2 + 1);
+          const int64_t o = (int64_t)p2 * P;
+          auto group = [&](bool v, int s, float4 rr, uchar4 k4, int x) {
+            if (!v) return;
+            float ay[4];
+            lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
+            const float4 zz = make_float4(fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
+                                          fmaf(a.a0, rr.w, ay[3]));
+            *reinterpret_cast<float4*>(a.z + o + x) = zz;
+            acc.add(rr.x, zz.x);
+            acc.add(rr.y, zz.y);
+            acc.add(rr.z, zz.z);
+            acc.add(rr.w, zz.w);
+          };
+          group(va, ya, rpa, kpa, xa);
+          group(vb, yb, rpb, kpb, xb);
+        }
+        // (D) inputs of the next step
+        if (t >= l1lo && t <= l1hi) load_kinds(t);
+        prefetch2(t - 2);
+      }
+      // (E) one barrier per step; a timed-out wait anywhere stops the block
+      if (__syncthreads_or(!wok)) { ok = false; break; }
+      // (F) raw plane t-2 has had its last reader
+      while (rel_next <= t - 2 && rel_next <= hi) { release(); rel_next++; }
+    }
+    if (!ok) break;
+    while (rel_next <= hi) { release(); rel_next++; }
+    item_first += hi - lo + 1;
+    __syncthreads();   // the next item rewrites the rings
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) {
+      atomicExch((unsigned long long*)&S->iscalars[I_ERR], 1ull);
+      for (long long L = waited; L < issued; L++) mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1));
+      S->iscalars[I_DONE] = 1;
+      S->iscalars[I_STATUS] = XF_ERR_CUDA;
+    }
+    __syncthreads();
+    return;
+  }
+  if (!publish_acc<float>(S, SL_D, SL_D, acc, sh, &last)) return;
+  double tot = finish_partials(S, SL_D, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[SL_D] = tot;
+    S->tickets[SL_D] = 0;
+    control_step(S, CTL_PCG_BETA);
+  }
+}
+
+size_t cp_smem(int R0, int R1) {
+  return 128 + (size_t)CP_NS * R0 * 4 + (size_t)CP_NY * R1 * 4 + 2 * (size_t)R1;
+}
+
+int cp_halo(int n3) { return (n3 + 1 + 3) & ~3; }
+
+}  // namespace
+
+// Monomial coefficients, in A, of the Chebyshev-iteration polynomial after two
+// matrix-vector products for A z = r over [lmax / ratio, lmax], scaled so that
+// the constant term is 1 (a positive multiple of a preconditioner leaves
+// preconditioned CG unchanged).
+void xf_cheb2_coeffs(double lmax, double ratio, float out[3]) {
+  const double lo = 1.0 / ratio, hi = 1.0;   // in units of lmax
+  const double theta = (hi + lo) / 2, delta = (hi - lo) / 2, sigma = theta / delta;
+  double rho = 1 / sigma;
+  std::vector<double> d = {1 / theta}, z = d;   // polynomials in lambda / lmax
+  for (int it = 0; it < 2; it++) {
+    std::vector<double> res(z.size() + 1, 0.0);
+    res[0] = 1.0;
+    for (size_t j = 0; j < z.size(); j++) res[j + 1] -= z[j];   // 1 - lambda z
+    const double rho_new = 1 / (2 * sigma - rho);
+    std::vector<double> dn(res.size(), 0.0);
+    for (size_t j = 0; j < d.size(); j++) dn[j] += rho_new * rho * d[j];
+    for (size_t j = 0; j < res.size(); j++) dn[j] += 2 * rho_new / delta * res[j];
+    d = dn;
+    z.resize(d.size(), 0.0);
+    for (size_t j = 0; j < d.size(); j++) z[j] += d[j];
+    rho = rho_new;
+  }
+  for (int j = 0; j < 3; j++) out[j] = (float)(z[j] / z[0] / pow(lmax, j));
+}
+
+bool xf_cg_poly_supported(const xf_grid* g) {
+  const int64_t P = (int64_t)g->n2 * g->n3;
+  if (!g->uniform || g->nbrow != 0 || P % 4 != 0 || g->n3 % 2 != 0 || g->n3 < 2 || g->n2 < 2) return false;
+  const int HA = cp_halo(g->n3);
+  return cp_smem(CP_TILE + 4 * HA, CP_TILE + 2 * HA) <= 226 * 1024;
+}
+
+void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]) {
+  const xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  CpArgs a;
+  a.kind = g->kind; a.r = r; a.z = z; a.S = ctx->scratch;
+  a.n1 = g->n1; a.n3 = g->n3; a.P = g->n2 * g->n3;
+  a.HA = cp_halo(g->n3);
+  a.R0 = CP_TILE + 4 * a.HA;
+  a.R1 = CP_TILE + 2 * a.HA;
+  a.tiles = (a.P + CP_TILE - 1) / CP_TILE;
+  a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
+  a.a0 = coeffs[0]; a.a1 = coeffs[1]; a.a2 = coeffs[2];
+  const size_t smem = cp_smem(a.R0, a.R1);
+  static size_t attr = 0;
+  if (attr < smem) {
+    cudaFuncSetAttribute(k_cg_poly2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  int resident = (int)((228 * 1024) / (smem + 2048));
+  if (resident > 2) resident = 2;
+  if (resident < 1) resident = 1;
+  const int64_t B = (int64_t)ctx->sm_count * resident;
+  int best = 8;
+  double best_cost = 1e30;
+  for (int L = 4; L <= 64; L++) {   // one wave where possible; cost ~ waves x (chunk + 5 pipeline steps)
+    const int64_t items = (int64_t)a.tiles * ((g->n1 + L - 1) / L);
+    const double cost = (double)((items + B - 1) / B) * (L + 5);
+    if (cost < best_cost) { best_cost = cost; best = L; }
+  }
+  a.chunk = best;
+  a.nchunk = (g->n1 + a.chunk - 1) / a.chunk;
+  int64_t blocks = B, items = (int64_t)a.tiles * a.nchunk;
+  if (blocks > items) blocks = items;
+  if (blocks > RED_MAX_BLOCKS) blocks = RED_MAX_BLOCKS;
+  if (const char* env = getenv("XF_POLY_BLOCKS")) {   // grid cap: several items per block (tests)
+    const long cap = strtol(env, nullptr, 10);
+    if (cap >= 1 && cap < blocks) blocks = cap;
+  }
+  k_cg_poly2<<<(int)blocks, CP_THREADS, smem, ctx->stream>>>(a);
+}

@@ -15,14 +15,15 @@ enum {
   D_RR = 32, D_RR_PREV, D_ALPHA, D_BETA, D_BB, D_THR, D_RTOL2, D_EPS,
   D_TAUK = 40, D_TAUK1, D_ALFAK, D_ALFAK1, D_RK1RK1, D_RKRK, D_EPSCUR, D_C1, D_C2, D_C3,
   D_PN = 52, D_PN1, D_AN, D_BN, D_WN, D_NORM,
-  D_ALFA = 60, D_RR64, D_BCG_A1
+  D_ALFA = 60, D_RR64, D_BCG_A1, D_RZ
 };
 // integer scalars
 // I_PAUSE: the mixed CG's inner recursion has met the tolerance (or the cap)
 // and waits for the true-residual replacement at the end of its chunk.
 // I_PBUF: which of the two direction buffers holds the current p (fused FP32
-// iteration).  I_ERR: a bounded wait in a staged kernel ran out.
-enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED, I_PAUSE, I_PBUF, I_ERR };
+// iteration).  I_ERR: a bounded wait in a staged kernel ran out.  I_PFIRST:
+// the preconditioned CG's next (r, z) starts the direction (beta = 0).
+enum { I_DONE = 0, I_STATUS, I_IT, I_REPL, I_NEEDREP, I_MAXIT, I_REPEVERY, I_MIXED, I_PAUSE, I_PBUF, I_ERR, I_PFIRST };
 
 enum {
   CTL_NONE = 0,
@@ -30,7 +31,8 @@ enum {
   CTL_RCG_INIT, CTL_RCG_TAU0, CTL_RCG_RES0, CTL_RCG_TAU, CTL_RCG_RES,
   CTL_BCGS_NORM0, CTL_BCGS_PN1, CTL_BCGS_AN, CTL_BCGS_WN, CTL_BCGS_END,
   CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES,
-  CTL_BICG_INIT, CTL_BICG_ALPHA, CTL_BICG_BETA
+  CTL_BICG_INIT, CTL_BICG_ALPHA, CTL_BICG_BETA,
+  CTL_PCG_BETA, CTL_PCG_ALPHA_FLIP, CTL_PCG_RR, CTL_PCG_REPL
 };
 
 template <typename T>
@@ -67,6 +69,7 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       d[D_RR64] = rr;
       d[D_BETA] = 0.0;   // the fused iteration forms p = r + beta p from p = 0
       I[I_IT] = 0; I[I_REPL] = 0; I[I_NEEDREP] = 0; I[I_DONE] = 0; I[I_STATUS] = XF_OK; I[I_PBUF] = 0;
+      I[I_PFIRST] = 1;
       if (isnan(rr)) finish(S, XF_NAN);
       else if (rr <= d[D_THR]) finish(S, XF_OK);
       break;
@@ -113,6 +116,43 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
         d[D_BETA] = r64 / d[D_RR_PREV];
         d[D_RR] = r64;
       }
+      break;
+    }
+    // ---- polynomially preconditioned mixed CG: rho = (r, z) ------------------
+    case CTL_PCG_BETA: {  // SL_D: (r, z) of the new residual
+      double rz = d[SL_D];
+      if (isnan(rz)) { finish(S, XF_NAN); break; }
+      if (!(rz > 0.0)) { finish(S, XF_BREAKDOWN); break; }
+      d[D_BETA] = I[I_PFIRST] ? 0.0 : rz / d[D_RZ];
+      I[I_PFIRST] = 0;
+      d[D_RZ] = rz;
+      break;
+    }
+    case CTL_PCG_ALPHA_FLIP: {  // SL_A: (p, q); the new p lives in the other buffer
+      I[I_PBUF] ^= 1;
+      double pq = d[SL_A];
+      if (isnan(pq)) finish(S, XF_NAN);
+      else if (!(pq > 0.0)) finish(S, XF_BREAKDOWN);
+      else d[D_ALPHA] = d[D_RZ] / pq;
+      break;
+    }
+    case CTL_PCG_RR: {  // SL_B: (r, r) after the update: the inner recursion's stop test
+      double rn = d[SL_B];
+      I[I_IT] += 1;
+      if (isnan(rn)) { finish(S, XF_NAN); break; }
+      d[D_RR] = rn;
+      if (rn <= d[D_THR] || I[I_IT] >= I[I_MAXIT]) I[I_PAUSE] = 1;
+      break;
+    }
+    case CTL_PCG_REPL: {  // SL_C+1: true r.r in FP64; the next (r, z) continues the direction
+      double r64 = d[SL_C + 1];
+      I[I_REPL] += 1;
+      I[I_NEEDREP] = 0;
+      I[I_PAUSE] = 0;
+      d[D_RR64] = r64;
+      if (isnan(r64)) finish(S, XF_NAN);
+      else if (r64 <= d[D_THR]) finish(S, XF_OK);
+      else if (I[I_IT] >= I[I_MAXIT]) finish(S, XF_MAXIT);
       break;
     }
     // ---- TSLAE::SolveByConjugateGradients (XSLAE.cpp:56-157) ---------------

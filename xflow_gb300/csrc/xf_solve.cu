@@ -27,6 +27,11 @@ void xf_cg_q32(const xf_op* op, const float* p, float* q);
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
 bool xf_cg_pq_supported(const xf_grid* g);
 void xf_cg_pq32(const xf_op* op, const float* r, float* pb0, float* pb1, float* q);
+bool xf_cg_pqb_supported(const xf_grid* g);
+void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int ctl);
+bool xf_cg_poly_supported(const xf_grid* g);
+void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]);
+void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 bool xf_cg_pqt_supported(const xf_grid* g);
 bool xf_cgf_supported(const xf_grid* g);
@@ -48,7 +53,7 @@ template <> struct V16<double> { typedef double2 type; };
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                                                        const T* __restrict__ q, int64_t n, DevScratch* S,
-                                                       const T* __restrict__ p_alt = nullptr) {
+                                                       const T* __restrict__ p_alt = nullptr, int ctl = CTL_CG_BETA) {
   __shared__ double sh[32];
   __shared__ bool last;
   if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
@@ -87,7 +92,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_cg_xr(T* __restrict__ x, T* __r
     if (threadIdx.x == 0) {
       S->scalars[SL_B] = t;
       S->tickets[SL_B] = 0;
-      control_step(S, CTL_CG_BETA);
+      control_step(S, ctl);
     }
   }
 }
@@ -497,7 +502,12 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   HostState hs = {0, 0, 0, 0, 0};
   double rel = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr;
-  float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr;
+  float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr, *z32 = nullptr;
+  const bool cheb = o.precond == XF_PRECOND_CHEB;
+  if (cheb && (!mixed || op->kind != XF_OP_LAPLACE || !xf_cg_poly_supported(g) || !xf_cg_pqb_supported(g)))
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED,
+                   "xf_solve: XF_PRECOND_CHEB needs mixed precision and a uniform Laplace grid without boundary rows "
+                   "(n2 n3 a multiple of 4, n3 even)");
   if (!mixed) {
     r = B.get<double>(n); p = B.get<double>(n); q = B.get<double>(n);
     if (!r || !p || !q) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
@@ -508,6 +518,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       p32b = B.get<float>(n);
       if (!p32b) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
     }
+    if (cheb && !(z32 = B.get<float>(n))) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
   }
   double* tmp = B.get<double>(n, false);
   if (!tmp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate residual");
@@ -533,6 +544,36 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         }
         k_cg_xr<double><<<xb64, RED_THREADS, 0, ctx->stream>>>(x, r, p, q, n, S);
         k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0);
+      };
+    } else if (cheb) {
+      // Polynomially preconditioned mixed CG, three kernels per iteration:
+      // K0 z = p(A) r with (r, z) and beta (both stencil levels in one pass),
+      // K1 p' = z + beta p inside the stencil with q = A p', (p', q), alpha,
+      // K2 e += alpha p', r -= alpha q with (r, r) for the stop test.  One
+      // graph chunk = `replace_every` iterations ending with the FP64 fold
+      // and the true-residual replacement; the next K0 continues the
+      // direction from the replaced residual.
+      chunk = o.replace_every;
+      float *e = e32, *r = r32, *pa = p32, *q = q32, *z = z32;
+      float* pb = p32b;
+      const double lmax = 4.0 * (g->ucx + g->ucy + g->ucz);   // Gershgorin bound of the uniform Laplace rows
+      const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : 30.0;
+      float coeffs[3];
+      xf_cheb2_coeffs(lmax, ratio, coeffs);
+      XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
+      XF_CUDA(ctx, cudaMemsetAsync(z, 0, n * 4, ctx->stream));
+      xf_cg_res64(op, x, b, r, SL_A, CTL_CG_INIT);
+      const int last = chunk - 1;
+      iter = [=](int c) {
+        xf_cg_poly_launch(op, r, z, coeffs);
+        xf_cg_pqb_launch(op, z, pa, pb, q, CTL_PCG_ALPHA_FLIP);
+        k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, r, pa, q, n, S, pb, CTL_PCG_RR);
+        if (c == last) {
+          k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
+          xf_cg_res64(op, x, b, r, SL_C, CTL_PCG_REPL);
+        }
       };
     } else if (lap && xf_cgf_supported(g) && getenv("XF_FUSED") && getenv("XF_FUSED")[0] == '1') {
       // (opt-in: measured slower than the three-kernel iteration so far)
