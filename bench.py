@@ -6,8 +6,10 @@ non-overlapping spheres with radii U[0.02, 0.06] masked Fictive; right-hand
 side = -div of an i.i.d. N(0,1) staggered velocity, projected to zero mean.
 One "step" is one solve from x = 0 to ||b - A x||_2 <= 1e-8 ||b||_2 (true
 FP64 residual).  The timed solver is the mixed-precision CG (FP32 stencil and
-vectors, FP64 dots/scalars, FP64 residual replacement every 50 iterations);
-plain FP64 CG on the same system is timed beside it as the judge.
+vectors, FP64 dots/scalars, FP64 residual replacement every 50 iterations)
+preconditioned by the degree-2 Chebyshev polynomial z = p(A) r (both stencil
+levels in one pass over memory); plain FP64 CG and the unpreconditioned
+mixed CG on the same system are timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xflow|reference]
 
@@ -226,9 +228,13 @@ def main():
     x = g.vec(np.zeros(g.shape))
     ncell = int(np.prod(g.shape))
 
-    def one(precision):
+    from xflow_gb300 import capi
+
+    cheb = {"precond": capi.XF_PRECOND_CHEB}   # the timed solver's preconditioner
+
+    def one(precision, **kw):
         x.fill(0.0)
-        return xf.solve(A, x, bv, method=xf.XF_CG, precision=precision, rtol=RTOL)
+        return xf.solve(A, x, bv, method=xf.XF_CG, precision=precision, rtol=RTOL, **kw)
 
     # FP64 plain CG: the judge (and the comparison point of the metric)
     one(xf.XF_PREC_FP64)
@@ -237,8 +243,12 @@ def main():
     fp64_ms = st64.ms
     fp64_iters = st64.iterations
 
+    # unpreconditioned mixed CG, beside it
+    one(xf.XF_PREC_MIXED)
+    st_plain = one(xf.XF_PREC_MIXED)
+
     for _ in range(args.warmup):
-        one(xf.XF_PREC_MIXED)
+        one(xf.XF_PREC_MIXED, **cheb)
     clocks = Clocks(local)
     ctx.synchronize()
     barrier(dist)
@@ -246,7 +256,7 @@ def main():
     t0 = time.perf_counter()
     dev_ms, launches, sts = [], 0, []
     for _ in range(args.steps):
-        st = one(xf.XF_PREC_MIXED)
+        st = one(xf.XF_PREC_MIXED, **cheb)
         dev_ms.append(st.ms)
         launches += int(st.reserved[0])
         sts.append(st)
@@ -271,7 +281,7 @@ def main():
         hx.numpy()[...] = 0.0
         ctx.synchronize()
         t1 = time.perf_counter()
-        s2 = xf.solve_host(A, hx.numpy(), hb.numpy(), method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL)
+        s2 = xf.solve_host(A, hx.numpy(), hb.numpy(), method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL, **cheb)
         t2 = time.perf_counter()
         if k >= args.warmup:
             e2e.append((t2 - t1) * 1e3)
@@ -283,11 +293,14 @@ def main():
     # its compulsory bytes per box cell; the dominant one by share of the
     # iteration is the headline.
     kms = xf.profile_cg_kernels(A, reps=20)
-    # compulsory bytes per box cell: pq_fused_f32 reads r, p, kind and writes
-    # p', q (17 B); the others as in their kernels' comments
+    # compulsory bytes per box cell: pq_fused_f32 reads z (or r), p, kind and
+    # writes p', q (17 B); poly2_f32 reads r, kind and writes z (9 B); the
+    # others as in their kernels' comments
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
-           "pq_fused_f32": 17, "pq_march_f32": 17}
-    if "pq_fused_f32" in kms:   # the solver's path on this grid: 2 kernels per iteration
+           "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9}
+    if "poly2_f32" in kms and "pq_fused_f32" in kms:   # the timed solver's path: 3 kernels per iteration
+        per_iter = {"poly2_f32": 1.0, "pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
+    elif "pq_fused_f32" in kms:
         per_iter = {"pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
     else:
         per_iter = {"stencil_f32": 1.0, "xr_update_f32": 1.0, "p_update_f32": 1.0, "residual_f64": 1.0 / 50}
@@ -335,12 +348,17 @@ def main():
         "config": {"workload": f"{args.size}^3 unit cube + ghost layer (box {g.shape[0]}^3), {N_SPHERES} spheres "
                                f"r~U[0.02,0.06], zero-mean -div(u) RHS, u~N(0,1), seed {SEED}",
                    "solver": "mixed-precision CG (FP32 matvec/vectors, FP64 dots, true-residual replacement/50)",
-                   "preconditioner": "none (the learned U-Net preconditioner is timed by bench.py --learned; it cuts iterations 2.8x at 256^3 but costs 40 ms per application)", "rtol": RTOL,
+                   "preconditioner": "degree-2 Chebyshev polynomial z = p(A) r over [lmax/30, lmax], both stencil "
+                                     "levels temporally blocked in one pass (the learned U-Net preconditioner is "
+                                     "timed by bench.py --learned: fewer iterations, but 27.6 ms per application)",
+                   "rtol": RTOL,
                    "l2": "working set ~0.6 GB > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},
         "iterations": st_last.iterations, "replacements": st_last.replacements, "rel_resid": st_last.rel_resid,
         "oracle_rel_resid": oracle_resid, "err_vs_fp64_cg": err_vs_fp64,
         "fp64_cg_ms": fp64_ms, "fp64_cg_iterations": fp64_iters, "fp64_cg_rel_resid": st64.rel_resid,
+        "mixed_cg_unpreconditioned": {"ms": st_plain.ms, "iterations": st_plain.iterations,
+                                      "rel_resid": st_plain.rel_resid},
         "speedup_vs_fp64_cg": fp64_ms / value if value > 0 else None,
         "wall_ms_per_step": wall / args.steps,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ncell * 8, "d2h_bytes_per_step": ncell * 8},
@@ -362,7 +380,8 @@ def main():
 
 def kernels_only(args):
     """Three launches of the FP32 and FP64 stencils and 32 iterations of the
-    mixed and FP64 CG on the full workload: a bounded command for ncu."""
+    preconditioned mixed, plain mixed and FP64 CG on the full workload: a
+    bounded command for ncu."""
     import xflow_gb300 as xf
 
     codes, sep, b = workload(args.size)
@@ -376,10 +395,12 @@ def kernels_only(args):
         for _ in range(3):
             A.apply(p, q, flags=xf.XF_ZERO_INACTIVE)
     bv = g.vec(b)
-    for prec in (xf.XF_PREC_MIXED, xf.XF_PREC_FP64):
+    from xflow_gb300 import capi
+
+    for prec, pre in ((xf.XF_PREC_MIXED, capi.XF_PRECOND_CHEB), (xf.XF_PREC_MIXED, None), (xf.XF_PREC_FP64, None)):
         x = g.vec(np.zeros(g.shape))
-        st = xf.solve(A, x, bv, method=xf.XF_CG, precision=prec, rtol=RTOL, maxit=32)
-        print(f"precision {prec}: {st.iterations} iterations, {st.ms:.2f} ms, status {st.status}")
+        st = xf.solve(A, x, bv, method=xf.XF_CG, precision=prec, rtol=RTOL, maxit=32, precond=pre)
+        print(f"precision {prec} preconditioner {pre}: {st.iterations} iterations, {st.ms:.2f} ms, status {st.status}")
     ctx.synchronize()
     return 0
 

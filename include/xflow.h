@@ -444,9 +444,9 @@ int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, co
  * direction update, [3] FP64 true residual r32 = b - A x, [4] FP64 stencil,
  * [5] FP32 stencil with the direction update fused in (p' = r + beta p,
  * q = A p', (p', q)) as the solver launches it, or -1 where the grid does not
- * take that path; [6] the same step by the register plane march where [5] is
- * the shared-memory tiled kernel, else -1.
- * ms_out holds 7 doubles.  Laplace operators only. */
+ * take that path; [6] the same step by the register plane march, else -1;
+ * [7] the polynomial preconditioner z = p(A) r with (r, z) (XF_PRECOND_CHEB),
+ * or -1.  ms_out holds 8 doubles.  Laplace operators only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
 /* ---- allocation-free inner product --------------------------------------- */

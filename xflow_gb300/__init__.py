@@ -288,13 +288,13 @@ def solve(op, x, b, **kw):
 
 
 CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "stencil_f64", "pq_fused_f32",
-              "pq_march_f32")
+              "pq_march_f32", "poly2_f32")
 
 
 def profile_cg_kernels(op, reps=20):
     """Average ms per launch of each CG-iteration kernel, timed alone
     (pq_fused_f32 is absent where the grid does not take the fused path)."""
-    out = (C.c_double * 7)()
+    out = (C.c_double * len(CG_KERNELS))()
     _check(op.grid.ctx.h, capi.lib().xf_profile_cg_kernels(op.h, int(reps), out))
     return {k: v for k, v in zip(CG_KERNELS, list(out)) if v >= 0}
 

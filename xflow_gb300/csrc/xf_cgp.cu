@@ -58,9 +58,15 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 
 // Fast Laplace row (uniform grid) of four consecutive cells whose centres are
 // c[0..3]: i-neighbours m, p; j-neighbours at -+n3 from s (shared memory,
-// 8-byte aligned); k-neighbours from s-1 and s+4.
+// 8-byte aligned); k-neighbours from the neighbouring lanes' groups (the
+// caller's consecutive lanes hold consecutive groups), s[-1] / s[4] at the
+// warp's ends.
 __device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, float4 m, float4 p, const float* s, int n3,
-                                     float cx, float cy, float cz, float out[4]) {
+                                     float cx, float cy, float cz, float out[4], bool last_group = false) {
+  const int lane = threadIdx.x & 31;
+  float left = __shfl_up_sync(0xffffffffu, c.w, 1), right = __shfl_down_sync(0xffffffffu, c.x, 1);
+  if (lane == 0) left = s[-1];
+  if (lane == 31 || last_group) right = s[4];   // the next lane holds no following group
   const float2 jm01 = *reinterpret_cast<const float2*>(s - n3), jm23 = *reinterpret_cast<const float2*>(s - n3 + 2);
   const float2 jp01 = *reinterpret_cast<const float2*>(s + n3), jp23 = *reinterpret_cast<const float2*>(s + n3 + 2);
   const float cc[4] = {c.x, c.y, c.z, c.w};
@@ -68,8 +74,8 @@ __device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, flo
   const float pp[4] = {p.x, p.y, p.z, p.w};
   const float jm[4] = {jm01.x, jm01.y, jm23.x, jm23.y};
   const float jp[4] = {jp01.x, jp01.y, jp23.x, jp23.y};
-  const float km[4] = {s[-1], cc[0], cc[1], cc[2]};
-  const float kp[4] = {cc[1], cc[2], cc[3], s[4]};
+  const float km[4] = {left, cc[0], cc[1], cc[2]};
+  const float kp[4] = {cc[1], cc[2], cc[3], right};
   const uint8_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
 #pragma unroll
   for (int v = 0; v < 4; v++) {
@@ -207,14 +213,20 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
           const float* Rp = rslot(p1 + 1);
           const uint8_t* kb = kbuf + (size_t)(p1 & 1) * R1;
           float* Y = yslot(p1);
-          for (int g = threadIdx.x; g < R1 / 4; g += CP_THREADS) {
-            const int s = HA + 4 * g;   // raw index of the group's first cell
+          // warp-uniform trip count (the shuffles need every lane); groups past
+          // the region end compute on in-bounds cells and are not stored
+          for (int g0 = 0; g0 < R1 / 4; g0 += CP_THREADS) {
+            const int g = g0 + (int)threadIdx.x;
+            const int gg = g < R1 / 4 ? g : R1 / 4 - 1;
+            const int s = HA + 4 * gg;   // raw index of the group's first cell
             const float4 c = ld4(Rc + s);
             float ar[4];
-            lap4(dtab, *reinterpret_cast<const uchar4*>(kb + 4 * g), c, ld4(Rm + s), ld4(Rp + s), Rc + s, n3, a.cx,
-                 a.cy, a.cz, ar);
-            *reinterpret_cast<float4*>(Y + 4 * g) = make_float4(fmaf(a.a2, ar[0], a.a1 * c.x), fmaf(a.a2, ar[1], a.a1 * c.y),
-                                                                fmaf(a.a2, ar[2], a.a1 * c.z), fmaf(a.a2, ar[3], a.a1 * c.w));
+            lap4(dtab, *reinterpret_cast<const uchar4*>(kb + 4 * gg), c, ld4(Rm + s), ld4(Rp + s), Rc + s, n3, a.cx,
+                 a.cy, a.cz, ar, g + 1 >= R1 / 4);
+            if (g < R1 / 4)
+              *reinterpret_cast<float4*>(Y + 4 * g) =
+                  make_float4(fmaf(a.a2, ar[0], a.a1 * c.x), fmaf(a.a2, ar[1], a.a1 * c.y),
+                              fmaf(a.a2, ar[2], a.a1 * c.z), fmaf(a.a2, ar[3], a.a1 * c.w));
           }
         }
         // (C) level 2 for plane t-3: z = a0 r + A y1 on the own cells, (r, z)
@@ -224,20 +236,28 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
           const float* Ym = yslot(p2 - 1);
           const float* Yp = yslot(p2 + 1);
           const int64_t o = (int64_t)p2 * P;
+          // (r, z) of this thread's cells: FP32 sum of the products plus the sum of
+          // their exact rounding errors, into the float-float accumulator per plane
+          float psum = 0.f, esum = 0.f;
           auto group = [&](bool v, int s, float4 rr, uchar4 k4, int x) {
-            if (!v) return;
             float ay[4];
             lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
-            const float4 zz = make_float4(fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
-                                          fmaf(a.a0, rr.w, ay[3]));
-            *reinterpret_cast<float4*>(a.z + o + x) = zz;
-            acc.add(rr.x, zz.x);
-            acc.add(rr.y, zz.y);
-            acc.add(rr.z, zz.z);
-            acc.add(rr.w, zz.w);
+            if (!v) return;
+            const float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
+                                 fmaf(a.a0, rr.w, ay[3])};
+            *reinterpret_cast<float4*>(a.z + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
+            const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const float pr = rv[q] * zz[q];
+              esum += fmaf(rv[q], zz[q], -pr);
+              psum += pr;
+            }
           };
           group(va, ya, rpa, kpa, xa);
           group(vb, yb, rpb, kpb, xb);
+          acc.add(psum, 1.f);
+          acc.add(esum, 1.f);
         }
         // (D) inputs of the next step
         if (t >= l1lo && t <= l1hi) load_kinds(t);

@@ -857,6 +857,12 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
     if (xf_cg_pqt_supported(g)) ms_out[6] = time([&] { xf_cg_pq32_variant(op, r, p, p2, q, 1); });
   }
+  ms_out[7] = -1.0;
+  if (xf_cg_poly_supported(g)) {
+    float coeffs[3];
+    xf_cheb2_coeffs(4.0 * (g->ucx + g->ucy + g->ucz), 30.0, coeffs);
+    ms_out[7] = time([&] { xf_cg_poly_launch(op, r, e, coeffs); });
+  }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   XF_CUDA(ctx, cudaGetLastError());
