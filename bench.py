@@ -137,6 +137,12 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
+def replica_value(dist, per_step_ms, world):
+    """Aggregate ms per solve of N independent replicas: the slowest rank's
+    total time over all ranks' solves (each rank ran len(per_step_ms))."""
+    return max_over_ranks(dist, float(np.sum(per_step_ms))) / (len(per_step_ms) * world)
+
+
 # ---------------------------------------------------------------------------
 def cpu_baseline(codes, sep, b, fp64_iters, sample_iters=10):
     """The oracle port's plain FP64 CG on this machine's host cores: a bounded
@@ -264,8 +270,7 @@ def main():
     wall = (time.perf_counter() - t0) * 1e3
     clk = clocks.stop()
     barrier(dist)
-    total_dev = max_over_ranks(dist, float(np.sum(dev_ms)))
-    value = total_dev / (args.steps * world)
+    value = replica_value(dist, dev_ms, world)
     xm = x.download()
     st_last = sts[-1]
 
@@ -286,7 +291,7 @@ def main():
         if k >= args.warmup:
             e2e.append((t2 - t1) * 1e3)
         assert s2.status == 0
-    e2e_ms = max_over_ranks(dist, float(np.sum(e2e))) / (args.steps * world)
+    e2e_ms = replica_value(dist, e2e, world)
 
     # Roofline: each kernel of the mixed CG iteration timed alone (CUDA events
     # on its launching stream, the solver's own launch configuration), with
