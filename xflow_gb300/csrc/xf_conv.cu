@@ -362,19 +362,19 @@ __global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
     cp_async_commit();
   };
   bool ok = true;
-  // Commits into stage st complete in order; step g is commit g / ST_STAGES of
-  // its stage.  seen[st] counts the ones observed, so a wait is idempotent and
-  // the barrier is never more than one phase ahead of it.
-  uint32_t seen[ST_STAGES] = {0, 0, 0, 0};
+  // Commits complete in issue order (each covers every earlier MMA), step g's
+  // being phase g / ST_STAGES of its stage's barrier.  `done` counts the steps
+  // this thread has seen complete, so a wait is idempotent; no stage's barrier
+  // runs a phase ahead of a waiting thread (a stage is refilled, and its next
+  // commit issued, only after every thread passed the wait for it).
+  int done = 0;
   auto wait_stage = [&](int g) {   // MMAs of step g have finished
-    const int st = g % ST_STAGES;
-    const uint32_t idx = (uint32_t)(g / ST_STAGES);
-    while (ok && seen[st] <= idx) {
-      if (!tc::mbar_wait(&mbar[st], seen[st] & 1)) { ok = false; break; }
-      seen[st]++;
+    while (ok && done <= g) {
+      if (!tc::mbar_wait(&mbar[done % ST_STAGES], (uint32_t)((done / ST_STAGES) & 1))) { ok = false; break; }
+      done++;
     }
   };
-  int64_t commits[ST_STAGES] = {0, 0, 0, 0};   // thread 0: commits issued per stage
+  int committed = 0;   // thread 0: steps whose MMAs it has committed
   issue(0);
   issue(1);
   int k = 0, u = 0;   // consumer: tile and step within it of step g
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
         tc::mma_bf16(tbase, ad, bd, idesc, u > 0 || kk > 0);
       }
       tc::mma_commit(&mbar[g % ST_STAGES]);
-      commits[g % ST_STAGES]++;
+      committed = g + 1;
     }
     if (++u != units) continue;
     u = 0;
@@ -410,13 +410,14 @@ __global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
     const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
     // pass 1: rows at the warp edges for the neighbouring warps
     for (int co = 0; co < Co; co += 8) {
-      float dm[8], dp[8];
-      tc::tmem_ld8(trow + (uint32_t)co, dm);
-      tc::tmem_ld8(trow + (uint32_t)(2 * Co + co), dp);
+      uint32_t dm[8], dp[8];
+      tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
+      tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
+      tc::tmem_wait_ld(dm, dp);
       if (lane == 31)
-        for (int q = 0; q < 8; q++) xch[0][warp][co + q] = dm[q];
+        for (int q = 0; q < 8; q++) xch[0][warp][co + q] = __uint_as_float(dm[q]);
       if (lane == 0)
-        for (int q = 0; q < 8; q++) xch[1][warp][co + q] = dp[q];
+        for (int q = 0; q < 8; q++) xch[1][warp][co + q] = __uint_as_float(dp[q]);
     }
     __syncthreads();
     const int r = warp * 32 + lane;
@@ -424,18 +425,19 @@ __global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
     const bool live = r >= 1 && r <= 126 && c < a.ncell;
     const float m = live ? (float)a.mask[c] : 0.f;
     for (int co = 0; co < Co; co += 8) {
-      float dm[8], d0[8], dp[8];
-      tc::tmem_ld8(trow + (uint32_t)co, dm);
-      tc::tmem_ld8(trow + (uint32_t)(Co + co), d0);
-      tc::tmem_ld8(trow + (uint32_t)(2 * Co + co), dp);
+      uint32_t dm[8], d0[8], dp[8];
+      tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
+      tc::tmem_ld8_nowait(trow + (uint32_t)(Co + co), d0);
+      tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
+      tc::tmem_wait_ld(dm, d0, dp);
       float v[8];
 #pragma unroll
       for (int q = 0; q < 8; q++) {
-        float prev = __shfl_up_sync(0xffffffffu, dm[q], 1);
-        float next = __shfl_down_sync(0xffffffffu, dp[q], 1);
+        float prev = __shfl_up_sync(0xffffffffu, __uint_as_float(dm[q]), 1);
+        float next = __shfl_down_sync(0xffffffffu, __uint_as_float(dp[q]), 1);
         if (lane == 0) prev = warp > 0 ? xch[0][warp - 1][co + q] : 0.f;
         if (lane == 31) next = warp < 3 ? xch[1][warp + 1][co + q] : 0.f;
-        v[q] = prev + d0[q] + next;
+        v[q] = prev + __uint_as_float(d0[q]) + next;
       }
       if (!live || co >= a.out_ch) continue;
       uint16_t gt[8];
@@ -469,11 +471,9 @@ __global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
   }
   // every commit thread 0 issued has been observed (bounded waits) before TMEM is freed
   if (threadIdx.x == 0) {
-    for (int st = 0; st < ST_STAGES; st++) {
-      while ((int64_t)seen[st] < commits[st]) {
-        if (!tc::mbar_wait(&mbar[st], seen[st] & 1)) break;
-        seen[st]++;
-      }
+    while (done < committed) {
+      if (!tc::mbar_wait(&mbar[done % ST_STAGES], (uint32_t)((done / ST_STAGES) & 1))) break;
+      done++;
     }
   }
   tc::fence_before_sync();
