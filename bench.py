@@ -110,6 +110,11 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
+def workload_name(size):
+    return (f"{size}^3 unit cube + ghost layer (box {size + 2}^3), {N_SPHERES} spheres r~U[0.02,0.06], "
+            f"zero-mean -div(u) RHS, u~N(0,1), seed {SEED}")
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -187,7 +192,7 @@ def reference_arm(args):
     line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "256^3 unit cube, 64 spheres, zero-mean divergence RHS, CG to 1e-8",
+            "config": {"workload": workload_name(N_CELLS),
                        "solver": "plain FP64 CG, oracle CPU port, all host cores"},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -350,8 +355,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 dots, scalars, residual replacement)", "data": "synthetic",
-        "config": {"workload": f"{args.size}^3 unit cube + ghost layer (box {g.shape[0]}^3), {N_SPHERES} spheres "
-                               f"r~U[0.02,0.06], zero-mean -div(u) RHS, u~N(0,1), seed {SEED}",
+        "config": {"workload": workload_name(args.size),
                    "solver": "mixed-precision CG (FP32 matvec/vectors, FP64 dots, true-residual replacement/50)",
                    "preconditioner": "degree-2 Chebyshev polynomial z = p(A) r over [lmax/30, lmax], both stencil "
                                      "levels temporally blocked in one pass (the learned U-Net preconditioner is "
