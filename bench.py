@@ -304,12 +304,16 @@ def main():
     # iteration is the headline.
     kms = xf.profile_cg_kernels(A, reps=20)
     # compulsory bytes per box cell: pq_fused_f32 reads z (or r), p, kind and
-    # writes p', q (17 B); poly2_f32 reads r, kind and writes z (9 B); the
-    # others as in their kernels' comments
+    # writes p', q (17 B); poly2_f32 reads r, kind and writes z (9 B);
+    # polyr_f32 reads r, q, e, p', kind and writes r', e, z (29 B); the others
+    # as in their kernels' comments
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
-           "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9}
-    if "poly2_f32" in kms and "pq_fused_f32" in kms:   # the timed solver's path: 3 kernels per iteration
-        per_iter = {"poly2_f32": 1.0, "pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
+           "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29}
+    if "polyr_f32" in kms and "pq_fused_f32" in kms:
+        # the timed solver's path, per chunk of 50: K0 once, K1 and the fused
+        # update + K0 49 times, K1 + the update + the FP64 replacement once
+        per_iter = {"polyr_f32": 49 / 50, "pq_fused_f32": 1.0, "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50,
+                    "residual_f64": 1 / 50}
     elif "pq_fused_f32" in kms:
         per_iter = {"pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
     else:

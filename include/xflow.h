@@ -446,7 +446,9 @@ int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, co
  * q = A p', (p', q)) as the solver launches it, or -1 where the grid does not
  * take that path; [6] the same step by the register plane march, else -1;
  * [7] the polynomial preconditioner z = p(A) r with (r, z) (XF_PRECOND_CHEB),
- * or -1.  ms_out holds 8 doubles.  Laplace operators only. */
+ * or -1; [8] the same launch with the residual update fused in (r' = r -
+ * alpha q, e += alpha p', z = p(A) r', (r', r'), (r', z)), or -1.  ms_out
+ * holds 9 doubles.  Laplace operators only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
 /* ---- allocation-free inner product --------------------------------------- */

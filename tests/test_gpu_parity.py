@@ -344,6 +344,38 @@ def test_chebyshev_preconditioned_mixed_cg(ctx, monkeypatch, n):
     monkeypatch.delenv("XF_POLY_BLOCKS", raising=False)
 
 
+@pytest.mark.parametrize("n,replace_every", [(48, 50), (70, 7), (64, 1)])
+def test_fused_residual_update_matches_separate_launches(ctx, monkeypatch, n, replace_every):
+    """The preconditioned solve with the residual update fused into the
+    polynomial pass (two residual buffers) against the same solve with the
+    update and the polynomial as separate launches: the iterates are the same
+    arithmetic, so the iteration counts and solutions agree exactly; also
+    with a capped grid (several work items per block: the q copies and the
+    raw ring carry their barrier phases across items) and with chunks of odd
+    and unit length (the residual ends a chunk in either buffer)."""
+    codes, nrm, sep, b = spheres_case(n, 8, 23)
+    g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
+    A = xf.Operator(g)
+    bv = g.vec(b)
+    for cap in (None, "5"):
+        if cap:
+            monkeypatch.setenv("XF_POLY_BLOCKS", cap)
+        else:
+            monkeypatch.delenv("XF_POLY_BLOCKS", raising=False)
+        out = {}
+        for fused in ("1", "0"):
+            monkeypatch.setenv("XF_POLYR", fused)
+            x = g.vec(np.zeros(g.shape))
+            st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=1e-9,
+                          precond=capi.XF_PRECOND_CHEB, replace_every=replace_every)
+            assert st.status == capi.XF_OK and st.rel_resid <= 1e-9, (fused, st.status, st.rel_resid)
+            out[fused] = (st.iterations, x.download())
+        assert out["1"][0] == out["0"][0]
+        assert np.array_equal(out["1"][1], out["0"][1])
+    monkeypatch.delenv("XF_POLY_BLOCKS", raising=False)
+    monkeypatch.delenv("XF_POLYR", raising=False)
+
+
 def test_chebyshev_preconditioner_needs_uniform_grid(ctx):
     codes, nrm = wl.poisson_cube(12, 12, 12)
     rng = np.random.Generator(np.random.PCG64(2))

@@ -288,7 +288,7 @@ def solve(op, x, b, **kw):
 
 
 CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "stencil_f64", "pq_fused_f32",
-              "pq_march_f32", "poly2_f32")
+              "pq_march_f32", "poly2_f32", "polyr_f32")
 
 
 def profile_cg_kernels(op, reps=20):

@@ -19,10 +19,20 @@
 //   - computes level 2 for plane t-3 on its own cells (z to global memory,
 //     the (r, z) partial),
 //   - loads the row kinds of plane t for the next step's level 1,
+//   - waits for raw plane t+1,
 // and synchronises once.  The stencil is the fast Laplace row of the CG
 // kernels (open-face diagonal, uniform coefficients); rows without an
 // equation give 0, so inactive cells keep z = 0.  Halo cells outside the box
 // hold stale values that only rows without an equation read.
+//
+// The fused form (FUSE) also carries the previous iteration's update: when
+// raw plane t+1 lands, the block applies r -= alpha q to it in shared memory
+// (q of the same region arrives by bulk copy into a one-plane buffer),
+// writes the updated residual of its own cells to the other residual buffer,
+// updates the FP32 correction e += alpha p' there and accumulates (r, r).  Halo
+// cells are updated redundantly with the same FMA as their owners, so every
+// block sees bit-identical values.  One launch then does the work of the
+// residual update kernel and of K0, and the iteration needs two kernels.
 //
 // Every mbarrier wait is bounded; a wait that runs out records I_ERR, lets the
 // copies in flight land (bounded), ends the solve with XF_ERR_CUDA and leaves.
@@ -44,9 +54,13 @@ constexpr int CP_NY = 4;                  // y1 ring: planes t-4 .. t-1
 
 struct CpArgs {
   const uint8_t* kind;
-  const float* r;
+  const float* r;             // residual (FUSE: before this launch's update)
   float* z;
   DevScratch* S;
+  const float* q;             // FUSE: A p' of the iteration
+  const float *pa, *pb;       // FUSE: direction buffers (I_PBUF names the current one)
+  float* e;                   // FUSE: FP32 correction
+  float* rout;                // FUSE: updated residual (own cells)
   int n1, n3, P;
   int HA, R0, R1;             // halo unit (multiple of 4), raw region TILE + 4 HA, level-1 region TILE + 2 HA
   int tiles, chunk, nchunk;   // work items: nchunk plane chunks x tiles
@@ -85,6 +99,7 @@ __device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, flo
   }
 }
 
+template <bool FUSE>
 __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constant__ CpArgs a) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ double sh[32];
@@ -93,19 +108,28 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
   DevScratch* S = a.S;
   if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
   const int n1 = a.n1, n3 = a.n3, P = a.P, HA = a.HA, R0 = a.R0, R1 = a.R1;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);          // CP_NS raw-plane barriers, then the q barrier
+  uint64_t* qbar = mbar + CP_NS;
   float* ring = reinterpret_cast<float*>(smem + 128);          // CP_NS x R0 raw r
   float* yring = ring + (size_t)CP_NS * R0;                     // CP_NY x R1 level-1 planes
-  uint8_t* kbuf = reinterpret_cast<uint8_t*>(yring + (size_t)CP_NY * R1);   // 2 x R1 row kinds
+  float* qbuf = yring + (size_t)CP_NY * R1;                     // FUSE: R0 cells of q
+  uint8_t* kbuf = reinterpret_cast<uint8_t*>(qbuf + (FUSE ? (size_t)R0 : 0));   // 2 x R1 row kinds
   const int64_t total = (int64_t)n1 * P;
   const int items = a.nchunk * a.tiles;
+  float alpha = 0.f;
+  const float* pdir = a.pa;
+  if (FUSE) {
+    alpha = (float)S->scalars[D_ALPHA];
+    if (S->iscalars[I_PBUF]) pdir = a.pb;
+  }
+  const float* r2src = FUSE ? a.rout : a.r;   // own-cell residual of level 2
   if (threadIdx.x < 64) {
     const int b = threadIdx.x;
     dtab[b] = a.cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + a.cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
               a.cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < CP_NS; s++) mbar_init(&mbar[s], 1);
+    for (int s = 0; s < CP_NS + (FUSE ? 1 : 0); s++) mbar_init(&mbar[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -117,6 +141,13 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     i1 = min(n1, i0 + a.chunk);
     lo = max(i0 - 2, 0);
     hi = min(i1 + 1, n1 - 1);
+  };
+  // the box cells [c_lo, c_hi) of the raw region of a plane, and its start
+  auto region = [&](int plane, int base, int64_t& reg_lo, int64_t& c_lo, int64_t& c_hi) {
+    reg_lo = (int64_t)plane * P + base - 2 * HA;
+    const int64_t reg_hi = reg_lo + R0;
+    c_lo = reg_lo < 0 ? 0 : reg_lo;
+    c_hi = reg_hi > total ? total : reg_hi;
   };
   // producer (thread 0): the stream of raw planes over this block's items
   int p_item = blockIdx.x, p_plane = 0, p_base = 0, p_hi = -1;
@@ -131,8 +162,8 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
   auto issue_one = [&]() -> bool {
     if (p_item >= items) return false;
     const int s = (int)(issued % CP_NS);
-    const int64_t reg_lo = (int64_t)p_plane * P + p_base - 2 * HA, reg_hi = reg_lo + R0;
-    const int64_t c_lo = reg_lo < 0 ? 0 : reg_lo, c_hi = reg_hi > total ? total : reg_hi;
+    int64_t reg_lo, c_lo, c_hi;
+    region(p_plane, p_base, reg_lo, c_lo, c_hi);
     const uint32_t bytes = (uint32_t)(c_hi - c_lo) * 4u;
     mbar_expect_tx(&mbar[s], bytes);
     bulk_g2s(ring + (size_t)s * R0 + (c_lo - reg_lo), a.r + c_lo, bytes, &mbar[s]);
@@ -157,8 +188,20 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       }
     }
   };
+  // FUSE: q of one raw plane into the one-plane buffer (thread 0; the previous
+  // reader of the buffer has passed a block barrier)
+  long long q_issued = 0, q_waited = 0;
+  auto issue_q = [&](int plane, int base) {
+    int64_t reg_lo, c_lo, c_hi;
+    region(plane, base, reg_lo, c_lo, c_hi);
+    const uint32_t bytes = (uint32_t)(c_hi - c_lo) * 4u;
+    fence_proxy_async();
+    mbar_expect_tx(qbar, bytes);
+    bulk_g2s(qbuf + (c_lo - reg_lo), a.q + c_lo, bytes, qbar);
+    q_issued++;
+  };
 
-  DotAcc<float> acc;
+  DotAcc<float> acc, acc_rr;
   bool ok = true;
   long long waited = 0;
   long long item_first = 0;
@@ -175,14 +218,22 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     const int xa = base + 4 * threadIdx.x, xb = xa + CP_TILE / 2;
     const bool va = xa < P, vb = xb < P;
     const int ya = HA + 4 * threadIdx.x, yb = ya + CP_TILE / 2;   // their index in the level-1 region
-    // level-2 inputs of the next plane, prefetched one step ahead
+    // level-2 inputs of the next plane, prefetched one step ahead (FUSE: the
+    // updated residual this thread wrote three steps earlier, read through L2)
     float4 rpa = make_float4(0.f, 0.f, 0.f, 0.f), rpb = rpa;
     uchar4 kpa = make_uchar4(0, 0, 0, 0), kpb = kpa;
     auto prefetch2 = [&](int pl) {
       if (pl < i0 || pl >= i1) return;
       const int64_t o = (int64_t)pl * P;
-      if (va) { rpa = __ldg(reinterpret_cast<const float4*>(a.r + o + xa)); kpa = *reinterpret_cast<const uchar4*>(a.kind + o + xa); }
-      if (vb) { rpb = __ldg(reinterpret_cast<const float4*>(a.r + o + xb)); kpb = *reinterpret_cast<const uchar4*>(a.kind + o + xb); }
+      if (FUSE) {
+        if (va) rpa = __ldcg(reinterpret_cast<const float4*>(r2src + o + xa));
+        if (vb) rpb = __ldcg(reinterpret_cast<const float4*>(r2src + o + xb));
+      } else {
+        if (va) rpa = __ldg(reinterpret_cast<const float4*>(r2src + o + xa));
+        if (vb) rpb = __ldg(reinterpret_cast<const float4*>(r2src + o + xb));
+      }
+      if (va) kpa = *reinterpret_cast<const uchar4*>(a.kind + o + xa);
+      if (vb) kpb = *reinterpret_cast<const uchar4*>(a.kind + o + xb);
     };
     // row kinds of a level-1 plane over the level-1 region (0 outside the box)
     auto load_kinds = [&](int pl) {
@@ -195,77 +246,164 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         reinterpret_cast<uint32_t*>(kb)[w] = v;
       }
     };
-    long long rel_next = lo;   // next plane whose raw slot is released
-    bool wok = true;
-    for (int t = i0 - 2; t <= i1 + 2; t++) {
-      // (A) raw plane t has landed
-      if (t >= lo && t <= hi) {
-        const long long L = item_first + (t - lo);
-        wok = mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1)) && wok;
-        if (wok) waited = L + 1;
+    // raw plane pl has landed (and, FUSE, its q)
+    auto wait_plane = [&](int pl) -> bool {
+      const long long L = item_first + (pl - lo);
+      bool w = mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1));
+      if (w) waited = L + 1;
+      if (FUSE && w) {
+        w = mbar_wait_bounded(qbar, (uint32_t)(q_waited & 1));
+        if (w) q_waited++;
       }
-      if (wok) {
-        // (B) level 1 for plane t-1: y1 = a1 r + a2 (A r) over the level-1 region
-        const int p1 = t - 1;
-        if (p1 >= l1lo && p1 <= l1hi) {
-          const float* Rc = rslot(p1);
-          const float* Rm = rslot(p1 - 1);
-          const float* Rp = rslot(p1 + 1);
-          const uint8_t* kb = kbuf + (size_t)(p1 & 1) * R1;
-          float* Y = yslot(p1);
-          // warp-uniform trip count (the shuffles need every lane); groups past
-          // the region end compute on in-bounds cells and are not stored
-          for (int g0 = 0; g0 < R1 / 4; g0 += CP_THREADS) {
-            const int g = g0 + (int)threadIdx.x;
-            const int gg = g < R1 / 4 ? g : R1 / 4 - 1;
-            const int s = HA + 4 * gg;   // raw index of the group's first cell
-            const float4 c = ld4(Rc + s);
-            float ar[4];
-            lap4(dtab, *reinterpret_cast<const uchar4*>(kb + 4 * gg), c, ld4(Rm + s), ld4(Rp + s), Rc + s, n3, a.cx,
-                 a.cy, a.cz, ar, g + 1 >= R1 / 4);
-            if (g < R1 / 4)
-              *reinterpret_cast<float4*>(Y + 4 * g) =
-                  make_float4(fmaf(a.a2, ar[0], a.a1 * c.x), fmaf(a.a2, ar[1], a.a1 * c.y),
-                              fmaf(a.a2, ar[2], a.a1 * c.z), fmaf(a.a2, ar[3], a.a1 * c.w));
+      return w;
+    };
+    // FUSE: e and p' of the own cells of the plane the step's update reaches,
+    // loaded at the top of the step so that their latency hides under the
+    // stencil levels
+    float4 ep[2], pp[2];
+    auto prefetch_e = [&](int pl) {
+      if (pl < i0 || pl >= i1) return;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = 4 * (int)threadIdx.x + h * (CP_TILE / 2);
+        if (base + c < P) {
+          const int64_t x = (int64_t)pl * P + base + c;
+          ep[h] = *reinterpret_cast<const float4*>(a.e + x);
+          pp[h] = __ldg(reinterpret_cast<const float4*>(pdir + x));
+        }
+      }
+    };
+    // FUSE: r -= alpha q over the box cells of raw plane pl; own cells of own
+    // planes also go to rout with e += alpha p' and (r, r)
+    auto update = [&](int pl) {
+      float* R = rslot(pl);
+      const int64_t reg_lo = (int64_t)pl * P + base - 2 * HA;
+      const bool own_plane = pl >= i0 && pl < i1;
+      float psum = 0.f, esum = 0.f;   // (r, r) of the own cells: products and their rounding errors
+      auto upd = [&](int s) -> float4 {
+        float4 rv = ld4(R + s);
+        const float4 qv = ld4(qbuf + s);
+        rv.x = fmaf(-alpha, qv.x, rv.x);
+        rv.y = fmaf(-alpha, qv.y, rv.y);
+        rv.z = fmaf(-alpha, qv.z, rv.z);
+        rv.w = fmaf(-alpha, qv.w, rv.w);
+        *reinterpret_cast<float4*>(R + s) = rv;
+        return rv;
+      };
+#pragma unroll
+      for (int h = 0; h < 2; h++) {   // the own-cell groups of level 2's mapping
+        const int c = 4 * (int)threadIdx.x + h * (CP_TILE / 2);
+        const int s = 2 * HA + c;
+        const int64_t x = reg_lo + s;
+        if (x >= total) continue;
+        const float4 rv = upd(s);
+        if (own_plane && base + c < P) {
+          *reinterpret_cast<float4*>(a.rout + x) = rv;
+          float4 ev = ep[h];
+          const float4 pv = pp[h];
+          ev.x = fmaf(alpha, pv.x, ev.x);
+          ev.y = fmaf(alpha, pv.y, ev.y);
+          ev.z = fmaf(alpha, pv.z, ev.z);
+          ev.w = fmaf(alpha, pv.w, ev.w);
+          *reinterpret_cast<float4*>(a.e + x) = ev;
+          const float rr[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const float pr = rr[k] * rr[k];
+            esum += fmaf(rr[k], rr[k], -pr);
+            psum += pr;
           }
         }
-        // (C) level 2 for plane t-3: z = a0 r + A y1 on the own cells, (r, z)
-        const int p2 = t - 3;
-        if (p2 >= i0 && p2 < i1) {
-          const float* Yc = yslot(p2);
-          const float* Ym = yslot(p2 - 1);
-          const float* Yp = yslot(p2 + 1);
-          const int64_t o = (int64_t)p2 * P;
-          // (r, z) of this thread's cells: FP32 sum of the products plus the sum of
-          // their exact rounding errors, into the float-float accumulator per plane
-          float psum = 0.f, esum = 0.f;
-          auto group = [&](bool v, int s, float4 rr, uchar4 k4, int x) {
-            float ay[4];
-            lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
-            if (!v) return;
-            const float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
-                                 fmaf(a.a0, rr.w, ay[3])};
-            *reinterpret_cast<float4*>(a.z + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
-            const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-              const float pr = rv[q] * zz[q];
-              esum += fmaf(rv[q], zz[q], -pr);
-              psum += pr;
-            }
-          };
-          group(va, ya, rpa, kpa, xa);
-          group(vb, yb, rpb, kpb, xb);
-          acc.add(psum, 1.f);
-          acc.add(esum, 1.f);
-        }
-        // (D) inputs of the next step
-        if (t >= l1lo && t <= l1hi) load_kinds(t);
-        prefetch2(t - 2);
       }
-      // (E) one barrier per step; a timed-out wait anywhere stops the block
+      if (own_plane) {
+        acc_rr.add(psum, 1.f);
+        acc_rr.add(esum, 1.f);
+      }
+      for (int hg = threadIdx.x; hg < HA; hg += CP_THREADS) {   // halo groups, either side
+        const int g = hg < HA / 2 ? hg : hg + CP_TILE / 4;
+        const int64_t x = reg_lo + 4 * g;
+        if (x >= 0 && x < total) upd(4 * g);
+      }
+    };
+    long long rel_next = lo;   // next plane whose raw slot is released
+    // the item's first raw plane
+    if (FUSE && threadIdx.x == 0) issue_q(lo, base);
+    if (FUSE) prefetch_e(lo);
+    bool wok = wait_plane(lo);
+    if (FUSE && wok) update(lo);
+    if (__syncthreads_or(!wok)) { ok = false; break; }
+    for (int t = i0 - 2; t <= i1 + 2; t++) {
+      const int pn = t + 1;   // the raw plane that lands during this step
+      const bool has_next = pn > lo && pn <= hi;
+      if (FUSE && has_next) {
+        if (threadIdx.x == 0) issue_q(pn, base);
+        prefetch_e(pn);
+      }
+      // (B) level 1 for plane t-1: y1 = a1 r + a2 (A r) over the level-1 region
+      const int p1 = t - 1;
+      if (p1 >= l1lo && p1 <= l1hi) {
+        const float* Rc = rslot(p1);
+        const float* Rm = rslot(p1 - 1);
+        const float* Rp = rslot(p1 + 1);
+        const uint8_t* kb = kbuf + (size_t)(p1 & 1) * R1;
+        float* Y = yslot(p1);
+        // warp-uniform trip count (the shuffles need every lane); groups past
+        // the region end compute on in-bounds cells and are not stored
+        for (int g0 = 0; g0 < R1 / 4; g0 += CP_THREADS) {
+          const int g = g0 + (int)threadIdx.x;
+          const int gg = g < R1 / 4 ? g : R1 / 4 - 1;
+          const int s = HA + 4 * gg;   // raw index of the group's first cell
+          const float4 c = ld4(Rc + s);
+          float ar[4];
+          lap4(dtab, *reinterpret_cast<const uchar4*>(kb + 4 * gg), c, ld4(Rm + s), ld4(Rp + s), Rc + s, n3, a.cx,
+               a.cy, a.cz, ar, g + 1 >= R1 / 4);
+          if (g < R1 / 4)
+            *reinterpret_cast<float4*>(Y + 4 * g) =
+                make_float4(fmaf(a.a2, ar[0], a.a1 * c.x), fmaf(a.a2, ar[1], a.a1 * c.y),
+                            fmaf(a.a2, ar[2], a.a1 * c.z), fmaf(a.a2, ar[3], a.a1 * c.w));
+        }
+      }
+      // (C) level 2 for plane t-3: z = a0 r + A y1 on the own cells, (r, z)
+      const int p2 = t - 3;
+      if (p2 >= i0 && p2 < i1) {
+        const float* Yc = yslot(p2);
+        const float* Ym = yslot(p2 - 1);
+        const float* Yp = yslot(p2 + 1);
+        const int64_t o = (int64_t)p2 * P;
+        // (r, z) of this thread's cells: FP32 sum of the products plus the sum of
+        // their exact rounding errors, into the float-float accumulator per plane
+        float psum = 0.f, esum = 0.f;
+        auto group = [&](bool v, int s, float4 rr, uchar4 k4, int x) {
+          float ay[4];
+          lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
+          if (!v) return;
+          const float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
+                               fmaf(a.a0, rr.w, ay[3])};
+          *reinterpret_cast<float4*>(a.z + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
+          const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const float pr = rv[q] * zz[q];
+            esum += fmaf(rv[q], zz[q], -pr);
+            psum += pr;
+          }
+        };
+        group(va, ya, rpa, kpa, xa);
+        group(vb, yb, rpb, kpb, xb);
+        acc.add(psum, 1.f);
+        acc.add(esum, 1.f);
+      }
+      // (D) inputs of the next step
+      if (t >= l1lo && t <= l1hi) load_kinds(t);
+      prefetch2(t - 2);
+      // (E) raw plane t+1 for the next step's level 1
+      if (has_next) {
+        wok = wait_plane(pn);
+        if (FUSE && wok) update(pn);
+      }
+      // (F) one barrier per step; a timed-out wait anywhere stops the block
       if (__syncthreads_or(!wok)) { ok = false; break; }
-      // (F) raw plane t-2 has had its last reader
+      // (G) raw plane t-2 has had its last reader
       while (rel_next <= t - 2 && rel_next <= hi) { release(); rel_next++; }
     }
     if (!ok) break;
@@ -277,23 +415,47 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     if (threadIdx.x == 0) {
       atomicExch((unsigned long long*)&S->iscalars[I_ERR], 1ull);
       for (long long L = waited; L < issued; L++) mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1));
+      if (FUSE && q_issued > q_waited) mbar_wait_bounded(qbar, (uint32_t)(q_waited & 1));
       S->iscalars[I_DONE] = 1;
       S->iscalars[I_STATUS] = XF_ERR_CUDA;
     }
     __syncthreads();
     return;
   }
-  if (!publish_acc<float>(S, SL_D, SL_D, acc, sh, &last)) return;
-  double tot = finish_partials(S, SL_D, sh);
+  if (!FUSE) {
+    if (!publish_acc<float>(S, SL_D, SL_D, acc, sh, &last)) return;
+    double tot = finish_partials(S, SL_D, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_D] = tot;
+      S->tickets[SL_D] = 0;
+      control_step(S, CTL_PCG_BETA);
+    }
+    return;
+  }
+  // FUSE: (r, r) of the updated residual and (r, z), one ticket
+  const double brr = block_sum_acc<float>(acc_rr, sh);
+  const double brz = block_sum_acc<float>(acc, sh);
   if (threadIdx.x == 0) {
-    S->scalars[SL_D] = tot;
+    S->partials[SL_B][lin_block()] = brr;
+    S->partials[SL_D][lin_block()] = brz;
+    __threadfence();
+    const unsigned int tk = atomicAdd(&S->tickets[SL_D], 1u);
+    last = (tk == (unsigned)num_blocks() - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double rr = finish_partials(S, SL_B, sh);
+  const double rz = finish_partials(S, SL_D, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[SL_B] = rr;
+    S->scalars[SL_D] = rz;
     S->tickets[SL_D] = 0;
-    control_step(S, CTL_PCG_BETA);
+    control_step(S, CTL_PCG_RR_BETA);
   }
 }
 
-size_t cp_smem(int R0, int R1) {
-  return 128 + (size_t)CP_NS * R0 * 4 + (size_t)CP_NY * R1 * 4 + 2 * (size_t)R1;
+size_t cp_smem(int R0, int R1, bool fuse) {
+  return 128 + (size_t)CP_NS * R0 * 4 + (size_t)CP_NY * R1 * 4 + (fuse ? (size_t)R0 * 4 : 0) + 2 * (size_t)R1;
 }
 
 int cp_halo(int n3) { return (n3 + 1 + 3) & ~3; }
@@ -329,14 +491,16 @@ bool xf_cg_poly_supported(const xf_grid* g) {
   const int64_t P = (int64_t)g->n2 * g->n3;
   if (!g->uniform || g->nbrow != 0 || P % 4 != 0 || g->n3 % 2 != 0 || g->n3 < 2 || g->n2 < 2) return false;
   const int HA = cp_halo(g->n3);
-  return cp_smem(CP_TILE + 4 * HA, CP_TILE + 2 * HA) <= 226 * 1024;
+  return cp_smem(CP_TILE + 4 * HA, CP_TILE + 2 * HA, true) <= 226 * 1024;
 }
 
-void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]) {
+namespace {
+
+template <bool FUSE>
+void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
-  CpArgs a;
-  a.kind = g->kind; a.r = r; a.z = z; a.S = ctx->scratch;
+  a.kind = g->kind; a.S = ctx->scratch;
   a.n1 = g->n1; a.n3 = g->n3; a.P = g->n2 * g->n3;
   a.HA = cp_halo(g->n3);
   a.R0 = CP_TILE + 4 * a.HA;
@@ -344,10 +508,10 @@ void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float co
   a.tiles = (a.P + CP_TILE - 1) / CP_TILE;
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
   a.a0 = coeffs[0]; a.a1 = coeffs[1]; a.a2 = coeffs[2];
-  const size_t smem = cp_smem(a.R0, a.R1);
+  const size_t smem = cp_smem(a.R0, a.R1, FUSE);
   static size_t attr = 0;
   if (attr < smem) {
-    cudaFuncSetAttribute(k_cg_poly2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_cg_poly2<FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = smem;
   }
   int resident = (int)((228 * 1024) / (smem + 2048));
@@ -370,5 +534,23 @@ void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float co
     const long cap = strtol(env, nullptr, 10);
     if (cap >= 1 && cap < blocks) blocks = cap;
   }
-  k_cg_poly2<<<(int)blocks, CP_THREADS, smem, ctx->stream>>>(a);
+  k_cg_poly2<FUSE><<<(int)blocks, CP_THREADS, smem, ctx->stream>>>(a);
+}
+
+}  // namespace
+
+void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]) {
+  CpArgs a = {};
+  a.r = r; a.z = z;
+  poly_launch<false>(op, a, coeffs);
+}
+
+// The fused launch: r_out = r - alpha q on the own cells, e += alpha p' (p' the
+// current direction buffer of pa / pb), z = p(A) r_out, (r_out, r_out) and
+// (r_out, z) -> the stop test and beta.  r and r_out are different buffers.
+void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const float* q, const float* pa,
+                        const float* pb, float* e, float* z, const float coeffs[3]) {
+  CpArgs a = {};
+  a.r = r; a.z = z; a.q = q; a.pa = pa; a.pb = pb; a.e = e; a.rout = r_out;
+  poly_launch<true>(op, a, coeffs);
 }

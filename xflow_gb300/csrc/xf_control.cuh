@@ -32,7 +32,7 @@ enum {
   CTL_BCGS_NORM0, CTL_BCGS_PN1, CTL_BCGS_AN, CTL_BCGS_WN, CTL_BCGS_END,
   CTL_MR_INIT, CTL_MR_ALFA, CTL_MR_RES,
   CTL_BICG_INIT, CTL_BICG_ALPHA, CTL_BICG_BETA,
-  CTL_PCG_BETA, CTL_PCG_ALPHA_FLIP, CTL_PCG_RR, CTL_PCG_REPL
+  CTL_PCG_BETA, CTL_PCG_ALPHA_FLIP, CTL_PCG_RR, CTL_PCG_REPL, CTL_PCG_RR_BETA
 };
 
 template <typename T>
@@ -119,6 +119,16 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       break;
     }
     // ---- polynomially preconditioned mixed CG: rho = (r, z) ------------------
+    case CTL_PCG_RR_BETA: {  // fused update + preconditioner: SL_B (r, r) after the update, SL_D (r, z)
+      double rn = d[SL_B];
+      I[I_IT] += 1;
+      if (isnan(rn)) { finish(S, XF_NAN); break; }
+      d[D_RR] = rn;
+      // a paused recursion keeps the previous (r, z): the replacement's own
+      // (r, z) continues the direction from it
+      if (rn <= d[D_THR] || I[I_IT] >= I[I_MAXIT]) { I[I_PAUSE] = 1; break; }
+    }
+      // fall through
     case CTL_PCG_BETA: {  // SL_D: (r, z) of the new residual
       double rz = d[SL_D];
       if (isnan(rz)) { finish(S, XF_NAN); break; }

@@ -31,6 +31,8 @@ bool xf_cg_pqb_supported(const xf_grid* g);
 void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int ctl);
 bool xf_cg_poly_supported(const xf_grid* g);
 void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]);
+void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const float* q, const float* pa,
+                        const float* pb, float* e, float* z, const float coeffs[3]);
 void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 bool xf_cg_pqt_supported(const xf_grid* g);
@@ -503,6 +505,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   double rel = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr;
   float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr, *z32 = nullptr;
+  float* r32b = nullptr;
   const bool cheb = o.precond == XF_PRECOND_CHEB;
   if (cheb && (!mixed || op->kind != XF_OP_LAPLACE || !xf_cg_poly_supported(g) || !xf_cg_pqb_supported(g)))
     return xf_fail(ctx, XF_ERR_UNSUPPORTED,
@@ -518,7 +521,8 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       p32b = B.get<float>(n);
       if (!p32b) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
     }
-    if (cheb && !(z32 = B.get<float>(n))) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
+    if (cheb && (!(z32 = B.get<float>(n)) || !(r32b = B.get<float>(n))))
+      return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
   }
   double* tmp = B.get<double>(n, false);
   if (!tmp) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate residual");
@@ -546,16 +550,21 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         k_cg_p<double><<<eb, 256, 0, ctx->stream>>>(p, r, n, S, 0);
       };
     } else if (cheb) {
-      // Polynomially preconditioned mixed CG, three kernels per iteration:
+      // Polynomially preconditioned mixed CG.  The kernels of an iteration:
       // K0 z = p(A) r with (r, z) and beta (both stencil levels in one pass),
       // K1 p' = z + beta p inside the stencil with q = A p', (p', q), alpha,
-      // K2 e += alpha p', r -= alpha q with (r, r) for the stop test.  One
-      // graph chunk = `replace_every` iterations ending with the FP64 fold
-      // and the true-residual replacement; the next K0 continues the
-      // direction from the replaced residual.
+      // K2 e += alpha p', r -= alpha q with (r, r) for the stop test.  K2 and
+      // the next K0 run as one fused launch (the update applied to each
+      // plane as it streams in, the residual alternating between two
+      // buffers), so a graph chunk of `replace_every` iterations is K0, then
+      // K1 + fused K2/K0 per iteration, and a last K1 + K2 with the FP64 fold
+      // and the true-residual replacement into the first buffer; the next
+      // chunk's K0 continues the direction from the replaced residual.
+      // XF_POLYR=0 runs K2 and K0 as separate launches.
       chunk = o.replace_every;
       float *e = e32, *r = r32, *pa = p32, *q = q32, *z = z32;
-      float* pb = p32b;
+      float *pb = p32b, *rb = r32b;
+      const bool fused = !(getenv("XF_POLYR") && getenv("XF_POLYR")[0] == '0');
       const double lmax = 4.0 * (g->ucx + g->ucy + g->ucz);   // Gershgorin bound of the uniform Laplace rows
       const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : 30.0;
       float coeffs[3];
@@ -567,9 +576,15 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       xf_cg_res64(op, x, b, r, SL_A, CTL_CG_INIT);
       const int last = chunk - 1;
       iter = [=](int c) {
-        xf_cg_poly_launch(op, r, z, coeffs);
+        // the residual before this iteration's update (fused: buffer c & 1)
+        float* rc = fused && (c & 1) ? rb : r;
+        if (!fused || c == 0) xf_cg_poly_launch(op, rc, z, coeffs);
         xf_cg_pqb_launch(op, z, pa, pb, q, CTL_PCG_ALPHA_FLIP);
-        k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, r, pa, q, n, S, pb, CTL_PCG_RR);
+        if (fused && c < last) {
+          xf_cg_polyr_launch(op, rc, (c & 1) ? r : rb, q, pa, pb, e, z, coeffs);
+        } else {
+          k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, rc, pa, q, n, S, pb, CTL_PCG_RR);
+        }
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
           xf_cg_res64(op, x, b, r, SL_C, CTL_PCG_REPL);
@@ -857,11 +872,14 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
     if (xf_cg_pqt_supported(g)) ms_out[6] = time([&] { xf_cg_pq32_variant(op, r, p, p2, q, 1); });
   }
-  ms_out[7] = -1.0;
+  ms_out[7] = ms_out[8] = -1.0;
   if (xf_cg_poly_supported(g)) {
     float coeffs[3];
     xf_cheb2_coeffs(4.0 * (g->ucx + g->ucy + g->ucz), 30.0, coeffs);
     ms_out[7] = time([&] { xf_cg_poly_launch(op, r, e, coeffs); });
+    float *r2 = B.get<float>(n), *z2 = B.get<float>(n);
+    if (!r2 || !z2) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
+    ms_out[8] = time([&] { xf_cg_polyr_launch(op, r, r2, q, p, p, e, z2, coeffs); });
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
