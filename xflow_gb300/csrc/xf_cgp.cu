@@ -18,8 +18,8 @@
 //     four-plane ring),
 //   - computes level 2 for plane t-3 on its own cells (z to global memory,
 //     the (r, z) partial),
-//   - loads the row kinds of plane t for the next step's level 1,
-//   - waits for raw plane t+1,
+//   - waits for raw plane t+1 (its row kinds over the level-1 region come
+//     with it, by a second bulk copy on the same barrier),
 // and synchronises once.  The stencil is the fast Laplace row of the CG
 // kernels (open-face diagonal, uniform coefficients); rows without an
 // equation give 0, so inactive cells keep z = 0.  Halo cells outside the box
@@ -63,6 +63,7 @@ struct CpArgs {
   float* rout;                // FUSE: updated residual (own cells)
   int n1, n3, P;
   int HA, R0, R1;             // halo unit (multiple of 4), raw region TILE + 4 HA, level-1 region TILE + 2 HA
+  int KS;                     // bytes of a row-kind slot: R1 + 32 rounded up to 16
   int tiles, chunk, nchunk;   // work items: nchunk plane chunks x tiles
   float cx, cy, cz;           // uniform Laplace coefficients
   float a0, a1, a2;           // Horner coefficients of p
@@ -113,8 +114,10 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
   float* ring = reinterpret_cast<float*>(smem + 128);          // CP_NS x R0 raw r
   float* yring = ring + (size_t)CP_NS * R0;                     // CP_NY x R1 level-1 planes
   float* qbuf = yring + (size_t)CP_NY * R1;                     // FUSE: R0 cells of q
-  uint8_t* kbuf = reinterpret_cast<uint8_t*>(qbuf + (FUSE ? (size_t)R0 : 0));   // 2 x R1 row kinds
+  uint8_t* kring = reinterpret_cast<uint8_t*>(qbuf + (FUSE ? (size_t)R0 : 0));   // CP_NS x KS row kinds
+  const int KS = a.KS;
   const int64_t total = (int64_t)n1 * P;
+  const int64_t total16 = (total + 15) & ~(int64_t)15;   // the kind array holds zero bytes up to here
   const int items = a.nchunk * a.tiles;
   float alpha = 0.f;
   const float* pdir = a.pa;
@@ -165,8 +168,14 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     int64_t reg_lo, c_lo, c_hi;
     region(p_plane, p_base, reg_lo, c_lo, c_hi);
     const uint32_t bytes = (uint32_t)(c_hi - c_lo) * 4u;
-    mbar_expect_tx(&mbar[s], bytes);
+    // row kinds of the level-1 region, widened to 16-byte boundaries
+    const int64_t x0 = (int64_t)p_plane * P + p_base - HA;
+    const int64_t k_lo = x0 & ~(int64_t)15, k_hi = (x0 + R1 + 15) & ~(int64_t)15;
+    const int64_t kc_lo = k_lo < 0 ? 0 : k_lo, kc_hi = k_hi > total16 ? total16 : k_hi;
+    const uint32_t kbytes = (uint32_t)(kc_hi - kc_lo);
+    mbar_expect_tx(&mbar[s], bytes + kbytes);
     bulk_g2s(ring + (size_t)s * R0 + (c_lo - reg_lo), a.r + c_lo, bytes, &mbar[s]);
+    bulk_g2s(kring + (size_t)s * KS + (kc_lo - k_lo), a.kind + kc_lo, kbytes, &mbar[s]);
     issued++;
     if (++p_plane > p_hi) {
       p_item += gridDim.x;
@@ -235,16 +244,11 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       if (va) kpa = *reinterpret_cast<const uchar4*>(a.kind + o + xa);
       if (vb) kpb = *reinterpret_cast<const uchar4*>(a.kind + o + xb);
     };
-    // row kinds of a level-1 plane over the level-1 region (0 outside the box)
-    auto load_kinds = [&](int pl) {
-      uint8_t* kb = kbuf + (size_t)(pl & 1) * R1;
-      const int64_t x0 = (int64_t)pl * P + base - HA;   // multiple of 4
-      for (int w = threadIdx.x; w < R1 / 4; w += CP_THREADS) {
-        const int64_t x = x0 + 4 * w;
-        uint32_t v = 0;
-        if (x >= 0 && x + 4 <= total) v = __ldg(reinterpret_cast<const uint32_t*>(a.kind + x));
-        reinterpret_cast<uint32_t*>(kb)[w] = v;
-      }
+    // row kinds of a loaded plane over its level-1 region (stale outside the
+    // box, where only rows without an equation read the level-1 values)
+    auto kslot = [&](int pl) {
+      const int64_t x0 = (int64_t)pl * P + base - HA;
+      return kring + (size_t)((item_first + (pl - lo)) % CP_NS) * KS + (int)(x0 & 15);
     };
     // raw plane pl has landed (and, FUSE, its q)
     auto wait_plane = [&](int pl) -> bool {
@@ -260,16 +264,17 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     // FUSE: e and p' of the own cells of the plane the step's update reaches,
     // loaded at the top of the step so that their latency hides under the
     // stencil levels
+    const int own_n = min(CP_TILE, P - base);   // own cells of the tile in a plane
     float4 ep[2], pp[2];
     auto prefetch_e = [&](int pl) {
       if (pl < i0 || pl >= i1) return;
+      const int64_t o = (int64_t)pl * P + base;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const int c = 4 * (int)threadIdx.x + h * (CP_TILE / 2);
-        if (base + c < P) {
-          const int64_t x = (int64_t)pl * P + base + c;
-          ep[h] = *reinterpret_cast<const float4*>(a.e + x);
-          pp[h] = __ldg(reinterpret_cast<const float4*>(pdir + x));
+        if (c < own_n) {
+          ep[h] = *reinterpret_cast<const float4*>(a.e + o + c);
+          pp[h] = __ldg(reinterpret_cast<const float4*>(pdir + o + c));
         }
       }
     };
@@ -278,7 +283,11 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     auto update = [&](int pl) {
       float* R = rslot(pl);
       const int64_t reg_lo = (int64_t)pl * P + base - 2 * HA;
+      const int s_lo = reg_lo < 0 ? (int)(-reg_lo) : 0;                          // box cells: raw [s_lo, s_hi)
+      const int s_hi = total - reg_lo < R0 ? (int)(total - reg_lo) : R0;
       const bool own_plane = pl >= i0 && pl < i1;
+      float* rown = a.rout + (int64_t)pl * P + base;
+      float* eown = a.e + (int64_t)pl * P + base;
       float psum = 0.f, esum = 0.f;   // (r, r) of the own cells: products and their rounding errors
       auto upd = [&](int s) -> float4 {
         float4 rv = ld4(R + s);
@@ -294,18 +303,17 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       for (int h = 0; h < 2; h++) {   // the own-cell groups of level 2's mapping
         const int c = 4 * (int)threadIdx.x + h * (CP_TILE / 2);
         const int s = 2 * HA + c;
-        const int64_t x = reg_lo + s;
-        if (x >= total) continue;
+        if (s >= s_hi) continue;
         const float4 rv = upd(s);
-        if (own_plane && base + c < P) {
-          *reinterpret_cast<float4*>(a.rout + x) = rv;
+        if (own_plane && c < own_n) {
+          *reinterpret_cast<float4*>(rown + c) = rv;
           float4 ev = ep[h];
           const float4 pv = pp[h];
           ev.x = fmaf(alpha, pv.x, ev.x);
           ev.y = fmaf(alpha, pv.y, ev.y);
           ev.z = fmaf(alpha, pv.z, ev.z);
           ev.w = fmaf(alpha, pv.w, ev.w);
-          *reinterpret_cast<float4*>(a.e + x) = ev;
+          *reinterpret_cast<float4*>(eown + c) = ev;
           const float rr[4] = {rv.x, rv.y, rv.z, rv.w};
 #pragma unroll
           for (int k = 0; k < 4; k++) {
@@ -320,9 +328,8 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         acc_rr.add(esum, 1.f);
       }
       for (int hg = threadIdx.x; hg < HA; hg += CP_THREADS) {   // halo groups, either side
-        const int g = hg < HA / 2 ? hg : hg + CP_TILE / 4;
-        const int64_t x = reg_lo + 4 * g;
-        if (x >= 0 && x < total) upd(4 * g);
+        const int s = 4 * (hg < HA / 2 ? hg : hg + CP_TILE / 4);
+        if (s >= s_lo && s < s_hi) upd(s);
       }
     };
     long long rel_next = lo;   // next plane whose raw slot is released
@@ -345,7 +352,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         const float* Rc = rslot(p1);
         const float* Rm = rslot(p1 - 1);
         const float* Rp = rslot(p1 + 1);
-        const uint8_t* kb = kbuf + (size_t)(p1 & 1) * R1;
+        const uint8_t* kb = kslot(p1);
         float* Y = yslot(p1);
         // warp-uniform trip count (the shuffles need every lane); groups past
         // the region end compute on in-bounds cells and are not stored
@@ -393,8 +400,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         acc.add(psum, 1.f);
         acc.add(esum, 1.f);
       }
-      // (D) inputs of the next step
-      if (t >= l1lo && t <= l1hi) load_kinds(t);
+      // (D) level-2 inputs of the next step
       prefetch2(t - 2);
       // (E) raw plane t+1 for the next step's level 1
       if (has_next) {
@@ -454,8 +460,11 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
   }
 }
 
+int cp_kslot(int R1) { return (R1 + 32 + 15) & ~15; }
+
 size_t cp_smem(int R0, int R1, bool fuse) {
-  return 128 + (size_t)CP_NS * R0 * 4 + (size_t)CP_NY * R1 * 4 + (fuse ? (size_t)R0 * 4 : 0) + 2 * (size_t)R1;
+  return 128 + (size_t)CP_NS * R0 * 4 + (size_t)CP_NY * R1 * 4 + (fuse ? (size_t)R0 * 4 : 0) +
+         (size_t)CP_NS * cp_kslot(R1);
 }
 
 int cp_halo(int n3) { return (n3 + 1 + 3) & ~3; }
@@ -505,6 +514,7 @@ void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
   a.HA = cp_halo(g->n3);
   a.R0 = CP_TILE + 4 * a.HA;
   a.R1 = CP_TILE + 2 * a.HA;
+  a.KS = cp_kslot(a.R1);
   a.tiles = (a.P + CP_TILE - 1) / CP_TILE;
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
   a.a0 = coeffs[0]; a.a1 = coeffs[1]; a.a2 = coeffs[2];

@@ -54,7 +54,7 @@ struct xf_grid {
   int64_t end_index;
   uint8_t* code;             // device, per cell: the reference point code (0..8)
   uint8_t* nflag;            // device, per Normal (code 5) cell: bit 0/1/2 = normal x/y/z nonzero
-  uint8_t* kind;             // device, per cell
+  uint8_t* kind;             // device, per cell, then 64 zero bytes
   uint8_t* smask;            // device, per cell (0/1)
   int32_t* inv;              // device, Rn index per cell (0 inactive)
   int32_t* brow_of;          // device, per cell: index into brow arrays or -1

@@ -414,7 +414,10 @@ extern "C" int xf_grid_create(xf_ctx* ctx, int n1, int n2, int n3, const int32_t
     G_TRY(cudaMalloc(&d_nrm, 3 * n * sizeof(double)));
     G_TRY(cudaMemcpyAsync(d_nrm, normals, 3 * n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   }
-  G_TRY(cudaMalloc(&g->kind, n));
+  // 64 zero bytes past the box: bulk copies of kind rows round their ends up
+  // to 16 bytes
+  G_TRY(cudaMalloc(&g->kind, n + 64));
+  G_TRY(cudaMemsetAsync(g->kind + n, 0, 64, ctx->stream));
   G_TRY(cudaMalloc(&g->smask, n));
   G_TRY(cudaMalloc(&d_isb, n));
   G_TRY(cudaMalloc(&g->inv, n * sizeof(int32_t)));
