@@ -36,6 +36,7 @@ N_CELLS = 256
 N_SPHERES = 64
 SEED = 20261203
 RTOL = 1e-8
+CHEB_DEGREE = int(os.environ.get("XF_BENCH_CHEB_DEGREE", "4"))   # degree of the polynomial preconditioner
 CALIB = os.path.join(ROOT, "profiles", "bench_calibration.json")
 
 
@@ -241,7 +242,7 @@ def main():
 
     from xflow_gb300 import capi
 
-    cheb = {"precond": capi.XF_PRECOND_CHEB}   # the timed solver's preconditioner
+    cheb = {"precond": capi.XF_PRECOND_CHEB, "cheb_degree": CHEB_DEGREE}   # the timed solver's preconditioner
 
     def one(precision, **kw):
         x.fill(0.0)
@@ -308,8 +309,16 @@ def main():
     # polyr_f32 reads r, q, e, p', kind and writes r', e, z (29 B); the others
     # as in their kernels' comments
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
-           "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29}
-    if "polyr_f32" in kms and "pq_fused_f32" in kms:
+           "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29,
+           "cheb4_first_fused_f32": 29, "cheb4_second_f32": 13}
+    if "cheb4_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE == 4:
+        # per chunk of 50: the two degree-4 passes once (the first without the
+        # update: timed as poly2_f32, the same work), then K1, the first pass
+        # with the update and the second pass 49 times, and K1 + the update +
+        # the FP64 replacement once
+        per_iter = {"cheb4_first_fused_f32": 49 / 50, "cheb4_second_f32": 1.0, "pq_fused_f32": 1.0,
+                    "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50, "residual_f64": 1 / 50}
+    elif "polyr_f32" in kms and "pq_fused_f32" in kms:
         # the timed solver's path, per chunk of 50: K0 once, K1 and the fused
         # update + K0 49 times, K1 + the update + the FP64 replacement once
         per_iter = {"polyr_f32": 49 / 50, "pq_fused_f32": 1.0, "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50,

@@ -39,6 +39,8 @@
 #include <stdint.h>
 #include <stdlib.h>
 
+#include <algorithm>
+#include <complex>
 #include <vector>
 
 #include "xf_bulk.cuh"
@@ -61,6 +63,7 @@ struct CpArgs {
   const float *pa, *pb;       // FUSE: direction buffers (I_PBUF names the current one)
   float* e;                   // FUSE: FP32 correction
   float* rout;                // FUSE: updated residual (own cells)
+  const float* dr;            // CP_SECOND: the residual of the (r, z) dot
   int n1, n3, P;
   int HA, R0, R1;             // halo unit (multiple of 4), raw region TILE + 4 HA, level-1 region TILE + 2 HA
   int KS;                     // bytes of a row-kind slot: R1 + 32 rounded up to 16
@@ -100,8 +103,18 @@ __device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, flo
   }
 }
 
-template <bool FUSE>
+// Launch modes.  A degree-2 preconditioner is one pass (CP_POLY, or
+// CP_POLY_FUSED carrying the residual update); a degree-4 one is the product
+// of two quadratic factors, z = p1(A) p2(A) r, in two passes: w = p2(A) r
+// (CP_FIRST, or CP_FIRST_FUSED with the update), then z = p1(A) w with the
+// (r, z) dot against the residual buffer dr (CP_SECOND).
+enum { CP_POLY = 0, CP_POLY_FUSED = 1, CP_FIRST = 2, CP_FIRST_FUSED = 3, CP_SECOND = 4 };
+
+template <int MODE>
 __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constant__ CpArgs a) {
+  constexpr bool FUSE = MODE == CP_POLY_FUSED || MODE == CP_FIRST_FUSED;
+  constexpr bool DOTZ = MODE == CP_POLY || MODE == CP_POLY_FUSED || MODE == CP_SECOND;   // (r, z)
+  constexpr bool DOTSEP = MODE == CP_SECOND;   // r of the dot is not the input
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ double sh[32];
   __shared__ bool last;
@@ -229,11 +242,15 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     const int ya = HA + 4 * threadIdx.x, yb = ya + CP_TILE / 2;   // their index in the level-1 region
     // level-2 inputs of the next plane, prefetched one step ahead (FUSE: the
     // updated residual this thread wrote three steps earlier, read through L2)
-    float4 rpa = make_float4(0.f, 0.f, 0.f, 0.f), rpb = rpa;
+    float4 rpa = make_float4(0.f, 0.f, 0.f, 0.f), rpb = rpa, dpa = rpa, dpb = rpa;
     uchar4 kpa = make_uchar4(0, 0, 0, 0), kpb = kpa;
     auto prefetch2 = [&](int pl) {
       if (pl < i0 || pl >= i1) return;
       const int64_t o = (int64_t)pl * P;
+      if (DOTSEP) {
+        if (va) dpa = __ldg(reinterpret_cast<const float4*>(a.dr + o + xa));
+        if (vb) dpb = __ldg(reinterpret_cast<const float4*>(a.dr + o + xb));
+      }
       if (FUSE) {
         if (va) rpa = __ldcg(reinterpret_cast<const float4*>(r2src + o + xa));
         if (vb) rpb = __ldcg(reinterpret_cast<const float4*>(r2src + o + xb));
@@ -380,13 +397,15 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         // (r, z) of this thread's cells: FP32 sum of the products plus the sum of
         // their exact rounding errors, into the float-float accumulator per plane
         float psum = 0.f, esum = 0.f;
-        auto group = [&](bool v, int s, float4 rr, uchar4 k4, int x) {
+        auto group = [&](bool v, int s, float4 rr, float4 dd, uchar4 k4, int x) {
           float ay[4];
           lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
           if (!v) return;
           const float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
                                fmaf(a.a0, rr.w, ay[3])};
           *reinterpret_cast<float4*>(a.z + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
+          if (!DOTZ) return;
+          if (DOTSEP) rr = dd;
           const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
 #pragma unroll
           for (int q = 0; q < 4; q++) {
@@ -395,10 +414,12 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
             psum += pr;
           }
         };
-        group(va, ya, rpa, kpa, xa);
-        group(vb, yb, rpb, kpb, xb);
-        acc.add(psum, 1.f);
-        acc.add(esum, 1.f);
+        group(va, ya, rpa, dpa, kpa, xa);
+        group(vb, yb, rpb, dpb, kpb, xb);
+        if (DOTZ) {
+          acc.add(psum, 1.f);
+          acc.add(esum, 1.f);
+        }
       }
       // (D) level-2 inputs of the next step
       prefetch2(t - 2);
@@ -426,6 +447,17 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       S->iscalars[I_STATUS] = XF_ERR_CUDA;
     }
     __syncthreads();
+    return;
+  }
+  if (MODE == CP_FIRST) return;   // the second pass reduces and steps the control
+  if (MODE == CP_FIRST_FUSED) {   // (r, r) of the updated residual: the stop test
+    if (!publish_acc<float>(S, SL_B, SL_B, acc_rr, sh, &last)) return;
+    double tot = finish_partials(S, SL_B, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[SL_B] = tot;
+      S->tickets[SL_B] = 0;
+      control_step(S, CTL_PCG_RR);
+    }
     return;
   }
   if (!FUSE) {
@@ -471,19 +503,20 @@ int cp_halo(int n3) { return (n3 + 1 + 3) & ~3; }
 
 }  // namespace
 
-// Monomial coefficients, in A, of the Chebyshev-iteration polynomial after two
-// matrix-vector products for A z = r over [lmax / ratio, lmax], scaled so that
-// the constant term is 1 (a positive multiple of a preconditioner leaves
-// preconditioned CG unchanged).
-void xf_cheb2_coeffs(double lmax, double ratio, float out[3]) {
-  const double lo = 1.0 / ratio, hi = 1.0;   // in units of lmax
+// Monomial coefficients, in mu = lambda / lmax, of the Chebyshev-iteration
+// polynomial after `deg` steps for A z = r over [lmax / ratio, lmax] (the
+// iteration z_{k+1} = z_k + d_{k+1}, d_{k+1} = rho_{k+1} rho_k d_k +
+// 2 rho_{k+1} / delta (r - A z_k)), scaled so that the constant term is 1 (a
+// positive multiple of a preconditioner leaves preconditioned CG unchanged).
+static std::vector<double> cheb_mu_coeffs(double ratio, int deg) {
+  const double lo = 1.0 / ratio, hi = 1.0;
   const double theta = (hi + lo) / 2, delta = (hi - lo) / 2, sigma = theta / delta;
   double rho = 1 / sigma;
-  std::vector<double> d = {1 / theta}, z = d;   // polynomials in lambda / lmax
-  for (int it = 0; it < 2; it++) {
+  std::vector<double> d = {1 / theta}, z = d;
+  for (int it = 0; it < deg; it++) {
     std::vector<double> res(z.size() + 1, 0.0);
     res[0] = 1.0;
-    for (size_t j = 0; j < z.size(); j++) res[j + 1] -= z[j];   // 1 - lambda z
+    for (size_t j = 0; j < z.size(); j++) res[j + 1] -= z[j];   // 1 - mu z
     const double rho_new = 1 / (2 * sigma - rho);
     std::vector<double> dn(res.size(), 0.0);
     for (size_t j = 0; j < d.size(); j++) dn[j] += rho_new * rho * d[j];
@@ -493,7 +526,77 @@ void xf_cheb2_coeffs(double lmax, double ratio, float out[3]) {
     for (size_t j = 0; j < d.size(); j++) z[j] += d[j];
     rho = rho_new;
   }
-  for (int j = 0; j < 3; j++) out[j] = (float)(z[j] / z[0] / pow(lmax, j));
+  const double c0 = z[0];
+  for (double& c : z) c /= c0;
+  return z;
+}
+
+// Degree 2: p(A) = out[0] + out[1] A + out[2] A^2.
+void xf_cheb2_coeffs(double lmax, double ratio, float out[3]) {
+  const std::vector<double> z = cheb_mu_coeffs(ratio, 2);
+  for (int j = 0; j < 3; j++) out[j] = (float)(z[j] / pow(lmax, j));
+}
+
+// Degree 4 as two real quadratic factors p(A) = p1(A) p2(A), each with
+// constant term 1: the four roots of p (Durand-Kerner iteration in complex
+// double) paired as conjugates, or, when real, the two smallest and the two
+// largest.  Returns false if the factors do not reproduce p to 1e-9.
+bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]) {
+  const std::vector<double> c = cheb_mu_coeffs(ratio, 4);
+  typedef std::complex<double> cd;
+  cd root[4];
+  for (int k = 0; k < 4; k++) root[k] = 2.0 * std::pow(cd(0.4, 0.9), k);
+  auto eval = [&](cd x) { return (((c[4] * x + c[3]) * x + c[2]) * x + c[1]) * x + c[0]; };
+  for (int it = 0; it < 2000; it++) {
+    double change = 0;
+    for (int k = 0; k < 4; k++) {
+      cd den = c[4];
+      for (int m = 0; m < 4; m++)
+        if (m != k) den *= root[k] - root[m];
+      const cd step = eval(root[k]) / den;
+      root[k] -= step;
+      change = std::max(change, std::abs(step) / std::max(1.0, std::abs(root[k])));
+    }
+    if (change < 1e-15) break;
+  }
+  std::sort(root, root + 4, [](const cd& x, const cd& y) { return x.real() < y.real(); });
+  // pairs: a complex root with the root nearest its conjugate, a real root
+  // with the next unused real root (real roots come in an even number)
+  auto is_real = [&](int k) { return std::abs(root[k].imag()) <= 1e-12 * std::max(1.0, std::abs(root[k])); };
+  int pair[4], np = 0;
+  bool used[4] = {false, false, false, false};
+  for (int k = 0; k < 4; k++) {
+    if (used[k]) continue;
+    int best = -1;
+    for (int m = k + 1; m < 4; m++) {
+      if (used[m] || is_real(m) != is_real(k)) continue;
+      if (best < 0 || std::abs(root[m] - std::conj(root[k])) < std::abs(root[best] - std::conj(root[k]))) best = m;
+      if (is_real(k)) break;
+    }
+    if (best < 0) return false;
+    used[k] = used[best] = true;
+    pair[np++] = k;
+    pair[np++] = best;
+  }
+  double q[2][3];
+  for (int f = 0; f < 2; f++) {
+    const cd ra = root[pair[2 * f]], rb = root[pair[2 * f + 1]];
+    const cd s1 = 1.0 / ra + 1.0 / rb, s2 = 1.0 / (ra * rb);
+    if (std::abs(s1.imag()) > 1e-9 * std::max(1.0, std::abs(s1)) || std::abs(s2.imag()) > 1e-9 * std::max(1.0, std::abs(s2)))
+      return false;
+    q[f][0] = 1.0; q[f][1] = -s1.real(); q[f][2] = s2.real();
+  }
+  for (int j = 0; j <= 4; j++) {   // (q1 q2)_j against c_j
+    double v = 0;
+    for (int i = 0; i <= 2; i++)
+      if (j - i >= 0 && j - i <= 2) v += q[0][i] * q[1][j - i];
+    if (std::abs(v - c[j]) > 1e-9 * std::max(1.0, std::abs(c[j]))) return false;
+  }
+  for (int j = 0; j < 3; j++) {
+    f1[j] = (float)(q[0][j] / pow(lmax, j));
+    f2[j] = (float)(q[1][j] / pow(lmax, j));
+  }
+  return true;
 }
 
 bool xf_cg_poly_supported(const xf_grid* g) {
@@ -505,8 +608,9 @@ bool xf_cg_poly_supported(const xf_grid* g) {
 
 namespace {
 
-template <bool FUSE>
+template <int MODE>
 void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
+  constexpr bool FUSE = MODE == CP_POLY_FUSED || MODE == CP_FIRST_FUSED;
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
   a.kind = g->kind; a.S = ctx->scratch;
@@ -521,7 +625,7 @@ void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
   const size_t smem = cp_smem(a.R0, a.R1, FUSE);
   static size_t attr = 0;
   if (attr < smem) {
-    cudaFuncSetAttribute(k_cg_poly2<FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_cg_poly2<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = smem;
   }
   int resident = (int)((228 * 1024) / (smem + 2048));
@@ -544,7 +648,7 @@ void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
     const long cap = strtol(env, nullptr, 10);
     if (cap >= 1 && cap < blocks) blocks = cap;
   }
-  k_cg_poly2<FUSE><<<(int)blocks, CP_THREADS, smem, ctx->stream>>>(a);
+  k_cg_poly2<MODE><<<(int)blocks, CP_THREADS, smem, ctx->stream>>>(a);
 }
 
 }  // namespace
@@ -552,7 +656,7 @@ void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
 void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float coeffs[3]) {
   CpArgs a = {};
   a.r = r; a.z = z;
-  poly_launch<false>(op, a, coeffs);
+  poly_launch<CP_POLY>(op, a, coeffs);
 }
 
 // The fused launch: r_out = r - alpha q on the own cells, e += alpha p' (p' the
@@ -562,5 +666,23 @@ void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const flo
                         const float* pb, float* e, float* z, const float coeffs[3]) {
   CpArgs a = {};
   a.r = r; a.z = z; a.q = q; a.pa = pa; a.pb = pb; a.e = e; a.rout = r_out;
-  poly_launch<true>(op, a, coeffs);
+  poly_launch<CP_POLY_FUSED>(op, a, coeffs);
+}
+
+// The two passes of a factored degree-4 preconditioner z = p1(A) p2(A) r:
+// the first gives w = p2(A) r (with the residual update fused in when q is
+// given: r_out = r - alpha q, e += alpha p', (r_out, r_out) -> the stop test),
+// the second z = p1(A) w with (r, z) -> beta, r the residual after the update.
+void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
+                             const float* pa, const float* pb, float* e, float* r_out) {
+  CpArgs a = {};
+  a.r = r; a.z = w; a.q = q; a.pa = pa; a.pb = pb; a.e = e; a.rout = r_out;
+  if (q) poly_launch<CP_FIRST_FUSED>(op, a, coeffs);
+  else poly_launch<CP_FIRST>(op, a, coeffs);
+}
+
+void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, float* z, const float coeffs[3]) {
+  CpArgs a = {};
+  a.r = w; a.z = z; a.dr = r;
+  poly_launch<CP_SECOND>(op, a, coeffs);
 }

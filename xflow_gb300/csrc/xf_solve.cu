@@ -34,6 +34,10 @@ void xf_cg_poly_launch(const xf_op* op, const float* r, float* z, const float co
 void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const float* q, const float* pa,
                         const float* pb, float* e, float* z, const float coeffs[3]);
 void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
+bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]);
+void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
+                             const float* pa, const float* pb, float* e, float* r_out);
+void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, float* z, const float coeffs[3]);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 bool xf_cg_pqt_supported(const xf_grid* g);
 bool xf_cgf_supported(const xf_grid* g);
@@ -505,8 +509,11 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   double rel = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr;
   float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr, *z32 = nullptr;
-  float* r32b = nullptr;
+  float *r32b = nullptr, *w32 = nullptr;
+  const int cheb_deg = o.reserved[2] > 0 ? o.reserved[2] : 4;
   const bool cheb = o.precond == XF_PRECOND_CHEB;
+  if (cheb && cheb_deg != 2 && cheb_deg != 4)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_solve: XF_PRECOND_CHEB degree (opts.reserved[2]) must be 2 or 4");
   if (cheb && (!mixed || op->kind != XF_OP_LAPLACE || !xf_cg_poly_supported(g) || !xf_cg_pqb_supported(g)))
     return xf_fail(ctx, XF_ERR_UNSUPPORTED,
                    "xf_solve: XF_PRECOND_CHEB needs mixed precision and a uniform Laplace grid without boundary rows "
@@ -521,7 +528,7 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       p32b = B.get<float>(n);
       if (!p32b) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
     }
-    if (cheb && (!(z32 = B.get<float>(n)) || !(r32b = B.get<float>(n))))
+    if (cheb && (!(z32 = B.get<float>(n)) || !(r32b = B.get<float>(n)) || (cheb_deg == 4 && !(w32 = B.get<float>(n)))))
       return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
   }
   double* tmp = B.get<double>(n, false);
@@ -560,15 +567,23 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       // K1 + fused K2/K0 per iteration, and a last K1 + K2 with the FP64 fold
       // and the true-residual replacement into the first buffer; the next
       // chunk's K0 continues the direction from the replaced residual.
-      // XF_POLYR=0 runs K2 and K0 as separate launches.
+      // Degree 4 (the default) splits K0 into two passes, one per quadratic
+      // factor of p: w = p2(A) r (fused with K2 as above) and z = p1(A) w with
+      // (r, z).  XF_POLYR=0 runs K2 and K0 as separate launches.
       chunk = o.replace_every;
       float *e = e32, *r = r32, *pa = p32, *q = q32, *z = z32;
-      float *pb = p32b, *rb = r32b;
+      float *pb = p32b, *rb = r32b, *w = w32;
       const bool fused = !(getenv("XF_POLYR") && getenv("XF_POLYR")[0] == '0');
+      const bool deg4 = cheb_deg == 4;
       const double lmax = 4.0 * (g->ucx + g->ucy + g->ucz);   // Gershgorin bound of the uniform Laplace rows
-      const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : 30.0;
-      float coeffs[3];
-      xf_cheb2_coeffs(lmax, ratio, coeffs);
+      const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : deg4 ? 120.0 : 30.0;
+      float coeffs[3], f1[3], f2[3];
+      if (deg4) {
+        if (!xf_cheb4_factors(lmax, ratio, f1, f2))
+          return xf_fail(ctx, XF_ERR_ARG, "xf_solve: no real quadratic factors of the degree-4 polynomial (ratio %g)", ratio);
+      } else {
+        xf_cheb2_coeffs(lmax, ratio, coeffs);
+      }
       XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
       XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
       XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
@@ -578,10 +593,23 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       iter = [=](int c) {
         // the residual before this iteration's update (fused: buffer c & 1)
         float* rc = fused && (c & 1) ? rb : r;
-        if (!fused || c == 0) xf_cg_poly_launch(op, rc, z, coeffs);
+        if (!fused || c == 0) {
+          if (deg4) {
+            xf_cg_poly_first_launch(op, rc, w, f2, nullptr, nullptr, nullptr, nullptr, nullptr);
+            xf_cg_poly_second_launch(op, w, rc, z, f1);
+          } else {
+            xf_cg_poly_launch(op, rc, z, coeffs);
+          }
+        }
         xf_cg_pqb_launch(op, z, pa, pb, q, CTL_PCG_ALPHA_FLIP);
         if (fused && c < last) {
-          xf_cg_polyr_launch(op, rc, (c & 1) ? r : rb, q, pa, pb, e, z, coeffs);
+          float* rn = (c & 1) ? r : rb;
+          if (deg4) {
+            xf_cg_poly_first_launch(op, rc, w, f2, q, pa, pb, e, rn);
+            xf_cg_poly_second_launch(op, w, rn, z, f1);
+          } else {
+            xf_cg_polyr_launch(op, rc, rn, q, pa, pb, e, z, coeffs);
+          }
         } else {
           k_cg_xr<float><<<xb32, RED_THREADS, 0, ctx->stream>>>(e, rc, pa, q, n, S, pb, CTL_PCG_RR);
         }
@@ -872,7 +900,7 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
     if (xf_cg_pqt_supported(g)) ms_out[6] = time([&] { xf_cg_pq32_variant(op, r, p, p2, q, 1); });
   }
-  ms_out[7] = ms_out[8] = -1.0;
+  ms_out[7] = ms_out[8] = ms_out[9] = ms_out[10] = -1.0;
   if (xf_cg_poly_supported(g)) {
     float coeffs[3];
     xf_cheb2_coeffs(4.0 * (g->ucx + g->ucy + g->ucz), 30.0, coeffs);
@@ -880,6 +908,11 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     float *r2 = B.get<float>(n), *z2 = B.get<float>(n);
     if (!r2 || !z2) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
     ms_out[8] = time([&] { xf_cg_polyr_launch(op, r, r2, q, p, p, e, z2, coeffs); });
+    float f1[3], f2[3];
+    if (xf_cheb4_factors(4.0 * (g->ucx + g->ucy + g->ucz), 120.0, f1, f2)) {
+      ms_out[9] = time([&] { xf_cg_poly_first_launch(op, r, z2, f2, q, p, p, e, r2); });
+      ms_out[10] = time([&] { xf_cg_poly_second_launch(op, z2, r2, e, f1); });
+    }
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
