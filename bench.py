@@ -7,9 +7,11 @@ side = -div of an i.i.d. N(0,1) staggered velocity, projected to zero mean.
 One "step" is one solve from x = 0 to ||b - A x||_2 <= 1e-8 ||b||_2 (true
 FP64 residual).  The timed solver is the mixed-precision CG (FP32 stencil and
 vectors, FP64 dots/scalars, FP64 residual replacement every 50 iterations)
-preconditioned by the degree-2 Chebyshev polynomial z = p(A) r (both stencil
-levels in one pass over memory); plain FP64 CG and the unpreconditioned
-mixed CG on the same system are timed beside it.
+preconditioned by the degree-8 Chebyshev polynomial z = p1(A) ... p4(A) r
+(four real quadratic factors, both stencil levels of each in one pass over
+memory, the residual update fused into the first pass); plain FP64 CG and
+the unpreconditioned mixed CG on the same system are timed beside it
+(XF_BENCH_CHEB_DEGREE=2, 4, ... 12 times another degree instead).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xflow|reference]
 
@@ -36,7 +38,8 @@ N_CELLS = 256
 N_SPHERES = 64
 SEED = 20261203
 RTOL = 1e-8
-CHEB_DEGREE = int(os.environ.get("XF_BENCH_CHEB_DEGREE", "4"))   # degree of the polynomial preconditioner
+CHEB_DEGREE = int(os.environ.get("XF_BENCH_CHEB_DEGREE", "8"))   # degree of the polynomial preconditioner
+CHEB_RATIO = {2: 30, 4: 120}.get(CHEB_DEGREE, 250)                # its default lambda_max / lambda_min
 CALIB = os.path.join(ROOT, "profiles", "bench_calibration.json")
 
 
@@ -310,14 +313,16 @@ def main():
     # as in their kernels' comments
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
            "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29,
-           "cheb4_first_fused_f32": 29, "cheb4_second_f32": 13}
-    if "cheb4_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE == 4:
-        # per chunk of 50: the two degree-4 passes once (the first without the
-        # update: timed as poly2_f32, the same work), then K1, the first pass
-        # with the update and the second pass 49 times, and K1 + the update +
-        # the FP64 replacement once
-        per_iter = {"cheb4_first_fused_f32": 49 / 50, "cheb4_second_f32": 1.0, "pq_fused_f32": 1.0,
-                    "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50, "residual_f64": 1 / 50}
+           "cheb_first_fused_f32": 29, "cheb_last_f32": 13, "cheb_middle_f32": 9}
+    if "cheb_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE >= 4:
+        # per chunk of 50: the passes of the m = degree / 2 factors once (the
+        # first without the update: timed as a middle pass, the same work),
+        # then K1, the first pass with the update, m - 2 middle passes and
+        # the last pass 49 times, and K1 + the update + the FP64 replacement
+        # once
+        m = CHEB_DEGREE // 2
+        per_iter = {"cheb_first_fused_f32": 49 / 50, "cheb_middle_f32": (m - 2) + 1 / 50,
+                    "cheb_last_f32": 1.0, "pq_fused_f32": 1.0, "xr_update_f32": 1 / 50, "residual_f64": 1 / 50}
     elif "polyr_f32" in kms and "pq_fused_f32" in kms:
         # the timed solver's path, per chunk of 50: K0 once, K1 and the fused
         # update + K0 49 times, K1 + the update + the FP64 replacement once
@@ -370,9 +375,13 @@ def main():
         "dtype": "f32 (f64 dots, scalars, residual replacement)", "data": "synthetic",
         "config": {"workload": workload_name(args.size),
                    "solver": "mixed-precision CG (FP32 matvec/vectors, FP64 dots, true-residual replacement/50)",
-                   "preconditioner": "degree-2 Chebyshev polynomial z = p(A) r over [lmax/30, lmax], both stencil "
-                                     "levels temporally blocked in one pass (the learned U-Net preconditioner is "
-                                     "timed by bench.py --learned: fewer iterations, but 27.6 ms per application)",
+                   "preconditioner": (f"degree-{CHEB_DEGREE} Chebyshev polynomial over [lmax/{CHEB_RATIO}, "
+                                      "lmax]" + (f" as {CHEB_DEGREE // 2} real quadratic factors, one two-level stencil "
+                                                 "pass each, the residual update fused into the first"
+                                                 if CHEB_DEGREE >= 4 else
+                                                 ", both stencil levels in one pass, the residual update fused in") +
+                                      " (the learned U-Net preconditioner is timed by bench.py --learned: fewer "
+                                      "iterations, but 26.1 ms per application)"),
                    "rtol": RTOL,
                    "l2": "working set ~0.6 GB > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},

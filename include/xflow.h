@@ -203,10 +203,11 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
 /* XF_PRECOND_CHEB: XF_CG with XF_PREC_MIXED on a uniform Laplace grid without
  * boundary rows, preconditioned by z = p(A) r, p the polynomial of `degree`
  * Chebyshev-iteration steps over [lambda_max / ratio, lambda_max]
- * (lambda_max the Gershgorin bound; degree = opts.reserved[2], 2 or 4,
- * default 4; ratio = opts.reserved[1], default 120 for degree 4 and 30 for
- * degree 2).  Degree 2 applies both stencil levels in one pass over memory;
- * degree 4 is the product of two real quadratic factors, one pass each. */
+ * (lambda_max the Gershgorin bound; degree = opts.reserved[2], even, 2 to 12,
+ * default 8; ratio = opts.reserved[1], default 30 for degree 2, 120 for
+ * degree 4 and 250 above).  Degree 2 applies both stencil levels in one pass
+ * over memory; degree 2 m is the product of m real quadratic factors, one
+ * pass each. */
 enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3 };
 
 typedef struct {
@@ -452,7 +453,8 @@ int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, co
  * alpha q, e += alpha p', z = p(A) r', (r', r'), (r', z)), or -1; [9] the
  * first pass of the degree-4 preconditioner with the update fused in (r' =
  * r - alpha q, e += alpha p', w = p2(A) r', (r', r')) and [10] its second pass
- * (z = p1(A) w, (r', z)), or -1.  ms_out holds 11 doubles.  Laplace operators
+ * (z = p1(A) w, (r', z)), or -1; [11] a middle pass of a higher degree (w' =
+ * p_k(A) w, no dot), or -1.  ms_out holds 12 doubles.  Laplace operators
  * only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 

@@ -318,8 +318,8 @@ def test_chebyshev_preconditioned_mixed_cg(ctx, monkeypatch, n):
     """Mixed CG with the Chebyshev polynomial preconditioner against plain
     mixed CG on the same system: degree 2 (both stencil levels of z = p(A) r
     in one pass) meets the same true FP64 tolerance in well under 0.6 x the
-    iterations, degree 4 (two passes, one per quadratic factor) in under 0.4 x,
-    and the solutions agree within the solve's own accuracy; also with a
+    iterations, degrees 4, 6, 8 (one pass per quadratic factor) in under 0.4,
+    0.32, 0.26 x, and the solutions agree within the solve's own accuracy; also with a
     capped grid (several work items per block, the cross-item load stream)."""
     codes, nrm, sep, b = spheres_case(n, 8, 21)
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
@@ -330,7 +330,7 @@ def test_chebyshev_preconditioned_mixed_cg(ctx, monkeypatch, n):
     assert s0.status == capi.XF_OK
     sm = codes != 0
     ref = x0.download()
-    for cap, deg in ((None, 2), (None, 4), ("3", 2), ("3", 4)):
+    for cap, deg in ((None, 2), (None, 4), (None, 6), ("3", 2), ("3", 4), ("3", 8)):
         if cap:
             monkeypatch.setenv("XF_POLY_BLOCKS", cap)
         else:
@@ -339,16 +339,17 @@ def test_chebyshev_preconditioned_mixed_cg(ctx, monkeypatch, n):
         st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=1e-9, precond=capi.XF_PRECOND_CHEB,
                       cheb_degree=deg)
         assert st.status == capi.XF_OK and st.rel_resid <= 1e-9, (deg, st.status, st.rel_resid)
-        assert st.iterations < (0.6 if deg == 2 else 0.4) * s0.iterations, (deg, st.iterations, s0.iterations)
+        assert st.iterations < {2: 0.6, 4: 0.4, 6: 0.32, 8: 0.26}[deg] * s0.iterations, (deg, st.iterations,
+                                                                                  s0.iterations)
         d = (x.download() - x.download()[sm].mean()) - (ref - ref[sm].mean())
         assert np.abs(d[sm]).max() <= 1e-6 * np.abs(ref[sm] - ref[sm].mean()).max()
     monkeypatch.delenv("XF_POLY_BLOCKS", raising=False)
 
 
 @pytest.mark.parametrize("n,replace_every,deg", [(48, 50, 2), (70, 7, 2), (64, 1, 2), (48, 50, 4), (70, 7, 4),
-                                                  (64, 1, 4)])
+                                                  (64, 1, 4), (48, 50, 6), (70, 7, 8)])
 def test_fused_residual_update_matches_separate_launches(ctx, monkeypatch, n, replace_every, deg):
-    """The preconditioned solve (degree 2 and 4) with the residual update
+    """The preconditioned solve (degrees 2 to 8) with the residual update
     fused into the (first) polynomial pass (two residual buffers) against the
     same solve with the
     update and the polynomial as separate launches: the iterates are the same

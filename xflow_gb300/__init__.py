@@ -268,8 +268,8 @@ class PackedOperator(Operator):
 def solve_opts(method=XF_CG, precision=XF_PREC_FP64, rtol=1e-8, atol=0.0, maxit=100000, replace_every=50,
                check_every=16, exact=False, precond=None, cheb_ratio=0, cheb_degree=0):
     """precond: capi.XF_PRECOND_CHEB with XF_CG and XF_PREC_MIXED for the polynomial preconditioner
-    (cheb_ratio: its lambda_max / lambda_min, 0 for the default; cheb_degree: 2 or 4, 0 for the
-    default 4)."""
+    (cheb_ratio: its lambda_max / lambda_min, 0 for the default; cheb_degree: even, 2 to 12, 0 for the
+    default 8)."""
     o = capi.SolveOpts()
     capi.lib().xf_solve_opts_default(C.byref(o))
     o.method, o.precision, o.rtol, o.atol, o.maxit = method, precision, rtol, atol, maxit
@@ -290,7 +290,8 @@ def solve(op, x, b, **kw):
 
 
 CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "stencil_f64", "pq_fused_f32",
-              "pq_march_f32", "poly2_f32", "polyr_f32", "cheb4_first_fused_f32", "cheb4_second_f32")
+              "pq_march_f32", "poly2_f32", "polyr_f32", "cheb_first_fused_f32", "cheb_last_f32",
+              "cheb_middle_f32")
 
 
 def profile_cg_kernels(op, reps=20):

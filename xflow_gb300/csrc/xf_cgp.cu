@@ -40,6 +40,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <array>
 #include <complex>
 #include <vector>
 
@@ -537,21 +538,28 @@ void xf_cheb2_coeffs(double lmax, double ratio, float out[3]) {
   for (int j = 0; j < 3; j++) out[j] = (float)(z[j] / pow(lmax, j));
 }
 
-// Degree 4 as two real quadratic factors p(A) = p1(A) p2(A), each with
-// constant term 1: the four roots of p (Durand-Kerner iteration in complex
-// double) paired as conjugates, or, when real, the two smallest and the two
-// largest.  Returns false if the factors do not reproduce p to 1e-9.
-bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]) {
-  const std::vector<double> c = cheb_mu_coeffs(ratio, 4);
+// An even degree d = 2 m (4 to 12) as m real quadratic factors
+// p(A) = p_1(A) ... p_m(A), each with constant term 1: the roots of p
+// (Durand-Kerner iteration in complex double) paired as conjugates, real
+// roots with their real neighbours.  f[k] holds factor k+1 as (1, b1, b2) in
+// A.  Returns false if the factors do not reproduce p to 1e-9 (relative to
+// the largest coefficient).
+bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]) {
+  if (deg < 4 || deg > 12 || deg % 2) return false;
+  const std::vector<double> c = cheb_mu_coeffs(ratio, deg);
   typedef std::complex<double> cd;
-  cd root[4];
-  for (int k = 0; k < 4; k++) root[k] = 2.0 * std::pow(cd(0.4, 0.9), k);
-  auto eval = [&](cd x) { return (((c[4] * x + c[3]) * x + c[2]) * x + c[1]) * x + c[0]; };
-  for (int it = 0; it < 2000; it++) {
+  std::vector<cd> root(deg);
+  for (int k = 0; k < deg; k++) root[k] = 2.0 * std::pow(cd(0.4, 0.9), k);
+  auto eval = [&](cd x) {
+    cd v = c[deg];
+    for (int j = deg - 1; j >= 0; j--) v = v * x + c[j];
+    return v;
+  };
+  for (int it = 0; it < 5000; it++) {
     double change = 0;
-    for (int k = 0; k < 4; k++) {
-      cd den = c[4];
-      for (int m = 0; m < 4; m++)
+    for (int k = 0; k < deg; k++) {
+      cd den = c[deg];
+      for (int m = 0; m < deg; m++)
         if (m != k) den *= root[k] - root[m];
       const cd step = eval(root[k]) / den;
       root[k] -= step;
@@ -559,42 +567,54 @@ bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]) {
     }
     if (change < 1e-15) break;
   }
-  std::sort(root, root + 4, [](const cd& x, const cd& y) { return x.real() < y.real(); });
+  std::sort(root.begin(), root.end(), [](const cd& x, const cd& y) { return x.real() < y.real(); });
   // pairs: a complex root with the root nearest its conjugate, a real root
   // with the next unused real root (real roots come in an even number)
   auto is_real = [&](int k) { return std::abs(root[k].imag()) <= 1e-12 * std::max(1.0, std::abs(root[k])); };
-  int pair[4], np = 0;
-  bool used[4] = {false, false, false, false};
-  for (int k = 0; k < 4; k++) {
+  std::vector<int> pair;
+  std::vector<bool> used(deg, false);
+  for (int k = 0; k < deg; k++) {
     if (used[k]) continue;
     int best = -1;
-    for (int m = k + 1; m < 4; m++) {
+    for (int m = k + 1; m < deg; m++) {
       if (used[m] || is_real(m) != is_real(k)) continue;
       if (best < 0 || std::abs(root[m] - std::conj(root[k])) < std::abs(root[best] - std::conj(root[k]))) best = m;
       if (is_real(k)) break;
     }
     if (best < 0) return false;
     used[k] = used[best] = true;
-    pair[np++] = k;
-    pair[np++] = best;
+    pair.push_back(k);
+    pair.push_back(best);
   }
-  double q[2][3];
-  for (int f = 0; f < 2; f++) {
-    const cd ra = root[pair[2 * f]], rb = root[pair[2 * f + 1]];
+  const int nf = deg / 2;
+  std::vector<double> prod = {1.0};
+  std::vector<std::array<double, 3>> q(nf);
+  for (int fi = 0; fi < nf; fi++) {
+    const cd ra = root[pair[2 * fi]], rb = root[pair[2 * fi + 1]];
     const cd s1 = 1.0 / ra + 1.0 / rb, s2 = 1.0 / (ra * rb);
     if (std::abs(s1.imag()) > 1e-9 * std::max(1.0, std::abs(s1)) || std::abs(s2.imag()) > 1e-9 * std::max(1.0, std::abs(s2)))
       return false;
-    q[f][0] = 1.0; q[f][1] = -s1.real(); q[f][2] = s2.real();
+    q[fi] = {1.0, -s1.real(), s2.real()};
+    std::vector<double> np(prod.size() + 2, 0.0);
+    for (size_t i = 0; i < prod.size(); i++)
+      for (int j = 0; j < 3; j++) np[i + j] += prod[i] * q[fi][j];
+    prod = np;
   }
-  for (int j = 0; j <= 4; j++) {   // (q1 q2)_j against c_j
-    double v = 0;
-    for (int i = 0; i <= 2; i++)
-      if (j - i >= 0 && j - i <= 2) v += q[0][i] * q[1][j - i];
-    if (std::abs(v - c[j]) > 1e-9 * std::max(1.0, std::abs(c[j]))) return false;
-  }
+  double cmax = 0;
+  for (double v : c) cmax = std::max(cmax, std::abs(v));
+  for (int j = 0; j <= deg; j++)
+    if (std::abs(prod[j] - c[j]) > 1e-9 * cmax) return false;
+  for (int fi = 0; fi < nf; fi++)
+    for (int j = 0; j < 3; j++) f[fi][j] = (float)(q[fi][j] / pow(lmax, j));
+  return true;
+}
+
+bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]) {
+  float f[2][3];
+  if (!xf_cheb_factors(lmax, ratio, 4, f)) return false;
   for (int j = 0; j < 3; j++) {
-    f1[j] = (float)(q[0][j] / pow(lmax, j));
-    f2[j] = (float)(q[1][j] / pow(lmax, j));
+    f1[j] = f[0][j];
+    f2[j] = f[1][j];
   }
   return true;
 }

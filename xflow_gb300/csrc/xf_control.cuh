@@ -56,6 +56,13 @@ __device__ inline void finish(DevScratch* S, long long status) {
   S->iscalars[I_STATUS] = status;
 }
 
+// Reliable updates of the preconditioned mixed CG: the FP32 recursion pauses
+// (and the true FP64 residual replaces it at the end of the graph chunk) once
+// its (r, r) has dropped by this factor since the last replacement, a 10^3
+// drop of the norm.  A strong preconditioner reaches FP32's floor within one
+// chunk, and continuing the direction from beyond that floor stalls.
+constexpr double PCG_REPL_DROP2 = 1e-6;
+
 // Runs in one thread (thread 0 of the last block of a reduction).
 __device__ inline void control_step(DevScratch* S, int ctl) {
   double* d = S->scalars;
@@ -126,7 +133,7 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       d[D_RR] = rn;
       // a paused recursion keeps the previous (r, z): the replacement's own
       // (r, z) continues the direction from it
-      if (rn <= d[D_THR] || I[I_IT] >= I[I_MAXIT]) { I[I_PAUSE] = 1; break; }
+      if (rn <= d[D_THR] || rn <= PCG_REPL_DROP2 * d[D_RR64] || I[I_IT] >= I[I_MAXIT]) { I[I_PAUSE] = 1; break; }
     }
       // fall through
     case CTL_PCG_BETA: {  // SL_D: (r, z) of the new residual
@@ -151,7 +158,7 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
       I[I_IT] += 1;
       if (isnan(rn)) { finish(S, XF_NAN); break; }
       d[D_RR] = rn;
-      if (rn <= d[D_THR] || I[I_IT] >= I[I_MAXIT]) I[I_PAUSE] = 1;
+      if (rn <= d[D_THR] || rn <= PCG_REPL_DROP2 * d[D_RR64] || I[I_IT] >= I[I_MAXIT]) I[I_PAUSE] = 1;
       break;
     }
     case CTL_PCG_REPL: {  // SL_C+1: true r.r in FP64; the next (r, z) continues the direction

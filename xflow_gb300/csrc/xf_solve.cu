@@ -15,6 +15,7 @@
 #include <stdlib.h>
 
 #include <functional>
+#include <utility>
 #include <vector>
 
 #include "xf_control.cuh"
@@ -35,6 +36,7 @@ void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const flo
                         const float* pb, float* e, float* z, const float coeffs[3]);
 void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
 bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]);
+bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]);
 void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
                              const float* pa, const float* pb, float* e, float* r_out);
 void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, float* z, const float coeffs[3]);
@@ -509,11 +511,11 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
   double rel = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr;
   float *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *p32b = nullptr, *z32 = nullptr;
-  float *r32b = nullptr, *w32 = nullptr;
-  const int cheb_deg = o.reserved[2] > 0 ? o.reserved[2] : 4;
+  float *r32b = nullptr, *w32 = nullptr, *w32b = nullptr;
+  const int cheb_deg = o.reserved[2] > 0 ? o.reserved[2] : 8;
   const bool cheb = o.precond == XF_PRECOND_CHEB;
-  if (cheb && cheb_deg != 2 && cheb_deg != 4)
-    return xf_fail(ctx, XF_ERR_ARG, "xf_solve: XF_PRECOND_CHEB degree (opts.reserved[2]) must be 2 or 4");
+  if (cheb && (cheb_deg < 2 || cheb_deg > 12 || cheb_deg % 2))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_solve: XF_PRECOND_CHEB degree (opts.reserved[2]) must be even, 2 to 12");
   if (cheb && (!mixed || op->kind != XF_OP_LAPLACE || !xf_cg_poly_supported(g) || !xf_cg_pqb_supported(g)))
     return xf_fail(ctx, XF_ERR_UNSUPPORTED,
                    "xf_solve: XF_PRECOND_CHEB needs mixed precision and a uniform Laplace grid without boundary rows "
@@ -528,7 +530,8 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       p32b = B.get<float>(n);
       if (!p32b) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
     }
-    if (cheb && (!(z32 = B.get<float>(n)) || !(r32b = B.get<float>(n)) || (cheb_deg == 4 && !(w32 = B.get<float>(n)))))
+    if (cheb && (!(z32 = B.get<float>(n)) || !(r32b = B.get<float>(n)) || (cheb_deg >= 4 && !(w32 = B.get<float>(n))) ||
+                 (cheb_deg >= 6 && !(w32b = B.get<float>(n)))))
       return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: cannot allocate CG vectors");
   }
   double* tmp = B.get<double>(n, false);
@@ -567,23 +570,34 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
       // K1 + fused K2/K0 per iteration, and a last K1 + K2 with the FP64 fold
       // and the true-residual replacement into the first buffer; the next
       // chunk's K0 continues the direction from the replaced residual.
-      // Degree 4 (the default) splits K0 into two passes, one per quadratic
-      // factor of p: w = p2(A) r (fused with K2 as above) and z = p1(A) w with
-      // (r, z).  XF_POLYR=0 runs K2 and K0 as separate launches.
+      // Degree 2 m >= 4 (8 is the default) splits K0 into m passes, one per
+      // quadratic factor of p: w = p_m(A) r (fused with K2 as above), m - 2
+      // passes w <- p_k(A) w, and z = p_1(A) w with (r, z).  XF_POLYR=0 runs
+      // K2 and K0 as separate launches.
       chunk = o.replace_every;
       float *e = e32, *r = r32, *pa = p32, *q = q32, *z = z32;
-      float *pb = p32b, *rb = r32b, *w = w32;
+      float *pb = p32b, *rb = r32b, *w = w32, *wb = w32b;
       const bool fused = !(getenv("XF_POLYR") && getenv("XF_POLYR")[0] == '0');
-      const bool deg4 = cheb_deg == 4;
+      const int nf = cheb_deg / 2;
       const double lmax = 4.0 * (g->ucx + g->ucy + g->ucz);   // Gershgorin bound of the uniform Laplace rows
-      const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : deg4 ? 120.0 : 30.0;
-      float coeffs[3], f1[3], f2[3];
-      if (deg4) {
-        if (!xf_cheb4_factors(lmax, ratio, f1, f2))
-          return xf_fail(ctx, XF_ERR_ARG, "xf_solve: no real quadratic factors of the degree-4 polynomial (ratio %g)", ratio);
+      const double ratio = o.reserved[1] > 0 ? (double)o.reserved[1] : nf > 2 ? 250.0 : nf > 1 ? 120.0 : 30.0;
+      float coeffs[3], f[6][3];
+      if (nf > 1) {
+        if (!xf_cheb_factors(lmax, ratio, cheb_deg, f))
+          return xf_fail(ctx, XF_ERR_ARG, "xf_solve: no real quadratic factors of the degree-%d polynomial (ratio %g)",
+                         cheb_deg, ratio);
       } else {
         xf_cheb2_coeffs(lmax, ratio, coeffs);
       }
+      // passes after the first: w <- p_k(A) w for k = m-1 .. 2 (ping-pong), then z = p_1(A) w
+      auto rest = [=](float* rres) {
+        float *src = w, *dst = wb;
+        for (int k = nf - 2; k >= 1; k--) {
+          xf_cg_poly_first_launch(op, src, dst, f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
+          std::swap(src, dst);
+        }
+        xf_cg_poly_second_launch(op, src, rres, z, f[0]);
+      };
       XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
       XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
       XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
@@ -594,9 +608,9 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         // the residual before this iteration's update (fused: buffer c & 1)
         float* rc = fused && (c & 1) ? rb : r;
         if (!fused || c == 0) {
-          if (deg4) {
-            xf_cg_poly_first_launch(op, rc, w, f2, nullptr, nullptr, nullptr, nullptr, nullptr);
-            xf_cg_poly_second_launch(op, w, rc, z, f1);
+          if (nf > 1) {
+            xf_cg_poly_first_launch(op, rc, w, f[nf - 1], nullptr, nullptr, nullptr, nullptr, nullptr);
+            rest(rc);
           } else {
             xf_cg_poly_launch(op, rc, z, coeffs);
           }
@@ -604,9 +618,9 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         xf_cg_pqb_launch(op, z, pa, pb, q, CTL_PCG_ALPHA_FLIP);
         if (fused && c < last) {
           float* rn = (c & 1) ? r : rb;
-          if (deg4) {
-            xf_cg_poly_first_launch(op, rc, w, f2, q, pa, pb, e, rn);
-            xf_cg_poly_second_launch(op, w, rn, z, f1);
+          if (nf > 1) {
+            xf_cg_poly_first_launch(op, rc, w, f[nf - 1], q, pa, pb, e, rn);
+            rest(rn);
           } else {
             xf_cg_polyr_launch(op, rc, rn, q, pa, pb, e, z, coeffs);
           }
@@ -900,7 +914,7 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     ms_out[5] = time([&] { xf_cg_pq32(op, r, p, p2, q); });
     if (xf_cg_pqt_supported(g)) ms_out[6] = time([&] { xf_cg_pq32_variant(op, r, p, p2, q, 1); });
   }
-  ms_out[7] = ms_out[8] = ms_out[9] = ms_out[10] = -1.0;
+  ms_out[7] = ms_out[8] = ms_out[9] = ms_out[10] = ms_out[11] = -1.0;
   if (xf_cg_poly_supported(g)) {
     float coeffs[3];
     xf_cheb2_coeffs(4.0 * (g->ucx + g->ucy + g->ucz), 30.0, coeffs);
@@ -912,6 +926,7 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
     if (xf_cheb4_factors(4.0 * (g->ucx + g->ucy + g->ucz), 120.0, f1, f2)) {
       ms_out[9] = time([&] { xf_cg_poly_first_launch(op, r, z2, f2, q, p, p, e, r2); });
       ms_out[10] = time([&] { xf_cg_poly_second_launch(op, z2, r2, e, f1); });
+      ms_out[11] = time([&] { xf_cg_poly_first_launch(op, z2, e, f1, nullptr, nullptr, nullptr, nullptr, nullptr); });
     }
   }
   cudaEventDestroy(t0);
