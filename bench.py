@@ -220,6 +220,8 @@ def main():
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
+    ap.add_argument("--degrees", default="",
+                    help="degree:ratio pairs (e.g. 4:120,8:250): one JSON line per preconditioner, best of 3 solves")
     ap.add_argument("--kernels-only", action="store_true",
                     help="a few launches of each hot kernel on the full grid (for ncu captures)")
     args = ap.parse_args()
@@ -227,6 +229,8 @@ def main():
         return reference_arm(args)
     if args.kernels_only:
         return kernels_only(args)
+    if args.degrees:
+        return degrees(args)
     if args.rows:
         return rows(args)
     if args.learned:
@@ -406,6 +410,31 @@ def main():
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def degrees(args):
+    """The timed solve with other degrees and intervals of the Chebyshev
+    preconditioner: iterations, true residual and device ms (best of 3)."""
+    import xflow_gb300 as xf
+    from xflow_gb300 import capi
+
+    codes, sep, b = workload(args.size)
+    ctx = xf.Context(0)
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    A = xf.Operator(g, xf.XF_OP_LAPLACE)
+    bv, x = g.vec(b), g.vec(np.zeros(g.shape))
+    for pair in args.degrees.split(","):
+        deg, ratio = (int(v) for v in pair.split(":"))
+        ms = []
+        for _ in range(3):
+            x.fill(0.0)
+            st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL,
+                          precond=capi.XF_PRECOND_CHEB, cheb_degree=deg, cheb_ratio=ratio)
+            assert st.status == 0, st.status
+            ms.append(st.ms)
+        print(json.dumps({"degree": deg, "ratio": ratio, "iterations": st.iterations, "rel_resid": st.rel_resid,
+                          "ms": min(ms)}), flush=True)
     return 0
 
 
