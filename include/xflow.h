@@ -458,6 +458,15 @@ int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, co
  * only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
+/* No counterpart in the reference (a self-test).  The time-step passes divide
+ * by grid spacings and the time step through their correctly rounded
+ * reciprocals and one FMA correction (Markstein's theorem), which must equal
+ * the IEEE division bit for bit.  Runs that division and the IEEE one on the
+ * device over n hashed operand pairs (mostly in the passes' operand ranges,
+ * a quarter fully random bit patterns) and writes the number of pairs whose
+ * results differ. */
+int xf_selftest_division(xf_ctx* ctx, long long n, unsigned long long seed, long long* mismatches);
+
 /* ---- allocation-free inner product --------------------------------------- */
 /* No counterpart in the reference (which has no device memory at all).
  * The masked FP64 dot of xf_dot, sum over c < n with d_mask[c] != 0 (d_mask

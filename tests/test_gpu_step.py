@@ -200,3 +200,12 @@ def test_momentum_equation_variable_viscosity(ctx):
     r = gu.vec(None)
     A.apply(xv, r, flags=xf.XF_ZERO_INACTIVE)
     assert np.abs(r.download()[sm] - b[sm]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("seed", [1, 20261203, 0xdeadbeef])
+def test_reciprocal_division_is_ieee_bit_for_bit(ctx, seed):
+    """The passes divide by spacings and the time step through correctly
+    rounded reciprocals and one FMA correction; over 2^26 hashed operand
+    pairs (the passes' operand ranges, plus fully random bit patterns) the
+    quotient equals the IEEE division's in every bit."""
+    assert xf.selftest_division(ctx, 1 << 26, seed) == 0

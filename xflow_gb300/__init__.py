@@ -294,6 +294,13 @@ CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "s
               "cheb_middle_f32")
 
 
+def selftest_division(ctx, n=1 << 24, seed=1):
+    """Pairs (of n) where the time-step passes' reciprocal-based division differs from the IEEE one."""
+    m = C.c_longlong()
+    _check(ctx.h, capi.lib().xf_selftest_division(ctx.h, int(n), int(seed), C.byref(m)))
+    return m.value
+
+
 def profile_cg_kernels(op, reps=20):
     """Average ms per launch of each CG-iteration kernel, timed alone
     (pq_fused_f32 is absent where the grid does not take the fused path)."""

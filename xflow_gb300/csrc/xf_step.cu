@@ -37,10 +37,58 @@ __device__ __forceinline__ void report(DevScratch* S, int kind, long long cell) 
   atomicMin(&S->iscalars[CHK0 + kind], cell);
 }
 
+// a / b correctly rounded, from y = RN(1/b) (the grid's reciprocal tables,
+// or 1/tau from the host).  q = RN(a y) lies within an ulp of a / b, the
+// residual r = a - b q is exact (one FMA), and RN(q + r y) = RN(a / b):
+// Markstein's theorem for FMA-based division (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; also Muller et al., Handbook of Floating-Point
+// Arithmetic, ch. 5).  Three FP64 operations instead of the IEEE division's
+// reciprocal iteration, which matters at GB300's FP64 rate (1/58 of FP32).
+// The theorem needs a normal, unclamped residual: a numerator or quotient
+// outside [2^-950, 2^1000) in magnitude (zero, tiny, huge, not finite, or a
+// divisor of 0 or infinity) takes the IEEE division itself.  Checked bit for
+// bit against the IEEE division by xf_selftest_division.
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  const double q = a * y;
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu, eq = ((unsigned)__double2hiint(q) >> 20) & 0x7ffu;
+  if (ea - (1023u - 950u) >= 1950u || eq - (1023u - 950u) >= 1950u) return a / b;
+  const double r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
+// (i, j, k) of flat cell c in a box with strides s1 = b2 b3, s2 = b3: 32-bit
+// divisions for boxes below 2^32 cells, 64-bit ones (a software routine of
+// about a hundred instructions each) above.
+template <bool SMALL>
+__device__ __forceinline__ void split3(int64_t c, int64_t s1, int64_t s2, int& i, int& j, int& k) {
+  if (SMALL) {
+    const unsigned cc = (unsigned)c, t1 = (unsigned)s1, t2 = (unsigned)s2;
+    const unsigned ii = cc / t1, r = cc - ii * t1, jj = r / t2;
+    i = (int)ii;
+    j = (int)jj;
+    k = (int)(r - jj * t2);
+  } else {
+    i = (int)(c / s1);
+    j = (int)((c - i * s1) / s2);
+    k = (int)(c - i * s1 - j * s2);
+  }
+}
+
+// Launch of a kernel templated on SMALL (box below 2^32 cells).
+#define XF_LAUNCH_BOX(kern, ncell, grid, block, ...)                                      \
+  do {                                                                                    \
+    if ((ncell) < (1ll << 32)) kern<true><<<(grid), (block), 0, ctx->stream>>>(__VA_ARGS__); \
+    else kern<false><<<(grid), (block), 0, ctx->stream>>>(__VA_ARGS__);                    \
+  } while (0)
+
+template <bool SMALL>
 __global__ void k_pressure_rhs(const uint8_t* __restrict__ code, int n1, int n2, int n3, const double* __restrict__ u,
                                const double* __restrict__ v, const double* __restrict__ w,
                                const double* __restrict__ hxU, const double* __restrict__ hyV,
-                               const double* __restrict__ hzW, const double* __restrict__ rho, double tau,
+                               const double* __restrict__ hzW, const double* __restrict__ rhxU,
+                               const double* __restrict__ rhyV, const double* __restrict__ rhzW,
+                               const double* __restrict__ rho, double tau, double rtau,
                                const double* __restrict__ border, double* __restrict__ rhs, DevScratch* S) {
   const int64_t n = (int64_t)n1 * n2 * n3;
   const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
@@ -50,7 +98,8 @@ __global__ void k_pressure_rhs(const uint8_t* __restrict__ code, int n1, int n2,
     if (m == PC_FICTIVE) {
       rhs[c] = 0;
     } else if (m == PC_ACTUAL) {
-      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
       if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
         report(S, E_RANGE, c);   // the reference would read outside the velocity boxes
         continue;
@@ -62,9 +111,9 @@ __global__ void k_pressure_rhs(const uint8_t* __restrict__ code, int n1, int n2,
       const double v_j_1 = v[cv - s2], v_j = v[cv];
       const double w_k_1 = w[cw - 1], w_k = w[cw];
       const double d = rho ? rho[c] : 1.0;
-      const double div_ = d * d * ((u_i - u_i_1) / hxU[i - 1]) + ((v_j - v_j_1) / hyV[j - 1]) +
-                          ((w_k - w_k_1) / hzW[k - 1]);
-      rhs[c] = -(div_ / tau);
+      const double div_ = d * d * div_rcp(u_i - u_i_1, hxU[i - 1], rhxU[i - 1]) +
+                          div_rcp(v_j - v_j_1, hyV[j - 1], rhyV[j - 1]) + div_rcp(w_k - w_k_1, hzW[k - 1], rhzW[k - 1]);
+      rhs[c] = -div_rcp(div_, tau, rtau);
     } else if (m == PC_PREDEFINED) {
       rhs[c] = border ? border[c] : 0.0;
     } else if (m == PC_PRENORMAL || m == PC_DEFINED || m == PC_NORMAL || m == PC_EQUATION || m == PC_PREEQUATION) {
@@ -78,10 +127,12 @@ __global__ void k_pressure_rhs(const uint8_t* __restrict__ code, int n1, int n2,
 // Velocity correction, pass 1 (every cell but PreDefined ones): axis 1..3;
 // the velocity box is b1 x b2 x b3, the pressure box has one more layer along
 // the axis.
+template <bool SMALL>
 __global__ void k_vel_pass1(int axis, const uint8_t* __restrict__ code, int b1, int b2, int b3,
                             const double* __restrict__ prev, double* __restrict__ cur, const double* __restrict__ p,
-                            const double* __restrict__ hP, const double* __restrict__ rho, double tau,
-                            const double* __restrict__ border, DevScratch* S) {
+                            const double* __restrict__ hP, const double* __restrict__ rhP,
+                            const double* __restrict__ rho, double tau, const double* __restrict__ border,
+                            DevScratch* S) {
   const int64_t n = (int64_t)b1 * b2 * b3;
   const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
   const int p2 = axis == 2 ? b2 + 1 : b2, p3 = axis == 3 ? b3 + 1 : b3;
@@ -93,10 +144,11 @@ __global__ void k_vel_pass1(int axis, const uint8_t* __restrict__ code, int b1, 
     if (m == PC_FICTIVE) {
       cur[c] = 0;
     } else if (m == PC_ACTUAL || m == PC_NORMAL || m == PC_EQUATION) {
-      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
       const int64_t cp = i * ps1 + j * ps2 + k;
-      const double h = axis == 1 ? hP[i] : axis == 2 ? hP[j] : hP[k];
-      const double gradP = (p[cp + pstep] - p[cp]) / h;
+      const int ih = axis == 1 ? i : axis == 2 ? j : k;
+      const double gradP = div_rcp(p[cp + pstep] - p[cp], hP[ih], rhP[ih]);
       cur[c] = prev[c] - tau * gradP / (rho ? rho[cp] : 1.0);
     } else if (m == PC_DEFINED) {
       const double defVal = border ? border[c] : 0.0;
@@ -112,13 +164,15 @@ __global__ void k_vel_pass1(int axis, const uint8_t* __restrict__ code, int b1, 
 
 // Pass 2: PreDefined cells mirror their single Actual neighbour about the
 // border value.
+template <bool SMALL>
 __global__ void k_vel_pass2(const uint8_t* __restrict__ code, int b1, int b2, int b3, const double* __restrict__ prev,
                             double* __restrict__ cur, const double* __restrict__ border, DevScratch* S) {
   const int64_t n = (int64_t)b1 * b2 * b3;
   const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     if (code[c] != PC_PREDEFINED) continue;
-    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
     const double defVal = border ? border[c] : 0.0;
     int64_t nb = -1;
     int count = 0;
@@ -143,11 +197,15 @@ __global__ void k_vel_pass2(const uint8_t* __restrict__ code, int b1, int b2, in
 }
 
 // Control balance: first strict maximum of |div u| over Actual pressure cells.
+template <bool SMALL>
 __global__ void __launch_bounds__(RED_THREADS) k_div_max(const uint8_t* __restrict__ code, int n1, int n2, int n3,
                                                          const double* __restrict__ u, const double* __restrict__ v,
                                                          const double* __restrict__ w, const double* __restrict__ hxU,
                                                          const double* __restrict__ hyV,
-                                                         const double* __restrict__ hzW, DevScratch* S, int slot) {
+                                                         const double* __restrict__ hzW,
+                                                         const double* __restrict__ rhxU,
+                                                         const double* __restrict__ rhyV,
+                                                         const double* __restrict__ rhzW, DevScratch* S, int slot) {
   __shared__ AbsMax sh[32];
   __shared__ bool last;
   const int64_t n = (int64_t)n1 * n2 * n3;
@@ -158,14 +216,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_div_max(const uint8_t* __restri
   best.c = -1;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     if (code[c] != PC_ACTUAL) continue;
-    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
     if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
       report(S, E_RANGE, c);   // the reference would read outside the velocity boxes
       continue;
     }
     const int64_t cu = i * s1 + j * s2 + k, cv = i * sv1 + j * s2 + k, cw = i * sw1 + j * sw2 + k;
-    const double div = ((u[cu] - u[cu - s1]) / hxU[i - 1]) + ((v[cv] - v[cv - s2]) / hyV[j - 1]) +
-                       ((w[cw] - w[cw - 1]) / hzW[k - 1]);
+    const double div = div_rcp(u[cu] - u[cu - s1], hxU[i - 1], rhxU[i - 1]) +
+                       div_rcp(v[cv] - v[cv - s2], hyV[j - 1], rhyV[j - 1]) +
+                       div_rcp(w[cw] - w[cw - 1], hzW[k - 1], rhzW[k - 1]);
     const double a = fabs(div);
     if (a > best.v) { best.v = a; best.c = c; }   // NaN never wins, as in the reference
   }
@@ -207,10 +267,12 @@ struct MomArgs {
   const uint8_t* nflag;
   const double *u, *v, *w, *vis, *border, *force;
   const double *hx, *hy, *hz;
+  const double *rhhx, *rhhy, *rhhz;   // RN(2 / (h[i-1] + h[i])) per index
   double *uTr, *vTr, *wTr, *visTr, *rp;
   DevScratch* S;
 };
 
+template <bool SMALL>
 __global__ void k_mom_transfer(MomArgs a) {
   const int64_t n = (int64_t)a.b1 * a.b2 * a.b3;
   const int64_t s1 = (int64_t)a.b2 * a.b3, s2 = a.b3;
@@ -224,7 +286,8 @@ __global__ void k_mom_transfer(MomArgs a) {
     double ut = 0, vt = 0, wt = 0, vist = 0, r = 0;
     if (m == PC_FICTIVE) {
     } else if (m == PC_ACTUAL) {
-      const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+      int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
       if (i < 1 || i > a.b1 - 2 || j < 1 || j > a.b2 - 2 || k < 1 || k > a.b3 - 2) {
         report(a.S, E_RANGE, c);   // the reference would read outside the boxes
         continue;
@@ -268,6 +331,7 @@ __global__ void k_mom_transfer(MomArgs a) {
 }
 
 // Pass 3 (XProblem.cpp:5352-5419): rp += dVis . (dVel + dU) on Actual cells.
+template <bool SMALL>
 __global__ void k_mom_viscous(MomArgs a) {
   const int64_t n = (int64_t)a.b1 * a.b2 * a.b3;
   const int64_t s1 = (int64_t)a.b2 * a.b3, s2 = a.b3;
@@ -275,18 +339,22 @@ __global__ void k_mom_viscous(MomArgs a) {
   const double* velTr = a.axis == 1 ? a.uTr : a.axis == 2 ? a.vTr : a.wTr;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     if (a.code[c] != PC_ACTUAL) continue;
-    const int i = (int)(c / s1), j = (int)((c - i * s1) / s2), k = (int)(c - i * s1 - j * s2);
+    int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
     const double ddx = a.hx[i] + a.hx[i - 1], ddy = a.hy[j] + a.hy[j - 1], ddz = a.hz[k] + a.hz[k - 1];
-    const double dVisX = (a.visTr[c + s1] - a.visTr[c - s1]) / ddx;
-    const double dVisY = (a.visTr[c + s2] - a.visTr[c - s2]) / ddy;
-    const double dVisZ = (a.visTr[c + 1] - a.visTr[c - 1]) / ddz;
+    // RN(1/(h[i-1] + h[i])) = RN(1/hh) / 2 exactly, hh = (h[i-1] + h[i]) / 2
+    const double rdx = 0.5 * a.rhhx[i], rdy = 0.5 * a.rhhy[j], rdz = 0.5 * a.rhhz[k];
+    const double dVisX = div_rcp(a.visTr[c + s1] - a.visTr[c - s1], ddx, rdx);
+    const double dVisY = div_rcp(a.visTr[c + s2] - a.visTr[c - s2], ddy, rdy);
+    const double dVisZ = div_rcp(a.visTr[c + 1] - a.visTr[c - 1], ddz, rdz);
     const double dd = a.axis == 1 ? ddx : a.axis == 2 ? ddy : ddz;
-    const double dU = (a.uTr[c + st] - a.uTr[c - st]) / dd;
-    const double dV = (a.vTr[c + st] - a.vTr[c - st]) / dd;
-    const double dW = (a.wTr[c + st] - a.wTr[c - st]) / dd;
-    const double dVelX = (velTr[c + s1] - velTr[c - s1]) / ddx;
-    const double dVelY = (velTr[c + s2] - velTr[c - s2]) / ddy;
-    const double dVelZ = (velTr[c + 1] - velTr[c - 1]) / ddz;
+    const double rd = a.axis == 1 ? rdx : a.axis == 2 ? rdy : rdz;
+    const double dU = div_rcp(a.uTr[c + st] - a.uTr[c - st], dd, rd);
+    const double dV = div_rcp(a.vTr[c + st] - a.vTr[c - st], dd, rd);
+    const double dW = div_rcp(a.wTr[c + st] - a.wTr[c - st], dd, rd);
+    const double dVelX = div_rcp(velTr[c + s1] - velTr[c - s1], ddx, rdx);
+    const double dVelY = div_rcp(velTr[c + s2] - velTr[c - s2], ddy, rdy);
+    const double dVelZ = div_rcp(velTr[c + 1] - velTr[c - 1], ddz, rdz);
     a.rp[c] = a.rp[c] + (dVisX * (dVelX + dU) + dVisY * (dVelY + dV) + dVisZ * (dVelZ + dW));
   }
 }
@@ -373,10 +441,11 @@ extern "C" int xf_pressure_rhs(const xf_grid* gp, const xf_vec* u, const xf_vec*
   if (!(tau != 0)) return xf_fail(ctx, XF_ERR_ARG, "xf_pressure_rhs: tau must be nonzero");
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   if ((st = clear_checks(ctx))) return st;
-  k_pressure_rhs<<<grid_blocks(ctx, gp->ncell, 256), 256, 0, ctx->stream>>>(
+  XF_LAUNCH_BOX(k_pressure_rhs, gp->ncell, grid_blocks(ctx, gp->ncell, 256), 256,
       gp->code, gp->n1, gp->n2, gp->n3, (const double*)u->data, (const double*)v->data, (const double*)w->data,
-      u->g->hx, v->g->hy, w->g->hz, density ? (const double*)density->data : nullptr, tau,
-      border ? (const double*)border->data : nullptr, (double*)rhs->data, ctx->scratch);
+      u->g->hx, v->g->hy, w->g->hz, u->g->rhx, v->g->rhy, w->g->rhz,
+      density ? (const double*)density->data : nullptr, tau, 1.0 / tau, border ? (const double*)border->data : nullptr,
+      (double*)rhs->data, ctx->scratch);
   long long chk[E_COUNT], cell;
   if ((st = read_checks(ctx, chk))) return st;
   const int kinds[] = {E_RANGE, E_NOTIMPL_P, E_UNKNOWN};
@@ -403,12 +472,13 @@ extern "C" int xf_velocity_correct(int axis, const xf_vec* vel_prev, const xf_ve
   int st;
   if ((st = clear_checks(ctx))) return st;
   const double* hP = axis == 1 ? gp->hx : axis == 2 ? gp->hy : gp->hz;
+  const double* rhP = axis == 1 ? gp->rhx : axis == 2 ? gp->rhy : gp->rhz;
   const int bl = grid_blocks(ctx, gv->ncell, 256);
   const double* bd = border ? (const double*)border->data : nullptr;
-  k_vel_pass1<<<bl, 256, 0, ctx->stream>>>(axis, gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
-                                           (double*)vel->data, (const double*)p->data, hP,
+  XF_LAUNCH_BOX(k_vel_pass1, gv->ncell, bl, 256, axis, gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
+                                           (double*)vel->data, (const double*)p->data, hP, rhP,
                                            density ? (const double*)density->data : nullptr, tau, bd, ctx->scratch);
-  k_vel_pass2<<<bl, 256, 0, ctx->stream>>>(gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
+  XF_LAUNCH_BOX(k_vel_pass2, gv->ncell, bl, 256, gv->code, gv->n1, gv->n2, gv->n3, (const double*)vel_prev->data,
                                            (double*)vel->data, bd, ctx->scratch);
   long long chk[E_COUNT], cell;
   if ((st = read_checks(ctx, chk))) return st;
@@ -429,9 +499,9 @@ extern "C" int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_ve
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   if ((st = clear_checks(ctx))) return st;
   const int bl = red_blocks(ctx, gp->ncell);
-  k_div_max<<<bl, RED_THREADS, 0, ctx->stream>>>(gp->code, gp->n1, gp->n2, gp->n3, (const double*)u->data,
+  XF_LAUNCH_BOX(k_div_max, gp->ncell, bl, RED_THREADS, gp->code, gp->n1, gp->n2, gp->n3, (const double*)u->data,
                                                  (const double*)v->data, (const double*)w->data, u->g->hx, v->g->hy,
-                                                 w->g->hz, ctx->scratch, SL_STEP);
+                                                 w->g->hz, u->g->rhx, v->g->rhy, w->g->rhz, ctx->scratch, SL_STEP);
   XF_CUDA(ctx, cudaGetLastError());
   XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->scalars[SL_STEP], 2 * sizeof(double),
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -497,17 +567,66 @@ extern "C" int xf_momentum_rhs(int axis, const xf_vec* u_prev, const xf_vec* v_p
   a.border = border ? (const double*)border->data : nullptr;
   a.force = force ? (const double*)force->data : nullptr;
   a.hx = gc->hx; a.hy = gc->hy; a.hz = gc->hz;
+  a.rhhx = gc->rhhx; a.rhhy = gc->rhhy; a.rhhz = gc->rhhz;
   a.uTr = (double*)u_tr->data; a.vTr = (double*)v_tr->data; a.wTr = (double*)w_tr->data;
   a.visTr = (double*)vis_tr->data; a.rp = (double*)rp->data;
   a.S = ctx->scratch;
   const int bl = grid_blocks(ctx, gc->ncell, 256);
-  k_mom_transfer<<<bl, 256, 0, ctx->stream>>>(a);
+  XF_LAUNCH_BOX(k_mom_transfer, gc->ncell, bl, 256, a);
   long long chk[E_COUNT], cell;
   if ((st = read_checks(ctx, chk))) return st;
   const int kinds[] = {E_RANGE, E_NOTIMPL_V, E_NOTIMPL_EQ, E_UNKNOWN};
   const int bad = first_error(chk, kinds, 4, &cell);
   if (bad >= 0) return fail_at(ctx, gc, bad, cell, "xf_momentum_rhs");
-  k_mom_viscous<<<bl, 256, 0, ctx->stream>>>(a);
+  XF_LAUNCH_BOX(k_mom_viscous, gc->ncell, bl, 256, a);
   XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of div_rcp against the IEEE division, bit for bit, over n hashed
+// operand pairs (splitmix64 of seed and index): three quarters with the
+// numerator's exponent within 2^+-60 and the divisor's within [2^-40, 2^10]
+// (field differences over spacings and time steps), the rest with fully
+// random bit patterns (zeros, subnormals, infinities and NaNs included).
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_div_selftest(long long n, unsigned long long seed, unsigned long long* mismatches) {
+  unsigned long long bad = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    unsigned long long ha = splitmix64(seed ^ (2ull * (unsigned long long)c)), hb = splitmix64(seed ^ (2ull * (unsigned long long)c + 1));
+    if ((ha & 3ull) != 0) {   // exponents in the ranges of the step kernels' operands
+      const unsigned long long ea = 1023ull - 60ull + ((ha >> 2) % 121ull), eb = 1023ull - 40ull + ((hb >> 2) % 51ull);
+      ha = (ha & 0x800fffffffffffffull) | (ea << 52);
+      hb = (hb & 0x800fffffffffffffull) | (eb << 52);
+    }
+    const double a = __longlong_as_double((long long)ha), b = __longlong_as_double((long long)hb);
+    const double y = 1.0 / b;
+    const double got = div_rcp(a, b, y), want = a / b;
+    const bool same = __double_as_longlong(got) == __double_as_longlong(want) || (isnan(got) && isnan(want));
+    if (!same) bad++;
+  }
+  if (bad) atomicAdd(mismatches, bad);
+}
+
+extern "C" int xf_selftest_division(xf_ctx* ctx, long long n, unsigned long long seed, long long* mismatches) {
+  if (!ctx || !mismatches || n < 0) return XF_ERR_ARG;
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  unsigned long long* d = nullptr;
+  XF_CUDA(ctx, cudaMallocAsync(&d, sizeof(unsigned long long), ctx->stream));
+  XF_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+  k_div_selftest<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(n, seed, d);
+  unsigned long long h = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFreeAsync(d, ctx->stream);
+  if (e != cudaSuccess) return xf_fail(ctx, XF_ERR_CUDA, "xf_selftest_division: %s", cudaGetErrorString(e));
+  *mismatches = (long long)h;
   return XF_OK;
 }
