@@ -243,7 +243,9 @@ void xf_solve_opts_default(xf_solve_opts* o);
  * result on exit.  x and b are FP64 vectors of op's grid. */
 int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, xf_solve_stats* stats);
 /* The same with host boxes (upload b and x, solve, download x): the call a
- * host-resident caller such as the reference's time loop makes. */
+ * host-resident caller such as the reference's time loop makes.  The
+ * operator keeps the two device boxes between calls (released by
+ * xf_op_destroy), so calls on one operator must not overlap. */
 int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                   xf_solve_stats* stats);
 

@@ -98,6 +98,9 @@ struct xf_op {
   int adD_set = 0;
   double ad_tau = 1, ad_D = 0;
   int ad_flags = 0, adv_set = 0;
+  // device staging boxes of xf_solve_host, kept between calls
+  xf_vec* host_x = nullptr;
+  xf_vec* host_b = nullptr;
 };
 
 // ---------------------------------------------------------------------------

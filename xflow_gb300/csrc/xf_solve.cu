@@ -988,14 +988,19 @@ extern "C" int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const x
 extern "C" int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                              xf_solve_stats* stats) {
   if (!op || !host_x || !host_b) return XF_ERR_ARG;
-  xf_vec *x = nullptr, *b = nullptr;
-  int st = xf_vec_create(op->g, XF_F64, &x);
-  if (st) return st;
-  st = xf_vec_create(op->g, XF_F64, &b);
-  if (st) { xf_vec_destroy(x); return st; }
-  if (!(st = xf_vec_upload(x, host_x)) && !(st = xf_vec_upload(b, host_b)) && !(st = xf_solve(op, opts, x, b, stats)))
-    st = xf_vec_download(x, host_x);
-  xf_vec_destroy(x);
-  xf_vec_destroy(b);
-  return st;
+  xf_ctx* ctx = op->g->ctx;
+  // The device boxes of x and b stay with the operator between calls (no
+  // allocation, zero fill or free per solve); the copies and the solve are
+  // queued on the context stream with one synchronisation at the end.
+  int st;
+  if (!op->host_x && (st = xf_vec_create(op->g, XF_F64, &op->host_x))) return st;
+  if (!op->host_b && (st = xf_vec_create(op->g, XF_F64, &op->host_b))) return st;
+  const size_t bytes = (size_t)op->g->ncell * sizeof(double);
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  XF_CUDA(ctx, cudaMemcpyAsync(op->host_x->data, host_x, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  XF_CUDA(ctx, cudaMemcpyAsync(op->host_b->data, host_b, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if ((st = xf_solve(op, opts, op->host_x, op->host_b, stats))) return st;
+  XF_CUDA(ctx, cudaMemcpyAsync(host_x, op->host_x->data, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return XF_OK;
 }

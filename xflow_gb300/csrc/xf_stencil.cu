@@ -262,6 +262,8 @@ extern "C" int xf_op_destroy(xf_op* op) {
   if (op->adD64) cudaFree(op->adD64);
   if (op->adD32) cudaFree(op->adD32);
   if (op->pack) xf_pack_free(op->pack);
+  if (op->host_x) xf_vec_destroy(op->host_x);
+  if (op->host_b) xf_vec_destroy(op->host_b);
   delete op;
   return XF_OK;
 }
