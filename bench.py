@@ -220,6 +220,9 @@ def main():
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
+    ap.add_argument("--unet-applies", type=int, default=0,
+                    help="apply a random-initialised U-Net this many times to the bench's right-hand side (a bounded "
+                         "command for per-layer launch lists)")
     ap.add_argument("--degrees", default="",
                     help="degree:ratio pairs (e.g. 4:120,8:250): one JSON line per preconditioner, best of 3 solves")
     ap.add_argument("--kernels-only", action="store_true",
@@ -231,6 +234,8 @@ def main():
         return kernels_only(args)
     if args.degrees:
         return degrees(args)
+    if args.unet_applies > 0:
+        return unet_applies(args)
     if args.rows:
         return rows(args)
     if args.learned:
@@ -410,6 +415,33 @@ def main():
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def unet_applies(args):
+    """K applications of a random-initialised U-Net (the learned
+    preconditioner's network; weights do not change its time) to the bench's
+    right-hand side: device ms per application."""
+    import torch
+
+    import xflow_gb300 as xf
+
+    codes, sep, b = workload(args.size)
+    ctx = xf.Context(0)
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    net = xf.UNet(g, seed=1)
+    bv, z = g.vec(b), g.vec(None)
+    net.apply(bv, z)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.unet_applies):
+        net.apply(bv, z)
+    e1.record(stream)
+    e1.synchronize()
+    print(json.dumps({"mode": "U-Net applications", "workload": workload_name(args.size),
+                      "applications": args.unet_applies, "ms_per_application": e0.elapsed_time(e1) / args.unet_applies}))
     return 0
 
 
