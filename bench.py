@@ -223,6 +223,8 @@ def main():
     ap.add_argument("--unet-applies", type=int, default=0,
                     help="apply a random-initialised U-Net this many times to the bench's right-hand side (a bounded "
                          "command for per-layer launch lists)")
+    ap.add_argument("--probes", action="store_true",
+                    help="tcgen05.mma issue rate versus N and the FP64 / FP32 FMA rates (one JSON line each)")
     ap.add_argument("--degrees", default="",
                     help="degree:ratio pairs (e.g. 4:120,8:250): one JSON line per preconditioner, best of 3 solves")
     ap.add_argument("--kernels-only", action="store_true",
@@ -236,6 +238,8 @@ def main():
         return degrees(args)
     if args.unet_applies > 0:
         return unet_applies(args)
+    if args.probes:
+        return probes(args)
     if args.rows:
         return rows(args)
     if args.learned:
@@ -415,6 +419,32 @@ def main():
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def probes(args):
+    """The measurements behind two design decisions: cycles per tcgen05.mma
+    versus N (1, 2, 4 CTAs per SM; both operand layouts) and the FP64 / FP32
+    FMA rates."""
+    import torch
+
+    import xflow_gb300 as xf
+
+    ctx = xf.Context(0)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for layout in (0, 1):
+        for n in (16, 32, 64, 128, 256):
+            for cps in (1, 2, 4):
+                if (32 if n <= 32 else n) * cps > 512:
+                    continue
+                cyc = xf.probe_mma_rate(ctx, n, cps, layout)
+                flop_clk = 2.0 * 128 * n * 16 / cyc
+                print(json.dumps({"probe": "tcgen05.mma kind::f16 M=128 K=16", "layout": layout, "n": n,
+                                  "ctas_per_sm": cps, "cycles_per_mma": cyc, "flop_per_clock_per_sm": flop_clk,
+                                  "tflops_at_2070mhz": flop_clk * 2.07e9 * sms / 1e12}), flush=True)
+    for fp64 in (1, 0):
+        print(json.dumps({"probe": "FMA chains", "dtype": "f64" if fp64 else "f32",
+                          "tflops": xf.probe_fma_rate(ctx, fp64)}), flush=True)
     return 0
 
 
