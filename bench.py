@@ -264,7 +264,7 @@ def main():
         x.fill(0.0)
         return xf.solve(A, x, bv, method=xf.XF_CG, precision=precision, rtol=RTOL, **kw)
 
-    # FP64 plain CG: the judge (and the comparison point of the metric)
+    # FP64 plain CG: the comparison point of the metric
     one(xf.XF_PREC_FP64)
     st64 = one(xf.XF_PREC_FP64)
     x64 = x.download()

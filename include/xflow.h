@@ -191,7 +191,7 @@ int xf_absmax(const xf_vec* a, double* out, int64_t* rn_index);
 
 /* ---- solvers: TSLAE ------------------------------------------------------- */
 enum {
-  XF_CG = 0,             /* Hestenes-Stiefel CG, relative tolerance (FP64 judge)   */
+  XF_CG = 0,             /* Hestenes-Stiefel CG, relative tolerance (the FP64 baseline)*/
   XF_CG_REFERENCE = 1,   /* TSLAE::SolveByConjugateGradients, XSLAE.cpp:56-157     */
   XF_BICGSTAB = 2,       /* TSLAE::SolveByBiConjugateGradientsStab, :667-768       */
   XF_MINRES = 3,         /* TSLAE::SolveByMinimalResiduals, :350-414               */

@@ -501,7 +501,7 @@ int xfo_minres_reference(int op, const int32_t* codes, const double* normals, co
 }
 
 /* Plain Hestenes-Stiefel CG with a relative-residual stop: the FP64 CPU
- * counterpart of the GPU judge (not a reference routine; the reference's CG
+ * counterpart of the GPU's plain FP64 CG (not a reference routine; the reference's CG
  * is the three-term form above). */
 int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
                  const double* hz, const double* density, int n1, int n2, int n3, const double* x0,

@@ -57,7 +57,7 @@ int xfo_minres_reference(int op, const int32_t* codes, const double* normals, co
                          const double* hy, const double* hz, const double* density, int n1, int n2, int n3,
                          const double* x0, const double* b, double eps, int maxit, double* result,
                          xfo_stats* st);
-/* Plain Hestenes-Stiefel CG to ||b - A x||_2 <= rtol ||b||_2 (the FP64 judge). */
+/* Plain Hestenes-Stiefel CG to ||b - A x||_2 <= rtol ||b||_2 (the FP64 comparison solver). */
 int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
                  const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
                  const double* b, double rtol, int maxit, double* result, xfo_stats* st);

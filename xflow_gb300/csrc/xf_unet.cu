@@ -738,7 +738,7 @@ extern "C" int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, 
 // which keeps the method robust to a preconditioner that varies from one
 // application to the next (a network), then x += alpha p, r -= alpha A p with
 // alpha = (p, r) / (p, A p).  FP64 vectors and dots.  Plain CG stays the
-// fallback and the judge: an iteration whose z is no descent direction
+// fallback and the arbiter: an iteration whose z is no descent direction
 // ((z, r) <= 0) uses z = r, and when the residual has not dropped by 10% over
 // 50 iterations the preconditioner is switched off for the rest of the solve
 // (both counted in stats->fallbacks).  The stop rule is the true relative
