@@ -209,6 +209,13 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
  * over memory; degree 2 m is the product of m real quadratic factors, one
  * pass each. */
 enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3 };
+/* Host only (no device work): the XF_PRECOND_CHEB polynomial as the solver
+ * builds it, in powers of A.  degree 2 writes its three Horner coefficients
+ * (a0, a1, a2: z = a0 r + A (a1 r + a2 A r)); degree 2m (4 to 12) writes m
+ * real quadratic factors (1, b1, b2), p = p_1 ... p_m, 3m floats.  Every
+ * form is scaled so that p(0) = 1.  XF_ERR_ARG when the roots do not pair
+ * into real factors that reproduce p. */
+int xf_cheb_factors_host(double lmax, double ratio, int degree, float* factors);
 
 typedef struct {
   int method;            /* XF_CG ...                                              */

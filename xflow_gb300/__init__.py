@@ -301,6 +301,17 @@ def selftest_division(ctx, n=1 << 24, seed=1):
     return m.value
 
 
+def cheb_factors(lmax, ratio, degree):
+    """The polynomial preconditioner's factors as the solver builds them (host only): degree 2 gives one row
+    (a0, a1, a2) of Horner coefficients, degree 2m gives m rows (1, b1, b2) of quadratic factors."""
+    m = 1 if degree == 2 else degree // 2
+    out = (C.c_float * (3 * m))()
+    st = capi.lib().xf_cheb_factors_host(float(lmax), float(ratio), int(degree), out)
+    if st != capi.XF_OK:
+        raise XFError(st, f"no real quadratic factors for degree {degree}, ratio {ratio}")
+    return np.array(list(out), dtype=np.float64).reshape(m, 3)
+
+
 def probe_mma_rate(ctx, n, ctas_per_sm=2, layout=0):
     """Clock cycles per tcgen05.mma of width n issued back to back (operands resident in shared memory)."""
     c = C.c_double()

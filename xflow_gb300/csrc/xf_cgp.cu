@@ -609,6 +609,22 @@ bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]) {
   return true;
 }
 
+// C ABI: the preconditioner's factors as the solver builds them.  degree 2:
+// the Horner coefficients (one factor); 4 to 12: the quadratic factors in the
+// order p_1 ... p_m (the solver applies p_m first).
+extern "C" int xf_cheb_factors_host(double lmax, double ratio, int degree, float* factors) {
+  if (!factors || !(lmax > 0) || !(ratio > 1) || degree < 2 || degree > 12 || degree % 2) return XF_ERR_ARG;
+  if (degree == 2) {
+    xf_cheb2_coeffs(lmax, ratio, factors);
+    return XF_OK;
+  }
+  float f[6][3];
+  if (!xf_cheb_factors(lmax, ratio, degree, f)) return XF_ERR_ARG;
+  for (int k = 0; k < degree / 2; k++)
+    for (int j = 0; j < 3; j++) factors[3 * k + j] = f[k][j];
+  return XF_OK;
+}
+
 bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]) {
   float f[2][3];
   if (!xf_cheb_factors(lmax, ratio, 4, f)) return false;
