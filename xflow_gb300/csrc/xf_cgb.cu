@@ -309,11 +309,12 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
   int ns = 2;
   if (const char* env = getenv("XF_PQB_NS")) ns = env[0] == '1' ? 1 : (env[0] == '4' && pqb_smem(a.RL, 4) <= 112 * 1024) ? 4 : 2;
   const size_t smem = pqb_smem(a.RL, ns);
-  static size_t attr_smem[5] = {0, 0, 0, 0, 0};
-  if (attr_smem[ns] < smem) {
+  static size_t attr_smem[5][64] = {};   // per ring depth and device
+  size_t& at = attr_smem[ns][ctx->device & 63];
+  if (at < smem) {
     cudaFuncSetAttribute(ns == 1 ? k_cg_pqb<1> : ns == 4 ? k_cg_pqb<4> : k_cg_pqb<2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_smem[ns] = smem;
+    at = smem;
   }
   // resident blocks per SM from shared memory (1 KB reserved per block) and the launch bounds
   int resident = (int)((228 * 1024) / (smem + 1024 + 1024));

@@ -659,10 +659,11 @@ void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
   a.a0 = coeffs[0]; a.a1 = coeffs[1]; a.a2 = coeffs[2];
   const size_t smem = cp_smem(a.R0, a.R1, FUSE);
-  static size_t attr = 0;
-  if (attr < smem) {
+  static size_t attr[64] = {};   // per device: the attribute belongs to the device's copy of the kernel
+  size_t& at = attr[ctx->device & 63];
+  if (at < smem) {
     cudaFuncSetAttribute(k_cg_poly2<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = smem;
+    at = smem;
   }
   int resident = (int)((228 * 1024) / (smem + 2048));
   if (resident > 2) resident = 2;
