@@ -182,9 +182,9 @@ __global__ void __launch_bounds__(PQB_THREADS, PQB_NS == 1 ? 4 : PQB_NS == 2 ? 3
           const float4 gb = fma4(beta, lds4(Q + sb), lds4(R + sb));
           *reinterpret_cast<float4*>(pj + sa) = ga;
           *reinterpret_cast<float4*>(pj + sb) = gb;
-          for (int h = threadIdx.x; h < 2 * HA; h += PQB_THREADS) {
-            const int t = h < HA ? h : h + PQB_TILE;
-            pj[t] = fmaf(beta, Q[t], R[t]);
+          for (int h = threadIdx.x; h < HA / 2; h += PQB_THREADS) {   // halo groups (HA % 4 == 0), either side
+            const int t = 4 * (h < HA / 4 ? h : h + PQB_TILE / 4);
+            *reinterpret_cast<float4*>(pj + t) = fma4(beta, lds4(Q + t), lds4(R + t));
           }
           if (j >= i0 && j < i1) {   // p' of the chunk's own cells, written once
             const int64_t pl = (int64_t)j * P;
