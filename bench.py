@@ -622,6 +622,14 @@ def rows(args):
             report("a18 IB forces (XProblem.cpp:8436-8547)", name + f", {nn} markers", ms)
             ms = timed(lambda: mk.spread(un, h0, 1))
             report("a19 IB spread (XProblem.cpp:8550-8617)", name + f", {nn} markers", ms)
+            # the same icosphere as a closed surface voxelised into the pressure box, its points spread
+            # over the channel [0, 4] x [0, 1] x [0, 1]
+            vs, fs = wl.icosphere_mesh(4)
+            vs = vs * 0.15 + np.array([1.0, 0.5, 0.5])
+            pts = [np.linspace(0.0, L, n_) for L, n_ in ((4.0, n1), (1.0, n2), (1.0, n3))]
+            ms = timed(lambda: xf.voxelize_mesh(ctx, cs["pc"], *pts, vs, fs, 0), reps=5)
+            report("voxelise a closed surface (planned boundary; host box in and out)",
+                   name + f", {len(fs)} triangles", ms)
         if n1 == 257:
             # VTK volume of the step (node box one smaller than the pressure box)
             node_codes = np.ascontiguousarray(cs["pc"][:-1, :-1, :-1])

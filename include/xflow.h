@@ -256,6 +256,20 @@ int xf_solve(xf_op* op, const xf_solve_opts* opts, xf_vec* x, const xf_vec* b, x
 int xf_solve_host(xf_op* op, const xf_solve_opts* opts, double* host_x, const double* host_b,
                   xf_solve_stats* stats);
 
+/* ---- voxelisation ----------------------------------------------------------- */
+/* Sets codes[(i n2 + j) n3 + k] = inside_code for every point (x_nodes[i],
+ * y_nodes[j], z_nodes[k]) inside the closed triangle surface (vertices: 3
+ * doubles each; faces: 3 vertex indices each), leaving the other codes as
+ * they are.  The planned boundary's voxeliser for the immersed-body
+ * configuration; no counterpart in the reference, which uses the STL
+ * vertices only as markers (XImmersedBoundary.cpp:1560-1570).  Parity of
+ * crossings along x with the rasterisation top-left rule on shared edges.
+ * XF_ERR_ARG for a face naming a vertex out of range or a ray crossing the
+ * surface more than 128 times.  codes is a host box. */
+int xf_voxelize_mesh(xf_ctx* ctx, int n1, int n2, int n3, const double* x_nodes, const double* y_nodes,
+                     const double* z_nodes, const double* vertices, long long nvert, const int32_t* faces,
+                     long long nface, int32_t inside_code, int32_t* codes);
+
 /* ---- time-step passes around the pressure solve --------------------------- */
 /* TVPProblem::SolveBySplitting (XProblem.cpp:5474-5829).  Staggered boxes as
  * the reference's grids (XStatement.h:127-135): for a pressure grid gp of

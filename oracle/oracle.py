@@ -333,3 +333,69 @@ def format_fixed6(values):
     buf = C.create_string_buffer(int(n))
     lib().xfo_format_fixed6(_p(v, C.c_double), v.size, buf, n)
     return buf.raw[:n]
+
+
+def voxelize_mesh(codes, x_nodes, y_nodes, z_nodes, vertices, faces, inside_code):
+    """Checker of the library's voxeliser (no counterpart in the reference,
+    which uses STL vertices only as markers, XImmersedBoundary.cpp:1560-1570;
+    parity unpinned by the reference).  The same rule, restated with numpy:
+    rays along x at (y[j], z[k]); a triangle is crossed where the ray's (y, z)
+    lies in its (y, z) projection, points on a projected edge counted by the
+    top-left rule of the counter-clockwise traversal; edge functions from the
+    endpoints in lexicographic order, negated for the other direction; a point
+    is inside when an odd number of crossing abscissae lie below its x.  Every
+    product and sum is rounded on its own, as on the device."""
+    out = np.array(codes, dtype=np.int32, copy=True)
+    x_nodes, y_nodes, z_nodes = (np.asarray(a, dtype=np.float64) for a in (x_nodes, y_nodes, z_nodes))
+    V = np.asarray(vertices, dtype=np.float64).reshape(-1, 3)
+    F = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+    A, B, C = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+
+    def edge_fn(a, b, pu, pv):
+        """a, b: (m, 2) endpoints (u = y, v = z); pu, pv: (r, 1) points -> (r, m)."""
+        fwd = (a[:, 0] < b[:, 0]) | ((a[:, 0] == b[:, 0]) & (a[:, 1] < b[:, 1]))
+        s = np.where(fwd[:, None], a, b)
+        t = np.where(fwd[:, None], b, a)
+        du, dv = t[:, 0] - s[:, 0], t[:, 1] - s[:, 1]
+        e = du * (pv - s[:, 1]) - dv * (pu - s[:, 0])
+        return np.where(fwd, e, -e)
+
+    def top_left(a, b):
+        du, dv = b[:, 0] - a[:, 0], b[:, 1] - a[:, 1]
+        return (dv < 0.0) | ((dv == 0.0) & (du > 0.0))
+
+    a2, b2_, c2_ = A[:, 1:], B[:, 1:], C[:, 1:]
+    # area of each projected triangle: the edge function of a -> b at c
+    fwd = (a2[:, 0] < b2_[:, 0]) | ((a2[:, 0] == b2_[:, 0]) & (a2[:, 1] < b2_[:, 1]))
+    s = np.where(fwd[:, None], a2, b2_)
+    t = np.where(fwd[:, None], b2_, a2)
+    ar = (t[:, 0] - s[:, 0]) * (c2_[:, 1] - s[:, 1]) - (t[:, 1] - s[:, 1]) * (c2_[:, 0] - s[:, 0])
+    area = np.where(fwd, ar, -ar)
+    keep = area != 0.0
+    ccw = area > 0
+    bb = np.where(ccw[:, None], b2_, c2_)[keep]
+    cc = np.where(ccw[:, None], c2_, b2_)[keep]
+    aa = a2[keep]
+    xa = A[keep, 0]
+    xb = np.where(ccw, B[:, 0], C[:, 0])[keep]
+    xc = np.where(ccw, C[:, 0], B[:, 0])[keep]
+    tl0, tl1, tl2 = top_left(aa, bb), top_left(bb, cc), top_left(cc, aa)
+    n1, n2, n3 = out.shape
+    jj, kk = np.meshgrid(np.arange(n2), np.arange(n3), indexing="ij")
+    jj, kk = jj.ravel(), kk.ravel()
+    for r0 in range(0, jj.size, 256):
+        j, k = jj[r0:r0 + 256], kk[r0:r0 + 256]
+        pu, pv = y_nodes[j][:, None], z_nodes[k][:, None]
+        e0, e1, e2 = edge_fn(aa, bb, pu, pv), edge_fn(bb, cc, pu, pv), edge_fn(cc, aa, pu, pv)
+        inside = (((e0 > 0) | ((e0 == 0) & tl0)) & ((e1 > 0) | ((e1 == 0) & tl1)) &
+                  ((e2 > 0) | ((e2 == 0) & tl2)))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            x = ((e1 * xa + e2 * xb) + e0 * xc) / ((e1 + e2) + e0)
+        for q in range(j.size):
+            xs = np.sort(x[q][inside[q]])
+            if xs.size == 0:
+                continue
+            below = np.searchsorted(xs, x_nodes, side="left")   # crossings strictly below each x[i]
+            sel = (below & 1) == 1
+            out[sel, j[q], k[q]] = inside_code
+    return out

@@ -301,6 +301,20 @@ def selftest_division(ctx, n=1 << 24, seed=1):
     return m.value
 
 
+def voxelize_mesh(ctx, codes, x_nodes, y_nodes, z_nodes, vertices, faces, inside_code):
+    """A copy of the point-code box with every point inside the closed triangle surface set to inside_code."""
+    out = np.ascontiguousarray(codes, dtype=np.int32).copy()
+    n1, n2, n3 = out.shape
+    xs, ys, zs = (np.ascontiguousarray(a, dtype=np.float64) for a in (x_nodes, y_nodes, z_nodes))
+    assert xs.size == n1 and ys.size == n2 and zs.size == n3
+    v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+    _check(ctx.h, capi.lib().xf_voxelize_mesh(ctx.h, n1, n2, n3, capi._ptr(xs), capi._ptr(ys), capi._ptr(zs),
+                                              capi._ptr(v), v.shape[0], capi._ptr(f), f.shape[0], int(inside_code),
+                                              capi._ptr(out)))
+    return out
+
+
 def cheb_factors(lmax, ratio, degree):
     """The polynomial preconditioner's factors as the solver builds them (host only): degree 2 gives one row
     (a0, a1, a2) of Horner coefficients, degree 2m gives m rows (1, b1, b2) of quadratic factors."""

@@ -284,6 +284,12 @@ def icosphere(subdiv: int) -> np.ndarray:
     split in four `subdiv` times with midpoints pushed to the sphere
     (10 * 4**subdiv + 2 vertices: 2562 at subdivision 4, the immersed-body
     config's marker set)."""
+    return icosphere_mesh(subdiv)[0]
+
+
+def icosphere_mesh(subdiv: int):
+    """The closed icosphere surface: (vertices (V, 3), faces (F, 3) int32,
+    outward counter-clockwise), 20 * 4**subdiv faces."""
     t = (1.0 + 5 ** 0.5) / 2
     v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
          (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
@@ -307,4 +313,23 @@ def icosphere(subdiv: int) -> np.ndarray:
             ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
             nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
         faces = nf
-    return np.array(verts)
+    return np.array(verts), np.array(faces, dtype=np.int32)
+
+
+def read_stl(path):
+    """Triangles of an ASCII or binary STL file as (vertices (V, 3) float64,
+    faces (F, 3) int32), vertices merged where their coordinates are equal
+    (the reference reads its geometry through stl_reader.h the same way)."""
+    data = open(path, "rb").read()
+    tri = None
+    if len(data) >= 84:
+        nf = int(np.frombuffer(data[80:84], "<u4")[0])
+        if 84 + 50 * nf == len(data):   # binary: 50-byte records after an 80-byte header
+            rec = np.frombuffer(data[84:], dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]))
+            tri = rec["v"].astype(np.float64)
+    if tri is None:
+        pts = [list(map(float, line.split()[1:4])) for line in data.decode("ascii", "replace").splitlines()
+               if line.strip().startswith("vertex")]
+        tri = np.array(pts, dtype=np.float64).reshape(-1, 3, 3)
+    verts, inv = np.unique(tri.reshape(-1, 3), axis=0, return_inverse=True)
+    return verts, inv.reshape(-1, 3).astype(np.int32)
