@@ -4,7 +4,7 @@
 // reference has no voxeliser and uses the STL vertices only as immersed
 // boundary markers, XImmersedBoundary.cpp:1560-1570).
 //
-// One thread per ray along x at (y[j], z[k]).  A triangle is crossed when the
+// One warp per ray along x at (y[j], z[k]).  A triangle is crossed when the
 // ray's (y, z) lies in its projection onto the (y, z) plane.  Points on a
 // projected edge follow the top-left rule of rasterisation: with the
 // triangle's projection traversed counter-clockwise, an edge counts when it
@@ -45,50 +45,90 @@ __device__ __forceinline__ bool top_left(P2 a, P2 b) {
   return dv < 0.0 || (dv == 0.0 && du > 0.0);
 }
 
-__global__ void k_voxelize(int n1, int n2, int n3, const double* __restrict__ xn, const double* __restrict__ yn,
-                           const double* __restrict__ zn, const double* __restrict__ V, const int32_t* __restrict__ F,
-                           long long nf, int32_t inside_code, int32_t* __restrict__ codes, int* __restrict__ err) {
-  const long long ray = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (ray >= (long long)n2 * n3) return;
+// Conservative (y, z) bounding box of each triangle in FP32, rounded outwards:
+// the ray test below rejects on it before the exact FP64 edge functions.
+__global__ void k_tri_boxes(const double* __restrict__ V, const int32_t* __restrict__ F, long long nf,
+                            float4* __restrict__ box) {
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
+    const int32_t ia = F[3 * f], ib = F[3 * f + 1], ic = F[3 * f + 2];
+    const double ya = V[3 * ia + 1], yb = V[3 * ib + 1], yc = V[3 * ic + 1];
+    const double za = V[3 * ia + 2], zb = V[3 * ib + 2], zc = V[3 * ic + 2];
+    box[f] = make_float4(__double2float_rd(fmin(ya, fmin(yb, yc))), __double2float_ru(fmax(ya, fmax(yb, yc))),
+                         __double2float_rd(fmin(za, fmin(zb, zc))), __double2float_ru(fmax(za, fmax(zb, zc))));
+  }
+}
+
+// One warp per ray: the lanes take the triangles in turn, the hits are
+// compacted into the warp's list by ballot, lane 0 sorts it, and the lanes
+// share the sweep along x.
+constexpr int VX_WARPS = 4;
+__global__ void __launch_bounds__(32 * VX_WARPS) k_voxelize(int n1, int n2, int n3, const double* __restrict__ xn,
+                                                           const double* __restrict__ yn, const double* __restrict__ zn,
+                                                           const double* __restrict__ V, const int32_t* __restrict__ F,
+                                                           const float4* __restrict__ box, long long nf,
+                                                           int32_t inside_code, int32_t* __restrict__ codes,
+                                                           int* __restrict__ err) {
+  __shared__ double xs_all[VX_WARPS][VX_MAXC];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long ray = blockIdx.x * (long long)VX_WARPS + warp;
+  if (ray >= (long long)n2 * n3) return;   // the whole warp
+  double* xs = xs_all[warp];
   const int j = (int)(ray / n3), k = (int)(ray - (long long)j * n3);
   const P2 p = {yn[j], zn[k]};
-  double xs[VX_MAXC];
+  const float pu_lo = __double2float_rd(p.u), pu_hi = __double2float_ru(p.u);
+  const float pv_lo = __double2float_rd(p.v), pv_hi = __double2float_ru(p.v);
   int nc = 0;
-  bool overflow = false;
-  for (long long f = 0; f < nf; f++) {
-    const int32_t ia = F[3 * f], ib = F[3 * f + 1], ic = F[3 * f + 2];
-    const P2 a = {V[3 * ia + 1], V[3 * ia + 2]}, b = {V[3 * ib + 1], V[3 * ib + 2]}, c = {V[3 * ic + 1], V[3 * ic + 2]};
-    const double area = edge_fn(a, b, c);
-    if (area == 0.0) continue;
-    // counter-clockwise traversal a -> b2 -> c2
-    const P2 b2 = area > 0 ? b : c, c2 = area > 0 ? c : b;
-    const double e0 = edge_fn(a, b2, p), e1 = edge_fn(b2, c2, p), e2 = edge_fn(c2, a, p);
-    const bool in = (e0 > 0.0 || (e0 == 0.0 && top_left(a, b2))) && (e1 > 0.0 || (e1 == 0.0 && top_left(b2, c2))) &&
-                    (e2 > 0.0 || (e2 == 0.0 && top_left(c2, a)));
-    if (!in) continue;
-    // barycentric x: weights e1 (opposite a), e2 (opposite b2), e0 (opposite c2)
-    const double xa = V[3 * ia], xb = area > 0 ? V[3 * ib] : V[3 * ic], xc = area > 0 ? V[3 * ic] : V[3 * ib];
-    const double num = __dadd_rn(__dadd_rn(__dmul_rn(e1, xa), __dmul_rn(e2, xb)), __dmul_rn(e0, xc));
-    const double x = __ddiv_rn(num, __dadd_rn(__dadd_rn(e1, e2), e0));
-    if (nc < VX_MAXC) xs[nc++] = x;
-    else overflow = true;
+  for (long long f0 = 0; f0 < nf; f0 += 32) {
+    const long long f = f0 + lane;
+    bool hit = false;
+    double x = 0.0;
+    if (f < nf) {
+      const float4 bx = box[f];
+      if (pu_hi >= bx.x && pu_lo <= bx.y && pv_hi >= bx.z && pv_lo <= bx.w) {
+        const int32_t ia = F[3 * f], ib = F[3 * f + 1], ic = F[3 * f + 2];
+        const P2 a = {V[3 * ia + 1], V[3 * ia + 2]}, b = {V[3 * ib + 1], V[3 * ib + 2]};
+        const P2 c = {V[3 * ic + 1], V[3 * ic + 2]};
+        const double area = edge_fn(a, b, c);
+        if (area != 0.0) {
+          // counter-clockwise traversal a -> b2 -> c2
+          const P2 b2 = area > 0 ? b : c, c2 = area > 0 ? c : b;
+          const double e0 = edge_fn(a, b2, p), e1 = edge_fn(b2, c2, p), e2 = edge_fn(c2, a, p);
+          hit = (e0 > 0.0 || (e0 == 0.0 && top_left(a, b2))) && (e1 > 0.0 || (e1 == 0.0 && top_left(b2, c2))) &&
+                (e2 > 0.0 || (e2 == 0.0 && top_left(c2, a)));
+          if (hit) {   // barycentric x: weights e1 (opposite a), e2 (opposite b2), e0 (opposite c2)
+            const double xa = V[3 * ia], xb = area > 0 ? V[3 * ib] : V[3 * ic], xc = area > 0 ? V[3 * ic] : V[3 * ib];
+            const double num = __dadd_rn(__dadd_rn(__dmul_rn(e1, xa), __dmul_rn(e2, xb)), __dmul_rn(e0, xc));
+            x = __ddiv_rn(num, __dadd_rn(__dadd_rn(e1, e2), e0));
+          }
+        }
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+      const int pos = nc + __popc(m & ((1u << lane) - 1u));
+      if (pos < VX_MAXC) xs[pos] = x;
+    }
+    nc += __popc(m);
   }
-  if (overflow) {
-    atomicExch(err, 1);
+  if (nc > VX_MAXC) {
+    if (lane == 0) atomicExch(err, 1);
     return;
   }
-  for (int a = 1; a < nc; a++) {   // insertion sort: a handful of crossings per ray
-    const double v = xs[a];
-    int b = a - 1;
-    while (b >= 0 && xs[b] > v) {
-      xs[b + 1] = xs[b];
-      b--;
+  __syncwarp();
+  if (lane == 0)
+    for (int q = 1; q < nc; q++) {   // insertion sort: a handful of crossings per ray
+      const double v = xs[q];
+      int r = q - 1;
+      while (r >= 0 && xs[r] > v) {
+        xs[r + 1] = xs[r];
+        r--;
+      }
+      xs[r + 1] = v;
     }
-    xs[b + 1] = v;
-  }
-  int c = 0;
-  for (int i = 0; i < n1; i++) {
+  __syncwarp();
+  for (int i = lane; i < n1; i += 32) {
     const double xi = xn[i];
+    int c = 0;
     while (c < nc && xs[c] < xi) c++;
     if (c & 1) codes[((long long)i * n2 + j) * n3 + k] = inside_code;
   }
@@ -119,9 +159,10 @@ extern "C" int xf_voxelize_mesh(xf_ctx* ctx, int n1, int n2, int n3, const doubl
   int32_t* df = (int32_t*)get((size_t)nface * 12);
   int32_t* dc = (int32_t*)get(nb * 4);
   int* derr = (int*)get(sizeof(int));
+  float4* dbox = (float4*)get((size_t)nface * sizeof(float4));
   int st = XF_OK, herr = 0;
   cudaError_t e = cudaSuccess;
-  if (!dx || !dy || !dz || !dv || !df || !dc || !derr) {
+  if (!dx || !dy || !dz || !dv || !df || !dc || !derr || !dbox) {
     st = xf_fail(ctx, XF_ERR_NOMEM, "xf_voxelize_mesh: device allocation");
   } else {
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x_nodes, n1 * 8, cudaMemcpyHostToDevice, ctx->stream);
@@ -131,10 +172,14 @@ extern "C" int xf_voxelize_mesh(xf_ctx* ctx, int n1, int n2, int n3, const doubl
     if (e == cudaSuccess && nface) e = cudaMemcpyAsync(df, faces, nface * 12, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dc, codes, nb * 4, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess && nface) {
+      k_tri_boxes<<<grid_blocks(ctx, nface, 256), 256, 0, ctx->stream>>>(dv, df, nface, dbox);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) {
       const long long rays = (long long)n2 * n3;
-      k_voxelize<<<(unsigned)((rays + 127) / 128), 128, 0, ctx->stream>>>(n1, n2, n3, dx, dy, dz, dv, df, nface,
-                                                                          inside_code, dc, derr);
+      k_voxelize<<<(unsigned)((rays + VX_WARPS - 1) / VX_WARPS), 32 * VX_WARPS, 0, ctx->stream>>>(
+          n1, n2, n3, dx, dy, dz, dv, df, dbox, nface, inside_code, dc, derr);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
