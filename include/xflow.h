@@ -505,9 +505,11 @@ int xf_probe_fma_rate(xf_ctx* ctx, int fp64, double* tflops);
 /* No counterpart in the reference (which has no device memory at all).
  * The masked FP64 dot of xf_dot, sum over c < n with d_mask[c] != 0 (d_mask
  * may be NULL: every element) of d_a[c]*d_b[c], written to *d_out, for
- * callers that cannot allocate device memory: code running during a CUDA
- * graph capture, in a host callback, or under a memory budget that forbids
- * allocation once a time loop is running.  All pointers are caller-owned
+ * callers that cannot allocate device memory: an application that carves all
+ * its device memory out of its own pool at start-up (a time loop under a
+ * fixed memory budget, or a GPU shared with a library that holds the rest),
+ * and loops that must not call cudaFree, which waits for the whole device to
+ * go idle.  All pointers are caller-owned
  * device memory; the call is asynchronous on `stream` (a cudaStream_t, NULL
  * for the legacy default stream) and allocates nothing: its scratch is a
  * 64 KiB file-scope device array that every device loading the library keeps

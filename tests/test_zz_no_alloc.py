@@ -1,5 +1,7 @@
 """xf_dot_noalloc, the inner product for callers that cannot allocate device
-memory (graph capture, host callbacks, a fixed memory budget): it must agree
+memory (an application pooling all of its device memory at start-up under a
+fixed budget, or a loop that must not call cudaFree and so wait for the whole
+device to go idle): it must agree
 with xf_dot, the allocating entry point, call after call, while keeping its
 scratch in a static device array.
 

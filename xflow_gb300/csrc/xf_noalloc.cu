@@ -1,7 +1,10 @@
 // xf_dot_noalloc: the masked FP64 inner product of xf_dot for callers that
-// cannot allocate device memory - code running while a CUDA graph is being
-// captured, inside a host callback, or under a memory budget that forbids new
-// allocations once a time loop has started.  It takes caller-owned device
+// cannot allocate device memory: a host application that carves all of its
+// device memory out of its own pool at start-up (a time loop run under a
+// fixed memory budget, or a GPU shared with another library that holds the
+// rest, where a new allocation fails part-way through a step), and loops
+// that must not call cudaFree, which waits for the whole device to go idle.
+// It takes caller-owned device
 // arrays and a caller-owned device result, and keeps its scratch (the
 // per-block partial sums and the last-block ticket) in a file-scope
 // __device__ array, so it calls no cudaMalloc, cudaFree or allocating library
