@@ -217,6 +217,10 @@ def main():
                     help="train the U-Net preconditioner and time it and its flexible CG at full size")
     ap.add_argument("--learned-applies-only", action="store_true", help="with --learned: no solves")
     ap.add_argument("--learned-max-its", type=int, default=0, help="with --learned: cap of the learned solve")
+    ap.add_argument("--two-level", action="store_true",
+                    help="time the learned two-level preconditioner (U-Net coarse solver + Chebyshev smoothing)")
+    ap.add_argument("--two-level-sweep", default="8:60:2,8:60:1,8:250:2,8:30:2,4:60:2,12:60:2",
+                    help="with --two-level: smoothing degree:ratio:FCG window triples")
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
@@ -240,6 +244,8 @@ def main():
         return unet_applies(args)
     if args.probes:
         return probes(args)
+    if args.two_level:
+        return two_level(args)
     if args.rows:
         return rows(args)
     if args.learned:
@@ -705,22 +711,14 @@ def unet_flops(shape):
     return ex, us
 
 
-def learned(args):
-    """The learned preconditioner at the bench's 256^3 system: a U-Net trained
-    on the GPU (this library's forward/backward kernels, Adam, the A-norm
-    loss) on (residual, error) pairs harvested from plain CG's own iterates on
-    a 64^3 system of the same sphere family, then applied by flexible CG
-    FCG(8) at full size.  Prints one JSON line: training time and loss, the
-    U-Net application time and tensor FLOP rate, and the learned FCG solve
-    (iterations, ms, true residual) beside plain FP64 CG on the same system.
-    --learned-max-its caps the learned solve (0: to the tolerance)."""
-    import torch
-
+def train_unet(ctx):
+    """Trains the U-Net on the GPU (this library's forward/backward kernels,
+    Adam, the A-norm loss) on (residual, error) pairs harvested from plain
+    CG's own iterates on a 64^3 system of the bench's sphere family (16
+    spheres, another seed).  Returns the parameters and a description."""
     import xflow_gb300 as xf
     from xflow_gb300 import workloads as wl
 
-    ctx = xf.Context(0)
-    stream = torch.cuda.ExternalStream(capi_stream(ctx))
     T = UNET_TRAIN
     codes, nrm, _, sep, _ = wl.spheres_grid(T["n"], T["spheres"], 0.02, 0.06, T["seed"])
     g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
@@ -741,7 +739,85 @@ def learned(args):
     ctx.synchronize()
     t2 = time.perf_counter()
     last = float(np.mean([net.train_step(r, e, update=False, op=A) for r, e in zip(rs, es)]))
-    params = net.params()
+    return net.params(), {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
+                          "steps": T["steps"], "lr": T["lr"], "s": t2 - t1, "harvest_s": t1 - t0,
+                          "anorm_loss_before": first, "anorm_loss_after": last}
+
+
+def two_level(args):
+    """The learned two-level preconditioner at the bench's 256^3 system: the
+    U-Net trained as for --learned (64^3 sphere family, another geometry) runs
+    on the coarse grid of 4^3 blocks (64^3) as the coarse solver, the FP32
+    Chebyshev passes smooth, and FCG(window) drives both.  Prints one JSON
+    line: training, the coarse application time, and per window the
+    iterations and ms of the solve to a true 1e-8 relative residual, beside
+    the untrained network and plain FP64 CG."""
+    import torch
+
+    import xflow_gb300 as xf
+    from xflow_gb300 import capi
+    from xflow_gb300 import workloads as wl
+
+    ctx = xf.Context(0)
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    params, train = train_unet(ctx)
+    codes, sep, b = workload(args.size)
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    A = xf.Operator(g)
+    cc, s1, s2, s3 = wl.coarse_grid(codes, sep, 4)
+    gc = xf.Grid(ctx, cc, s1, s2, s3, None)
+    net = xf.UNet(gc, params)
+    bv = g.vec(b)
+    rc, zc = gc.vec(np.zeros(gc.shape)), gc.vec(None)
+    for _ in range(3):
+        net.apply(rc, zc)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        net.apply(rc, zc)
+    e1.record(stream)
+    e1.synchronize()
+    line = {"mode": "learned two-level preconditioner", "workload": f"{args.size}^3 spheres system (the bench's)",
+            "coarse_grid": f"{gc.shape[0] - 2}^3 blocks of 4^3", "train": train,
+            "coarse_unet_apply_ms": e0.elapsed_time(e1) / 10, "solves": {}}
+    sweep = [tuple(int(v) for v in c.split(":")) for c in args.two_level_sweep.split(",")]
+    fresh = xf.UNet(gc, seed=1)
+    for label, nn in (("trained", net), ("untrained", fresh)):
+        for deg, ratio, w in sweep if nn is net else sweep[:1]:
+            best = None
+            for _ in range(2):
+                x = g.vec(np.zeros(g.shape))
+                st = xf.solve_fcg(A, x, bv, unet=nn, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, window=w,
+                                  degree=deg, ratio=ratio)
+                if best is None or st.ms < best["ms"]:
+                    best = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid,
+                            "status": int(st.status), "fallbacks": st.fallbacks}
+            line["solves"][f"{label} degree {deg} ratio {ratio} window {w}"] = best
+    x = g.vec(np.zeros(g.shape))
+    st = xf.solve(A, x, bv, method=xf.XF_CG, rtol=RTOL)
+    line["plain_fp64_cg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid}
+    print(json.dumps(line))
+    return 0
+
+
+def learned(args):
+    """The learned preconditioner at the bench's 256^3 system: a U-Net trained
+    on the GPU (this library's forward/backward kernels, Adam, the A-norm
+    loss) on (residual, error) pairs harvested from plain CG's own iterates on
+    a 64^3 system of the same sphere family, then applied by flexible CG
+    FCG(8) at full size.  Prints one JSON line: training time and loss, the
+    U-Net application time and tensor FLOP rate, and the learned FCG solve
+    (iterations, ms, true residual) beside plain FP64 CG on the same system.
+    --learned-max-its caps the learned solve (0: to the tolerance)."""
+    import torch
+
+    import xflow_gb300 as xf
+    from xflow_gb300 import workloads as wl
+
+    ctx = xf.Context(0)
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    params, train = train_unet(ctx)
     codes2, sep2, b2 = workload(args.size)
     g2 = xf.Grid(ctx, codes2, sep2, sep2, sep2, None)
     A2 = xf.Operator(g2)
@@ -761,9 +837,7 @@ def learned(args):
     apply_ms = e0.elapsed_time(e1) / reps
     ex, us = unet_flops(g2.shape)
     line = {"mode": "learned preconditioner", "workload": f"{args.size}^3 spheres system (the bench's)",
-            "train": {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
-                      "steps": T["steps"], "lr": T["lr"], "s": t2 - t1, "harvest_s": t1 - t0,
-                      "anorm_loss_before": first, "anorm_loss_after": last},
+            "train": train,
             "unet_apply_ms": apply_ms, "tensor_tflops_executed": ex / (apply_ms * 1e-3) / 1e12,
             "tensor_tflops_useful": us / (apply_ms * 1e-3) / 1e12, "tflop_per_apply": ex / 1e12}
     if not args.learned_applies_only:

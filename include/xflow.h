@@ -208,7 +208,17 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
  * degree 4 and 250 above).  Degree 2 applies both stencil levels in one pass
  * over memory; degree 2 m is the product of m real quadratic factors, one
  * pass each. */
-enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3 };
+/* XF_PRECOND_UNET2: xf_solve_fcg with the network as the coarse solver of a
+ * two-level preconditioner (no counterpart in the reference).  The network is
+ * built on a coarse grid whose interior cells are F x F x F blocks of the
+ * operator's interior (F >= 2, equal on every axis); with P the
+ * piecewise-constant prolongation over the blocks, y = P U-Net(P^T r),
+ * omega = (y, r) / (y, A y) and z = omega y + s p(A) (r - omega A y), p the
+ * XF_PRECOND_CHEB polynomial (FP32 passes; degree opts.reserved[2], default
+ * 8; ratio opts.reserved[1], default 60) scaled by s so that
+ * lambda s p(lambda) is closest to 1 on its interval.  Uniform Laplace grids
+ * without boundary rows. */
+enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3, XF_PRECOND_UNET2 = 4 };
 /* Host only (no device work): the XF_PRECOND_CHEB polynomial as the solver
  * builds it, in powers of A.  degree 2 writes its three Horner coefficients
  * (a0, a1, a2: z = a0 r + A (a1 r + a2 A r)); degree 2m (4 to 12) writes m
@@ -454,7 +464,8 @@ int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, const xf_ve
 /* Flexible CG, truncated FCG(m): each preconditioned residual is
  * A-orthogonalised against the last m directions (m = opts->reserved[0],
  * 1..8, default 8), robust to a preconditioner that varies between
- * applications.  Preconditioner opts->precond: XF_PRECOND_UNET (u),
+ * applications.  Preconditioner opts->precond: XF_PRECOND_UNET (u on the
+ * operator's grid), XF_PRECOND_UNET2 (u on the coarse grid, see above),
  * XF_PRECOND_JACOBI (Laplace diagonal) or none; FP64; stops on the true
  * relative residual (opts->rtol).  Plain CG is the fallback (counted in
  * stats->fallbacks): per iteration when z is no descent direction, for good

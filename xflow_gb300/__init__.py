@@ -15,8 +15,8 @@ import numpy as np
 from . import capi
 from .capi import (XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE, XF_BICG, XF_BICGSTAB, XF_CG,  # noqa: F401
                    XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE, XF_IB_POS, XF_IB_VEL, XF_MINRES,
-                   XF_OP_ADVDIFF, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_ZERO_INACTIVE,
-                   XFError)
+                   XF_OP_ADVDIFF, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_PRECOND_UNET2,
+                   XF_ZERO_INACTIVE, XFError)
 
 
 def _check(ctx_handle, st):
@@ -617,10 +617,14 @@ class UNet(_Owned):
             pass
 
 
-def solve_fcg(op, x, b, unet=None, precond=None, rtol=1e-8, maxit=100000, window=8):
-    """Flexible CG, FCG(window), with the U-Net (default when given), Jacobi or no preconditioner."""
+def solve_fcg(op, x, b, unet=None, precond=None, rtol=1e-8, maxit=100000, window=8, degree=0, ratio=0):
+    """Flexible CG, FCG(window), with the U-Net (default when given), Jacobi or no preconditioner.
+    precond=XF_PRECOND_UNET2 with a U-Net built on the coarse grid of F^3 blocks (`workloads.coarse_grid`)
+    runs the learned two-level preconditioner."""
     o = solve_opts(method=capi.XF_FCG, rtol=rtol, maxit=maxit)
     o.reserved[0] = int(window)
+    o.reserved[1] = int(ratio)    # XF_PRECOND_UNET2: smoothing interval ratio (0: default)
+    o.reserved[2] = int(degree)   # XF_PRECOND_UNET2: smoothing degree (0: default)
     o.precond = precond if precond is not None else (capi.XF_PRECOND_UNET if unet is not None else
                                                      capi.XF_PRECOND_NONE)
     st = capi.SolveStats()

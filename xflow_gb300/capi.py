@@ -19,7 +19,7 @@ XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE = 1, 2
 XF_EXACT, XF_ZERO_INACTIVE = 1, 2
 XF_CG, XF_CG_REFERENCE, XF_BICGSTAB, XF_MINRES, XF_BICG, XF_FCG = 0, 1, 2, 3, 4, 5
 XF_PREC_FP64, XF_PREC_MIXED = 0, 1
-XF_PRECOND_NONE, XF_PRECOND_JACOBI, XF_PRECOND_UNET, XF_PRECOND_CHEB = 0, 1, 2, 3
+XF_PRECOND_NONE, XF_PRECOND_JACOBI, XF_PRECOND_UNET, XF_PRECOND_CHEB, XF_PRECOND_UNET2 = 0, 1, 2, 3, 4
 XF_IB_ELASTIC, XF_IB_TARGET, XF_IB_FIXED_ELASTIC, XF_IB_PLAIN, XF_IB_FIXED_STRETCHING = 0, 1, 2, 3, 4
 XF_IB_POS, XF_IB_VEL, XF_IB_FORCE = 0, 1, 2
 

@@ -31,6 +31,11 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
 void xf_dot_async(const xf_grid* g, int dtype, const void* a, const void* b, int slot);
 int xf_op_ready(const xf_op* op);
+bool xf_cg_poly_supported(const xf_grid* g);
+bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]);
+void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
+void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
+                             const float* pa, const float* pb, float* e, float* r_out);
 
 namespace {
 
@@ -762,8 +767,77 @@ __global__ void k_jacobi(const double* __restrict__ r, const double* __restrict_
   }
 }
 
-// scalar slots: 0..7 (z, A p_j); 10 (z, r); 11 (r, r); 12 (p, r); 14/15 matvec dots
-enum { FS_ZR = 10, FS_RR = 11, FS_PR = 12, FS_PQ = 14 };
+// The learned two-level preconditioner (XF_PRECOND_UNET2).  The network is
+// built on a coarse grid whose interior cells are the F x F x F blocks of the
+// fine interior (ghost layers match), and serves as the coarse solver; the
+// FP32 Chebyshev polynomial of the mixed CG (factored, one two-level pass
+// per factor) smooths what it leaves:
+//   y = P N(P^T r)             P: piecewise constant over the blocks
+//   omega = (y, r) / (y, A y)  the A-norm optimal step along y (the network's
+//                              output scale is arbitrary)
+//   z = omega y + s p(A) (r - omega A y)
+// s makes lambda s p(lambda) closest to 1 on [lambda_max / ratio, lambda_max].
+__global__ void k_restrict_blocks(const double* __restrict__ r, int f2, int f3, int F, double* __restrict__ rc, int c1,
+                                  int c2, int c3) {
+  const int64_t nc = (int64_t)c1 * c2 * c3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    const int K = (int)(c % c3);
+    const int64_t t = c / c3;
+    const int J = (int)(t % c2), I = (int)(t / c2);
+    double v = 0.0;
+    if (I > 0 && I < c1 - 1 && J > 0 && J < c2 - 1 && K > 0 && K < c3 - 1) {
+      const int i0 = 1 + (I - 1) * F, j0 = 1 + (J - 1) * F, k0 = 1 + (K - 1) * F;
+      for (int a = 0; a < F; a++)
+        for (int b = 0; b < F; b++) {
+          const double* row = r + ((int64_t)(i0 + a) * f2 + (j0 + b)) * f3 + k0;
+          for (int q = 0; q < F; q++) v += row[q];
+        }
+    }
+    rc[c] = v;
+  }
+}
+__global__ void k_prolong_blocks(const double* __restrict__ zc, int c2, int c3, int F, const uint8_t* __restrict__ smask,
+                                 int f1, int f2, int f3, double* __restrict__ y) {
+  const int64_t n = (int64_t)f1 * f2 * f3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(c % f3);
+    const int64_t t = c / f3;
+    const int j = (int)(t % f2), i = (int)(t / f2);
+    double v = 0.0;
+    if (smask[c] && i > 0 && i < f1 - 1 && j > 0 && j < f2 - 1 && k > 0 && k < f3 - 1)
+      v = zc[((int64_t)(1 + (i - 1) / F) * c2 + (1 + (j - 1) / F)) * c3 + (1 + (k - 1) / F)];
+    y[c] = v;
+  }
+}
+__global__ void k_sub_f32(const double* __restrict__ r, const double* __restrict__ q, double om, int64_t n,
+                          float* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = (float)(r[c] - om * q[c]);
+}
+__global__ void k_twolevel_z(const double* __restrict__ y, const float* __restrict__ w, double om, double sc,
+                             const uint8_t* __restrict__ smask, int64_t n, double* __restrict__ z) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    z[c] = smask[c] ? om * y[c] + sc * (double)w[c] : 0.0;
+}
+
+// The factor of the smoothing polynomial: 2 / (min + max) of lambda p(lambda)
+// over [lmax / ratio, lmax], p the product of the quadratic factors.
+static double cheb_scale(const float (*f)[3], int nf, double lmax, double ratio) {
+  double gmin = 1e300, gmax = -1e300;
+  const double lo = lmax / ratio;
+  for (int q = 0; q <= 8192; q++) {
+    const double lam = lo + (lmax - lo) * q / 8192.0;
+    double p = 1.0;
+    for (int k = 0; k < nf; k++) p *= (double)f[k][0] + lam * ((double)f[k][1] + lam * (double)f[k][2]);
+    gmin = fmin(gmin, lam * p);
+    gmax = fmax(gmax, lam * p);
+  }
+  return 2.0 / (gmin + gmax);
+}
+
+// scalar slots: 0..7 (z, A p_j); 8 (y, A y), 9 (y, r) of the two-level preconditioner; 10 (z, r); 11 (r, r);
+// 12 (p, r); 14/15 matvec dots
+enum { FS_YAY = 8, FS_YR = 9, FS_ZR = 10, FS_RR = 11, FS_PR = 12, FS_PQ = 14 };
 
 static int read_n(xf_ctx* ctx, int first, int count, double* out) {
   XF_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, &ctx->scratch->scalars[first], count * 8, cudaMemcpyDeviceToHost,
@@ -788,6 +862,39 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   const int m = o.reserved[0] > 0 ? (o.reserved[0] > 8 ? 8 : o.reserved[0]) : 8;
   if (o.precond == XF_PRECOND_UNET && (!u || u->g != g))
     return xf_fail(ctx, XF_ERR_ARG, "xf_solve_fcg: XF_PRECOND_UNET needs a network built on the operator's grid");
+  // two-level: the network's grid is the coarse grid of F^3 blocks
+  const bool two = o.precond == XF_PRECOND_UNET2;
+  int F = 0;
+  const xf_grid* cg = two && u ? u->g : nullptr;
+  if (two) {
+    if (!u || u->ctx != ctx)
+      return xf_fail(ctx, XF_ERR_ARG, "xf_solve_fcg: XF_PRECOND_UNET2 needs a network on the same context");
+    if (cg->n1 > 2) F = (g->n1 - 2) / (cg->n1 - 2);
+    if (F < 2 || (g->n1 - 2) != F * (cg->n1 - 2) || (g->n2 - 2) != F * (cg->n2 - 2) || (g->n3 - 2) != F * (cg->n3 - 2))
+      return xf_fail(ctx, XF_ERR_ARG,
+                     "xf_solve_fcg: XF_PRECOND_UNET2: the network's grid must have interiors of F x F x F blocks of "
+                     "the operator's (F >= 2, the same on every axis)");
+    if (op->kind != XF_OP_LAPLACE || !xf_cg_poly_supported(g))
+      return xf_fail(ctx, XF_ERR_UNSUPPORTED,
+                     "xf_solve_fcg: XF_PRECOND_UNET2 smooths with the Chebyshev passes: a uniform Laplace grid without "
+                     "boundary rows");
+  }
+  // smoothing polynomial: degree opts->reserved[2] (even, 2 to 12, default 8) over
+  // [lambda_max / ratio, lambda_max], ratio = opts->reserved[1] (default 60)
+  const int tl_deg = o.reserved[2] > 0 ? o.reserved[2] : 8;
+  const double tl_ratio = o.reserved[1] > 1 ? (double)o.reserved[1] : 60.0;
+  const int tl_nf = tl_deg / 2;
+  float tl_f[6][3];
+  double tl_scale = 0.0;
+  if (two) {
+    if (tl_deg < 2 || tl_deg > 12 || tl_deg % 2)
+      return xf_fail(ctx, XF_ERR_ARG, "xf_solve_fcg: XF_PRECOND_UNET2 degree (opts.reserved[2]) must be even, 2 to 12");
+    const double lmax = 4.0 * (g->ucx + g->ucy + g->ucz);   // Gershgorin bound of the uniform Laplace rows
+    if (tl_nf == 1) xf_cheb2_coeffs(lmax, tl_ratio, tl_f[0]);
+    else if (!xf_cheb_factors(lmax, tl_ratio, tl_deg, tl_f))
+      return xf_fail(ctx, XF_ERR_ARG, "xf_solve_fcg: no quadratic factors of the smoothing polynomial");
+    tl_scale = cheb_scale(tl_f, tl_nf, lmax, tl_ratio);
+  }
   if (o.precond == XF_PRECOND_JACOBI && op->kind != XF_OP_LAPLACE)
     return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve_fcg: Jacobi uses the Laplace diagonal");
   int rc;
@@ -813,6 +920,39 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   double *P[8] = {nullptr}, *Q[8] = {nullptr};
   bool okb = r && z && pn && qn;
   for (int j = 0; j < m && okb; j++) okb = (P[j] = buf()) && (Q[j] = buf());
+  // two-level: y, A y (fine FP64), the smoother's FP32 ping-pong pair, the coarse r and z
+  double *ty = nullptr, *tqy = nullptr, *trc = nullptr, *tzc = nullptr;
+  float *t32a = nullptr, *t32b = nullptr;
+  if (two && okb) {
+    okb = (ty = buf()) && (tqy = buf());
+    for (int h = 0; h < 2 && okb; h++) {
+      float* p = nullptr;
+      okb = cudaMalloc(&p, n * 4) == cudaSuccess;
+      if (!okb) cudaGetLastError();
+      else bufs.push_back((double*)p);   // freed with the rest
+      (h ? t32b : t32a) = p;
+    }
+    if (okb) {
+      const int64_t nc = cg->ncell;
+      for (int h = 0; h < 2 && okb; h++) {
+        double* p = nullptr;
+        okb = cudaMalloc(&p, nc * 8) == cudaSuccess;
+        if (!okb) cudaGetLastError();
+        else bufs.push_back(p);
+        (h ? tzc : trc) = p;
+      }
+    }
+    if (okb) {   // the Chebyshev passes return at once while a mixed solve's done / pause flags are set
+      long long zero3[3] = {0, 0, 0};
+      okb = cudaMemcpyAsync(&ctx->scratch->iscalars[I_DONE], zero3, 8, cudaMemcpyHostToDevice, ctx->stream) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(&ctx->scratch->iscalars[I_PAUSE], zero3, 8, cudaMemcpyHostToDevice, ctx->stream) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(&ctx->scratch->iscalars[I_ERR], zero3, 8, cudaMemcpyHostToDevice, ctx->stream) ==
+                cudaSuccess &&
+            cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+    }
+  }
   if (!okb) {
     cleanup();
     return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve_fcg: allocation");
@@ -829,6 +969,28 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   };
   auto apply_m = [&]() -> int {   // z = M r
     if (precond == XF_PRECOND_UNET) return xf_unet_apply_dev(u, r, z);
+    if (precond == XF_PRECOND_UNET2) {
+      k_restrict_blocks<<<grid_blocks(ctx, cg->ncell, 256), 256, 0, s>>>(r, g->n2, g->n3, F, trc, cg->n1, cg->n2,
+                                                                        cg->n3);
+      int st2 = xf_unet_apply_dev(u, trc, tzc);
+      if (st2) return st2;
+      k_prolong_blocks<<<eb, 256, 0, s>>>(tzc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, ty);
+      MvReq<double> my;   // A y, (y, A y)
+      my.x = ty; my.y = tqy; my.w = ty; my.zero_inactive = 1; my.slot = FS_YAY;
+      xf_mv64(op, my);
+      xf_dot_async(g, XF_F64, ty, r, FS_YR);
+      double v[2];
+      if ((st2 = read_n(ctx, FS_YAY, 2, v))) return st2;
+      const double om = (v[0] > 0 && std::isfinite(v[0]) && std::isfinite(v[1])) ? v[1] / v[0] : 0.0;
+      k_sub_f32<<<eb, 256, 0, s>>>(r, tqy, om, n, t32a);   // r - omega A y, FP32
+      float *src = t32a, *dst = t32b;
+      for (int k = tl_nf - 1; k >= 0; k--) {
+        xf_cg_poly_first_launch(op, src, dst, tl_f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
+        std::swap(src, dst);
+      }
+      k_twolevel_z<<<eb, 256, 0, s>>>(ty, src, om, tl_scale, g->smask, n, z);
+      return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+    }
     if (precond == XF_PRECOND_JACOBI) {
       k_jacobi<<<eb, 256, 0, s>>>(r, g->diag, g->kind, n, z);
       return XF_OK;
@@ -910,7 +1072,12 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   cleanup();
-  if (o.precond == XF_PRECOND_UNET && (rc = xf_conv_status(ctx))) return rc;
+  if ((o.precond == XF_PRECOND_UNET || two) && (rc = xf_conv_status(ctx))) return rc;
+  if (two) {   // a bounded wait of a Chebyshev pass that gave up
+    long long err = 0;
+    XF_CUDA(ctx, cudaMemcpy(&err, &ctx->scratch->iscalars[I_ERR], 8, cudaMemcpyDeviceToHost));
+    if (err) return xf_fail(ctx, XF_ERR_CUDA, "xf_solve_fcg: a smoothing pass timed out on a copy");
+  }
   const double rel = bb > 0 ? sqrt(tr[1] / bb) : sqrt(tr[1]);
   st->status = status == XF_OK && rel > o.rtol ? XF_STALL : status;
   st->iterations = it;

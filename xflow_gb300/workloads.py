@@ -180,6 +180,24 @@ def spheres_grid(n: int, nspheres: int, rmin: float, rmax: float, seed: int):
     return codes, np.zeros((nb, nb, nb, 3)), nodes, sep, (np.array(centres), np.array(radii))
 
 
+def coarse_grid(codes: np.ndarray, sep, F: int):
+    """Point codes and separations of the coarse grid whose interior cells are
+    the F x F x F blocks of a fine grid's interior (ghost layers match): a
+    block with any active fine cell is Actual, else Fictive; the ghost layer is
+    Fictive.  `sep` is the fine grid's uniform separations (one axis).  This is
+    the grid of the learned two-level preconditioner's network."""
+    n = np.array(codes.shape) - 2
+    if np.any(n % F):
+        raise ValueError(f"interior {tuple(n)} is not a whole number of {F}^3 blocks")
+    act = space_mask(codes)[1:-1, 1:-1, 1:-1].astype(bool)
+    m = act.reshape(n[0] // F, F, n[1] // F, F, n[2] // F, F).any(axis=(1, 3, 5))
+    out = np.zeros(tuple(n // F + 2), np.int32)
+    out[1:-1, 1:-1, 1:-1][m] = ACTUAL
+    _drop_isolated(out)
+    H = float(sep[0]) * F
+    return out, np.full(out.shape[0] - 1, H), np.full(out.shape[1] - 1, H), np.full(out.shape[2] - 1, H)
+
+
 def _drop_isolated(codes: np.ndarray) -> None:
     act = codes == ACTUAL
     nonfict = codes != FICTIVE
