@@ -5,13 +5,17 @@ Workload (synthetic, seeded): unit cube, 256^3 cells plus a ghost layer
 non-overlapping spheres with radii U[0.02, 0.06] masked Fictive; right-hand
 side = -div of an i.i.d. N(0,1) staggered velocity, projected to zero mean.
 One "step" is one solve from x = 0 to ||b - A x||_2 <= 1e-8 ||b||_2 (true
-FP64 residual).  The timed solver is the mixed-precision CG (FP32 stencil and
-vectors, FP64 dots/scalars, FP64 residual replacement every 50 iterations)
-preconditioned by the degree-8 Chebyshev polynomial z = p1(A) ... p4(A) r
-(four real quadratic factors, both stencil levels of each in one pass over
-memory, the residual update fused into the first pass); plain FP64 CG and
-the unpreconditioned mixed CG on the same system are timed beside it
-(XF_BENCH_CHEB_DEGREE=2, 4, ... 12 times another degree instead).
+FP64 residual).  The timed solver is the learned two-level preconditioner
+under mixed-precision flexible CG: FP32 vectors and stencils, FP64 dots, the
+FP32 recursion refreshed from the true FP64 residual every 50 iterations or
+after a 10^3 drop; preconditioner z = omega y + s p(A)(r - omega A y) with
+y = P U-Net(P^T r) on the coarse grid of 4^3 blocks (BF16 tcgen05
+convolutions) and p the degree-8 Chebyshev polynomial over
+[lmax/60, lmax] as four FP32 two-level stencil passes.  The network is
+trained on the GPU before the timed region, on a 64^3 system of the same
+sphere family (another geometry).  Plain FP64 CG, the unpreconditioned mixed
+CG and the Chebyshev-preconditioned mixed CG without the network (degree
+XF_BENCH_CHEB_DEGREE, default 8) are timed beside it on the same system.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xflow|reference]
 
@@ -41,6 +45,11 @@ RTOL = 1e-8
 CHEB_DEGREE = int(os.environ.get("XF_BENCH_CHEB_DEGREE", "8"))   # degree of the polynomial preconditioner
 CHEB_RATIO = {2: 30, 4: 120}.get(CHEB_DEGREE, 250)                # its default lambda_max / lambda_min
 CALIB = os.path.join(ROOT, "profiles", "bench_calibration.json")
+# the timed solver: learned two-level preconditioner under mixed-precision FCG
+TL_BLOCK = 4     # coarse cells are 4^3 blocks of the fine interior
+TL_DEGREE = 8    # smoothing polynomial degree (factored into TL_DEGREE / 2 passes)
+TL_RATIO = int(os.environ.get("XF_BENCH_TL_RATIO", "60"))   # its lambda_max / lambda_min
+TL_WINDOW = int(os.environ.get("XF_BENCH_TL_WINDOW", "1"))  # FCG window
 
 
 def workload(n=N_CELLS):
@@ -219,8 +228,11 @@ def main():
     ap.add_argument("--learned-max-its", type=int, default=0, help="with --learned: cap of the learned solve")
     ap.add_argument("--two-level", action="store_true",
                     help="time the learned two-level preconditioner (U-Net coarse solver + Chebyshev smoothing)")
-    ap.add_argument("--two-level-sweep", default="8:60:2,8:60:1,8:250:2,8:30:2,4:60:2,12:60:2",
-                    help="with --two-level: smoothing degree:ratio:FCG window triples")
+    ap.add_argument("--two-level-profile", action="store_true",
+                    help="with --two-level: one 10-iteration solve with untrained weights (for a launch list)")
+    ap.add_argument("--two-level-sweep",
+                    default="8:60:2:32,8:60:2:64,8:60:1:32,8:250:2:32,8:30:2:32,4:60:2:32,4:30:2:32,12:60:2:32",
+                    help="with --two-level: smoothing degree:ratio:FCG window:vector bits (32 mixed, 64) entries")
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
@@ -281,8 +293,29 @@ def main():
     one(xf.XF_PREC_MIXED)
     st_plain = one(xf.XF_PREC_MIXED)
 
+    # the Chebyshev-preconditioned mixed CG (the same smoother, no network), beside it
+    one(xf.XF_PREC_MIXED, **cheb)
+    cheb_sts = [one(xf.XF_PREC_MIXED, **cheb) for _ in range(args.steps)]
+
+    # The timed solver: the learned two-level preconditioner under mixed-precision
+    # FCG.  The U-Net is trained first (outside the timed region: once per
+    # geometry family) on a 64^3 system of the sphere family, then runs on the
+    # coarse grid of 4^3 blocks of this system.
+    from xflow_gb300 import workloads as wl
+
+    params, train = train_unet(ctx)
+    cc, s1, s2, s3 = wl.coarse_grid(codes, sep, TL_BLOCK)
+    gc = xf.Grid(ctx, cc, s1, s2, s3, None)
+    net = xf.UNet(gc, params)
+
+    def learned_solve(zero=True):
+        if zero:
+            x.fill(0.0)
+        return xf.solve_fcg(A, x, bv, unet=net, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, window=TL_WINDOW,
+                            degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED)
+
     for _ in range(args.warmup):
-        one(xf.XF_PREC_MIXED, **cheb)
+        learned_solve()
     clocks = Clocks(local)
     ctx.synchronize()
     barrier(dist)
@@ -290,7 +323,8 @@ def main():
     t0 = time.perf_counter()
     dev_ms, launches, sts = [], 0, []
     for _ in range(args.steps):
-        st = one(xf.XF_PREC_MIXED, **cheb)
+        st = learned_solve()
+        assert st.status == 0, st.status
         dev_ms.append(st.ms)
         launches += int(st.reserved[0])
         sts.append(st)
@@ -302,8 +336,9 @@ def main():
     xm = x.download()
     st_last = sts[-1]
 
-    # End to end through the host-buffer C-ABI call: H2D of b and x0, solve,
-    # D2H of x, every step, from pinned host memory.
+    # End to end through the C ABI from host buffers: H2D of b and x0 from
+    # pinned host memory, the learned solve, D2H of x into pinned memory, every
+    # step.
     import torch
 
     hb = torch.empty(g.shape, dtype=torch.float64, pin_memory=True)
@@ -314,12 +349,28 @@ def main():
         hx.numpy()[...] = 0.0
         ctx.synchronize()
         t1 = time.perf_counter()
-        s2 = xf.solve_host(A, hx.numpy(), hb.numpy(), method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL, **cheb)
+        bv.upload(hb.numpy())
+        x.upload(hx.numpy())
+        s2 = learned_solve(zero=False)
+        x.download(out=hx.numpy())
         t2 = time.perf_counter()
         if k >= args.warmup:
             e2e.append((t2 - t1) * 1e3)
         assert s2.status == 0
     e2e_ms = replica_value(dist, e2e, world)
+    # one coarse network application, CUDA events on the context stream
+    stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    rc, zc = gc.vec(np.zeros(gc.shape)), gc.vec(None)
+    net.apply(rc, zc)
+    ctx.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(10):
+        net.apply(rc, zc)
+    ev1.record(stream)
+    ev1.synchronize()
+    unet_ms = ev0.elapsed_time(ev1) / 10
+    unet_ex, _ = unet_flops(gc.shape)
 
     # Roofline: each kernel of the mixed CG iteration timed alone (CUDA events
     # on its launching stream, the solver's own launch configuration), with
@@ -333,7 +384,12 @@ def main():
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
            "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29,
            "cheb_first_fused_f32": 29, "cheb_last_f32": 13, "cheb_middle_f32": 9}
-    if "cheb_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE >= 4:
+    if "cheb_middle_f32" in kms and "stencil_f32" in kms:
+        # the learned two-level iteration: the smoother's TL_DEGREE / 2 factor
+        # passes (each the middle-pass kernel, w' = p_k(A) w), and two FP32
+        # stencils with a dot (A y of the coarse correction, A p)
+        per_iter = {"cheb_middle_f32": TL_DEGREE // 2, "stencil_f32": 2.0}
+    elif "cheb_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE >= 4:
         # per chunk of 50: the passes of the m = degree / 2 factors once (the
         # first without the update: timed as a middle pass, the same work),
         # then K1, the first pass with the update, m - 2 middle passes and
@@ -391,16 +447,17 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (f64 dots, scalars, residual replacement)", "data": "synthetic",
+        "dtype": "f32 vectors and stencils, bf16 network (fp32 accumulate), f64 dots/scalars/residual refresh",
+        "data": "synthetic",
         "config": {"workload": workload_name(args.size),
-                   "solver": "mixed-precision CG (FP32 matvec/vectors, FP64 dots, true-residual replacement/50)",
-                   "preconditioner": (f"degree-{CHEB_DEGREE} Chebyshev polynomial over [lmax/{CHEB_RATIO}, "
-                                      "lmax]" + (f" as {CHEB_DEGREE // 2} real quadratic factors, one two-level stencil "
-                                                 "pass each, the residual update fused into the first"
-                                                 if CHEB_DEGREE >= 4 else
-                                                 ", both stencil levels in one pass, the residual update fused in") +
-                                      " (the learned U-Net preconditioner is timed by bench.py --learned: fewer "
-                                      "iterations, but 26.1 ms per application)"),
+                   "solver": (f"mixed-precision flexible CG, FCG({TL_WINDOW}) (FP32 vectors and stencils, FP64 dots, "
+                              "true FP64 residual refresh every 50 iterations or after a 10^3 drop)"),
+                   "preconditioner": (f"learned two-level: 3-level U-Net (16/32/64 channels, BF16 tcgen05 "
+                                      f"convolutions) on the coarse grid of {TL_BLOCK}^3 blocks as the coarse solver, "
+                                      f"degree-{TL_DEGREE} Chebyshev smoothing over [lmax/{TL_RATIO}, lmax] as "
+                                      f"{TL_DEGREE // 2} FP32 two-level stencil passes"),
+                   "training": (f"on the GPU before the timed region: {train['steps']} Adam steps on "
+                                f"{train['pairs']} (residual, error) pairs from plain CG on a {train['grid']} system"),
                    "rtol": RTOL,
                    "l2": "working set ~0.6 GB > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},
@@ -409,6 +466,12 @@ def main():
         "fp64_cg_ms": fp64_ms, "fp64_cg_iterations": fp64_iters, "fp64_cg_rel_resid": st64.rel_resid,
         "mixed_cg_unpreconditioned": {"ms": st_plain.ms, "iterations": st_plain.iterations,
                                       "rel_resid": st_plain.rel_resid},
+        "mixed_cg_chebyshev": {"ms": float(np.mean([c.ms for c in cheb_sts])), "iterations": cheb_sts[-1].iterations,
+                               "rel_resid": cheb_sts[-1].rel_resid,
+                               "preconditioner": f"degree-{CHEB_DEGREE} Chebyshev, ratio {CHEB_RATIO}, no network"},
+        "train": train,
+        "coarse_unet": {"grid": f"{gc.shape[0] - 2}^3 (+ ghost layer)", "ms_per_apply": unet_ms,
+                        "tflops_executed": unet_ex / (unet_ms * 1e-3) / 1e12},
         "speedup_vs_fp64_cg": fp64_ms / value if value > 0 else None,
         "wall_ms_per_step": wall / args.steps,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ncell * 8, "d2h_bytes_per_step": ncell * 8},
@@ -760,6 +823,20 @@ def two_level(args):
 
     ctx = xf.Context(0)
     stream = torch.cuda.ExternalStream(capi_stream(ctx))
+    if args.two_level_profile:   # launch list of a short solve: untrained weights (the same kernels), 10 iterations
+        codes, sep, b = workload(args.size)
+        g = xf.Grid(ctx, codes, sep, sep, sep, None)
+        cc, s1, s2, s3 = wl.coarse_grid(codes, sep, TL_BLOCK)
+        gc = xf.Grid(ctx, cc, s1, s2, s3, None)
+        net = xf.UNet(gc, seed=1)
+        A = xf.Operator(g)
+        for maxit in (2, 10):
+            x = g.vec(np.zeros(g.shape))
+            st = xf.solve_fcg(A, x, g.vec(b), unet=net, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, maxit=maxit,
+                              window=TL_WINDOW, degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED)
+            print(json.dumps({"mode": "two-level profile", "maxit": maxit, "iterations": st.iterations,
+                              "ms": st.ms, "launches": int(st.reserved[0]), "status": int(st.status)}))
+        return 0
     params, train = train_unet(ctx)
     codes, sep, b = workload(args.size)
     g = xf.Grid(ctx, codes, sep, sep, sep, None)
@@ -784,16 +861,17 @@ def two_level(args):
     sweep = [tuple(int(v) for v in c.split(":")) for c in args.two_level_sweep.split(",")]
     fresh = xf.UNet(gc, seed=1)
     for label, nn in (("trained", net), ("untrained", fresh)):
-        for deg, ratio, w in sweep if nn is net else sweep[:1]:
+        for deg, ratio, w, bits in sweep if nn is net else sweep[:1]:
+            prec = xf.XF_PREC_MIXED if bits == 32 else xf.XF_PREC_FP64
             best = None
             for _ in range(2):
                 x = g.vec(np.zeros(g.shape))
                 st = xf.solve_fcg(A, x, bv, unet=nn, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, window=w,
-                                  degree=deg, ratio=ratio)
+                                  degree=deg, ratio=ratio, precision=prec)
                 if best is None or st.ms < best["ms"]:
                     best = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid,
-                            "status": int(st.status), "fallbacks": st.fallbacks}
-            line["solves"][f"{label} degree {deg} ratio {ratio} window {w}"] = best
+                            "status": int(st.status), "fallbacks": st.fallbacks, "refreshes": st.replacements}
+            line["solves"][f"{label} degree {deg} ratio {ratio} window {w} fp{bits}"] = best
     x = g.vec(np.zeros(g.shape))
     st = xf.solve(A, x, bv, method=xf.XF_CG, rtol=RTOL)
     line["plain_fp64_cg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid}

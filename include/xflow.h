@@ -229,7 +229,7 @@ int xf_cheb_factors_host(double lmax, double ratio, int degree, float* factors);
 
 typedef struct {
   int method;            /* XF_CG ...                                              */
-  int precision;         /* XF_PREC_FP64 or XF_PREC_MIXED (CG only)                */
+  int precision;         /* XF_PREC_FP64 or XF_PREC_MIXED (CG; FCG + UNET2)        */
   int precond;           /* XF_PRECOND_*                                           */
   int maxit;             /* iteration cap; 0 = 100000                              */
   double rtol;           /* relative tolerance on ||b - A x||_2 / ||b||_2 (XF_CG,  */
@@ -251,7 +251,7 @@ typedef struct {
   double rel_resid;      /* final true ||b - A x||_2 / ||b||_2, FP64               */
   double abs_resid;      /* final value the method's own stopping rule tested      */
   double ms;             /* device time of the solve                               */
-  double reserved[4];
+  double reserved[4];    /* [0]: kernels launched (mixed CG, mixed FCG)            */
 } xf_solve_stats;
 
 void xf_solve_opts_default(xf_solve_opts* o);
@@ -466,7 +466,11 @@ int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, const xf_ve
  * 1..8, default 8), robust to a preconditioner that varies between
  * applications.  Preconditioner opts->precond: XF_PRECOND_UNET (u on the
  * operator's grid), XF_PRECOND_UNET2 (u on the coarse grid, see above),
- * XF_PRECOND_JACOBI (Laplace diagonal) or none; FP64; stops on the true
+ * XF_PRECOND_JACOBI (Laplace diagonal) or none; FP64, or with
+ * XF_PRECOND_UNET2 and opts->precision = XF_PREC_MIXED the correction,
+ * residual and directions in FP32 with FP64 dots, refreshed from the true
+ * FP64 residual every opts->replace_every iterations or after a 10^3 drop of
+ * the FP32 residual (window kept); stops on the true
  * relative residual (opts->rtol).  Plain CG is the fallback (counted in
  * stats->fallbacks): per iteration when z is no descent direction, for good
  * when the residual stalls. */

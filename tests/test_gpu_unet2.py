@@ -2,8 +2,10 @@
 coarse grid of 4 x 4 x 4 blocks is the coarse solver, the FP32 Chebyshev
 passes smooth, and the flexible CG drives both.
 
-Bars: every solve reaches a true 1e-8 relative residual, recomputed in FP64
-by the oracle; the two-level preconditioner needs far fewer iterations than
+Bars: every solve, FP64 or mixed precision (FP32 vectors, FP64 dots),
+reaches a true 1e-8 relative residual, recomputed in FP64 by the oracle, and
+repeats its iteration count on a second solve; the two-level preconditioner
+needs far fewer iterations than
 plain and Jacobi FCG; a network trained on another geometry's coarse system
 does at least as well as the untrained one; grids that are not block
 coarsenings of each other are refused.
@@ -73,7 +75,11 @@ def test_two_level_fcg_converges_with_fewer_iterations(ctx):
     for name, kw in (("plain", {}), ("jacobi", {"precond": capi.XF_PRECOND_JACOBI}),
                      ("two_level_untrained", {"unet": fresh, "precond": capi.XF_PRECOND_UNET2}),
                      ("two_level", {"unet": trained, "precond": capi.XF_PRECOND_UNET2}),
-                     ("two_level_w2", {"unet": trained, "precond": capi.XF_PRECOND_UNET2, "window": 2})):
+                     ("two_level_w2", {"unet": trained, "precond": capi.XF_PRECOND_UNET2, "window": 2}),
+                     ("two_level_mixed", {"unet": trained, "precond": capi.XF_PRECOND_UNET2, "window": 2,
+                                          "precision": xf.XF_PREC_MIXED}),
+                     ("two_level_mixed_deg4", {"unet": trained, "precond": capi.XF_PRECOND_UNET2, "window": 2,
+                                               "precision": xf.XF_PREC_MIXED, "degree": 4, "ratio": 30})):
         for rep in range(2):   # a second solve in a row starts from the same state
             x = g.vec(np.zeros(g.shape))
             st = xf.solve_fcg(A, x, bv, rtol=1e-8, **kw)
@@ -89,6 +95,7 @@ def test_two_level_fcg_converges_with_fewer_iterations(ctx):
     assert its["two_level"] < 0.25 * its["plain"], its
     assert its["two_level"] < 0.5 * its["jacobi"], its
     assert its["two_level"] <= its["two_level_untrained"], its
+    assert its["two_level_mixed"] <= 1.3 * its["two_level_w2"] + 3, its   # FP32 vectors cost few iterations
 
 
 @pytest.mark.gpu

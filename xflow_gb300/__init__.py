@@ -141,8 +141,11 @@ class Vec(_Owned):
         _check(self.grid.ctx.h, capi.lib().xf_vec_upload(self.h, capi._ptr(a)))
         return self
 
-    def download(self):
-        out = np.empty(self.grid.shape, np.float64)
+    def download(self, out=None):
+        """The box as a new array, or into `out` (C-contiguous float64 of the box's size, e.g. pinned memory)."""
+        if out is None:
+            out = np.empty(self.grid.shape, np.float64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == int(np.prod(self.grid.shape))
         _check(self.grid.ctx.h, capi.lib().xf_vec_download(self.h, capi._ptr(out)))
         return out
 
@@ -617,11 +620,14 @@ class UNet(_Owned):
             pass
 
 
-def solve_fcg(op, x, b, unet=None, precond=None, rtol=1e-8, maxit=100000, window=8, degree=0, ratio=0):
+def solve_fcg(op, x, b, unet=None, precond=None, rtol=1e-8, maxit=100000, window=8, degree=0, ratio=0,
+              precision=XF_PREC_FP64):
     """Flexible CG, FCG(window), with the U-Net (default when given), Jacobi or no preconditioner.
     precond=XF_PRECOND_UNET2 with a U-Net built on the coarse grid of F^3 blocks (`workloads.coarse_grid`)
-    runs the learned two-level preconditioner."""
+    runs the learned two-level preconditioner, in FP64 or (precision=XF_PREC_MIXED) with FP32 vectors and
+    FP64 dots."""
     o = solve_opts(method=capi.XF_FCG, rtol=rtol, maxit=maxit)
+    o.precision = int(precision)
     o.reserved[0] = int(window)
     o.reserved[1] = int(ratio)    # XF_PRECOND_UNET2: smoothing interval ratio (0: default)
     o.reserved[2] = int(degree)   # XF_PRECOND_UNET2: smoothing degree (0: default)

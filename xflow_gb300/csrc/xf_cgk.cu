@@ -72,14 +72,15 @@ __device__ __forceinline__ T lap_fast(uint8_t kb, T cxm, T cxp, T cym, T cyp, T 
 template <typename T, bool RES>
 __device__ __forceinline__ void finish_cg_kernel(DevScratch* S, const CgqArgs<T>& a, const DotAcc<T>& acc, double* sh,
                                                  bool* last) {
-  const int slot = RES ? a.slot + 1 : SL_A;
-  const int ticket = RES ? a.slot : SL_A;
+  // RES: (r, r) -> slot + 1; otherwise (p, q) -> slot (SL_A for the CG's own launches)
+  const int slot = RES ? a.slot + 1 : a.slot;
+  const int ticket = a.slot;
   if (!publish_acc<T>(S, slot, ticket, acc, sh, last)) return;
   double tot = finish_partials(S, slot, sh);
   if (threadIdx.x == 0) {
     S->scalars[slot] = tot;
     S->tickets[ticket] = 0;
-    control_step(S, RES ? a.ctl : CTL_CG_ALPHA);
+    control_step(S, a.ctl);
   }
 }
 
@@ -715,6 +716,11 @@ void xf_cg_q64(const xf_op* op, const double* p, double* q) {
 }
 void xf_cg_q32(const xf_op* op, const float* p, float* q) {
   launch_cg_q<float, false>(op, p, q, nullptr, nullptr, SL_A, CTL_CG_ALPHA);
+}
+// q = A p with (p, q) -> scalars[slot] and no control step (the flexible CG's
+// host loop reads the dot).  Laplace operators only.
+void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot) {
+  launch_cg_q<float, false>(op, p, q, nullptr, nullptr, slot, CTL_NONE);
 }
 // r32 = float(b - A x) in FP64, (r, r) -> scalars[slot + 1], then control `ctl`.
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl) {

@@ -29,6 +29,8 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
                    const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
                    int relu, const void* gate, int gate_ld);
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
+void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot);
+void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
 void xf_dot_async(const xf_grid* g, int dtype, const void* a, const void* b, int slot);
 int xf_op_ready(const xf_op* op);
 bool xf_cg_poly_supported(const xf_grid* g);
@@ -579,6 +581,8 @@ static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_off) {
                                                  chunk, y.gw, y.gb);
 }
 
+// Kernels one forward pass launches, with xf_unet_apply_dev's output conversion.
+constexpr int UNET_FORWARD_LAUNCHES = 18;
 static int forward(xf_unet* u, const double* r) {
   xf_ctx* ctx = u->ctx;
   cudaStream_t s = ctx->stream;
@@ -777,7 +781,8 @@ __global__ void k_jacobi(const double* __restrict__ r, const double* __restrict_
 //                              output scale is arbitrary)
 //   z = omega y + s p(A) (r - omega A y)
 // s makes lambda s p(lambda) closest to 1 on [lambda_max / ratio, lambda_max].
-__global__ void k_restrict_blocks(const double* __restrict__ r, int f2, int f3, int F, double* __restrict__ rc, int c1,
+template <typename T>
+__global__ void k_restrict_blocks(const T* __restrict__ r, int f2, int f3, int F, double* __restrict__ rc, int c1,
                                   int c2, int c3) {
   const int64_t nc = (int64_t)c1 * c2 * c3;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
@@ -789,15 +794,16 @@ __global__ void k_restrict_blocks(const double* __restrict__ r, int f2, int f3, 
       const int i0 = 1 + (I - 1) * F, j0 = 1 + (J - 1) * F, k0 = 1 + (K - 1) * F;
       for (int a = 0; a < F; a++)
         for (int b = 0; b < F; b++) {
-          const double* row = r + ((int64_t)(i0 + a) * f2 + (j0 + b)) * f3 + k0;
-          for (int q = 0; q < F; q++) v += row[q];
+          const T* row = r + ((int64_t)(i0 + a) * f2 + (j0 + b)) * f3 + k0;
+          for (int q = 0; q < F; q++) v += (double)row[q];
         }
     }
     rc[c] = v;
   }
 }
+template <typename T>
 __global__ void k_prolong_blocks(const double* __restrict__ zc, int c2, int c3, int F, const uint8_t* __restrict__ smask,
-                                 int f1, int f2, int f3, double* __restrict__ y) {
+                                 int f1, int f2, int f3, T* __restrict__ y) {
   const int64_t n = (int64_t)f1 * f2 * f3;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(c % f3);
@@ -806,18 +812,121 @@ __global__ void k_prolong_blocks(const double* __restrict__ zc, int c2, int c3, 
     double v = 0.0;
     if (smask[c] && i > 0 && i < f1 - 1 && j > 0 && j < f2 - 1 && k > 0 && k < f3 - 1)
       v = zc[((int64_t)(1 + (i - 1) / F) * c2 + (1 + (j - 1) / F)) * c3 + (1 + (k - 1) / F)];
-    y[c] = v;
+    y[c] = (T)v;
   }
 }
-__global__ void k_sub_f32(const double* __restrict__ r, const double* __restrict__ q, double om, int64_t n,
+template <typename T>
+__global__ void k_sub_f32(const T* __restrict__ r, const T* __restrict__ q, double om, int64_t n,
                           float* __restrict__ out) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
-    out[c] = (float)(r[c] - om * q[c]);
+    out[c] = (float)((double)r[c] - om * (double)q[c]);
 }
-__global__ void k_twolevel_z(const double* __restrict__ y, const float* __restrict__ w, double om, double sc,
-                             const uint8_t* __restrict__ smask, int64_t n, double* __restrict__ z) {
+template <typename T>
+__global__ void k_twolevel_z(const T* __restrict__ y, const float* __restrict__ w, double om, double sc,
+                             const uint8_t* __restrict__ smask, int64_t n, T* __restrict__ z) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
-    z[c] = smask[c] ? om * y[c] + sc * (double)w[c] : 0.0;
+    z[c] = smask[c] ? (T)(om * (double)y[c] + sc * (double)w[c]) : (T)0;
+}
+// The F = 4 transfers of the mixed path.  Restriction: one thread per coarse
+// cell, its 64 loads unrolled (a warp reads 32 consecutive runs of 4 floats).
+// Prolongation: 2-D grid over (j, k) plane positions and i planes, 32-bit
+// index arithmetic.
+__global__ void k_restrict4(const float* __restrict__ r, int f2, int f3, double* __restrict__ rc, int c1, int c2,
+                            int c3) {
+  const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, I = blockIdx.z;
+  if (K >= c3) return;
+  double v = 0.0;
+  if (I > 0 && I < c1 - 1 && J > 0 && J < c2 - 1 && K > 0 && K < c3 - 1) {
+    const int64_t base = ((int64_t)(1 + 4 * (I - 1)) * f2 + (1 + 4 * (J - 1))) * f3 + (1 + 4 * (K - 1));
+    float part[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      float sa = 0.f;
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const float* row = r + base + ((int64_t)a * f2 + b) * f3;
+        sa += (__ldg(row) + __ldg(row + 1)) + (__ldg(row + 2) + __ldg(row + 3));
+      }
+      part[a] = sa;
+    }
+    v = ((double)part[0] + (double)part[1]) + ((double)part[2] + (double)part[3]);
+  }
+  rc[((int64_t)I * c2 + J) * c3 + K] = v;
+}
+__global__ void k_prolong4(const double* __restrict__ zc, int c2, int c3, const uint8_t* __restrict__ smask, int f1,
+                           int f2, int f3, float* __restrict__ y) {
+  const int P = f2 * f3;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (p >= P) return;
+  const int j = p / f3, k = p - j * f3;
+  const int64_t c = (int64_t)i * P + p;
+  float v = 0.f;
+  if (smask[c] && i > 0 && i < f1 - 1 && j > 0 && j < f2 - 1 && k > 0 && k < f3 - 1)
+    v = (float)zc[((int64_t)(1 + ((i - 1) >> 2)) * c2 + (1 + ((j - 1) >> 2))) * c3 + (1 + ((k - 1) >> 2))];
+  y[c] = v;
+}
+// (a, b) of FP32 boxes that are zero off the active set: exact products
+// accumulated in float-float per thread and per warp, FP64 across warps and
+// blocks; 16-byte loads.  -> scalars[slot]
+__global__ void __launch_bounds__(RED_THREADS) k_dot_f4(const float* __restrict__ a, const float* __restrict__ b,
+                                                        int64_t n, DevScratch* S, int slot) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  DotAcc<float> acc;
+  const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  const float4* b4 = reinterpret_cast<const float4*>(b);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n4; c += stride) {
+    const float4 x = __ldg(a4 + c), y = __ldg(b4 + c);
+    acc.add(x.x, y.x);
+    acc.add(x.y, y.y);
+    acc.add(x.z, y.z);
+    acc.add(x.w, y.w);
+  }
+  for (int64_t c = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += stride) acc.add(a[c], b[c]);
+  if (!publish_acc<float>(S, slot, slot, acc, sh, &last)) return;
+  const double t = finish_partials(S, slot, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[slot] = t;
+    S->tickets[slot] = 0;
+  }
+}
+// FP32 forms with omega = (y, r) / (y, A y) read from the device scalars (no host round trip)
+__device__ __forceinline__ double tl_omega(const double* scal, int s_yay, int s_yr) {
+  const double yay = scal[s_yay], yr = scal[s_yr];
+  return (yay > 0 && isfinite(yay) && isfinite(yr)) ? yr / yay : 0.0;
+}
+__global__ void k_sub_dev(const float* __restrict__ r, const float* __restrict__ q, const double* scal, int s_yay,
+                          int s_yr, int64_t n, float* __restrict__ out) {
+  const float om = (float)tl_omega(scal, s_yay, s_yr);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = fmaf(-om, q[c], r[c]);
+}
+__global__ void k_twolevel_dev(const float* __restrict__ y, const float* __restrict__ w, const double* scal, int s_yay,
+                               int s_yr, float sc, const uint8_t* __restrict__ smask, int64_t n, float* __restrict__ z) {
+  const float om = (float)tl_omega(scal, s_yay, s_yr);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    z[c] = smask[c] ? fmaf(om, y[c], sc * w[c]) : 0.f;
+}
+// mixed FCG vector kernels (FP32 vectors)
+__global__ void k_fcg_update_f(float* __restrict__ e, float* __restrict__ r, const float* __restrict__ p,
+                               const float* __restrict__ q, float alpha, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    e[c] = fmaf(alpha, p[c], e[c]);
+    r[c] = fmaf(-alpha, q[c], r[c]);
+  }
+}
+__global__ void k_axpy_f(float* __restrict__ y, const float* __restrict__ x, float a, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    y[c] = fmaf(a, x[c], y[c]);
+}
+__global__ void k_d2f(const double* __restrict__ a, int64_t n, float* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = (float)a[c];
+}
+__global__ void k_fold_f2d(double* __restrict__ x, const float* __restrict__ e, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    x[c] += (double)e[c];
 }
 
 // The factor of the smoothing polynomial: 2 / (min + max) of lambda p(lambda)
@@ -844,6 +953,209 @@ static int read_n(xf_ctx* ctx, int first, int count, double* out) {
                                ctx->stream));
   XF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   for (int q = 0; q < count; q++) out[q] = ctx->host_scalars[q];
+  return XF_OK;
+}
+
+// Mixed-precision FCG(m) with the learned two-level preconditioner: the
+// correction e, the residual r, the directions and their images are FP32;
+// the dots are accumulated in FP64 (exact FP32 products summed in
+// float-float, then FP64); alpha and the window coefficients are FP64.  The
+// FP32 recursion is refreshed from the true residual b - A x, computed in
+// FP64 after x += e, every `replace_every` iterations, whenever its (r, r)
+// has dropped by 10^6 since the last refresh, and when it meets the
+// tolerance; the window of directions is kept across a refresh (each new
+// direction is still A-orthogonalised against it).  The solve ends only on
+// the true FP64 residual.
+static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, int m, int F, const float (*tl_f)[3],
+                               int tl_nf, double tl_scale, xf_vec* xv, const xf_vec* bv, xf_solve_stats* st) {
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  const xf_grid* cg = u->g;
+  const int64_t n = g->ncell, nc = cg->ncell;
+  cudaStream_t s = ctx->stream;
+  const int eb = grid_blocks(ctx, n, 256);
+  const int db = red_blocks(ctx, (n + 3) / 4);
+  auto fdot = [&](const float* a, const float* b2, int slot) {
+    k_dot_f4<<<db, RED_THREADS, 0, s>>>(a, b2, n, ctx->scratch, slot);
+  };
+  std::vector<void*> bufs;
+  auto alloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    cudaMemsetAsync(p, 0, bytes, s);
+    bufs.push_back(p);
+    return p;
+  };
+  auto cleanup = [&]() {
+    for (void* p : bufs) cudaFree(p);
+  };
+  auto fail = [&](int code, const char* msg) {
+    cleanup();
+    return xf_fail(ctx, code, "xf_solve_fcg: %s", msg);
+  };
+  double *rc = (double*)alloc(nc * 8), *zc = (double*)alloc(nc * 8);
+  float *r = (float*)alloc(n * 4), *e = (float*)alloc(n * 4), *z = (float*)alloc(n * 4), *y = (float*)alloc(n * 4);
+  float *ay = (float*)alloc(n * 4), *w0 = (float*)alloc(n * 4), *w1 = (float*)alloc(n * 4);
+  float *P[9] = {nullptr}, *Q[9] = {nullptr};   // ring of m + 1: the new direction and the window
+  bool ok = rc && zc && r && e && z && y && ay && w0 && w1;
+  for (int j = 0; j <= m && ok; j++) ok = (P[j] = (float*)alloc(n * 4)) && (Q[j] = (float*)alloc(n * 4));
+  if (ok) {   // the Chebyshev passes return at once while a mixed solve's done / pause flags are set
+    long long zero = 0;
+    ok = cudaMemcpyAsync(&ctx->scratch->iscalars[I_DONE], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaMemcpyAsync(&ctx->scratch->iscalars[I_PAUSE], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaMemcpyAsync(&ctx->scratch->iscalars[I_ERR], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaStreamSynchronize(s) == cudaSuccess;
+  }
+  if (!ok) return fail(XF_ERR_NOMEM, "allocation");
+  double* x = (double*)xv->data;
+  const double* b = (const double*)bv->data;
+  int precond = XF_PRECOND_UNET2, rcode;
+  long long launches = 0;   // this library's kernels launched by the solve
+  // z = M r in FP32
+  auto apply_m = [&]() -> int {
+    if (precond != XF_PRECOND_UNET2) {
+      return cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+    }
+    if (F == 4)
+      k_restrict4<<<dim3((cg->n3 + 63) / 64, cg->n2, cg->n1), 64, 0, s>>>(r, g->n2, g->n3, rc, cg->n1, cg->n2, cg->n3);
+    else
+      k_restrict_blocks<float><<<grid_blocks(ctx, nc, 256), 256, 0, s>>>(r, g->n2, g->n3, F, rc, cg->n1, cg->n2,
+                                                                         cg->n3);
+    int st2 = xf_unet_apply_dev(u, rc, zc);
+    if (st2) return st2;
+    if (F == 4)
+      k_prolong4<<<dim3((g->n2 * g->n3 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1, g->n2,
+                                                                         g->n3, y);
+    else
+      k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
+    xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
+    xf_dot_async(cg, XF_F64, zc, rc, FS_YR);   // (y, r) = (z_c, P^T r)
+    const double* scal = ctx->scratch->scalars;
+    k_sub_dev<<<eb, 256, 0, s>>>(r, ay, scal, FS_YAY, FS_YR, n, w0);   // r - omega A y
+    float *src = w0, *dst = w1;
+    for (int k = tl_nf - 1; k >= 0; k--) {
+      xf_cg_poly_first_launch(op, src, dst, tl_f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
+      std::swap(src, dst);
+    }
+    k_twolevel_dev<<<eb, 256, 0, s>>>(y, src, scal, FS_YAY, FS_YR, (float)tl_scale, g->smask, n, z);
+    launches += 6 + UNET_FORWARD_LAUNCHES + tl_nf;
+    return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+  };
+  // r = float(b - A x), the residual computed in FP64 (zero off the active set), its (r, r) in FP64
+  // -> scalars[FS_PQ + 1]
+  auto true_residual = [&](double* rr) -> int {
+    xf_cg_res64(op, x, b, r, FS_PQ, CTL_NONE);
+    launches++;
+    double v[2];
+    int st2 = read_n(ctx, FS_PQ, 2, v);
+    *rr = v[1];
+    return st2;
+  };
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  xf_dot_async(g, XF_F64, b, b, FS_RR);
+  launches++;
+  double bb;
+  if ((rcode = read_n(ctx, FS_RR, 1, &bb))) return fail(rcode, "scalar read");
+  const double thr = o.rtol * o.rtol * bb;
+  const int every = o.replace_every > 0 ? o.replace_every : 50;
+  double pq_win[9] = {0};
+  int it = 0, nwin = 0, head = 0, status = XF_OK, repl = 0;
+  double rr_true = 0.0, rr_prev_true = 0.0;
+  int prev_cycle = 0;
+  for (;;) {
+    if ((rcode = true_residual(&rr_true))) return fail(rcode, "scalar read");
+    if (rr_true <= thr) break;
+    if (std::isnan(rr_true)) { status = XF_NAN; break; }
+    if (it >= o.maxit) { status = XF_MAXIT; break; }
+    if (repl > 0 && precond == XF_PRECOND_UNET2 && prev_cycle >= 10 && !(rr_true < 0.81 * rr_prev_true)) {
+      // no progress over a whole refresh cycle of 10 or more iterations: plain CG from here on (the fallback)
+      precond = XF_PRECOND_NONE;
+      st->fallbacks++;
+    }
+    rr_prev_true = rr_true;
+    XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, s));
+    const double rr_start = rr_true;
+    const int it_start = it;
+    double rr = rr_true;
+    bool brk = false;
+    while (true) {
+      it++;
+      if ((rcode = apply_m())) return fail(rcode, "preconditioner");
+      // (z, r) and (z, A p_j) over the window, one read
+      auto dots_z = [&](double* zq) -> int {
+        fdot(z, r, FS_ZR);
+        for (int j = 0; j < nwin; j++) fdot(z, Q[(head + m + 1 - 1 - j) % (m + 1)], j);
+        launches += 1 + nwin;
+        return read_n(ctx, 0, FS_ZR + 1, zq);
+      };
+      double zq[FS_ZR + 1];
+      if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
+      if (!(zq[FS_ZR] > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
+        st->fallbacks++;
+        XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s));
+        if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
+      }
+      // the new direction p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j into ring slot `head`
+      float *pn = P[head], *qn = Q[head];
+      XF_CUDA(ctx, cudaMemcpyAsync(pn, z, n * 4, cudaMemcpyDeviceToDevice, s));
+      if (nwin > 0) {
+        for (int j = 0; j < nwin; j++) {
+          const int sl = (head + m + 1 - 1 - j) % (m + 1);
+          if (pq_win[sl] > 0) {
+            k_axpy_f<<<eb, 256, 0, s>>>(pn, P[sl], (float)(-zq[j] / pq_win[sl]), n);
+            launches++;
+          }
+        }
+      }
+      xf_cg_q32_dot(op, pn, qn, FS_PQ);   // q = A p, (p, q)
+      fdot(pn, r, FS_PR);
+      launches += 2;
+      double v3[3];   // slots FS_PR .. FS_PQ
+      if ((rcode = read_n(ctx, FS_PR, FS_PQ - FS_PR + 1, v3))) return fail(rcode, "scalar read");
+      const double pr = v3[0], pq = v3[FS_PQ - FS_PR];
+      if (!(pq > 0)) {
+        status = std::isnan(pq) ? XF_NAN : XF_BREAKDOWN;
+        brk = true;
+        break;
+      }
+      k_fcg_update_f<<<eb, 256, 0, s>>>(e, r, pn, qn, (float)(pr / pq), n);
+      pq_win[head] = pq;
+      head = (head + 1) % (m + 1);
+      if (nwin < m) nwin++;
+      fdot(r, r, FS_RR);
+      launches += 2;   // the update and (r, r)
+      if ((rcode = read_n(ctx, FS_RR, 1, &rr))) return fail(rcode, "scalar read");
+      if (std::isnan(rr) || rr <= thr || rr <= 1e-6 * rr_start || it - it_start >= every || it >= o.maxit) break;
+    }
+    k_fold_f2d<<<eb, 256, 0, s>>>(x, e, n);   // x += e in FP64
+    launches++;
+    repl++;
+    prev_cycle = it - it_start;
+    if (brk) {   // report the true residual of the final x
+      if ((rcode = true_residual(&rr_true))) return fail(rcode, "scalar read");
+      break;
+    }
+  }
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+  XF_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  cleanup();
+  if ((rcode = xf_conv_status(ctx))) return rcode;
+  long long err = 0;   // a bounded wait of a Chebyshev pass that gave up
+  XF_CUDA(ctx, cudaMemcpy(&err, &ctx->scratch->iscalars[I_ERR], 8, cudaMemcpyDeviceToHost));
+  if (err) return xf_fail(ctx, XF_ERR_CUDA, "xf_solve_fcg: a smoothing pass timed out on a copy");
+  const double rel = bb > 0 ? sqrt(rr_true / bb) : sqrt(rr_true);
+  st->status = status == XF_OK && rel > o.rtol ? XF_STALL : status;
+  st->iterations = it;
+  st->replacements = repl;
+  st->reserved[0] = (double)launches;
+  st->rel_resid = rel;
+  st->abs_resid = sqrt(rr_true);
+  st->ms = ms;
   return XF_OK;
 }
 
@@ -901,6 +1213,9 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   if ((rc = xf_op_ready(op))) return rc;
   memset(st, 0, sizeof(*st));
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (two && o.precision == XF_PREC_MIXED) return fcg_mixed_two_level(op, u, o, m, F, tl_f, tl_nf, tl_scale, xv, bv, st);
+  if (o.precision == XF_PREC_MIXED)
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve_fcg: mixed precision is for XF_PRECOND_UNET2");
   const int64_t n = g->ncell;
   std::vector<double*> bufs;
   auto buf = [&]() -> double* {
@@ -970,11 +1285,11 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
   auto apply_m = [&]() -> int {   // z = M r
     if (precond == XF_PRECOND_UNET) return xf_unet_apply_dev(u, r, z);
     if (precond == XF_PRECOND_UNET2) {
-      k_restrict_blocks<<<grid_blocks(ctx, cg->ncell, 256), 256, 0, s>>>(r, g->n2, g->n3, F, trc, cg->n1, cg->n2,
-                                                                        cg->n3);
+      k_restrict_blocks<double><<<grid_blocks(ctx, cg->ncell, 256), 256, 0, s>>>(r, g->n2, g->n3, F, trc, cg->n1,
+                                                                                cg->n2, cg->n3);
       int st2 = xf_unet_apply_dev(u, trc, tzc);
       if (st2) return st2;
-      k_prolong_blocks<<<eb, 256, 0, s>>>(tzc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, ty);
+      k_prolong_blocks<double><<<eb, 256, 0, s>>>(tzc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, ty);
       MvReq<double> my;   // A y, (y, A y)
       my.x = ty; my.y = tqy; my.w = ty; my.zero_inactive = 1; my.slot = FS_YAY;
       xf_mv64(op, my);
@@ -982,13 +1297,13 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
       double v[2];
       if ((st2 = read_n(ctx, FS_YAY, 2, v))) return st2;
       const double om = (v[0] > 0 && std::isfinite(v[0]) && std::isfinite(v[1])) ? v[1] / v[0] : 0.0;
-      k_sub_f32<<<eb, 256, 0, s>>>(r, tqy, om, n, t32a);   // r - omega A y, FP32
+      k_sub_f32<double><<<eb, 256, 0, s>>>(r, tqy, om, n, t32a);   // r - omega A y, FP32
       float *src = t32a, *dst = t32b;
       for (int k = tl_nf - 1; k >= 0; k--) {
         xf_cg_poly_first_launch(op, src, dst, tl_f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
         std::swap(src, dst);
       }
-      k_twolevel_z<<<eb, 256, 0, s>>>(ty, src, om, tl_scale, g->smask, n, z);
+      k_twolevel_z<double><<<eb, 256, 0, s>>>(ty, src, om, tl_scale, g->smask, n, z);
       return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
     }
     if (precond == XF_PRECOND_JACOBI) {
