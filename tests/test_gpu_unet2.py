@@ -7,8 +7,8 @@ reaches a true 1e-8 relative residual, recomputed in FP64 by the oracle, and
 repeats its iteration count on a second solve; the two-level preconditioner
 needs far fewer iterations than
 plain and Jacobi FCG; a network trained on another geometry's coarse system
-does at least as well as the untrained one; grids that are not block
-coarsenings of each other are refused.
+does at least as well as the untrained one; training is bit-reproducible;
+grids that are not block coarsenings of each other are refused.
 """
 import numpy as np
 import pytest
@@ -96,6 +96,22 @@ def test_two_level_fcg_converges_with_fewer_iterations(ctx):
     assert its["two_level"] < 0.5 * its["jacobi"], its
     assert its["two_level"] <= its["two_level_untrained"], its
     assert its["two_level_mixed"] <= 1.3 * its["two_level_w2"] + 3, its   # FP32 vectors cost few iterations
+
+
+@pytest.mark.gpu
+def test_training_is_deterministic(ctx):
+    # the reductions of the training step (sums of squares, weight and bias gradients) are fixed-order:
+    # two networks trained alike end bit-identical, so a trained solver's iteration count is reproducible
+    _, _, _, _, _, gt, At = fine_and_coarse(ctx, 64, 12, 11)
+    bs = wl.divergence_rhs(np.asarray(gt.codes), (np.full(gt.shape[0] - 1, 1 / 16),) * 3, 300)
+    rs, es = xf.harvest_pairs(At, gt.vec(bs), iters=(2, 8, 30))
+    out = []
+    for _ in range(2):
+        net = xf.UNet(gt, seed=1)
+        for step in range(30):
+            net.train_step(rs[step % 3], es[step % 3], lr=2e-3, op=At)
+        out.append(net.params())
+    assert np.array_equal(out[0], out[1])
 
 
 @pytest.mark.gpu

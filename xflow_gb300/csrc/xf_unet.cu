@@ -90,6 +90,10 @@ struct xf_unet {
   float* gsum = nullptr;            // FP32 [level-0 cells x 16]: S0 gradient accumulator
   float* gsum1 = nullptr;           // FP32 [level-1 cells x 32]: S1 gradient accumulator
   double* red = nullptr;            // device reductions: [0] sum r^2, [1] sum e^2, [2] loss
+  double* rpart = nullptr;          // per-block partials of the sums of squares, 2 x RP_MAX
+  unsigned* rtick = nullptr;        // their last-block tickets
+  float* wpart = nullptr;           // per-chunk weight-gradient partials [chunk][27][co][ci]
+  float* bpart = nullptr;           // per-chunk bias-gradient partials [chunk][co]
   double* zd = nullptr;             // level-0 box, FP64: the output (A-norm loss)
   double* az = nullptr;             // A zd
   int step = 0;
@@ -212,12 +216,33 @@ __global__ void k_skip_grad(const uint16_t* __restrict__ gskip, int gld, float* 
 }
 
 // Sum of squares over the active cells (FP64 atomics into red[slot]).
-__global__ void k_sumsq(const double* __restrict__ x, const uint8_t* __restrict__ m, int64_t n, double* red, int slot) {
+// Per-block partials, summed in block order by the last block to finish, so
+// the result does not depend on scheduling (256 threads, at most RP_MAX blocks).
+constexpr int RP_MAX = 4096;
+__global__ void __launch_bounds__(256) k_sumsq(const double* __restrict__ x, const uint8_t* __restrict__ m, int64_t n,
+                                               double* red, int slot, double* part, unsigned* tick) {
+  __shared__ double sw[8];
+  __shared__ bool last;
   double s = 0;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
     if (m[c]) s += x[c] * x[c];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&red[slot], s);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0;
+    for (int w = 0; w < 8; w++) b += sw[w];
+    part[slot * RP_MAX + blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(&tick[slot], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double t = 0;
+  for (unsigned k = 0; k < gridDim.x; k++) t += __ldcg(&part[slot * RP_MAX + k]);
+  red[slot] = t;
+  tick[slot] = 0;
 }
 
 // Level-0 input: channel 0 = r / rms(r) on active cells, channels 1..15 = 0.
@@ -261,9 +286,17 @@ __global__ void k_unet_loss(const float* __restrict__ z, const double* __restric
 // Block = (tap, chunk of cells); the chunk's gradient and input rows are
 // staged in shared memory, each thread owns co*ci/256 (co, ci) pairs.
 constexpr int WG_CELLS = 64;
+// Cells per weight-gradient block: 4096, or more so that a level has at most
+// WG_MAX_CHUNKS chunks (the partial buffers' size).
+constexpr int WG_MAX_CHUNKS = 128;
+static int64_t wg_chunk(int64_t n) {
+  int64_t c = (n + WG_MAX_CHUNKS - 1) / WG_MAX_CHUNKS;
+  c = (c + WG_CELLS - 1) / WG_CELLS * WG_CELLS;
+  return c < 4096 ? 4096 : c;
+}
 __global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, int gld, const uint16_t* __restrict__ x,
                                                int xld, int ci, int co, int n2, int n3, int64_t ncell, int chunk,
-                                               float* __restrict__ gw, float* __restrict__ gb) {
+                                               float* __restrict__ wpart, float* __restrict__ bpart) {
   extern __shared__ float wsm[];
   float* sg = wsm;                   // [WG_CELLS][co]
   float* sx = wsm + WG_CELLS * co;   // [WG_CELLS][ci]
@@ -301,9 +334,24 @@ __global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, i
   }
   for (int q = 0; q < per; q++) {
     const int pr = threadIdx.x + q * 256;
-    if (pr < npair) atomicAdd(&gw[(int64_t)t * npair + pr], accv[q]);
+    if (pr < npair) wpart[((int64_t)blockIdx.x * 27 + t) * npair + pr] = accv[q];
   }
-  if (t == 13 && threadIdx.x < co) atomicAdd(&gb[threadIdx.x], accb);
+  if (t == 13 && threadIdx.x < co) bpart[(int64_t)blockIdx.x * co + threadIdx.x] = accb;
+}
+// gw[t][co][ci] += sum over chunks in chunk order, gb likewise (deterministic).
+__global__ void k_wgrad_sum(const float* __restrict__ wpart, const float* __restrict__ bpart, int nchunk, int64_t nw,
+                            int co, float* __restrict__ gw, float* __restrict__ gb) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u < nw) {
+    float s = 0.f;
+    for (int c = 0; c < nchunk; c++) s += wpart[(int64_t)c * nw + u];
+    gw[u] += s;
+  }
+  if (u < co) {
+    float s = 0.f;
+    for (int c = 0; c < nchunk; c++) s += bpart[(int64_t)c * co + u];
+    gb[u] += s;
+  }
 }
 
 // Adam step on one layer (bias-corrected, step counts from 1), then the BF16
@@ -392,6 +440,10 @@ static void unet_free(xf_unet* u) {
   if (u->gsum) cudaFree(u->gsum);
   if (u->gsum1) cudaFree(u->gsum1);
   if (u->red) cudaFree(u->red);
+  if (u->rpart) cudaFree(u->rpart);
+  if (u->rtick) cudaFree(u->rtick);
+  if (u->wpart) cudaFree(u->wpart);
+  if (u->bpart) cudaFree(u->bpart);
   if (u->zd) cudaFree(u->zd);
   if (u->az) cudaFree(u->az);
   delete u;
@@ -472,6 +524,19 @@ extern "C" int xf_unet_create(const xf_grid* g, xf_unet** out) {
               cudaMalloc(&u->gsum1, u->L[1].n * 32 * 4) != cudaSuccess || cudaMalloc(&u->red, 8 * 8) != cudaSuccess ||
               cudaMalloc(&u->zd, u->L[0].n * 8) != cudaSuccess || cudaMalloc(&u->az, u->L[0].n * 8) != cudaSuccess))
     st = XF_ERR_NOMEM;
+  if (!st) {   // partial buffers of the deterministic reductions
+    int64_t wneed = 1;
+    for (int k = 0; k < NLAYER; k++) {
+      const int64_t n = u->L[LLEV[k]].n, chunk = wg_chunk(n), nchunk = (n + chunk - 1) / chunk;
+      const int64_t need = nchunk * 27 * u->ly[k].co * u->ly[k].ci;
+      if (need > wneed) wneed = need;
+    }
+    if (cudaMalloc(&u->rpart, 2 * RP_MAX * 8) != cudaSuccess || cudaMalloc(&u->rtick, 4 * 4) != cudaSuccess ||
+        cudaMalloc(&u->wpart, wneed * 4) != cudaSuccess || cudaMalloc(&u->bpart, WG_MAX_CHUNKS * 64 * 4) != cudaSuccess)
+      st = XF_ERR_NOMEM;
+    else
+      cudaMemsetAsync(u->rtick, 0, 4 * 4, ctx->stream);
+  }
   if (!st) {
     cudaMemsetAsync(u->zout, 0, u->L[0].n * 4, ctx->stream);
     cudaMemsetAsync(u->gsum, 0, u->L[0].n * 16 * 4, ctx->stream);
@@ -574,11 +639,15 @@ static int dgrad(xf_unet* u, int k, const Act& g, void* out, int out_ld, const A
 static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_off) {
   const Layer& y = u->ly[k];
   const Level& L = u->L[LLEV[k]];
-  const int chunk = 4096;
-  dim3 grid((unsigned)((L.n + chunk - 1) / chunk), 27);
+  const int64_t chunk = wg_chunk(L.n);
+  const int nchunk = (int)((L.n + chunk - 1) / chunk);
+  dim3 grid((unsigned)nchunk, 27);
   const size_t smem = (size_t)WG_CELLS * (y.co + y.ci) * 4;
   k_wgrad<<<grid, 256, smem, u->ctx->stream>>>(g.p0(u->L), g.C, x.p0(u->L) + x_off, x.C, y.ci, y.co, L.n2, L.n3, L.n,
-                                                 chunk, y.gw, y.gb);
+                                                 (int)chunk, u->wpart, u->bpart);
+  const int64_t nw = (int64_t)27 * y.co * y.ci;
+  k_wgrad_sum<<<(unsigned)((nw + 255) / 256), 256, 0, u->ctx->stream>>>(u->wpart, u->bpart, nchunk, nw, y.co, y.gw,
+                                                                        y.gb);
 }
 
 // Kernels one forward pass launches, with xf_unet_apply_dev's output conversion.
@@ -589,7 +658,7 @@ static int forward(xf_unet* u, const double* r) {
   const Level* L = u->L;
   int st;
   XF_CUDA(ctx, cudaMemsetAsync(u->red, 0, 8 * 8, s));
-  k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0);
+  k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0, u->rpart, u->rtick);
   k_unet_input<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, (double)L[0].active,
                                                     u->X0.p0(L));
   if ((st = conv(u, ENC0A, u->X0, 0, u->A0.p0(L), 16, 16, 0))) return st;
@@ -633,7 +702,7 @@ static int backward(xf_unet* u, const double* r, const double* e, const xf_op* o
     k_anorm_grad<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, u->az, L[0].mask, L[0].n, ctx->scratch, u->red,
                                                       u->G0_16a.p0(L));
   } else {
-    k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1);
+    k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1, u->rpart, u->rtick);
     k_unet_loss<<<ublocks(ctx, L[0].n), 256, 0, s>>>(u->zout, e, L[0].mask, L[0].n, (double)L[0].active, u->red,
                                                      u->G0_16a.p0(L));
   }
