@@ -10,8 +10,8 @@ under mixed-precision flexible CG: FP32 vectors and stencils, FP64 dots, the
 FP32 recursion refreshed from the true FP64 residual every 50 iterations or
 after a 10^3 drop; preconditioner z = omega y + s p(A)(r - omega A y) with
 y = P U-Net(P^T r) on the coarse grid of 4^3 blocks (BF16 tcgen05
-convolutions) and p the degree-8 Chebyshev polynomial over
-[lmax/60, lmax] as four FP32 two-level stencil passes.  The network is
+convolutions) and p the degree-6 Chebyshev polynomial over
+[lmax/20, lmax] as three FP32 two-level stencil passes.  The network is
 trained on the GPU before the timed region, on a 64^3 system of the same
 sphere family (another geometry).  Plain FP64 CG, the unpreconditioned mixed
 CG and the Chebyshev-preconditioned mixed CG without the network (degree
@@ -47,8 +47,8 @@ CHEB_RATIO = {2: 30, 4: 120}.get(CHEB_DEGREE, 250)                # its default 
 CALIB = os.path.join(ROOT, "profiles", "bench_calibration.json")
 # the timed solver: learned two-level preconditioner under mixed-precision FCG
 TL_BLOCK = 4     # coarse cells are 4^3 blocks of the fine interior
-TL_DEGREE = 8    # smoothing polynomial degree (factored into TL_DEGREE / 2 passes)
-TL_RATIO = int(os.environ.get("XF_BENCH_TL_RATIO", "60"))   # its lambda_max / lambda_min
+TL_DEGREE = int(os.environ.get("XF_BENCH_TL_DEGREE", "6"))  # smoothing polynomial degree (TL_DEGREE / 2 passes)
+TL_RATIO = int(os.environ.get("XF_BENCH_TL_RATIO", "20"))   # its lambda_max / lambda_min
 TL_WINDOW = int(os.environ.get("XF_BENCH_TL_WINDOW", "1"))  # FCG window
 
 
