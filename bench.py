@@ -440,7 +440,7 @@ def main():
         os.makedirs(os.path.dirname(CALIB), exist_ok=True)
         try:
             json.dump({"workload": "256^3 spheres, seed %d" % SEED, "fp64_cg_iterations": fp64_iters,
-                       "mixed_cg_iterations": st_last.iterations}, open(CALIB, "w"))
+                       "timed_solver_iterations": st_last.iterations}, open(CALIB, "w"))
         except OSError:
             pass
 
