@@ -922,6 +922,33 @@ __global__ void k_restrict4(const float* __restrict__ r, int f2, int f3, double*
   }
   rc[((int64_t)I * c2 + J) * c3 + K] = v;
 }
+// Four consecutive cells of a plane per thread (plane size a multiple of 4): one
+// 4-byte mask load and one 16-byte store.
+__global__ void k_prolong4v(const double* __restrict__ zc, int c2, int c3, const uint8_t* __restrict__ smask, int f1,
+                            int f2, int f3, float* __restrict__ y) {
+  const int P = f2 * f3;
+  const int p0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x), i = blockIdx.y;
+  if (p0 >= P) return;
+  const int64_t c0 = (int64_t)i * P + p0;
+  const uchar4 m4 = *reinterpret_cast<const uchar4*>(smask + c0);
+  const unsigned char mk[4] = {m4.x, m4.y, m4.z, m4.w};
+  int j = p0 / f3, k = p0 - j * f3;
+  float v[4];
+  const bool irow = i > 0 && i < f1 - 1;
+  const int64_t ib = (int64_t)(1 + ((i - 1) >> 2)) * c2;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    float t = 0.f;
+    if (mk[q] && irow && j > 0 && j < f2 - 1 && k > 0 && k < f3 - 1)
+      t = (float)__ldg(&zc[(ib + (1 + ((j - 1) >> 2))) * c3 + (1 + ((k - 1) >> 2))]);
+    v[q] = t;
+    if (++k == f3) {
+      k = 0;
+      j++;
+    }
+  }
+  *reinterpret_cast<float4*>(y + c0) = make_float4(v[0], v[1], v[2], v[3]);
+}
 __global__ void k_prolong4(const double* __restrict__ zc, int c2, int c3, const uint8_t* __restrict__ smask, int f1,
                            int f2, int f3, float* __restrict__ y) {
   const int P = f2 * f3;
@@ -971,11 +998,16 @@ __global__ void k_sub_dev(const float* __restrict__ r, const float* __restrict__
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
     out[c] = fmaf(-om, q[c], r[c]);
 }
+// z (and a second copy z2, the FCG's next direction before its orthogonalisation)
 __global__ void k_twolevel_dev(const float* __restrict__ y, const float* __restrict__ w, const double* scal, int s_yay,
-                               int s_yr, float sc, const uint8_t* __restrict__ smask, int64_t n, float* __restrict__ z) {
+                               int s_yr, float sc, const uint8_t* __restrict__ smask, int64_t n, float* __restrict__ z,
+                               float* __restrict__ z2) {
   const float om = (float)tl_omega(scal, s_yay, s_yr);
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
-    z[c] = smask[c] ? fmaf(om, y[c], sc * w[c]) : 0.f;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const float v = smask[c] ? fmaf(om, y[c], sc * w[c]) : 0.f;
+    z[c] = v;
+    z2[c] = v;
+  }
 }
 // mixed FCG vector kernels (FP32 vectors)
 __global__ void k_fcg_update_f(float* __restrict__ e, float* __restrict__ r, const float* __restrict__ p,
@@ -1084,9 +1116,13 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
   int precond = XF_PRECOND_UNET2, rcode;
   long long launches = 0;   // this library's kernels launched by the solve
   // z = M r in FP32
-  auto apply_m = [&]() -> int {
+  // z = M r in FP32, also into z2 (the next direction's slot)
+  auto apply_m = [&](float* z2) -> int {
     if (precond != XF_PRECOND_UNET2) {
-      return cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+      return cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                     cudaMemcpyAsync(z2, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                 ? XF_OK
+                 : XF_ERR_CUDA;
     }
     if (F == 4)
       k_restrict4<<<dim3((cg->n3 + 63) / 64, cg->n2, cg->n1), 64, 0, s>>>(r, g->n2, g->n3, rc, cg->n1, cg->n2, cg->n3);
@@ -1095,7 +1131,10 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
                                                                          cg->n3);
     int st2 = xf_unet_apply_dev(u, rc, zc);
     if (st2) return st2;
-    if (F == 4)
+    if (F == 4 && (g->n2 * g->n3) % 4 == 0)
+      k_prolong4v<<<dim3((g->n2 * g->n3 / 4 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1,
+                                                                              g->n2, g->n3, y);
+    else if (F == 4)
       k_prolong4<<<dim3((g->n2 * g->n3 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1, g->n2,
                                                                          g->n3, y);
     else
@@ -1109,7 +1148,7 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       xf_cg_poly_first_launch(op, src, dst, tl_f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
       std::swap(src, dst);
     }
-    k_twolevel_dev<<<eb, 256, 0, s>>>(y, src, scal, FS_YAY, FS_YR, (float)tl_scale, g->smask, n, z);
+    k_twolevel_dev<<<eb, 256, 0, s>>>(y, src, scal, FS_YAY, FS_YR, (float)tl_scale, g->smask, n, z, z2);
     launches += 6 + UNET_FORWARD_LAUNCHES + tl_nf;
     return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
   };
@@ -1152,7 +1191,8 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
     bool brk = false;
     while (true) {
       it++;
-      if ((rcode = apply_m())) return fail(rcode, "preconditioner");
+      float *pn = P[head], *qn = Q[head];
+      if ((rcode = apply_m(pn))) return fail(rcode, "preconditioner");
       // (z, r) and (z, A p_j) over the window, one read
       auto dots_z = [&](double* zq) -> int {
         fdot(z, r, FS_ZR);
@@ -1165,11 +1205,10 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       if (!(zq[FS_ZR] > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
         st->fallbacks++;
         XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s));
+        XF_CUDA(ctx, cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s));
         if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
       }
-      // the new direction p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j into ring slot `head`
-      float *pn = P[head], *qn = Q[head];
-      XF_CUDA(ctx, cudaMemcpyAsync(pn, z, n * 4, cudaMemcpyDeviceToDevice, s));
+      // the new direction p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j in ring slot `head` (holding z)
       if (nwin > 0) {
         for (int j = 0; j < nwin; j++) {
           const int sl = (head + m + 1 - 1 - j) % (m + 1);
