@@ -276,7 +276,7 @@ def main():
 
     from xflow_gb300 import capi
 
-    cheb = {"precond": capi.XF_PRECOND_CHEB, "cheb_degree": CHEB_DEGREE}   # the timed solver's preconditioner
+    cheb = {"precond": capi.XF_PRECOND_CHEB, "cheb_degree": CHEB_DEGREE}   # the comparison mixed CG's polynomial
 
     def one(precision, **kw):
         x.fill(0.0)
@@ -399,7 +399,7 @@ def main():
         per_iter = {"cheb_first_fused_f32": 49 / 50, "cheb_middle_f32": (m - 2) + 1 / 50,
                     "cheb_last_f32": 1.0, "pq_fused_f32": 1.0, "xr_update_f32": 1 / 50, "residual_f64": 1 / 50}
     elif "polyr_f32" in kms and "pq_fused_f32" in kms:
-        # the timed solver's path, per chunk of 50: K0 once, K1 and the fused
+        # the degree-2 polynomial path, per chunk of 50: K0 once, K1 and the fused
         # update + K0 49 times, K1 + the update + the FP64 replacement once
         per_iter = {"polyr_f32": 49 / 50, "pq_fused_f32": 1.0, "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50,
                     "residual_f64": 1 / 50}
