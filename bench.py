@@ -5,23 +5,35 @@ Workload (synthetic, seeded): unit cube, 256^3 cells plus a ghost layer
 non-overlapping spheres with radii U[0.02, 0.06] masked Fictive; right-hand
 side = -div of an i.i.d. N(0,1) staggered velocity, projected to zero mean.
 One "step" is one solve from x = 0 to ||b - A x||_2 <= 1e-8 ||b||_2 (true
-FP64 residual).  The timed solver is the learned two-level preconditioner
-under mixed-precision flexible CG: FP32 vectors and stencils, FP64 dots, the
-FP32 recursion refreshed from the true FP64 residual every 50 iterations or
-after a 10^3 drop; preconditioner z = omega y + s p(A)(r - omega A y) with
-y = P U-Net(P^T r) on the coarse grid of 4^3 blocks (BF16 tcgen05
-convolutions) and p the degree-6 Chebyshev polynomial over
-[lmax/20, lmax] as three FP32 two-level stencil passes.  The network is
-trained on the GPU before the timed region, on a 64^3 system of the same
-sphere family (another geometry).  Plain FP64 CG, the unpreconditioned mixed
-CG and the Chebyshev-preconditioned mixed CG without the network (degree
-XF_BENCH_CHEB_DEGREE, default 8) are timed beside it on the same system.
+FP64 residual).
+
+The timed solver is the learned two-level preconditioner under
+mixed-precision flexible CG: FP32 vectors and stencils, FP64 dots, the FP32
+recursion refreshed from the true FP64 residual every 50 iterations or after
+a 10^3 drop of its residual norm; preconditioner
+z = omega y + s p(A)(r - omega A y) with y = P U-Net(P^T r) on the coarse
+grid of 4^3 blocks (BF16 tcgen05 convolutions) and p the degree-6 Chebyshev
+polynomial over [lmax/20, lmax] as three FP32 two-level stencil passes.  The
+network is trained on the GPU before the timed region, on a 64^3 system of
+the same sphere family (another geometry).  After the timed region: the same
+solver to 1e-10, plain FP64 CG (the metric's comparator), the
+unpreconditioned mixed CG and the Chebyshev-preconditioned mixed CG without
+the network on the same system, and the CPU baseline: one full FP64 CG solve
+on all host cores (`cpu_baseline`, measured), whose solution the timed
+result is compared with.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xflow|reference]
+    python bench.py --rows       # the other rows of the path at their sizes
+    python bench.py --learned    # the U-Net as a full-resolution preconditioner
+    python bench.py --size 64 --maxit 10 --steps 1 --warmup 1   # bounded run for launch lists
+
+`--impl reference`: every step is one full FP64 CG solve of the same system
+on the host cores (the CPU restatement of the reference's operator rows).
 
 Multi-GPU: the path is one solve per GPU ("replicas only"); N ranks each solve
 their own copy and `value` is the aggregate ms per solve (max-over-ranks time
-divided by all ranks' solves).
+divided by all ranks' solves).  `--gpus N` outside torchrun starts the N
+ranks itself.
 """
 import argparse
 import json
@@ -29,7 +41,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -42,14 +53,13 @@ N_CELLS = 256
 N_SPHERES = 64
 SEED = 20261203
 RTOL = 1e-8
-CHEB_DEGREE = int(os.environ.get("XF_BENCH_CHEB_DEGREE", "8"))   # degree of the polynomial preconditioner
-CHEB_RATIO = {2: 30, 4: 120}.get(CHEB_DEGREE, 250)                # its default lambda_max / lambda_min
-CALIB = os.path.join(ROOT, "profiles", "bench_calibration.json")
+CHEB_DEGREE = 8     # degree of the comparison mixed CG's polynomial preconditioner
+CHEB_RATIO = 250    # its lambda_max / lambda_min
 # the timed solver: learned two-level preconditioner under mixed-precision FCG
 TL_BLOCK = 4     # coarse cells are 4^3 blocks of the fine interior
-TL_DEGREE = int(os.environ.get("XF_BENCH_TL_DEGREE", "6"))  # smoothing polynomial degree (TL_DEGREE / 2 passes)
-TL_RATIO = int(os.environ.get("XF_BENCH_TL_RATIO", "20"))   # its lambda_max / lambda_min
-TL_WINDOW = int(os.environ.get("XF_BENCH_TL_WINDOW", "1"))  # FCG window
+TL_DEGREE = 6    # smoothing polynomial degree (TL_DEGREE / 2 passes)
+TL_RATIO = 20    # its lambda_max / lambda_min
+TL_WINDOW = 1    # FCG window
 
 
 def workload(n=N_CELLS):
@@ -162,102 +172,124 @@ def replica_value(dist, per_step_ms, world):
 
 
 # ---------------------------------------------------------------------------
-def cpu_baseline(codes, sep, b, fp64_iters, sample_iters=10):
-    """The oracle port's plain FP64 CG on this machine's host cores: a bounded
-    sample of `sample_iters` iterations at full size, extrapolated to the
-    iteration count plain FP64 CG needs on this system."""
+def cpu_fp64_solve(codes, sep, b, threads):
+    """One plain FP64 CG solve of the system on the host cores, from x = 0 to
+    the bench's relative tolerance: the oracle's restatement of the
+    reference's operator rows (T3dLaplaceOperator, XOperator.cpp:938-1129) in
+    a Hestenes-Stiefel CG, OpenMP over `threads` host threads.  Returns
+    (solution, ms, iterations, relative residual)."""
     from oracle import oracle as O
 
-    threads = os.cpu_count() or 1
     O.set_threads(threads)
     g = O.Grid(codes, np.zeros(codes.shape + (3,)), sep, sep, sep)
     t0 = time.perf_counter()
-    _, st = O.cg_plain(O.LAPLACE, g, np.zeros(codes.shape), b, 1e-30, maxit=sample_iters)
-    dt = time.perf_counter() - t0
+    x, st = O.cg_plain(O.LAPLACE, g, np.zeros(codes.shape), b, RTOL)
+    ms = (time.perf_counter() - t0) * 1e3
     O.set_threads(1)
-    per_it = dt * 1e3 / max(1, st.iterations)
-    return {"value": per_it * fp64_iters, "unit": "ms", "cores": threads, "kind": "port",
-            "sample": f"{st.iterations} FP64 CG iterations at 256^3 (incl. setup of the first residual), "
-                      f"{per_it:.1f} ms/iteration x {fp64_iters} iterations (extrapolated)"}
+    return x, ms, st.iterations, st.resid
+
+
+def cpu_one_thread_iteration_ms(codes, sep, b, iters=3):
+    """Per-iteration cost of the same CPU CG on one host thread: a bounded
+    sample (`iters` iterations after the set-up, which is timed apart)."""
+    from oracle import oracle as O
+
+    O.set_threads(1)
+    g = O.Grid(codes, np.zeros(codes.shape + (3,)), sep, sep, sep)
+    t0 = time.perf_counter()
+    O.cg_plain(O.LAPLACE, g, np.zeros(codes.shape), b, 1e-30, maxit=1)
+    t1 = time.perf_counter()
+    O.cg_plain(O.LAPLACE, g, np.zeros(codes.shape), b, 1e-30, maxit=1 + iters)
+    t2 = time.perf_counter()
+    return ((t2 - t1) - (t1 - t0)) * 1e3 / iters
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 def reference_arm(args):
+    """The reference's CPU path on this machine's host cores: every step is one
+    full FP64 CG solve of the bench's system to the bench's tolerance (the
+    oracle restatement of the reference's operator rows, all host threads);
+    warm-up steps are the same solve, untimed."""
     world, rank, local, dist = dist_init()
     if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
         return 0
-    codes, sep, b = workload()
-    iters = None
-    if os.path.exists(CALIB):
-        iters = json.load(open(CALIB)).get("fp64_cg_iterations")
-    if iters is None:
-        iters = 1000
-        note = " (iteration count not calibrated: 1000 assumed)"
-    else:
-        note = ""
-    vals = []
+    codes, sep, b = workload(args.size)
+    threads = host_threads()
+    vals, its, res = [], [], []
     for k in range(args.warmup + args.steps):
-        cb = cpu_baseline(codes, sep, b, iters, sample_iters=4)
+        _, ms, it, rel = cpu_fp64_solve(codes, sep, b, threads)
         if k >= args.warmup:
-            vals.append(cb["value"])
+            vals.append(ms)
+            its.append(it)
+            res.append(rel)
     v = float(np.mean(vals))
-    cb["value"] = v
-    cb["sample"] += note
-    line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(N_CELLS),
-                       "solver": "plain FP64 CG, oracle CPU port, all host cores"},
-            "impl": "reference", "cpu_baseline": cb,
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": bench_config(args.size),
+            "impl": "reference",
+            "solver": f"plain FP64 CG on the host cores (oracle restatement of the reference's operator rows, "
+                      f"OpenMP, {threads} threads), from x = 0 to the true relative residual {RTOL:g}",
+            "iterations": its[-1], "rel_resid": res[-1], "ranks_with_work": 1,
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+                             "sample": f"measured: {args.steps} full solves at {args.size}^3 "
+                                       f"({its[-1]} iterations each), mean ms per solve; nproc {os.cpu_count()}"},
             "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
     return 0
 
 
+def bench_config(size):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": workload_name(size), "rtol": RTOL,
+            "l2": "working set > 129 MB L2 (no flush needed)"}
+
+
+def relaunch(args, argv):
+    """`--gpus N` (N > 1) outside torchrun: start N ranks of this script with
+    torch.distributed.run on 127.0.0.1 and return their exit status (rank 0
+    prints the line)."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + list(argv)
+    return subprocess.run(cmd).returncode
+
+
 # ---------------------------------------------------------------------------
-def main():
+def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xflow", choices=["xflow", "reference"])
-    ap.add_argument("--size", type=int, default=N_CELLS)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", type=int, default=N_CELLS, help="interior cells per axis (a multiple of 16)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline solve")
+    ap.add_argument("--maxit", type=int, default=0,
+                    help="cap the timed solver's iterations (a bounded command for launch lists; no bench line)")
     ap.add_argument("--learned", action="store_true",
                     help="train the U-Net preconditioner and time it and its flexible CG at full size")
-    ap.add_argument("--learned-applies-only", action="store_true", help="with --learned: no solves")
-    ap.add_argument("--learned-max-its", type=int, default=0, help="with --learned: cap of the learned solve")
-    ap.add_argument("--two-level", action="store_true",
-                    help="time the learned two-level preconditioner (U-Net coarse solver + Chebyshev smoothing)")
-    ap.add_argument("--two-level-profile", action="store_true",
-                    help="with --two-level: one 10-iteration solve with untrained weights (for a launch list)")
-    ap.add_argument("--two-level-sweep",
-                    default="8:60:2:32,8:60:2:64,8:60:1:32,8:250:2:32,8:30:2:32,4:60:2:32,4:30:2:32,12:60:2:32",
-                    help="with --two-level: smoothing degree:ratio:FCG window:vector bits (32 mixed, 64) entries")
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
-    ap.add_argument("--unet-applies", type=int, default=0,
-                    help="apply a random-initialised U-Net this many times to the bench's right-hand side (a bounded "
-                         "command for per-layer launch lists)")
-    ap.add_argument("--probes", action="store_true",
-                    help="tcgen05.mma issue rate versus N and the FP64 / FP32 FMA rates (one JSON line each)")
-    ap.add_argument("--degrees", default="",
-                    help="degree:ratio pairs (e.g. 4:120,8:250): one JSON line per preconditioner, best of 3 solves")
-    ap.add_argument("--kernels-only", action="store_true",
-                    help="a few launches of each hot kernel on the full grid (for ncu captures)")
-    args = ap.parse_args()
+    argv = sys.argv[1:] if argv is None else argv
+    args = ap.parse_args(argv)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch(args, argv)
     if args.impl == "reference":
         return reference_arm(args)
-    if args.kernels_only:
-        return kernels_only(args)
-    if args.degrees:
-        return degrees(args)
-    if args.unet_applies > 0:
-        return unet_applies(args)
-    if args.probes:
-        return probes(args)
-    if args.two_level:
-        return two_level(args)
     if args.rows:
         return rows(args)
     if args.learned:
@@ -275,44 +307,31 @@ def main():
     ncell = int(np.prod(g.shape))
 
     from xflow_gb300 import capi
-
-    cheb = {"precond": capi.XF_PRECOND_CHEB, "cheb_degree": CHEB_DEGREE}   # the comparison mixed CG's polynomial
-
-    def one(precision, **kw):
-        x.fill(0.0)
-        return xf.solve(A, x, bv, method=xf.XF_CG, precision=precision, rtol=RTOL, **kw)
-
-    # FP64 plain CG: the comparison point of the metric
-    one(xf.XF_PREC_FP64)
-    st64 = one(xf.XF_PREC_FP64)
-    x64 = x.download()
-    fp64_ms = st64.ms
-    fp64_iters = st64.iterations
-
-    # unpreconditioned mixed CG, beside it
-    one(xf.XF_PREC_MIXED)
-    st_plain = one(xf.XF_PREC_MIXED)
-
-    # the Chebyshev-preconditioned mixed CG (the same smoother, no network), beside it
-    one(xf.XF_PREC_MIXED, **cheb)
-    cheb_sts = [one(xf.XF_PREC_MIXED, **cheb) for _ in range(args.steps)]
+    from xflow_gb300 import workloads as wl
 
     # The timed solver: the learned two-level preconditioner under mixed-precision
     # FCG.  The U-Net is trained first (outside the timed region: once per
     # geometry family) on a 64^3 system of the sphere family, then runs on the
     # coarse grid of 4^3 blocks of this system.
-    from xflow_gb300 import workloads as wl
-
     params, train = train_unet(ctx)
     cc, s1, s2, s3 = wl.coarse_grid(codes, sep, TL_BLOCK)
     gc = xf.Grid(ctx, cc, s1, s2, s3, None)
     net = xf.UNet(gc, params)
 
-    def learned_solve(zero=True):
+    def learned_solve(zero=True, rtol=RTOL, maxit=0):
         if zero:
             x.fill(0.0)
-        return xf.solve_fcg(A, x, bv, unet=net, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, window=TL_WINDOW,
-                            degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED)
+        return xf.solve_fcg(A, x, bv, unet=net, precond=capi.XF_PRECOND_UNET2, rtol=rtol, window=TL_WINDOW,
+                            degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED, maxit=maxit)
+
+    if args.maxit > 0:   # bounded command for launch lists and ncu captures
+        for _ in range(args.warmup + args.steps):
+            st = learned_solve(maxit=args.maxit)
+        ctx.synchronize()
+        print(json.dumps({"mode": "bounded timed-solver run", "workload": workload_name(args.size),
+                          "maxit": args.maxit, "iterations": st.iterations, "launches_per_solve": int(st.reserved[0]),
+                          "status": int(st.status)}))
+        return 0
 
     for _ in range(args.warmup):
         learned_solve()
@@ -358,6 +377,28 @@ def main():
             e2e.append((t2 - t1) * 1e3)
         assert s2.status == 0
     e2e_ms = replica_value(dist, e2e, world)
+
+    # The same solver to the config's outer-refinement tolerance, 1e-10 (once, after the timed region)
+    st10 = learned_solve(rtol=1e-10)
+    x10 = x.download()
+
+    # Comparison solvers on the same system (after the timed region): plain
+    # FP64 CG (the metric's comparator), unpreconditioned mixed CG, and the
+    # Chebyshev-preconditioned mixed CG without the network.
+    cheb = {"precond": capi.XF_PRECOND_CHEB, "cheb_degree": CHEB_DEGREE}
+
+    def one(precision, **kw):
+        x.fill(0.0)
+        return xf.solve(A, x, bv, method=xf.XF_CG, precision=precision, rtol=RTOL, **kw)
+
+    one(xf.XF_PREC_FP64)
+    st64 = one(xf.XF_PREC_FP64)
+    x64 = x.download()
+    one(xf.XF_PREC_MIXED)
+    st_plain = one(xf.XF_PREC_MIXED)
+    one(xf.XF_PREC_MIXED, **cheb)
+    cheb_sts = [one(xf.XF_PREC_MIXED, **cheb) for _ in range(3)]
+
     # one coarse network application, CUDA events on the context stream
     stream = torch.cuda.ExternalStream(capi_stream(ctx))
     rc, zc = gc.vec(np.zeros(gc.shape)), gc.vec(None)
@@ -372,9 +413,9 @@ def main():
     unet_ms = ev0.elapsed_time(ev1) / 10
     unet_ex, _ = unet_flops(gc.shape)
 
-    # Roofline: each kernel of the mixed CG iteration timed alone (CUDA events
-    # on its launching stream, the solver's own launch configuration), with
-    # its compulsory bytes per box cell; the dominant one by share of the
+    # Roofline: each stencil kernel timed alone (CUDA events on its launching
+    # stream, the solver's own launch configuration), with its compulsory
+    # bytes per box cell; the one with the largest share of the timed
     # iteration is the headline.
     kms = xf.profile_cg_kernels(A, reps=20)
     # compulsory bytes per box cell: pq_fused_f32 reads z (or r), p, kind and
@@ -384,33 +425,14 @@ def main():
     bpc = {"stencil_f32": 9, "xr_update_f32": 24, "p_update_f32": 12, "residual_f64": 29, "stencil_f64": 25,
            "pq_fused_f32": 17, "pq_march_f32": 17, "poly2_f32": 9, "polyr_f32": 29,
            "cheb_first_fused_f32": 29, "cheb_last_f32": 13, "cheb_middle_f32": 9}
-    if "cheb_middle_f32" in kms and "stencil_f32" in kms:
-        # the learned two-level iteration: the smoother's TL_DEGREE / 2 factor
-        # passes (each the middle-pass kernel, w' = p_k(A) w), and two FP32
-        # stencils with a dot (A y of the coarse correction, A p)
-        per_iter = {"cheb_middle_f32": TL_DEGREE // 2, "stencil_f32": 2.0}
-    elif "cheb_first_fused_f32" in kms and "pq_fused_f32" in kms and CHEB_DEGREE >= 4:
-        # per chunk of 50: the passes of the m = degree / 2 factors once (the
-        # first without the update: timed as a middle pass, the same work),
-        # then K1, the first pass with the update, m - 2 middle passes and
-        # the last pass 49 times, and K1 + the update + the FP64 replacement
-        # once
-        m = CHEB_DEGREE // 2
-        per_iter = {"cheb_first_fused_f32": 49 / 50, "cheb_middle_f32": (m - 2) + 1 / 50,
-                    "cheb_last_f32": 1.0, "pq_fused_f32": 1.0, "xr_update_f32": 1 / 50, "residual_f64": 1 / 50}
-    elif "polyr_f32" in kms and "pq_fused_f32" in kms:
-        # the degree-2 polynomial path, per chunk of 50: K0 once, K1 and the fused
-        # update + K0 49 times, K1 + the update + the FP64 replacement once
-        per_iter = {"polyr_f32": 49 / 50, "pq_fused_f32": 1.0, "poly2_f32": 1 / 50, "xr_update_f32": 1 / 50,
-                    "residual_f64": 1 / 50}
-    elif "pq_fused_f32" in kms:
-        per_iter = {"pq_fused_f32": 1.0, "xr_update_f32": 1.0, "residual_f64": 1.0 / 50}
-    else:
-        per_iter = {"stencil_f32": 1.0, "xr_update_f32": 1.0, "p_update_f32": 1.0, "residual_f64": 1.0 / 50}
+    # the learned two-level iteration: the smoother's TL_DEGREE / 2 factor
+    # passes (each the middle-pass kernel, w' = p_k(A) w), and two FP32
+    # stencils with a dot (A y of the coarse correction, A p)
+    per_iter = {"cheb_middle_f32": TL_DEGREE // 2, "stencil_f32": 2.0}
     peak, peak_kind = peaks()
     kernels = {k: {"ms": kms[k], "bytes_per_cell": bpc[k], "GB_s": ncell * bpc[k] / (kms[k] * 1e-3) / 1e9,
                    "frac": ncell * bpc[k] / (kms[k] * 1e-3) / 1e9 / peak} for k in kms}
-    share = {k: kms[k] * w for k, w in per_iter.items()}
+    share = {k: kms[k] * w for k, w in per_iter.items() if k in kms}
     dom = max(share, key=share.get)
     alg_bytes = ncell * bpc[dom]
     mv_ms = kms[dom]
@@ -420,50 +442,62 @@ def main():
     if os.path.exists(prof):
         traffic = json.load(open(prof)).get(dom)
 
-    # FP64 error of the timed result: against the FP64 CG solution, and its
-    # true residual recomputed by the CPU oracle in FP64.
-    sm = codes != 0
+    # FP64 error of the timed result: against the FP64 GPU CG solution and the
+    # FP64 CPU solve, both as the max-norm of the zero-mean difference over the
+    # solution's zero-mean range (the all-Neumann system fixes x up to a
+    # constant); its true residual recomputed by the CPU oracle in FP64.
     act = np.isin(codes, (1, 4, 5, 6, 8))
-    d = (xm - xm[act].mean()) - (x64 - x64[act].mean())
-    err_vs_fp64 = float(np.abs(d[act]).max() / np.abs(x64[act] - x64[act].mean()).max())
-    oracle_resid = None
+
+    def rel_err(xa, xb):
+        d = (xa - xa[act].mean()) - (xb - xb[act].mean())
+        return float(np.abs(d[act]).max() / np.abs(xb[act] - xb[act].mean()).max())
+
+    err_vs_fp64 = rel_err(xm, x64)
+    oracle_resid = oracle_resid10 = None
     cpu = None
+    cpu_extra = {}
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
 
-        O.set_threads(os.cpu_count() or 1)
+        threads = host_threads()
+        O.set_threads(threads)
         og = O.Grid(codes, np.zeros(codes.shape + (3,)), sep, sep, sep)
         r = O.apply(O.LAPLACE, og, xm, b, -1)
         oracle_resid = float(np.linalg.norm(r[act]) / np.linalg.norm(b[act]))
+        r = O.apply(O.LAPLACE, og, x10, b, -1)
+        oracle_resid10 = float(np.linalg.norm(r[act]) / np.linalg.norm(b[act]))
         O.set_threads(1)
-        cpu = cpu_baseline(codes, sep, b, fp64_iters)
-        os.makedirs(os.path.dirname(CALIB), exist_ok=True)
-        try:
-            json.dump({"workload": "256^3 spheres, seed %d" % SEED, "fp64_cg_iterations": fp64_iters,
-                       "timed_solver_iterations": st_last.iterations}, open(CALIB, "w"))
-        except OSError:
-            pass
+        xc, cms, cit, crel = cpu_fp64_solve(codes, sep, b, threads)
+        one_ms = cpu_one_thread_iteration_ms(codes, sep, b)
+        cpu = {"value": cms, "unit": "ms", "cores": threads, "kind": "port",
+               "sample": f"measured: one full FP64 CG solve at {args.size}^3 from x = 0 to {RTOL:g} "
+                         f"({cit} iterations, true relative residual {crel:.3g}; oracle restatement of the "
+                         f"reference's operator rows, OpenMP, {threads} threads; nproc {os.cpu_count()})"}
+        cpu_extra = {"cpu_fp64_one_thread_ms_per_iteration": one_ms,
+                     "cpu_fp64_one_thread_note": "per-iteration cost on 1 host thread, 3 iterations (bounded sample)",
+                     "err_vs_cpu_fp64": rel_err(xm, xc), "err_1e10_vs_cpu_fp64": rel_err(x10, xc)}
 
     line = {
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 vectors and stencils, bf16 network (fp32 accumulate), f64 dots/scalars/residual refresh",
         "data": "synthetic",
-        "config": {"workload": workload_name(args.size),
-                   "solver": (f"mixed-precision flexible CG, FCG({TL_WINDOW}) (FP32 vectors and stencils, FP64 dots, "
-                              "true FP64 residual refresh every 50 iterations or after a 10^3 drop)"),
-                   "preconditioner": (f"learned two-level: 3-level U-Net (16/32/64 channels, BF16 tcgen05 "
-                                      f"convolutions) on the coarse grid of {TL_BLOCK}^3 blocks as the coarse solver, "
-                                      f"degree-{TL_DEGREE} Chebyshev smoothing over [lmax/{TL_RATIO}, lmax] as "
-                                      f"{TL_DEGREE // 2} FP32 two-level stencil passes"),
-                   "training": (f"on the GPU before the timed region: {train['steps']} Adam steps on "
-                                f"{train['pairs']} (residual, error) pairs from plain CG on a {train['grid']} system"),
-                   "rtol": RTOL,
-                   "l2": "working set ~0.6 GB > 129 MB L2 (no flush needed)",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(args.size),
+        "solver": (f"mixed-precision flexible CG, FCG({TL_WINDOW}) (FP32 vectors and stencils, FP64 dots, "
+                   "true FP64 residual refresh every 50 iterations or after a 10^3 drop of the residual norm)"),
+        "preconditioner": (f"learned two-level: 3-level U-Net (16/32/64 channels, BF16 tcgen05 "
+                           f"convolutions) on the coarse grid of {TL_BLOCK}^3 blocks as the coarse solver, "
+                           f"degree-{TL_DEGREE} Chebyshev smoothing over [lmax/{TL_RATIO}, lmax] as "
+                           f"{TL_DEGREE // 2} FP32 two-level stencil passes"),
+        "training": (f"on the GPU before the timed region: {train['steps']} Adam steps on "
+                     f"{train['pairs']} (residual, error) pairs from plain CG on a {train['grid']} system"),
+        "parallelism": f"replicas x{world}",
         "iterations": st_last.iterations, "replacements": st_last.replacements, "rel_resid": st_last.rel_resid,
+        "fallbacks": st_last.fallbacks,
         "oracle_rel_resid": oracle_resid, "err_vs_fp64_cg": err_vs_fp64,
-        "fp64_cg_ms": fp64_ms, "fp64_cg_iterations": fp64_iters, "fp64_cg_rel_resid": st64.rel_resid,
+        "refine_1e10": {"ms": st10.ms, "iterations": st10.iterations, "rel_resid": st10.rel_resid,
+                        "oracle_rel_resid": oracle_resid10, "status": int(st10.status)},
+        "fp64_cg_ms": st64.ms, "fp64_cg_iterations": st64.iterations, "fp64_cg_rel_resid": st64.rel_resid,
         "mixed_cg_unpreconditioned": {"ms": st_plain.ms, "iterations": st_plain.iterations,
                                       "rel_resid": st_plain.rel_resid},
         "mixed_cg_chebyshev": {"ms": float(np.mean([c.ms for c in cheb_sts])), "iterations": cheb_sts[-1].iterations,
@@ -472,7 +506,7 @@ def main():
         "train": train,
         "coarse_unet": {"grid": f"{gc.shape[0] - 2}^3 (+ ghost layer)", "ms_per_apply": unet_ms,
                         "tflops_executed": unet_ex / (unet_ms * 1e-3) / 1e12},
-        "speedup_vs_fp64_cg": fp64_ms / value if value > 0 else None,
+        "speedup_vs_fp64_cg": st64.ms / value if value > 0 else None,
         "wall_ms_per_step": wall / args.steps,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ncell * 8, "d2h_bytes_per_step": ncell * 8},
         "gpu_launches": launches,
@@ -484,115 +518,11 @@ def main():
     }
     if cpu:
         line["cpu_baseline"] = cpu
+        line.update(cpu_extra)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
-    return 0
-
-
-def probes(args):
-    """The measurements behind two design decisions: cycles per tcgen05.mma
-    versus N (1, 2, 4 CTAs per SM; both operand layouts) and the FP64 / FP32
-    FMA rates."""
-    import torch
-
-    import xflow_gb300 as xf
-
-    ctx = xf.Context(0)
-    sms = torch.cuda.get_device_properties(0).multi_processor_count
-    for layout in (0, 1):
-        for n in (16, 32, 64, 128, 256):
-            for cps in (1, 2, 4):
-                if (32 if n <= 32 else n) * cps > 512:
-                    continue
-                cyc = xf.probe_mma_rate(ctx, n, cps, layout)
-                flop_clk = 2.0 * 128 * n * 16 / cyc
-                print(json.dumps({"probe": "tcgen05.mma kind::f16 M=128 K=16", "layout": layout, "n": n,
-                                  "ctas_per_sm": cps, "cycles_per_mma": cyc, "flop_per_clock_per_sm": flop_clk,
-                                  "tflops_at_2070mhz": flop_clk * 2.07e9 * sms / 1e12}), flush=True)
-    for fp64 in (1, 0):
-        print(json.dumps({"probe": "FMA chains", "dtype": "f64" if fp64 else "f32",
-                          "tflops": xf.probe_fma_rate(ctx, fp64)}), flush=True)
-    return 0
-
-
-def unet_applies(args):
-    """K applications of a random-initialised U-Net (the learned
-    preconditioner's network; weights do not change its time) to the bench's
-    right-hand side: device ms per application."""
-    import torch
-
-    import xflow_gb300 as xf
-
-    codes, sep, b = workload(args.size)
-    ctx = xf.Context(0)
-    stream = torch.cuda.ExternalStream(capi_stream(ctx))
-    g = xf.Grid(ctx, codes, sep, sep, sep, None)
-    net = xf.UNet(g, seed=1)
-    bv, z = g.vec(b), g.vec(None)
-    net.apply(bv, z)
-    ctx.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.unet_applies):
-        net.apply(bv, z)
-    e1.record(stream)
-    e1.synchronize()
-    print(json.dumps({"mode": "U-Net applications", "workload": workload_name(args.size),
-                      "applications": args.unet_applies, "ms_per_application": e0.elapsed_time(e1) / args.unet_applies}))
-    return 0
-
-
-def degrees(args):
-    """The timed solve with other degrees and intervals of the Chebyshev
-    preconditioner: iterations, true residual and device ms (best of 3)."""
-    import xflow_gb300 as xf
-    from xflow_gb300 import capi
-
-    codes, sep, b = workload(args.size)
-    ctx = xf.Context(0)
-    g = xf.Grid(ctx, codes, sep, sep, sep, None)
-    A = xf.Operator(g, xf.XF_OP_LAPLACE)
-    bv, x = g.vec(b), g.vec(np.zeros(g.shape))
-    for pair in args.degrees.split(","):
-        deg, ratio = (int(v) for v in pair.split(":"))
-        ms = []
-        for _ in range(3):
-            x.fill(0.0)
-            st = xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_MIXED, rtol=RTOL,
-                          precond=capi.XF_PRECOND_CHEB, cheb_degree=deg, cheb_ratio=ratio)
-            assert st.status == 0, st.status
-            ms.append(st.ms)
-        print(json.dumps({"degree": deg, "ratio": ratio, "iterations": st.iterations, "rel_resid": st.rel_resid,
-                          "ms": min(ms)}), flush=True)
-    return 0
-
-
-def kernels_only(args):
-    """Three launches of the FP32 and FP64 stencils and 32 iterations of the
-    preconditioned mixed, plain mixed and FP64 CG on the full workload: a
-    bounded command for ncu."""
-    import xflow_gb300 as xf
-
-    codes, sep, b = workload(args.size)
-    ctx = xf.Context(0)
-    g = xf.Grid(ctx, codes, sep, sep, sep, None)
-    A = xf.Operator(g, xf.XF_OP_LAPLACE)
-    rng = np.random.Generator(np.random.PCG64(1))
-    xh = rng.standard_normal(g.shape)
-    for dt in (xf.XF_F32, xf.XF_F64):
-        p, q = g.vec(xh, dt), g.vec(None, dt)
-        for _ in range(3):
-            A.apply(p, q, flags=xf.XF_ZERO_INACTIVE)
-    bv = g.vec(b)
-    from xflow_gb300 import capi
-
-    for prec, pre in ((xf.XF_PREC_MIXED, capi.XF_PRECOND_CHEB), (xf.XF_PREC_MIXED, None), (xf.XF_PREC_FP64, None)):
-        x = g.vec(np.zeros(g.shape))
-        st = xf.solve(A, x, bv, method=xf.XF_CG, precision=prec, rtol=RTOL, maxit=32, precond=pre)
-        print(f"precision {prec} preconditioner {pre}: {st.iterations} iterations, {st.ms:.2f} ms, status {st.status}")
-    ctx.synchronize()
     return 0
 
 
@@ -805,78 +735,6 @@ def train_unet(ctx):
     return net.params(), {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
                           "steps": T["steps"], "lr": T["lr"], "s": t2 - t1, "harvest_s": t1 - t0,
                           "anorm_loss_before": first, "anorm_loss_after": last}
-
-
-def two_level(args):
-    """The learned two-level preconditioner at the bench's 256^3 system: the
-    U-Net trained as for --learned (64^3 sphere family, another geometry) runs
-    on the coarse grid of 4^3 blocks (64^3) as the coarse solver, the FP32
-    Chebyshev passes smooth, and FCG(window) drives both.  Prints one JSON
-    line: training, the coarse application time, and per window the
-    iterations and ms of the solve to a true 1e-8 relative residual, beside
-    the untrained network and plain FP64 CG."""
-    import torch
-
-    import xflow_gb300 as xf
-    from xflow_gb300 import capi
-    from xflow_gb300 import workloads as wl
-
-    ctx = xf.Context(0)
-    stream = torch.cuda.ExternalStream(capi_stream(ctx))
-    if args.two_level_profile:   # launch list of a short solve: untrained weights (the same kernels), 10 iterations
-        codes, sep, b = workload(args.size)
-        g = xf.Grid(ctx, codes, sep, sep, sep, None)
-        cc, s1, s2, s3 = wl.coarse_grid(codes, sep, TL_BLOCK)
-        gc = xf.Grid(ctx, cc, s1, s2, s3, None)
-        net = xf.UNet(gc, seed=1)
-        A = xf.Operator(g)
-        for maxit in (2, 10):
-            x = g.vec(np.zeros(g.shape))
-            st = xf.solve_fcg(A, x, g.vec(b), unet=net, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, maxit=maxit,
-                              window=TL_WINDOW, degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED)
-            print(json.dumps({"mode": "two-level profile", "maxit": maxit, "iterations": st.iterations,
-                              "ms": st.ms, "launches": int(st.reserved[0]), "status": int(st.status)}))
-        return 0
-    params, train = train_unet(ctx)
-    codes, sep, b = workload(args.size)
-    g = xf.Grid(ctx, codes, sep, sep, sep, None)
-    A = xf.Operator(g)
-    cc, s1, s2, s3 = wl.coarse_grid(codes, sep, 4)
-    gc = xf.Grid(ctx, cc, s1, s2, s3, None)
-    net = xf.UNet(gc, params)
-    bv = g.vec(b)
-    rc, zc = gc.vec(np.zeros(gc.shape)), gc.vec(None)
-    for _ in range(3):
-        net.apply(rc, zc)
-    ctx.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(10):
-        net.apply(rc, zc)
-    e1.record(stream)
-    e1.synchronize()
-    line = {"mode": "learned two-level preconditioner", "workload": f"{args.size}^3 spheres system (the bench's)",
-            "coarse_grid": f"{gc.shape[0] - 2}^3 blocks of 4^3", "train": train,
-            "coarse_unet_apply_ms": e0.elapsed_time(e1) / 10, "solves": {}}
-    sweep = [tuple(int(v) for v in c.split(":")) for c in args.two_level_sweep.split(",")]
-    fresh = xf.UNet(gc, seed=1)
-    for label, nn in (("trained", net), ("untrained", fresh)):
-        for deg, ratio, w, bits in sweep if nn is net else sweep[:1]:
-            prec = xf.XF_PREC_MIXED if bits == 32 else xf.XF_PREC_FP64
-            best = None
-            for _ in range(2):
-                x = g.vec(np.zeros(g.shape))
-                st = xf.solve_fcg(A, x, bv, unet=nn, precond=capi.XF_PRECOND_UNET2, rtol=RTOL, window=w,
-                                  degree=deg, ratio=ratio, precision=prec)
-                if best is None or st.ms < best["ms"]:
-                    best = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid,
-                            "status": int(st.status), "fallbacks": st.fallbacks, "refreshes": st.replacements}
-            line["solves"][f"{label} degree {deg} ratio {ratio} window {w} fp{bits}"] = best
-    x = g.vec(np.zeros(g.shape))
-    st = xf.solve(A, x, bv, method=xf.XF_CG, rtol=RTOL)
-    line["plain_fp64_cg"] = {"iterations": st.iterations, "ms": st.ms, "rel_resid": st.rel_resid}
-    print(json.dumps(line))
-    return 0
 
 
 def learned(args):

@@ -505,17 +505,6 @@ int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
  * results differ. */
 int xf_selftest_division(xf_ctx* ctx, long long n, unsigned long long seed, long long* mismatches);
 
-/* No counterpart in the reference (measurement probes behind design
- * decisions).  xf_probe_mma_rate: clock cycles per tcgen05.mma (M = 128,
- * K = 16, BF16 in, FP32 in TMEM) of width n (16, 32, 64, 128 or 256) issued
- * back to back by one thread per CTA, ctas_per_sm CTAs per SM (n columns x
- * CTAs <= 512), operands resident in shared memory in layout 0 (no-swizzle
- * K-major, LBO 128 B, SBO 1 KB) or 1 (column of chunks).  xf_probe_fma_rate:
- * TFLOP/s of eight independent FMA chains per thread, FP64 (fp64 = 1) or
- * FP32. */
-int xf_probe_mma_rate(xf_ctx* ctx, int n, int ctas_per_sm, int layout, double* cycles_per_mma);
-int xf_probe_fma_rate(xf_ctx* ctx, int fp64, double* tflops);
-
 /* ---- allocation-free inner product --------------------------------------- */
 /* No counterpart in the reference (which has no device memory at all).
  * The masked FP64 dot of xf_dot, sum over c < n with d_mask[c] != 0 (d_mask
@@ -531,8 +520,9 @@ int xf_probe_fma_rate(xf_ctx* ctx, int fp64, double* tflops);
  * until exit.  n beyond XF_NOALLOC_MAX_ELEMS returns XF_ERR_ARG.  Calls share
  * that scratch, so calls that overlap on the GPU race; calls ordered on one
  * stream do not.  The first call on a device resolves the scratch address
- * (cudaGetSymbolAddress, that device current): make it before any stream
- * capture. */
+ * (cudaGetSymbolAddress, that device current) and keeps it: make that call
+ * before any stream capture, and restart the process after a
+ * cudaDeviceReset before calling again. */
 #define XF_NOALLOC_MAX_ELEMS (8192LL * 256LL * 16LL)
 int xf_dot_noalloc(const double* d_a, const double* d_b, const uint8_t* d_mask, int64_t n, double* d_out,
                    void* stream);

@@ -500,9 +500,77 @@ int xfo_minres_reference(int op, const int32_t* codes, const double* normals, co
   return XFO_OK;
 }
 
+/* Laplace grids whose active cells are all Actual (XOperator.cpp:994-1019)
+ * and interior: the flux-form rows of lap_row, written as straight-line code
+ * over k (each row the same divisions and roundings as lap_row; Fictive
+ * neighbours select a zero flux), y = 0 on other cells, and (p, y) summed on
+ * the way.  One OpenMP team over i planes; the k loop vectorises (IEEE
+ * division in every lane). */
+static int all_actual_interior(const sys_t* S) {
+  if (S->op != XFO_OP_LAPLACE) return 0;
+  const xfo_grid* g = &S->g;
+  for (int i = 0; i < g->n1; i++)
+    for (int j = 0; j < g->n2; j++)
+      for (int k = 0; k < g->n3; k++) {
+        const int64_t c = ((int64_t)i * g->n2 + j) * g->n3 + k;
+        if (!S->smask[c]) continue;
+        if (g->codes[c] != ACT) return 0;
+        if (i == 0 || j == 0 || k == 0 || i == g->n1 - 1 || j == g->n2 - 1 || k == g->n3 - 1) return 0;
+      }
+  return 1;
+}
+
+static double lap_actual_sweep(const sys_t* S, const double* f, double* y, const double* hz2) {
+  const xfo_grid* g = &S->g;
+  const int n1 = g->n1, n2 = g->n2, n3 = g->n3;
+  const int64_t s1 = g->s1, s2 = g->s2;
+  const int32_t* mask = g->codes;
+  double pq = 0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : pq) if (g_threads > 1)
+  for (int i = 0; i < n1; i++) {
+    for (int j = 0; j < n2; j++) {
+      const int64_t row0 = (int64_t)i * s1 + (int64_t)j * s2;
+      if (i == 0 || j == 0 || i == n1 - 1 || j == n2 - 1) {
+        for (int k = 0; k < n3; k++) y[row0 + k] = 0;
+        continue;
+      }
+      const double hxm = g->hx[i - 1], hxp = g->hx[i], hym = g->hy[j - 1], hyp = g->hy[j];
+      const double hx_2X = (hxm + hxp) / 2, hx_2Y = (hym + hyp) / 2;
+      const double* hz = g->hz;
+      y[row0] = 0;
+      y[row0 + n3 - 1] = 0;
+      double acc = 0;
+#pragma omp simd reduction(+ : acc)
+      for (int k = 1; k < n3 - 1; k++) {
+        const int64_t c = row0 + k;
+        double f_i_1 = (f[c] - f[c - s1]) / hxm;
+        double f_i = (f[c + s1] - f[c]) / hxp;
+        double f_j_1 = (f[c] - f[c - s2]) / hym;
+        double f_j = (f[c + s2] - f[c]) / hyp;
+        double f_k_1 = (f[c] - f[c - 1]) / hz[k - 1];
+        double f_k = (f[c + 1] - f[c]) / hz[k];
+        f_i_1 = mask[c - s1] == FICT ? 0.0 : f_i_1;
+        f_i = mask[c + s1] == FICT ? 0.0 : f_i;
+        f_j_1 = mask[c - s2] == FICT ? 0.0 : f_j_1;
+        f_j = mask[c + s2] == FICT ? 0.0 : f_j;
+        f_k_1 = mask[c - 1] == FICT ? 0.0 : f_k_1;
+        f_k = mask[c + 1] == FICT ? 0.0 : f_k;
+        const double v = -((f_i - f_i_1) / hx_2X + (f_j - f_j_1) / hx_2Y + (f_k - f_k_1) / hz2[k]);
+        const double yv = mask[c] == ACT ? v : 0.0;
+        y[c] = yv;
+        acc += f[c] * yv;
+      }
+      pq += acc;
+    }
+  }
+  return pq;
+}
+
 /* Plain Hestenes-Stiefel CG with a relative-residual stop: the FP64 CPU
- * counterpart of the GPU's plain FP64 CG (not a reference routine; the reference's CG
- * is the three-term form above). */
+ * counterpart of the GPU's plain FP64 CG (not a reference routine; the
+ * reference's CG is the three-term form above).  Its rows are the reference
+ * operator's (lap_row / row); on all-Actual Laplace grids the fused sweep
+ * above computes them with (p, A p), and the vector update computes (r, r). */
 int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const double* hx, const double* hy,
                  const double* hz, const double* density, int n1, int n2, int n3, const double* x0,
                  const double* b, double rtol, int maxit, double* result, xfo_stats* st) {
@@ -510,6 +578,9 @@ int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const doub
   if (sys_init(&S, op, codes, normals, hx, hy, hz, density, n1, n2, n3)) return XFO_ERR_MASK;
   const int64_t n = S.n;
   const uint8_t* m = S.smask;
+  const int fast = all_actual_interior(&S);
+  double* hz2 = (double*)calloc((size_t)n3, sizeof(double));
+  for (int k = 1; k < n3 - 1; k++) hz2[k] = (hz[k - 1] + hz[k]) / 2;
   memcpy(result, x0, (size_t)n * sizeof(double));
   double *r = zeros(n), *p = zeros(n), *q = zeros(n);
   apply(&S, result, b, -1, r); /* r = A x - b */
@@ -523,25 +594,32 @@ int xfo_cg_plain(int op, const int32_t* codes, const double* normals, const doub
   while (rr > thr) {
     if (maxit > 0 && it >= maxit) { st->status = 13; break; }
     it++;
-    apply(&S, p, NULL, 0, q);
-    double alpha = rr / xfo_dot(p, q, m, n);
+    double pq;
+    if (fast) {
+      pq = lap_actual_sweep(&S, p, q, hz2);
+    } else {
+      apply(&S, p, NULL, 0, q);
+      pq = xfo_dot(p, q, m, n);
+    }
+    const double alpha = rr / pq;
     double rr_new = 0;
-#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : rr_new) if (g_threads > 1)
-    for (int64_t c = 0; c < n; c++)
-      if (m[c]) {
-        result[c] += alpha * p[c];
-        r[c] -= alpha * q[c];
-        rr_new += r[c] * r[c];
-      }
-    double beta = rr_new / rr;
+#pragma omp parallel for simd num_threads(g_threads) schedule(static) reduction(+ : rr_new) if (g_threads > 1)
+    for (int64_t c = 0; c < n; c++) {
+      const double mk = m[c] ? 1.0 : 0.0;
+      const double xn = result[c] + alpha * p[c];
+      const double rn = r[c] - alpha * q[c];
+      result[c] = m[c] ? xn : result[c];
+      r[c] = m[c] ? rn : r[c];
+      rr_new += mk * (rn * rn);
+    }
+    const double beta = rr_new / rr;
     rr = rr_new;
-#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
-    for (int64_t c = 0; c < n; c++)
-      if (m[c]) p[c] = r[c] + beta * p[c];
+#pragma omp parallel for simd num_threads(g_threads) schedule(static) if (g_threads > 1)
+    for (int64_t c = 0; c < n; c++) p[c] = m[c] ? r[c] + beta * p[c] : p[c];
   }
   st->iterations = it;
   st->resid = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
-  free(r); free(p); free(q); free(S.smask);
+  free(r); free(p); free(q); free(hz2); free(S.smask);
   return XFO_OK;
 }
 

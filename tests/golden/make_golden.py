@@ -3,10 +3,11 @@
 Test infrastructure only.  Builds oracle/_ref/ref_driver (the reference's own
 XSLAE/XOperator/XSpace/... sources compiled in place by oracle/Makefile), feeds
 it seeded inputs and stores inputs + outputs as .npz files here.  Needs the
-reference tree (REF, default /root/reference); the fixtures it writes are what
+reference tree, named by the environment variable XFLOW_REF (build the driver
+first: `make -C oracle ref REF=$XFLOW_REF`); the fixtures it writes are what
 the tests read, so the tests themselves never need the reference.
 
-    python tests/golden/make_golden.py [pack | npy]
+    XFLOW_REF=<reference tree> python tests/golden/make_golden.py [pack | npy]
 """
 import os
 import subprocess

@@ -82,7 +82,8 @@ def case(shape, ci, co, seed):
     return x, W, bias, mask
 
 
-@pytest.mark.parametrize("ci,co", [(16, 16), (16, 32), (32, 64), (96, 32), (48, 16)])
+# (32, 96) and (16, 128): 3 co > 256, the per-tap kernel (k_conv3_tc); the rest stack the k taps
+@pytest.mark.parametrize("ci,co", [(16, 16), (16, 32), (32, 64), (96, 32), (48, 16), (32, 96), (16, 128)])
 def test_conv_fp32_out(ctx, ci, co):
     x, W, bias, mask = case((10, 9, 12), ci, co, ci * 100 + co)
     for relu in (0, 1):

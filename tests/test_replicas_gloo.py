@@ -58,3 +58,21 @@ def test_single_process_has_no_collective():
     w, r, local, dist = bench.dist_init()
     assert (w, r, local, dist) == (1, 0, 0, None)
     assert bench.replica_value(None, [2.0, 4.0], 1) == 3.0
+
+
+def test_gpus_flag_starts_the_ranks_itself():
+    """`bench.py --gpus 2` outside torchrun starts two ranks (torch.distributed.run
+    on 127.0.0.1, gloo); the reference arm works on rank 0 only and prints one
+    line whose n_gpus is the number of ranks that ran."""
+    import subprocess
+
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "16",
+                          "--steps", "1", "--warmup", "0", "--gpus", "2"], capture_output=True, text=True, env=env,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(s) for s in out.stdout.splitlines() if s.startswith("{")]
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["ranks_with_work"] == 1
+    assert d["rel_resid"] <= 1e-8 and d["steps"] == 1

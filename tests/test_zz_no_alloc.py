@@ -58,3 +58,40 @@ def test_dot_noalloc_matches_xf_dot_twice_in_a_row():
         assert st == capi.XF_ERR_ARG
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("n", [3_000_001, 8192 * 256 * 16])
+def test_dot_noalloc_many_blocks_and_the_maximum_size(n):
+    """Hundreds to thousands of blocks (the last block's loop over the partials
+    runs several rounds), masked and unmasked, up to exactly the largest
+    accepted size; checked against an order-independent bound
+    |got - exact| <= 1e-13 sum |a b|."""
+    torch = pytest.importorskip("torch")
+    import math
+
+    ctx = xf.Context(0)
+    try:
+        gen = torch.Generator(device="cpu").manual_seed(n % 1000)
+        a_h = torch.randn(n, dtype=torch.float64, generator=gen)
+        b_h = torch.randn(n, dtype=torch.float64, generator=gen)
+        m_h = (torch.rand(n, generator=gen) < 0.7).to(torch.uint8)
+        a, b, m = a_h.cuda(), b_h.cuda(), m_h.cuda()
+        out = torch.full((1,), np.nan, dtype=torch.float64, device="cuda")
+        L = capi.lib()
+        stream = L.xf_stream(ctx.h)
+        prod = (a_h * b_h).numpy()
+        for mask in (m, None):
+            terms = prod[m_h.numpy().astype(bool)] if mask is not None else prod
+            exact = math.fsum(terms)
+            for _ in range(2):
+                out.fill_(np.nan)
+                torch.cuda.synchronize()
+                st = L.xf_dot_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                      C.c_void_p(mask.data_ptr()) if mask is not None else None, C.c_int64(n),
+                                      C.c_void_p(out.data_ptr()), stream)
+                assert st == capi.XF_OK
+                ctx.synchronize()
+                assert abs(float(out.item()) - exact) <= 1e-13 * float(np.abs(terms).sum())
+    finally:
+        ctx.close()
+

@@ -329,20 +329,6 @@ def cheb_factors(lmax, ratio, degree):
     return np.array(list(out), dtype=np.float64).reshape(m, 3)
 
 
-def probe_mma_rate(ctx, n, ctas_per_sm=2, layout=0):
-    """Clock cycles per tcgen05.mma of width n issued back to back (operands resident in shared memory)."""
-    c = C.c_double()
-    _check(ctx.h, capi.lib().xf_probe_mma_rate(ctx.h, int(n), int(ctas_per_sm), int(layout), C.byref(c)))
-    return c.value
-
-
-def probe_fma_rate(ctx, fp64):
-    """TFLOP/s of independent FMA chains, FP64 or FP32."""
-    t = C.c_double()
-    _check(ctx.h, capi.lib().xf_probe_fma_rate(ctx.h, int(bool(fp64)), C.byref(t)))
-    return t.value
-
-
 def profile_cg_kernels(op, reps=20):
     """Average ms per launch of each CG-iteration kernel, timed alone
     (pq_fused_f32 is absent where the grid does not take the fused path)."""

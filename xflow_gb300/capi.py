@@ -35,7 +35,7 @@ EXPORTS = [
     "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
     "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
     "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
-    "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_probe_mma_rate", "xf_probe_fma_rate", "xf_dot_noalloc",
+    "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_dot_noalloc",
 ]
 
 
@@ -103,8 +103,6 @@ def lib():
         L.xf_dot_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
         L.xf_profile_cg_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.xf_selftest_division.argtypes = [vp, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
-        L.xf_probe_mma_rate.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
-        L.xf_probe_fma_rate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.xf_cheb_factors_host.argtypes = [C.c_double, C.c_double, C.c_int, C.POINTER(C.c_float)]
         L.xf_voxelize_mesh.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_longlong, vp, C.c_longlong,
                                        C.c_int32, vp]

@@ -304,21 +304,18 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
   a.tiles = (a.P + PQB_TILE - 1) / PQB_TILE;
   a.cx = (float)g->ucx; a.cy = (float)g->ucy; a.cz = (float)g->ucz;
   a.ctl = ctl;
-  // ring depth 2 (3 blocks per SM); XF_PQB_NS = 1 or 4 selects the 1-deep ring
-  // (4 blocks per SM) or the 4-deep one (2 blocks per SM)
-  int ns = 2;
-  if (const char* env = getenv("XF_PQB_NS")) ns = env[0] == '1' ? 1 : (env[0] == '4' && pqb_smem(a.RL, 4) <= 112 * 1024) ? 4 : 2;
+  // ring depth 2 (3 blocks per SM)
+  const int ns = 2;
   const size_t smem = pqb_smem(a.RL, ns);
   static size_t attr_smem[5][64] = {};   // per ring depth and device
   size_t& at = attr_smem[ns][ctx->device & 63];
   if (at < smem) {
-    cudaFuncSetAttribute(ns == 1 ? k_cg_pqb<1> : ns == 4 ? k_cg_pqb<4> : k_cg_pqb<2>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_cg_pqb<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     at = smem;
   }
   // resident blocks per SM from shared memory (1 KB reserved per block) and the launch bounds
   int resident = (int)((228 * 1024) / (smem + 1024 + 1024));
-  if (resident > (ns == 1 ? 4 : 3)) resident = ns == 1 ? 4 : 3;
+  if (resident > 3) resident = 3;
   if (resident < 1) resident = 1;
   const int64_t B = (int64_t)ctx->sm_count * resident;
   // plane chunk: the length whose last wave wastes least (cost ~ waves x (chunk + 1))
@@ -339,10 +336,5 @@ void xf_cg_pqb_launch(const xf_op* op, const float* r, float* pb0, float* pb1, f
     const long cap = strtol(env, nullptr, 10);
     if (cap >= 1 && cap < blocks) blocks = cap;
   }
-  if (ns == 1)
-    k_cg_pqb<1><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
-  else if (ns == 4)
-    k_cg_pqb<4><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
-  else
-    k_cg_pqb<2><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
+  k_cg_pqb<2><<<(int)blocks, PQB_THREADS, smem, ctx->stream>>>(a);
 }

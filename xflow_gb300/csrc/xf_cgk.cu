@@ -700,7 +700,7 @@ static void launch_cg_q(const xf_op* op, const T* x, T* y, const T* b, float* y3
   dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
   constexpr bool D = std::is_same<T, double>::value;
   if constexpr (!D && !RES) {
-    if (two && g->uniform && !(getenv("XF_Q2_PLAIN") && getenv("XF_Q2_PLAIN")[0] == '1')) {
+    if (two && g->uniform) {
       if (g->nbrow > 0) k_cg_q2u<true><<<grid, CGK_THREADS, 0, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
       else k_cg_q2u<false><<<grid, CGK_THREADS, 0, ctx->stream>>>(a, (float)g->ucx, (float)g->ucy, (float)g->ucz);
       return;

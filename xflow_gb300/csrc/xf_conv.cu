@@ -500,8 +500,8 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
   a.out32 = out_fp32 ? (float*)out : nullptr;
   a.out_ld = out_ld; a.out_ch = out_ch; a.relu = relu; a.err = err;
   const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
-  if (3 * co <= 256 && !(getenv("XF_CONV_TAPS") && getenv("XF_CONV_TAPS")[0] == '1')) {
-    // k-taps stacked along N (XF_CONV_TAPS=1 selects the per-tap kernel)
+  if (3 * co <= 256) {
+    // k-taps stacked along N (the per-tap kernel below takes wider outputs)
     const int KC = ci == 16 ? 16 : ci == 48 ? 48 : ci % 32 == 0 ? 32 : 16;
     auto kern = KC == 16 ? k_conv3_st<16> : KC == 32 ? k_conv3_st<32> : k_conv3_st<48>;
     const size_t smem = (size_t)ST_STAGES * ((128 + 3 * co) * KC * 2);

@@ -20,8 +20,10 @@
 //    sums.  Calls ordered on one stream are safe; the ticket is returned to
 //    zero by each call's last block.
 //  * The first call on a device resolves the scratch's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress (with that device current) and keeps it; make that
+//    first call before any stream capture.  The address belongs to the
+//    device's primary context: after cudaDeviceReset the process must be
+//    restarted before it calls this entry point again.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -109,6 +111,12 @@ extern "C" int xf_dot_noalloc(const double* d_a, const double* d_b, const uint8_
   const int64_t per_block = (int64_t)XF_NOALLOC_THREADS * XF_NOALLOC_PER_THREAD;
   int blocks = (int)((n + per_block - 1) / per_block);
   if (blocks < 1) blocks = 1;
-  k_dot_noalloc<<<blocks, XF_NOALLOC_THREADS, 0, (cudaStream_t)stream>>>(d_a, d_b, d_mask, n, d_out, g_scratch_ptr[dev]);
-  return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
+  // launched through cudaLaunchKernel so that its own status is returned (an
+  // earlier, unrelated error is neither reported nor cleared here)
+  NoallocScratch* scr = g_scratch_ptr[dev];
+  void* args[] = {(void*)&d_a, (void*)&d_b, (void*)&d_mask, (void*)&n, (void*)&d_out, (void*)&scr};
+  return cudaLaunchKernel((const void*)k_dot_noalloc, dim3(blocks), dim3(XF_NOALLOC_THREADS), args, 0,
+                          (cudaStream_t)stream) == cudaSuccess
+             ? XF_OK
+             : XF_ERR_CUDA;
 }

@@ -42,9 +42,6 @@ void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const fl
 void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, float* z, const float coeffs[3]);
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 bool xf_cg_pqt_supported(const xf_grid* g);
-bool xf_cgf_supported(const xf_grid* g);
-int xf_cgf_prepare(xf_ctx* ctx, const xf_grid* g);
-void xf_cgf_iteration(const xf_op* op, float* r, float* e, float* p0, float* p1);
 int xf_op_ready(const xf_op* op);
 
 #define GUARD_DONE(S) \
@@ -410,23 +407,7 @@ static int read_state(xf_ctx* ctx, HostState* hs) {
 // Runs `iter` (which enqueues one iteration) until the device flags done:
 // chunks of `chunk` iterations are captured once into a CUDA graph; the state
 // of chunk k is read while chunk k+1 is already queued.
-static int run_loop_direct(xf_ctx* ctx, const std::function<void(int)>& iter, int chunk, int maxit, HostState* hs) {
-  const int max_chunks = maxit / chunk + 3;
-  long long kernels = hs->kernels;
-  for (int k = 0; k < max_chunks; k++) {
-    for (int c = 0; c < chunk; c++) iter(c);
-    int st = read_state(ctx, hs);
-    if (st) return st;
-    if (hs->done) break;
-  }
-  hs->kernels = kernels;
-  return XF_OK;
-}
-
 static int run_loop(xf_ctx* ctx, const std::function<void(int)>& iter, int chunk, int maxit, HostState* hs) {
-  // XF_NO_GRAPH=1: enqueue the same kernels without graph capture (diagnostics).
-  static const bool no_graph = getenv("XF_NO_GRAPH") && getenv("XF_NO_GRAPH")[0] == '1';
-  if (no_graph) return run_loop_direct(ctx, iter, chunk, maxit, hs);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   XF_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -630,28 +611,6 @@ static int solve_cg(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const xf_vec*
         if (c == last) {
           k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
           xf_cg_res64(op, x, b, r, SL_C, CTL_PCG_REPL);
-        }
-      };
-    } else if (lap && xf_cgf_supported(g) && getenv("XF_FUSED") && getenv("XF_FUSED")[0] == '1') {
-      // (opt-in: measured slower than the three-kernel iteration so far)
-      // Staged fused iteration: K1 (p = r + beta p, (p, A p)) and K2 (A p
-      // recomputed, e += alpha p, r -= alpha A p, (r, r)); p ping-pongs
-      // between p32 and q32.  One graph chunk = `replace_every` iterations
-      // ending with the FP64 fold and true-residual replacement.
-      chunk = o.replace_every;
-      int rcp = xf_cgf_prepare(ctx, g);
-      if (rcp) return rcp;
-      float *e = e32, *r = r32, *pa = p32, *pb = q32;
-      XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, ctx->stream));
-      XF_CUDA(ctx, cudaMemsetAsync(pa, 0, n * 4, ctx->stream));
-      XF_CUDA(ctx, cudaMemsetAsync(pb, 0, n * 4, ctx->stream));
-      xf_cg_res64(op, x, b, r, SL_A, CTL_CG_INIT);
-      const int last = chunk - 1;
-      iter = [=](int c) {
-        xf_cgf_iteration(op, r, e, pa, pb);
-        if (c == last) {
-          k_fold<<<eb, 256, 0, ctx->stream>>>(x, e, n, S, 2);
-          xf_cg_res64(op, x, b, r, SL_C, CTL_MIXED_REPL);
         }
       };
     } else if (lap && p32b && !(getenv("XF_PQ_FUSE") && getenv("XF_PQ_FUSE")[0] == '0')) {

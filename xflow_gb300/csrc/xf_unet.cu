@@ -410,6 +410,8 @@ __global__ void k_f2d_mask(const float* __restrict__ z, const uint8_t* __restric
 // ---------------------------------------------------------------------------
 // Host side
 static int ublocks(xf_ctx* ctx, int64_t n) { return grid_blocks(ctx, n, 256); }
+// k_sumsq's grid: its partial buffer holds RP_MAX blocks (the loop is grid-stride)
+static int sumsq_blocks(xf_ctx* ctx, int64_t n) { return std::min(ublocks(ctx, n), RP_MAX); }
 
 static int act_alloc(xf_unet* u, Act& a, int level, int C) {
   a.level = level;
@@ -658,7 +660,7 @@ static int forward(xf_unet* u, const double* r) {
   const Level* L = u->L;
   int st;
   XF_CUDA(ctx, cudaMemsetAsync(u->red, 0, 8 * 8, s));
-  k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0, u->rpart, u->rtick);
+  k_sumsq<<<sumsq_blocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0, u->rpart, u->rtick);
   k_unet_input<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, (double)L[0].active,
                                                     u->X0.p0(L));
   if ((st = conv(u, ENC0A, u->X0, 0, u->A0.p0(L), 16, 16, 0))) return st;
@@ -702,7 +704,7 @@ static int backward(xf_unet* u, const double* r, const double* e, const xf_op* o
     k_anorm_grad<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, u->az, L[0].mask, L[0].n, ctx->scratch, u->red,
                                                       u->G0_16a.p0(L));
   } else {
-    k_sumsq<<<ublocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1, u->rpart, u->rtick);
+    k_sumsq<<<sumsq_blocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1, u->rpart, u->rtick);
     k_unet_loss<<<ublocks(ctx, L[0].n), 256, 0, s>>>(u->zout, e, L[0].mask, L[0].n, (double)L[0].active, u->red,
                                                      u->G0_16a.p0(L));
   }
@@ -922,8 +924,11 @@ __global__ void k_restrict4(const float* __restrict__ r, int f2, int f3, double*
   }
   rc[((int64_t)I * c2 + J) * c3 + K] = v;
 }
-// Four consecutive cells of a plane per thread (plane size a multiple of 4): one
-// 4-byte mask load and one 16-byte store.
+// Four consecutive cells of a plane per thread: one 4-byte mask load and one
+// 16-byte store.  With F = 4 every fine interior extent is a multiple of 4, so
+// n2 = 4a + 2 and n3 = 4b + 2 and the plane size n2 n3 is a multiple of 4;
+// with the 256-byte aligned allocations of y and the space mask, every
+// thread's group then starts on a 16-byte (y) and 4-byte (mask) boundary.
 __global__ void k_prolong4v(const double* __restrict__ zc, int c2, int c3, const uint8_t* __restrict__ smask, int f1,
                             int f2, int f3, float* __restrict__ y) {
   const int P = f2 * f3;
@@ -948,18 +953,6 @@ __global__ void k_prolong4v(const double* __restrict__ zc, int c2, int c3, const
     }
   }
   *reinterpret_cast<float4*>(y + c0) = make_float4(v[0], v[1], v[2], v[3]);
-}
-__global__ void k_prolong4(const double* __restrict__ zc, int c2, int c3, const uint8_t* __restrict__ smask, int f1,
-                           int f2, int f3, float* __restrict__ y) {
-  const int P = f2 * f3;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
-  if (p >= P) return;
-  const int j = p / f3, k = p - j * f3;
-  const int64_t c = (int64_t)i * P + p;
-  float v = 0.f;
-  if (smask[c] && i > 0 && i < f1 - 1 && j > 0 && j < f2 - 1 && k > 0 && k < f3 - 1)
-    v = (float)zc[((int64_t)(1 + ((i - 1) >> 2)) * c2 + (1 + ((j - 1) >> 2))) * c3 + (1 + ((k - 1) >> 2))];
-  y[c] = v;
 }
 // (a, b) of FP32 boxes that are zero off the active set: exact products
 // accumulated in float-float per thread and per warp, FP64 across warps and
@@ -1131,12 +1124,9 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
                                                                          cg->n3);
     int st2 = xf_unet_apply_dev(u, rc, zc);
     if (st2) return st2;
-    if (F == 4 && (g->n2 * g->n3) % 4 == 0)
+    if (F == 4)   // n2 n3 is a multiple of 4 (see k_prolong4v)
       k_prolong4v<<<dim3((g->n2 * g->n3 / 4 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1,
                                                                               g->n2, g->n3, y);
-    else if (F == 4)
-      k_prolong4<<<dim3((g->n2 * g->n3 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1, g->n2,
-                                                                         g->n3, y);
     else
       k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
     xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
