@@ -251,6 +251,28 @@ def momentum_rhs(axis, codes, u, v, w, hx, hy, hz, vis=None, border=None, force=
     return tuple(out), st, bad.value
 
 
+def adi_line_coeffs(direction, codes, hx, hy, hz, vec_tr, D, tau):
+    """The reference's ADI line coefficients (a, b, c) along `direction` at every Actual point
+    (XProblem.cpp:3149-3190); NaN elsewhere."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    out = [np.full(codes.shape, np.nan) for _ in range(3)]
+    lib().xfo_adi_line_coeffs(int(direction), _p(codes, C.c_int32), *codes.shape, _p(f64(hx), C.c_double),
+                              _p(f64(hy), C.c_double), _p(f64(hz), C.c_double), _p(f64(vec_tr), C.c_double),
+                              _p(f64(D), C.c_double), C.c_double(tau), *(_p(o, C.c_double) for o in out))
+    return tuple(out)
+
+
+def adi_first_rhs(codes, hx, hy, hz, f_1, u, v, w, D, rp, tau):
+    """The right-hand side of the first splitting step's x lines at every Actual point
+    (XProblem.cpp:3192-3276); NaN elsewhere."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    f = np.full(codes.shape, np.nan)
+    d = lambda a: _p(f64(a), C.c_double)  # noqa: E731
+    lib().xfo_adi_first_rhs(_p(codes, C.c_int32), *codes.shape, d(hx), d(hy), d(hz), d(f_1), d(u), d(v), d(w), d(D),
+                            d(rp), C.c_double(tau), _p(f, C.c_double))
+    return f
+
+
 def divergence_max(codes, u, v, w, hxU, hyV, hzW):
     codes = np.ascontiguousarray(codes, np.int32)
     ijk = np.zeros(3, np.int32)

@@ -5,13 +5,17 @@
 // reference itself rather than from a restatement.
 //
 // Usage: ref_driver <task> <input.bin> <output.bin>
-//   task = matvec | solve | thomas | ib | pack | npy
-//   (npy writes <output.bin>.npy through the reference's cnpy::npy_save)
+//   task = matvec | solve | thomas | ib | pack | npy | step
+//   (npy writes <output.bin>.npy through the reference's cnpy::npy_save;
+//   step runs TVPProblem::SolveBySplitting and writes its VTK files under
+//   ../Res/ relative to the working directory, as the reference does)
 //
 // File format (both directions): a sequence of records
 //   char name[32]; char kind ('d' double / 'i' int32); int64 count; data[count]
+#include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <unistd.h>
 #include <cstring>
 #include <cmath>
 #include <map>
@@ -29,6 +33,8 @@
 #include "XProblem.h"
 #include "XImmersedBoundary.h"
 #include "cnpy.h"
+
+#include <omp.h>
 
 struct Rec { char kind; std::vector<double> d; std::vector<int> i; };
 typedef std::map<std::string, Rec> Bag;
@@ -407,6 +413,230 @@ static void task_npy(Bag& b, const char* out) {
   cnpy::npy_save(std::string(out) + ".npy", b["data"].d.data(), shape.data(), (unsigned int)shape.size(), "w");
 }
 
+// ---------------------------------------------------------------------------
+// The time step itself: TVPProblem::SolveBySplitting (XProblem.cpp:4255-6650)
+// run for two steps on grids, border values, forces and an initial
+// concentration taken from the input, through a subclass that supplies them
+// by the reference's own virtual hooks (BuildGrid*, GetBorderCondition*,
+// GetForce, InitialConcentrationDistribution) and reads state back through
+// others (GetForce's transfer-velocity argument, ComputeStress,
+// CountBoundaryP/Concentration/Viscosity).  Three routines the step calls
+// from XSLAE.o and the C library are wrapped at link time
+// (-Wl,--wrap, oracle/Makefile) so that values that live only inside
+// SolveBySplitting can be read as they pass:
+//   TSLAE::SolveByBiConjugateGradientsStab  the pressure system's right-hand
+//       side and warm start (XProblem.cpp:5570-5588); with zero_p set, the
+//       capture step's solve is replaced by p = 0, so that the velocity
+//       correction (XProblem.cpp:5663, u = u_ - tau gradP / rho) hands back
+//       the intermediate velocity u_ itself;
+//   TSLAE::SolveByScalarRunning  every ADI line system (a, b, c, f and the
+//       solution) of the capture step, in call order;
+//   __printf_chk  the control balance's value and cell (XProblem.cpp:5829),
+//       read from the call's arguments rather than from the printed text.
+// Nothing else is replaced: the rest of the step is the reference's code.
+static Writer* g_out = NULL;
+static int g_step = 0;          // time step in progress (from the hooks' arguments)
+static int g_capture = 2;       // the step whose values are written
+static int g_zero_p = 0;
+static std::vector<int> g_line_m, g_line_eq;
+static std::vector<double> g_line_a, g_line_b, g_line_c, g_line_f, g_line_u;
+
+struct SlaePeek : TSLAE {   // pointers to TSLAE's protected members (no object of this type exists)
+  static TRnSpace* TSLAE::*fx_() { return &SlaePeek::fx; }
+  static TRnSpace* TSLAE::*fb_() { return &SlaePeek::fb; }
+  static TRnSpace* TSLAE::*fres_() { return &SlaePeek::fResult; }
+};
+
+static std::vector<double> box_of(TRnSpace& v, int n1, int n2, int n3) {
+  TRnRelease3dSpace& x = dynamic_cast<TRnRelease3dSpace&>(v);
+  std::vector<double> out((size_t)n1 * n2 * n3);
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) out[((size_t)i * n2 + j) * n3 + k] = x[i][j][k];
+  return out;
+}
+static std::vector<int> g_pdims;   // pressure box
+
+extern "C" void __real__ZN5TSLAE31SolveByBiConjugateGradientsStabEv(TSLAE* self);
+extern "C" void __wrap__ZN5TSLAE31SolveByBiConjugateGradientsStabEv(TSLAE* self) {
+  const bool cap = g_out && g_step == g_capture;
+  if (cap) {
+    g_out->d("rhs", box_of(*(self->*SlaePeek::fb_()), g_pdims[0], g_pdims[1], g_pdims[2]));
+    g_out->d("p0", box_of(*(self->*SlaePeek::fx_()), g_pdims[0], g_pdims[1], g_pdims[2]));
+  }
+  if (cap && g_zero_p) {
+    *(self->*SlaePeek::fres_()) |= 0;
+    return;
+  }
+  __real__ZN5TSLAE31SolveByBiConjugateGradientsStabEv(self);
+}
+
+extern "C" void __real__ZN5TSLAE20SolveByScalarRunningEiPdPKdS2_S2_S2_(int, double*, const double*, const double*,
+                                                                         const double*, const double*);
+extern "C" void __wrap__ZN5TSLAE20SolveByScalarRunningEiPdPKdS2_S2_S2_(int M, double* U, const double* A,
+                                                                         const double* B, const double* C,
+                                                                         const double* F) {
+  __real__ZN5TSLAE20SolveByScalarRunningEiPdPKdS2_S2_S2_(M, U, A, B, C, F);
+  if (!(g_out && g_step == g_capture)) return;
+  g_line_m.push_back(M);
+  g_line_eq.push_back(omp_get_thread_num());
+  g_line_a.insert(g_line_a.end(), A, A + M + 1);
+  g_line_b.insert(g_line_b.end(), B, B + M + 1);
+  g_line_c.insert(g_line_c.end(), C, C + M + 1);
+  g_line_f.insert(g_line_f.end(), F, F + M + 1);
+  g_line_u.insert(g_line_u.end(), U, U + M + 1);
+}
+
+// SolveBySplitting's teardown (XProblem.cpp:6652-6680) deletes the pressure
+// vector, the right-hand side and the operator twice: once through
+// `delete slae` (TSLAE::~TSLAE deletes its A, x and b, XSLAE.cpp:21-30) and
+// again by name.  Every value has been read by then, so the step task writes
+// its last records and ends the process when that teardown announces itself.
+static void step_finish() {
+  g_out->i("line_m", g_line_m);
+  g_out->i("line_thread", g_line_eq);
+  g_out->d("line_a", g_line_a);
+  g_out->d("line_b", g_line_b);
+  g_out->d("line_c", g_line_c);
+  g_out->d("line_f", g_line_f);
+  g_out->d("line_u", g_line_u);
+  fclose(g_out->f);
+  fflush(stderr);
+  _exit(0);
+}
+extern "C" int __wrap___printf_chk(int flag, const char* fmt, ...) {
+  (void)flag;
+  if (g_out && strncmp(fmt, "Deleting temporary objects: Starting", 36) == 0) step_finish();
+  va_list ap;
+  va_start(ap, fmt);
+  if (g_out && g_step == g_capture && strncmp(fmt, "Control balance: OK. (point", 27) == 0) {
+    va_list aq;
+    va_copy(aq, ap);
+    int i = va_arg(aq, int), j = va_arg(aq, int), k = va_arg(aq, int);
+    double v = va_arg(aq, double);
+    va_end(aq);
+    std::vector<int> ijk(3);
+    ijk[0] = i; ijk[1] = j; ijk[2] = k;
+    g_out->i("div_ijk", ijk);
+    g_out->s("div_max", v);
+  }
+  int r = vfprintf(stderr, fmt, ap);   // the reference's progress log, kept off the driver's stdout
+  va_end(ap);
+  return r;
+}
+
+static T3dNormalGrid* grid_from(Bag& b, const std::string& pre) {
+  const std::vector<int>& dims = I(b, (pre + "_dims").c_str());
+  const int n1 = dims[0], n2 = dims[1], n3 = dims[2];
+  TSeparator* s1 = new TRandomSeparator(n1, D(b, (pre + "_x").c_str()).data());
+  TSeparator* s2 = new TRandomSeparator(n2, D(b, (pre + "_y").c_str()).data());
+  TSeparator* s3 = new TRandomSeparator(n3, D(b, (pre + "_z").c_str()).data());
+  const std::vector<int>& codes = I(b, (pre + "_codes").c_str());
+  const std::vector<double>* nrm = b.count(pre + "_nrm") ? &D(b, (pre + "_nrm").c_str()) : NULL;
+  T3dNumberMask& mask = *(new T3dNumberMask(n1, n2, n3));
+  T3dVector**** normals = new T3dVector***[n1];
+  for (int i = 0; i < n1; i++) {
+    normals[i] = new T3dVector**[n2];
+    for (int j = 0; j < n2; j++) {
+      normals[i][j] = new T3dVector*[n3];
+      for (int k = 0; k < n3; k++) {
+        const size_t c = ((size_t)i * n2 + j) * n3 + k;
+        mask[i][j][k] = codes[c];
+        T3dVector* nv = NULL;
+        if (nrm && ((*nrm)[3 * c] != 0 || (*nrm)[3 * c + 1] != 0 || (*nrm)[3 * c + 2] != 0)) {
+          nv = new T3dVector; nv->X = (*nrm)[3 * c]; nv->Y = (*nrm)[3 * c + 1]; nv->Z = (*nrm)[3 * c + 2];
+        }
+        normals[i][j][k] = nv;
+      }
+    }
+  }
+  return new T3dNormalGrid(s1, s2, s3, mask, normals);
+}
+
+class StepProblem : public TVPProblem {
+ public:
+  StepProblem(Bag& bag, double tEnd, double tau, double mu1, double mu2, double rho1, double rho2)
+      : TVPProblem(tEnd, tau, mu1, mu2, rho1, rho2), b(bag) {}
+  void run() {
+    Initialize();
+    Solve();
+  }
+  using TVPProblem::ComputeStress;
+
+ protected:
+  Bag& b;
+  double box_value(const char* pre, const char* rec, int i, int j, int k) {
+    const std::vector<int>& dims = I(b, (std::string(pre) + "_dims").c_str());
+    return D(b, rec)[((size_t)i * dims[1] + j) * dims[2] + k];
+  }
+  std::vector<int> dims(const char* pre) { return I(b, (std::string(pre) + "_dims").c_str()); }
+  void record(const char* name, TRnSpace& v, const char* pre) {
+    std::vector<int> d = dims(pre);
+    g_out->d(name, box_of(v, d[0], d[1], d[2]));
+  }
+  virtual TMaskGenerator* CreateStatement() { return NULL; }
+  virtual TNodesGrid* BuildGrid() { return grid_from(b, "n"); }
+  virtual TNodesGrid* BuildGridU() { return grid_from(b, "u"); }
+  virtual TNodesGrid* BuildGridV() { return grid_from(b, "v"); }
+  virtual TNodesGrid* BuildGridW() { return grid_from(b, "w"); }
+  virtual TNodesGrid* BuildGridP() { return grid_from(b, "p"); }
+  virtual double GetBorderConditionU(int i, int j, int k, int) { return box_value("u", "u_bc", i, j, k); }
+  virtual double GetBorderConditionV(int i, int j, int k, int) { return box_value("v", "v_bc", i, j, k); }
+  virtual double GetBorderConditionW(int i, int j, int k, int) { return box_value("w", "w_bc", i, j, k); }
+  virtual double GetBorderConditionP(int i, int j, int k, int) { return box_value("p", "p_bc", i, j, k); }
+  virtual bool InitialConcentrationDistribution(int i, int j, int k, int, int, int) {
+    return box_value("p", "conc0", i, j, k) != 0;
+  }
+  virtual void GetForce(TRnRelease3dSpace& force, T3dNormalGrid&, T3dNormalGrid&, TRnRelease3dSpace& velocity,
+                        const int axis, const int ts) {
+    g_step = ts;
+    const char* pre = axis == 1 ? "u" : axis == 2 ? "v" : "w";
+    if (ts == g_capture) record(axis == 1 ? "tr_1" : axis == 2 ? "tr_2" : "tr_3", velocity, pre);
+    std::vector<int> d = dims(pre);
+    const std::vector<double>& f = D(b, axis == 1 ? "force_u" : axis == 2 ? "force_v" : "force_w");
+    for (int i = 0; i < d[0]; i++)
+      for (int j = 0; j < d[1]; j++)
+        for (int k = 0; k < d[2]; k++) force[i][j][k] = f[((size_t)i * d[1] + j) * d[2] + k];
+  }
+  virtual void ComputeStress(TRnRelease3dSpace& U, TRnRelease3dSpace& V, TRnRelease3dSpace& W, int ts) {
+    g_step = ts;
+    const char* nu = ts == g_capture ? "u" : "s1_u";
+    const char* nv = ts == g_capture ? "v" : "s1_v";
+    const char* nw = ts == g_capture ? "w" : "s1_w";
+    if (ts == g_capture || ts == g_capture - 1) {
+      record(nu, U, "u");
+      record(nv, V, "v");
+      record(nw, W, "w");
+    }
+  }
+  virtual void CountBoundaryP(TRnRelease3dSpace& p) {
+    if (g_step == g_capture) record("p", p, "p");
+    else if (g_step == g_capture - 1) record("s1_p", p, "p");
+  }
+  virtual void CountBoundaryConcentration(TRnRelease3dSpace& c) {
+    if (g_step == g_capture) record("cnc", c, "p");
+    else if (g_step == g_capture - 1) record("s1_cnc", c, "p");
+  }
+  virtual void CountBoundaryViscosity(TRnRelease3dSpace& v) {
+    if (g_step == g_capture) record("vis", v, "p");
+    else if (g_step == g_capture - 1) record("s1_vis", v, "p");
+  }
+};
+
+static void task_step(Bag& b, Writer& w) {
+  const std::vector<double>& prm = D(b, "params");   // tau, mu1, mu2, rho1, rho2
+  g_out = &w;
+  g_pdims = I(b, "p_dims");
+  g_capture = 2;
+  g_zero_p = I(b, "zero_p")[0];
+  TProblem::GlobalUsePackOperator = false;   // the TSLAE-on-the-box path (XFlow.cpp:51)
+  TProblem::GlobalTurbulenceMode = false;
+  TProblem::GlobalSaveStep = 2;              // VTK of steps 1 and 2
+  StepProblem* P = new StepProblem(b, 2 * prm[0], prm[0], prm[1], prm[2], prm[3], prm[4]);
+  P->run();   // ends in step_finish() at the reference's teardown
+  throw std::runtime_error("the time step returned without reaching its teardown");
+}
+
 int main(int argc, char** argv) {
   if (argc != 4) { fprintf(stderr, "usage: ref_driver task in out\n"); return 2; }
   try {
@@ -419,6 +649,7 @@ int main(int argc, char** argv) {
     else if (t == "ib") task_ib(b, w);
     else if (t == "pack") task_pack(b, w);
     else if (t == "npy") task_npy(b, argv[3]);
+    else if (t == "step") task_step(b, w);
     else { fprintf(stderr, "unknown task\n"); return 2; }
   } catch (const char* e) {
     fprintf(stderr, "reference threw: %s\n", e); return 3;

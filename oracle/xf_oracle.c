@@ -1140,15 +1140,86 @@ int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, c
  * (1/tau) f_c, in the reference's operation order; PreDefined / PreNormal rows
  * as the Laplace operator's.  vel[d] is the advecting component along d at the
  * cell; flags bit 0 convective, bit 1 diffusive. */
-static double ad_dir(const double* h, int m, double vd, double D, double conv, double diff, double fm, double fc,
-                     double fp) {
+/* One direction's implicit line coefficients of the split transfer equation
+ * at an Actual point, central scheme (SolveTransferEquation__,
+ * XProblem.cpp:3179-3184, schemeType 0) without the 1/tau of B. */
+static void ad_coeffs(const double* h, int m, double vd, double D, double conv, double diff, double* A, double* B,
+                      double* C) {
   double h_1 = h[m - 1], hh = h[m];
   double hx2 = h[m - 1] + h[m];
   double hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / 2;
-  double A = conv * (0.5 * (-vd / hx2)) + diff * (0.5 * (-(D)*hh / hxhxh));
-  double B = diff * (0.5 * (D)*hx2 / hxhxh);
-  double C = conv * (0.5 * (vd / hx2)) + diff * (0.5 * (-(D)*h_1 / hxhxh));
+  *A = conv * (0.5 * (-vd / hx2)) + diff * (0.5 * (-(D)*hh / hxhxh));
+  *B = diff * (0.5 * (D)*hx2 / hxhxh);
+  *C = conv * (0.5 * (vd / hx2)) + diff * (0.5 * (-(D)*h_1 / hxhxh));
+}
+
+static double ad_dir(const double* h, int m, double vd, double D, double conv, double diff, double fm, double fc,
+                     double fp) {
+  double A, B, C;
+  ad_coeffs(h, m, vd, D, conv, diff, &A, &B, &C);
   return A * fm + B * fc + C * fp;
+}
+
+/* The line systems of the split transfer equation as the reference builds
+ * them for every Actual point of a box (SolveTransferEquation__,
+ * XProblem.cpp:3149-3190 and 3192-3276, central scheme): for direction
+ * dir (1 x, 2 y, 3 z) the coefficients a, b = 1/tau + (diffusion part), c
+ * with vecTr the transfer velocity along dir and D the point's diffusion
+ * coefficient (diffCoefVar); and, for the x lines of the first splitting
+ * step (the only sweep whose right-hand side reads f_1 alone), the
+ * right-hand side f.  Other points are left untouched. */
+void xfo_adi_line_coeffs(int dir, const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                         const double* hz, const double* vecTr, const double* D, double tau, double* a, double* b,
+                         double* c) {
+  const double* h = dir == 1 ? hx : dir == 2 ? hy : hz;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+        if (codes[q] != ACT) continue;
+        const int m = dir == 1 ? i : dir == 2 ? j : k;
+        double A, B, C;
+        ad_coeffs(h, m, vecTr[q], D[q], 1.0, 1.0, &A, &B, &C);
+        a[q] = A;
+        b[q] = 1 / tau + B;
+        c[q] = C;
+      }
+}
+
+void xfo_adi_first_rhs(const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                       const double* hz, const double* f_1, const double* u, const double* v, const double* w,
+                       const double* D, const double* rp, double tau, double* f) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+        if (codes[q] != ACT) continue;
+        const double hX = hx[i], h_1X = hx[i - 1], hx2X = hx[i - 1] + hx[i];
+        const double hxhxhX = hx[i - 1] * hx[i] * (hx[i - 1] + hx[i]) / 2;
+        const double hY = hy[j], h_1Y = hy[j - 1], hx2Y = hy[j - 1] + hy[j];
+        const double hxhxhY = hy[j - 1] * hy[j] * (hy[j - 1] + hy[j]) / 2;
+        const double hZ = hz[k], h_1Z = hz[k - 1], hx2Z = hz[k - 1] + hz[k];
+        const double hxhxhZ = hz[k - 1] * hz[k] * (hz[k - 1] + hz[k]) / 2;
+        const double dc = D[q];
+        double F = (1 / tau) * f_1[q] + rp[q];
+        F = F + (0.5 * (-u[q]) * (f_1[q + s1] - f_1[q - s1]) / hx2X);
+        F = F + (0.5 * (dc) * ((hX * f_1[q - s1] - hx2X * f_1[q] + h_1X * f_1[q + s1]) / hxhxhX));
+        double FC = 0, FD = 0;
+        for (int item = 1; item <= 2; item++) {   /* both items read f_1 in the first step */
+          FC = FC + 0.5 * (-v[q]) * (f_1[q + s2] - f_1[q - s2]) / hx2Y;
+          FD = FD + 0.5 * (dc) * ((hY * f_1[q - s2] - hx2Y * f_1[q] + h_1Y * f_1[q + s2]) / hxhxhY);
+        }
+        F = F + FC + FD;
+        FC = 0;
+        FD = 0;
+        for (int item = 1; item <= 2; item++) {
+          FC = FC + 0.5 * (-w[q]) * (f_1[q + 1] - f_1[q - 1]) / hx2Z;
+          FD = FD + 0.5 * (dc) * ((hZ * f_1[q - 1] - hx2Z * f_1[q] + h_1Z * f_1[q + 1]) / hxhxhZ);
+        }
+        F = F + FC + FD;
+        f[q] = F;
+      }
 }
 
 int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,

@@ -125,6 +125,16 @@ int xfo_momentum_rhs(int axis, const int32_t* codes, const double* normals, int 
                      const double* hy, const double* hz, const double* border, const double* force, double* uTr,
                      double* vTr, double* wTr, double* visTr, double* rp, int64_t* bad);
 
+/* The reference's ADI line coefficients (XProblem.cpp:3149-3276): per
+ * direction a, b, c at every Actual point, and the first sweep's x-line
+ * right-hand side. */
+void xfo_adi_line_coeffs(int dir, const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                         const double* hz, const double* vecTr, const double* D, double tau, double* a, double* b,
+                         double* c);
+void xfo_adi_first_rhs(const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                       const double* hz, const double* f_1, const double* u, const double* v, const double* w,
+                       const double* D, const double* rp, double tau, double* f);
+
 #ifdef __cplusplus
 }
 #endif

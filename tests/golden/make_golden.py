@@ -289,10 +289,97 @@ def npy_fixtures():
             f.write(blob)
 
 
+def step_fixture():
+    """Two time steps of the reference's TVPProblem::SolveBySplitting on
+    workloads.reference_step_case (ref_driver task `step`), run twice: as
+    given, and with the second step's pressure solve replaced by p = 0, which
+    makes its velocity correction return the intermediate velocity u_.
+    Writes step_channel.npz: the statement, the state after step 1 (the
+    inputs of step 2), step 2's pressure right-hand side, corrected
+    velocities, control balance, ADI line systems, transfer velocities and
+    its VTK file."""
+    case = wl.reference_step_case()
+    rec = {"params": case["params"], "conc0": case["conc0"].ravel().astype(np.float64)}
+    for pre in ("p", "u", "v", "w", "n"):
+        codes, xyz, nrm, bc = case[pre]
+        rec[pre + "_dims"] = np.array(codes.shape, np.int32)
+        rec[pre + "_codes"] = codes.ravel()
+        rec[pre + "_x"], rec[pre + "_y"], rec[pre + "_z"] = xyz
+        if nrm is not None:
+            rec[pre + "_nrm"] = nrm.ravel()
+        if bc is not None:
+            rec[pre + "_bc"] = bc.ravel()
+    for pre, f in zip("uvw", case["force"]):
+        rec["force_" + pre] = f.ravel()
+    outs = {}
+    for zero_p in (0, 1):
+        with tempfile.TemporaryDirectory() as td:
+            wd = os.path.join(td, "run")
+            os.makedirs(wd)
+            os.makedirs(os.path.join(td, "Res"))
+            fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+            write_bag(fin, dict(rec, zero_p=np.array([zero_p], np.int32)))
+            # one OpenMP thread (OMP_THREAD_LIMIT caps the step's num_threads(3)
+            # regions): the three momentum equations then call the line
+            # solver in order, eq 1, 2, 3
+            env = dict(os.environ, OMP_NUM_THREADS="1", OMP_THREAD_LIMIT="1")
+            p = subprocess.run([DRIVER, "step", fin, fout], capture_output=True, text=True, timeout=600, env=env,
+                               cwd=wd)
+            if p.returncode != 0:
+                raise RuntimeError(f"step: {p.stderr[-2000:]}")
+            outs[zero_p] = read_bag(fout)
+            vtks = sorted(os.listdir(os.path.join(td, "Res")))
+            if zero_p == 0:
+                if len(vtks) != 2:
+                    raise RuntimeError(f"step: expected two VTK files, got {vtks}")
+                # flow0.0000.vtk is step 1; the other is step 2
+                outs["vtk"] = open(os.path.join(td, "Res", [v for v in vtks if v != "flow0.0000.vtk"][0]), "rb").read()
+    a, b = outs[0], outs[1]
+    save = {}
+    for pre in ("p", "u", "v", "w", "n"):
+        codes, xyz, nrm, bc = case[pre]
+        save[pre + "_codes"] = codes
+        save[pre + "_x"], save[pre + "_y"], save[pre + "_z"] = xyz
+        if nrm is not None:
+            save[pre + "_nrm"] = nrm
+        if bc is not None:
+            save[pre + "_bc"] = bc
+    shp = {pre: case[pre][0].shape for pre in ("p", "u", "v", "w")}
+    save.update(params=case["params"], conc0=case["conc0"],
+                force_u=case["force"][0], force_v=case["force"][1], force_w=case["force"][2])
+    # state after step 1 (the inputs of step 2)
+    for c in "uvw":
+        save["s1_" + c] = a["s1_" + c].reshape(shp[c])
+    for k in ("s1_p", "s1_cnc", "s1_vis"):
+        save[k] = a[k].reshape(shp["p"])
+    # step 2 as given
+    save["rhs"] = a["rhs"].reshape(shp["p"])
+    save["p0"] = a["p0"].reshape(shp["p"])
+    save["p"] = a["p"].reshape(shp["p"])
+    for c in "uvw":
+        save[c] = a[c].reshape(shp[c])
+        save["int_" + c] = b[c].reshape(shp[c])    # intermediate velocity (p = 0 run)
+    for q, c in zip((1, 2, 3), "uvw"):
+        save[f"tr_{q}"] = a[f"tr_{q}"].reshape(shp[c])
+    save["cnc"] = a["cnc"].reshape(shp["p"])
+    save["vis"] = a["vis"].reshape(shp["p"])
+    save["div_max"] = a["div_max"][0]
+    save["div_ijk"] = a["div_ijk"]
+    for k in ("line_m", "line_thread", "line_a", "line_b", "line_c", "line_f", "line_u"):
+        save[k] = a[k]
+    save["vtk"] = np.frombuffer(outs["vtk"], np.uint8)
+    # the p = 0 run must agree with the real one up to its pressure solve
+    assert np.array_equal(a["rhs"], b["rhs"]) and np.array_equal(a["line_f"][:1000], b["line_f"][:1000])
+    np.savez_compressed(os.path.join(HERE, "step_channel.npz"), **save)
+    print("step_channel.npz:", {k: np.shape(v) for k, v in save.items() if k.startswith(("line", "vtk", "rhs"))})
+
+
 if __name__ == "__main__":
     # `make_golden.py pack` / `npy` regenerate only those fixtures
     if sys.argv[1:] == ["pack"]:
         pack_fixtures()
+    elif sys.argv[1:] == ["step"]:
+        step_fixture()
     elif sys.argv[1:] == ["npy"]:
         npy_fixtures()
     else:

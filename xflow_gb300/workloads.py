@@ -351,3 +351,73 @@ def read_stl(path):
         tri = np.array(pts, dtype=np.float64).reshape(-1, 3, 3)
     verts, inv = np.unique(tri.reshape(-1, 3), axis=0, return_inverse=True)
     return verts, inv.reshape(-1, 3).astype(np.int32)
+
+
+def reference_step_case(n1=11, n2=8, n3=9, seed=11):
+    """A channel statement the reference's own time step (TVPProblem::
+    SolveBySplitting, XProblem.cpp:4255-6650) runs as given: every velocity
+    line through Actual points starts and ends on a border point (the ADI
+    sector rule, XProblem.cpp:2940-2960), and every PreDefined velocity point
+    has exactly one Actual neighbour (XProblem.cpp:5698-5735).
+
+    Pressure box n1 x n2 x n3: Actual interior, Fictive ghost layer except a
+    PreDefined outlet face (i = n1 - 1, outward normal +x, seeded border
+    pressures).  u box (n1-1) x n2 x n3: Defined inflow face (u = 1), seeded
+    PreDefined outflow face, PreDefined no-slip walls (0) on the j and k
+    faces; v and w boxes likewise with Defined zero normal velocity on their
+    own walls and PreDefined zero tangential values elsewhere.  Box edges are
+    Fictive.  Coordinates are seeded and non-uniform; the staggered boxes sit
+    at the midpoints of the pressure nodes and the node box (the VTK grid) at
+    (x_u, y_v, z_w).  Also seeded: per-cell forces for the three momentum
+    equations, and an initial concentration blob (0.45 where set,
+    XProblem.cpp:4636-4650) that gives non-uniform density and viscosity."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xp = [np.concatenate([[0.0], np.cumsum(rng.uniform(0.8, 1.2, n - 1) / (n - 1))]) for n in (n1, n2, n3)]
+    mid = [0.5 * (a[:-1] + a[1:]) for a in xp]
+
+    def faces(shape, normal_axis, normal_code, normal_val, tangential_val_hi):
+        """codes/border values of a staggered box: Actual interior, the two
+        faces across `normal_axis` Defined (normal_code), the others
+        PreDefined; edges and corners Fictive."""
+        c = np.zeros(shape, np.int32)
+        bc = np.zeros(shape)
+        c[1:-1, 1:-1, 1:-1] = 1
+        for ax in range(3):
+            for side in (0, -1):
+                sl = [slice(1, -1)] * 3
+                sl[ax] = side
+                sl = tuple(sl)
+                c[sl] = normal_code if ax == normal_axis else 4
+        return c, bc
+
+    uc, ubc = faces((n1 - 1, n2, n3), 0, 3, 1.0, None)
+    # x faces of the u box: inflow Defined u = 1, outflow PreDefined (seeded)
+    uc[0, 1:-1, 1:-1] = 3
+    ubc[0, 1:-1, 1:-1] = 1.0
+    uc[-1, 1:-1, 1:-1] = 4
+    ubc[-1, 1:-1, 1:-1] = rng.uniform(0.8, 1.2, (n2 - 2, n3 - 2))
+    vc, vbc = faces((n1, n2 - 1, n3), 1, 3, 0.0, None)
+    vbc[-1, 1:-1, 1:-1] = rng.uniform(-0.1, 0.1, (n2 - 3, n3 - 2))
+    wc, wbc = faces((n1, n2, n3 - 1), 2, 3, 0.0, None)
+    wbc[-1, 1:-1, 1:-1] = rng.uniform(-0.1, 0.1, (n2 - 2, n3 - 3))
+
+    pc = np.zeros((n1, n2, n3), np.int32)
+    pc[1:-1, 1:-1, 1:-1] = 1
+    pc[-1, 1:-1, 1:-1] = 4
+    pnrm = np.zeros((n1, n2, n3, 3))
+    pnrm[-1, 1:-1, 1:-1, 0] = 1.0
+    pbc = np.zeros((n1, n2, n3))
+    pbc[-1, 1:-1, 1:-1] = rng.uniform(-0.5, 0.5, (n2 - 2, n3 - 2))
+
+    nc = np.zeros((n1 - 1, n2 - 1, n3 - 1), np.int32)
+    nc[1:-1, 1:-1, 1:-1] = 1
+
+    ii, jj, kk = np.meshgrid(*(np.arange(n) for n in (n1, n2, n3)), indexing="ij")
+    conc0 = (((ii - n1 / 3) ** 2 + (jj - n2 / 2) ** 2 + (kk - n3 / 2) ** 2) < (min(n1, n2, n3) / 3.5) ** 2)
+    conc0 = (conc0 & (pc == 1)).astype(np.int32)
+    force = [rng.standard_normal(c.shape) * 0.3 for c in (uc, vc, wc)]
+    return dict(p=(pc, (xp[0], xp[1], xp[2]), pnrm, pbc), u=(uc, (mid[0], xp[1], xp[2]), None, ubc),
+                v=(vc, (xp[0], mid[1], xp[2]), None, vbc), w=(wc, (xp[0], xp[1], mid[2]), None, wbc),
+                n=(nc, (mid[0], mid[1], mid[2]), None, None), conc0=conc0, force=force,
+                params=np.array([1.0 / 512, 0.02, 0.05, 1.0, 1.6]))
+
