@@ -819,10 +819,12 @@ extern "C" int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, 
 // application to the next (a network), then x += alpha p, r -= alpha A p with
 // alpha = (p, r) / (p, A p).  FP64 vectors and dots.  Plain CG stays the
 // fallback and the arbiter: an iteration whose z is no descent direction
-// ((z, r) <= 0) uses z = r, and when the residual has not dropped by 10% over
-// 50 iterations the preconditioner is switched off for the rest of the solve
-// (both counted in stats->fallbacks).  The stop rule is the true relative
+// ((z, r) <= 0, or not finite) uses z = r; the third such iteration, or a
+// residual that has not dropped by 10% over 50 iterations, switches the
+// preconditioner off for the rest of the solve (all counted in
+// stats->fallbacks).  The stop rule is the true relative
 // residual ||b - A x|| <= rtol ||b||.  m = opts->reserved[0] (1..8, default 8).
+constexpr int FCG_STRIKES = 3;   // non-descent preconditioned directions before the network is switched off
 __global__ void k_fcg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
                              const double* __restrict__ q, double alpha, int64_t n) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
@@ -1193,7 +1195,7 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       double zq[FS_ZR + 1];
       if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
       if (!(zq[FS_ZR] > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
-        st->fallbacks++;
+        if (++st->fallbacks >= FCG_STRIKES) precond = XF_PRECOND_NONE;   // and from the third on, for good
         XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s));
         XF_CUDA(ctx, cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s));
         if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
@@ -1435,7 +1437,7 @@ extern "C" int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf
     double zr;
     if ((rc = read_n(ctx, FS_ZR, 1, &zr))) return fail(rc, "scalar read");
     if (!(zr > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
-      st->fallbacks++;
+      if (++st->fallbacks >= FCG_STRIKES) precond = XF_PRECOND_NONE;   // and from the third on, for good
       XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 8, cudaMemcpyDeviceToDevice, s));
     }
     // p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j over the window
