@@ -681,8 +681,10 @@ def rows(args):
     return 0
 
 
-UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=(200, 201, 202), iters=(2, 5, 10, 20, 40, 80, 120, 160, 240),
-                  steps=600, lr=2e-3)
+# 72 (residual, error) pairs (8 right-hand sides x 9 CG iterates) of a 64^3 system of the sphere family,
+# 3000 Adam steps with the learning rate halved every 1000 steps
+UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=tuple(range(200, 208)),
+                  iters=(2, 5, 10, 20, 40, 80, 120, 160, 240), steps=3000, lr=1e-3, halvings=3)
 
 
 def unet_flops(shape):
@@ -728,12 +730,13 @@ def train_unet(ctx):
     t1 = time.perf_counter()
     for step in range(T["steps"]):
         q = step % len(rs)
-        net.train_step(rs[q], es[q], lr=T["lr"], op=A)
+        net.train_step(rs[q], es[q], lr=T["lr"] * 0.5 ** (T["halvings"] * step / T["steps"]), op=A)
     ctx.synchronize()
     t2 = time.perf_counter()
     last = float(np.mean([net.train_step(r, e, update=False, op=A) for r, e in zip(rs, es)]))
     return net.params(), {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
-                          "steps": T["steps"], "lr": T["lr"], "s": t2 - t1, "harvest_s": t1 - t0,
+                          "steps": T["steps"], "lr": T["lr"], "lr_halvings": T["halvings"], "s": t2 - t1,
+                          "harvest_s": t1 - t0,
                           "anorm_loss_before": first, "anorm_loss_after": last}
 
 

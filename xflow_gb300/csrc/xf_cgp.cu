@@ -34,6 +34,15 @@
 // block sees bit-identical values.  One launch then does the work of the
 // residual update kernel and of K0, and the iteration needs two kernels.
 //
+// The learned two-level preconditioner's smoother (xf_unet.cu) uses two more
+// forms around its factor passes: the first pass takes its input as
+// r - omega q (q = A y of the prolongated coarse correction y, omega from the
+// device scalars), applied to each raw plane as it lands and to the own cells
+// of level 2; the last pass writes z = omega y + s w of its output w (zero
+// off the active set) to two buffers and reduces (z, r) and (z, q_w) with q_w
+// the flexible CG's last direction image.  They replace the separate
+// subtraction, combination and dot kernels.
+//
 // Every mbarrier wait is bounded; a wait that runs out records I_ERR, lets the
 // copies in flight land (bounded), ends the solve with XF_ERR_CUDA and leaves.
 #include <stdint.h>
@@ -64,7 +73,15 @@ struct CpArgs {
   const float *pa, *pb;       // FUSE: direction buffers (I_PBUF names the current one)
   float* e;                   // FUSE: FP32 correction
   float* rout;                // FUSE: updated residual (own cells)
-  const float* dr;            // CP_SECOND: the residual of the (r, z) dot
+  const float* dr;            // CP_SECOND / two-level last pass: the residual of the (r, z) dot
+  // two-level forms (CP_TL_*): omega = tl_omega(scalars, s_yay, s_yr)
+  int s_yay, s_yr;
+  const float* ty;            // last pass: the prolongated coarse correction y
+  const uint8_t* smask;       // last pass: space mask
+  float* z2;                  // last pass: second copy of z
+  const float* qw;            // last pass: the last direction image (nullptr: no second dot)
+  float tsc;                  // last pass: the smoother's scale s
+  int s_zr, s_zq;             // last pass: slots of (z, r) and (z, q_w)
   int n1, n3, P;
   int HA, R0, R1;             // halo unit (multiple of 4), raw region TILE + 4 HA, level-1 region TILE + 2 HA
   int KS;                     // bytes of a row-kind slot: R1 + 32 rounded up to 16
@@ -109,13 +126,19 @@ __device__ __forceinline__ void lap4(const float* dtab, uchar4 k4, float4 c, flo
 // of two quadratic factors, z = p1(A) p2(A) r, in two passes: w = p2(A) r
 // (CP_FIRST, or CP_FIRST_FUSED with the update), then z = p1(A) w with the
 // (r, z) dot against the residual buffer dr (CP_SECOND).
-enum { CP_POLY = 0, CP_POLY_FUSED = 1, CP_FIRST = 2, CP_FIRST_FUSED = 3, CP_SECOND = 4 };
+// CP_TL_FIRST, CP_TL_LAST and CP_TL_BOTH are the two-level forms (see the
+// top of this file) of a first, last or only factor pass.
+enum { CP_POLY = 0, CP_POLY_FUSED = 1, CP_FIRST = 2, CP_FIRST_FUSED = 3, CP_SECOND = 4, CP_TL_FIRST = 5,
+       CP_TL_LAST = 6, CP_TL_BOTH = 7 };
 
 template <int MODE>
 __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constant__ CpArgs a) {
   constexpr bool FUSE = MODE == CP_POLY_FUSED || MODE == CP_FIRST_FUSED;
-  constexpr bool DOTZ = MODE == CP_POLY || MODE == CP_POLY_FUSED || MODE == CP_SECOND;   // (r, z)
-  constexpr bool DOTSEP = MODE == CP_SECOND;   // r of the dot is not the input
+  constexpr bool IN_SUB = MODE == CP_TL_FIRST || MODE == CP_TL_BOTH;   // input r - omega q
+  constexpr bool OUT_TL = MODE == CP_TL_LAST || MODE == CP_TL_BOTH;    // output omega y + s w, two dots
+  constexpr bool QBUF = FUSE || IN_SUB;        // q of each raw plane arrives by bulk copy
+  constexpr bool DOTZ = MODE == CP_POLY || MODE == CP_POLY_FUSED || MODE == CP_SECOND || OUT_TL;   // (r, z)
+  constexpr bool DOTSEP = MODE == CP_SECOND || OUT_TL;   // r of the dot is not the input
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ double sh[32];
   __shared__ bool last;
@@ -127,18 +150,21 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
   uint64_t* qbar = mbar + CP_NS;
   float* ring = reinterpret_cast<float*>(smem + 128);          // CP_NS x R0 raw r
   float* yring = ring + (size_t)CP_NS * R0;                     // CP_NY x R1 level-1 planes
-  float* qbuf = yring + (size_t)CP_NY * R1;                     // FUSE: R0 cells of q
-  uint8_t* kring = reinterpret_cast<uint8_t*>(qbuf + (FUSE ? (size_t)R0 : 0));   // CP_NS x KS row kinds
+  float* qbuf = yring + (size_t)CP_NY * R1;                     // QBUF: R0 cells of q
+  uint8_t* kring = reinterpret_cast<uint8_t*>(qbuf + (QBUF ? (size_t)R0 : 0));   // CP_NS x KS row kinds
   const int KS = a.KS;
   const int64_t total = (int64_t)n1 * P;
   const int64_t total16 = (total + 15) & ~(int64_t)15;   // the kind array holds zero bytes up to here
   const int items = a.nchunk * a.tiles;
-  float alpha = 0.f;
+  float alpha = 0.f;   // FUSE: the update's step; IN_SUB: omega
   const float* pdir = a.pa;
   if (FUSE) {
     alpha = (float)S->scalars[D_ALPHA];
     if (S->iscalars[I_PBUF]) pdir = a.pb;
   }
+  float om = 0.f;
+  if (IN_SUB || OUT_TL) om = (float)tl_omega(S->scalars, a.s_yay, a.s_yr);
+  if (IN_SUB) alpha = om;
   const float* r2src = FUSE ? a.rout : a.r;   // own-cell residual of level 2
   if (threadIdx.x < 64) {
     const int b = threadIdx.x;
@@ -146,7 +172,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
               a.cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < CP_NS + (FUSE ? 1 : 0); s++) mbar_init(&mbar[s], 1);
+    for (int s = 0; s < CP_NS + (QBUF ? 1 : 0); s++) mbar_init(&mbar[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -244,13 +270,30 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     // level-2 inputs of the next plane, prefetched one step ahead (FUSE: the
     // updated residual this thread wrote three steps earlier, read through L2)
     float4 rpa = make_float4(0.f, 0.f, 0.f, 0.f), rpb = rpa, dpa = rpa, dpb = rpa;
-    uchar4 kpa = make_uchar4(0, 0, 0, 0), kpb = kpa;
+    float4 qpa = rpa, qpb = rpa, ypa = rpa, ypb = rpa, wpa = rpa, wpb = rpa;   // IN_SUB: q; OUT_TL: y, q_w
+    uchar4 kpa = make_uchar4(0, 0, 0, 0), kpb = kpa, mpa = kpa, mpb = kpa;   // OUT_TL: space mask
     auto prefetch2 = [&](int pl) {
       if (pl < i0 || pl >= i1) return;
       const int64_t o = (int64_t)pl * P;
       if (DOTSEP) {
         if (va) dpa = __ldg(reinterpret_cast<const float4*>(a.dr + o + xa));
         if (vb) dpb = __ldg(reinterpret_cast<const float4*>(a.dr + o + xb));
+      }
+      if (IN_SUB) {
+        if (va) qpa = __ldg(reinterpret_cast<const float4*>(a.q + o + xa));
+        if (vb) qpb = __ldg(reinterpret_cast<const float4*>(a.q + o + xb));
+      }
+      if (OUT_TL) {
+        if (va) {
+          ypa = __ldg(reinterpret_cast<const float4*>(a.ty + o + xa));
+          mpa = *reinterpret_cast<const uchar4*>(a.smask + o + xa);
+          if (a.qw) wpa = __ldg(reinterpret_cast<const float4*>(a.qw + o + xa));
+        }
+        if (vb) {
+          ypb = __ldg(reinterpret_cast<const float4*>(a.ty + o + xb));
+          mpb = *reinterpret_cast<const uchar4*>(a.smask + o + xb);
+          if (a.qw) wpb = __ldg(reinterpret_cast<const float4*>(a.qw + o + xb));
+        }
       }
       if (FUSE) {
         if (va) rpa = __ldcg(reinterpret_cast<const float4*>(r2src + o + xa));
@@ -273,7 +316,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       const long long L = item_first + (pl - lo);
       bool w = mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1));
       if (w) waited = L + 1;
-      if (FUSE && w) {
+      if (QBUF && w) {
         w = mbar_wait_bounded(qbar, (uint32_t)(q_waited & 1));
         if (w) q_waited++;
       }
@@ -323,7 +366,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         const int s = 2 * HA + c;
         if (s >= s_hi) continue;
         const float4 rv = upd(s);
-        if (own_plane && c < own_n) {
+        if (FUSE && own_plane && c < own_n) {
           *reinterpret_cast<float4*>(rown + c) = rv;
           float4 ev = ep[h];
           const float4 pv = pp[h];
@@ -341,7 +384,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
           }
         }
       }
-      if (own_plane) {
+      if (FUSE && own_plane) {
         acc_rr.add(psum, 1.f);
         acc_rr.add(esum, 1.f);
       }
@@ -352,17 +395,17 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     };
     long long rel_next = lo;   // next plane whose raw slot is released
     // the item's first raw plane
-    if (FUSE && threadIdx.x == 0) issue_q(lo, base);
+    if (QBUF && threadIdx.x == 0) issue_q(lo, base);
     if (FUSE) prefetch_e(lo);
     bool wok = wait_plane(lo);
-    if (FUSE && wok) update(lo);
+    if (QBUF && wok) update(lo);
     if (__syncthreads_or(!wok)) { ok = false; break; }
     for (int t = i0 - 2; t <= i1 + 2; t++) {
       const int pn = t + 1;   // the raw plane that lands during this step
       const bool has_next = pn > lo && pn <= hi;
-      if (FUSE && has_next) {
+      if (QBUF && has_next) {
         if (threadIdx.x == 0) issue_q(pn, base);
-        prefetch_e(pn);
+        if (FUSE) prefetch_e(pn);
       }
       // (B) level 1 for plane t-1: y1 = a1 r + a2 (A r) over the level-1 region
       const int p1 = t - 1;
@@ -397,13 +440,27 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
         const int64_t o = (int64_t)p2 * P;
         // (r, z) of this thread's cells: FP32 sum of the products plus the sum of
         // their exact rounding errors, into the float-float accumulator per plane
-        float psum = 0.f, esum = 0.f;
-        auto group = [&](bool v, int s, float4 rr, float4 dd, uchar4 k4, int x) {
+        float psum = 0.f, esum = 0.f, psum2 = 0.f, esum2 = 0.f;
+        auto group = [&](bool v, int s, float4 rr, float4 dd, uchar4 k4, int x, float4 qq, float4 yy, uchar4 mm,
+                         float4 ww) {
           float ay[4];
           lap4(dtab, k4, ld4(Yc + s), ld4(Ym + s), ld4(Yp + s), Yc + s, n3, a.cx, a.cy, a.cz, ay);
           if (!v) return;
-          const float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
-                               fmaf(a.a0, rr.w, ay[3])};
+          if (IN_SUB) {   // the pass input r - omega q, as the raw planes got it
+            rr.x = fmaf(-om, qq.x, rr.x);
+            rr.y = fmaf(-om, qq.y, rr.y);
+            rr.z = fmaf(-om, qq.z, rr.z);
+            rr.w = fmaf(-om, qq.w, rr.w);
+          }
+          float zz[4] = {fmaf(a.a0, rr.x, ay[0]), fmaf(a.a0, rr.y, ay[1]), fmaf(a.a0, rr.z, ay[2]),
+                         fmaf(a.a0, rr.w, ay[3])};
+          if (OUT_TL) {   // z = omega y + s w on the active set, 0 elsewhere
+            const float yv[4] = {yy.x, yy.y, yy.z, yy.w};
+            const unsigned char mv[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) zz[q] = mv[q] ? fmaf(om, yv[q], a.tsc * zz[q]) : 0.f;
+            *reinterpret_cast<float4*>(a.z2 + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
+          }
           *reinterpret_cast<float4*>(a.z + o + x) = make_float4(zz[0], zz[1], zz[2], zz[3]);
           if (!DOTZ) return;
           if (DOTSEP) rr = dd;
@@ -414,12 +471,25 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
             esum += fmaf(rv[q], zz[q], -pr);
             psum += pr;
           }
+          if (OUT_TL) {
+            const float wv[4] = {ww.x, ww.y, ww.z, ww.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const float pr = wv[q] * zz[q];
+              esum2 += fmaf(wv[q], zz[q], -pr);
+              psum2 += pr;
+            }
+          }
         };
-        group(va, ya, rpa, dpa, kpa, xa);
-        group(vb, yb, rpb, dpb, kpb, xb);
+        group(va, ya, rpa, dpa, kpa, xa, qpa, ypa, mpa, wpa);
+        group(vb, yb, rpb, dpb, kpb, xb, qpb, ypb, mpb, wpb);
         if (DOTZ) {
           acc.add(psum, 1.f);
           acc.add(esum, 1.f);
+        }
+        if (OUT_TL) {
+          acc_rr.add(psum2, 1.f);
+          acc_rr.add(esum2, 1.f);
         }
       }
       // (D) level-2 inputs of the next step
@@ -427,7 +497,7 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
       // (E) raw plane t+1 for the next step's level 1
       if (has_next) {
         wok = wait_plane(pn);
-        if (FUSE && wok) update(pn);
+        if (QBUF && wok) update(pn);
       }
       // (F) one barrier per step; a timed-out wait anywhere stops the block
       if (__syncthreads_or(!wok)) { ok = false; break; }
@@ -443,14 +513,35 @@ __global__ void __launch_bounds__(CP_THREADS, 2) k_cg_poly2(const __grid_constan
     if (threadIdx.x == 0) {
       atomicExch((unsigned long long*)&S->iscalars[I_ERR], 1ull);
       for (long long L = waited; L < issued; L++) mbar_wait_bounded(&mbar[L % CP_NS], (uint32_t)((L / CP_NS) & 1));
-      if (FUSE && q_issued > q_waited) mbar_wait_bounded(qbar, (uint32_t)(q_waited & 1));
+      if (QBUF && q_issued > q_waited) mbar_wait_bounded(qbar, (uint32_t)(q_waited & 1));
       S->iscalars[I_DONE] = 1;
       S->iscalars[I_STATUS] = XF_ERR_CUDA;
     }
     __syncthreads();
     return;
   }
-  if (MODE == CP_FIRST) return;   // the second pass reduces and steps the control
+  if (MODE == CP_FIRST || MODE == CP_TL_FIRST) return;   // a later pass reduces
+  if (OUT_TL) {   // (z, r) and (z, q_w), one ticket; no control step (the flexible CG reads them)
+    const double bzr = block_sum_acc<float>(acc, sh);
+    const double bzq = block_sum_acc<float>(acc_rr, sh);
+    if (threadIdx.x == 0) {
+      S->partials[a.s_zr][lin_block()] = bzr;
+      S->partials[a.s_zq][lin_block()] = bzq;
+      __threadfence();
+      const unsigned int tk = atomicAdd(&S->tickets[a.s_zr], 1u);
+      last = (tk == (unsigned)num_blocks() - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    const double zr = finish_partials(S, a.s_zr, sh);
+    const double zq = finish_partials(S, a.s_zq, sh);
+    if (threadIdx.x == 0) {
+      S->scalars[a.s_zr] = zr;
+      if (a.qw) S->scalars[a.s_zq] = zq;
+      S->tickets[a.s_zr] = 0;
+    }
+    return;
+  }
   if (MODE == CP_FIRST_FUSED) {   // (r, r) of the updated residual: the stop test
     if (!publish_acc<float>(S, SL_B, SL_B, acc_rr, sh, &last)) return;
     double tot = finish_partials(S, SL_B, sh);
@@ -646,7 +737,8 @@ namespace {
 
 template <int MODE>
 void poly_launch(const xf_op* op, CpArgs& a, const float coeffs[3]) {
-  constexpr bool FUSE = MODE == CP_POLY_FUSED || MODE == CP_FIRST_FUSED;
+  // a one-plane q buffer in shared memory: the fused update and the two-level first pass
+  constexpr bool FUSE = MODE == CP_POLY_FUSED || MODE == CP_FIRST_FUSED || MODE == CP_TL_FIRST || MODE == CP_TL_BOTH;
   const xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
   a.kind = g->kind; a.S = ctx->scratch;
@@ -722,4 +814,21 @@ void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, f
   CpArgs a = {};
   a.r = w; a.z = z; a.dr = r;
   poly_launch<CP_SECOND>(op, a, coeffs);
+}
+
+// The two-level smoother's first (input r - omega q) and last (output
+// z = omega y + s w into z and z2, (z, r) -> s_zr and, with qw, (z, qw) ->
+// s_zq) factor passes, or both in one (a single factor).  omega comes from
+// the device scalars s_yay, s_yr.
+void xf_cg_poly_tl_launch(const xf_op* op, bool first, bool last, const float* in, const float* q, float* out,
+                          const float coeffs[3], int s_yay, int s_yr, const float* y, float tsc, float* z2,
+                          const float* r, const float* qw, int s_zr, int s_zq) {
+  CpArgs a = {};
+  a.r = in; a.z = out; a.q = q;
+  a.s_yay = s_yay; a.s_yr = s_yr;
+  a.ty = y; a.smask = op->g->smask; a.z2 = z2; a.dr = r; a.qw = qw; a.tsc = tsc; a.s_zr = s_zr; a.s_zq = s_zq;
+  if (first && last) poly_launch<CP_TL_BOTH>(op, a, coeffs);
+  else if (first) poly_launch<CP_TL_FIRST>(op, a, coeffs);
+  else if (last) poly_launch<CP_TL_LAST>(op, a, coeffs);
+  else poly_launch<CP_FIRST>(op, a, coeffs);
 }

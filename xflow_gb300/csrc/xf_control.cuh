@@ -302,3 +302,11 @@ __device__ inline void control_step(DevScratch* S, int ctl) {
     default: break;
   }
 }
+
+// The learned two-level preconditioner's step along the prolongated coarse
+// correction y: omega = (y, r) / (y, A y), 0 when (y, A y) is not positive or
+// either dot is not finite.
+__device__ __forceinline__ double tl_omega(const double* scal, int s_yay, int s_yr) {
+  const double yay = scal[s_yay], yr = scal[s_yr];
+  return (yay > 0 && isfinite(yay) && isfinite(yr)) ? yr / yay : 0.0;
+}

@@ -36,6 +36,9 @@ int xf_op_ready(const xf_op* op);
 bool xf_cg_poly_supported(const xf_grid* g);
 bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]);
 void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
+void xf_cg_poly_tl_launch(const xf_op* op, bool first, bool last, const float* in, const float* q, float* out,
+                          const float coeffs[3], int s_yay, int s_yr, const float* y, float tsc, float* z2,
+                          const float* r, const float* qw, int s_zr, int s_zq);
 void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
                              const float* pa, const float* pb, float* e, float* r_out);
 
@@ -982,28 +985,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_f4(const float* __restrict_
     S->tickets[slot] = 0;
   }
 }
-// FP32 forms with omega = (y, r) / (y, A y) read from the device scalars (no host round trip)
-__device__ __forceinline__ double tl_omega(const double* scal, int s_yay, int s_yr) {
-  const double yay = scal[s_yay], yr = scal[s_yr];
-  return (yay > 0 && isfinite(yay) && isfinite(yr)) ? yr / yay : 0.0;
-}
-__global__ void k_sub_dev(const float* __restrict__ r, const float* __restrict__ q, const double* scal, int s_yay,
-                          int s_yr, int64_t n, float* __restrict__ out) {
-  const float om = (float)tl_omega(scal, s_yay, s_yr);
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
-    out[c] = fmaf(-om, q[c], r[c]);
-}
-// z (and a second copy z2, the FCG's next direction before its orthogonalisation)
-__global__ void k_twolevel_dev(const float* __restrict__ y, const float* __restrict__ w, const double* scal, int s_yay,
-                               int s_yr, float sc, const uint8_t* __restrict__ smask, int64_t n, float* __restrict__ z,
-                               float* __restrict__ z2) {
-  const float om = (float)tl_omega(scal, s_yay, s_yr);
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-    const float v = smask[c] ? fmaf(om, y[c], sc * w[c]) : 0.f;
-    z[c] = v;
-    z2[c] = v;
-  }
-}
 // mixed FCG vector kernels (FP32 vectors)
 __global__ void k_fcg_update_f(float* __restrict__ e, float* __restrict__ r, const float* __restrict__ p,
                                const float* __restrict__ q, float alpha, int64_t n) {
@@ -1110,9 +1091,11 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
   const double* b = (const double*)bv->data;
   int precond = XF_PRECOND_UNET2, rcode;
   long long launches = 0;   // this library's kernels launched by the solve
-  // z = M r in FP32
-  // z = M r in FP32, also into z2 (the next direction's slot)
-  auto apply_m = [&](float* z2) -> int {
+  // z = M r in FP32, also into z2 (the next direction's slot); with the
+  // network on, also (z, r) -> FS_ZR and, when qw is given, (z, qw) -> slot 0
+  // (the smoother's last pass reduces them); returns whether it did
+  auto apply_m = [&](float* z2, const float* qw, bool* dots_done) -> int {
+    *dots_done = false;
     if (precond != XF_PRECOND_UNET2) {
       return cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
                      cudaMemcpyAsync(z2, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess
@@ -1133,15 +1116,18 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
     xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
     xf_dot_async(cg, XF_F64, zc, rc, FS_YR);   // (y, r) = (z_c, P^T r)
-    const double* scal = ctx->scratch->scalars;
-    k_sub_dev<<<eb, 256, 0, s>>>(r, ay, scal, FS_YAY, FS_YR, n, w0);   // r - omega A y
-    float *src = w0, *dst = w1;
+    // the smoother: its first pass takes r - omega A y, its last writes
+    // z = omega y + s p(A)(r - omega A y) and reduces the dots
+    float *src = nullptr, *dst = w0;
     for (int k = tl_nf - 1; k >= 0; k--) {
-      xf_cg_poly_first_launch(op, src, dst, tl_f[k], nullptr, nullptr, nullptr, nullptr, nullptr);
-      std::swap(src, dst);
+      const bool first = k == tl_nf - 1, last = k == 0;
+      xf_cg_poly_tl_launch(op, first, last, first ? r : src, ay, last ? z : dst, tl_f[k], FS_YAY, FS_YR, y,
+                           (float)tl_scale, z2, r, qw, FS_ZR, 0);
+      src = dst;
+      dst = dst == w0 ? w1 : w0;
     }
-    k_twolevel_dev<<<eb, 256, 0, s>>>(y, src, scal, FS_YAY, FS_YR, (float)tl_scale, g->smask, n, z, z2);
-    launches += 6 + UNET_FORWARD_LAUNCHES + tl_nf;
+    *dots_done = true;
+    launches += 4 + UNET_FORWARD_LAUNCHES + tl_nf;
     return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
   };
   // r = float(b - A x), the residual computed in FP64 (zero off the active set), its (r, r) in FP64
@@ -1184,21 +1170,24 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
     while (true) {
       it++;
       float *pn = P[head], *qn = Q[head];
-      if ((rcode = apply_m(pn))) return fail(rcode, "preconditioner");
-      // (z, r) and (z, A p_j) over the window, one read
-      auto dots_z = [&](double* zq) -> int {
-        fdot(z, r, FS_ZR);
-        for (int j = 0; j < nwin; j++) fdot(z, Q[(head + m + 1 - 1 - j) % (m + 1)], j);
-        launches += 1 + nwin;
+      // (z, r) and (z, A p_j) over the window, one read (the smoother's last
+      // pass has reduced (z, r) and the newest window term already)
+      const float* q_newest = nwin > 0 ? Q[(head + m) % (m + 1)] : nullptr;
+      bool fused_dots = false;
+      if ((rcode = apply_m(pn, q_newest, &fused_dots))) return fail(rcode, "preconditioner");
+      auto dots_z = [&](double* zq, bool fused) -> int {
+        if (!fused) fdot(z, r, FS_ZR);
+        for (int j = fused ? 1 : 0; j < nwin; j++) fdot(z, Q[(head + m + 1 - 1 - j) % (m + 1)], j);
+        launches += (fused ? 0 : 1) + nwin - (fused && nwin > 0 ? 1 : 0);
         return read_n(ctx, 0, FS_ZR + 1, zq);
       };
       double zq[FS_ZR + 1];
-      if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
+      if ((rcode = dots_z(zq, fused_dots))) return fail(rcode, "scalar read");
       if (!(zq[FS_ZR] > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
         if (++st->fallbacks >= FCG_STRIKES) precond = XF_PRECOND_NONE;   // and from the third on, for good
         XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s));
         XF_CUDA(ctx, cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s));
-        if ((rcode = dots_z(zq))) return fail(rcode, "scalar read");
+        if ((rcode = dots_z(zq, false))) return fail(rcode, "scalar read");
       }
       // the new direction p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j in ring slot `head` (holding z)
       if (nwin > 0) {
