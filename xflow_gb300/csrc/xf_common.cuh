@@ -101,6 +101,9 @@ struct xf_op {
   // device staging boxes of xf_solve_host, kept between calls
   xf_vec* host_x = nullptr;
   xf_vec* host_b = nullptr;
+  // unique per operator ever created (a graph built for one operator is never
+  // replayed on another that reuses its address)
+  unsigned long long serial = 0;
 };
 
 // ---------------------------------------------------------------------------

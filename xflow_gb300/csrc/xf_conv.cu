@@ -487,6 +487,18 @@ constexpr int I_CONV_ERR = 60;
 static int* conv_err_flag(xf_ctx* ctx) { return reinterpret_cast<int*>(&ctx->scratch->iscalars[I_CONV_ERR]); }
 
 // Launch on the context stream (arguments checked by the caller).
+// The dynamic shared-memory attribute of a convolution kernel, raised once
+// per kernel and device to the largest size asked for (so that the launches
+// of a captured solve set no attribute).
+static cudaError_t set_max_smem(const void* kern, int which, int device, size_t smem) {
+  static size_t done[4][64] = {};
+  size_t& d = done[which][device & 63];
+  if (smem <= d) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) d = smem;
+  return e;
+}
+
 int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci, const void* weights,
                    const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
                    int relu, const void* gate, int gate_ld) {
@@ -505,7 +517,7 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
     const int KC = ci == 16 ? 16 : ci == 48 ? 48 : ci % 32 == 0 ? 32 : 16;
     auto kern = KC == 16 ? k_conv3_st<16> : KC == 32 ? k_conv3_st<32> : k_conv3_st<48>;
     const size_t smem = (size_t)ST_STAGES * ((128 + 3 * co) * KC * 2);
-    XF_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    XF_CUDA(ctx, set_max_smem((const void*)kern, KC == 16 ? 0 : KC == 32 ? 1 : 2, ctx->device, smem));
     int per_sm = (int)((227 * 1024) / (smem + 3 * 1024 + 1024));
     per_sm = min(per_sm, (int)(512 / tmem_cols(3 * co)));
     per_sm = min(per_sm, 16);
@@ -518,7 +530,7 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
     return XF_OK;
   }
   const size_t smem = (size_t)CONV_STAGES * (TC_M * ci * 2 + co * ci * 2);
-  XF_CUDA(ctx, cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  XF_CUDA(ctx, set_max_smem((const void*)k_conv3_tc, 3, ctx->device, smem));
   // Residency from the kernel's real limits: shared memory (227 KB per SM, with
   // ~1 KB static and reserved per CTA), tensor-memory columns (512 per SM) and
   // threads (2048 per SM).

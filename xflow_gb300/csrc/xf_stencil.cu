@@ -7,6 +7,7 @@
 // prefetching plane i+2 while it computes plane i.  Consecutive threads own
 // consecutive k, so every plane access is coalesced; the j+-1 / k+-1
 // neighbours are re-reads of lines the neighbouring threads just fetched (L1/L2).
+#include <atomic>
 #include <type_traits>
 
 #include "xf_control.cuh"
@@ -231,8 +232,10 @@ extern "C" int xf_op_create(xf_grid* g, int kind, xf_op** out) {
                    "operator %d is not defined at cell (%d,%d,%d): the reference throws or reads outside its arrays there",
                    kind, i, j, k);
   }
+  static std::atomic<unsigned long long> serials{0};
   xf_op* op = new xf_op();
   op->g = g; op->kind = kind; op->rho = nullptr; op->rho32 = nullptr; op->rho_set = 0;
+  op->serial = ++serials;
   if (kind == XF_OP_VARDIV) {
     xf_ctx* ctx = g->ctx;
     if (cudaMalloc(&op->rho, g->ncell * 8) != cudaSuccess || cudaMalloc(&op->rho32, g->ncell * 4) != cudaSuccess) {

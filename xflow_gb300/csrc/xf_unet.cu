@@ -78,7 +78,11 @@ struct Layer {
 
 }  // namespace
 
+struct TlGraph;   // the graph-driven mixed two-level solve, kept with the network (below)
+void xf_tl_graph_free(TlGraph* t);
+
 struct xf_unet {
+  TlGraph* tlg = nullptr;
   xf_ctx* ctx;
   const xf_grid* g;
   Level L[3];
@@ -451,6 +455,7 @@ static void unet_free(xf_unet* u) {
   if (u->bpart) cudaFree(u->bpart);
   if (u->zd) cudaFree(u->zd);
   if (u->az) cudaFree(u->az);
+  if (u->tlg) xf_tl_graph_free(u->tlg);
   delete u;
 }
 
@@ -962,10 +967,12 @@ __global__ void k_prolong4v(const double* __restrict__ zc, int c2, int c3, const
 // (a, b) of FP32 boxes that are zero off the active set: exact products
 // accumulated in float-float per thread and per warp, FP64 across warps and
 // blocks; 16-byte loads.  -> scalars[slot]
+// skip (may be null): a device flag; when set the dot is not computed
 __global__ void __launch_bounds__(RED_THREADS) k_dot_f4(const float* __restrict__ a, const float* __restrict__ b,
-                                                        int64_t n, DevScratch* S, int slot) {
+                                                        int64_t n, DevScratch* S, int slot, const int* skip) {
   __shared__ double sh[32];
   __shared__ bool last;
+  if (skip && *skip) return;
   DotAcc<float> acc;
   const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
   const float4* a4 = reinterpret_cast<const float4*>(a);
@@ -1033,18 +1040,226 @@ static int read_n(xf_ctx* ctx, int first, int count, double* out) {
   return XF_OK;
 }
 
-// Mixed-precision FCG(m) with the learned two-level preconditioner: the
-// correction e, the residual r, the directions and their images are FP32;
-// the dots are accumulated in FP64 (exact FP32 products summed in
-// float-float, then FP64); alpha and the window coefficients are FP64.  The
-// FP32 recursion is refreshed from the true residual b - A x, computed in
-// FP64 after x += e, every `replace_every` iterations, whenever its (r, r)
-// has dropped by 10^6 since the last refresh, and when it meets the
-// tolerance; the window of directions is kept across a refresh (each new
-// direction is still A-orthogonalised against it).  The solve ends only on
-// the true FP64 residual.
-static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, int m, int F, const float (*tl_f)[3],
-                               int tl_nf, double tl_scale, xf_vec* xv, const xf_vec* bv, xf_solve_stats* st) {
+// ---------------------------------------------------------------------------
+// Mixed-precision FCG(m) with the learned two-level preconditioner, driven
+// entirely on the device: the correction e, the residual r, the directions
+// and their images are FP32; the dots are accumulated in FP64 (exact FP32
+// products summed in float-float, then FP64); alpha and the window
+// coefficients are FP64.  The FP32 recursion is refreshed from the true
+// residual b - A x, computed in FP64 after x += e, every `replace_every`
+// iterations, whenever its (r, r) has dropped by 10^6 since the last
+// refresh, and when it meets the tolerance; the window of directions is kept
+// across a refresh.  The solve ends only on the true FP64 residual.
+//
+// Every scalar decision (alpha, the window coefficients, the fallback to
+// z = r, the refresh and stop tests) is taken by one-thread control kernels
+// on the device, and the whole solve is one CUDA graph with conditional
+// nodes, so it needs no host round trip:
+//
+//   init: (b, b), the tolerance, the state
+//   WHILE (not done):
+//     IF (refresh):   x += e (after a cycle), e = 0, r = float(b - A x) in
+//                     FP64 with (r, r); the stop, iteration-cap and stall
+//                     tests
+//     IF (head == 0): one iteration with direction slot 0
+//     ...
+//     IF (head == m): one iteration with direction slot m
+//     the loop guard
+//
+// The m + 1 iteration blocks are the ring positions of the new direction, so
+// every kernel argument is fixed at capture.  Inside an iteration block:
+//   IF/ELSE (network on): z = M r (restriction, U-Net, prolongation, A y, the
+//                         smoother passes reducing (z, r), (z, q_0)) /
+//                         z = r with its dots
+//   IF (no descent direction, (z, r) <= 0): z = r with its dots; the third
+//                         time the network is switched off
+//   p = z - sum_j (z, q_j) / (p_j, q_j) p_j, q = A p, (p, q), (p, r), alpha,
+//   e += alpha p, r -= alpha q, (r, r), the cycle-end test.
+// The loop guard ends the loop when the solve is done, and with an error
+// status if a pass made no iteration (the control always runs one per pass
+// until it ends the solve) or the passes exceed the iteration cap, so the
+// device loop ends whatever the handles hold.  The graph, the workspace and
+// the state are built once per operator, vectors and settings, and kept with
+// the network.
+struct TlCtl {
+  double bb, thr, rr_true, rr_prev_true, rr, rr_start, alpha;
+  double pq_win[9];
+  float coef[8];
+  int use_coef[8];
+  int win_off[8];   // window dot j skipped (j >= nwin)
+  int it, it_start, maxit, every, repl, prev_cycle, fallbacks, precond_on, head, nwin, done, status, brk, cycle_ran;
+  int passes, it_seen;   // the loop guard
+  long long launches;
+};
+struct TlParams {
+  double rtol2;
+  int maxit, every;
+  // kernels per segment, for the launch count
+  int n_ref, n_iter, n_on, n_off, n_fb;
+};
+struct TlHandles {
+  cudaGraphConditionalHandle main, ref, blk[9], pre[9], fb[9];
+};
+
+struct TlGraph {
+  unsigned long long op_serial = 0;
+  const void *x = nullptr, *b = nullptr;
+  int m = 0, F = 0, nf = 0;
+  float f[6][3] = {};
+  double scale = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void*> bufs;
+  TlCtl* ctl = nullptr;
+  TlParams* prm = nullptr;
+  ~TlGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : bufs) cudaFree(p);
+  }
+};
+
+void xf_tl_graph_free(TlGraph* t) { delete t; }
+
+__global__ void k_tl_init(DevScratch* S, TlCtl* c, const TlParams* p, TlHandles h, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  cudaGraphSetConditional(h.ref, 1u);   // the loop starts with a refresh
+  for (int k = 0; k <= m; k++) cudaGraphSetConditional(h.blk[k], 0u);
+  c->passes = 0; c->it_seen = 0;
+  c->bb = S->scalars[FS_RR];
+  c->thr = p->rtol2 * c->bb;
+  c->maxit = p->maxit; c->every = p->every;
+  c->it = 0; c->it_start = 0; c->repl = 0; c->prev_cycle = 0; c->fallbacks = 0; c->precond_on = 1;
+  c->head = 0; c->nwin = 0; c->done = 0; c->status = XF_OK; c->brk = 0; c->cycle_ran = 0;
+  c->rr_true = 0; c->rr_prev_true = 0; c->rr = 0; c->rr_start = 0; c->alpha = 0;
+  for (int j = 0; j < 9; j++) c->pq_win[j] = 0;
+  for (int j = 0; j < 8; j++) { c->coef[j] = 0.f; c->use_coef[j] = 0; c->win_off[j] = 1; }
+  c->launches = 2;
+}
+// x += e after a cycle (none before the first)
+__global__ void k_tl_fold(double* __restrict__ x, const float* __restrict__ e, int64_t n, const TlCtl* c) {
+  if (!c->cycle_ran) return;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    x[q] += (double)e[q];
+}
+// after the refresh: the stop, cap and stall tests; the next block
+__global__ void k_tl_top(DevScratch* S, TlCtl* c, const TlParams* p, TlHandles h, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  c->cycle_ran = 0;
+  c->launches += p->n_ref;
+  const double rr = S->scalars[FS_PQ + 1];
+  c->rr_true = rr;
+  if (c->brk) {
+    c->done = 1;
+  } else if (rr <= c->thr) {
+    c->done = 1;
+  } else if (isnan(rr)) {
+    c->done = 1; c->status = XF_NAN;
+  } else if (c->it >= c->maxit) {
+    c->done = 1; c->status = XF_MAXIT;
+  } else {
+    // no progress over a whole refresh cycle of 10 or more iterations: plain CG from here on
+    if (c->repl > 0 && c->precond_on && c->prev_cycle >= 10 && !(rr < 0.81 * c->rr_prev_true)) {
+      c->precond_on = 0;
+      c->fallbacks++;
+    }
+    c->rr_prev_true = rr;
+    c->rr_start = rr;
+    c->rr = rr;
+    c->it_start = c->it;
+  }
+  cudaGraphSetConditional(h.main, c->done ? 0u : 1u);
+  cudaGraphSetConditional(h.ref, 0u);
+  for (int k = 0; k <= m; k++) cudaGraphSetConditional(h.blk[k], (!c->done && k == c->head) ? 1u : 0u);
+}
+__global__ void k_tl_it(TlCtl* c, const TlParams* p, cudaGraphConditionalHandle pre, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  c->it++;
+  for (int j = 0; j < m; j++) c->win_off[j] = j >= c->nwin;
+  c->launches += p->n_iter + (c->precond_on ? p->n_on : p->n_off);
+  cudaGraphSetConditional(pre, c->precond_on ? 1u : 0u);
+}
+__global__ void k_tl_z(DevScratch* S, TlCtl* c, const TlParams* p, cudaGraphConditionalHandle fb) {
+  if (threadIdx.x | blockIdx.x) return;
+  const bool bad = !(S->scalars[FS_ZR] > 0) && c->precond_on;   // no descent direction: use r this time
+  if (bad) {
+    if (++c->fallbacks >= FCG_STRIKES) c->precond_on = 0;   // and from the third on, for good
+    c->launches += p->n_fb;
+  }
+  cudaGraphSetConditional(fb, bad ? 1u : 0u);
+}
+// the window coefficients -(z, q_j) / (p_j, q_j) of the block with direction slot hd
+__global__ void k_tl_coef(const DevScratch* S, TlCtl* c, int hd, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  for (int j = 0; j < m; j++) {
+    const int sl = (hd + m - j) % (m + 1);
+    const bool use = j < c->nwin && c->pq_win[sl] > 0;
+    c->use_coef[j] = use;
+    c->coef[j] = use ? (float)(-S->scalars[j] / c->pq_win[sl]) : 0.f;
+  }
+}
+__global__ void k_tl_axpy(float* __restrict__ y, const float* __restrict__ x, const TlCtl* c, int j, int64_t n) {
+  if (!c->use_coef[j]) return;
+  const float a = c->coef[j];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    y[q] = fmaf(a, x[q], y[q]);
+}
+__global__ void k_tl_alpha(const DevScratch* S, TlCtl* c, int hd, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  const double pr = S->scalars[FS_PR], pq = S->scalars[FS_PQ];
+  if (!(pq > 0)) {
+    c->status = isnan(pq) ? XF_NAN : XF_BREAKDOWN;
+    c->brk = 1;
+    return;
+  }
+  c->alpha = pr / pq;
+  c->pq_win[hd] = pq;
+  c->head = (hd + 1) % (m + 1);
+  if (c->nwin < m) c->nwin++;
+}
+__global__ void k_tl_update(float* __restrict__ e, float* __restrict__ r, const float* __restrict__ p,
+                            const float* __restrict__ q, const TlCtl* c, int64_t n) {
+  if (c->brk) return;
+  const float alpha = (float)c->alpha;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    e[k] = fmaf(alpha, p[k], e[k]);
+    r[k] = fmaf(-alpha, q[k], r[k]);
+  }
+}
+// The last node of the loop body: see the loop guard above.
+__global__ void k_tl_guard(TlCtl* c, TlHandles h) {
+  if (threadIdx.x | blockIdx.x) return;
+  c->passes++;
+  if (!c->done && (c->it == c->it_seen || c->passes > c->maxit + 16)) {
+    c->done = 1;
+    c->status = XF_ERR_CUDA;
+  }
+  c->it_seen = c->it;
+  cudaGraphSetConditional(h.main, c->done ? 0u : 1u);
+}
+// the cycle-end test after the iteration in block hd; sets the next block
+__global__ void k_tl_rr(const DevScratch* S, TlCtl* c, TlHandles h, int hd, int m) {
+  if (threadIdx.x | blockIdx.x) return;
+  bool end = c->brk != 0;
+  if (!end) {
+    const double rr = S->scalars[FS_RR];
+    c->rr = rr;
+    end = isnan(rr) || rr <= c->thr || rr <= 1e-6 * c->rr_start || c->it - c->it_start >= c->every ||
+          c->it >= c->maxit;
+  }
+  if (end) {
+    c->cycle_ran = 1;
+    c->repl++;
+    c->prev_cycle = c->it - c->it_start;
+    cudaGraphSetConditional(h.ref, 1u);
+    for (int k = hd + 1; k <= m; k++) cudaGraphSetConditional(h.blk[k], 0u);
+  } else {
+    cudaGraphSetConditional(h.blk[hd < m ? hd + 1 : 0], 1u);
+  }
+}
+
+static int tl_graph_build(xf_op* op, xf_unet* u, int m, int F, const float (*tl_f)[3], int tl_nf, double tl_scale,
+                          xf_vec* xv, const xf_vec* bv, TlGraph** out) {
   xf_grid* g = op->g;
   xf_ctx* ctx = g->ctx;
   const xf_grid* cg = u->g;
@@ -1052,10 +1267,11 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
   cudaStream_t s = ctx->stream;
   const int eb = grid_blocks(ctx, n, 256);
   const int db = red_blocks(ctx, (n + 3) / 4);
-  auto fdot = [&](const float* a, const float* b2, int slot) {
-    k_dot_f4<<<db, RED_THREADS, 0, s>>>(a, b2, n, ctx->scratch, slot);
+  TlGraph* t = new TlGraph();
+  auto fail = [&](int code, const char* msg) {
+    delete t;
+    return xf_fail(ctx, code, "xf_solve_fcg: %s", msg);
   };
-  std::vector<void*> bufs;
   auto alloc = [&](size_t bytes) -> void* {
     void* p = nullptr;
     if (cudaMalloc(&p, bytes) != cudaSuccess) {
@@ -1063,52 +1279,131 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       return nullptr;
     }
     cudaMemsetAsync(p, 0, bytes, s);
-    bufs.push_back(p);
+    t->bufs.push_back(p);
     return p;
-  };
-  auto cleanup = [&]() {
-    for (void* p : bufs) cudaFree(p);
-  };
-  auto fail = [&](int code, const char* msg) {
-    cleanup();
-    return xf_fail(ctx, code, "xf_solve_fcg: %s", msg);
   };
   double *rc = (double*)alloc(nc * 8), *zc = (double*)alloc(nc * 8);
   float *r = (float*)alloc(n * 4), *e = (float*)alloc(n * 4), *z = (float*)alloc(n * 4), *y = (float*)alloc(n * 4);
   float *ay = (float*)alloc(n * 4), *w0 = (float*)alloc(n * 4), *w1 = (float*)alloc(n * 4);
+  t->ctl = (TlCtl*)alloc(sizeof(TlCtl));
+  t->prm = (TlParams*)alloc(sizeof(TlParams));
   float *P[9] = {nullptr}, *Q[9] = {nullptr};   // ring of m + 1: the new direction and the window
-  bool ok = rc && zc && r && e && z && y && ay && w0 && w1;
+  bool ok = rc && zc && r && e && z && y && ay && w0 && w1 && t->ctl && t->prm;
   for (int j = 0; j <= m && ok; j++) ok = (P[j] = (float*)alloc(n * 4)) && (Q[j] = (float*)alloc(n * 4));
-  if (ok) {   // the Chebyshev passes return at once while a mixed solve's done / pause flags are set
-    long long zero = 0;
-    ok = cudaMemcpyAsync(&ctx->scratch->iscalars[I_DONE], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaMemcpyAsync(&ctx->scratch->iscalars[I_PAUSE], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaMemcpyAsync(&ctx->scratch->iscalars[I_ERR], &zero, 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaStreamSynchronize(s) == cudaSuccess;
-  }
   if (!ok) return fail(XF_ERR_NOMEM, "allocation");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(XF_ERR_CUDA, "workspace");
   double* x = (double*)xv->data;
   const double* b = (const double*)bv->data;
-  int precond = XF_PRECOND_UNET2, rcode;
-  long long launches = 0;   // this library's kernels launched by the solve
-  // z = M r in FP32, also into z2 (the next direction's slot); with the
-  // network on, also (z, r) -> FS_ZR and, when qw is given, (z, qw) -> slot 0
-  // (the smoother's last pass reduces them); returns whether it did
-  auto apply_m = [&](float* z2, const float* qw, bool* dots_done) -> int {
-    *dots_done = false;
-    if (precond != XF_PRECOND_UNET2) {
-      return cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
-                     cudaMemcpyAsync(z2, r, n * 4, cudaMemcpyDeviceToDevice, s) == cudaSuccess
-                 ? XF_OK
-                 : XF_ERR_CUDA;
-    }
+  DevScratch* S = ctx->scratch;
+  TlCtl* c = t->ctl;
+  const TlParams* prm = t->prm;
+  auto fdot = [&](const float* a, const float* b2, int slot, const int* skip) {
+    k_dot_f4<<<db, RED_THREADS, 0, s>>>(a, b2, n, S, slot, skip);
+  };
+  // the window dots j = j0 .. m-1 of block hd (skipped on the device while j >= nwin)
+  auto win_dots = [&](int hd, int j0) {
+    for (int j = j0; j < m; j++) fdot(z, Q[(hd + m - j) % (m + 1)], j, &c->win_off[j]);
+  };
+  // warm the network's kernels (attributes, first launches) outside capture
+  int rcode = xf_unet_apply_dev(u, rc, zc);
+  if (rcode) {
+    delete t;
+    return rcode;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(XF_ERR_CUDA, "warm-up");
+
+  TlHandles H;
+  cudaGraph_t top = nullptr;
+  if (cudaGraphCreate(&top, 0) != cudaSuccess) return fail(XF_ERR_CUDA, "graph");
+  t->graph = top;
+  cudaError_t ce = cudaSuccess;
+  // capture a sequence into graph gr after the nodes deps ...
+  auto begin = [&](cudaGraph_t gr, const cudaGraphNode_t* deps, size_t nd) {
+    if (ce == cudaSuccess) ce = cudaStreamBeginCaptureToGraph(s, gr, deps, nullptr, nd, cudaStreamCaptureModeThreadLocal);
+  };
+  // ... and end it, returning its tail
+  auto end_tail = [&](std::vector<cudaGraphNode_t>& tail) {
+    if (ce != cudaSuccess) return;
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* d = nullptr;
+    size_t nd = 0;
+    ce = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &d, nullptr, &nd);
+    if (ce == cudaSuccess) tail.assign(d, d + nd);
+    cudaGraph_t dummy = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &dummy);
+    if (ce == cudaSuccess) ce = e2;
+  };
+  auto add_cond = [&](cudaGraph_t gr, const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle hnd,
+                      cudaGraphConditionalNodeType type, unsigned size, cudaGraph_t* bodies,
+                      cudaGraphNode_t* node) {
+    if (ce != cudaSuccess) return;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hnd;
+    np.conditional.type = type;
+    np.conditional.size = size;
+    ce = cudaGraphAddNode(node, gr, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np);
+    if (ce == cudaSuccess)
+      for (unsigned q = 0; q < size; q++) bodies[q] = np.conditional.phGraph_out[q];
+  };
+  auto handle = [&](cudaGraph_t gr, cudaGraphConditionalHandle* hnd, unsigned dflt, unsigned flags) {
+    if (ce == cudaSuccess) ce = cudaGraphConditionalHandleCreate(hnd, gr, dflt, flags);
+  };
+
+  // the loop node and the handles of its body's blocks first (the init kernel sets them)
+  std::vector<cudaGraphNode_t> tail, unused;
+  handle(top, &H.main, 1, cudaGraphCondAssignDefault);
+  cudaGraph_t wbody = nullptr;
+  cudaGraphNode_t wnode = nullptr;
+  add_cond(top, {}, H.main, cudaGraphCondTypeWhile, 1, &wbody, &wnode);
+  handle(wbody, &H.ref, 1, 0);
+  for (int k = 0; k <= m; k++) handle(wbody, &H.blk[k], 0, 0);
+  // init: (b, b), the state, the block handles; before the loop
+  begin(top, nullptr, 0);
+  xf_dot_async(g, XF_F64, b, b, FS_RR);
+  k_tl_init<<<1, 32, 0, s>>>(S, c, prm, H, m);
+  end_tail(tail);
+  if (ce == cudaSuccess) {
+    const std::vector<cudaGraphNode_t> to(tail.size(), wnode);   // every tail node before the loop
+    ce = cudaGraphAddDependencies(top, tail.data(), to.data(), nullptr, tail.size());
+  }
+  // refresh block
+  cudaGraph_t rbody = nullptr;
+  cudaGraphNode_t prev = nullptr;
+  add_cond(wbody, {}, H.ref, cudaGraphCondTypeIf, 1, &rbody, &prev);
+  begin(rbody, nullptr, 0);
+  k_tl_fold<<<eb, 256, 0, s>>>(x, e, n, c);
+  cudaMemsetAsync(e, 0, n * 4, s);
+  xf_cg_res64(op, x, b, r, FS_PQ, CTL_NONE);   // r = float(b - A x), (r, r) in FP64 -> FS_PQ + 1
+  k_tl_top<<<1, 32, 0, s>>>(S, c, prm, H, m);   // reads H.main, H.ref, H.blk only
+  end_tail(unused);
+  // iteration blocks
+  int n_on = 0, n_off = 0, n_fb = 0, n_iter = 0;
+  for (int hd = 0; hd <= m; hd++) {
+    cudaGraph_t bbody = nullptr;
+    cudaGraphNode_t bnode = nullptr;
+    add_cond(wbody, {prev}, H.blk[hd], cudaGraphCondTypeIf, 1, &bbody, &bnode);
+    prev = bnode;
+    handle(bbody, &H.pre[hd], 0, 0);
+    handle(bbody, &H.fb[hd], 0, 0);
+    float* pn = P[hd];
+    float* qn = Q[hd];
+    const float* q_newest = Q[(hd + m) % (m + 1)];
+    // it++, the network-on test
+    begin(bbody, nullptr, 0);
+    k_tl_it<<<1, 32, 0, s>>>(c, prm, H.pre[hd], m);
+    end_tail(tail);
+    cudaGraph_t ie[2] = {nullptr, nullptr};
+    cudaGraphNode_t ienode = nullptr;
+    add_cond(bbody, tail, H.pre[hd], cudaGraphCondTypeIf, 2, ie, &ienode);
+    // network on: z = M r with (z, r) and (z, q_newest)
+    begin(ie[0], nullptr, 0);
     if (F == 4)
       k_restrict4<<<dim3((cg->n3 + 63) / 64, cg->n2, cg->n1), 64, 0, s>>>(r, g->n2, g->n3, rc, cg->n1, cg->n2, cg->n3);
     else
       k_restrict_blocks<float><<<grid_blocks(ctx, nc, 256), 256, 0, s>>>(r, g->n2, g->n3, F, rc, cg->n1, cg->n2,
                                                                          cg->n3);
-    int st2 = xf_unet_apply_dev(u, rc, zc);
-    if (st2) return st2;
+    if (ce == cudaSuccess && (rcode = xf_unet_apply_dev(u, rc, zc))) ce = cudaErrorUnknown;
     if (F == 4)   // n2 n3 is a multiple of 4 (see k_prolong4v)
       k_prolong4v<<<dim3((g->n2 * g->n3 / 4 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1,
                                                                               g->n2, g->n3, y);
@@ -1116,134 +1411,130 @@ static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, in
       k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
     xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
     xf_dot_async(cg, XF_F64, zc, rc, FS_YR);   // (y, r) = (z_c, P^T r)
-    // the smoother: its first pass takes r - omega A y, its last writes
-    // z = omega y + s p(A)(r - omega A y) and reduces the dots
-    float *src = nullptr, *dst = w0;
-    for (int k = tl_nf - 1; k >= 0; k--) {
-      const bool first = k == tl_nf - 1, last = k == 0;
-      xf_cg_poly_tl_launch(op, first, last, first ? r : src, ay, last ? z : dst, tl_f[k], FS_YAY, FS_YR, y,
-                           (float)tl_scale, z2, r, qw, FS_ZR, 0);
-      src = dst;
-      dst = dst == w0 ? w1 : w0;
-    }
-    *dots_done = true;
-    launches += 4 + UNET_FORWARD_LAUNCHES + tl_nf;
-    return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ERR_CUDA;
-  };
-  // r = float(b - A x), the residual computed in FP64 (zero off the active set), its (r, r) in FP64
-  // -> scalars[FS_PQ + 1]
-  auto true_residual = [&](double* rr) -> int {
-    xf_cg_res64(op, x, b, r, FS_PQ, CTL_NONE);
-    launches++;
-    double v[2];
-    int st2 = read_n(ctx, FS_PQ, 2, v);
-    *rr = v[1];
-    return st2;
-  };
-  XF_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-  xf_dot_async(g, XF_F64, b, b, FS_RR);
-  launches++;
-  double bb;
-  if ((rcode = read_n(ctx, FS_RR, 1, &bb))) return fail(rcode, "scalar read");
-  const double thr = o.rtol * o.rtol * bb;
-  const int every = o.replace_every > 0 ? o.replace_every : 50;
-  double pq_win[9] = {0};
-  int it = 0, nwin = 0, head = 0, status = XF_OK, repl = 0;
-  double rr_true = 0.0, rr_prev_true = 0.0;
-  int prev_cycle = 0;
-  for (;;) {
-    if ((rcode = true_residual(&rr_true))) return fail(rcode, "scalar read");
-    if (rr_true <= thr) break;
-    if (std::isnan(rr_true)) { status = XF_NAN; break; }
-    if (it >= o.maxit) { status = XF_MAXIT; break; }
-    if (repl > 0 && precond == XF_PRECOND_UNET2 && prev_cycle >= 10 && !(rr_true < 0.81 * rr_prev_true)) {
-      // no progress over a whole refresh cycle of 10 or more iterations: plain CG from here on (the fallback)
-      precond = XF_PRECOND_NONE;
-      st->fallbacks++;
-    }
-    rr_prev_true = rr_true;
-    XF_CUDA(ctx, cudaMemsetAsync(e, 0, n * 4, s));
-    const double rr_start = rr_true;
-    const int it_start = it;
-    double rr = rr_true;
-    bool brk = false;
-    while (true) {
-      it++;
-      float *pn = P[head], *qn = Q[head];
-      // (z, r) and (z, A p_j) over the window, one read (the smoother's last
-      // pass has reduced (z, r) and the newest window term already)
-      const float* q_newest = nwin > 0 ? Q[(head + m) % (m + 1)] : nullptr;
-      bool fused_dots = false;
-      if ((rcode = apply_m(pn, q_newest, &fused_dots))) return fail(rcode, "preconditioner");
-      auto dots_z = [&](double* zq, bool fused) -> int {
-        if (!fused) fdot(z, r, FS_ZR);
-        for (int j = fused ? 1 : 0; j < nwin; j++) fdot(z, Q[(head + m + 1 - 1 - j) % (m + 1)], j);
-        launches += (fused ? 0 : 1) + nwin - (fused && nwin > 0 ? 1 : 0);
-        return read_n(ctx, 0, FS_ZR + 1, zq);
-      };
-      double zq[FS_ZR + 1];
-      if ((rcode = dots_z(zq, fused_dots))) return fail(rcode, "scalar read");
-      if (!(zq[FS_ZR] > 0) && precond != XF_PRECOND_NONE) {   // no descent direction: use r this time
-        if (++st->fallbacks >= FCG_STRIKES) precond = XF_PRECOND_NONE;   // and from the third on, for good
-        XF_CUDA(ctx, cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s));
-        XF_CUDA(ctx, cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s));
-        if ((rcode = dots_z(zq, false))) return fail(rcode, "scalar read");
+    {
+      // the smoother: its first pass takes r - omega A y, its last writes
+      // z = omega y + s p(A)(r - omega A y) (also into the direction slot) and reduces the dots
+      float *src = nullptr, *dst = w0;
+      for (int k = tl_nf - 1; k >= 0; k--) {
+        const bool first = k == tl_nf - 1, last = k == 0;
+        xf_cg_poly_tl_launch(op, first, last, first ? r : src, ay, last ? z : dst, tl_f[k], FS_YAY, FS_YR, y,
+                             (float)tl_scale, pn, r, q_newest, FS_ZR, 0);
+        src = dst;
+        dst = dst == w0 ? w1 : w0;
       }
-      // the new direction p = z - sum_j (z, A p_j) / (p_j, A p_j) p_j in ring slot `head` (holding z)
-      if (nwin > 0) {
-        for (int j = 0; j < nwin; j++) {
-          const int sl = (head + m + 1 - 1 - j) % (m + 1);
-          if (pq_win[sl] > 0) {
-            k_axpy_f<<<eb, 256, 0, s>>>(pn, P[sl], (float)(-zq[j] / pq_win[sl]), n);
-            launches++;
-          }
-        }
-      }
-      xf_cg_q32_dot(op, pn, qn, FS_PQ);   // q = A p, (p, q)
-      fdot(pn, r, FS_PR);
-      launches += 2;
-      double v3[3];   // slots FS_PR .. FS_PQ
-      if ((rcode = read_n(ctx, FS_PR, FS_PQ - FS_PR + 1, v3))) return fail(rcode, "scalar read");
-      const double pr = v3[0], pq = v3[FS_PQ - FS_PR];
-      if (!(pq > 0)) {
-        status = std::isnan(pq) ? XF_NAN : XF_BREAKDOWN;
-        brk = true;
-        break;
-      }
-      k_fcg_update_f<<<eb, 256, 0, s>>>(e, r, pn, qn, (float)(pr / pq), n);
-      pq_win[head] = pq;
-      head = (head + 1) % (m + 1);
-      if (nwin < m) nwin++;
-      fdot(r, r, FS_RR);
-      launches += 2;   // the update and (r, r)
-      if ((rcode = read_n(ctx, FS_RR, 1, &rr))) return fail(rcode, "scalar read");
-      if (std::isnan(rr) || rr <= thr || rr <= 1e-6 * rr_start || it - it_start >= every || it >= o.maxit) break;
     }
-    k_fold_f2d<<<eb, 256, 0, s>>>(x, e, n);   // x += e in FP64
-    launches++;
-    repl++;
-    prev_cycle = it - it_start;
-    if (brk) {   // report the true residual of the final x
-      if ((rcode = true_residual(&rr_true))) return fail(rcode, "scalar read");
-      break;
-    }
+    win_dots(hd, 1);
+    end_tail(unused);
+    n_on = 4 + UNET_FORWARD_LAUNCHES + tl_nf + (m - 1);
+    // network off: z = r with its dots
+    begin(ie[1], nullptr, 0);
+    cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s);
+    fdot(z, r, FS_ZR, nullptr);
+    win_dots(hd, 0);
+    end_tail(unused);
+    n_off = 1 + m;
+    // the descent test
+    begin(bbody, &ienode, 1);
+    k_tl_z<<<1, 32, 0, s>>>(S, c, prm, H.fb[hd]);
+    end_tail(tail);
+    cudaGraph_t fbody = nullptr;
+    cudaGraphNode_t fnode = nullptr;
+    add_cond(bbody, tail, H.fb[hd], cudaGraphCondTypeIf, 1, &fbody, &fnode);
+    begin(fbody, nullptr, 0);
+    cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(pn, r, n * 4, cudaMemcpyDeviceToDevice, s);
+    fdot(z, r, FS_ZR, nullptr);
+    win_dots(hd, 0);
+    end_tail(unused);
+    n_fb = 1 + m;
+    // the new direction, its image, alpha, the update, the cycle-end test
+    begin(bbody, &fnode, 1);
+    k_tl_coef<<<1, 32, 0, s>>>(S, c, hd, m);
+    for (int j = 0; j < m; j++) k_tl_axpy<<<eb, 256, 0, s>>>(pn, P[(hd + m - j) % (m + 1)], c, j, n);
+    xf_cg_q32_dot(op, pn, qn, FS_PQ);   // q = A p, (p, q)
+    fdot(pn, r, FS_PR, nullptr);
+    k_tl_alpha<<<1, 32, 0, s>>>(S, c, hd, m);
+    k_tl_update<<<eb, 256, 0, s>>>(e, r, pn, qn, c, n);
+    fdot(r, r, FS_RR, &c->brk);
+    k_tl_rr<<<1, 32, 0, s>>>(S, c, H, hd, m);
+    end_tail(unused);
+    // it, z-test, coef, m axpys, stencil + dot, alpha, update, rr, test, and the loop guard
+    n_iter = 3 + m + 2 + 1 + 1 + 1 + 1 + 1;
   }
+  // the loop guard, last in the body
+  begin(wbody, &prev, 1);
+  k_tl_guard<<<1, 32, 0, s>>>(c, H);
+  end_tail(unused);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return fail(rcode ? rcode : XF_ERR_CUDA, rcode ? "preconditioner" : "graph capture");
+  }
+  ce = cudaGraphInstantiate(&t->exec, top, 0);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return fail(XF_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  TlParams hp = {};
+  hp.n_ref = 3; hp.n_iter = n_iter; hp.n_on = n_on; hp.n_off = n_off; hp.n_fb = n_fb;
+  if (cudaMemcpy(t->prm, &hp, sizeof(hp), cudaMemcpyHostToDevice) != cudaSuccess) return fail(XF_ERR_CUDA, "params");
+  t->op_serial = op->serial; t->x = xv->data; t->b = bv->data; t->m = m; t->F = F; t->nf = tl_nf;
+  memcpy(t->f, tl_f, sizeof(float) * 3 * tl_nf);
+  t->scale = tl_scale;
+  *out = t;
+  return XF_OK;
+}
+
+static int fcg_mixed_two_level(xf_op* op, xf_unet* u, const xf_solve_opts& o, int m, int F, const float (*tl_f)[3],
+                               int tl_nf, double tl_scale, xf_vec* xv, const xf_vec* bv, xf_solve_stats* st) {
+  xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  cudaStream_t s = ctx->stream;
+  TlGraph* t = u->tlg;
+  const bool same = t && t->op_serial == op->serial && t->x == xv->data && t->b == bv->data && t->m == m &&
+                    t->F == F && t->nf == tl_nf && t->scale == tl_scale &&
+                    memcmp(t->f, tl_f, sizeof(float) * 3 * tl_nf) == 0;
+  if (!same) {
+    if (t) {
+      cudaStreamSynchronize(s);
+      delete t;
+      u->tlg = nullptr;
+    }
+    int rc = tl_graph_build(op, u, m, F, tl_f, tl_nf, tl_scale, xv, bv, &u->tlg);
+    if (rc) return rc;
+    t = u->tlg;
+  }
+  // the Chebyshev passes return at once while a mixed solve's done / pause flags are set
+  long long zero = 0;
+  XF_CUDA(ctx, cudaMemcpyAsync(&ctx->scratch->iscalars[I_DONE], &zero, 8, cudaMemcpyHostToDevice, s));
+  XF_CUDA(ctx, cudaMemcpyAsync(&ctx->scratch->iscalars[I_PAUSE], &zero, 8, cudaMemcpyHostToDevice, s));
+  XF_CUDA(ctx, cudaMemcpyAsync(&ctx->scratch->iscalars[I_ERR], &zero, 8, cudaMemcpyHostToDevice, s));
+  struct { double rtol2; int maxit, every; } p3 = {o.rtol * o.rtol, o.maxit, o.replace_every > 0 ? o.replace_every : 50};
+  static_assert(offsetof(TlParams, rtol2) == 0 && offsetof(TlParams, maxit) == 8 && offsetof(TlParams, every) == 12,
+                "TlParams layout");
+  XF_CUDA(ctx, cudaMemcpyAsync(t->prm, &p3, 16, cudaMemcpyHostToDevice, s));
+  XF_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  XF_CUDA(ctx, cudaGraphLaunch(t->exec, s));
   XF_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
-  XF_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  TlCtl hc;
+  XF_CUDA(ctx, cudaMemcpyAsync(&hc, t->ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  XF_CUDA(ctx, cudaStreamSynchronize(s));
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  cleanup();
+  int rcode;
   if ((rcode = xf_conv_status(ctx))) return rcode;
   long long err = 0;   // a bounded wait of a Chebyshev pass that gave up
   XF_CUDA(ctx, cudaMemcpy(&err, &ctx->scratch->iscalars[I_ERR], 8, cudaMemcpyDeviceToHost));
   if (err) return xf_fail(ctx, XF_ERR_CUDA, "xf_solve_fcg: a smoothing pass timed out on a copy");
-  const double rel = bb > 0 ? sqrt(rr_true / bb) : sqrt(rr_true);
-  st->status = status == XF_OK && rel > o.rtol ? XF_STALL : status;
-  st->iterations = it;
-  st->replacements = repl;
-  st->reserved[0] = (double)launches;
+  if (hc.status == XF_ERR_CUDA) return xf_fail(ctx, XF_ERR_CUDA, "xf_solve_fcg: the device loop stopped without progress");
+  const double rel = hc.bb > 0 ? sqrt(hc.rr_true / hc.bb) : sqrt(hc.rr_true);
+  st->status = hc.status == XF_OK && rel > o.rtol ? XF_STALL : hc.status;
+  st->iterations = hc.it;
+  st->replacements = hc.repl;
+  st->fallbacks = hc.fallbacks;
+  st->reserved[0] = (double)hc.launches;
   st->rel_resid = rel;
-  st->abs_resid = sqrt(rr_true);
+  st->abs_resid = sqrt(hc.rr_true);
   st->ms = ms;
   return XF_OK;
 }
