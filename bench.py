@@ -284,6 +284,9 @@ def main(argv=None):
     ap.add_argument("--rows", action="store_true",
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
+    ap.add_argument("--timeloop", action="store_true",
+                    help="time the GPU time loop: the lid-driven cavity (64^3, 10 steps) and the channel with the "
+                         "immersed icosphere (256x64x64, 100 steps)")
     argv = sys.argv[1:] if argv is None else argv
     args = ap.parse_args(argv)
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
@@ -292,6 +295,8 @@ def main(argv=None):
         return reference_arm(args)
     if args.rows:
         return rows(args)
+    if args.timeloop:
+        return timeloop(args)
     if args.learned:
         return learned(args)
 
@@ -683,6 +688,35 @@ def rows(args):
 
 # 72 (residual, error) pairs (8 right-hand sides x 9 CG iterates) of a 64^3 system of the sphere family,
 # 3000 Adam steps with the learning rate halved every 1000 steps
+def timeloop(args):
+    """The time step of TVPProblem::SolveBySplitting on the GPU
+    (xflow_gb300.timeloop): momentum by the implicit transfer operator under
+    BiCGStab, pressure by mixed-precision CG (the cavity's all-Neumann system)
+    or BiCGStab (the channel's outlet rows), correction and control balance,
+    all FP64 but the cavity's pressure solve.  One JSON line per statement:
+    per-step ms (wall, synchronised; the first step, which builds the solver
+    graphs, apart), iterations and the control balance of the last step."""
+    import xflow_gb300 as xf
+    from xflow_gb300 import timeloop as tl
+
+    ctx = xf.Context(0)
+    cases = (("lid-driven cavity", tl.cavity(64, re=100.0, tau=1e-3), None, 10),
+             ("channel with an immersed sphere", tl.channel(256, 64, 64, re=200.0, tau=2e-3),
+              tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4), 100))
+    for label, st, mk, steps in cases:
+        loop = tl.SplittingLoop(ctx, st, markers=mk)
+        recs = [loop.step() for _ in range(steps)]
+        line = {"mode": "time loop", "statement": st["name"], "steps": steps,
+                "markers": None if mk is None else int(len(mk["pos"])),
+                "first_step_ms": recs[0]["ms"], "ms_per_step": float(np.mean([r["ms"] for r in recs[1:]])),
+                "momentum_iterations_mean": float(np.mean([r["momentum_iterations"] for r in recs])),
+                "pressure_iterations_mean": float(np.mean([r["pressure_iterations"] for r in recs])),
+                "last": recs[-1]}
+        print(json.dumps(line), flush=True)
+        del loop
+    return 0
+
+
 UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=tuple(range(200, 208)),
                   iters=(2, 5, 10, 20, 40, 80, 120, 160, 240), steps=3000, lr=1e-3, halvings=3)
 

@@ -291,6 +291,27 @@ int xf_voxelize_mesh(xf_ctx* ctx, int n1, int n2, int n3, const double* x_nodes,
  * bit-identical to the reference's loops.  A cell the reference throws on
  * returns XF_ERR_MASK (or XF_ERR_CHECK for its value checks), naming the first
  * such cell in its loop order. */
+/* Right-hand side of the implicit transfer equation that replaces the ADI
+ * sweeps of one velocity component (SolveTransferEquation__, XProblem.cpp:
+ * 5421, 2784-3420; solved with XF_OP_ADVDIFF): out = (1/tau) f_prev + rp on
+ * Actual points (the line systems' base term, XProblem.cpp:3192), rp on the
+ * other active points (border rows: rp holds the border value
+ * xf_momentum_rhs put there), f_prev on inactive points.  FP64 boxes of one
+ * velocity grid. */
+int xf_transfer_rhs(const xf_vec* f_prev, const xf_vec* rp, double tau, xf_vec* out);
+/* After that solve: every PreDefined point of vel becomes 2 border - (its one
+ * Actual neighbour), as the reference's ADI sweeps recalculate their sector
+ * ends (XProblem.cpp:2996-3003), so the border rows hold to rounding before
+ * xf_velocity_correct checks them.  XF_ERR_MASK for a PreDefined point with
+ * no or several Actual neighbours (the reference's throws). */
+int xf_border_recalc(const xf_vec* border, xf_vec* vel);
+/* A zero-gradient (outflow) face for a time loop: each PreDefined point of vel's
+ * grid on face (axis 1..3, side 0 low / 1 high) gets, in border, the current
+ * value of its Actual neighbour across the face; the next step's semi-sum row
+ * then makes the face value follow the interior (lagged by one step).  No
+ * counterpart in the reference, whose border values come from its statement's
+ * GetBorderCondition* hooks. */
+int xf_border_follow(const xf_vec* vel, xf_vec* border, int axis, int side);
 /* Pressure right-hand side (XProblem.cpp:5474-5512): Fictive 0; Actual
  * -(rho^2 du/dx + dv/dy + dw/dz) / tau; PreDefined the border value. */
 int xf_pressure_rhs(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, const xf_vec* density,

@@ -410,6 +410,25 @@ def velocity_correct(axis, vel_prev, p, tau, vel, density=None, border=None):
     return vel
 
 
+def transfer_rhs(f_prev, rp, tau, out):
+    """out |= the implicit transfer equation's right-hand side: (1/tau) f_prev + rp on Actual points, rp on the
+    border rows (XProblem.cpp:3192)."""
+    _check(out.grid.ctx.h, capi.lib().xf_transfer_rhs(f_prev.h, rp.h, float(tau), out.h))
+    return out
+
+
+def border_recalc(vel, border=None):
+    """PreDefined points of vel |= 2 border - their Actual neighbour (XProblem.cpp:2996-3003)."""
+    _check(vel.grid.ctx.h, capi.lib().xf_border_recalc(_h(border), vel.h))
+    return vel
+
+
+def border_follow(vel, border, axis, side):
+    """border |= on face (axis, side), the values of vel's Actual neighbours (a lagged zero-gradient face)."""
+    _check(vel.grid.ctx.h, capi.lib().xf_border_follow(vel.h, border.h, int(axis), int(side)))
+    return border
+
+
 def divergence_max(gp, u, v, w):
     """(max |div u| over Actual cells, (i, j, k)) as the control balance (XProblem.cpp:5782-5829)."""
     val = C.c_double()

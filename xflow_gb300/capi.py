@@ -35,7 +35,7 @@ EXPORTS = [
     "xf_ib_interpolate", "xf_ib_update_position", "xf_ib_compute_forces", "xf_ib_spread",
     "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
     "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
-    "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_dot_noalloc",
+    "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_dot_noalloc", "xf_transfer_rhs", "xf_border_recalc", "xf_border_follow",
 ]
 
 
@@ -100,6 +100,9 @@ def lib():
         L.xf_solve_opts_default.argtypes = [C.POINTER(SolveOpts)]
         L.xf_solve.argtypes = [vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
         L.xf_solve_host.argtypes = [vp, C.POINTER(SolveOpts), vp, vp, C.POINTER(SolveStats)]
+        L.xf_transfer_rhs.argtypes = [vp, vp, C.c_double, vp]
+        L.xf_border_recalc.argtypes = [vp, vp]
+        L.xf_border_follow.argtypes = [vp, vp, C.c_int, C.c_int]
         L.xf_dot_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
         L.xf_profile_cg_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.xf_selftest_division.argtypes = [vp, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]

@@ -165,8 +165,11 @@ __global__ void k_vel_pass1(int axis, const uint8_t* __restrict__ code, int b1, 
 // Pass 2: PreDefined cells mirror their single Actual neighbour about the
 // border value.
 template <bool SMALL>
+// (check = false: only the assignment, the closing border recalculation of
+// the reference's ADI sweeps for PreDefined sector ends, XProblem.cpp:2996-3003)
 __global__ void k_vel_pass2(const uint8_t* __restrict__ code, int b1, int b2, int b3, const double* __restrict__ prev,
-                            double* __restrict__ cur, const double* __restrict__ border, DevScratch* S) {
+                            double* __restrict__ cur, const double* __restrict__ border, DevScratch* S,
+                            bool check = true) {
   const int64_t n = (int64_t)b1 * b2 * b3;
   const int64_t s1 = (int64_t)b2 * b3, s2 = b3;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
@@ -190,8 +193,7 @@ __global__ void k_vel_pass2(const uint8_t* __restrict__ code, int b1, int b2, in
       }
     if (count <= 0) { report(S, E_PREDEF_NONE, c); continue; }
     if (count > 1) { report(S, E_PREDEF_MANY, c); continue; }
-    const double check = fabs(prev[c] - (2 * defVal - prev[nb]));
-    if (check > 1e-10) report(S, E_PREDEF_VALUE, c);
+    if (check && fabs(prev[c] - (2 * defVal - prev[nb])) > 1e-10) report(S, E_PREDEF_VALUE, c);
     cur[c] = 2 * defVal - cur[nb];
   }
 }
@@ -612,6 +614,101 @@ __global__ void k_div_selftest(long long n, unsigned long long seed, unsigned lo
     if (!same) bad++;
   }
   if (bad) atomicAdd(mismatches, bad);
+}
+
+// Right-hand side of the implicit transfer equation that replaces the ADI
+// sweeps of one velocity component (SolveTransferEquation__, XProblem.cpp:
+// 5421 and 2784-3420): (1/tau) f_1 + rp on Actual points, the line systems'
+// base term (XProblem.cpp:3192), and rp (the border value the momentum
+// right-hand side put there) on the other active points, whose rows are the
+// grid's border rows; inactive points keep f_1.
+__global__ void k_transfer_rhs(const uint8_t* __restrict__ code, int64_t n, const double* __restrict__ f,
+                               const double* __restrict__ rp, double itau, double* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int m = code[c];
+    double v = f[c];
+    if (m == 1) v = itau * f[c] + rp[c];
+    else if (m == 4 || m == 5 || m == 6 || m == 8) v = rp[c];
+    out[c] = v;
+  }
+}
+
+extern "C" int xf_transfer_rhs(const xf_vec* f_prev, const xf_vec* rp, double tau, xf_vec* out) {
+  if (!f_prev || !rp || !out) return XF_ERR_ARG;
+  const xf_grid* g = out->g;
+  xf_ctx* ctx = g->ctx;
+  if (!is_f64(f_prev) || !is_f64(rp) || !is_f64(out) || !same_box(f_prev, g) || !same_box(rp, g))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_transfer_rhs: FP64 boxes of one grid expected");
+  if (!(tau != 0)) return xf_fail(ctx, XF_ERR_ARG, "xf_transfer_rhs: tau must be nonzero");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  k_transfer_rhs<<<grid_blocks(ctx, g->ncell, 256), 256, 0, ctx->stream>>>(
+      g->code, g->ncell, (const double*)f_prev->data, (const double*)rp->data, 1.0 / tau, (double*)out->data);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// The border values of an implicit transfer solve made exact: every
+// PreDefined point becomes 2 b - (its Actual neighbour), as the reference's
+// ADI sweeps recalculate their sector ends (XProblem.cpp:2996-3003), so that
+// the velocity correction's border check holds to rounding.
+extern "C" int xf_border_recalc(const xf_vec* border, xf_vec* vel) {
+  if (!vel) return XF_ERR_ARG;
+  const xf_grid* g = vel->g;
+  xf_ctx* ctx = g->ctx;
+  if (!is_f64(vel) || (border && (!is_f64(border) || !same_box(border, g))))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_border_recalc: FP64 boxes of one grid expected");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  int st;
+  if ((st = clear_checks(ctx))) return st;
+  XF_LAUNCH_BOX(k_vel_pass2, g->ncell, grid_blocks(ctx, g->ncell, 256), 256, g->code, g->n1, g->n2, g->n3,
+                (const double*)vel->data, (double*)vel->data, border ? (const double*)border->data : nullptr,
+                ctx->scratch, false);
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int kinds[] = {E_PREDEF_NONE, E_PREDEF_MANY};
+  const int bad = first_error(chk, kinds, 2, &cell);
+  if (bad >= 0) return fail_at(ctx, g, bad, cell, "xf_border_recalc");
+  return XF_OK;
+}
+
+// A zero-gradient (outflow) face: each PreDefined point on face (axis, side)
+// takes the current value of its Actual neighbour across the face as its
+// border value, so the next step's semi-sum row makes the face value follow
+// the interior (lagged by one step).
+__global__ void k_border_follow(const uint8_t* __restrict__ code, int n1, int n2, int n3, int axis, int side,
+                                const double* __restrict__ vel, double* __restrict__ border) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int na = axis == 0 ? n1 : axis == 1 ? n2 : n3;
+  const int la = axis == 0 ? n2 : n1, lb = axis == 2 ? n2 : n3;   // the face plane's two other axes
+  const int64_t np = (int64_t)la * lb;
+  const int f = side ? na - 1 : 0, inward = side ? -1 : 1;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np; q += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(q / lb), y = (int)(q - (int64_t)x * lb);
+    int i, j, k;
+    if (axis == 0) { i = f; j = x; k = y; }
+    else if (axis == 1) { i = x; j = f; k = y; }
+    else { i = x; j = y; k = f; }
+    const int64_t c = i * s1 + j * s2 + k;
+    if (code[c] != PC_PREDEFINED) continue;
+    const int64_t nb = c + inward * (axis == 0 ? s1 : axis == 1 ? s2 : 1);
+    if (code[nb] == PC_ACTUAL) border[c] = vel[nb];
+  }
+}
+
+extern "C" int xf_border_follow(const xf_vec* vel, xf_vec* border, int axis, int side) {
+  if (!vel || !border) return XF_ERR_ARG;
+  const xf_grid* g = vel->g;
+  xf_ctx* ctx = g->ctx;
+  if (axis < 1 || axis > 3 || (side != 0 && side != 1))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_border_follow: axis 1..3 and side 0 or 1 expected");
+  if (!is_f64(vel) || !is_f64(border) || !same_box(border, g))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_border_follow: FP64 boxes of one grid expected");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int64_t np = axis == 1 ? (int64_t)g->n2 * g->n3 : axis == 2 ? (int64_t)g->n1 * g->n3 : (int64_t)g->n1 * g->n2;
+  k_border_follow<<<grid_blocks(ctx, np, 256), 256, 0, ctx->stream>>>(g->code, g->n1, g->n2, g->n3, axis - 1, side,
+                                                                      (const double*)vel->data, (double*)border->data);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
 }
 
 extern "C" int xf_selftest_division(xf_ctx* ctx, long long n, unsigned long long seed, long long* mismatches) {

@@ -1,0 +1,227 @@
+"""The time step of TVPProblem::SolveBySplitting (XProblem.cpp:4255-6650) on
+the GPU, every pass through the C ABI of include/xflow.h:
+
+  momentum, per velocity component eq (XProblem.cpp:5017-5446):
+    xf_momentum_rhs      transfer velocities, face viscosity, border values,
+                         forces, viscous terms (the reference's loops)
+    xf_transfer_rhs      (1/tau) f_1 + rp
+    XF_OP_ADVDIFF solve  the implicit transfer equation, unsplit (the sum of
+                         the reference's three ADI line operators), BiCGStab
+    xf_border_recalc     the PreDefined border values exact, as the ADI
+                         sweeps leave them
+  pressure (XProblem.cpp:5452-5594):
+    xf_pressure_rhs, then the pressure solve (mixed-precision CG on
+    all-Neumann systems, BiCGStab where border rows make it nonsymmetric)
+  xf_velocity_correct per component (XProblem.cpp:5598-5777)
+  xf_divergence_max, the control balance (XProblem.cpp:5782-5829)
+
+With markers, each momentum equation's force is the immersed boundary's
+(TImmersedBoundaryProblem::GetForce order, XProblem.cpp:8350-8353):
+interpolate the component's velocity at the markers, move them, compute
+their forces, spread them into the force box.
+
+Statements are boxes: a pressure grid of n1 x n2 x n3 cell centres with a
+ghost layer, staggered velocity grids one smaller along their own axis
+(XStatement.h:127-135), Actual interiors; on every face of a velocity box
+the component normal to the face is Defined (its value kept) and the
+tangential ones PreDefined (the semi-sum across the face equals the border
+value, XOperator.cpp:1034-1069), box edges Fictive.  The concentration and
+density transport of the reference's step is not part of these statements
+(single fluid, rho = 1).
+"""
+import time
+
+import numpy as np
+
+from . import capi
+
+FICTIVE, ACTUAL, DEFINED, PREDEFINED = 0, 1, 3, 4
+
+
+def _face_slices(shape, ax, side):
+    sl = [slice(1, n - 1) for n in shape]
+    sl[ax] = 0 if side == 0 else shape[ax] - 1
+    return tuple(sl)
+
+
+def velocity_box(pshape, axis, faces):
+    """Codes, outward normals and border values of velocity component `axis`
+    (0 u, 1 v, 2 w) for a pressure box of shape pshape.  faces[(ax, side)]
+    gives this component's value on that face (side 0 low, 1 high); the
+    faces listed in faces['outflow'] make the normal component PreDefined
+    there too (its value then plays the outflow's border value)."""
+    shape = list(pshape)
+    shape[axis] -= 1
+    shape = tuple(shape)
+    codes = np.zeros(shape, np.int32)
+    nrm = np.zeros(shape + (3,))
+    bc = np.zeros(shape)
+    codes[1:-1, 1:-1, 1:-1] = ACTUAL
+    outflow = faces.get("outflow", ())
+    for ax in range(3):
+        for side in (0, 1):
+            sl = _face_slices(shape, ax, side)
+            pre = ax != axis or (ax, side) in outflow
+            codes[sl] = PREDEFINED if pre else DEFINED
+            if pre:
+                nrm[sl + (ax,)] = -1.0 if side == 0 else 1.0
+            bc[sl] = faces.get((ax, side), 0.0)
+    return codes, nrm, bc
+
+
+def cavity(n, lid=1.0, re=100.0, tau=1e-3, noise=1e-3, seed=1):
+    """The lid-driven cavity: unit cube of n^3 cells (h = 1/n), lid velocity u
+    = `lid` on the top face z = 1, no-slip elsewhere, all-Neumann pressure,
+    viscosity 1/Re, initial velocity zero plus seeded i.i.d. N(0, noise) on
+    the Actual points."""
+    B = n + 2
+    pshape = (B, B, B)
+    h = [np.full(B - 1, 1.0 / n)] * 3
+    pc = np.zeros(pshape, np.int32)
+    pc[1:-1, 1:-1, 1:-1] = ACTUAL
+    comps = [velocity_box(pshape, 0, {(2, 1): lid}), velocity_box(pshape, 1, {}), velocity_box(pshape, 2, {})]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vel0 = []
+    for codes, _, bc in comps:
+        v = np.where(codes == DEFINED, bc, 0.0)
+        v[codes == ACTUAL] = rng.normal(0.0, noise, int((codes == ACTUAL).sum()))
+        vel0.append(v)
+    return dict(name=f"lid-driven cavity {n}^3, Re={re:g}, dt={tau:g}", p=(pc, None, None, h), comps=comps,
+                h=h, vel0=vel0, vis=1.0 / re, tau=tau, pressure="neumann")
+
+
+def channel(nx, ny, nz, length=4.0, u_in=1.0, re=200.0, tau=2e-3):
+    """The channel [0, length] x [0, 1] x [0, 1] of nx x ny x nz cells:
+    Defined inflow u = u_in at x = 0, a zero-gradient outflow at x = length
+    (PreDefined pressure 0; PreDefined velocities whose border values follow
+    the last interior layer, lagged by a step), walls with zero normal
+    velocity and zero tangential border values, viscosity 1/Re; the velocity
+    starts at the inflow value."""
+    pshape = (nx + 2, ny + 2, nz + 2)
+    h = [np.full(nx + 1, length / nx), np.full(ny + 1, 1.0 / ny), np.full(nz + 1, 1.0 / nz)]
+    pc = np.zeros(pshape, np.int32)
+    pc[1:-1, 1:-1, 1:-1] = ACTUAL
+    pn = np.zeros(pshape + (3,))
+    pc[-1, 1:-1, 1:-1] = PREDEFINED
+    pn[-1, 1:-1, 1:-1, 0] = 1.0
+    pbc = np.zeros(pshape)
+    out = {"outflow": ((0, 1),)}
+    ufaces = dict(out)
+    ufaces.update({(0, 0): u_in, (0, 1): u_in})
+    comps = [velocity_box(pshape, 0, ufaces), velocity_box(pshape, 1, dict(out)), velocity_box(pshape, 2, dict(out))]
+    vel0 = []
+    for a, (codes, _, bc) in enumerate(comps):
+        v = np.where(codes == DEFINED, bc, 0.0)
+        if a == 0:
+            v[codes == ACTUAL] = u_in
+        vel0.append(v)
+    return dict(name=f"channel {nx}x{ny}x{nz} on [0,{length:g}]x[0,1]x[0,1], Re={re:g}, dt={tau:g}",
+                p=(pc, pn, pbc, h), comps=comps, h=h, vel0=vel0, vis=1.0 / re, tau=tau, pressure="outlet",
+                follow=((1, 1),))
+
+
+def sphere_markers(center, radius, subdiv=4, stiffness=1e3):
+    """Target markers on an icosphere (subdivision 4: 2562 vertices), each
+    pulled back to its own starting point (TTargetNode, XImmersedBoundary.cpp:
+    720-759); the marker area is the sphere's over the markers."""
+    from . import workloads as wl
+
+    verts = wl.icosphere(subdiv) * radius + np.asarray(center, float)
+    nn = len(verts)
+    idx = np.arange(nn)
+    return dict(pos=verts, ref=verts.copy(), kind=np.full(nn, capi.XF_IB_TARGET, np.int32),
+                nxt=np.roll(idx, -1).astype(np.int32), prv=np.roll(idx, 1).astype(np.int32), dist0=np.zeros(nn),
+                curv0=np.zeros((nn, 3)), stiff=np.ones(nn),
+                params=np.array([stiffness, 0.0, 0.0, 4 * np.pi * radius * radius / nn]))
+
+
+class SplittingLoop:
+    """The time loop of a statement (cavity(), channel()) on one device:
+    `step()` advances one time step and returns its per-step figures."""
+
+    def __init__(self, ctx, st, markers=None, momentum_rtol=1e-10, pressure_rtol=1e-8):
+        import xflow_gb300 as xf
+
+        self.xf, self.ctx, self.st = xf, ctx, st
+        self.tau = st["tau"]
+        pc, pn, pbc, hp = st["p"]
+        self.gp = xf.Grid(ctx, pc, *hp, pn)
+        self.pbc = self.gp.vec(pbc) if pbc is not None else None
+        self.g, self.bc, self.vel, self.mid, self.ops, self.rhs = [], [], [], [], [], []
+        for a, (codes, nrm, bc) in enumerate(st["comps"]):
+            hh = [hp[d][:-1] if d == a else hp[d] for d in range(3)]
+            hh[a] = 0.5 * (hp[a][:-1] + hp[a][1:])   # staggered nodes sit between the pressure nodes
+            g = xf.Grid(ctx, codes, *hh, nrm)
+            self.g.append(g)
+            self.bc.append(g.vec(bc))
+            self.vel.append(g.vec(st["vel0"][a]))
+            self.mid.append(g.vec(st["vel0"][a]))
+            self.ops.append(xf.Operator(g, xf.XF_OP_ADVDIFF))
+            self.rhs.append(g.vec(None))
+        self.mom = [tuple(g.vec(None) for _ in range(5)) for g in self.g]
+        self.force = [g.vec(np.zeros(g.shape)) for g in self.g]
+        self.vis = self.gp.vec(np.full(self.gp.shape, st["vis"]))
+        self.pop = xf.Operator(self.gp, xf.XF_OP_LAPLACE)
+        self.p = self.gp.vec(np.zeros(self.gp.shape))
+        self.prhs = self.gp.vec(None)
+        self.markers = None
+        if markers is not None:
+            m = markers
+            self.markers = xf.Markers(ctx, m["pos"], m["ref"], m["kind"], m["nxt"], m["prv"], m["dist0"], m["curv0"],
+                                      m["stiff"], m["params"])
+            self.h0 = np.array([hp[0][0], hp[1][0], hp[2][0]])
+        self.momentum_rtol, self.pressure_rtol = momentum_rtol, pressure_rtol
+        self.steps = 0
+
+    def step(self):
+        xf, tau = self.xf, self.tau
+        self.ctx.synchronize()
+        t0 = time.perf_counter()
+        its = []
+        u1, v1, w1 = self.vel
+        for axis, side in self.st.get("follow", ()):   # zero-gradient faces take the interior's values
+            for a in range(3):
+                xf.border_follow(self.vel[a], self.bc[a], axis, side)
+        for a in range(3):
+            force = None
+            if self.markers is not None:   # GetForce: interpolate, move, forces, spread
+                self.force[a].fill(0.0)
+                self.markers.interpolate(self.vel[a], self.h0, a + 1)
+                self.markers.update_position(a + 1, tau)
+                self.markers.compute_forces(a + 1)
+                self.markers.spread(self.force[a], self.h0, a + 1)
+                force = self.force[a]
+            uTr, vTr, wTr, visTr, rp = xf.momentum_rhs(a + 1, self.g[a], u1, v1, w1, vis=self.vis, border=self.bc[a],
+                                                       force=force, out=self.mom[a])
+            A = self.ops[a]
+            A.set_advection(uTr, vTr, wTr, tau, 0.0, capi.XF_ADV_CONVECTIVE | capi.XF_ADV_DIFFUSIVE)
+            A.set_diffusion_field(visTr)
+            xf.transfer_rhs(self.vel[a], rp, tau, self.rhs[a])
+            self.mid[a].assign(self.vel[a])   # warm start from f_1 (its Defined points hold their values)
+            # BiCGStab's own stop rule, max |r| <= atol (XSLAE.cpp:712-716), relative to the right-hand side
+            s = xf.solve(A, self.mid[a], self.rhs[a], method=xf.XF_BICGSTAB,
+                         atol=self.momentum_rtol * self.rhs[a].absmax()[0], maxit=20000)
+            if s.status != capi.XF_OK:
+                raise xf.XFError(s.status, f"momentum equation {a + 1}: status {s.status}")
+            xf.border_recalc(self.mid[a], self.bc[a])   # the sector ends exact, as the ADI leaves them
+            its.append(s.iterations)
+        xf.pressure_rhs(self.gp, *self.mid, tau, self.prhs, border=self.pbc)
+        if self.st["pressure"] == "neumann":
+            s = xf.solve(self.pop, self.p, self.prhs, method=xf.XF_CG, precision=xf.XF_PREC_MIXED,
+                         rtol=self.pressure_rtol, maxit=100000)
+        else:
+            s = xf.solve(self.pop, self.p, self.prhs, method=xf.XF_BICGSTAB,
+                         atol=self.pressure_rtol * self.prhs.absmax()[0], maxit=100000)
+        if s.status != capi.XF_OK:
+            raise xf.XFError(s.status, f"pressure: status {s.status}")
+        its.append(s.iterations)
+        for a in range(3):
+            xf.velocity_correct(a + 1, self.mid[a], self.p, tau, self.vel[a], border=self.bc[a])
+        div, ijk = xf.divergence_max(self.gp, *self.vel)
+        self.ctx.synchronize()
+        self.steps += 1
+        return {"step": self.steps, "ms": (time.perf_counter() - t0) * 1e3, "momentum_iterations": its[:3],
+                "pressure_iterations": its[3], "divergence_max": div, "divergence_cell": ijk}
+
+    def fields(self):
+        return [v.download() for v in self.vel] + [self.p.download()]
