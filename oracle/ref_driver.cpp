@@ -5,7 +5,7 @@
 // reference itself rather than from a restatement.
 //
 // Usage: ref_driver <task> <input.bin> <output.bin>
-//   task = matvec | solve | thomas | ib | pack | npy | step
+//   task = matvec | solve | thomas | ib | pack | npy | step | timing
 //   (npy writes <output.bin>.npy through the reference's cnpy::npy_save;
 //   step runs TVPProblem::SolveBySplitting and writes its VTK files under
 //   ../Res/ relative to the working directory, as the reference does)
@@ -13,6 +13,7 @@
 // File format (both directions): a sequence of records
 //   char name[32]; char kind ('d' double / 'i' int32); int64 count; data[count]
 #include <cstdarg>
+#include <ctime>
 #include <cstdio>
 #include <cstdlib>
 #include <unistd.h>
@@ -637,6 +638,52 @@ static void task_step(Bag& b, Writer& w) {
   throw std::runtime_error("the time step returned without reaching its teardown");
 }
 
+// ---------------------------------------------------------------------------
+// Timing of the reference's own vector and operator calls, to anchor the
+// oracle port's CPU times: `reps` of y |= A(x) (XSpace.cpp:3013-3217 driving
+// XOperator.cpp:938-1129), (x, y) (XSpace.cpp:3261-3342) and
+// z |= p1 x + p2 y (XSpace.cpp:2489-3010), each averaged, then (when "cg" is
+// given) one TSLAE::SolveByConjugateGradients from x0 (XSLAE.cpp:56-157,
+// its own absolute 1e-5 stop rule) timed whole.
+static double now_s() {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+static void task_timing(Bag& b, Writer& w) {
+  Setup s = build(b, 31);
+  const int reps = I(b, "reps")[0];
+  TNodesGrid** grids = new TNodesGrid*[1]; grids[0] = s.grid;
+  T3dLaplaceOperator& A = *(new T3dLaplaceOperator(s.model, 1, grids));
+  TRnRelease3dSpace& x = vec_from(s, D(b, "x"));
+  TRnRelease3dSpace& y = vec_from(s, D(b, "x"));
+  TRnRelease3dSpace& z = vec_from(s, D(b, "x"));
+  double t0 = now_s();
+  for (int q = 0; q < reps; q++) y |= ((TRnLinearOperator&)A)(x);
+  w.s("matvec_s", (now_s() - t0) / reps);
+  double acc = 0;
+  t0 = now_s();
+  for (int q = 0; q < reps; q++) acc += (x, y);
+  w.s("dot_s", (now_s() - t0) / reps);
+  w.s("dot_sum", acc);
+  t0 = now_s();
+  for (int q = 0; q < reps; q++) z |= 0.75 * x + (-1.25) * y;
+  w.s("lincomb_s", (now_s() - t0) / reps);
+  if (b.count("cg")) {
+    TRnRelease3dSpace& x0 = vec_from(s, D(b, "x0"));
+    TRnRelease3dSpace& rhs = vec_from(s, D(b, "b"));
+    TSLAE* slae = new TSLAE(A, x0, rhs);
+    t0 = now_s();
+    slae->SolveByConjugateGradients();
+    w.s("cg_s", now_s() - t0);
+    TRnRelease3dSpace& res = dynamic_cast<TRnRelease3dSpace&>(const_cast<TRnSpace&>((const TRnSpace&)slae->Result));
+    TRnRelease3dSpace& r = *(new TRnRelease3dSpace(s.model));
+    r |= ((TRnLinearOperator&)A)(res) - rhs;
+    w.s("cg_resid_l2", r.Norma(0));
+  }
+}
+
 int main(int argc, char** argv) {
   if (argc != 4) { fprintf(stderr, "usage: ref_driver task in out\n"); return 2; }
   try {
@@ -650,6 +697,7 @@ int main(int argc, char** argv) {
     else if (t == "pack") task_pack(b, w);
     else if (t == "npy") task_npy(b, argv[3]);
     else if (t == "step") task_step(b, w);
+    else if (t == "timing") task_timing(b, w);
     else { fprintf(stderr, "unknown task\n"); return 2; }
   } catch (const char* e) {
     fprintf(stderr, "reference threw: %s\n", e); return 3;
