@@ -4,6 +4,7 @@
 // B (N x K), K contiguous, FP32 accumulation in tensor memory.  It is the
 // building block the implicit-GEMM convolutions below use, exposed so that
 // its operand layout and descriptors are checked on their own.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <stdlib.h>
@@ -262,7 +263,8 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// The same convolution with the three k-taps of each (di, dj) stacked along N.
+// The same convolution with the three k-taps of each (di, dj) stacked along N,
+// fed by the tensor memory accelerator.
 //
 // A tcgen05.mma of M = 128, K = 16 costs about the same time for any N up to
 // 32 (about 39 cycles on GB300; 44 at N = 64, 60 at 128), so one MMA of
@@ -274,211 +276,321 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
 //     y[c0 + r - 1] = D_-1[r - 1] + D_0[r] + D_+1[r + 1],   r = 1 .. 126,
 // neighbouring TMEM rows coming from the neighbouring lanes (warp shuffles; a
 // shared-memory exchange across warps).  A tile therefore yields 126 cells;
-// the last tile starts at ncell - 126 (its overlap rewrites identical values)
-// so that every row read stays inside the zero margins.
+// the last tile starts at ncell - 126 (its overlap rewrites identical values).
 //
-// Operands (slab x channel chunk of KC <= 48 channels) are copied with
-// cp.async (16 bytes per copy) into a ring of ST_STAGES shared-memory stages;
-// a stage is refilled once the MMAs that read it two steps earlier have
-// committed to its mbarrier.  Requires 3 Co <= 256 (Co <= 80).
-constexpr int ST_STAGES = 4;
+// A pipeline step is one (slab, 16-channel chunk): a 128 x 16 block of X and
+// a 3 Co x 16 block of W, each one 2-D tensor copy (cp.async.bulk.tensor)
+// with the 32-byte swizzle, which writes exactly the K-major SWIZZLE_32B
+// operand layout the MMA descriptors name (rows of 32 bytes, the two 16-byte
+// halves of rows 4..7 of every 8-row group exchanged).  Rows outside the box
+// [0, ncell) read as zeros (the copy's out-of-bounds fill), like the zero
+// margins.  The CTA is persistent and warp-specialised:
+//   warp 4, one thread: issues the copies of each step into a ring of
+//       stages (full barrier: the copies' transaction bytes; empty barrier:
+//       the MMA that read the stage has completed);
+//   warp 5, one thread: one MMA per step into one of two TMEM accumulators
+//       (so the epilogue of a tile overlaps the next tile's MMAs), a commit
+//       per stage and one per finished tile;
+//   warps 0-3: the epilogue, TMEM lanes 32 w .. 32 w + 31.
+// Every wait is bounded by the SM clock; a wait that runs out sets the
+// kernel's error flag and an abort flag in shared memory that ends every
+// role's loop, after which the copies and MMAs in flight are waited for
+// (bounded) before TMEM is freed.  Requires 3 Co <= 256 (Co <= 80), Ci and Co
+// multiples of 16.
+constexpr int TM_THREADS = 192;
+constexpr int TM_MAX_STAGES = 12;
+constexpr long long TM_WAIT_CYCLES = 1ll << 31;   // about a second at the SM clock
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+// K-major operand descriptor for the 32-byte swizzle: rows of 32 bytes, 8-row
+// groups 256 bytes apart (SBO); the leading offset is unused for a K extent
+// within the swizzle span.
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;              // LBO (unused): 16 bytes
+  d |= (uint64_t)(256 >> 4) << 32;     // SBO: 8 rows x 32 bytes
+  d |= (uint64_t)1 << 46;              // descriptor version of this architecture
+  d |= (uint64_t)6 << 61;              // layout: SWIZZLE_32B
+  return d;
 }
 
-template <int KC>   // channels per pipeline step (16, 32 or 48)
-__global__ void __launch_bounds__(128) k_conv3_st(ConvArgs a) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t mbar[ST_STAGES];
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_addr(mbar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(mbar)) : "memory");
+}
+// 2-D tensor copy global -> shared, completing on `mbar` (transaction bytes).
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          tc::smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc::smem_addr(mbar))
+      : "memory");
+}
+// Waits for phase `parity` of `mbar`; false when the abort flag is raised or
+// the wait runs past TM_WAIT_CYCLES (which raises it).
+__device__ __forceinline__ bool tm_wait(uint64_t* mbar, uint32_t parity, volatile int* abort_flag,
+                                        bool honour_abort = true) {
+  const uint32_t a = tc::smem_addr(mbar);
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (honour_abort && *abort_flag) return false;
+    if (clock64() - t0 > TM_WAIT_CYCLES) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+// Barrier 1 over the four epilogue warps with an AND of `pred`.
+__device__ __forceinline__ bool epi_sync_and(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "barrier.cta.red.and.pred q, 1, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)pred)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void epi_sync() { asm volatile("barrier.cta.sync 1, 128;" ::: "memory"); }
+
+// Shared-memory plan of one CTA (host and device).
+struct TmPlan {
+  int stage_bytes, stages, acc_off, tmem_cols, smem_bytes;
+};
+__host__ __device__ inline TmPlan tm_plan(int Co, int per_sm_budget) {
+  TmPlan p;
+  const int n3 = 3 * Co;
+  p.stage_bytes = ((128 * 32 + n3 * 32) + 1023) / 1024 * 1024;
+  p.acc_off = (n3 + 31) / 32 * 32;
+  p.tmem_cols = (int)tmem_cols(p.acc_off + n3);
+  int st = (per_sm_budget - 1024) / p.stage_bytes;
+  p.stages = st > TM_MAX_STAGES ? TM_MAX_STAGES : st < 3 ? 3 : st;
+  p.smem_bytes = p.stages * p.stage_bytes + 1024;   // + alignment slack
+  return p;
+}
+
+__global__ void __launch_bounds__(TM_THREADS) k_conv3_tma(ConvArgs a, const __grid_constant__ CUtensorMap tmX,
+                                                          const __grid_constant__ CUtensorMap tmW, TmPlan plan) {
+  extern __shared__ uint8_t dsm[];
+  __shared__ uint64_t full[TM_MAX_STAGES], empty[TM_MAX_STAGES], tfull[2], tempty[2], mdone;
   __shared__ uint32_t tmem_base;
-  __shared__ float xch[2][4][80];   // per warp: lane 31's D_-1 row, lane 0's D_+1 row
-  constexpr int kg = KC / 8;        // 16-byte chunks per operand row
-  const int Ci = a.Ci, Co = a.Co, N3 = 3 * Co;
-  const int nk = Ci / KC;           // channel chunks per slab
-  const int units = 9 * nk;         // pipeline steps per tile
-  const int stage_a = 128 * KC * 2, stage_b = N3 * KC * 2, stage = stage_a + stage_b;
+  __shared__ int abort_flag;
+  __shared__ float xch[4][2][80];   // per warp: lane 31's D_-1 row, lane 0's D_+1 row
+  const int Ci = a.Ci, Co = a.Co, N3 = 3 * Co, nk = Ci / 16;
+  const int steps = 9 * nk;   // pipeline steps per tile
+  const int S = plan.stages;
+  const uint32_t ab = 128 * 32, bb = (uint32_t)N3 * 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t ncols = tmem_cols(N3);
-  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
-  if (threadIdx.x == 0)
-    for (int s = 0; s < ST_STAGES; s++) tc::mbar_init(&mbar[s], 1);
+  // 1024-byte aligned stages (the swizzle pattern repeats every 256 bytes)
+  const uint32_t raw = tc::smem_addr(dsm);
+  uint8_t* smem = dsm + ((1024u - (raw & 1023u)) & 1023u);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, (uint32_t)plan.tmem_cols);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int q = 0; q < 2; q++) {
+      tc::mbar_init(&tfull[q], 1);
+      tc::mbar_init(&tempty[q], 128);
+    }
+    tc::mbar_init(&mdone, 1);
+    abort_flag = 0;
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = tmem_base;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, N3);
-  const uint32_t lbo = 128, sbo = (uint32_t)kg * 128;
+  volatile int* abort_p = &abort_flag;
   const int64_t P = (int64_t)a.n2 * a.n3;
   const int64_t ntiles = (a.ncell + 125) / 126;
   const int my_tiles = ntiles > blockIdx.x ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-  const int total = my_tiles * units;   // this CTA's pipeline steps
-  auto tile_start = [&](int k) {         // first output cell of this CTA's k-th tile
+  auto tile_start = [&](int k) {   // first output cell of this CTA's k-th tile
     const int64_t st = ((int64_t)blockIdx.x + (int64_t)k * gridDim.x) * 126;
     return st + 126 > a.ncell ? (a.ncell > 126 ? a.ncell - 126 : (int64_t)0) : st;
   };
-  // This thread's A copy chunks, fixed for every step: rows r = v / kg, chunk
-  // q = v % kg for v = tid + 128 i (i < kg): shared offsets and global offsets
-  // relative to the step's first row.
-  uint32_t a_soff[kg];
-  int64_t a_goff[kg];
-#pragma unroll
-  for (int i = 0; i < kg; i++) {
-    const int v = threadIdx.x + 128 * i, r = v / kg, q = v - r * kg;
-    a_soff[i] = (uint32_t)((r >> 3) * kg * 128 + q * 128 + (r & 7) * 16);
-    a_goff[i] = (int64_t)r * a.in_ld + q * 8;
-  }
-  // producer counters of the step being issued: tile kp, slab sp, channel chunk cpk
-  int kp = 0, sp = 0, cpk = 0;
-  int64_t row_base = my_tiles ? tile_start(0) - 1 : 0;
-  auto issue = [&](int gp) {   // copies of step gp into stage gp % ST_STAGES (an empty group past the end)
-    if (gp < total) {
-      const int di = sp / 3 - 1, dj = sp % 3 - 1;
-      const int64_t row0 = row_base + di * P + dj * (int64_t)a.n3;
-      uint8_t* sA = smem + (gp % ST_STAGES) * stage;
-      uint8_t* sB = sA + stage_a;
-      const uint16_t* src_a = a.in + row0 * a.in_ld + cpk * KC;
-#pragma unroll
-      for (int i = 0; i < kg; i++) cp_async16(sA + a_soff[i], src_a + a_goff[i]);
-      const uint16_t* src_b = a.W + (int64_t)sp * N3 * Ci + cpk * KC;
-      for (int v = threadIdx.x; v < N3 * kg; v += 128) {
-        const int n = v / kg, q = v - n * kg;
-        cp_async16(sB + (n >> 3) * kg * 128 + q * 128 + (n & 7) * 16, src_b + (int64_t)n * Ci + q * 8);
-      }
-      // advance to the next step
-      if (++cpk == nk) {
-        cpk = 0;
-        if (++sp == 9) {
-          sp = 0;
-          if (++kp < my_tiles) row_base = tile_start(kp) - 1;
+
+  if (warp == 4) {
+    if (lane == 0) {   // ---- producer
+      int g = 0;
+      int last[TM_MAX_STAGES];
+      for (int s = 0; s < TM_MAX_STAGES; s++) last[s] = -1;
+      bool ok = true;
+      for (int k = 0; k < my_tiles && ok; k++) {
+        const int64_t row_base = tile_start(k) - 1;
+        for (int sl = 0; sl < 9 && ok; sl++) {
+          const int di = sl / 3 - 1, dj = sl % 3 - 1;
+          const int row0 = (int)(row_base + di * P + dj * (int64_t)a.n3);
+          for (int c = 0; c < nk; c++, g++) {
+            const int st = g % S;
+            if (g >= S && !tm_wait(&empty[st], (uint32_t)(((g / S) - 1) & 1), abort_p)) {
+              ok = false;
+              break;
+            }
+            uint8_t* sa = smem + st * plan.stage_bytes;
+            mbar_expect_tx(&full[st], ab + bb);
+            tma_load_2d(sa, &tmX, c * 16, row0, &full[st]);
+            tma_load_2d(sa + ab, &tmW, c * 16, sl * N3, &full[st]);
+            last[st] = g;
+          }
         }
       }
+      // every copy issued has landed before the CTA may leave
+      for (int s = 0; s < S; s++)
+        if (last[s] >= 0) tm_wait(&full[s], (uint32_t)((last[s] / S) & 1), abort_p, false);
     }
-    cp_async_commit();
-  };
-  bool ok = true;
-  // Commits complete in issue order (each covers every earlier MMA), step g's
-  // being phase g / ST_STAGES of its stage's barrier.  `done` counts the steps
-  // this thread has seen complete, so a wait is idempotent; no stage's barrier
-  // runs a phase ahead of a waiting thread (a stage is refilled, and its next
-  // commit issued, only after every thread passed the wait for it).
-  int done = 0;
-  auto wait_stage = [&](int g) {   // MMAs of step g have finished
-    while (ok && done <= g) {
-      if (!tc::mbar_wait(&mbar[done % ST_STAGES], (uint32_t)((done / ST_STAGES) & 1))) { ok = false; break; }
-      done++;
-    }
-  };
-  int committed = 0;   // thread 0: steps whose MMAs it has committed
-  issue(0);
-  issue(1);
-  int k = 0, u = 0;   // consumer: tile and step within it of step g
-  for (int g = 0; g < total && ok; g++) {
-    // refill the stage of step g - 2 (its MMAs committed two steps ago) with step g + 2
-    if (g >= 2) wait_stage(g - 2);
-    issue(g + 2);
-    cp_async_wait<2>();   // this thread's copies of step g have landed
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    tc::fence_after_sync();
-    if (threadIdx.x == 0) {
-      const uint8_t* sA = smem + (g % ST_STAGES) * stage;
-      const uint8_t* sB = sA + stage_a;
-#pragma unroll
-      for (int kk = 0; kk < KC / 16; kk++) {
-        const uint64_t ad = tc::smem_desc(tc::smem_addr(sA + kk * 256), lbo, sbo);
-        const uint64_t bd = tc::smem_desc(tc::smem_addr(sB + kk * 256), lbo, sbo);
-        tc::mma_bf16(tbase, ad, bd, idesc, u > 0 || kk > 0);
-      }
-      tc::mma_commit(&mbar[g % ST_STAGES]);
-      committed = g + 1;
-    }
-    if (++u != units) continue;
-    u = 0;
-    // ---- epilogue of the tile: the accumulator is complete once step g's MMAs are
-    wait_stage(g);
-    if (!__syncthreads_and(ok)) { ok = false; break; }
-    tc::fence_after_sync();
-    const int64_t c0 = tile_start(k++);
-    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
-    // pass 1: rows at the warp edges for the neighbouring warps
-    for (int co = 0; co < Co; co += 8) {
-      uint32_t dm[8], dp[8];
-      tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
-      tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
-      tc::tmem_wait_ld(dm, dp);
-      if (lane == 31)
-        for (int q = 0; q < 8; q++) xch[0][warp][co + q] = __uint_as_float(dm[q]);
-      if (lane == 0)
-        for (int q = 0; q < 8; q++) xch[1][warp][co + q] = __uint_as_float(dp[q]);
-    }
-    __syncthreads();
-    const int r = warp * 32 + lane;
-    const int64_t c = c0 + r - 1;
-    const bool live = r >= 1 && r <= 126 && c < a.ncell;
-    const float m = live ? (float)a.mask[c] : 0.f;
-    for (int co = 0; co < Co; co += 8) {
-      uint32_t dm[8], d0[8], dp[8];
-      tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
-      tc::tmem_ld8_nowait(trow + (uint32_t)(Co + co), d0);
-      tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
-      tc::tmem_wait_ld(dm, d0, dp);
-      float v[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        float prev = __shfl_up_sync(0xffffffffu, __uint_as_float(dm[q]), 1);
-        float next = __shfl_down_sync(0xffffffffu, __uint_as_float(dp[q]), 1);
-        if (lane == 0) prev = warp > 0 ? xch[0][warp - 1][co + q] : 0.f;
-        if (lane == 31) next = warp < 3 ? xch[1][warp + 1][co + q] : 0.f;
-        v[q] = prev + __uint_as_float(d0[q]) + next;
-      }
-      if (!live || co >= a.out_ch) continue;
-      uint16_t gt[8];
-      if (a.gate) *reinterpret_cast<uint4*>(gt) = *reinterpret_cast<const uint4*>(a.gate + c * a.gate_ld + co);
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        float x = v[q] + (a.bias ? a.bias[co + q] : 0.f);
-        if (a.relu) x = fmaxf(x, 0.f);
-        if (a.gate && ((gt[q] & 0x8000u) || !(gt[q] & 0x7FFFu))) x = 0.f;   // gate value <= 0
-        v[q] = x * m;
-      }
-      if (a.out16) {
-        uint32_t pk[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
-          pk[q] = *reinterpret_cast<const uint32_t*>(&h);
+    __syncwarp();
+  } else if (warp == 5) {
+    if (lane == 0) {   // ---- MMA issuer
+      const uint32_t idesc = tc::idesc_bf16_f32(128, N3);
+      int g = 0;
+      bool ok = true;
+      for (int k = 0; k < my_tiles && ok; k++) {
+        const int acc = k & 1;
+        if (k >= 2 && !tm_wait(&tempty[acc], (uint32_t)(((k / 2) - 1) & 1), abort_p)) break;
+        tc::fence_after_sync();
+        const uint32_t dacc = tbase + (uint32_t)(acc * plan.acc_off);
+        for (int u = 0; u < steps; u++, g++) {
+          const int st = g % S;
+          if (!tm_wait(&full[st], (uint32_t)((g / S) & 1), abort_p)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint8_t* sa = smem + st * plan.stage_bytes;
+          tc::mma_bf16(dacc, smem_desc_sw32(tc::smem_addr(sa)), smem_desc_sw32(tc::smem_addr(sa + ab)), idesc,
+                       u > 0);
+          tc::mma_commit(&empty[st]);
         }
-        *reinterpret_cast<uint4*>(a.out16 + c * a.out_ld + co) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-      } else {
-        const int nq = min(8, a.out_ch - co);
-        for (int q = 0; q < nq; q++) a.out32[c * a.out_ld + co + q] = v[q];
+        if (ok) tc::mma_commit(&tfull[acc]);
       }
+      // every MMA issued has completed before TMEM is freed
+      tc::mma_commit(&mdone);
+      tm_wait(&mdone, 0, abort_p, false);
     }
-    tc::fence_before_sync();
-    __syncthreads();   // TMEM and the exchange rows are read before the next tile reuses them
-  }
-  cp_async_wait<0>();   // no copy may land after the block leaves
-  if (!ok) {
-    if (threadIdx.x == 0) atomicExch(a.err, 1);
-  }
-  // every commit thread 0 issued has been observed (bounded waits) before TMEM is freed
-  if (threadIdx.x == 0) {
-    while (done < committed) {
-      if (!tc::mbar_wait(&mbar[done % ST_STAGES], (uint32_t)((done / ST_STAGES) & 1))) break;
-      done++;
+    __syncwarp();
+  } else {   // ---- epilogue, warps 0-3
+    for (int k = 0; k < my_tiles; k++) {
+      const int acc = k & 1;
+      const bool got = tm_wait(&tfull[acc], (uint32_t)((k / 2) & 1), abort_p);
+      if (!epi_sync_and(got)) break;
+      tc::fence_after_sync();
+      const int64_t c0 = tile_start(k);
+      const uint32_t trow = tbase + (uint32_t)(acc * plan.acc_off) + ((uint32_t)(warp * 32) << 16);
+      // pass 1: rows at the warp edges for the neighbouring warps
+      for (int co = 0; co < Co; co += 8) {
+        uint32_t dm[8], dp[8];
+        tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
+        tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
+        tc::tmem_wait_ld(dm, dp);
+        if (lane == 31)
+          for (int q = 0; q < 8; q++) xch[warp][0][co + q] = __uint_as_float(dm[q]);
+        if (lane == 0)
+          for (int q = 0; q < 8; q++) xch[warp][1][co + q] = __uint_as_float(dp[q]);
+      }
+      epi_sync();
+      const int r = warp * 32 + lane;
+      const int64_t c = c0 + r - 1;
+      const bool live = r >= 1 && r <= 126 && c < a.ncell;
+      const float m = live ? (float)a.mask[c] : 0.f;
+      for (int co = 0; co < Co; co += 8) {
+        uint32_t dm[8], d0[8], dp[8];
+        tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
+        tc::tmem_ld8_nowait(trow + (uint32_t)(Co + co), d0);
+        tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
+        tc::tmem_wait_ld(dm, d0, dp);
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          float prev = __shfl_up_sync(0xffffffffu, __uint_as_float(dm[q]), 1);
+          float next = __shfl_down_sync(0xffffffffu, __uint_as_float(dp[q]), 1);
+          if (lane == 0) prev = warp > 0 ? xch[warp - 1][0][co + q] : 0.f;
+          if (lane == 31) next = warp < 3 ? xch[warp + 1][1][co + q] : 0.f;
+          v[q] = prev + __uint_as_float(d0[q]) + next;
+        }
+        if (!live || co >= a.out_ch) continue;
+        uint16_t gt[8];
+        if (a.gate) *reinterpret_cast<uint4*>(gt) = *reinterpret_cast<const uint4*>(a.gate + c * a.gate_ld + co);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          float x = v[q] + (a.bias ? a.bias[co + q] : 0.f);
+          if (a.relu) x = fmaxf(x, 0.f);
+          if (a.gate && ((gt[q] & 0x8000u) || !(gt[q] & 0x7FFFu))) x = 0.f;   // gate value <= 0
+          v[q] = x * m;
+        }
+        if (a.out16) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+            pk[q] = *reinterpret_cast<const uint32_t*>(&h);
+          }
+          *reinterpret_cast<uint4*>(a.out16 + c * a.out_ld + co) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        } else {
+          const int nq = min(8, a.out_ch - co);
+          for (int q = 0; q < nq; q++) a.out32[c * a.out_ld + co + q] = v[q];
+        }
+      }
+      // the accumulator is read: the MMA issuer may overwrite it two tiles on
+      tc::fence_before_sync();
+      mbar_arrive(&tempty[acc]);
+      epi_sync();   // the exchange rows are read before the next tile rewrites them
     }
   }
-  tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, ncols);
+  if (threadIdx.x == 0 && abort_flag) atomicExch(a.err, 1);
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, (uint32_t)plan.tmem_cols);
+}
+
+// cuTensorMapEncodeTiled, from the driver at run time (the library links the
+// runtime only).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+// A BF16 matrix of `rows` x `cols` (row pitch `ld` elements) read in boxes of
+// box_rows x 16 columns with the 32-byte swizzle; rows outside [0, rows) read
+// as zeros.
+static bool encode_sw32(CUtensorMap* m, const void* base, int64_t rows, int cols, int ld, int box_rows) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {16, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Error flag of the convolutions: a slot of the context scratch, cleared by
@@ -513,19 +625,24 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_l
   a.out_ld = out_ld; a.out_ch = out_ch; a.relu = relu; a.err = err;
   const int64_t ntiles = (a.ncell + TC_M - 1) / TC_M;
   if (3 * co <= 256) {
-    // k-taps stacked along N (the per-tap kernel below takes wider outputs)
-    const int KC = ci == 16 ? 16 : ci == 48 ? 48 : ci % 32 == 0 ? 32 : 16;
-    auto kern = KC == 16 ? k_conv3_st<16> : KC == 32 ? k_conv3_st<32> : k_conv3_st<48>;
-    const size_t smem = (size_t)ST_STAGES * ((128 + 3 * co) * KC * 2);
-    XF_CUDA(ctx, set_max_smem((const void*)kern, KC == 16 ? 0 : KC == 32 ? 1 : 2, ctx->device, smem));
-    int per_sm = (int)((227 * 1024) / (smem + 3 * 1024 + 1024));
-    per_sm = min(per_sm, (int)(512 / tmem_cols(3 * co)));
-    per_sm = min(per_sm, 16);
-    if (per_sm < 1) per_sm = 1;
+    // k-taps stacked along N, operands by tensor copies (the per-tap kernel
+    // below takes wider outputs).  CTAs per SM: tensor-memory columns (512 per
+    // SM) first, then the shared memory (227 KB per SM, with ~4 KB static and
+    // reserved per CTA) is split between them.
+    const int tcols = (int)tmem_cols((3 * co + 31) / 32 * 32 + 3 * co);
+    int per_sm = 512 / tcols;
+    if (per_sm > 4) per_sm = 4;
+    const TmPlan plan = tm_plan(co, (227 * 1024) / per_sm - 4 * 1024);
+    if (a.ncell + (int64_t)n2 * n3 + n3 + 2 > 2147483647LL)   // the copies' row coordinates are 32-bit
+      return xf_fail(ctx, XF_ERR_ARG, "convolution: box too large for 32-bit copy coordinates");
+    CUtensorMap tmX, tmW;
+    if (!encode_sw32(&tmX, in, a.ncell, ci, in_ld, 128) || !encode_sw32(&tmW, weights, 27LL * co, ci, ci, 3 * co))
+      return xf_fail(ctx, XF_ERR_CUDA, "convolution: tensor map encoding failed");
+    XF_CUDA(ctx, set_max_smem((const void*)k_conv3_tma, 0, ctx->device, (size_t)plan.smem_bytes));
     const int64_t tiles = (a.ncell + 125) / 126;
     int64_t blocks = (int64_t)ctx->sm_count * per_sm;
     if (blocks > tiles) blocks = tiles;
-    kern<<<(int)blocks, 128, smem, ctx->stream>>>(a);
+    k_conv3_tma<<<(int)blocks, TM_THREADS, plan.smem_bytes, ctx->stream>>>(a, tmX, tmW, plan);
     XF_CUDA(ctx, cudaGetLastError());
     return XF_OK;
   }
