@@ -435,23 +435,27 @@ int xf_ib_spread(xf_ib* ib, xf_vec* force, const double* h0, int axis);
 int xf_tc_gemm_bf16(xf_ctx* ctx, int N, int K, const uint16_t* host_a, const uint16_t* host_b, float* host_d,
                     int variant);
 
-/* 3x3x3 convolution of a channels-last BF16 activation box on the tensor cores
- * (implicit GEMM: 128-cell tiles, 27 taps x ci/16 MMAs accumulated in tensor
- * memory).  n1 x n2 x n3 is the level's box (ghost layer included); `in`
- * points at cell 0 of the input slice (ci channels, row pitch in_ld) inside an
- * allocation that extends XF_CONV_MARGIN(n2, n3) rows before cell 0 and after
+/* 3x3x3 convolution of a BF16 activation box on the tensor cores (implicit
+ * GEMM: 126- or 128-cell tiles, 27 taps x ci/16 MMAs accumulated in tensor
+ * memory).  n1 x n2 x n3 is the level's box (ghost layer included).
+ * Activations are stored in channel planes of 8: plane q holds channels
+ * 8q .. 8q+7 of every cell, 16 bytes per cell, element (cell c, channel ch) at
+ * (ch / 8) * plane_stride + c * 8 + ch % 8 (elements).  `in` points at cell 0
+ * of the input slice's first plane (ci channels, plane stride in_ps elements),
+ * and every plane extends XF_CONV_MARGIN(n2, n3) cells before cell 0 and after
  * the last cell, all holding 0, as must every ghost and inactive cell (the
  * ghost layer is the zero padding).  weights [27][co][ci] BF16 with tap
  * t = 9 (di+1) + 3 (dj+1) + (dk+1); bias [co] FP32 or NULL; mask [cells] 0/1.
  * out = mask * act(conv + bias), act = ReLU when relu != 0, first out_ch
- * channels, BF16 (out_fp32 = 0) or FP32, row pitch out_ld, at `out` (cell 0).
+ * channels: BF16 planes of stride out_pitch elements (out_fp32 = 0, out_ch a
+ * multiple of 8) or FP32 cell rows of pitch out_pitch, at `out` (cell 0).
  * ci, co multiples of 16 up to 128; device pointers, 16-byte aligned;
  * asynchronous on the context stream (xf_conv_status reports a tensor-core
  * wait that ran out).  No counterpart in the reference. */
 #define XF_CONV_MARGIN(n2, n3) ((int64_t)(n2) * (n3) + (n3) + 1 + 128)
-int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci, const void* weights,
-                   const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
-                   int relu);
+int xf_conv3d_bf16(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int64_t in_ps, int ci, const void* weights,
+                   const float* bias, int co, const uint8_t* mask, void* out, int64_t out_pitch, int out_ch,
+                   int out_fp32, int relu);
 int xf_conv_status(xf_ctx* ctx);
 
 /* The learned preconditioner: a 3-level 3-D U-Net (16/32/64 channels, 3x3x3

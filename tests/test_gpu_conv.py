@@ -50,25 +50,37 @@ def conv_ref(x, W, bias, mask, relu):
 
 
 def run_conv(ctx, x, W, bias, mask, relu, out_fp32, out_ch=None):
+    """Activations in channel planes of 8 (plane q: channels 8q..8q+7 of every
+    cell, each plane with its zero margins); FP32 output as cell rows."""
     n1, n2, n3, ci = x.shape
     co = W.shape[1]
     out_ch = co if out_ch is None else out_ch
     n = n1 * n2 * n3
     margin = n2 * n3 + n3 + 1 + 128
-    xb = torch.zeros((n + 2 * margin, ci), dtype=torch.bfloat16, device="cuda")
-    xb[margin:margin + n] = torch.from_numpy(x.reshape(n, ci).astype(np.float32)).to("cuda", torch.bfloat16)
+    rows = n + 2 * margin
+    xb = torch.zeros((ci // 8, rows, 8), dtype=torch.bfloat16, device="cuda")
+    planes = x.reshape(n, ci // 8, 8).transpose(1, 0, 2).astype(np.float32)
+    xb[:, margin:margin + n] = torch.from_numpy(np.ascontiguousarray(planes)).to("cuda", torch.bfloat16)
     Wt = torch.from_numpy(W.astype(np.float32)).to("cuda", torch.bfloat16).contiguous()
     bt = torch.from_numpy(bias.astype(np.float32)).cuda() if bias is not None else None
     mt = torch.from_numpy(mask.reshape(n).astype(np.uint8)).cuda()
-    out = torch.zeros((n, out_ch), dtype=torch.float32 if out_fp32 else torch.bfloat16, device="cuda")
+    if out_fp32:
+        out = torch.zeros((n, out_ch), dtype=torch.float32, device="cuda")
+        pitch = out_ch
+    else:
+        out = torch.zeros((out_ch // 8, n, 8), dtype=torch.bfloat16, device="cuda")
+        pitch = n * 8
     torch.cuda.synchronize()
-    st = capi.lib().xf_conv3d_bf16(ctx.h, n1, n2, n3, C.c_void_p(xb.data_ptr() + margin * ci * 2), ci, ci,
+    st = capi.lib().xf_conv3d_bf16(ctx.h, n1, n2, n3, C.c_void_p(xb.data_ptr() + margin * 8 * 2), rows * 8, ci,
                                    C.c_void_p(Wt.data_ptr()), C.c_void_p(bt.data_ptr()) if bt is not None else None,
-                                   co, C.c_void_p(mt.data_ptr()), C.c_void_p(out.data_ptr()), out_ch, out_ch,
+                                   co, C.c_void_p(mt.data_ptr()), C.c_void_p(out.data_ptr()), pitch, out_ch,
                                    int(out_fp32), int(relu))
     xf._check(ctx.h, st)
     xf._check(ctx.h, capi.lib().xf_conv_status(ctx.h))
-    return out.float().cpu().numpy().reshape(n1, n2, n3, out_ch)
+    y = out.float().cpu().numpy()
+    if not out_fp32:
+        y = y.transpose(1, 0, 2).reshape(n, out_ch)
+    return y.reshape(n1, n2, n3, out_ch)
 
 
 def case(shape, ci, co, seed):

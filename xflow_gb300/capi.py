@@ -110,8 +110,8 @@ def lib():
         L.xf_voxelize_mesh.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_longlong, vp, C.c_longlong,
                                        C.c_int32, vp]
         L.xf_tc_gemm_bf16.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, C.c_int]
-        L.xf_conv3d_bf16.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp,
-                                     C.c_int, C.c_int, C.c_int, C.c_int]
+        L.xf_conv3d_bf16.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int64, C.c_int, vp, vp, C.c_int, vp, vp,
+                                     C.c_int64, C.c_int, C.c_int, C.c_int]
         L.xf_conv_status.argtypes = [vp]
         L.xf_unet_create.argtypes = [vp, C.POINTER(vp)]
         L.xf_unet_destroy.argtypes = [vp]

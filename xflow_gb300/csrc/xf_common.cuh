@@ -288,3 +288,20 @@ __device__ inline double finish_partials(DevScratch* S, int slot, double* sh) {
   for (int b = threadIdx.x; b < nb; b += blockDim.x) v += __ldcg(&S->partials[slot][b]);
   return block_sum(v, sh);
 }
+
+// ---------------------------------------------------------------------------
+// BF16 activations of the learned preconditioner are stored in channel planes
+// of 8: plane q holds channels 8q .. 8q+7 of every cell, 16 bytes per cell,
+// so element (cell c, channel ch) sits at (ch / 8) * plane_stride + c * 8 +
+// ch % 8.  A block of consecutive cells of one plane is then the canonical
+// K-major operand layout of the tensor cores (core matrices of 8 rows x 16
+// bytes), copied by one bulk copy whatever its first cell.
+//
+// Convolution weights for the tensor cores, tiled per (16-channel input
+// chunk c, slab s = 3 (di+1) + (dj+1), 8-channel half q, stacked output row
+// n = dk_index * Co + o, 8 channels): the 9 slabs of one chunk are contiguous,
+// and each (c, s) block is the canonical K-major B operand of one MMA.
+__host__ __device__ inline int64_t conv_tiled_index(int t, int o, int i, int co, int ci) {
+  const int s = t / 3, n = (t % 3) * co + o, c = i >> 4, q = (i >> 3) & 1, e = i & 7;
+  return ((((int64_t)c * 9 + s) * 2 + q) * (3 * co) + n) * 8 + e;
+}

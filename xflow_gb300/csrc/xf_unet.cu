@@ -25,9 +25,9 @@
 
 #include "xf_control.cuh"
 
-int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int in_ld, int ci, const void* weights,
-                   const float* bias, int co, const uint8_t* mask, void* out, int out_ld, int out_ch, int out_fp32,
-                   int relu, const void* gate, int gate_ld);
+int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int64_t in_ps, int ci, const void* weights,
+                   const void* tiled, const float* bias, int co, const uint8_t* mask, void* out, int64_t out_pitch,
+                   int out_ch, int out_fp32, int relu, const void* gate, int64_t gate_ps);
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
 void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot);
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
@@ -51,12 +51,15 @@ struct Level {
   int64_t active = 0;
 };
 
-// channels-last BF16 activation box with its zero margins
+// BF16 activation box in channel planes of 8 (xf_common.cuh), every plane
+// with its zero margins
 struct Act {
   uint16_t* base = nullptr;
   int C = 0, level = 0;
-  int64_t rows = 0;
-  uint16_t* p0(const Level* L) const { return base + L[level].margin * C; }
+  int64_t rows = 0;   // cells per plane, margins included
+  int64_t ps() const { return rows * 8; }
+  uint16_t* p0(const Level* L) const { return base + L[level].margin * 8; }                 // plane 0, cell 0
+  uint16_t* ch(const Level* L, int c0) const { return p0(L) + (int64_t)(c0 / 8) * ps(); }   // channel c0's plane
 };
 
 enum { ENC0A, ENC0B, ENC1A, ENC1B, MIDA, MIDB, DEC1A, DEC1B, DEC0A, DEC0B, OUTL, NLAYER };
@@ -72,6 +75,7 @@ struct Layer {
   float* b = nullptr;         // [co]
   uint16_t* w16 = nullptr;    // BF16 [27][co][ci]
   uint16_t* wt16 = nullptr;   // BF16 flipped transpose [27][ci][co]: w16[26-t][co][ci]
+  uint16_t *w16t = nullptr, *wt16t = nullptr;   // the same two in the tensor cores' tiled order
   float *gw = nullptr, *gb = nullptr;                  // gradients
   float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;   // Adam moments
 };
@@ -132,27 +136,44 @@ __device__ __forceinline__ uint16_t f2bf(float x) {
 }
 
 // Average of the 8 children (inactive children hold 0), times the coarse mask.
-// src: fine slice (pointer at cell 0, pitch sld), dst: coarse (pitch dld), C channels.
-__global__ void k_pool(const uint16_t* __restrict__ src, int sld, int f2, int f3, uint16_t* __restrict__ dst,
-                       int dld, const uint8_t* __restrict__ cmask, int c1, int c2, int c3, int C) {
-  const int64_t n = (int64_t)c1 * c2 * c3 * C;
+// src: fine slice (plane 0 at cell 0, plane stride sps), dst: coarse (dps),
+// C channels; one thread per cell and plane (16 bytes).
+__device__ __forceinline__ void bf8_acc(float (&s)[8], uint4 v) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    s[2 * q] += bf2f((uint16_t)(w[q] & 0xFFFFu));
+    s[2 * q + 1] += bf2f((uint16_t)(w[q] >> 16));
+  }
+}
+__device__ __forceinline__ uint4 bf8_pack(const float (&s)[8], float scale) {
+  uint32_t w[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) w[q] = (uint32_t)f2bf(s[2 * q] * scale) | ((uint32_t)f2bf(s[2 * q + 1] * scale) << 16);
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__global__ void k_pool(const uint16_t* __restrict__ src, int64_t sps, int f2, int f3, uint16_t* __restrict__ dst,
+                       int64_t dps, const uint8_t* __restrict__ cmask, int c1, int c2, int c3, int C) {
+  const int C8 = C / 8;
+  const int64_t n = (int64_t)c1 * c2 * c3 * C8;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = u / C;
-    const int ch = (int)(u - c * C);
+    const int64_t c = u / C8;
+    const int g = (int)(u - c * C8);
     const int I = (int)(c / ((int64_t)c2 * c3)), J = (int)((c / c3) % c2), K = (int)(c % c3);
-    float s = 0.f;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (cmask[c])
       for (int a = 0; a < 2; a++)
         for (int b = 0; b < 2; b++)
           for (int d = 0; d < 2; d++)
-            s += bf2f(src[(((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * sld + ch]);
-    dst[c * dld + ch] = f2bf(s * 0.125f);
+            bf8_acc(s, *reinterpret_cast<const uint4*>(
+                           src + g * sps + (((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * 8));
+    *reinterpret_cast<uint4*>(dst + g * dps + c * 8) = bf8_pack(s, 0.125f);
   }
 }
 
 // Pooling backward: every active fine child receives 1/8 of its parent's
 // gradient, added to an FP32 accumulator (pitch ald).
-__global__ void k_pool_bwd(const uint16_t* __restrict__ gcoarse, int gld, int c2, int c3,
+__global__ void k_pool_bwd(const uint16_t* __restrict__ gcoarse, int64_t gps, int c2, int c3,
                            const uint8_t* __restrict__ fmask, int f1, int f2, int f3, float* __restrict__ acc,
                            int ald, int C) {
   const int64_t n = (int64_t)f1 * f2 * f3 * C;
@@ -162,69 +183,71 @@ __global__ void k_pool_bwd(const uint16_t* __restrict__ gcoarse, int gld, int c2
     if (!fmask[c]) continue;
     const int i = (int)(c / ((int64_t)f2 * f3)), j = (int)((c / f3) % f2), k = (int)(c % f3);
     const int64_t pc = ((int64_t)(1 + (i - 1) / 2) * c2 + (1 + (j - 1) / 2)) * c3 + (1 + (k - 1) / 2);
-    acc[c * ald + ch] += 0.125f * bf2f(gcoarse[pc * gld + ch]);
+    acc[c * ald + ch] += 0.125f * bf2f(gcoarse[(ch >> 3) * gps + pc * 8 + (ch & 7)]);
   }
 }
 
 // Nearest upsampling of a coarse slice into a fine slice, times the fine mask;
-// 8 channels (16 bytes) per thread (C, pitches and slice offsets are multiples of 8).
-__global__ void k_upsample(const uint16_t* __restrict__ src, int sld, int c2, int c3, uint16_t* __restrict__ dst,
-                           int dld, const uint8_t* __restrict__ fmask, int f1, int f2, int f3, int C) {
+// one plane (8 channels, 16 bytes) per thread.
+__global__ void k_upsample(const uint16_t* __restrict__ src, int64_t sps, int c2, int c3, uint16_t* __restrict__ dst,
+                           int64_t dps, const uint8_t* __restrict__ fmask, int f1, int f2, int f3, int C) {
   const int C8 = C / 8;
   const int64_t n = (int64_t)f1 * f2 * f3 * C8;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = u / C8;
-    const int ch = (int)(u - c * C8) * 8;
+    const int g = (int)(u - c * C8);
     uint4 v = make_uint4(0, 0, 0, 0);
     if (fmask[c]) {
       const int i = (int)(c / ((int64_t)f2 * f3)), j = (int)((c / f3) % f2), k = (int)(c % f3);
       const int64_t pc = ((int64_t)(1 + (i - 1) / 2) * c2 + (1 + (j - 1) / 2)) * c3 + (1 + (k - 1) / 2);
-      v = *reinterpret_cast<const uint4*>(src + pc * sld + ch);
+      v = *reinterpret_cast<const uint4*>(src + g * sps + pc * 8);
     }
-    *reinterpret_cast<uint4*>(dst + c * dld + ch) = v;
+    *reinterpret_cast<uint4*>(dst + g * dps + c * 8) = v;
   }
 }
 
 // Upsampling backward: a coarse cell's gradient is the sum over its 8
 // children; then x coarse mask and the coarse activation's ReLU gate.
-__global__ void k_upsample_bwd(const uint16_t* __restrict__ gfine, int gld, int f2, int f3,
-                               const uint16_t* __restrict__ gate, int gtld, const uint8_t* __restrict__ cmask,
-                               int c1, int c2, int c3, uint16_t* __restrict__ dst, int dld, int C) {
+__global__ void k_upsample_bwd(const uint16_t* __restrict__ gfine, int64_t gps, int f2, int f3,
+                               const uint16_t* __restrict__ gate, int64_t gtps, const uint8_t* __restrict__ cmask,
+                               int c1, int c2, int c3, uint16_t* __restrict__ dst, int64_t dps, int C) {
   const int64_t n = (int64_t)c1 * c2 * c3 * C;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = u / C;
     const int ch = (int)(u - c * C);
     float s = 0.f;
-    if (cmask[c] && bf2f(gate[c * gtld + ch]) > 0.f) {
+    const int64_t pl = (int64_t)(ch >> 3), e = ch & 7;
+    if (cmask[c] && bf2f(gate[pl * gtps + c * 8 + e]) > 0.f) {
       const int I = (int)(c / ((int64_t)c2 * c3)), J = (int)((c / c3) % c2), K = (int)(c % c3);
       for (int a = 0; a < 2; a++)
         for (int b = 0; b < 2; b++)
           for (int d = 0; d < 2; d++)
-            s += bf2f(gfine[(((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * gld + ch]);
+            s += bf2f(gfine[pl * gps + (((int64_t)(2 * I - 1 + a) * f2 + (2 * J - 1 + b)) * f3 + (2 * K - 1 + d)) * 8 + e]);
     }
-    dst[c * dld + ch] = f2bf(s);
+    dst[pl * dps + c * 8 + e] = f2bf(s);
   }
 }
 
 // Skip gradient: dPre = (skip part of the decoder's input gradient + pooled
 // path's accumulator) x mask x ReLU gate; the accumulator is cleared.
-__global__ void k_skip_grad(const uint16_t* __restrict__ gskip, int gld, float* __restrict__ acc, int ald,
-                            const uint16_t* __restrict__ gate, int gtld, const uint8_t* __restrict__ mask, int64_t ncell,
-                            uint16_t* __restrict__ dst, int dld, int C) {
+__global__ void k_skip_grad(const uint16_t* __restrict__ gskip, int64_t gps, float* __restrict__ acc, int ald,
+                            const uint16_t* __restrict__ gate, int64_t gtps, const uint8_t* __restrict__ mask,
+                            int64_t ncell, uint16_t* __restrict__ dst, int64_t dps, int C) {
   const int64_t n = ncell * C;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = u / C;
     const int ch = (int)(u - c * C);
-    float v = bf2f(gskip[c * gld + ch]) + acc[c * ald + ch];
+    const int64_t o = c * 8 + (ch & 7), pl = ch >> 3;
+    float v = bf2f(gskip[pl * gps + o]) + acc[c * ald + ch];
     acc[c * ald + ch] = 0.f;
-    if (!mask[c] || !(bf2f(gate[c * gtld + ch]) > 0.f)) v = 0.f;
-    dst[c * dld + ch] = f2bf(v);
+    if (!mask[c] || !(bf2f(gate[pl * gtps + o]) > 0.f)) v = 0.f;
+    dst[pl * dps + o] = f2bf(v);
   }
 }
 
-// Sum of squares over the active cells (FP64 atomics into red[slot]).
-// Per-block partials, summed in block order by the last block to finish, so
-// the result does not depend on scheduling (256 threads, at most RP_MAX blocks).
+// Sum of squares over the active cells into red[slot].  Per-block partials,
+// summed in a fixed order by the last block to finish, so the result does
+// not depend on scheduling (256 threads, at most RP_MAX blocks).
 constexpr int RP_MAX = 4096;
 __global__ void __launch_bounds__(256) k_sumsq(const double* __restrict__ x, const uint8_t* __restrict__ m, int64_t n,
                                                double* red, int slot, double* part, unsigned* tick) {
@@ -244,32 +267,42 @@ __global__ void __launch_bounds__(256) k_sumsq(const double* __restrict__ x, con
     last = atomicAdd(&tick[slot], 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
+  // the last block sums the partials: thread t takes t, t + 256, ... in
+  // order, then a fixed tree over the threads (the same order every run)
   __threadfence();
   double t = 0;
-  for (unsigned k = 0; k < gridDim.x; k++) t += __ldcg(&part[slot * RP_MAX + k]);
-  red[slot] = t;
-  tick[slot] = 0;
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += 256) t += __ldcg(&part[slot * RP_MAX + k]);
+  __shared__ double st[256];
+  st[threadIdx.x] = t;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) st[threadIdx.x] += st[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    red[slot] = st[0];
+    tick[slot] = 0;
+  }
 }
 
 // Level-0 input: channel 0 = r / rms(r) on active cells, channels 1..15 = 0.
 __global__ void k_unet_input(const double* __restrict__ r, const uint8_t* __restrict__ m, int64_t n,
-                             const double* __restrict__ red, double count, uint16_t* __restrict__ x0) {
+                             const double* __restrict__ red, double count, uint16_t* __restrict__ x0, int64_t ps) {
   const double ss = red[0];
   const float inv = ss > 0 ? (float)(1.0 / sqrt(ss / count)) : 0.f;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     uint16_t v[16] = {0};
     if (m[c]) v[0] = f2bf((float)r[c] * inv);
-    uint4* d = reinterpret_cast<uint4*>(x0 + c * 16);
-    d[0] = *reinterpret_cast<uint4*>(&v[0]);
-    d[1] = *reinterpret_cast<uint4*>(&v[8]);
+    *reinterpret_cast<uint4*>(x0 + c * 8) = *reinterpret_cast<uint4*>(&v[0]);
+    *reinterpret_cast<uint4*>(x0 + ps + c * 8) = *reinterpret_cast<uint4*>(&v[8]);
   }
 }
 
 // Loss (mean over active cells of (z - t)^2, t = e / rms(e)) and its
 // gradient as the output layer's 16-channel dPre (channel 0).
 __global__ void k_unet_loss(const float* __restrict__ z, const double* __restrict__ e, const uint8_t* __restrict__ m,
-                            int64_t n, double count, double* red, uint16_t* __restrict__ g16) {
+                            int64_t n, double count, double* red, uint16_t* __restrict__ g16, int64_t ps) {
   const double ss = red[1];
   const double inv = ss > 0 ? 1.0 / sqrt(ss / count) : 0.0;
   double l = 0;
@@ -280,9 +313,8 @@ __global__ void k_unet_loss(const float* __restrict__ z, const double* __restric
       l += d * d;
       v[0] = f2bf((float)(2.0 * d / count));
     }
-    uint4* dst = reinterpret_cast<uint4*>(g16 + c * 16);
-    dst[0] = *reinterpret_cast<uint4*>(&v[0]);
-    dst[1] = *reinterpret_cast<uint4*>(&v[8]);
+    *reinterpret_cast<uint4*>(g16 + c * 8) = *reinterpret_cast<uint4*>(&v[0]);
+    *reinterpret_cast<uint4*>(g16 + ps + c * 8) = *reinterpret_cast<uint4*>(&v[8]);
   }
   for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(&red[2], l / count);
@@ -301,8 +333,9 @@ static int64_t wg_chunk(int64_t n) {
   c = (c + WG_CELLS - 1) / WG_CELLS * WG_CELLS;
   return c < 4096 ? 4096 : c;
 }
-__global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, int gld, const uint16_t* __restrict__ x,
-                                               int xld, int ci, int co, int n2, int n3, int64_t ncell, int chunk,
+__global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, int64_t gps,
+                                               const uint16_t* __restrict__ x, int64_t xps, int ci, int co, int n2,
+                                               int n3, int64_t ncell, int chunk,
                                                float* __restrict__ wpart, float* __restrict__ bpart) {
   extern __shared__ float wsm[];
   float* sg = wsm;                   // [WG_CELLS][co]
@@ -321,11 +354,11 @@ __global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, i
     __syncthreads();
     for (int u = threadIdx.x; u < WG_CELLS * co; u += 256) {
       const int r = u / co, ch = u - r * co;
-      sg[u] = r < nc ? bf2f(g[(cb + r) * gld + ch]) : 0.f;
+      sg[u] = r < nc ? bf2f(g[(ch >> 3) * gps + (cb + r) * 8 + (ch & 7)]) : 0.f;
     }
     for (int u = threadIdx.x; u < WG_CELLS * ci; u += 256) {
       const int r = u / ci, ch = u - r * ci;
-      sx[u] = r < nc ? bf2f(x[(cb + r + off) * xld + ch]) : 0.f;
+      sx[u] = r < nc ? bf2f(x[(ch >> 3) * xps + (cb + r + off) * 8 + (ch & 7)]) : 0.f;
     }
     __syncthreads();
     for (int q = 0; q < per; q++) {
@@ -362,7 +395,8 @@ __global__ void k_wgrad_sum(const float* __restrict__ wpart, const float* __rest
 }
 
 // Adam step on one layer (bias-corrected, step counts from 1), then the BF16
-// copies: w16[t][co][ci] and the flipped transpose wt16[26-t][ci][co].
+// copies: w16[t][co][ci] and the flipped transpose wt16[26-t][ci][co], each
+// also in the tiled order.
 __global__ void k_adam(float* w, float* gwt, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
                        float c1, float c2, int clear) {
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
@@ -377,7 +411,7 @@ __global__ void k_adam(float* w, float* gwt, float* m, float* v, int64_t n, floa
 }
 
 __global__ void k_weights_bf16(const float* __restrict__ w, int co, int ci, uint16_t* __restrict__ w16,
-                               uint16_t* __restrict__ wt16) {
+                               uint16_t* __restrict__ wt16, uint16_t* __restrict__ w16t, uint16_t* __restrict__ wt16t) {
   const int64_t n = (int64_t)27 * co * ci;
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
     const int t = (int)(u / ((int64_t)co * ci));
@@ -385,6 +419,8 @@ __global__ void k_weights_bf16(const float* __restrict__ w, int co, int ci, uint
     const uint16_t h = f2bf(w[u]);
     w16[u] = h;
     wt16[((int64_t)(26 - t) * ci + i) * co + o] = h;
+    w16t[conv_tiled_index(t, o, i, co, ci)] = h;
+    wt16t[conv_tiled_index(26 - t, i, o, ci, co)] = h;
   }
 }
 
@@ -394,7 +430,7 @@ __global__ void k_weights_bf16(const float* __restrict__ w, int co, int ci, uint
 // 16-channel dPre (channel 0).
 __global__ void k_anorm_grad(const double* __restrict__ r, const double* __restrict__ az,
                              const uint8_t* __restrict__ m, int64_t n, const DevScratch* __restrict__ S, double* red,
-                             uint16_t* __restrict__ g16) {
+                             uint16_t* __restrict__ g16, int64_t ps) {
   const double zr = S->scalars[10], zaz = S->scalars[11], er = S->scalars[12];
   const bool ok = zaz > 0 && er > 0;
   const double c1 = ok ? -1 / sqrt(zaz * er) : 0.0, c2 = ok ? zr / zaz : 0.0;
@@ -402,9 +438,8 @@ __global__ void k_anorm_grad(const double* __restrict__ r, const double* __restr
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     uint16_t v[16] = {0};
     if (m[c]) v[0] = f2bf((float)(c1 * (r[c] - c2 * az[c])));
-    uint4* dst = reinterpret_cast<uint4*>(g16 + c * 16);
-    dst[0] = *reinterpret_cast<uint4*>(&v[0]);
-    dst[1] = *reinterpret_cast<uint4*>(&v[8]);
+    *reinterpret_cast<uint4*>(g16 + c * 8) = *reinterpret_cast<uint4*>(&v[0]);
+    *reinterpret_cast<uint4*>(g16 + ps + c * 8) = *reinterpret_cast<uint4*>(&v[8]);
   }
 }
 
@@ -441,7 +476,7 @@ static void unet_free(xf_unet* u) {
   for (int l = 1; l < 3; l++)
     if (u->L[l].mask) cudaFree(u->L[l].mask);
   for (Layer& y : u->ly) {
-    void* ps[] = {y.w, y.b, y.w16, y.wt16, y.gw, y.gb, y.mw, y.vw, y.mb, y.vb};
+    void* ps[] = {y.w, y.b, y.w16, y.wt16, y.w16t, y.wt16t, y.gw, y.gb, y.mw, y.vw, y.mb, y.vb};
     for (void* p : ps)
       if (p) cudaFree(p);
   }
@@ -519,7 +554,8 @@ extern "C" int xf_unet_create(const xf_grid* g, xf_unet** out) {
     float** fb[] = {&y.b, &y.gb, &y.mb, &y.vb};
     for (float** p : fb)
       if (!st && cudaMalloc(p, y.co * 4) != cudaSuccess) st = XF_ERR_NOMEM;
-    if (!st && (cudaMalloc(&y.w16, y.nw * 2) != cudaSuccess || cudaMalloc(&y.wt16, y.nw * 2) != cudaSuccess))
+    if (!st && (cudaMalloc(&y.w16, y.nw * 2) != cudaSuccess || cudaMalloc(&y.wt16, y.nw * 2) != cudaSuccess ||
+                cudaMalloc(&y.w16t, y.nw * 2) != cudaSuccess || cudaMalloc(&y.wt16t, y.nw * 2) != cudaSuccess))
       st = XF_ERR_NOMEM;
     if (!st) {
       cudaMemsetAsync(y.w, 0, y.nw * 4, ctx->stream); cudaMemsetAsync(y.gw, 0, y.nw * 4, ctx->stream);
@@ -527,6 +563,7 @@ extern "C" int xf_unet_create(const xf_grid* g, xf_unet** out) {
       cudaMemsetAsync(y.b, 0, y.co * 4, ctx->stream); cudaMemsetAsync(y.gb, 0, y.co * 4, ctx->stream);
       cudaMemsetAsync(y.mb, 0, y.co * 4, ctx->stream); cudaMemsetAsync(y.vb, 0, y.co * 4, ctx->stream);
       cudaMemsetAsync(y.w16, 0, y.nw * 2, ctx->stream); cudaMemsetAsync(y.wt16, 0, y.nw * 2, ctx->stream);
+      cudaMemsetAsync(y.w16t, 0, y.nw * 2, ctx->stream); cudaMemsetAsync(y.wt16t, 0, y.nw * 2, ctx->stream);
     }
   }
   if (!st && (cudaMalloc(&u->zout, u->L[0].n * 4) != cudaSuccess ||
@@ -598,7 +635,7 @@ static int params_io(xf_unet* u, float* host, int which, bool upload) {
       XF_CUDA(ctx, cudaMemcpy(w, hw.data(), y.nw * 4, cudaMemcpyHostToDevice));
       XF_CUDA(ctx, cudaMemcpy(b, hb.data(), y.co * 4, cudaMemcpyHostToDevice));
       if (which == 0)
-        k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, ctx->stream>>>(y.w, y.co, y.ci, y.w16, y.wt16);
+        k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, ctx->stream>>>(y.w, y.co, y.ci, y.w16, y.wt16, y.w16t, y.wt16t);
     } else {
       XF_CUDA(ctx, cudaMemcpy(host + o, w, y.nw * 4, cudaMemcpyDeviceToHost));
       XF_CUDA(ctx, cudaMemcpy(host + o + y.nw, b, y.co * 4, cudaMemcpyDeviceToHost));
@@ -631,30 +668,33 @@ extern "C" int xf_unet_get_grads(xf_unet* u, float* host) {
 // ---------------------------------------------------------------------------
 // Forward pass on the residual box r (FP64, the grid's layout); the output
 // (FP32, level-0 box) lands in u->zout.
-static int conv(xf_unet* u, int k, const Act& in, int in_off, void* out, int out_ld, int out_ch, int out_fp32) {
+// `in` from channel in_c0 on; `out` a plane-0 pointer with plane stride
+// out_pitch (BF16), or FP32 rows of pitch out_pitch.
+static int conv(xf_unet* u, int k, const Act& in, int in_c0, void* out, int64_t out_pitch, int out_ch, int out_fp32) {
   const Layer& y = u->ly[k];
   const Level& L = u->L[LLEV[k]];
-  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, in.p0(u->L) + in_off, in.C, y.ci, y.w16, y.b, y.co, L.mask, out,
-                        out_ld, out_ch, out_fp32, LRELU[k], nullptr, 0);
+  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, in.ch(u->L, in_c0), in.ps(), y.ci, y.w16, y.w16t, y.b, y.co, L.mask,
+                        out, out_pitch, out_ch, out_fp32, LRELU[k], nullptr, 0);
 }
 // Input gradient of layer k from its pre-activation gradient g: the convolution
 // with the flipped transposed weights, x mask, x the ReLU gate of `gate` (the
 // input activation) when given.
-static int dgrad(xf_unet* u, int k, const Act& g, void* out, int out_ld, const Act* gate, int gate_off) {
+static int dgrad(xf_unet* u, int k, const Act& g, const Act& out, int out_c0, const Act* gate, int gate_c0) {
   const Layer& y = u->ly[k];
   const Level& L = u->L[LLEV[k]];
-  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, g.p0(u->L), g.C, y.co, y.wt16, nullptr, y.ci, L.mask, out, out_ld,
-                        y.ci, 0, 0, gate ? (const void*)(gate->p0(u->L) + gate_off) : nullptr, gate ? gate->C : 0);
+  return xf_conv_launch(u->ctx, L.n1, L.n2, L.n3, g.p0(u->L), g.ps(), y.co, y.wt16, y.wt16t, nullptr, y.ci, L.mask,
+                        out.ch(u->L, out_c0), out.ps(), y.ci, 0, 0,
+                        gate ? (const void*)gate->ch(u->L, gate_c0) : nullptr, gate ? gate->ps() : 0);
 }
-static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_off) {
+static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_c0) {
   const Layer& y = u->ly[k];
   const Level& L = u->L[LLEV[k]];
   const int64_t chunk = wg_chunk(L.n);
   const int nchunk = (int)((L.n + chunk - 1) / chunk);
   dim3 grid((unsigned)nchunk, 27);
   const size_t smem = (size_t)WG_CELLS * (y.co + y.ci) * 4;
-  k_wgrad<<<grid, 256, smem, u->ctx->stream>>>(g.p0(u->L), g.C, x.p0(u->L) + x_off, x.C, y.ci, y.co, L.n2, L.n3, L.n,
-                                                 (int)chunk, u->wpart, u->bpart);
+  k_wgrad<<<grid, 256, smem, u->ctx->stream>>>(g.p0(u->L), g.ps(), x.ch(u->L, x_c0), x.ps(), y.ci, y.co, L.n2, L.n3,
+                                                 L.n, (int)chunk, u->wpart, u->bpart);
   const int64_t nw = (int64_t)27 * y.co * y.ci;
   k_wgrad_sum<<<(unsigned)((nw + 255) / 256), 256, 0, u->ctx->stream>>>(u->wpart, u->bpart, nchunk, nw, y.co, y.gw,
                                                                         y.gb);
@@ -670,25 +710,25 @@ static int forward(xf_unet* u, const double* r) {
   XF_CUDA(ctx, cudaMemsetAsync(u->red, 0, 8 * 8, s));
   k_sumsq<<<sumsq_blocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, 0, u->rpart, u->rtick);
   k_unet_input<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, L[0].mask, L[0].n, u->red, (double)L[0].active,
-                                                    u->X0.p0(L));
-  if ((st = conv(u, ENC0A, u->X0, 0, u->A0.p0(L), 16, 16, 0))) return st;
-  if ((st = conv(u, ENC0B, u->A0, 0, u->CAT0.p0(L) + 32, 48, 16, 0))) return st;   // S0
-  k_pool<<<ublocks(ctx, L[1].n * 16), 256, 0, s>>>(u->CAT0.p0(L) + 32, 48, L[0].n2, L[0].n3, u->P1.p0(L), 16,
-                                                   L[1].mask, L[1].n1, L[1].n2, L[1].n3, 16);
-  if ((st = conv(u, ENC1A, u->P1, 0, u->A1.p0(L), 32, 32, 0))) return st;
-  if ((st = conv(u, ENC1B, u->A1, 0, u->CAT1.p0(L) + 64, 96, 32, 0))) return st;   // S1
-  k_pool<<<ublocks(ctx, L[2].n * 32), 256, 0, s>>>(u->CAT1.p0(L) + 64, 96, L[1].n2, L[1].n3, u->P2.p0(L), 32,
-                                                   L[2].mask, L[2].n1, L[2].n2, L[2].n3, 32);
-  if ((st = conv(u, MIDA, u->P2, 0, u->M2a.p0(L), 64, 64, 0))) return st;
-  if ((st = conv(u, MIDB, u->M2a, 0, u->M2b.p0(L), 64, 64, 0))) return st;
-  k_upsample<<<ublocks(ctx, L[1].n * 8), 256, 0, s>>>(u->M2b.p0(L), 64, L[2].n2, L[2].n3, u->CAT1.p0(L), 96,
-                                                       L[1].mask, L[1].n1, L[1].n2, L[1].n3, 64);
-  if ((st = conv(u, DEC1A, u->CAT1, 0, u->D1a.p0(L), 32, 32, 0))) return st;
-  if ((st = conv(u, DEC1B, u->D1a, 0, u->D1b.p0(L), 32, 32, 0))) return st;
-  k_upsample<<<ublocks(ctx, L[0].n * 4), 256, 0, s>>>(u->D1b.p0(L), 32, L[1].n2, L[1].n3, u->CAT0.p0(L), 48,
-                                                       L[0].mask, L[0].n1, L[0].n2, L[0].n3, 32);
-  if ((st = conv(u, DEC0A, u->CAT0, 0, u->D0a.p0(L), 16, 16, 0))) return st;
-  if ((st = conv(u, DEC0B, u->D0a, 0, u->D0b.p0(L), 16, 16, 0))) return st;
+                                                    u->X0.p0(L), u->X0.ps());
+  if ((st = conv(u, ENC0A, u->X0, 0, u->A0.p0(L), u->A0.ps(), 16, 0))) return st;
+  if ((st = conv(u, ENC0B, u->A0, 0, u->CAT0.ch(L, 32), u->CAT0.ps(), 16, 0))) return st;   // S0
+  k_pool<<<ublocks(ctx, L[1].n * 2), 256, 0, s>>>(u->CAT0.ch(L, 32), u->CAT0.ps(), L[0].n2, L[0].n3, u->P1.p0(L),
+                                                  u->P1.ps(), L[1].mask, L[1].n1, L[1].n2, L[1].n3, 16);
+  if ((st = conv(u, ENC1A, u->P1, 0, u->A1.p0(L), u->A1.ps(), 32, 0))) return st;
+  if ((st = conv(u, ENC1B, u->A1, 0, u->CAT1.ch(L, 64), u->CAT1.ps(), 32, 0))) return st;   // S1
+  k_pool<<<ublocks(ctx, L[2].n * 4), 256, 0, s>>>(u->CAT1.ch(L, 64), u->CAT1.ps(), L[1].n2, L[1].n3, u->P2.p0(L),
+                                                  u->P2.ps(), L[2].mask, L[2].n1, L[2].n2, L[2].n3, 32);
+  if ((st = conv(u, MIDA, u->P2, 0, u->M2a.p0(L), u->M2a.ps(), 64, 0))) return st;
+  if ((st = conv(u, MIDB, u->M2a, 0, u->M2b.p0(L), u->M2b.ps(), 64, 0))) return st;
+  k_upsample<<<ublocks(ctx, L[1].n * 8), 256, 0, s>>>(u->M2b.p0(L), u->M2b.ps(), L[2].n2, L[2].n3, u->CAT1.p0(L),
+                                                       u->CAT1.ps(), L[1].mask, L[1].n1, L[1].n2, L[1].n3, 64);
+  if ((st = conv(u, DEC1A, u->CAT1, 0, u->D1a.p0(L), u->D1a.ps(), 32, 0))) return st;
+  if ((st = conv(u, DEC1B, u->D1a, 0, u->D1b.p0(L), u->D1b.ps(), 32, 0))) return st;
+  k_upsample<<<ublocks(ctx, L[0].n * 4), 256, 0, s>>>(u->D1b.p0(L), u->D1b.ps(), L[1].n2, L[1].n3, u->CAT0.p0(L),
+                                                       u->CAT0.ps(), L[0].mask, L[0].n1, L[0].n2, L[0].n3, 32);
+  if ((st = conv(u, DEC0A, u->CAT0, 0, u->D0a.p0(L), u->D0a.ps(), 16, 0))) return st;
+  if ((st = conv(u, DEC0B, u->D0a, 0, u->D0b.p0(L), u->D0b.ps(), 16, 0))) return st;
   if ((st = conv(u, OUTL, u->D0b, 0, u->zout, 1, 1, 1))) return st;
   XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
@@ -710,50 +750,52 @@ static int backward(xf_unet* u, const double* r, const double* e, const xf_op* o
     xf_dot_async(u->g, XF_F64, u->zd, u->az, 11);
     xf_dot_async(u->g, XF_F64, e, r, 12);
     k_anorm_grad<<<ublocks(ctx, L[0].n), 256, 0, s>>>(r, u->az, L[0].mask, L[0].n, ctx->scratch, u->red,
-                                                      u->G0_16a.p0(L));
+                                                      u->G0_16a.p0(L), u->G0_16a.ps());
   } else {
     k_sumsq<<<sumsq_blocks(ctx, L[0].n), 256, 0, s>>>(e, L[0].mask, L[0].n, u->red, 1, u->rpart, u->rtick);
     k_unet_loss<<<ublocks(ctx, L[0].n), 256, 0, s>>>(u->zout, e, L[0].mask, L[0].n, (double)L[0].active, u->red,
-                                                     u->G0_16a.p0(L));
+                                                     u->G0_16a.p0(L), u->G0_16a.ps());
   }
   // out, dec0b, dec0a
   wgrad(u, OUTL, u->G0_16a, u->D0b, 0);
-  if ((st = dgrad(u, OUTL, u->G0_16a, u->G0_16b.p0(L), 16, &u->D0b, 0))) return st;
+  if ((st = dgrad(u, OUTL, u->G0_16a, u->G0_16b, 0, &u->D0b, 0))) return st;
   wgrad(u, DEC0B, u->G0_16b, u->D0a, 0);
-  if ((st = dgrad(u, DEC0B, u->G0_16b, u->G0_16a.p0(L), 16, &u->D0a, 0))) return st;
+  if ((st = dgrad(u, DEC0B, u->G0_16b, u->G0_16a, 0, &u->D0a, 0))) return st;
   wgrad(u, DEC0A, u->G0_16a, u->CAT0, 0);
-  if ((st = dgrad(u, DEC0A, u->G0_16a, u->G0_48.p0(L), 48, nullptr, 0))) return st;
+  if ((st = dgrad(u, DEC0A, u->G0_16a, u->G0_48, 0, nullptr, 0))) return st;
   // up(D1b) part -> dec1b's pre-activation gradient
-  k_upsample_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G0_48.p0(L), 48, L[0].n2, L[0].n3, u->D1b.p0(L), 32,
-                                                           L[1].mask, L[1].n1, L[1].n2, L[1].n3, u->G1_32a.p0(L), 32,
-                                                           32);
+  k_upsample_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G0_48.p0(L), u->G0_48.ps(), L[0].n2, L[0].n3,
+                                                           u->D1b.p0(L), u->D1b.ps(), L[1].mask, L[1].n1, L[1].n2,
+                                                           L[1].n3, u->G1_32a.p0(L), u->G1_32a.ps(), 32);
   wgrad(u, DEC1B, u->G1_32a, u->D1a, 0);
-  if ((st = dgrad(u, DEC1B, u->G1_32a, u->G1_32b.p0(L), 32, &u->D1a, 0))) return st;
+  if ((st = dgrad(u, DEC1B, u->G1_32a, u->G1_32b, 0, &u->D1a, 0))) return st;
   wgrad(u, DEC1A, u->G1_32b, u->CAT1, 0);
-  if ((st = dgrad(u, DEC1A, u->G1_32b, u->G1_96.p0(L), 96, nullptr, 0))) return st;
+  if ((st = dgrad(u, DEC1A, u->G1_32b, u->G1_96, 0, nullptr, 0))) return st;
   // up(M2b) part -> mid_b
-  k_upsample_bwd<<<ublocks(ctx, L[2].n * 64), 256, 0, s>>>(u->G1_96.p0(L), 96, L[1].n2, L[1].n3, u->M2b.p0(L), 64,
-                                                           L[2].mask, L[2].n1, L[2].n2, L[2].n3, u->G2_64a.p0(L), 64,
-                                                           64);
+  k_upsample_bwd<<<ublocks(ctx, L[2].n * 64), 256, 0, s>>>(u->G1_96.p0(L), u->G1_96.ps(), L[1].n2, L[1].n3,
+                                                           u->M2b.p0(L), u->M2b.ps(), L[2].mask, L[2].n1, L[2].n2,
+                                                           L[2].n3, u->G2_64a.p0(L), u->G2_64a.ps(), 64);
   wgrad(u, MIDB, u->G2_64a, u->M2a, 0);
-  if ((st = dgrad(u, MIDB, u->G2_64a, u->G2_64b.p0(L), 64, &u->M2a, 0))) return st;
+  if ((st = dgrad(u, MIDB, u->G2_64a, u->G2_64b, 0, &u->M2a, 0))) return st;
   wgrad(u, MIDA, u->G2_64b, u->P2, 0);
-  if ((st = dgrad(u, MIDA, u->G2_64b, u->G2_32.p0(L), 32, nullptr, 0))) return st;
-  k_pool_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G2_32.p0(L), 32, L[2].n2, L[2].n3, L[1].mask, L[1].n1,
-                                                       L[1].n2, L[1].n3, u->gsum1, 32, 32);
+  if ((st = dgrad(u, MIDA, u->G2_64b, u->G2_32, 0, nullptr, 0))) return st;
+  k_pool_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G2_32.p0(L), u->G2_32.ps(), L[2].n2, L[2].n3, L[1].mask,
+                                                       L[1].n1, L[1].n2, L[1].n3, u->gsum1, 32, 32);
   // S1 = enc1b output: skip gradient + pooled path
-  k_skip_grad<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G1_96.p0(L) + 64, 96, u->gsum1, 32, u->CAT1.p0(L) + 64,
-                                                        96, L[1].mask, L[1].n, u->G1_32a.p0(L), 32, 32);
+  k_skip_grad<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G1_96.ch(L, 64), u->G1_96.ps(), u->gsum1, 32,
+                                                        u->CAT1.ch(L, 64), u->CAT1.ps(), L[1].mask, L[1].n,
+                                                        u->G1_32a.p0(L), u->G1_32a.ps(), 32);
   wgrad(u, ENC1B, u->G1_32a, u->A1, 0);
-  if ((st = dgrad(u, ENC1B, u->G1_32a, u->G1_32b.p0(L), 32, &u->A1, 0))) return st;
+  if ((st = dgrad(u, ENC1B, u->G1_32a, u->G1_32b, 0, &u->A1, 0))) return st;
   wgrad(u, ENC1A, u->G1_32b, u->P1, 0);
-  if ((st = dgrad(u, ENC1A, u->G1_32b, u->G1_16.p0(L), 16, nullptr, 0))) return st;
-  k_pool_bwd<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G1_16.p0(L), 16, L[1].n2, L[1].n3, L[0].mask, L[0].n1,
-                                                       L[0].n2, L[0].n3, u->gsum, 16, 16);
-  k_skip_grad<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G0_48.p0(L) + 32, 48, u->gsum, 16, u->CAT0.p0(L) + 32,
-                                                        48, L[0].mask, L[0].n, u->G0_16a.p0(L), 16, 16);
+  if ((st = dgrad(u, ENC1A, u->G1_32b, u->G1_16, 0, nullptr, 0))) return st;
+  k_pool_bwd<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G1_16.p0(L), u->G1_16.ps(), L[1].n2, L[1].n3, L[0].mask,
+                                                       L[0].n1, L[0].n2, L[0].n3, u->gsum, 16, 16);
+  k_skip_grad<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G0_48.ch(L, 32), u->G0_48.ps(), u->gsum, 16,
+                                                        u->CAT0.ch(L, 32), u->CAT0.ps(), L[0].mask, L[0].n,
+                                                        u->G0_16a.p0(L), u->G0_16a.ps(), 16);
   wgrad(u, ENC0B, u->G0_16a, u->A0, 0);
-  if ((st = dgrad(u, ENC0B, u->G0_16a, u->G0_16b.p0(L), 16, &u->A0, 0))) return st;
+  if ((st = dgrad(u, ENC0B, u->G0_16a, u->G0_16b, 0, &u->A0, 0))) return st;
   wgrad(u, ENC0A, u->G0_16b, u->X0, 0);
   XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
@@ -807,7 +849,7 @@ extern "C" int xf_unet_train_step(xf_unet* u, const xf_op* op, const xf_vec* r, 
     for (Layer& y : u->ly) {
       k_adam<<<ublocks(ctx, y.nw), 256, 0, s>>>(y.w, y.gw, y.mw, y.vw, y.nw, (float)lr, b1, b2, 1e-8f, c1, c2, 0);
       k_adam<<<1, 256, 0, s>>>(y.b, y.gb, y.mb, y.vb, y.co, (float)lr, b1, b2, 1e-8f, c1, c2, 0);
-      k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, s>>>(y.w, y.co, y.ci, y.w16, y.wt16);
+      k_weights_bf16<<<ublocks(ctx, y.nw), 256, 0, s>>>(y.w, y.co, y.ci, y.w16, y.wt16, y.w16t, y.wt16t);
     }
   }
   XF_CUDA(ctx, cudaGetLastError());
