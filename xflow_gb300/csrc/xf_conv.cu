@@ -289,8 +289,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
 // accumulates D_dk over the nine slabs and the input chunks, and the epilogue
 // applies the k shift on the output side:
 //     y[c0 + r - 1] = D_-1[r - 1] + D_0[r] + D_+1[r + 1],   r = 1 .. 126,
-// neighbouring TMEM rows coming from the neighbouring lanes (warp shuffles; a
-// shared-memory exchange across warps).  A tile therefore yields 126 cells;
+// neighbouring TMEM rows coming from the neighbouring lanes (warp shuffles;
+// across warps, the edge rows through shared memory as 16-byte stores by
+// lanes 31 and 0 and 16-byte loads by every lane: scalar single-lane
+// exchanges cost about three times as long).  A tile therefore yields 126 cells;
 // the last tile starts at ncell - 126 (its overlap rewrites identical values).
 //
 // A pipeline stage is one (tile, 16-channel input chunk): for each of the
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(BK_THREADS) k_conv3_bulk(ConvArgs a, BkPlan pl
   __shared__ uint64_t full[BK_MAX_STAGES], empty[BK_MAX_STAGES], tfull[2], tempty[2], wfull, mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ float xch[2][4][2][80];   // per tile parity and warp: lane 31's D_-1 row, lane 0's D_+1 row
+  __shared__ __align__(16) float xch[2][4][2][80];   // per tile parity and warp: lane 31's D_-1 row, lane 0's D_+1 row
   const int Ci = a.Ci, Co = a.Co, N3 = 3 * Co, nk = Ci / 16;
   const int S = plan.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -539,39 +541,49 @@ __global__ void __launch_bounds__(BK_THREADS) k_conv3_bulk(ConvArgs a, BkPlan pl
       const int64_t c0 = tile_start(k);
       const uint32_t trow = tbase + (uint32_t)(acc * plan.acc_off) + ((uint32_t)(warp * 32) << 16);
       float(*xc)[2][80] = xch[acc];
-      // pass 1: rows at the warp edges for the neighbouring warps
-      for (int co = 0; co < Co; co += 8) {
-        uint32_t dm[8], dp[8];
-        tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
-        tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
-        tc::tmem_wait_ld(dm, dp);
-        if (lane == 31)
-          for (int q = 0; q < 8; q++) xc[warp][0][co + q] = __uint_as_float(dm[q]);
-        if (lane == 0)
-          for (int q = 0; q < 8; q++) xc[warp][1][co + q] = __uint_as_float(dp[q]);
-      }
-      epi_sync();
       const int r = warp * 32 + lane;
       const int64_t c = c0 + r - 1;
       const bool live = r >= 1 && r <= 126 && c < a.ncell;
       const float m = live ? (float)a.mask[c] : 0.f;
-      for (int co = 0; co < Co; co += 8) {
-        uint32_t dm[8], d0[8], dp[8];
-        tc::tmem_ld8_nowait(trow + (uint32_t)co, dm);
-        tc::tmem_ld8_nowait(trow + (uint32_t)(Co + co), d0);
-        tc::tmem_ld8_nowait(trow + (uint32_t)(2 * Co + co), dp);
+      // the neighbour row a lane needs from another warp: lane 0 warp-1's
+      // D_-1 edge, lane 31 warp+1's D_+1 edge (others read one and discard it)
+      const float* nbr = lane == 0 ? xc[warp > 0 ? warp - 1 : 0][0] : xc[warp < 3 ? warp + 1 : 3][1];
+      const bool has_nbr = lane == 0 ? warp > 0 : warp < 3;
+      // 16 output channels at a time: D_-1, D_0 and D_+1 columns in three
+      // loads under one wait
+      for (int co = 0; co < Co; co += 16) {
+        uint32_t dm[16], d0[16], dp[16];
+        tc::tmem_ld16_nowait(trow + (uint32_t)co, dm);
+        tc::tmem_ld16_nowait(trow + (uint32_t)(Co + co), d0);
+        tc::tmem_ld16_nowait(trow + (uint32_t)(2 * Co + co), dp);
         tc::tmem_wait_ld(dm, d0, dp);
-        float v[8];
+        if (lane == 31 || lane == 0) {
+          const uint32_t* e = lane == 31 ? dm : dp;
+          float4* dst = reinterpret_cast<float4*>(&xc[warp][lane == 31 ? 0 : 1][co]);
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
+          for (int j = 0; j < 4; j++)
+            dst[j] = make_float4(__uint_as_float(e[4 * j]), __uint_as_float(e[4 * j + 1]),
+                                 __uint_as_float(e[4 * j + 2]), __uint_as_float(e[4 * j + 3]));
+        }
+        epi_sync();
+        float nb[16];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float4 w4 = reinterpret_cast<const float4*>(nbr + co)[j];
+          nb[4 * j] = w4.x; nb[4 * j + 1] = w4.y; nb[4 * j + 2] = w4.z; nb[4 * j + 3] = w4.w;
+        }
+        float v[2][8];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
           float prev = __shfl_up_sync(0xffffffffu, __uint_as_float(dm[q]), 1);
           float next = __shfl_down_sync(0xffffffffu, __uint_as_float(dp[q]), 1);
-          if (lane == 0) prev = warp > 0 ? xc[warp - 1][0][co + q] : 0.f;
-          if (lane == 31) next = warp < 3 ? xc[warp + 1][1][co + q] : 0.f;
-          v[q] = prev + __uint_as_float(d0[q]) + next;
+          const float e = has_nbr ? nb[q] : 0.f;
+          if (lane == 0) prev = e;
+          if (lane == 31) next = e;
+          v[q >> 3][q & 7] = prev + __uint_as_float(d0[q]) + next;
         }
-        if (!live || co >= a.out_ch) continue;
-        conv_store8(a, c, co, m, v);
+        if (live && co < a.out_ch) conv_store8(a, c, co, m, v[0]);
+        if (live && co + 8 < a.out_ch) conv_store8(a, c, co + 8, m, v[1]);
       }
       // the accumulator is read: the MMA issuer may overwrite it two tiles on
       tc::fence_before_sync();
