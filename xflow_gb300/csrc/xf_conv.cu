@@ -302,9 +302,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
 // memory when they fit beside two stages, else each stage also carries its
 // chunk's nine B blocks.  Each control step therefore covers nine MMAs.
 // The CTA is persistent and warp-specialised:
-//   warp 4, one thread: issues each stage's copies into a ring (full
-//       barrier: the copies' transaction bytes; empty barrier: the MMAs
-//       that read the stage have completed);
+//   warp 4: issues each stage's copies into a ring, one copy per lane (one
+//       thread issuing all of them was the pipeline's bottleneck), lane 0
+//       keeping the barriers (full: the copies' transaction bytes; empty: the MMAs that
+//       read the stage have completed);
 //   warp 5, one thread: the MMAs into one of two TMEM accumulators (the
 //       epilogue of a tile overlaps the next tile's MMAs), a commit per
 //       stage and one per finished tile;
@@ -451,42 +452,45 @@ __global__ void __launch_bounds__(BK_THREADS) k_conv3_bulk(ConvArgs a, BkPlan pl
     return st + 126 > a.ncell ? (a.ncell > 126 ? a.ncell - 126 : (int64_t)0) : st;
   };
 
-  if (warp == 4) {
-    if (lane == 0) {   // ---- producer
-      if (plan.resident && my_tiles > 0) {
-        mbar_expect_tx(&wfull, plan.w_bytes);
-        bulk_load(wsm, a.Wt, plan.w_bytes, &wfull);
-      }
-      int st = 0, pass = 0, issued = 0;
-      bool ok = true;
-      for (int k = 0; k < my_tiles && ok; k++) {
-        const int64_t row_base = tile_start(k) - 1;
-        for (int c = 0; c < nk; c++) {
-          if (pass > 0 && !bk_wait(&empty[st], (uint32_t)((pass - 1) & 1), abort_p)) {
+  if (warp == 4) {   // ---- producer: lane 0 takes the barriers, lanes 0..17 one A copy each
+    if (plan.resident && my_tiles > 0 && lane == 0) {
+      mbar_expect_tx(&wfull, plan.w_bytes);
+      bulk_load(wsm, a.Wt, plan.w_bytes, &wfull);
+    }
+    // this lane's copy: slab sl = lane / 2, plane q = lane % 2 (lane 18: the
+    // streamed weights)
+    const int sl = lane >> 1, q = lane & 1;
+    const int64_t slab_off = (sl / 3 - 1) * P + (sl % 3 - 1) * (int64_t)a.n3;
+    int st = 0, pass = 0, issued = 0;
+    bool ok = true;
+    for (int k = 0; k < my_tiles && ok; k++) {
+      const int64_t row_base = tile_start(k) - 1;
+      for (int c = 0; c < nk; c++) {
+        if (pass > 0) {
+          bool w = true;
+          if (lane == 0) w = bk_wait(&empty[st], (uint32_t)((pass - 1) & 1), abort_p);
+          if (!__shfl_sync(0xffffffffu, w, 0)) {
             ok = false;
             break;
           }
-          uint8_t* sa = stg + st * plan.stage_bytes;
-          mbar_expect_tx(&full[st], BK_A + (plan.resident ? 0u : plan.b_bytes));
-          const uint16_t* src0 = a.in + (2 * c) * a.in_ps;
-          const uint16_t* src1 = src0 + a.in_ps;
-#pragma unroll 1
-          for (int sl = 0; sl < 9; sl++) {
-            const int di = sl / 3 - 1, dj = sl % 3 - 1;
-            const int64_t row0 = row_base + di * P + dj * (int64_t)a.n3;
-            bulk_load(sa + sl * BK_SLAB, src0 + row0 * 8, 2048, &full[st]);
-            bulk_load(sa + sl * BK_SLAB + 2048, src1 + row0 * 8, 2048, &full[st]);
-          }
-          if (!plan.resident) bulk_load(sa + BK_A, a.Wt + (int64_t)c * 9 * N3 * 16, plan.b_bytes, &full[st]);
-          issued++;
-          if (++st == S) {
-            st = 0;
-            pass++;
-          }
+        }
+        uint8_t* sa = stg + st * plan.stage_bytes;
+        if (lane == 0) mbar_expect_tx(&full[st], BK_A + (plan.resident ? 0u : plan.b_bytes));
+        if (lane < 18)
+          bulk_load(sa + sl * BK_SLAB + q * 2048, a.in + (2 * c + q) * a.in_ps + (row_base + slab_off) * 8, 2048,
+                    &full[st]);
+        else if (lane == 18 && !plan.resident)
+          bulk_load(sa + BK_A, a.Wt + (int64_t)c * 9 * N3 * 16, plan.b_bytes, &full[st]);
+        issued++;
+        if (++st == S) {
+          st = 0;
+          pass++;
         }
       }
-      // every copy issued has landed before the CTA may leave: the last
-      // phase of each stage used, and the weights
+    }
+    // every copy issued has landed before the CTA may leave: the last phase
+    // of each stage used, and the weights
+    if (lane == 0) {
       for (int s = 0; s < S; s++) {
         const int n = issued / S + (s < issued % S ? 1 : 0);   // uses of stage s
         if (n > 0) bk_wait(&full[s], (uint32_t)((n - 1) & 1), abort_p, false);
