@@ -722,6 +722,99 @@ void xf_cg_q32(const xf_op* op, const float* p, float* q) {
 void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot) {
   launch_cg_q<float, false>(op, p, q, nullptr, nullptr, slot, CTL_NONE);
 }
+
+// The coarse correction of the learned two-level preconditioner, prolongated
+// and multiplied by A in one pass: y = P zc (the value of the cell's
+// 4 x 4 x 4 block, 0 on inactive cells), q = A y and (y, q) -> scalars[slot].
+// zc is the network's FP32 output (its FP64 copy is an exact widening, and a
+// conversion from FP64 per fine cell would run on the FP64 pipe, 1/58 of the
+// FP32 rate here).  Every value y takes at a stencil point is a coarse value
+// (0 behind a closed face), and the row is k_cg_q2u's expression with
+// k_cg_q2u's thread mapping and accumulation order, so y, q and (y, q) are bit
+// for bit those of the prolongation followed by xf_cg_q32_dot.  Uniform
+// Laplace grids without boundary rows, n3 even.
+__global__ void __launch_bounds__(CGK_THREADS, 4) k_tl_prolong_ay(CgqArgs<float> a, const float* __restrict__ zc,
+                                                                  int c2, int c3, float* __restrict__ yout,
+                                                                  float cx, float cy, float cz) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  __shared__ float dtab[64];
+  DevScratch* S = a.S;
+  if (S->iscalars[I_DONE] || S->iscalars[I_PAUSE]) return;
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x;
+    dtab[b] = cx * (float)(((b >> 0) & 1) + ((b >> 1) & 1)) + cy * (float)(((b >> 2) & 1) + ((b >> 3) & 1)) +
+              cz * (float)(((b >> 4) & 1) + ((b >> 5) & 1));
+  }
+  __syncthreads();
+  const StencilGrid<float>& g = a.g;
+  const int n1 = g.n1, n3 = g.n3;
+  const int P = g.n2 * n3;
+  const int p0 = 2 * (blockIdx.x * CGK_THREADS + threadIdx.x);
+  const int i0 = blockIdx.y * a.chunk, i1 = min(n1, i0 + a.chunk);
+  DotAcc<float> acc;
+  if (p0 < P) {
+    const int j = p0 / n3, k0 = p0 - j * n3;
+    // coarse index of a fine cell's block (interior cells only)
+    auto blk = [&](int i, int jj, int k) -> int64_t {
+      return ((int64_t)(1 + ((i - 1) >> 2)) * c2 + (1 + ((jj - 1) >> 2))) * c3 + (1 + ((k - 1) >> 2));
+    };
+    auto cv = [&](int64_t b) -> float { return __ldg(zc + b); };
+    for (int i = i0; i < i1; i++) {
+      const int c = i * P + p0;
+      const uchar2 kk = __ldg(reinterpret_cast<const uchar2*>(g.kind + c));
+      const uint8_t kbs[2] = {kk.x, kk.y};
+      float yv[2], out[2];
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        const uint8_t kb = kbs[t];
+        const int k = k0 + t;
+        if (row_of(kb) == ROW_NONE) {
+          yv[t] = 0.f;
+          out[t] = 0.f;
+          continue;
+        }
+        const int64_t bc = blk(i, j, k);
+        const float yc = cv(bc);
+        // a neighbour's value: its block's (the own block's unless across a block face), 0 behind a closed face
+        auto nb = [&](uint8_t bit, int ii, int jj, int kz) -> float {
+          if (!(kb & bit)) return 0.f;
+          const int64_t bn = blk(ii, jj, kz);
+          return bn == bc ? yc : cv(bn);
+        };
+        const float ypx = nb(K_PX, i + 1, j, k), ymx = nb(K_MX, i - 1, j, k);
+        const float ypy = nb(K_PY, i, j + 1, k), ymy = nb(K_MY, i, j - 1, k);
+        const float ypz = nb(K_PZ, i, j, k + 1), ymz = nb(K_MZ, i, j, k - 1);
+        yv[t] = yc;
+        out[t] = fmaf(dtab[kb & 63], yc, -fmaf(cx, ypx + ymx, fmaf(cy, ypy + ymy, cz * (ypz + ymz))));
+      }
+      acc.add(yv[0], out[0]);
+      acc.add(yv[1], out[1]);
+      *reinterpret_cast<float2*>(yout + c) = make_float2(yv[0], yv[1]);
+      *reinterpret_cast<float2*>(a.y + c) = make_float2(out[0], out[1]);
+    }
+  }
+  finish_cg_kernel<float, false>(S, a, acc, sh, &last);
+}
+
+bool xf_tl_prolong_ay_supported(const xf_grid* g) { return g->uniform && g->nbrow == 0 && g->n3 % 2 == 0; }
+
+void xf_tl_prolong_ay(const xf_op* op, const float* zc, int c2, int c3, float* y, float* ay, int slot) {
+  const xf_grid* g = op->g;
+  xf_ctx* ctx = g->ctx;
+  CgqArgs<float> a;
+  a.g = make_stencil_grid<float>(g, nullptr);
+  a.x = nullptr; a.y = ay; a.b = nullptr; a.y32 = nullptr; a.diag = g->diag; a.S = ctx->scratch; a.slot = slot;
+  a.ctl = CTL_NONE;
+  const int P = g->n2 * g->n3;
+  const int bx = (P / 2 + CGK_THREADS - 1) / CGK_THREADS;
+  int chunk = 16;
+  while ((int64_t)bx * ((g->n1 + chunk - 1) / chunk) > RED_MAX_BLOCKS) chunk *= 2;
+  a.chunk = chunk;
+  dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
+  k_tl_prolong_ay<<<grid, CGK_THREADS, 0, ctx->stream>>>(a, zc, c2, c3, y, (float)g->ucx, (float)g->ucy,
+                                                          (float)g->ucz);
+}
 // r32 = float(b - A x) in FP64, (r, r) -> scalars[slot + 1], then control `ctl`.
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl) {
   launch_cg_q<double, true>(op, x, nullptr, b, r32, slot, ctl);

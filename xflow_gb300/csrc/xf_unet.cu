@@ -30,6 +30,8 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int64_t 
                    int out_ch, int out_fp32, int relu, const void* gate, int64_t gate_ps);
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
 void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot);
+bool xf_tl_prolong_ay_supported(const xf_grid* g);
+void xf_tl_prolong_ay(const xf_op* op, const float* zc, int c2, int c3, float* y, float* ay, int slot);
 void xf_cg_res64(const xf_op* op, const double* x, const double* b, float* r32, int slot, int ctl);
 void xf_dot_async(const xf_grid* g, int dtype, const void* a, const void* b, int slot);
 int xf_op_ready(const xf_op* op);
@@ -1259,13 +1261,47 @@ __global__ void k_tl_alpha(const DevScratch* S, TlCtl* c, int hd, int m) {
   c->head = (hd + 1) % (m + 1);
   if (c->nwin < m) c->nwin++;
 }
-__global__ void k_tl_update(float* __restrict__ e, float* __restrict__ r, const float* __restrict__ p,
-                            const float* __restrict__ q, const TlCtl* c, int64_t n) {
+// e += alpha p, r -= alpha q and (r, r) into scalars[slot] in the same pass;
+// the grid, the thread mapping and the accumulation order are k_dot_f4's, so
+// (r, r) is bit for bit the separate dot's.
+__global__ void __launch_bounds__(RED_THREADS) k_tl_update(float* __restrict__ e, float* __restrict__ r,
+                                                           const float* __restrict__ p, const float* __restrict__ q,
+                                                           const TlCtl* c, int64_t n, DevScratch* S, int slot) {
+  __shared__ double sh[32];
+  __shared__ bool last;
   if (c->brk) return;
   const float alpha = (float)c->alpha;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+  DotAcc<float> acc;
+  const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
+  float4* e4 = reinterpret_cast<float4*>(e);
+  float4* r4 = reinterpret_cast<float4*>(r);
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  const float4* q4 = reinterpret_cast<const float4*>(q);
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n4; k += stride) {
+    float4 ev = e4[k], rv = r4[k];
+    const float4 pv = __ldg(p4 + k), qv = __ldg(q4 + k);
+    ev.x = fmaf(alpha, pv.x, ev.x); ev.y = fmaf(alpha, pv.y, ev.y);
+    ev.z = fmaf(alpha, pv.z, ev.z); ev.w = fmaf(alpha, pv.w, ev.w);
+    rv.x = fmaf(-alpha, qv.x, rv.x); rv.y = fmaf(-alpha, qv.y, rv.y);
+    rv.z = fmaf(-alpha, qv.z, rv.z); rv.w = fmaf(-alpha, qv.w, rv.w);
+    e4[k] = ev;
+    r4[k] = rv;
+    acc.add(rv.x, rv.x);
+    acc.add(rv.y, rv.y);
+    acc.add(rv.z, rv.z);
+    acc.add(rv.w, rv.w);
+  }
+  for (int64_t k = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += stride) {
     e[k] = fmaf(alpha, p[k], e[k]);
-    r[k] = fmaf(-alpha, q[k], r[k]);
+    const float rv = fmaf(-alpha, q[k], r[k]);
+    r[k] = rv;
+    acc.add(rv, rv);
+  }
+  if (!publish_acc<float>(S, slot, slot, acc, sh, &last)) return;
+  const double t = finish_partials(S, slot, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[slot] = t;
+    S->tickets[slot] = 0;
   }
 }
 // The last node of the loop body: see the loop guard above.
@@ -1446,12 +1482,16 @@ static int tl_graph_build(xf_op* op, xf_unet* u, int m, int F, const float (*tl_
       k_restrict_blocks<float><<<grid_blocks(ctx, nc, 256), 256, 0, s>>>(r, g->n2, g->n3, F, rc, cg->n1, cg->n2,
                                                                          cg->n3);
     if (ce == cudaSuccess && (rcode = xf_unet_apply_dev(u, rc, zc))) ce = cudaErrorUnknown;
-    if (F == 4)   // n2 n3 is a multiple of 4 (see k_prolong4v)
-      k_prolong4v<<<dim3((g->n2 * g->n3 / 4 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask, g->n1,
-                                                                              g->n2, g->n3, y);
-    else
-      k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
-    xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
+    if (F == 4 && xf_tl_prolong_ay_supported(g)) {   // y = P zc, A y and (y, A y) in one pass
+      xf_tl_prolong_ay(op, u->zout, cg->n2, cg->n3, y, ay, FS_YAY);   // the network's FP32 output
+    } else {
+      if (F == 4)   // n2 n3 is a multiple of 4 (see k_prolong4v)
+        k_prolong4v<<<dim3((g->n2 * g->n3 / 4 + 255) / 256, g->n1), 256, 0, s>>>(zc, cg->n2, cg->n3, g->smask,
+                                                                                g->n1, g->n2, g->n3, y);
+      else
+        k_prolong_blocks<float><<<eb, 256, 0, s>>>(zc, cg->n2, cg->n3, F, g->smask, g->n1, g->n2, g->n3, y);
+      xf_cg_q32_dot(op, y, ay, FS_YAY);           // A y, (y, A y)
+    }
     xf_dot_async(cg, XF_F64, zc, rc, FS_YR);   // (y, r) = (z_c, P^T r)
     {
       // the smoother: its first pass takes r - omega A y, its last writes
@@ -1467,7 +1507,7 @@ static int tl_graph_build(xf_op* op, xf_unet* u, int m, int F, const float (*tl_
     }
     win_dots(hd, 1);
     end_tail(unused);
-    n_on = 4 + UNET_FORWARD_LAUNCHES + tl_nf + (m - 1);
+    n_on = (F == 4 && xf_tl_prolong_ay_supported(g) ? 3 : 4) + UNET_FORWARD_LAUNCHES + tl_nf + (m - 1);
     // network off: z = r with its dots
     begin(ie[1], nullptr, 0);
     cudaMemcpyAsync(z, r, n * 4, cudaMemcpyDeviceToDevice, s);
@@ -1497,12 +1537,11 @@ static int tl_graph_build(xf_op* op, xf_unet* u, int m, int F, const float (*tl_
     xf_cg_q32_dot(op, pn, qn, FS_PQ);   // q = A p, (p, q)
     fdot(pn, r, FS_PR, nullptr);
     k_tl_alpha<<<1, 32, 0, s>>>(S, c, hd, m);
-    k_tl_update<<<eb, 256, 0, s>>>(e, r, pn, qn, c, n);
-    fdot(r, r, FS_RR, &c->brk);
+    k_tl_update<<<db, RED_THREADS, 0, s>>>(e, r, pn, qn, c, n, S, FS_RR);   // with (r, r)
     k_tl_rr<<<1, 32, 0, s>>>(S, c, H, hd, m);
     end_tail(unused);
-    // it, z-test, coef, m axpys, stencil + dot, alpha, update, rr, test, and the loop guard
-    n_iter = 3 + m + 2 + 1 + 1 + 1 + 1 + 1;
+    // it, z-test, coef, m axpys, stencil + dot, alpha, update with (r, r), test, and the loop guard
+    n_iter = 3 + m + 2 + 1 + 1 + 1 + 1;
   }
   // the loop guard, last in the body
   begin(wbody, &prev, 1);
