@@ -517,8 +517,12 @@ int xf_solve_fcg(xf_op* op, xf_unet* u, const xf_solve_opts* opts, xf_vec* x, co
  * first pass of the degree-4 preconditioner with the update fused in (r' =
  * r - alpha q, e += alpha p', w = p2(A) r', (r', r')) and [10] its second pass
  * (z = p1(A) w, (r', z)), or -1; [11] a middle pass of a higher degree (w' =
- * p_k(A) w, no dot), or -1.  ms_out holds 12 doubles.  Laplace operators
- * only. */
+ * p_k(A) w, no dot), or -1; the learned two-level preconditioner's passes
+ * on the fine grid (interiors multiples of 4, uniform, no boundary rows, else
+ * -1): [12] y = P zc with A y and (y, A y), [13] the smoother's first pass on
+ * r - omega A y, [14] its last pass (z = omega y + s p1(A) w, also into the
+ * direction slot, with (z, r) and (z, q)).  ms_out holds 15 doubles.  Laplace
+ * operators only. */
 int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out);
 
 /* No counterpart in the reference (a self-test).  The time-step passes divide

@@ -294,7 +294,7 @@ def solve(op, x, b, **kw):
 
 CG_KERNELS = ("stencil_f32", "xr_update_f32", "p_update_f32", "residual_f64", "stencil_f64", "pq_fused_f32",
               "pq_march_f32", "poly2_f32", "polyr_f32", "cheb_first_fused_f32", "cheb_last_f32",
-              "cheb_middle_f32")
+              "cheb_middle_f32", "tl_prolong_ay_f32", "tl_first_f32", "tl_last_f32")
 
 
 def selftest_division(ctx, n=1 << 24, seed=1):

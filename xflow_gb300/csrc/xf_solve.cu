@@ -37,6 +37,11 @@ void xf_cg_polyr_launch(const xf_op* op, const float* r, float* r_out, const flo
 void xf_cheb2_coeffs(double lmax, double ratio, float out[3]);
 bool xf_cheb4_factors(double lmax, double ratio, float f1[3], float f2[3]);
 bool xf_cheb_factors(double lmax, double ratio, int deg, float (*f)[3]);
+bool xf_tl_prolong_ay_supported(const xf_grid* g);
+void xf_tl_prolong_ay(const xf_op* op, const float* zc, int c2, int c3, float* y, float* ay, int slot);
+void xf_cg_poly_tl_launch(const xf_op* op, bool first, bool last, const float* in, const float* q, float* out,
+                          const float coeffs[3], int s_yay, int s_yr, const float* y, float tsc, float* z2,
+                          const float* r, const float* qw, int s_zr, int s_zq);
 void xf_cg_poly_first_launch(const xf_op* op, const float* r, float* w, const float coeffs[3], const float* q,
                              const float* pa, const float* pb, float* e, float* r_out);
 void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, float* z, const float coeffs[3]);
@@ -886,6 +891,27 @@ extern "C" int xf_profile_cg_kernels(xf_op* op, int reps, double* ms_out) {
       ms_out[9] = time([&] { xf_cg_poly_first_launch(op, r, z2, f2, q, p, p, e, r2); });
       ms_out[10] = time([&] { xf_cg_poly_second_launch(op, z2, r2, e, f1); });
       ms_out[11] = time([&] { xf_cg_poly_first_launch(op, z2, e, f1, nullptr, nullptr, nullptr, nullptr, nullptr); });
+    }
+  }
+  ms_out[12] = ms_out[13] = ms_out[14] = -1.0;
+  if (xf_cg_poly_supported(g) && xf_tl_prolong_ay_supported(g) && (g->n1 - 2) % 4 == 0 && (g->n2 - 2) % 4 == 0 &&
+      (g->n3 - 2) % 4 == 0) {
+    // the learned two-level preconditioner's fine-grid passes: y = P zc with
+    // A y and (y, A y); the smoother's first pass on r - omega A y; its last,
+    // z = omega y + s p1(A) w into z and the direction slot with (z, r), (z, q)
+    const int c2 = (g->n2 - 2) / 4 + 2, c3 = (g->n3 - 2) / 4 + 2;
+    const int64_t nc = (int64_t)((g->n1 - 2) / 4 + 2) * c2 * c3;
+    float *zc = B.get<float>(nc), *y = B.get<float>(n), *w = B.get<float>(n), *z2 = B.get<float>(n);
+    if (!zc || !y || !w || !z2) return xf_fail(ctx, XF_ERR_NOMEM, "xf_profile_cg_kernels: allocation");
+    float f1[3], f2[3];
+    if (xf_cheb4_factors(4.0 * (g->ucx + g->ucy + g->ucz), 6.0, f1, f2)) {
+      ms_out[12] = time([&] { xf_tl_prolong_ay(op, zc, c2, c3, y, q, SL_C); });
+      ms_out[13] = time([&] {
+        xf_cg_poly_tl_launch(op, true, false, r, q, w, f2, SL_C, SL_C + 1, y, 1.f, p, r, q, SL_C + 2, SL_C + 3);
+      });
+      ms_out[14] = time([&] {
+        xf_cg_poly_tl_launch(op, false, true, w, q, e, f1, SL_C, SL_C + 1, y, 1.f, p, r, q, SL_C + 2, SL_C + 3);
+      });
     }
   }
   cudaEventDestroy(t0);
