@@ -755,36 +755,47 @@ __global__ void __launch_bounds__(CGK_THREADS, 4) k_tl_prolong_ay(CgqArgs<float>
   DotAcc<float> acc;
   if (p0 < P) {
     const int j = p0 / n3, k0 = p0 - j * n3;
-    // coarse index of a fine cell's block (interior cells only)
-    auto blk = [&](int i, int jj, int k) -> int64_t {
-      return ((int64_t)(1 + ((i - 1) >> 2)) * c2 + (1 + ((jj - 1) >> 2))) * c3 + (1 + ((k - 1) >> 2));
-    };
-    auto cv = [&](int64_t b) -> float { return __ldg(zc + b); };
+    // block coordinates and block-face flags of this thread's row and its two
+    // cells (interior cells only; ghost cells take the ROW_NONE branch): a
+    // neighbour across a block face is the next block's value, else the own
+    const int sJ = c3, sI = c2 * c3;
+    const int Jb = 1 + ((j - 1) >> 2);
+    const bool jlo = ((j - 1) & 3) == 0, jhi = ((j - 1) & 3) == 3;
+    int Kb[2];
+    bool klo[2], khi[2];
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const int k = k0 + t;
+      Kb[t] = 1 + ((k - 1) >> 2);
+      klo[t] = ((k - 1) & 3) == 0;
+      khi[t] = ((k - 1) & 3) == 3;
+    }
     for (int i = i0; i < i1; i++) {
       const int c = i * P + p0;
       const uchar2 kk = __ldg(reinterpret_cast<const uchar2*>(g.kind + c));
       const uint8_t kbs[2] = {kk.x, kk.y};
+      const int Ib = 1 + ((i - 1) >> 2);
+      const bool ilo = ((i - 1) & 3) == 0, ihi = ((i - 1) & 3) == 3;
+      const int brow = (Ib * c2 + Jb) * c3;
       float yv[2], out[2];
 #pragma unroll
       for (int t = 0; t < 2; t++) {
         const uint8_t kb = kbs[t];
-        const int k = k0 + t;
         if (row_of(kb) == ROW_NONE) {
           yv[t] = 0.f;
           out[t] = 0.f;
           continue;
         }
-        const int64_t bc = blk(i, j, k);
-        const float yc = cv(bc);
-        // a neighbour's value: its block's (the own block's unless across a block face), 0 behind a closed face
-        auto nb = [&](uint8_t bit, int ii, int jj, int kz) -> float {
+        const int bc = brow + Kb[t];
+        const float yc = __ldg(zc + bc);
+        // a neighbour's value: the next block's across a block face, else the own; 0 behind a closed face
+        auto nb = [&](uint8_t bit, bool cross, int off) -> float {
           if (!(kb & bit)) return 0.f;
-          const int64_t bn = blk(ii, jj, kz);
-          return bn == bc ? yc : cv(bn);
+          return cross ? __ldg(zc + bc + off) : yc;
         };
-        const float ypx = nb(K_PX, i + 1, j, k), ymx = nb(K_MX, i - 1, j, k);
-        const float ypy = nb(K_PY, i, j + 1, k), ymy = nb(K_MY, i, j - 1, k);
-        const float ypz = nb(K_PZ, i, j, k + 1), ymz = nb(K_MZ, i, j, k - 1);
+        const float ypx = nb(K_PX, ihi, sI), ymx = nb(K_MX, ilo, -sI);
+        const float ypy = nb(K_PY, jhi, sJ), ymy = nb(K_MY, jlo, -sJ);
+        const float ypz = nb(K_PZ, khi[t], 1), ymz = nb(K_MZ, klo[t], -1);
         yv[t] = yc;
         out[t] = fmaf(dtab[kb & 63], yc, -fmaf(cx, ypx + ymx, fmaf(cy, ypy + ymy, cz * (ypz + ymz))));
       }

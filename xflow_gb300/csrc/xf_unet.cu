@@ -1233,6 +1233,49 @@ __global__ void k_tl_z(DevScratch* S, TlCtl* c, const TlParams* p, cudaGraphCond
   cudaGraphSetConditional(fb, bad ? 1u : 0u);
 }
 // the window coefficients -(z, q_j) / (p_j, q_j) of the block with direction slot hd
+// The window's last term of the new direction with (p, r): p += coef_j p_j
+// (when the control kept term j) and (p, r) into scalars[slot] in one pass;
+// k_dot_f4's grid, mapping and order, so (p, r) is bit for bit the separate dot's.
+__global__ void __launch_bounds__(RED_THREADS) k_tl_axpy_pr(float* __restrict__ y, const float* __restrict__ x,
+                                                            const float* __restrict__ r, const TlCtl* c, int j,
+                                                            int64_t n, DevScratch* S, int slot) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const bool use = c->use_coef[j] != 0;
+  const float a = c->coef[j];
+  DotAcc<float> acc;
+  const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
+  float4* y4 = reinterpret_cast<float4*>(y);
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n4; k += stride) {
+    float4 v = y4[k];
+    if (use) {
+      const float4 xv = __ldg(x4 + k);
+      v.x = fmaf(a, xv.x, v.x); v.y = fmaf(a, xv.y, v.y); v.z = fmaf(a, xv.z, v.z); v.w = fmaf(a, xv.w, v.w);
+      y4[k] = v;
+    }
+    const float4 rv = __ldg(r4 + k);
+    acc.add(v.x, rv.x);
+    acc.add(v.y, rv.y);
+    acc.add(v.z, rv.z);
+    acc.add(v.w, rv.w);
+  }
+  for (int64_t k = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += stride) {
+    float v = y[k];
+    if (use) {
+      v = fmaf(a, x[k], v);
+      y[k] = v;
+    }
+    acc.add(v, r[k]);
+  }
+  if (!publish_acc<float>(S, slot, slot, acc, sh, &last)) return;
+  const double t = finish_partials(S, slot, sh);
+  if (threadIdx.x == 0) {
+    S->scalars[slot] = t;
+    S->tickets[slot] = 0;
+  }
+}
 __global__ void k_tl_coef(const DevScratch* S, TlCtl* c, int hd, int m) {
   if (threadIdx.x | blockIdx.x) return;
   for (int j = 0; j < m; j++) {
@@ -1533,15 +1576,16 @@ static int tl_graph_build(xf_op* op, xf_unet* u, int m, int F, const float (*tl_
     // the new direction, its image, alpha, the update, the cycle-end test
     begin(bbody, &fnode, 1);
     k_tl_coef<<<1, 32, 0, s>>>(S, c, hd, m);
-    for (int j = 0; j < m; j++) k_tl_axpy<<<eb, 256, 0, s>>>(pn, P[(hd + m - j) % (m + 1)], c, j, n);
+    for (int j = 0; j < m - 1; j++) k_tl_axpy<<<eb, 256, 0, s>>>(pn, P[(hd + m - j) % (m + 1)], c, j, n);
+    k_tl_axpy_pr<<<db, RED_THREADS, 0, s>>>(pn, P[(hd + 1) % (m + 1)], r, c, m - 1, n, S, FS_PR);   // with (p, r)
     xf_cg_q32_dot(op, pn, qn, FS_PQ);   // q = A p, (p, q)
-    fdot(pn, r, FS_PR, nullptr);
     k_tl_alpha<<<1, 32, 0, s>>>(S, c, hd, m);
     k_tl_update<<<db, RED_THREADS, 0, s>>>(e, r, pn, qn, c, n, S, FS_RR);   // with (r, r)
     k_tl_rr<<<1, 32, 0, s>>>(S, c, H, hd, m);
     end_tail(unused);
-    // it, z-test, coef, m axpys, stencil + dot, alpha, update with (r, r), test, and the loop guard
-    n_iter = 3 + m + 2 + 1 + 1 + 1 + 1;
+    // it, z-test, coef, m axpys (the last with (p, r)), stencil + dot, alpha, update with (r, r), test, and
+    // the loop guard
+    n_iter = 3 + m + 1 + 1 + 1 + 1 + 1;
   }
   // the loop guard, last in the body
   begin(wbody, &prev, 1);
