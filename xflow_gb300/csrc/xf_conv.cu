@@ -610,12 +610,214 @@ static int* conv_err_flag(xf_ctx* ctx) { return reinterpret_cast<int*>(&ctx->scr
 // per kernel and device to the largest size asked for (so that the launches
 // of a captured solve set no attribute).
 static cudaError_t set_max_smem(const void* kern, int which, int device, size_t smem) {
-  static size_t done[2][64] = {};
+  static size_t done[3][64] = {};
   size_t& d = done[which][device & 63];
   if (smem <= d) return cudaSuccess;
   const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) d = smem;
   return e;
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient of the convolution on the tensor cores:
+//     dW[t][co][ci] = sum over cells c of g[c][co] x[c + off_t][ci].
+// With the activations in channel planes, 8 consecutive cells of one plane
+// are also the canonical MN-major core matrix (8 channels along M or N, one
+// cell per 16-byte row along K), so the sum over cells is the K dimension of
+// an MMA: M = 128 rows of stacked (tap, input channel) pairs (128 / ci taps per
+// row tile), N = co, A = the shifted x blocks, B = g.  A stage is 128 cells:
+// per (tap, plane) of the row tile and per plane of g one 2 KB bulk copy (one
+// per lane of the producer warp), eight MMAs of K = 16 cells.  Each CTA takes
+// one row tile and one range of cells (a multiple of 128: the cells past the
+// box read the zero margins), accumulates in TMEM, and writes its FP32
+// partial; k_wgrad_tc_sum adds the ranges in a fixed order (deterministic).
+// Descriptors: no swizzle, MN-major (instruction descriptor bits 15 and 16),
+// LBO = the K-direction core-matrix stride (128 bytes), SBO = the MN-direction
+// stride (2 KB).
+constexpr int WG_KC = 128;                         // cells per stage
+constexpr int WG_STAGES = 3;
+constexpr uint32_t WG_BLOCK = WG_KC * 16;          // one (tap, plane) block of a stage
+constexpr uint32_t WG_A = 16 * WG_BLOCK;           // the row tile's A region (16 blocks)
+
+struct WgArgs {
+  const uint16_t* g;   // plane 0, cell 0
+  int64_t gps;
+  int co;
+  const uint16_t* x;
+  int64_t xps;
+  int ci;
+  int n2, n3;
+  int taps, mtiles, splits, stages;   // taps per row tile, row tiles, cell ranges, stages per range
+  int64_t chunks;                      // 128-cell stages in all
+  uint32_t stage_bytes;
+  float* partial;   // [mtile][split][128][co]
+  int* err;
+};
+
+__global__ void __launch_bounds__(BK_THREADS) k_wgrad_tc(WgArgs a) {
+  extern __shared__ uint8_t dsm[];
+  __shared__ uint64_t full[WG_STAGES], empty[WG_STAGES], mdone;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x % a.mtiles, sp = blockIdx.x / a.mtiles;
+  const int cp = a.ci / 8, t0 = mt * a.taps, tn = min(27, t0 + a.taps) - t0;
+  const int ga = tn * cp, gb = a.co / 8;   // blocks of A and of B per stage
+  const uint32_t raw = tc::smem_addr(dsm);
+  uint8_t* smem = dsm + ((1024u - (raw & 1023u)) & 1023u);
+  const uint32_t ncols = tmem_cols(a.co);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < WG_STAGES; st++) {
+      tc::mbar_init(&full[st], 1);
+      tc::mbar_init(&empty[st], 1);
+    }
+    tc::mbar_init(&mdone, 1);
+    abort_flag = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = tmem_base;
+  volatile int* abort_p = &abort_flag;
+  const int64_t P = (int64_t)a.n2 * a.n3;
+  const int64_t cell0 = (int64_t)sp * a.stages * WG_KC;
+  // this range's stages: the last range stops at the box's last 128-cell chunk
+  const int my_stages = (int)min((int64_t)a.stages, a.chunks - (int64_t)sp * a.stages);
+  if (warp == 4) {   // ---- producer: one copy per lane
+    const bool is_a = lane < ga, is_b = lane >= ga && lane < ga + gb;
+    const uint16_t* src = nullptr;
+    uint32_t dst_off = 0;
+    if (is_a) {
+      const int t = t0 + lane / cp, q = lane % cp;
+      const int64_t off = (t / 9 - 1) * P + ((t / 3) % 3 - 1) * (int64_t)a.n3 + (t % 3 - 1);
+      src = a.x + q * a.xps + off * 8;
+      dst_off = (uint32_t)lane * WG_BLOCK;
+    } else if (is_b) {
+      const int q = lane - ga;
+      src = a.g + q * a.gps;
+      dst_off = WG_A + (uint32_t)q * WG_BLOCK;
+    }
+    int st = 0, pass = 0, issued = 0;
+    for (int k = 0; k < my_stages; k++) {
+      if (pass > 0) {
+        bool w = true;
+        if (lane == 0) w = bk_wait(&empty[st], (uint32_t)((pass - 1) & 1), abort_p);
+        if (!__shfl_sync(0xffffffffu, w, 0)) break;
+      }
+      uint8_t* sa = smem + st * a.stage_bytes;
+      if (lane == 0) mbar_expect_tx(&full[st], (uint32_t)(ga + gb) * WG_BLOCK);
+      if (is_a || is_b) bulk_load(sa + dst_off, src + (cell0 + (int64_t)k * WG_KC) * 8, WG_BLOCK, &full[st]);
+      issued++;
+      if (++st == WG_STAGES) {
+        st = 0;
+        pass++;
+      }
+    }
+    if (lane == 0)   // every copy issued has landed before the CTA may leave
+      for (int s2 = 0; s2 < WG_STAGES; s2++) {
+        const int n = issued / WG_STAGES + (s2 < issued % WG_STAGES ? 1 : 0);
+        if (n > 0) bk_wait(&full[s2], (uint32_t)((n - 1) & 1), abort_p, false);
+      }
+    __syncwarp();
+  } else if (warp == 5) {
+    if (lane == 0) {   // ---- MMA issuer
+      const uint32_t idesc = tc::idesc_bf16_f32(128, a.co) | (1u << 15) | (1u << 16);   // A and B MN-major
+      int st = 0, pass = 0;
+      for (int k = 0; k < my_stages; k++) {
+        if (!bk_wait(&full[st], (uint32_t)(pass & 1), abort_p)) break;
+        tc::fence_after_sync();
+        const uint8_t* sa = smem + st * a.stage_bytes;
+#pragma unroll 1
+        for (int kk = 0; kk < WG_KC / 16; kk++) {
+          const uint64_t ad = tc::smem_desc(tc::smem_addr(sa + kk * 256), 128, WG_BLOCK);
+          const uint64_t bd = tc::smem_desc(tc::smem_addr(sa + WG_A + kk * 256), 128, WG_BLOCK);
+          tc::mma_bf16(tbase, ad, bd, idesc, k > 0 || kk > 0);
+        }
+        tc::mma_commit(&empty[st]);
+        if (++st == WG_STAGES) {
+          st = 0;
+          pass++;
+        }
+      }
+      tc::mma_commit(&mdone);   // every MMA issued
+    }
+    __syncwarp();
+  } else {   // ---- epilogue, warps 0-3: the partial of this tile and range
+    const bool got = bk_wait(&mdone, 0, abort_p, false);
+    if (__all_sync(0xffffffffu, got) && !*abort_p) {
+      tc::fence_after_sync();
+      const int row = warp * 32 + lane;
+      float* dst = a.partial + (((int64_t)mt * a.splits + sp) * 128 + row) * a.co;
+      for (int co = 0; co < a.co; co += 8) {
+        float v[8];
+        tc::tmem_ld8(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)co, v);
+        *reinterpret_cast<float4*>(dst + co) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4*>(dst + co + 4) = make_float4(v[4], v[5], v[6], v[7]);
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_flag) atomicExch(a.err, 1);
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, ncols);
+}
+
+// gw[t][co][ci] += the ranges' partials in range order.
+__global__ void k_wgrad_tc_sum(const float* __restrict__ partial, int mtiles, int splits, int taps, int ci, int co,
+                               float* __restrict__ gw) {
+  const int64_t n = (int64_t)27 * co * ci;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(u / ((int64_t)co * ci));
+    const int o = (int)((u / ci) % co), i = (int)(u % ci);
+    const int mt = t / taps, row = (t - mt * taps) * ci + i;
+    float s = 0.f;
+    for (int sp = 0; sp < splits; sp++) s += partial[(((int64_t)mt * splits + sp) * 128 + row) * co + o];
+    gw[u] += s;
+  }
+}
+
+// The row tiles and cell ranges of a layer's weight gradient, and the FP32
+// partial buffer it needs (floats).
+void xf_wgrad_tc_plan(const xf_ctx* ctx, int64_t ncell, int ci, int co, int* mtiles, int* splits, int* stages,
+                      int64_t* partial_floats) {
+  const int taps = 128 / ci;
+  *mtiles = (27 + taps - 1) / taps;
+  const int64_t chunks = (ncell + WG_KC - 1) / WG_KC;
+  int64_t sp = ((int64_t)ctx->sm_count * 2 + *mtiles - 1) / *mtiles;
+  if (sp > chunks) sp = chunks;
+  if (sp < 1) sp = 1;
+  *stages = (int)((chunks + sp - 1) / sp);
+  *splits = (int)((chunks + *stages - 1) / *stages);
+  *partial_floats = (int64_t)*mtiles * *splits * 128 * co;
+}
+
+// gw ([27][co][ci] FP32) += the weight gradient of g (co channels) against x
+// (ci channels), both BF16 planes with their zero margins; partial holds
+// xf_wgrad_tc_plan's floats.  ci and co multiples of 16, ci <= 128, co <= 64.
+int xf_wgrad_tc(xf_ctx* ctx, int n1, int n2, int n3, const void* g, int64_t gps, int co, const void* x, int64_t xps,
+                int ci, float* partial, float* gw) {
+  if (ci % 16 || co % 16 || ci < 16 || ci > 128 || co < 16 || co > 64)
+    return xf_fail(ctx, XF_ERR_ARG, "weight gradient: channel counts out of range");
+  WgArgs a;
+  a.g = (const uint16_t*)g; a.gps = gps; a.co = co;
+  a.x = (const uint16_t*)x; a.xps = xps; a.ci = ci;
+  a.n2 = n2; a.n3 = n3;
+  int64_t pf = 0;
+  xf_wgrad_tc_plan(ctx, (int64_t)n1 * n2 * n3, ci, co, &a.mtiles, &a.splits, &a.stages, &pf);
+  a.taps = 128 / ci;
+  a.chunks = ((int64_t)n1 * n2 * n3 + WG_KC - 1) / WG_KC;
+  a.stage_bytes = (WG_A + (uint32_t)co / 8 * WG_BLOCK + 1023) / 1024 * 1024;
+  a.partial = partial;
+  a.err = conv_err_flag(ctx);
+  const size_t smem = (size_t)WG_STAGES * a.stage_bytes + 1024;
+  XF_CUDA(ctx, set_max_smem((const void*)k_wgrad_tc, 2, ctx->device, smem));
+  k_wgrad_tc<<<a.mtiles * a.splits, BK_THREADS, smem, ctx->stream>>>(a);
+  const int64_t nw = (int64_t)27 * co * ci;
+  k_wgrad_tc_sum<<<(unsigned)((nw + 255) / 256), 256, 0, ctx->stream>>>(partial, a.mtiles, a.splits, a.taps, ci, co,
+                                                                        gw);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
 }
 
 // Launch on the context stream (arguments checked by the caller).  `weights`

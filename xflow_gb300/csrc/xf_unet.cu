@@ -29,6 +29,10 @@ int xf_conv_launch(xf_ctx* ctx, int n1, int n2, int n3, const void* in, int64_t 
                    const void* tiled, const float* bias, int co, const uint8_t* mask, void* out, int64_t out_pitch,
                    int out_ch, int out_fp32, int relu, const void* gate, int64_t gate_ps);
 void xf_mv64(const xf_op* op, const MvReq<double>& q);
+void xf_wgrad_tc_plan(const xf_ctx* ctx, int64_t ncell, int ci, int co, int* mtiles, int* splits, int* stages,
+                      int64_t* partial_floats);
+int xf_wgrad_tc(xf_ctx* ctx, int n1, int n2, int n3, const void* g, int64_t gps, int co, const void* x, int64_t xps,
+                int ci, float* partial, float* gw);
 void xf_cg_q32_dot(const xf_op* op, const float* p, float* q, int slot);
 bool xf_tl_prolong_ay_supported(const xf_grid* g);
 void xf_tl_prolong_ay(const xf_op* op, const float* zc, int c2, int c3, float* y, float* ay, int slot);
@@ -105,7 +109,7 @@ struct xf_unet {
   double* red = nullptr;            // device reductions: [0] sum r^2, [1] sum e^2, [2] loss
   double* rpart = nullptr;          // per-block partials of the sums of squares, 2 x RP_MAX
   unsigned* rtick = nullptr;        // their last-block tickets
-  float* wpart = nullptr;           // per-chunk weight-gradient partials [chunk][27][co][ci]
+  float* wpart = nullptr;           // tensor-core weight-gradient partials [row tile][cell range][128][co]
   float* bpart = nullptr;           // per-chunk bias-gradient partials [chunk][co]
   double* zd = nullptr;             // level-0 box, FP64: the output (A-norm loss)
   double* az = nullptr;             // A zd
@@ -322,78 +326,40 @@ __global__ void k_unet_loss(const float* __restrict__ z, const double* __restric
   if ((threadIdx.x & 31) == 0) atomicAdd(&red[2], l / count);
 }
 
-// Weight gradient on the CUDA cores in FP32: gw[t][co][ci] += sum over cells
-// of g[c][co] * x[c + off_t][ci]; gb[co] += sum g[c][co] (tap 13 blocks).
-// Block = (tap, chunk of cells); the chunk's gradient and input rows are
-// staged in shared memory, each thread owns co*ci/256 (co, ci) pairs.
-constexpr int WG_CELLS = 64;
-// Cells per weight-gradient block: 4096, or more so that a level has at most
-// WG_MAX_CHUNKS chunks (the partial buffers' size).
+// Bias gradient gb[co] += sum over cells of g[c][co] (the weight gradients run
+// on the tensor cores, xf_wgrad_tc).  Block = (8-channel plane, chunk of
+// cells); each thread sums 8 channels over its cells, the block in a fixed
+// tree, and k_bgrad_sum adds the chunks in order (deterministic).
+// Cells per block: 4096, or more so that a level has at most WG_MAX_CHUNKS
+// chunks (the partial buffer's size).
 constexpr int WG_MAX_CHUNKS = 128;
 static int64_t wg_chunk(int64_t n) {
   int64_t c = (n + WG_MAX_CHUNKS - 1) / WG_MAX_CHUNKS;
-  c = (c + WG_CELLS - 1) / WG_CELLS * WG_CELLS;
+  c = (c + 255) / 256 * 256;
   return c < 4096 ? 4096 : c;
 }
-__global__ void __launch_bounds__(256) k_wgrad(const uint16_t* __restrict__ g, int64_t gps,
-                                               const uint16_t* __restrict__ x, int64_t xps, int ci, int co, int n2,
-                                               int n3, int64_t ncell, int chunk,
-                                               float* __restrict__ wpart, float* __restrict__ bpart) {
-  extern __shared__ float wsm[];
-  float* sg = wsm;                   // [WG_CELLS][co]
-  float* sx = wsm + WG_CELLS * co;   // [WG_CELLS][ci]
-  const int t = blockIdx.y;
-  const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
-  const int64_t off = di * (int64_t)n2 * n3 + dj * (int64_t)n3 + dk;
-  const int npair = co * ci;
-  const int per = (npair + 255) / 256;   // <= 24 (96 x 64 / 256)
-  float accv[24];
-  for (int q = 0; q < per; q++) accv[q] = 0.f;
-  float accb = 0.f;
+__global__ void __launch_bounds__(256) k_bgrad(const uint16_t* __restrict__ g, int64_t gps, int64_t ncell, int chunk,
+                                               int co, float* __restrict__ bpart) {
+  __shared__ float red[8][256];
+  const int q = blockIdx.y;
   const int64_t c_beg = (int64_t)blockIdx.x * chunk, c_end = min(ncell, c_beg + chunk);
-  for (int64_t cb = c_beg; cb < c_end; cb += WG_CELLS) {
-    const int nc = (int)min((int64_t)WG_CELLS, c_end - cb);
+  float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int64_t c = c_beg + threadIdx.x; c < c_end; c += 256) bf8_acc(s, *reinterpret_cast<const uint4*>(g + q * gps + c * 8));
+  for (int e = 0; e < 8; e++) red[e][threadIdx.x] = s[e];
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+      for (int e = 0; e < 8; e++) red[e][threadIdx.x] += red[e][threadIdx.x + h];
     __syncthreads();
-    for (int u = threadIdx.x; u < WG_CELLS * co; u += 256) {
-      const int r = u / co, ch = u - r * co;
-      sg[u] = r < nc ? bf2f(g[(ch >> 3) * gps + (cb + r) * 8 + (ch & 7)]) : 0.f;
-    }
-    for (int u = threadIdx.x; u < WG_CELLS * ci; u += 256) {
-      const int r = u / ci, ch = u - r * ci;
-      sx[u] = r < nc ? bf2f(x[(ch >> 3) * xps + (cb + r + off) * 8 + (ch & 7)]) : 0.f;
-    }
-    __syncthreads();
-    for (int q = 0; q < per; q++) {
-      const int pr = threadIdx.x + q * 256;
-      if (pr >= npair) break;
-      const int o = pr / ci, i = pr - o * ci;
-      float s = 0.f;
-      for (int r = 0; r < WG_CELLS; r++) s = fmaf(sg[r * co + o], sx[r * ci + i], s);
-      accv[q] += s;
-    }
-    if (t == 13 && threadIdx.x < co)
-      for (int r = 0; r < WG_CELLS; r++) accb += sg[r * co + threadIdx.x];
   }
-  for (int q = 0; q < per; q++) {
-    const int pr = threadIdx.x + q * 256;
-    if (pr < npair) wpart[((int64_t)blockIdx.x * 27 + t) * npair + pr] = accv[q];
-  }
-  if (t == 13 && threadIdx.x < co) bpart[(int64_t)blockIdx.x * co + threadIdx.x] = accb;
+  if (threadIdx.x < 8) bpart[(int64_t)blockIdx.x * co + q * 8 + threadIdx.x] = red[threadIdx.x][0];
 }
-// gw[t][co][ci] += sum over chunks in chunk order, gb likewise (deterministic).
-__global__ void k_wgrad_sum(const float* __restrict__ wpart, const float* __restrict__ bpart, int nchunk, int64_t nw,
-                            int co, float* __restrict__ gw, float* __restrict__ gb) {
-  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (u < nw) {
-    float s = 0.f;
-    for (int c = 0; c < nchunk; c++) s += wpart[(int64_t)c * nw + u];
-    gw[u] += s;
-  }
-  if (u < co) {
-    float s = 0.f;
-    for (int c = 0; c < nchunk; c++) s += bpart[(int64_t)c * co + u];
-    gb[u] += s;
-  }
+__global__ void k_bgrad_sum(const float* __restrict__ bpart, int nchunk, int co, float* __restrict__ gb) {
+  const int u = threadIdx.x;
+  if (u >= co) return;
+  float s = 0.f;
+  for (int c = 0; c < nchunk; c++) s += bpart[(int64_t)c * co + u];
+  gb[u] += s;
 }
 
 // Adam step on one layer (bias-corrected, step counts from 1), then the BF16
@@ -576,8 +542,9 @@ extern "C" int xf_unet_create(const xf_grid* g, xf_unet** out) {
   if (!st) {   // partial buffers of the deterministic reductions
     int64_t wneed = 1;
     for (int k = 0; k < NLAYER; k++) {
-      const int64_t n = u->L[LLEV[k]].n, chunk = wg_chunk(n), nchunk = (n + chunk - 1) / chunk;
-      const int64_t need = nchunk * 27 * u->ly[k].co * u->ly[k].ci;
+      int mt, sp, stg;
+      int64_t need;
+      xf_wgrad_tc_plan(ctx, u->L[LLEV[k]].n, u->ly[k].ci, u->ly[k].co, &mt, &sp, &stg, &need);
       if (need > wneed) wneed = need;
     }
     if (cudaMalloc(&u->rpart, 2 * RP_MAX * 8) != cudaSuccess || cudaMalloc(&u->rtick, 4 * 4) != cudaSuccess ||
@@ -688,18 +655,20 @@ static int dgrad(xf_unet* u, int k, const Act& g, const Act& out, int out_c0, co
                         out.ch(u->L, out_c0), out.ps(), y.ci, 0, 0,
                         gate ? (const void*)gate->ch(u->L, gate_c0) : nullptr, gate ? gate->ps() : 0);
 }
-static void wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_c0) {
+// Weight and bias gradients of layer k from its pre-activation gradient g and
+// its input x (from channel x_c0 on): the weights on the tensor cores.
+static int wgrad(xf_unet* u, int k, const Act& g, const Act& x, int x_c0) {
   const Layer& y = u->ly[k];
   const Level& L = u->L[LLEV[k]];
+  const int st = xf_wgrad_tc(u->ctx, L.n1, L.n2, L.n3, g.p0(u->L), g.ps(), y.co, x.ch(u->L, x_c0), x.ps(), y.ci,
+                             u->wpart, y.gw);
+  if (st) return st;
   const int64_t chunk = wg_chunk(L.n);
   const int nchunk = (int)((L.n + chunk - 1) / chunk);
-  dim3 grid((unsigned)nchunk, 27);
-  const size_t smem = (size_t)WG_CELLS * (y.co + y.ci) * 4;
-  k_wgrad<<<grid, 256, smem, u->ctx->stream>>>(g.p0(u->L), g.ps(), x.ch(u->L, x_c0), x.ps(), y.ci, y.co, L.n2, L.n3,
-                                                 L.n, (int)chunk, u->wpart, u->bpart);
-  const int64_t nw = (int64_t)27 * y.co * y.ci;
-  k_wgrad_sum<<<(unsigned)((nw + 255) / 256), 256, 0, u->ctx->stream>>>(u->wpart, u->bpart, nchunk, nw, y.co, y.gw,
-                                                                        y.gb);
+  k_bgrad<<<dim3((unsigned)nchunk, (unsigned)(y.co / 8)), 256, 0, u->ctx->stream>>>(g.p0(u->L), g.ps(), L.n,
+                                                                                    (int)chunk, y.co, u->bpart);
+  k_bgrad_sum<<<1, 64, 0, u->ctx->stream>>>(u->bpart, nchunk, y.co, y.gb);
+  return XF_OK;
 }
 
 // Kernels one forward pass launches, with xf_unet_apply_dev's output conversion.
@@ -759,27 +728,27 @@ static int backward(xf_unet* u, const double* r, const double* e, const xf_op* o
                                                      u->G0_16a.p0(L), u->G0_16a.ps());
   }
   // out, dec0b, dec0a
-  wgrad(u, OUTL, u->G0_16a, u->D0b, 0);
+  if ((st = wgrad(u, OUTL, u->G0_16a, u->D0b, 0))) return st;
   if ((st = dgrad(u, OUTL, u->G0_16a, u->G0_16b, 0, &u->D0b, 0))) return st;
-  wgrad(u, DEC0B, u->G0_16b, u->D0a, 0);
+  if ((st = wgrad(u, DEC0B, u->G0_16b, u->D0a, 0))) return st;
   if ((st = dgrad(u, DEC0B, u->G0_16b, u->G0_16a, 0, &u->D0a, 0))) return st;
-  wgrad(u, DEC0A, u->G0_16a, u->CAT0, 0);
+  if ((st = wgrad(u, DEC0A, u->G0_16a, u->CAT0, 0))) return st;
   if ((st = dgrad(u, DEC0A, u->G0_16a, u->G0_48, 0, nullptr, 0))) return st;
   // up(D1b) part -> dec1b's pre-activation gradient
   k_upsample_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G0_48.p0(L), u->G0_48.ps(), L[0].n2, L[0].n3,
                                                            u->D1b.p0(L), u->D1b.ps(), L[1].mask, L[1].n1, L[1].n2,
                                                            L[1].n3, u->G1_32a.p0(L), u->G1_32a.ps(), 32);
-  wgrad(u, DEC1B, u->G1_32a, u->D1a, 0);
+  if ((st = wgrad(u, DEC1B, u->G1_32a, u->D1a, 0))) return st;
   if ((st = dgrad(u, DEC1B, u->G1_32a, u->G1_32b, 0, &u->D1a, 0))) return st;
-  wgrad(u, DEC1A, u->G1_32b, u->CAT1, 0);
+  if ((st = wgrad(u, DEC1A, u->G1_32b, u->CAT1, 0))) return st;
   if ((st = dgrad(u, DEC1A, u->G1_32b, u->G1_96, 0, nullptr, 0))) return st;
   // up(M2b) part -> mid_b
   k_upsample_bwd<<<ublocks(ctx, L[2].n * 64), 256, 0, s>>>(u->G1_96.p0(L), u->G1_96.ps(), L[1].n2, L[1].n3,
                                                            u->M2b.p0(L), u->M2b.ps(), L[2].mask, L[2].n1, L[2].n2,
                                                            L[2].n3, u->G2_64a.p0(L), u->G2_64a.ps(), 64);
-  wgrad(u, MIDB, u->G2_64a, u->M2a, 0);
+  if ((st = wgrad(u, MIDB, u->G2_64a, u->M2a, 0))) return st;
   if ((st = dgrad(u, MIDB, u->G2_64a, u->G2_64b, 0, &u->M2a, 0))) return st;
-  wgrad(u, MIDA, u->G2_64b, u->P2, 0);
+  if ((st = wgrad(u, MIDA, u->G2_64b, u->P2, 0))) return st;
   if ((st = dgrad(u, MIDA, u->G2_64b, u->G2_32, 0, nullptr, 0))) return st;
   k_pool_bwd<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G2_32.p0(L), u->G2_32.ps(), L[2].n2, L[2].n3, L[1].mask,
                                                        L[1].n1, L[1].n2, L[1].n3, u->gsum1, 32, 32);
@@ -787,18 +756,18 @@ static int backward(xf_unet* u, const double* r, const double* e, const xf_op* o
   k_skip_grad<<<ublocks(ctx, L[1].n * 32), 256, 0, s>>>(u->G1_96.ch(L, 64), u->G1_96.ps(), u->gsum1, 32,
                                                         u->CAT1.ch(L, 64), u->CAT1.ps(), L[1].mask, L[1].n,
                                                         u->G1_32a.p0(L), u->G1_32a.ps(), 32);
-  wgrad(u, ENC1B, u->G1_32a, u->A1, 0);
+  if ((st = wgrad(u, ENC1B, u->G1_32a, u->A1, 0))) return st;
   if ((st = dgrad(u, ENC1B, u->G1_32a, u->G1_32b, 0, &u->A1, 0))) return st;
-  wgrad(u, ENC1A, u->G1_32b, u->P1, 0);
+  if ((st = wgrad(u, ENC1A, u->G1_32b, u->P1, 0))) return st;
   if ((st = dgrad(u, ENC1A, u->G1_32b, u->G1_16, 0, nullptr, 0))) return st;
   k_pool_bwd<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G1_16.p0(L), u->G1_16.ps(), L[1].n2, L[1].n3, L[0].mask,
                                                        L[0].n1, L[0].n2, L[0].n3, u->gsum, 16, 16);
   k_skip_grad<<<ublocks(ctx, L[0].n * 16), 256, 0, s>>>(u->G0_48.ch(L, 32), u->G0_48.ps(), u->gsum, 16,
                                                         u->CAT0.ch(L, 32), u->CAT0.ps(), L[0].mask, L[0].n,
                                                         u->G0_16a.p0(L), u->G0_16a.ps(), 16);
-  wgrad(u, ENC0B, u->G0_16a, u->A0, 0);
+  if ((st = wgrad(u, ENC0B, u->G0_16a, u->A0, 0))) return st;
   if ((st = dgrad(u, ENC0B, u->G0_16a, u->G0_16b, 0, &u->A0, 0))) return st;
-  wgrad(u, ENC0A, u->G0_16b, u->X0, 0);
+  if ((st = wgrad(u, ENC0A, u->G0_16b, u->X0, 0))) return st;
   XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
 }
