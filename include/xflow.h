@@ -53,8 +53,10 @@ enum { XF_F64 = 0, XF_F32 = 1 };
  * by xf_op_set_advection). */
 enum { XF_OP_LAPLACE = 0, XF_OP_VARDIV = 1, XF_OP_PACK = 2, XF_OP_ADVDIFF = 3 };
 /* xf_op_set_advection flags (THydrodynamicsProblem's flagConvective and
- * flagDiffusion, XProblem.cpp:1236-1238) */
-enum { XF_ADV_CONVECTIVE = 1, XF_ADV_DIFFUSIVE = 2 };
+ * flagDiffusion, XProblem.cpp:1236-1238; XF_ADV_UPWIND: its first-order
+ * upwind scheme, schemeType 1 of SolveTransferEquation_, XProblem.cpp:
+ * 1828-1843, the concentration equation's) */
+enum { XF_ADV_CONVECTIVE = 1, XF_ADV_DIFFUSIVE = 2, XF_ADV_UPWIND = 4 };
 
 /* xf_matvec flags */
 enum {
@@ -133,10 +135,14 @@ int xf_op_set_density(xf_op* op, const double* host_density_box);
  *   B_d = diff 0.5 D hx2 / hxhxh                              (f[m])
  *   C_d = conv 0.5 (vd / hx2) + diff 0.5 (-D h_1 / hxhxh)     (f[m+1])
  *   (A f)_c = (1/tau) f_c + sum_d (A_d f[m-1] + B_d f_c + C_d f[m+1]),
- * in that evaluation order.  PreDefined and PreNormal rows are the Laplace
+ * in that evaluation order.  With XF_ADV_UPWIND the convective part takes
+ * the upstream neighbour over h (vd < 0: B_d += conv 0.5 (-vd / h),
+ * C_d += conv 0.5 (vd / h); else A_d += conv 0.5 (-vd / h),
+ * B_d += conv 0.5 (vd / h)); B_d is the convective term plus the diffusive
+ * one, in that order.  PreDefined and PreNormal rows are the Laplace
  * operator's (semi-sum, normal derivative).  u, v, w are FP64 boxes of the
  * operator's grid (NULL: 0), copied into the operator; flags are
- * XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE.  Nonsymmetric: solve it with
+ * XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE | XF_ADV_UPWIND.  Nonsymmetric: solve it with
  * XF_BICGSTAB, XF_MINRES, or XF_BICG on its packed form. */
 int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, const xf_vec* w, double tau,
                         double diff_coef, int flags);
@@ -348,6 +354,23 @@ int xf_divergence_max(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const
 int xf_momentum_rhs(int axis, const xf_vec* u_prev, const xf_vec* v_prev, const xf_vec* w_prev, const xf_vec* vis,
                     const xf_vec* border, const xf_vec* force, xf_vec* u_tr, xf_vec* v_tr, xf_vec* w_tr,
                     xf_vec* vis_tr, xf_vec* rp);
+
+/* Transfer terms of the concentration equation (TVPProblem::SolveBySplitting,
+ * XProblem.cpp:5886-5935) on the concentration grid gc (the pressure box):
+ *  - Actual points: u_tr = (u[i-1] + u[i]) / 2, v_tr and w_tr likewise from
+ *    the staggered boxes, rp = 0;
+ *  - PreDefined points: zero velocities, rp = inlet on the face i = 0
+ *    (ConcentrationInletCondition; inlet NULL: 0), 0 elsewhere;
+ *  - Fictive and PreNormal points: all zero.
+ * The outputs are distinct FP64 vectors of gc; u, v, w the staggered boxes.
+ * Defined, Normal, Equation and PreEquation points (the reference's throws),
+ * unknown codes and Actual points on the box face return XF_ERR_MASK naming
+ * the first in its loop order.  Bit-identical to the reference's loop.  The
+ * equation itself is XF_OP_ADVDIFF with XF_ADV_CONVECTIVE | XF_ADV_UPWIND
+ * (and XF_ADV_DIFFUSIVE for a nonzero coefficient), right-hand side
+ * xf_transfer_rhs(c_prev, rp, tau). */
+int xf_conc_transfer(const xf_grid* gc, const xf_vec* u, const xf_vec* v, const xf_vec* w, const xf_vec* inlet,
+                     xf_vec* u_tr, xf_vec* v_tr, xf_vec* w_tr, xf_vec* rp);
 
 /* ---- field output ----------------------------------------------------------- */
 /* VTK legacy ASCII volume of one time step, replacing the writer in

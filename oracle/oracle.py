@@ -273,6 +273,41 @@ def adi_first_rhs(codes, hx, hy, hz, f_1, u, v, w, D, rp, tau):
     return f
 
 
+def adi_upwind_coeffs(direction, codes, hx, hy, hz, vec_tr, D, tau):
+    """The concentration's upwind ADI line coefficients (a, b, c) along `direction` at every Actual
+    point (SolveTransferEquation_, schemeType 1, XProblem.cpp:1828-1843); NaN elsewhere."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    out = [np.full(codes.shape, np.nan) for _ in range(3)]
+    lib().xfo_adi_upwind_coeffs(int(direction), _p(codes, C.c_int32), *codes.shape, _p(f64(hx), C.c_double),
+                                _p(f64(hy), C.c_double), _p(f64(hz), C.c_double), _p(f64(vec_tr), C.c_double),
+                                C.c_double(D), C.c_double(tau), *(_p(o, C.c_double) for o in out))
+    return tuple(out)
+
+
+def adi_first_rhs_upwind(codes, hx, hy, hz, f_1, u, v, w, D, rp, tau):
+    """The upwind first-direction right-hand side at every Actual point (XProblem.cpp:1848-1912 with
+    schemeType 1) for a scalar diffusion coefficient D; NaN elsewhere."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    out = np.full(codes.shape, np.nan)
+    d = lambda a: _p(f64(a), C.c_double)  # noqa: E731
+    lib().xfo_adi_first_rhs_upwind(_p(codes, C.c_int32), *codes.shape, d(hx), d(hy), d(hz), d(f_1), d(u), d(v),
+                                   d(w), C.c_double(D), d(rp), C.c_double(tau), _p(out, C.c_double))
+    return out
+
+
+def conc_transfer(codes, u, v, w, inlet=None):
+    """The concentration equation's transfer terms (uTr, vTr, wTr, rpTr) on its grid
+    (XProblem.cpp:5886-5935); status 1 (a point type the reference throws on) or 2 (an Actual point on the
+    box face) and the flat index of the first such point."""
+    codes = np.ascontiguousarray(codes, np.int32)
+    out = [np.zeros(codes.shape) for _ in range(4)]
+    bad = C.c_int64(-1)
+    st = lib().xfo_conc_transfer(_p(codes, C.c_int32), *codes.shape, _p(f64(u), C.c_double), _p(f64(v), C.c_double),
+                                 _p(f64(w), C.c_double), _p(f64(inlet), C.c_double) if inlet is not None else None,
+                                 *(_p(o, C.c_double) for o in out), C.byref(bad))
+    return tuple(out), st, bad.value
+
+
 def divergence_max(codes, u, v, w, hxU, hyV, hzW):
     codes = np.ascontiguousarray(codes, np.int32)
     ijk = np.zeros(3, np.int32)

@@ -1153,11 +1153,99 @@ static void ad_coeffs(const double* h, int m, double vd, double D, double conv, 
   *C = conv * (0.5 * (vd / hx2)) + diff * (0.5 * (-(D)*h_1 / hxhxh));
 }
 
+/* The upwind form of the same coefficients (SolveTransferEquation_, schemeType
+ * 1, XProblem.cpp:1828-1843: the concentration's scheme), the 1/tau of b
+ * excluded: the convective term takes the upstream neighbour by the sign of
+ * vd, with the spacing hx[m] on either side as the reference writes it.  B is
+ * returned as its two terms (convective, diffusive) so that b = 1/tau + Bc + Bd
+ * can be formed in the reference's order. */
+static void ad_coeffs_upwind(const double* h, int m, double vd, double D, double conv, double diff, double* A,
+                             double* Bc, double* Bd, double* C) {
+  double h_1 = h[m - 1], hh = h[m];
+  double hx2 = h[m - 1] + h[m];
+  double hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / 2;
+  if (vd < 0) {
+    *A = diff * (0.5 * (-(D)*hh / hxhxh));
+    *Bc = conv * (0.5 * (-vd / hh));
+    *C = conv * (0.5 * (vd / hh)) + diff * (0.5 * (-(D)*h_1 / hxhxh));
+  } else {
+    *A = conv * (0.5 * (-vd / hh)) + diff * (0.5 * (-(D)*hh / hxhxh));
+    *Bc = conv * (0.5 * (vd / hh));
+    *C = diff * (0.5 * (-(D)*h_1 / hxhxh));
+  }
+  *Bd = diff * (0.5 * (D)*hx2 / hxhxh);
+}
+
 static double ad_dir(const double* h, int m, double vd, double D, double conv, double diff, double fm, double fc,
                      double fp) {
   double A, B, C;
   ad_coeffs(h, m, vd, D, conv, diff, &A, &B, &C);
   return A * fm + B * fc + C * fp;
+}
+static double ad_dir_upwind(const double* h, int m, double vd, double D, double conv, double diff, double fm,
+                            double fc, double fp) {
+  double A, Bc, Bd, C;
+  ad_coeffs_upwind(h, m, vd, D, conv, diff, &A, &Bc, &Bd, &C);
+  return A * fm + (Bc + Bd) * fc + C * fp;
+}
+
+/* The concentration's upwind line coefficients at every Actual point
+ * (SolveTransferEquation_ with schemeType 1, XProblem.cpp:1828-1843): a,
+ * b = 1/tau + convective + diffusive part (in the reference's order), c;
+ * other points untouched. */
+void xfo_adi_upwind_coeffs(int dir, const int32_t* codes, int n1, int n2, int n3, const double* hx,
+                           const double* hy, const double* hz, const double* vecTr, double D, double tau, double* a,
+                           double* b, double* c) {
+  const double* h = dir == 1 ? hx : dir == 2 ? hy : hz;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+        if (codes[q] != ACT) continue;
+        const int m = dir == 1 ? i : dir == 2 ? j : k;
+        double A, Bc, Bd, C;
+        ad_coeffs_upwind(h, m, vecTr[q], D, 1.0, 1.0, &A, &Bc, &Bd, &C);
+        a[q] = A;
+        b[q] = 1 / tau + Bc + Bd;
+        c[q] = C;
+      }
+}
+
+/* The concentration equation's transfer terms on its grid (the loop of
+ * TVPProblem::SolveBySplitting, XProblem.cpp:5886-5935): Actual points take
+ * the averages of the two staggered velocities around them, PreDefined
+ * points on the inlet face (i = 0) the inlet value (inlet[] or 0), every
+ * other term 0.  Returns 0; 1 at the first point of a type the reference
+ * throws on, 2 at an Actual point on the box face (*bad its flat index). */
+int xfo_conc_transfer(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                      const double* w, const double* inlet, double* uTr, double* vTr, double* wTr, double* rpTr,
+                      int64_t* bad) {
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+        const int m = codes[q];
+        uTr[q] = vTr[q] = wTr[q] = rpTr[q] = 0;
+        if (m == ACT) {
+          if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
+            *bad = q;   /* the reference would read outside the velocity boxes */
+            return 2;
+          }
+          /* u box (n1-1) x n2 x n3, v n1 x (n2-1) x n3, w n1 x n2 x (n3-1) */
+          const double* ub = u + ((int64_t)(i - 1) * n2 + j) * n3 + k;
+          const double* vb = v + ((int64_t)i * (n2 - 1) + (j - 1)) * n3 + k;
+          const double* wb = w + ((int64_t)i * n2 + j) * (n3 - 1) + (k - 1);
+          uTr[q] = (ub[0] + ub[(int64_t)n2 * n3]) / 2;
+          vTr[q] = (vb[0] + vb[n3]) / 2;
+          wTr[q] = (wb[0] + wb[1]) / 2;
+        } else if (m == 4) {   /* PreDefined */
+          if (i == 0 && inlet) rpTr[q] = inlet[q];
+        } else if (m != 0 && m != 6) {
+          *bad = q;
+          return 1;
+        }
+      }
+  return 0;
 }
 
 /* The line systems of the split transfer equation as the reference builds
@@ -1222,6 +1310,47 @@ void xfo_adi_first_rhs(const int32_t* codes, int n1, int n2, int n3, const doubl
       }
 }
 
+/* The same first-direction right-hand side in the upwind form (schemeType 1,
+ * XProblem.cpp:1857-1912): each convective difference is the one-sided
+ * difference toward the upstream neighbour over hx[m]. */
+static double up_diff(double vel, double fm, double fc, double fp, double h) {
+  return vel < 0 ? 0.5 * (-vel) * (fp - fc) / h : 0.5 * (-vel) * (fc - fm) / h;
+}
+void xfo_adi_first_rhs_upwind(const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                              const double* hz, const double* f_1, const double* u, const double* v,
+                              const double* w, double dc, const double* rp, double tau, double* f) {
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+        if (codes[q] != ACT) continue;
+        const double hX = hx[i], h_1X = hx[i - 1], hx2X = hx[i - 1] + hx[i];
+        const double hxhxhX = hx[i - 1] * hx[i] * (hx[i - 1] + hx[i]) / 2;
+        const double hY = hy[j], h_1Y = hy[j - 1], hx2Y = hy[j - 1] + hy[j];
+        const double hxhxhY = hy[j - 1] * hy[j] * (hy[j - 1] + hy[j]) / 2;
+        const double hZ = hz[k], h_1Z = hz[k - 1], hx2Z = hz[k - 1] + hz[k];
+        const double hxhxhZ = hz[k - 1] * hz[k] * (hz[k - 1] + hz[k]) / 2;
+        double F = (1 / tau) * f_1[q] + rp[q];
+        F = F + up_diff(u[q], f_1[q - s1], f_1[q], f_1[q + s1], hX);
+        F = F + (0.5 * (dc) * ((hX * f_1[q - s1] - hx2X * f_1[q] + h_1X * f_1[q + s1]) / hxhxhX));
+        double FC = 0, FD = 0;
+        for (int item = 1; item <= 2; item++) {   /* both items read f_1 in the first step */
+          FC = FC + up_diff(v[q], f_1[q - s2], f_1[q], f_1[q + s2], hY);
+          FD = FD + 0.5 * (dc) * ((hY * f_1[q - s2] - hx2Y * f_1[q] + h_1Y * f_1[q + s2]) / hxhxhY);
+        }
+        F = F + FC + FD;
+        FC = 0;
+        FD = 0;
+        for (int item = 1; item <= 2; item++) {
+          FC = FC + up_diff(w[q], f_1[q - 1], f_1[q], f_1[q + 1], hZ);
+          FD = FD + 0.5 * (dc) * ((hZ * f_1[q - 1] - hx2Z * f_1[q] + h_1Z * f_1[q + 1]) / hxhxhZ);
+        }
+        F = F + FC + FD;
+        f[q] = F;
+      }
+}
+
 int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
                       const double* hz, const double* u, const double* v, const double* w, double tau, double D,
                       const double* Dfield, int flags, int n1, int n2, int n3, const double* x, double* y) {
@@ -1242,9 +1371,15 @@ int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double*
         const double fc = x[c];
         const double Dc = Dfield ? Dfield[c] : D;   /* diffCoefVar[i][j][k], XProblem.cpp:3204 */
         double res = itau * fc;
-        res = res + ad_dir(hx, i, u ? u[c] : 0.0, Dc, conv, diff, x[c - s1], fc, x[c + s1]);
-        res = res + ad_dir(hy, j, v ? v[c] : 0.0, Dc, conv, diff, x[c - s2], fc, x[c + s2]);
-        res = res + ad_dir(hz, k, w ? w[c] : 0.0, Dc, conv, diff, x[c - 1], fc, x[c + 1]);
+        if (flags & 4) {   /* the upwind form */
+          res = res + ad_dir_upwind(hx, i, u ? u[c] : 0.0, Dc, conv, diff, x[c - s1], fc, x[c + s1]);
+          res = res + ad_dir_upwind(hy, j, v ? v[c] : 0.0, Dc, conv, diff, x[c - s2], fc, x[c + s2]);
+          res = res + ad_dir_upwind(hz, k, w ? w[c] : 0.0, Dc, conv, diff, x[c - 1], fc, x[c + 1]);
+        } else {
+          res = res + ad_dir(hx, i, u ? u[c] : 0.0, Dc, conv, diff, x[c - s1], fc, x[c + s1]);
+          res = res + ad_dir(hy, j, v ? v[c] : 0.0, Dc, conv, diff, x[c - s2], fc, x[c + s2]);
+          res = res + ad_dir(hz, k, w ? w[c] : 0.0, Dc, conv, diff, x[c - 1], fc, x[c + 1]);
+        }
         y[c] = res;
       }
   return XFO_OK;

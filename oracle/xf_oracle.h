@@ -112,6 +112,15 @@ int xfo_bicg_reference(int64_t R, const int32_t* a_ptr, const int32_t* a_cols, c
 int xfo_apply_advdiff(const int32_t* codes, const double* normals, const double* hx, const double* hy,
                       const double* hz, const double* u, const double* v, const double* w, double tau, double D,
                       const double* Dfield, int flags, int n1, int n2, int n3, const double* x, double* y);
+void xfo_adi_upwind_coeffs(int dir, const int32_t* codes, int n1, int n2, int n3, const double* hx,
+                           const double* hy, const double* hz, const double* vecTr, double D, double tau, double* a,
+                           double* b, double* c);
+void xfo_adi_first_rhs_upwind(const int32_t* codes, int n1, int n2, int n3, const double* hx, const double* hy,
+                              const double* hz, const double* f_1, const double* u, const double* v,
+                              const double* w, double dc, const double* rp, double tau, double* f);
+int xfo_conc_transfer(const int32_t* codes, int n1, int n2, int n3, const double* u, const double* v,
+                      const double* w, const double* inlet, double* uTr, double* vTr, double* wTr, double* rpTr,
+                      int64_t* bad);
 
 /* Momentum right-hand side of one velocity component (XProblem.cpp:
  * 5088-5419): transfer velocities, face viscosity and rp on the component's

@@ -106,3 +106,42 @@ def line_mismatches(G, momentum_fields, adi_line_coeffs, adi_first_rhs):
                 call += 1
             bad[(axis, direction)] = nb
     return bad, call
+
+
+def conc_codes(G):
+    return conc_mask(G["p_codes"], [G[c + "_codes"] for c in "uvw"])
+
+
+def conc_line_mismatches(G, transfer, adi_upwind_coeffs, adi_first_rhs_upwind):
+    """Compares the captured step-2 line systems of the concentration equation
+    (SolveTransferEquation_ with schemeType 1 and diffusion 0, the calls after
+    the three momentum equations') with the upwind coefficients built from
+    `transfer` = (uTr, vTr, wTr, rpTr) on the concentration grid: a, b, c of
+    every Actual row in all three sweeps, f of the first.  Returns
+    ({direction: mismatching rows}, {direction: rows}, index after the last
+    call used)."""
+    lm = G["line_m"]
+    off = np.concatenate([[0], np.cumsum(lm + 1)])
+    call = sum(len(sectors(G[c + "_codes"], d)) for c in "uvw" for d in (1, 2, 3))
+    cc, hh = conc_codes(G), G["hp"]
+    uT, vT, wT, rp = transfer
+    f1 = adi_first_rhs_upwind(cc, *hh, G["s1_cnc"], uT, vT, wT, 0.0, rp, G["tau"])
+    bad, rows = {}, {}
+    for direction, vt in ((1, uT), (2, vT), (3, wT)):
+        a, b, cf = adi_upwind_coeffs(direction, cc, *hh, vt, 0.0, G["tau"])
+        nb = nr = 0
+        for cells in sectors(cc, direction):
+            M, o = int(lm[call]), int(off[call])
+            fl = 0 if cc[cells[0]] in (3, 7) else 1
+            fr = 0 if cc[cells[-1]] in (3, 7) else 1
+            assert M == len(cells) - 1 + fl + fr, "line layout differs from the sector scan"
+            for r in range(1 + fl, M - fr):
+                cell = cells[r - fl]
+                nr += 1
+                if (G["line_a"][o + r], G["line_b"][o + r], G["line_c"][o + r]) != (a[cell], b[cell], cf[cell]):
+                    nb += 1
+                if direction == 1 and G["line_f"][o + r] != f1[cell]:
+                    nb += 1
+            call += 1
+        bad[direction], rows[direction] = nb, nr
+    return bad, rows, call

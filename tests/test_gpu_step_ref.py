@@ -4,7 +4,10 @@ tests/golden/step_channel.npz), with no restatement in between: pressure
 right-hand side (XProblem.cpp:5474-5512), velocity correction
 (:5598-5777), control balance (:5782-5829), the momentum right-hand side
 (:5088-5419) checked through the reference's own ADI line systems
-(:3149-3276), and the device-formatted VTK file (:6132-6345).  Bar:
+(:3149-3276), the concentration equation's transfer terms (:5886-5935) and
+the upwind advection operator's coefficients checked through its captured
+line systems (SolveTransferEquation_, schemeType 1, :1822-1912), and the
+device-formatted VTK file (:6132-6345).  Bar:
 bit-exact, byte-identical file."""
 import os
 
@@ -78,6 +81,69 @@ def test_momentum_rhs_matches_reference_line_systems(ctx, G):
     bad, used = step_ref.line_mismatches(G, fields, O.adi_line_coeffs, O.adi_first_rhs)
     assert all(v == 0 for v in bad.values()), bad
     assert used > 0
+
+
+def conc_fields(ctx, G):
+    gc = xf.Grid(ctx, step_ref.conc_codes(G), *G["hp"])
+    g = grids(ctx, G)
+    out = xf.conc_transfer(gc, g["u"].vec(G["u"]), g["v"].vec(G["v"]), g["w"].vec(G["w"]))
+    return gc, out
+
+
+def test_conc_transfer_matches_reference_line_systems(ctx, G):
+    gc, out = conc_fields(ctx, G)
+    got = tuple(o.download() for o in out)
+    want, st, _ = O.conc_transfer(step_ref.conc_codes(G), G["u"], G["v"], G["w"])
+    assert st == 0
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+    bad, rows, used = step_ref.conc_line_mismatches(G, got, O.adi_upwind_coeffs, O.adi_first_rhs_upwind)
+    assert all(v == 0 for v in bad.values()), bad
+    assert used == len(G["line_m"])
+
+
+def test_upwind_operator_coefficients_match_reference_lines(ctx, G):
+    """The packed form of the upwind operator built on the device from the device's transfer velocities: the
+    neighbour coefficient of every Actual row toward m-1 / m+1 along each direction is the captured line's a / c,
+    bit for bit (the operator's rows evaluated on unit probes)."""
+    gc, (uT, vT, wT, rp) = conc_fields(ctx, G)
+    A = xf.Operator(gc, xf.XF_OP_ADVDIFF)
+    A.set_advection(uT, vT, wT, G["tau"], 0.0, xf.XF_ADV_CONVECTIVE | xf.XF_ADV_DIFFUSIVE | xf.XF_ADV_UPWIND)
+    ptr, cols, vals = xf.PackedOperator(A).csr()
+    inv, _ = gc.rn_map()
+    cc = step_ref.conc_codes(G)
+    n1, n2, n3 = cc.shape
+    coef = {}
+    for r in range(len(ptr) - 1):
+        for t in range(ptr[r], ptr[r + 1]):
+            coef[(r, int(cols[t]))] = vals[t]
+    lm = G["line_m"]
+    off = np.concatenate([[0], np.cumsum(lm + 1)])
+    call = sum(len(step_ref.sectors(G[c + "_codes"], d)) for c in "uvw" for d in (1, 2, 3))
+    checked = 0
+    for direction, step in ((1, (1, 0, 0)), (2, (0, 1, 0)), (3, (0, 0, 1))):
+        for cells in step_ref.sectors(cc, direction):
+            o = int(off[call])
+            for r, cell in enumerate(cells[1:-1], start=2):   # PreNormal ends: row 0 is the extra border row
+                row = inv[cell]
+                lo = tuple(x - s for x, s in zip(cell, step))
+                hi = tuple(x + s for x, s in zip(cell, step))
+                assert coef.get((row, inv[lo]), 0.0) == G["line_a"][o + r]
+                assert coef.get((row, inv[hi]), 0.0) == G["line_c"][o + r]
+                checked += 1
+            call += 1
+    assert checked == 3 * int((cc == 1).sum())
+
+
+def test_conc_transfer_reports_the_first_throwing_point(ctx, G):
+    cc = step_ref.conc_codes(G)
+    cc[0, 3, 4] = 3   # Defined: not implemented for the concentration
+    cc[4, 0, 4] = 5
+    gc = xf.Grid(ctx, cc, *G["hp"])
+    g = grids(ctx, G)
+    with pytest.raises(xf.XFError) as e:
+        xf.conc_transfer(gc, g["u"].vec(G["u"]), g["v"].vec(G["v"]), g["w"].vec(G["w"]))
+    assert e.value.status == xf.capi.XF_ERR_MASK and "(0, 3, 4)" in str(e.value)
 
 
 def test_vtk_matches_reference_file(ctx, G, tmp_path):

@@ -13,7 +13,7 @@ import weakref
 import numpy as np
 
 from . import capi
-from .capi import (XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE, XF_BICG, XF_BICGSTAB, XF_CG,  # noqa: F401
+from .capi import (XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE, XF_ADV_UPWIND, XF_BICG, XF_BICGSTAB, XF_CG,  # noqa: F401
                    XF_CG_REFERENCE, XF_EXACT, XF_F32, XF_F64, XF_IB_FORCE, XF_IB_POS, XF_IB_VEL, XF_MINRES,
                    XF_OP_ADVDIFF, XF_OP_LAPLACE, XF_OP_VARDIV, XF_PREC_FP64, XF_PREC_MIXED, XF_PRECOND_UNET2,
                    XF_ZERO_INACTIVE, XFError)
@@ -443,6 +443,14 @@ def momentum_rhs(axis, gc, u_prev, v_prev, w_prev, vis=None, border=None, force=
     out = out if out is not None else tuple(gc.vec(None) for _ in range(5))
     _check(gc.ctx.h, capi.lib().xf_momentum_rhs(int(axis), u_prev.h, v_prev.h, w_prev.h, _h(vis), _h(border),
                                                  _h(force), *(o.h for o in out)))
+    return out
+
+
+def conc_transfer(gc, u, v, w, inlet=None, out=None):
+    """Transfer terms of the concentration equation on its grid gc (XProblem.cpp:5886-5935): returns the Vecs
+    (uTr, vTr, wTr, rp), reusing `out` when given; inlet is the PreDefined inlet values on the face i = 0."""
+    out = out if out is not None else tuple(gc.vec(None) for _ in range(4))
+    _check(gc.ctx.h, capi.lib().xf_conc_transfer(gc.h, u.h, v.h, w.h, _h(inlet), *(o.h for o in out)))
     return out
 
 

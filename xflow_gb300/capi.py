@@ -15,7 +15,7 @@ XF_ERR_CHECK = 7
 XF_STALL, XF_DIVERGED, XF_NAN, XF_MAXIT, XF_BREAKDOWN = 10, 11, 12, 13, 14
 XF_F64, XF_F32 = 0, 1
 XF_OP_LAPLACE, XF_OP_VARDIV, XF_OP_PACK, XF_OP_ADVDIFF = 0, 1, 2, 3
-XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE = 1, 2
+XF_ADV_CONVECTIVE, XF_ADV_DIFFUSIVE, XF_ADV_UPWIND = 1, 2, 4
 XF_EXACT, XF_ZERO_INACTIVE = 1, 2
 XF_CG, XF_CG_REFERENCE, XF_BICGSTAB, XF_MINRES, XF_BICG, XF_FCG = 0, 1, 2, 3, 4, 5
 XF_PREC_FP64, XF_PREC_MIXED = 0, 1
@@ -36,6 +36,7 @@ EXPORTS = [
     "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
     "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
     "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_dot_noalloc", "xf_transfer_rhs", "xf_border_recalc", "xf_border_follow",
+    "xf_conc_transfer",
 ]
 
 
@@ -126,6 +127,7 @@ def lib():
         L.xf_velocity_correct.argtypes = [C.c_int, vp, vp, vp, C.c_double, vp, vp]
         L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]
         L.xf_momentum_rhs.argtypes = [C.c_int] + [vp] * 11
+        L.xf_conc_transfer.argtypes = [vp] * 9
         L.xf_vtk_write.argtypes = [C.c_char_p] + [vp] * 12
         L.xf_format_fixed6.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.POINTER(C.c_int64)]
         L.xf_npy_write.argtypes = [C.c_char_p, vp]

@@ -182,6 +182,7 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
     a.g.adDf = !op->adD_set ? nullptr : D64 ? (const T*)op->adD64 : (const T*)op->adD32;
     a.g.ad_conv = (op->ad_flags & XF_ADV_CONVECTIVE) ? T(1) : T(0);
     a.g.ad_diff = (op->ad_flags & XF_ADV_DIFFUSIVE) ? T(1) : T(0);
+    a.g.ad_upwind = (op->ad_flags & XF_ADV_UPWIND) ? 1 : 0;
     k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     return;
   }
@@ -293,7 +294,7 @@ extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, 
   if (!op) return XF_ERR_ARG;
   xf_ctx* ctx = op->g->ctx;
   if (op->kind != XF_OP_ADVDIFF) return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_advection: not an advection-diffusion operator");
-  if (!(tau != 0) || (flags & ~(XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE)))
+  if (!(tau != 0) || (flags & ~(XF_ADV_CONVECTIVE | XF_ADV_DIFFUSIVE | XF_ADV_UPWIND)))
     return xf_fail(ctx, XF_ERR_ARG, "xf_op_set_advection: tau must be nonzero and flags XF_ADV_*");
   const xf_vec* vel[3] = {u, v, w};
   for (int d = 0; d < 3; d++)

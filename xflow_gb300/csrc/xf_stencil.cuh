@@ -28,6 +28,7 @@ struct StencilGrid {
   const T* __restrict__ adv0; const T* __restrict__ adv1; const T* __restrict__ adv2;
   const T* __restrict__ adDf;   // per-cell D of the variable-viscosity form, or null
   T ad_itau, ad_D, ad_conv, ad_diff;
+  int ad_upwind;   // the first-order upwind form of the convective term
   int n1, n2, n3;
   int s1, s2;
 };
@@ -202,12 +203,41 @@ __device__ __forceinline__ T ad_dir(const T* __restrict__ h, int m, T vd, T D, T
   return A * fm + B * fc + C * fp;
 }
 
+// The upwind form (schemeType 1 of SolveTransferEquation_, XProblem.cpp:
+// 1828-1843): the convective term takes the upstream neighbour over h[m];
+// the centre coefficient is the convective term plus the diffusive one.
+template <typename T>
+__device__ __forceinline__ T ad_dir_upwind(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T fm, T fc,
+                                           T fp) {
+  const T h_1 = h[m - 1], hh = h[m];
+  const T hx2 = h[m - 1] + h[m];
+  const T hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / T(2);
+  const T Bd = diff * (T(0.5) * (D)*hx2 / hxhxh);
+  T A, Bc, C;
+  if (vd < T(0)) {
+    A = diff * (T(0.5) * (-(D)*hh / hxhxh));
+    Bc = conv * (T(0.5) * (-vd / hh));
+    C = conv * (T(0.5) * (vd / hh)) + diff * (T(0.5) * (-(D)*h_1 / hxhxh));
+  } else {
+    A = conv * (T(0.5) * (-vd / hh)) + diff * (T(0.5) * (-(D)*hh / hxhxh));
+    Bc = conv * (T(0.5) * (vd / hh));
+    C = diff * (T(0.5) * (-(D)*h_1 / hxhxh));
+  }
+  return A * fm + (Bc + Bd) * fc + C * fp;
+}
+
 template <typename T>
 __device__ __forceinline__ T ad_actual(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c) {
   const int s1 = g.s1, s2 = g.s2;
   const T fc = f[c];
   const T D = g.adDf ? g.adDf[c] : g.ad_D;   // diffCoefVar[i][j][k] (XProblem.cpp:3204) or the constant
   T res = g.ad_itau * fc;
+  if (g.ad_upwind) {
+    res = res + ad_dir_upwind<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
+    res = res + ad_dir_upwind<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
+    res = res + ad_dir_upwind<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
+    return res;
+  }
   res = res + ad_dir<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
   res = res + ad_dir<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
   res = res + ad_dir<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);

@@ -7,7 +7,9 @@
 //                       XProblem.cpp:5598-5777;
 //  xf_divergence_max    the "control balance" check, XProblem.cpp:5782-5829;
 //  xf_momentum_rhs      transfer velocities, face viscosity and right-hand
-//                       side of one velocity equation, XProblem.cpp:5088-5419.
+//                       side of one velocity equation, XProblem.cpp:5088-5419;
+//  xf_conc_transfer     transfer velocities and right-hand side of the
+//                       concentration equation, XProblem.cpp:5886-5935.
 //
 // Staggered boxes follow the reference's grids (XStatement.h:127-135): with the
 // pressure box n1 x n2 x n3, the u box is (n1-1) x n2 x n3, v is n1 x (n2-1) x n3
@@ -29,7 +31,7 @@ enum { PC_FICTIVE = 0, PC_ACTUAL = 1, PC_DEFINED = 3, PC_PREDEFINED = 4, PC_NORM
 
 // Error kinds, each the minimum offending cell in iscalars[CHK0 + kind].
 enum { CHK0 = 48, E_RANGE = 0, E_NOTIMPL_P, E_UNKNOWN, E_DEFINED, E_PREDEF_NONE, E_PREDEF_MANY, E_PREDEF_VALUE,
-       E_NOTIMPL_V, E_NOTIMPL_EQ, E_COUNT };
+       E_NOTIMPL_V, E_NOTIMPL_EQ, E_NOTIMPL_C, E_RANGE_C, E_COUNT };
 constexpr long long NO_CELL = 0x7f7f7f7f7f7f7f7fLL;   // cudaMemset byte 0x7f
 constexpr int SL_STEP = 8;                              // reduction slot of xf_divergence_max (and SL_STEP + 1)
 
@@ -414,6 +416,8 @@ static const char* check_message(int kind) {
     case E_PREDEF_MANY: return "PreDefined border condition checking error - actual values count > 1";
     case E_PREDEF_VALUE: return "PreDefined border condition checking error - value incorrect";
     case E_NOTIMPL_V: return "Method is not implemented for this point border type of velocity";
+    case E_NOTIMPL_C: return "Method is not implemented for this point border type of concentration";
+    case E_RANGE_C: return "an Actual concentration cell on the box face (the reference reads outside the velocity boxes)";
     case E_NOTIMPL_EQ:
       return "Method is not implemented for this point border type of velocity and this equation number and this "
              "normal vector";
@@ -582,6 +586,81 @@ extern "C" int xf_momentum_rhs(int axis, const xf_vec* u_prev, const xf_vec* v_p
   if (bad >= 0) return fail_at(ctx, gc, bad, cell, "xf_momentum_rhs");
   XF_LAUNCH_BOX(k_mom_viscous, gc->ncell, bl, 256, a);
   XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// The concentration equation's transfer terms (TVPProblem::SolveBySplitting,
+// XProblem.cpp:5886-5935) on the concentration grid (the pressure box):
+// Actual points the averages of the two staggered velocities around them
+// (u (n1-1) x n2 x n3, v n1 x (n2-1) x n3, w n1 x n2 x (n3-1)) and rp 0;
+// PreDefined points zero velocities and, on the inlet face i = 0, the inlet
+// value (ConcentrationInletCondition; NULL: 0); Fictive and PreNormal points
+// zeros; every other code a throw of the reference.
+template <bool SMALL>
+__global__ void k_conc_transfer(const uint8_t* __restrict__ code, int n1, int n2, int n3,
+                                const double* __restrict__ u, const double* __restrict__ v,
+                                const double* __restrict__ w, const double* __restrict__ inlet,
+                                double* __restrict__ uTr, double* __restrict__ vTr, double* __restrict__ wTr,
+                                double* __restrict__ rpTr, DevScratch* S) {
+  const int64_t n = (int64_t)n1 * n2 * n3;
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int64_t sv1 = (int64_t)(n2 - 1) * n3, sw1 = (int64_t)n2 * (n3 - 1), sw2 = n3 - 1;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int m = code[c];
+    double ut = 0, vt = 0, wt = 0, rp = 0;
+    if (m == PC_ACTUAL) {
+      int i, j, k;
+      split3<SMALL>(c, s1, s2, i, j, k);
+      if (i < 1 || i > n1 - 2 || j < 1 || j > n2 - 2 || k < 1 || k > n3 - 2) {
+        report(S, E_RANGE_C, c);
+        continue;
+      }
+      const int64_t cu = i * s1 + j * s2 + k, cv = i * sv1 + j * s2 + k, cw = i * sw1 + j * sw2 + k;
+      ut = (u[cu - s1] + u[cu]) / 2;
+      vt = (v[cv - s2] + v[cv]) / 2;
+      wt = (w[cw - 1] + w[cw]) / 2;
+    } else if (m == PC_PREDEFINED) {
+      if (inlet && c < s1) rp = inlet[c];   // i == 0
+    } else if (m == PC_DEFINED || m == PC_NORMAL || m == PC_EQUATION || m == PC_PREEQUATION) {
+      report(S, E_NOTIMPL_C, c);
+      continue;
+    } else if (m != PC_FICTIVE && m != PC_PRENORMAL) {
+      report(S, E_UNKNOWN, c);
+      continue;
+    }
+    uTr[c] = ut;
+    vTr[c] = vt;
+    wTr[c] = wt;
+    rpTr[c] = rp;
+  }
+}
+
+extern "C" int xf_conc_transfer(const xf_grid* gc, const xf_vec* u, const xf_vec* v, const xf_vec* w,
+                                const xf_vec* inlet, xf_vec* u_tr, xf_vec* v_tr, xf_vec* w_tr, xf_vec* rp) {
+  if (!gc || !u_tr || !v_tr || !w_tr || !rp) return XF_ERR_ARG;
+  xf_ctx* ctx = gc->ctx;
+  int st;
+  if ((st = check_staggered(ctx, gc, u, v, w, "xf_conc_transfer"))) return st;
+  const xf_vec* outs[4] = {u_tr, v_tr, w_tr, rp};
+  for (int q = 0; q < 4; q++) {
+    if (!is_f64(outs[q]) || outs[q]->g != gc)
+      return xf_fail(ctx, XF_ERR_ARG, "xf_conc_transfer: outputs must be FP64 vectors of the concentration grid");
+    for (int r = q + 1; r < 4; r++)
+      if (outs[q] == outs[r]) return xf_fail(ctx, XF_ERR_ARG, "xf_conc_transfer: outputs must be distinct");
+  }
+  if (inlet && (!is_f64(inlet) || !same_box(inlet, gc)))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_conc_transfer: inlet must be an FP64 box of the concentration grid");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((st = clear_checks(ctx))) return st;
+  XF_LAUNCH_BOX(k_conc_transfer, gc->ncell, grid_blocks(ctx, gc->ncell, 256), 256, gc->code, gc->n1, gc->n2, gc->n3,
+                (const double*)u->data, (const double*)v->data, (const double*)w->data,
+                inlet ? (const double*)inlet->data : nullptr, (double*)u_tr->data, (double*)v_tr->data,
+                (double*)w_tr->data, (double*)rp->data, ctx->scratch);
+  long long chk[E_COUNT], cell;
+  if ((st = read_checks(ctx, chk))) return st;
+  const int kinds[] = {E_RANGE_C, E_NOTIMPL_C, E_UNKNOWN};
+  const int bad = first_error(chk, kinds, 3, &cell);
+  if (bad >= 0) return fail_at(ctx, gc, bad, cell, "xf_conc_transfer");
   return XF_OK;
 }
 
