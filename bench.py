@@ -286,8 +286,12 @@ def main(argv=None):
                     help="time the other rows of the path (time-step passes, IB, Thomas, packed SpMV, VTK)")
     ap.add_argument("--rows-no-cpu", action="store_true", help="with --rows: skip the CPU writer beside the VTK row")
     ap.add_argument("--timeloop", action="store_true",
-                    help="time the GPU time loop: the lid-driven cavity (64^3, 10 steps) and the channel with the "
-                         "immersed icosphere (256x64x64, 100 steps)")
+                    help="time the GPU time loop: the lid-driven cavity (64^3, 10 steps), the channel with the "
+                         "immersed icosphere (256x64x64, 100 steps) and the full loop (512x128x128 with the sphere "
+                         "and a passive scalar, learned pressure solve against a plain FP64 run)")
+    ap.add_argument("--loop-steps", type=int, default=20,
+                    help="with --timeloop: steps of the 512x128x128 loop (each run)")
+    ap.add_argument("--loop-only", action="store_true", help="with --timeloop: the 512x128x128 loop alone")
     argv = sys.argv[1:] if argv is None else argv
     args = ap.parse_args(argv)
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
@@ -718,7 +722,7 @@ def timeloop(args):
     cases = (("lid-driven cavity", tl.cavity(64, re=100.0, tau=1e-3), None, 10),
              ("channel with an immersed sphere", tl.channel(256, 64, 64, re=200.0, tau=2e-3),
               tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4), 100))
-    for label, st, mk, steps in cases:
+    for label, st, mk, steps in (() if args.loop_only else cases):
         loop = tl.SplittingLoop(ctx, st, markers=mk)
         recs = [loop.step() for _ in range(steps)]
         line = {"mode": "time loop", "statement": st["name"], "steps": steps,
@@ -729,7 +733,59 @@ def timeloop(args):
                 "last": recs[-1]}
         print(json.dumps(line), flush=True)
         del loop
+    full_loop(ctx, args.loop_steps)
     return 0
+
+
+def full_loop(ctx, steps):
+    """The full loop: the 512x128x128 channel on [0,4]x[0,1]^2 (8,388,608
+    cells, h = 1/128), inflow u = 1, convective flux-balanced outflow,
+    free-slip walls (lagged zero-gradient tangential values), Re = 200,
+    dt = 2e-3, the icosphere of radius 0.15 at (1, 0.5, 0.5) as 2,562 target
+    markers, and a passive scalar (Schmidt 1) entering as a Gaussian blob of
+    sigma 0.05 on the inlet, transported by the upwind operator under minimal
+    residuals.  Two runs from the same state: the pressure by the learned
+    two-level mixed-precision FCG (the network trained as for the headline),
+    and by plain FP64 CG, both warm-started from the previous step.  One JSON
+    line: per-step ms of both (wall, synchronised, first step apart),
+    iterations, and the drift of the velocity and the scalar between them."""
+    import xflow_gb300 as xf
+    from xflow_gb300 import timeloop as tl
+
+    params, train = train_unet(ctx)
+    base = tl.channel(512, 128, 128, re=200.0, tau=2e-3, outflow="convective", walls="free_slip")
+    mk = tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4)
+    runs = {}
+    for solver in ("learned", "fp64"):
+        st = tl.with_scalar(base, tl.gaussian_inlet(base["p"][0].shape, base["h"], sigma=0.05))
+        loop = tl.SplittingLoop(ctx, st, markers=mk, pressure_solver=solver,
+                                net_params=params if solver == "learned" else None)
+        recs = [loop.step() for _ in range(steps)]
+        runs[solver] = (recs, loop.fields())
+        del loop
+    (lr, lf), (fr, ff) = runs["learned"], runs["fp64"]
+    vel_scale = max(np.abs(f).max() for f in ff[:3])
+    drift_u = max(np.abs(a - b).max() for a, b in zip(lf[:3], ff[:3])) / vel_scale
+    act = base["p"][0] == 1
+    pl, pf = lf[3][act], ff[3][act]
+    drift_p = np.abs((pl - pl.mean()) - (pf - pf.mean())).max() / np.abs(pf - pf.mean()).max()
+    cl, cf = lf[4], ff[4]
+    drift_c = float(np.abs(cl - cf).max())
+
+    def summary(recs):
+        return {"first_step_ms": recs[0]["ms"], "ms_per_step": float(np.mean([r["ms"] for r in recs[1:]])),
+                "pressure_iterations_mean": float(np.mean([r["pressure_iterations"] for r in recs])),
+                "momentum_iterations_mean": float(np.mean([r["momentum_iterations"] for r in recs])),
+                "scalar_iterations_mean": float(np.mean([r["scalar_iterations"] for r in recs])),
+                "pressure_fallbacks": int(sum(r["pressure_fallbacks"] for r in recs)), "last": recs[-1]}
+
+    line = {"mode": "full loop", "statement": st["name"] + ", Gaussian inlet sigma=0.05",
+            "cells": int(act.sum()), "steps": steps, "markers": int(len(mk["pos"])),
+            "learned": summary(lr), "fp64": summary(fr),
+            "drift_vs_fp64": {"velocity_rel": float(drift_u), "pressure_rel": float(drift_p), "scalar_abs": drift_c,
+                              "scalar_max": float(cf[base["p"][0] == 1].max())},
+            "network": train}
+    print(json.dumps(line), flush=True)
 
 
 UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=tuple(range(200, 208)),

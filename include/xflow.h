@@ -305,10 +305,11 @@ int xf_voxelize_mesh(xf_ctx* ctx, int n1, int n2, int n3, const double* x_nodes,
  * xf_momentum_rhs put there), f_prev on inactive points.  FP64 boxes of one
  * velocity grid. */
 int xf_transfer_rhs(const xf_vec* f_prev, const xf_vec* rp, double tau, xf_vec* out);
-/* After that solve: every PreDefined point of vel becomes 2 border - (its one
- * Actual neighbour), as the reference's ADI sweeps recalculate their sector
- * ends (XProblem.cpp:2996-3003), so the border rows hold to rounding before
- * xf_velocity_correct checks them.  XF_ERR_MASK for a PreDefined point with
+/* After that solve, the sector ends as the reference's ADI sweeps recalculate
+ * them (XProblem.cpp:2975-3003): every Defined point with an Actual neighbour
+ * takes its border value, and every PreDefined point becomes 2 border - (its
+ * one Actual neighbour), so the border rows hold (exactly, and to rounding)
+ * before xf_velocity_correct checks them.  XF_ERR_MASK for a PreDefined point with
  * no or several Actual neighbours (the reference's throws). */
 int xf_border_recalc(const xf_vec* border, xf_vec* vel);
 /* A zero-gradient (outflow) face for a time loop: each PreDefined point of vel's
@@ -318,6 +319,17 @@ int xf_border_recalc(const xf_vec* border, xf_vec* vel);
  * counterpart in the reference, whose border values come from its statement's
  * GetBorderCondition* hooks. */
 int xf_border_follow(const xf_vec* vel, xf_vec* border, int axis, int side);
+/* A convective outflow for a time loop, on the high face of `axis` (1..3) of
+ * vel's grid for the component normal to that face (its Defined points): each
+ * border value b takes one explicit upwind step of db/dt + speed db/dn = 0,
+ * b' = b - (speed tau / h) (b - v_a), h the spacing across the face and v_a
+ * the point's neighbour inside; then all of them shift by one amount so that
+ * the outlet's area-weighted sum equals the inlet's (the Defined points of the
+ * low face), which keeps an all-Neumann pressure system consistent.  Areas
+ * are the products of the face cells' widths.  No counterpart in the
+ * reference, whose border values come from its statement's hooks.  FP64
+ * vectors of one velocity grid; one block, deterministic. */
+int xf_outflow_convective(const xf_vec* vel, xf_vec* border, int axis, double speed, double tau);
 /* Pressure right-hand side (XProblem.cpp:5474-5512): Fictive 0; Actual
  * -(rho^2 du/dx + dv/dy + dw/dz) / tau; PreDefined the border value. */
 int xf_pressure_rhs(const xf_grid* gp, const xf_vec* u, const xf_vec* v, const xf_vec* w, const xf_vec* density,

@@ -1,7 +1,8 @@
 """GPU parity of the implicit advection-diffusion operator (momentum /
 transport: the reference's ADI line coefficients, XProblem.cpp:1236-1238,
-summed over the three directions) against the oracle's restatement, and its
-solves by the reference Krylov methods.
+summed over the three directions; with XF_ADV_UPWIND the upwind scheme of
+the concentration equation, :1828-1843) against the oracle's restatement,
+and its solves by the reference Krylov methods.
 
 Bars: FP64 rows bit-exact; FP32 rows within 2e-6 x max|y|; the packed form
 within 1e-13 x max|y| (row dot in pack order vs the stencil's expression
@@ -41,7 +42,7 @@ def case(ctx, shape=(12, 11, 13), seed=3, tau=1e-2, D=0.05, flags=3):
     return g, A, og, vel, rng
 
 
-@pytest.mark.parametrize("flags", [1, 2, 3])
+@pytest.mark.parametrize("flags", [1, 2, 3, 5, 7])   # 4: the upwind form
 def test_advdiff_rows_match_oracle(ctx, flags):
     g, A, og, vel, rng = case(ctx, flags=flags)
     x = rng.standard_normal(g.shape)
@@ -81,6 +82,21 @@ def test_advdiff_solves(ctx):
     st = xf.solve(P, x, bv, method=xf.XF_BICG, atol=1e-9)
     assert st.status == capi.XF_OK, st.status
     assert np.abs(x.download()[sm] - xt[sm]).max() <= 1e-6 * np.abs(xt[sm]).max()
+
+
+def test_upwind_transport_solves(ctx):
+    """The concentration equation's operator (upwind convection plus diffusion) under minimal residuals and
+    BiCGStab recovers a manufactured solution."""
+    g, A, og, vel, rng = case(ctx, shape=(18, 16, 17), seed=11, flags=7)
+    sm = og.smask.astype(bool)
+    xt = np.where(sm, rng.standard_normal(g.shape), 0.0)
+    b = O.apply_advdiff(og, xt, *vel, 1e-2, 0.05, 7)
+    bv = g.vec(b)
+    for method in (xf.XF_MINRES, xf.XF_BICGSTAB):
+        x = g.vec(np.zeros(g.shape))
+        st = xf.solve(A, x, bv, method=method, atol=1e-10)
+        assert st.status == capi.XF_OK, (method, st.status)
+        assert np.abs(x.download()[sm] - xt[sm]).max() <= 1e-6 * np.abs(xt[sm]).max()
 
 
 def test_advdiff_needs_coefficients(ctx):

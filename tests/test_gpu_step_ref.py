@@ -17,6 +17,7 @@ import pytest
 import step_ref
 import xflow_gb300 as xf
 from oracle import oracle as O
+from xflow_gb300 import timeloop as tl
 
 pytestmark = pytest.mark.gpu
 
@@ -84,7 +85,12 @@ def test_momentum_rhs_matches_reference_line_systems(ctx, G):
 
 
 def conc_fields(ctx, G):
-    gc = xf.Grid(ctx, step_ref.conc_codes(G), *G["hp"])
+    """The concentration grid (Actual interior, PreNormal faces with their normals; the box edges, which no line
+    reaches, Fictive) and the device's transfer terms on it."""
+    codes, nrm = tl.scalar_box(G["p_codes"].shape)
+    ref = step_ref.conc_codes(G)
+    assert np.array_equal(codes == 1, ref == 1) and np.all(ref[codes == 6] == 6)
+    gc = xf.Grid(ctx, codes, *G["hp"], nrm)
     g = grids(ctx, G)
     out = xf.conc_transfer(gc, g["u"].vec(G["u"]), g["v"].vec(G["v"]), g["w"].vec(G["w"]))
     return gc, out

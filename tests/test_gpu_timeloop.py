@@ -61,3 +61,79 @@ def test_channel_with_an_immersed_sphere_runs_and_stays_bounded():
             assert rec["divergence_max"] * (4.0 / 64) < 0.05, rec
     finally:
         ctx.close()
+
+
+def scalar_channel(nx, ny, nz):
+    st = tl.channel(nx, ny, nz, tau=2e-3, outflow="convective", walls="free_slip")
+    return tl.with_scalar(st, tl.gaussian_inlet(st["p"][0].shape, st["h"], sigma=0.15))
+
+
+def test_scalar_channel_three_steps_match_the_cpu_restatement():
+    """The channel with a convective, flux-balanced outflow, free-slip walls
+    (lagged zero-gradient tangential border values) and a passive scalar
+    entering as a Gaussian blob on the inlet: three steps against the CPU
+    restatement (the oracle's pinned passes, its restatement of the outflow
+    pass, numpy solves).  Bar: velocities within 1e-7 of their range,
+    zero-mean pressure within 1e-6, scalar within 1e-7 of its inlet peak;
+    the outlet's flux equals the inlet's to rounding."""
+    import copy
+
+    import timeloop_cpu
+
+    ctx = xf.Context(0)
+    try:
+        st = scalar_channel(24, 8, 8)
+        cpu = copy.deepcopy(st)
+        loop = tl.SplittingLoop(ctx, st, momentum_rtol=1e-13, pressure_rtol=1e-11, pressure_solver="fp64",
+                                scalar_rtol=1e-13)
+        vel = [v.copy() for v in cpu["vel0"]]
+        p = np.zeros(cpu["p"][0].shape)
+        c = cpu["scalar"]["c0"].copy()
+        act_p = cpu["p"][0] == 1
+        for k in range(3):
+            rec = loop.step()
+            vel, p, (div, ijk), c = timeloop_cpu.step(cpu, vel, p, scalar=c)
+            got = loop.fields()
+            for a in range(3):
+                m = cpu["comps"][a][0] != 0
+                scale = np.abs(vel[a][m]).max()
+                assert np.abs(got[a][m] - vel[a][m]).max() <= 1e-7 * scale, (k, a)
+            gp, cp = got[3][act_p], p[act_p]
+            d = (gp - gp.mean()) - (cp - cp.mean())
+            assert np.abs(d).max() <= 1e-6 * np.abs(cp - cp.mean()).max(), k
+            mc = cpu["scalar"]["codes"] != 0
+            assert np.abs(got[4][mc] - c[mc]).max() <= 1e-7, k
+            assert rec["scalar_iterations"] > 0 and rec["pressure_iterations"] > 0
+            u = got[0]
+            assert abs(u[-1, 1:-1, 1:-1].sum() - u[0, 1:-1, 1:-1].sum()) <= 1e-12 * u[0, 1:-1, 1:-1].sum()
+        inner = got[4][cpu["scalar"]["codes"] == 1]
+        assert 0.01 < inner.max() <= 1.0 and inner.min() >= -1e-12   # the blob entered, bounded
+    finally:
+        ctx.close()
+
+
+def test_learned_and_mixed_pressure_solves_stay_on_the_fp64_trajectory():
+    """Warm-started pressure solves by mixed-precision CG and by the learned
+    two-level FCG (untrained network: its fallback keeps it convergent) give
+    the plain FP64 run's fields after three steps, within a few times the
+    pressure tolerance (1e-8)."""
+    ctx = xf.Context(0)
+    try:
+        runs = {}
+        for solver in ("fp64", "mixed", "learned"):
+            st = scalar_channel(32, 16, 16)
+            loop = tl.SplittingLoop(ctx, st, pressure_solver=solver,
+                                    net_params=xf.unet_init_params(1) if solver == "learned" else None)
+            for _ in range(3):
+                rec = loop.step()
+            runs[solver] = loop.fields()
+            assert rec["pressure_iterations"] > 0, solver
+            del loop
+        ref = runs["fp64"]
+        for solver in ("mixed", "learned"):
+            for a in range(3):
+                scale = np.abs(ref[a]).max()
+                assert np.abs(runs[solver][a] - ref[a]).max() <= 1e-6 * scale, (solver, a)
+            assert np.abs(runs[solver][4] - ref[4]).max() <= 1e-6, solver
+    finally:
+        ctx.close()

@@ -36,12 +36,81 @@ def bicgstab(apply, x, b, act, tol):
     raise RuntimeError("CPU BiCGStab did not converge")
 
 
-def step(st, vel, p, tol_mom=1e-12, rtol_p=1e-12):
-    """One time step of the statement `st` (timeloop.cavity / channel, no
-    markers) from the velocity boxes `vel` and pressure `p`; returns the new
-    velocity boxes, the pressure and the control balance."""
+def face(shape, axis, side):
+    """Index of the face plane (axis 1..3, side 0 low / 1 high) of a box."""
+    sl = [slice(None)] * 3
+    sl[axis - 1] = 0 if side == 0 else shape[axis - 1] - 1
+    return tuple(sl)
+
+
+def inward(shape, axis, side):
+    """Index of the layer next to that face, inside."""
+    sl = [slice(None)] * 3
+    sl[axis - 1] = 1 if side == 0 else shape[axis - 1] - 2
+    return tuple(sl)
+
+
+def border_follow(codes, vel, bc, axis, side):
+    """PreDefined points of the face take their Actual neighbour's value as border value (xf_border_follow)."""
+    f, n = face(codes.shape, axis, side), inward(codes.shape, axis, side)
+    m = (codes[f] == 4) & (codes[n] == 1)
+    bc[f] = np.where(m, vel[n], bc[f])
+
+
+def outflow_convective(codes, vel, bc, h, axis, speed, tau):
+    """xf_outflow_convective: the Defined outlet values (high face of `axis`) take an upwind step of
+    db/dt + speed db/dn = 0, then shift so that their area-weighted sum equals the inlet face's.  The sums
+    are formed in float64 by numpy (another order than the device's tree): agreement to rounding."""
+    f0, f1, n1 = face(codes.shape, axis, 0), face(codes.shape, axis, 1), inward(codes.shape, axis, 1)
+    oth = [d for d in range(3) if d != axis - 1]
+    wid = []
+    for d in oth:
+        hd, n = h[d], codes.shape[d]
+        w = np.zeros(n)
+        w[1:n - 1] = (hd[:-1] + hd[1:])[: n - 2] / 2
+        wid.append(w)
+    area = wid[0][:, None] * wid[1][None, :]
+    c = speed * tau / h[axis - 1][codes.shape[axis - 1] - 2]
+    m_in, m_out = codes[f0] == 3, codes[f1] == 3
+    b = bc[f1].copy()
+    b = np.where(m_out, b - c * (b - vel[n1]), b)
+    s_in = (area * bc[f0])[m_in].sum()
+    s_out, a_out = (area * b)[m_out].sum(), area[m_out].sum()
+    b = np.where(m_out, b + (s_in - s_out) / a_out, b)
+    bc[f1] = b
+
+
+def scalar_step(sc, hp, vel, c, tau, tol=1e-13):
+    """The concentration equation (XProblem.cpp:5850-5977) from the corrected velocities, with the upwind
+    transfer operator unsplit and solved by BiCGStab (the GPU uses minimal residuals)."""
+    codes = sc["codes"]
+    (uT, vT, wT, rp), s, _ = O.conc_transfer(codes, vel[0], vel[1], vel[2], inlet=sc["inlet"])
+    assert s == 0
+    act = np.isin(codes, ACTIVE)
+    rhs = np.where(codes == 1, (1 / tau) * c + rp, np.where(act, rp, c))
+    og = O.Grid(codes, sc["nrm"], *hp)
+    apply = lambda x: O.apply_advdiff(og, x, uT, vT, wT, tau, sc["D"], 7)  # noqa: E731
+    x, _ = bicgstab(apply, c.copy(), rhs, act, tol * np.abs(rhs[act]).max())
+    return x
+
+
+def step(st, vel, p, tol_mom=1e-12, rtol_p=1e-12, scalar=None):
+    """One time step of the statement `st` (timeloop.cavity / channel /
+    with_scalar, no markers) from the velocity boxes `vel`, pressure `p` (and
+    the scalar box `scalar`); returns the new velocity boxes, the pressure and the control
+    balance (and the scalar).  The border values of `st` are updated in
+    place, as the GPU loop updates its border boxes."""
     tau = st["tau"]
     pc, pn, pbc, hp = st["p"]
+    for axis, side in st.get("follow", ()):
+        for a, (codes, _, bc) in enumerate(st["comps"]):
+            border_follow(codes, vel[a], bc, axis, side)
+    if "convective" in st:
+        axis, speed = st["convective"]
+        codes, _, bc = st["comps"][axis - 1]
+        hh = [hp[d] for d in range(3)]
+        hh[axis - 1] = 0.5 * (hp[axis - 1][:-1] + hp[axis - 1][1:])
+        outflow_convective(codes, vel[axis - 1], bc, hh, axis, speed, tau)
     hs = []
     mid = []
     for a, (codes, nrm, bc) in enumerate(st["comps"]):
@@ -57,6 +126,10 @@ def step(st, vel, p, tol_mom=1e-12, rtol_p=1e-12):
         og = O.Grid(codes, nrm, *hh)
         apply = lambda x: O.apply_advdiff(og, x, uT, vT, wT, tau, 0.0, 3, Dfield=visT)  # noqa: E731
         x, _ = bicgstab(apply, vel[a].copy(), rhs, act, tol_mom * np.abs(rhs[act]).max())
+        for c in zip(*np.nonzero(codes == 3)):   # Defined sector ends take their border value
+            nb = [tuple(np.add(c, d)) for d in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))]
+            if any(all(0 <= q[t] < codes.shape[t] for t in range(3)) and codes[q] == 1 for q in nb):
+                x[c] = bc[c]
         for c in zip(*np.nonzero(codes == 4)):   # the PreDefined border values exact
             nb = [tuple(np.add(c, d)) for d in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))]
             nb = [q for q in nb if all(0 <= q[t] < codes.shape[t] for t in range(3)) and codes[q] == 1]
@@ -72,4 +145,6 @@ def step(st, vel, p, tol_mom=1e-12, rtol_p=1e-12):
         assert s == 0
         out.append(v)
     div = O.divergence_max(pc, out[0], out[1], out[2], hs[0][0], hs[1][1], hs[2][2])
+    if scalar is not None:
+        return out, p, div, scalar_step(st["scalar"], hp, out, scalar, tau)
     return out, p, div

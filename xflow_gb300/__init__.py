@@ -429,6 +429,13 @@ def border_follow(vel, border, axis, side):
     return border
 
 
+def outflow_convective(vel, border, axis, speed, tau):
+    """border |= on the high face of `axis`, the Defined outlet values advanced by db/dt + speed db/dn = 0 and
+    shifted so the outlet's flux equals the inlet's (a convective outflow with mass balance)."""
+    _check(vel.grid.ctx.h, capi.lib().xf_outflow_convective(vel.h, border.h, int(axis), float(speed), float(tau)))
+    return border
+
+
 def divergence_max(gp, u, v, w):
     """(max |div u| over Actual cells, (i, j, k)) as the control balance (XProblem.cpp:5782-5829)."""
     val = C.c_double()

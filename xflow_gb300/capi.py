@@ -36,7 +36,7 @@ EXPORTS = [
     "xf_tc_gemm_bf16", "xf_conv3d_bf16", "xf_conv_status", "xf_unet_create", "xf_unet_destroy",
     "xf_unet_param_count", "xf_unet_set_params", "xf_unet_get_params", "xf_unet_get_grads", "xf_unet_apply",
     "xf_unet_train_step", "xf_solve_fcg", "xf_profile_cg_kernels", "xf_selftest_division", "xf_voxelize_mesh", "xf_cheb_factors_host", "xf_dot_noalloc", "xf_transfer_rhs", "xf_border_recalc", "xf_border_follow",
-    "xf_conc_transfer",
+    "xf_conc_transfer", "xf_outflow_convective",
 ]
 
 
@@ -128,6 +128,7 @@ def lib():
         L.xf_divergence_max.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), vp]
         L.xf_momentum_rhs.argtypes = [C.c_int] + [vp] * 11
         L.xf_conc_transfer.argtypes = [vp] * 9
+        L.xf_outflow_convective.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double]
         L.xf_vtk_write.argtypes = [C.c_char_p] + [vp] * 12
         L.xf_format_fixed6.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.POINTER(C.c_int64)]
         L.xf_npy_write.argtypes = [C.c_char_p, vp]

@@ -726,10 +726,30 @@ extern "C" int xf_transfer_rhs(const xf_vec* f_prev, const xf_vec* rp, double ta
   return XF_OK;
 }
 
-// The border values of an implicit transfer solve made exact: every
-// PreDefined point becomes 2 b - (its Actual neighbour), as the reference's
-// ADI sweeps recalculate their sector ends (XProblem.cpp:2996-3003), so that
-// the velocity correction's border check holds to rounding.
+// Defined points that end a line sector (an Actual neighbour along some axis)
+// take their border value, as the ADI sweeps assign them (XProblem.cpp:
+// 2975-2980 and the sector end after it).
+template <bool SMALL>
+__global__ void k_defined_ends(const uint8_t* __restrict__ code, int n1, int n2, int n3,
+                               const double* __restrict__ border, double* __restrict__ vel) {
+  const int64_t n = (int64_t)n1 * n2 * n3;
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (code[c] != PC_DEFINED) continue;
+    int i, j, k;
+    split3<SMALL>(c, s1, s2, i, j, k);
+    const bool end = (i > 0 && code[c - s1] == PC_ACTUAL) || (i < n1 - 1 && code[c + s1] == PC_ACTUAL) ||
+                     (j > 0 && code[c - s2] == PC_ACTUAL) || (j < n2 - 1 && code[c + s2] == PC_ACTUAL) ||
+                     (k > 0 && code[c - 1] == PC_ACTUAL) || (k < n3 - 1 && code[c + 1] == PC_ACTUAL);
+    if (end) vel[c] = border ? border[c] : 0.0;
+  }
+}
+
+// The border values of an implicit transfer solve made exact, as the
+// reference's ADI sweeps recalculate their sector ends (XProblem.cpp:
+// 2975-3003): Defined sector ends take the border value, and every PreDefined
+// point becomes 2 b - (its Actual neighbour), so that the velocity
+// correction's border checks hold (exactly, and to rounding).
 extern "C" int xf_border_recalc(const xf_vec* border, xf_vec* vel) {
   if (!vel) return XF_ERR_ARG;
   const xf_grid* g = vel->g;
@@ -739,6 +759,8 @@ extern "C" int xf_border_recalc(const xf_vec* border, xf_vec* vel) {
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   int st;
   if ((st = clear_checks(ctx))) return st;
+  XF_LAUNCH_BOX(k_defined_ends, g->ncell, grid_blocks(ctx, g->ncell, 256), 256, g->code, g->n1, g->n2, g->n3,
+                border ? (const double*)border->data : nullptr, (double*)vel->data);
   XF_LAUNCH_BOX(k_vel_pass2, g->ncell, grid_blocks(ctx, g->ncell, 256), 256, g->code, g->n1, g->n2, g->n3,
                 (const double*)vel->data, (double*)vel->data, border ? (const double*)border->data : nullptr,
                 ctx->scratch, false);
@@ -786,6 +808,89 @@ extern "C" int xf_border_follow(const xf_vec* vel, xf_vec* border, int axis, int
   const int64_t np = axis == 1 ? (int64_t)g->n2 * g->n3 : axis == 2 ? (int64_t)g->n1 * g->n3 : (int64_t)g->n1 * g->n2;
   k_border_follow<<<grid_blocks(ctx, np, 256), 256, 0, ctx->stream>>>(g->code, g->n1, g->n2, g->n3, axis - 1, side,
                                                                       (const double*)vel->data, (double*)border->data);
+  XF_CUDA(ctx, cudaGetLastError());
+  return XF_OK;
+}
+
+// A convective outflow on the high face of `axis` for the component normal to
+// it: one block walks the face plane, advances each Defined outlet point's
+// border value by an explicit upwind step of dv/dt + speed dv/dn = 0, sums
+// the area-weighted outlet and inlet (low face) values and the outlet area in
+// a fixed-order tree, then shifts the outlet so the two fluxes balance.
+constexpr int OF_THREADS = 1024;
+
+__device__ __forceinline__ double face_width(const double* __restrict__ h, int t, int n) {
+  return (t >= 1 && t <= n - 2) ? (h[t - 1] + h[t]) / 2 : 0.0;   // the cell around node t
+}
+
+__global__ void __launch_bounds__(OF_THREADS)
+    k_outflow_convective(const uint8_t* __restrict__ code, int n1, int n2, int n3, int axis,
+                         const double* __restrict__ vel, double* __restrict__ border, const double* __restrict__ hx,
+                         const double* __restrict__ hy, const double* __restrict__ hz, double speed_tau) {
+  __shared__ double red[3][OF_THREADS];
+  const int64_t s1 = (int64_t)n2 * n3, s2 = n3;
+  const int na = axis == 0 ? n1 : axis == 1 ? n2 : n3;
+  const int la = axis == 0 ? n2 : n1, lb = axis == 2 ? n2 : n3;   // the face plane's two other axes
+  const double* ha = axis == 0 ? hy : hx;
+  const double* hb = axis == 2 ? hy : hz;
+  const double* hn = axis == 0 ? hx : axis == 1 ? hy : hz;
+  const int64_t step = axis == 0 ? s1 : axis == 1 ? s2 : 1;
+  const int64_t np = (int64_t)la * lb;
+  const double c = speed_tau / hn[na - 2];   // Courant number across the face
+  const int tid = threadIdx.x;
+  double in_sum = 0, out_sum = 0, out_area = 0;
+  for (int64_t q = tid; q < np; q += OF_THREADS) {
+    const int x = (int)(q / lb), y = (int)(q - (int64_t)x * lb);
+    int64_t c0;
+    if (axis == 0) c0 = x * s2 + y;
+    else if (axis == 1) c0 = x * s1 + y;
+    else c0 = x * s1 + y * s2;
+    const int64_t c1 = c0 + (int64_t)(na - 1) * step;
+    const double w = face_width(ha, x, la) * face_width(hb, y, lb);
+    if (code[c0] == PC_DEFINED) in_sum += w * border[c0];
+    if (code[c1] == PC_DEFINED) {
+      double v = border[c1];
+      v = v - c * (v - vel[c1 - step]);
+      border[c1] = v;
+      out_sum += w * v;
+      out_area += w;
+    }
+  }
+  red[0][tid] = in_sum;
+  red[1][tid] = out_sum;
+  red[2][tid] = out_area;
+  __syncthreads();
+  for (int h = OF_THREADS / 2; h > 0; h >>= 1) {
+    if (tid < h)
+      for (int t = 0; t < 3; t++) red[t][tid] += red[t][tid + h];
+    __syncthreads();
+  }
+  const double shift = red[2][0] > 0 ? (red[0][0] - red[1][0]) / red[2][0] : 0.0;
+  for (int64_t q = tid; q < np; q += OF_THREADS) {   // each thread revisits its own points
+    const int x = (int)(q / lb), y = (int)(q - (int64_t)x * lb);
+    int64_t c0;
+    if (axis == 0) c0 = x * s2 + y;
+    else if (axis == 1) c0 = x * s1 + y;
+    else c0 = x * s1 + y * s2;
+    const int64_t c1 = c0 + (int64_t)(na - 1) * step;
+    if (code[c1] == PC_DEFINED) border[c1] += shift;
+  }
+}
+
+extern "C" int xf_outflow_convective(const xf_vec* vel, xf_vec* border, int axis, double speed, double tau) {
+  if (!vel || !border) return XF_ERR_ARG;
+  const xf_grid* g = vel->g;
+  xf_ctx* ctx = g->ctx;
+  if (axis < 1 || axis > 3) return xf_fail(ctx, XF_ERR_ARG, "xf_outflow_convective: axis 1..3 expected");
+  if (!is_f64(vel) || !is_f64(border) || !same_box(border, g) || border->g != g)
+    return xf_fail(ctx, XF_ERR_ARG, "xf_outflow_convective: FP64 vectors of one grid expected");
+  const int na = axis == 1 ? g->n1 : axis == 2 ? g->n2 : g->n3;
+  if (na < 3 || !(speed >= 0) || !(tau > 0))
+    return xf_fail(ctx, XF_ERR_ARG, "xf_outflow_convective: a box of 3 layers or more, speed >= 0 and tau > 0");
+  XF_CUDA(ctx, cudaSetDevice(ctx->device));
+  k_outflow_convective<<<1, OF_THREADS, 0, ctx->stream>>>(g->code, g->n1, g->n2, g->n3, axis - 1,
+                                                          (const double*)vel->data, (double*)border->data, g->hx,
+                                                          g->hy, g->hz, speed * tau);
   XF_CUDA(ctx, cudaGetLastError());
   return XF_OK;
 }
