@@ -85,11 +85,15 @@ def test_momentum_rhs_matches_reference_line_systems(ctx, G):
 
 
 def conc_fields(ctx, G):
-    """The concentration grid (Actual interior, PreNormal faces with their normals; the box edges, which no line
-    reaches, Fictive) and the device's transfer terms on it."""
-    codes, nrm = tl.scalar_box(G["p_codes"].shape)
-    ref = step_ref.conc_codes(G)
-    assert np.array_equal(codes == 1, ref == 1) and np.all(ref[codes == 6] == 6)
+    """The reference's concentration grid with normals for its PreNormal rows (the outward normal on the box
+    faces; along x for the interior corner point that no momentum box interior covers) and the box edges, which
+    no line reaches, Fictive; and the device's transfer terms on it."""
+    box, nrm = tl.scalar_box(G["p_codes"].shape)
+    codes = step_ref.conc_codes(G)
+    codes[box == 0] = 0
+    for c in zip(*np.nonzero((codes == 6) & (box == 1))):
+        assert codes[c[0] - 1, c[1], c[2]] == 1
+        nrm[c] = (1.0, 0.0, 0.0)
     gc = xf.Grid(ctx, codes, *G["hp"], nrm)
     g = grids(ctx, G)
     out = xf.conc_transfer(gc, g["u"].vec(G["u"]), g["v"].vec(G["v"]), g["w"].vec(G["w"]))
