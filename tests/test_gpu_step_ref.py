@@ -135,11 +135,11 @@ def test_upwind_operator_coefficients_match_reference_lines(ctx, G):
         for cells in step_ref.sectors(cc, direction):
             o = int(off[call])
             for r, cell in enumerate(cells[1:-1], start=2):   # PreNormal ends: row 0 is the extra border row
-                row = inv[cell]
+                row = inv[cell] - 1   # Rn indices are 1-based, the CSR 0-based
                 lo = tuple(x - s for x, s in zip(cell, step))
                 hi = tuple(x + s for x, s in zip(cell, step))
-                assert coef.get((row, inv[lo]), 0.0) == G["line_a"][o + r]
-                assert coef.get((row, inv[hi]), 0.0) == G["line_c"][o + r]
+                assert coef.get((row, inv[lo] - 1), 0.0) == G["line_a"][o + r]
+                assert coef.get((row, inv[hi] - 1), 0.0) == G["line_c"][o + r]
                 checked += 1
             call += 1
     assert checked == 3 * int((cc == 1).sum())

@@ -121,7 +121,7 @@ def test_learned_and_mixed_pressure_solves_stay_on_the_fp64_trajectory():
     try:
         runs = {}
         for solver in ("fp64", "mixed", "learned"):
-            st = scalar_channel(32, 16, 16)
+            st = scalar_channel(64, 16, 16)   # h = 1/16 on every axis: the two-level solver wants a uniform grid
             loop = tl.SplittingLoop(ctx, st, pressure_solver=solver,
                                     net_params=xf.unet_init_params(1) if solver == "learned" else None)
             for _ in range(3):
