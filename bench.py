@@ -743,8 +743,8 @@ def full_loop(ctx, steps):
     free-slip walls (lagged zero-gradient tangential values), Re = 200,
     dt = 2e-3, the icosphere of radius 0.15 at (1, 0.5, 0.5) as 2,562 target
     markers, and a passive scalar (Schmidt 1) entering as a Gaussian blob of
-    sigma 0.05 on the inlet, transported by the upwind operator under minimal
-    residuals.  Two runs from the same state: the pressure by the learned
+    sigma 0.05 on the inlet, transported by the upwind operator under
+    BiCGStab.  Two runs from the same state: the pressure by the learned
     two-level mixed-precision FCG (the network trained as for the headline),
     and by plain FP64 CG, both warm-started from the previous step.  One JSON
     line: per-step ms of both (wall, synchronised, first step apart),

@@ -121,7 +121,8 @@ def test_learned_and_mixed_pressure_solves_stay_on_the_fp64_trajectory():
     try:
         runs = {}
         for solver in ("fp64", "mixed", "learned"):
-            st = scalar_channel(64, 16, 16)   # h = 1/16 on every axis: the two-level solver wants a uniform grid
+            st = scalar_channel(128, 32, 32)   # h = 1/32 on every axis (the two-level solver's coarse grid is
+            # isotropic), coarse interior 32x8x8 (the network wants 8 or more cells per axis)
             loop = tl.SplittingLoop(ctx, st, pressure_solver=solver,
                                     net_params=xf.unet_init_params(1) if solver == "learned" else None)
             for _ in range(3):

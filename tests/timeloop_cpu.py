@@ -82,7 +82,7 @@ def outflow_convective(codes, vel, bc, h, axis, speed, tau):
 
 def scalar_step(sc, hp, vel, c, tau, tol=1e-13):
     """The concentration equation (XProblem.cpp:5850-5977) from the corrected velocities, with the upwind
-    transfer operator unsplit and solved by BiCGStab (the GPU uses minimal residuals)."""
+    transfer operator unsplit and solved by BiCGStab, as on the GPU."""
     codes = sc["codes"]
     (uT, vT, wT, rp), s, _ = O.conc_transfer(codes, vel[0], vel[1], vel[2], inlet=sc["inlet"])
     assert s == 0

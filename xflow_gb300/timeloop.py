@@ -18,7 +18,7 @@ the GPU, every pass through the C ABI of include/xflow.h:
     xf_conc_transfer     transfer velocities from the corrected velocities,
                          the inlet values on the PreDefined inlet points
     XF_OP_ADVDIFF solve  the upwind transfer operator (SolveTransferEquation_'s
-                         scheme), unsplit, minimal residuals
+                         scheme), unsplit, BiCGStab
 
 With markers, each momentum equation's force is the immersed boundary's
 (TImmersedBoundaryProblem::GetForce order, XProblem.cpp:8350-8353):
@@ -339,9 +339,12 @@ class SplittingLoop:
                                    capi.XF_ADV_CONVECTIVE | capi.XF_ADV_DIFFUSIVE | capi.XF_ADV_UPWIND)
             xf.transfer_rhs(self.c, rp, tau, self.crhs)
             self.cnext.assign(self.c)
-            # minimal residuals with the reference's stop rule, ||r||_2 <= atol, relative to the right-hand side
-            s = xf.solve(self.cop, self.cnext, self.crhs, method=xf.XF_MINRES,
-                         atol=self.scalar_rtol * self.crhs.norm(), maxit=20000)
+            # BiCGStab, max |r| <= atol relative to the right-hand side, as the momentum equations.  Minimal
+            # residuals (x += alpha r) stalls here: the border rows (semi-sums of scale 1/2, normal differences
+            # of scale 1/h) sit beside Actual rows of scale 1/tau, and at 128x32x32 it had gained one decade
+            # in 400 iterations where BiCGStab reaches 1e-10 in about 110.
+            s = xf.solve(self.cop, self.cnext, self.crhs, method=xf.XF_BICGSTAB,
+                         atol=self.scalar_rtol * self.crhs.absmax()[0], maxit=20000)
             if s.status != capi.XF_OK:
                 raise xf.XFError(s.status, f"concentration: status {s.status}")
             self.c, self.cnext = self.cnext, self.c
