@@ -777,7 +777,9 @@ def full_loop(ctx, steps):
                 "pressure_iterations_mean": float(np.mean([r["pressure_iterations"] for r in recs])),
                 "momentum_iterations_mean": float(np.mean([r["momentum_iterations"] for r in recs])),
                 "scalar_iterations_mean": float(np.mean([r["scalar_iterations"] for r in recs])),
-                "pressure_fallbacks": int(sum(r["pressure_fallbacks"] for r in recs)), "last": recs[-1]}
+                "pressure_fallbacks": int(sum(r["pressure_fallbacks"] for r in recs)),
+                "phase_ms_mean": {k: float(np.mean([r["phase_ms"][k] for r in recs[1:]])) for k in recs[0]["phase_ms"]},
+                "last": recs[-1]}
 
     line = {"mode": "full loop", "statement": st["name"] + ", Gaussian inlet sigma=0.05",
             "cells": int(act.sum()), "steps": steps, "markers": int(len(mk["pos"])),

@@ -98,6 +98,11 @@ struct xf_op {
   int adD_set = 0;
   double ad_tau = 1, ad_D = 0;
   int ad_flags = 0, adv_set = 0;
+  // the FP64 Actual rows' coefficients (9 per cell, SoA), refreshed by
+  // xf_op_ready after either setter; invalid until then (rows then compute
+  // them on the fly, with the same result)
+  mutable double* adc64 = nullptr;
+  mutable int adc_valid = 0;
   // device staging boxes of xf_solve_host, kept between calls
   xf_vec* host_x = nullptr;
   xf_vec* host_b = nullptr;

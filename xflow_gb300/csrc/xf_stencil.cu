@@ -152,6 +152,36 @@ __global__ void __launch_bounds__(MV_THREADS) k_matvec(MatvecArgs<T> a) {
   }
 }
 
+// The advection fields of an XF_OP_ADVDIFF operator in a stencil grid.
+template <typename T>
+static void set_ad_fields(StencilGrid<T>& s, const xf_op* op) {
+  constexpr bool D64 = std::is_same<T, double>::value;
+  s.adv0 = D64 ? (const T*)op->adv64[0] : (const T*)op->adv32[0];
+  s.adv1 = D64 ? (const T*)op->adv64[1] : (const T*)op->adv32[1];
+  s.adv2 = D64 ? (const T*)op->adv64[2] : (const T*)op->adv32[2];
+  s.ad_itau = (T)(1 / op->ad_tau);
+  s.ad_D = (T)op->ad_D;
+  s.adDf = !op->adD_set ? nullptr : D64 ? (const T*)op->adD64 : (const T*)op->adD32;
+  s.ad_conv = (op->ad_flags & XF_ADV_CONVECTIVE) ? T(1) : T(0);
+  s.ad_diff = (op->ad_flags & XF_ADV_DIFFUSIVE) ? T(1) : T(0);
+  s.ad_upwind = (op->ad_flags & XF_ADV_UPWIND) ? 1 : 0;
+  s.adc = (D64 && op->adc_valid) ? (const T*)op->adc64 : nullptr;
+  s.adc_n = op->g->ncell;
+}
+
+// The FP64 coefficient table of the Actual rows (the operator's own
+// expressions, so the rows read from it are the same doubles).
+__global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, double* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (row_of(g.kind[c]) != ROW_ACTUAL) continue;
+    const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
+    double q[9];
+    ad_coefs<double>(g, i, j, k, (int)c, q);
+#pragma unroll
+    for (int t = 0; t < 9; t++) out[t * n + c] = q[t];
+  }
+}
+
 template <typename T>
 static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   const xf_grid* g = op->g;
@@ -173,16 +203,7 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   dim3 grid(bx, (g->n1 + chunk - 1) / chunk);
   const bool use_d = std::is_same<T, double>::value && op->kind == XF_OP_LAPLACE && !q.exact;
   if (op->kind == XF_OP_ADVDIFF) {
-    constexpr bool D64 = std::is_same<T, double>::value;
-    a.g.adv0 = D64 ? (const T*)op->adv64[0] : (const T*)op->adv32[0];
-    a.g.adv1 = D64 ? (const T*)op->adv64[1] : (const T*)op->adv32[1];
-    a.g.adv2 = D64 ? (const T*)op->adv64[2] : (const T*)op->adv32[2];
-    a.g.ad_itau = (T)(1 / op->ad_tau);
-    a.g.ad_D = (T)op->ad_D;
-    a.g.adDf = !op->adD_set ? nullptr : D64 ? (const T*)op->adD64 : (const T*)op->adD32;
-    a.g.ad_conv = (op->ad_flags & XF_ADV_CONVECTIVE) ? T(1) : T(0);
-    a.g.ad_diff = (op->ad_flags & XF_ADV_DIFFUSIVE) ? T(1) : T(0);
-    a.g.ad_upwind = (op->ad_flags & XF_ADV_UPWIND) ? 1 : 0;
+    set_ad_fields<T>(a.g, op);
     k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     return;
   }
@@ -265,6 +286,7 @@ extern "C" int xf_op_destroy(xf_op* op) {
   }
   if (op->adD64) cudaFree(op->adD64);
   if (op->adD32) cudaFree(op->adD32);
+  if (op->adc64) cudaFree(op->adc64);
   if (op->pack) xf_pack_free(op->pack);
   if (op->host_x) xf_vec_destroy(op->host_x);
   if (op->host_b) xf_vec_destroy(op->host_b);
@@ -302,6 +324,11 @@ extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, 
       return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_advection: velocities must be FP64 boxes of the operator's grid");
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   const int64_t n = op->g->ncell;
+  op->adc_valid = 0;
+  if (!op->adc64 && cudaMalloc(&op->adc64, 9 * n * 8) != cudaSuccess) {
+    cudaGetLastError();
+    return xf_fail(ctx, XF_ERR_NOMEM, "xf_op_set_advection: allocation");
+  }
   for (int d = 0; d < 3; d++) {
     if (!op->adv64[d] && (cudaMalloc(&op->adv64[d], n * 8) != cudaSuccess ||
                           cudaMalloc(&op->adv32[d], n * 4) != cudaSuccess)) {
@@ -325,6 +352,7 @@ extern "C" int xf_op_set_diffusion_field(xf_op* op, const xf_vec* d) {
   xf_ctx* ctx = op->g->ctx;
   if (op->kind != XF_OP_ADVDIFF)
     return xf_fail(ctx, XF_ERR_STATE, "xf_op_set_diffusion_field: not an advection-diffusion operator");
+  op->adc_valid = 0;
   if (!d) {
     op->adD_set = 0;
     return XF_OK;
@@ -347,6 +375,17 @@ extern "C" int xf_op_set_diffusion_field(xf_op* op, const xf_vec* d) {
 int xf_op_ready(const xf_op* op) {
   if (op->kind == XF_OP_ADVDIFF && !op->adv_set)
     return xf_fail(op->g->ctx, XF_ERR_STATE, "advection-diffusion operator used before xf_op_set_advection");
+  if (op->kind == XF_OP_ADVDIFF && !op->adc_valid && op->adc64) {   // refresh the coefficient table
+    xf_ctx* ctx = op->g->ctx;
+    XF_CUDA(ctx, cudaSetDevice(ctx->device));
+    StencilGrid<double> s = make_stencil_grid<double>(op->g, nullptr);
+    op->adc_valid = 0;
+    set_ad_fields<double>(s, op);
+    const int64_t n = op->g->ncell;
+    k_ad_coeffs<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, op->adc64);
+    XF_CUDA(ctx, cudaGetLastError());
+    op->adc_valid = 1;
+  }
   if (op->kind == XF_OP_VARDIV && !op->rho_set)
     return xf_fail(op->g->ctx, XF_ERR_STATE, "variable-density operator used before xf_op_set_density");
   return XF_OK;

@@ -27,6 +27,10 @@ struct StencilGrid {
   // ADVDIFF: advecting velocity per direction, 1/tau, D and the two flags as 0/1
   const T* __restrict__ adv0; const T* __restrict__ adv1; const T* __restrict__ adv2;
   const T* __restrict__ adDf;   // per-cell D of the variable-viscosity form, or null
+  // the Actual rows' nine coefficients (A, B, C per direction, SoA with
+  // stride adc_n), precomputed from the fields above, or null
+  const T* __restrict__ adc;
+  int64_t adc_n;
   T ad_itau, ad_D, ad_conv, ad_diff;
   int ad_upwind;   // the first-order upwind form of the convective term
   int n1, n2, n3;
@@ -193,27 +197,26 @@ __device__ __forceinline__ T fast_vd_actual(const StencilGrid<T>& g, const T* __
 // x, y, z after (1/tau) f_c.  Neighbour values are read as they are (the
 // solver keeps inactive cells at 0).
 template <typename T>
-__device__ __forceinline__ T ad_dir(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T fm, T fc, T fp) {
+__device__ __forceinline__ void ad_coef(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T& A, T& B, T& C) {
   const T h_1 = h[m - 1], hh = h[m];
   const T hx2 = h[m - 1] + h[m];
   const T hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / T(2);
-  const T A = conv * (T(0.5) * (-vd / hx2)) + diff * (T(0.5) * (-(D)*hh / hxhxh));
-  const T B = diff * (T(0.5) * (D)*hx2 / hxhxh);
-  const T C = conv * (T(0.5) * (vd / hx2)) + diff * (T(0.5) * (-(D)*h_1 / hxhxh));
-  return A * fm + B * fc + C * fp;
+  A = conv * (T(0.5) * (-vd / hx2)) + diff * (T(0.5) * (-(D)*hh / hxhxh));
+  B = diff * (T(0.5) * (D)*hx2 / hxhxh);
+  C = conv * (T(0.5) * (vd / hx2)) + diff * (T(0.5) * (-(D)*h_1 / hxhxh));
 }
 
 // The upwind form (schemeType 1 of SolveTransferEquation_, XProblem.cpp:
 // 1828-1843): the convective term takes the upstream neighbour over h[m];
 // the centre coefficient is the convective term plus the diffusive one.
 template <typename T>
-__device__ __forceinline__ T ad_dir_upwind(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T fm, T fc,
-                                           T fp) {
+__device__ __forceinline__ void ad_coef_upwind(const T* __restrict__ h, int m, T vd, T D, T conv, T diff, T& A, T& B,
+                                               T& C) {
   const T h_1 = h[m - 1], hh = h[m];
   const T hx2 = h[m - 1] + h[m];
   const T hxhxh = h[m - 1] * h[m] * (h[m - 1] + h[m]) / T(2);
   const T Bd = diff * (T(0.5) * (D)*hx2 / hxhxh);
-  T A, Bc, C;
+  T Bc;
   if (vd < T(0)) {
     A = diff * (T(0.5) * (-(D)*hh / hxhxh));
     Bc = conv * (T(0.5) * (-vd / hh));
@@ -223,24 +226,42 @@ __device__ __forceinline__ T ad_dir_upwind(const T* __restrict__ h, int m, T vd,
     Bc = conv * (T(0.5) * (vd / hh));
     C = diff * (T(0.5) * (-(D)*h_1 / hxhxh));
   }
-  return A * fm + (Bc + Bd) * fc + C * fp;
+  B = Bc + Bd;
 }
 
+// The nine coefficients of the Actual row at (i, j, k): A, B, C along x, y, z.
+template <typename T>
+__device__ __forceinline__ void ad_coefs(const StencilGrid<T>& g, int i, int j, int k, int c, T* q) {
+  const T D = g.adDf ? g.adDf[c] : g.ad_D;   // diffCoefVar[i][j][k] (XProblem.cpp:3204) or the constant
+  if (g.ad_upwind) {
+    ad_coef_upwind<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, q[0], q[1], q[2]);
+    ad_coef_upwind<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, q[3], q[4], q[5]);
+    ad_coef_upwind<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, q[6], q[7], q[8]);
+  } else {
+    ad_coef<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, q[0], q[1], q[2]);
+    ad_coef<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, q[3], q[4], q[5]);
+    ad_coef<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, q[6], q[7], q[8]);
+  }
+}
+
+// (1/tau) f_c, then per direction A f[m-1] + B f_c + C f[m+1] in that order;
+// from the precomputed table when there is one (the same doubles: the FP64
+// divisions of the coefficients are paid once per set-up, not per apply).
 template <typename T>
 __device__ __forceinline__ T ad_actual(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c) {
   const int s1 = g.s1, s2 = g.s2;
   const T fc = f[c];
-  const T D = g.adDf ? g.adDf[c] : g.ad_D;   // diffCoefVar[i][j][k] (XProblem.cpp:3204) or the constant
-  T res = g.ad_itau * fc;
-  if (g.ad_upwind) {
-    res = res + ad_dir_upwind<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
-    res = res + ad_dir_upwind<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
-    res = res + ad_dir_upwind<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
-    return res;
+  T q[9];
+  if (g.adc) {
+#pragma unroll
+    for (int t = 0; t < 9; t++) q[t] = g.adc[t * g.adc_n + c];
+  } else {
+    ad_coefs<T>(g, i, j, k, c, q);
   }
-  res = res + ad_dir<T>(g.hx, i, g.adv0[c], D, g.ad_conv, g.ad_diff, f[c - s1], fc, f[c + s1]);
-  res = res + ad_dir<T>(g.hy, j, g.adv1[c], D, g.ad_conv, g.ad_diff, f[c - s2], fc, f[c + s2]);
-  res = res + ad_dir<T>(g.hz, k, g.adv2[c], D, g.ad_conv, g.ad_diff, f[c - 1], fc, f[c + 1]);
+  T res = g.ad_itau * fc;
+  res = res + (q[0] * f[c - s1] + q[1] * fc + q[2] * f[c + s1]);
+  res = res + (q[3] * f[c - s2] + q[4] * fc + q[5] * f[c + s2]);
+  res = res + (q[6] * f[c - 1] + q[7] * fc + q[8] * f[c + 1]);
   return res;
 }
 

@@ -281,6 +281,15 @@ class SplittingLoop:
         xf, tau = self.xf, self.tau
         self.ctx.synchronize()
         t0 = time.perf_counter()
+        phase = {"borders": 0.0, "ib": 0.0, "momentum": 0.0, "pressure": 0.0, "correction": 0.0, "scalar": 0.0}
+        mark = [t0]
+
+        def lap(name):   # wall ms of each phase (synchronised; the step's own total is the record's ms)
+            self.ctx.synchronize()
+            t = time.perf_counter()
+            phase[name] += (t - mark[0]) * 1e3
+            mark[0] = t
+
         its = []
         u1, v1, w1 = self.vel
         for axis, side in self.st.get("follow", ()):   # zero-gradient faces take the interior's values
@@ -289,6 +298,7 @@ class SplittingLoop:
         if "convective" in self.st:   # the outlet's normal velocity: convective outflow, flux balanced
             axis, speed = self.st["convective"]
             xf.outflow_convective(self.vel[axis - 1], self.bc[axis - 1], axis, speed, tau)
+        lap("borders")
         for a in range(3):
             force = None
             if self.markers is not None:   # GetForce: interpolate, move, forces, spread
@@ -298,6 +308,7 @@ class SplittingLoop:
                 self.markers.compute_forces(a + 1)
                 self.markers.spread(self.force[a], self.h0, a + 1)
                 force = self.force[a]
+                lap("ib")
             uTr, vTr, wTr, visTr, rp = xf.momentum_rhs(a + 1, self.g[a], u1, v1, w1, vis=self.vis, border=self.bc[a],
                                                        force=force, out=self.mom[a])
             A = self.ops[a]
@@ -312,6 +323,7 @@ class SplittingLoop:
                 raise xf.XFError(s.status, f"momentum equation {a + 1}: status {s.status}")
             xf.border_recalc(self.mid[a], self.bc[a])   # the sector ends exact, as the ADI leaves them
             its.append(s.iterations)
+            lap("momentum")
         xf.pressure_rhs(self.gp, *self.mid, tau, self.prhs, border=self.pbc)
         # every pressure solve starts from the previous step's pressure
         if self.st["pressure"] == "neumann" and self.pressure_solver == "learned":
@@ -329,9 +341,11 @@ class SplittingLoop:
         if s.status != capi.XF_OK:
             raise xf.XFError(s.status, f"pressure: status {s.status}")
         its.append(s.iterations)
+        lap("pressure")
         for a in range(3):
             xf.velocity_correct(a + 1, self.mid[a], self.p, tau, self.vel[a], border=self.bc[a])
         div, ijk = xf.divergence_max(self.gp, *self.vel)
+        lap("correction")
         rec = {"pressure_iterations": its[3], "pressure_fallbacks": int(getattr(s, "fallbacks", 0))}
         if self.scalar is not None:   # the concentration equation, from the corrected velocities
             uT, vT, wT, rp = xf.conc_transfer(self.gc, *self.vel, inlet=self.cin, out=self.ctr)
@@ -349,10 +363,11 @@ class SplittingLoop:
                 raise xf.XFError(s.status, f"concentration: status {s.status}")
             self.c, self.cnext = self.cnext, self.c
             rec["scalar_iterations"] = s.iterations
+            lap("scalar")
         self.ctx.synchronize()
         self.steps += 1
         rec.update({"step": self.steps, "ms": (time.perf_counter() - t0) * 1e3, "momentum_iterations": its[:3],
-                    "divergence_max": div, "divergence_cell": ijk})
+                    "divergence_max": div, "divergence_cell": ijk, "phase_ms": phase})
         return rec
 
     def fields(self):
