@@ -292,6 +292,10 @@ def main(argv=None):
     ap.add_argument("--loop-steps", type=int, default=20,
                     help="with --timeloop: steps of the 512x128x128 loop (each run)")
     ap.add_argument("--loop-only", action="store_true", help="with --timeloop: the 512x128x128 loop alone")
+    ap.add_argument("--loop-solver", default="compare", choices=["compare", "learned", "mixed", "fp64"],
+                    help="with --timeloop: the 512x128x128 loop's pressure solver; compare (default) runs the learned "
+                         "solver and plain FP64 CG and reports the drift between them, the others one run (mixed and "
+                         "fp64 without training: a bounded command for launch lists)")
     argv = sys.argv[1:] if argv is None else argv
     args = ap.parse_args(argv)
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
@@ -733,11 +737,11 @@ def timeloop(args):
                 "last": recs[-1]}
         print(json.dumps(line), flush=True)
         del loop
-    full_loop(ctx, args.loop_steps)
+    full_loop(ctx, args.loop_steps, args.loop_solver)
     return 0
 
 
-def full_loop(ctx, steps):
+def full_loop(ctx, steps, solver_choice="compare"):
     """The full loop: the 512x128x128 channel on [0,4]x[0,1]^2 (8,388,608
     cells, h = 1/128), inflow u = 1, convective flux-balanced outflow,
     free-slip walls (lagged zero-gradient tangential values), Re = 200,
@@ -752,25 +756,18 @@ def full_loop(ctx, steps):
     import xflow_gb300 as xf
     from xflow_gb300 import timeloop as tl
 
-    params, train = train_unet(ctx)
+    solvers = ("learned", "fp64") if solver_choice == "compare" else (solver_choice,)
+    params, train = train_unet(ctx) if "learned" in solvers else (None, None)
     base = tl.channel(512, 128, 128, re=200.0, tau=2e-3, outflow="convective", walls="free_slip")
     mk = tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4)
     runs = {}
-    for solver in ("learned", "fp64"):
+    for solver in solvers:
         st = tl.with_scalar(base, tl.gaussian_inlet(base["p"][0].shape, base["h"], sigma=0.05))
         loop = tl.SplittingLoop(ctx, st, markers=mk, pressure_solver=solver,
                                 net_params=params if solver == "learned" else None)
         recs = [loop.step() for _ in range(steps)]
         runs[solver] = (recs, loop.fields())
         del loop
-    (lr, lf), (fr, ff) = runs["learned"], runs["fp64"]
-    vel_scale = max(np.abs(f).max() for f in ff[:3])
-    drift_u = max(np.abs(a - b).max() for a, b in zip(lf[:3], ff[:3])) / vel_scale
-    act = base["p"][0] == 1
-    pl, pf = lf[3][act], ff[3][act]
-    drift_p = np.abs((pl - pl.mean()) - (pf - pf.mean())).max() / np.abs(pf - pf.mean()).max()
-    cl, cf = lf[4], ff[4]
-    drift_c = float(np.abs(cl - cf).max())
 
     def summary(recs):
         return {"first_step_ms": recs[0]["ms"], "ms_per_step": float(np.mean([r["ms"] for r in recs[1:]])),
@@ -780,6 +777,19 @@ def full_loop(ctx, steps):
                 "pressure_fallbacks": int(sum(r["pressure_fallbacks"] for r in recs)),
                 "phase_ms_mean": {k: float(np.mean([r["phase_ms"][k] for r in recs[1:]])) for k in recs[0]["phase_ms"]},
                 "last": recs[-1]}
+
+    if solver_choice != "compare":
+        print(json.dumps({"mode": "full loop", "statement": st["name"], "steps": steps, "pressure": solver_choice,
+                          solver_choice: summary(runs[solver_choice][0])}), flush=True)
+        return
+    (lr, lf), (fr, ff) = runs["learned"], runs["fp64"]
+    vel_scale = max(np.abs(f).max() for f in ff[:3])
+    drift_u = max(np.abs(a - b).max() for a, b in zip(lf[:3], ff[:3])) / vel_scale
+    act = base["p"][0] == 1
+    pl, pf = lf[3][act], ff[3][act]
+    drift_p = np.abs((pl - pl.mean()) - (pf - pf.mean())).max() / np.abs(pf - pf.mean()).max()
+    cl, cf = lf[4], ff[4]
+    drift_c = float(np.abs(cl - cf).max())
 
     line = {"mode": "full loop", "statement": st["name"] + ", Gaussian inlet sigma=0.05",
             "cells": int(act.sum()), "steps": steps, "markers": int(len(mk["pos"])),
