@@ -135,7 +135,12 @@ int xf_op_set_density(xf_op* op, const double* host_density_box);
  *   B_d = diff 0.5 D hx2 / hxhxh                              (f[m])
  *   C_d = conv 0.5 (vd / hx2) + diff 0.5 (-D h_1 / hxhxh)     (f[m+1])
  *   (A f)_c = (1/tau) f_c + sum_d (A_d f[m-1] + B_d f_c + C_d f[m+1]),
- * in that evaluation order.  With XF_ADV_UPWIND the convective part takes
+ * in that evaluation order with XF_EXACT (FP64).  Without it, FP64 rows read
+ * a table of seven coefficients per cell (the centre 1/tau + B_x + B_y + B_z
+ * and the six neighbours'), built once after each xf_op_set_advection /
+ * xf_op_set_diffusion_field, and apply them by FMAs: within a few units in
+ * the last place of the exact rows, at 7 FP64 operations a row instead of
+ * 19 and 15 divisions.  With XF_ADV_UPWIND the convective part takes
  * the upstream neighbour over h (vd < 0: B_d += conv 0.5 (-vd / h),
  * C_d += conv 0.5 (vd / h); else A_d += conv 0.5 (-vd / h),
  * B_d += conv 0.5 (vd / h)); B_d is the convective term plus the diffusive

@@ -4,7 +4,8 @@ summed over the three directions; with XF_ADV_UPWIND the upwind scheme of
 the concentration equation, :1828-1843) against the oracle's restatement,
 and its solves by the reference Krylov methods.
 
-Bars: FP64 rows bit-exact; FP32 rows within 2e-6 x max|y|; the packed form
+Bars: FP64 rows with XF_EXACT bit-exact, the fast FP64 rows (the seven-
+coefficient table) within 1e-13 x max|y|; FP32 rows within 2e-6 x max|y|; the packed form
 within 1e-13 x max|y| (row dot in pack order vs the stencil's expression
 order); solves of a manufactured system reach their stop rule and recover the
 solution within 1e-6 relative max-norm.
@@ -49,9 +50,13 @@ def test_advdiff_rows_match_oracle(ctx, flags):
     want = O.apply_advdiff(og, x, *vel, 1e-2, 0.05, flags)
     sm = og.smask.astype(bool)
     y = g.vec(None)
-    A.apply(g.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    A.apply(g.vec(x), y, flags=xf.XF_ZERO_INACTIVE | xf.XF_EXACT)
     got = y.download()
     np.testing.assert_array_equal(got[sm], want[sm])
+    A.apply(g.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    fast = y.download()
+    assert np.abs(fast[sm] - want[sm]).max() <= 1e-13 * np.abs(want[sm]).max()
+    assert not np.array_equal(fast[sm], want[sm])   # the fast form is the one a plain apply takes
     y32 = g.vec(None, xf.XF_F32)
     A.apply(g.vec(x, xf.XF_F32), y32, flags=xf.XF_ZERO_INACTIVE)
     assert np.abs(y32.download()[sm] - want[sm]).max() <= 2e-6 * np.abs(want[sm]).max()

@@ -98,9 +98,9 @@ struct xf_op {
   int adD_set = 0;
   double ad_tau = 1, ad_D = 0;
   int ad_flags = 0, adv_set = 0;
-  // the FP64 Actual rows' coefficients (9 per cell, SoA), refreshed by
-  // xf_op_ready after either setter; invalid until then (rows then compute
-  // them on the fly, with the same result)
+  // the FP64 fast Actual rows' coefficients (7 per cell, SoA), refreshed by
+  // xf_op_ready after either setter; invalid until then (the rows then take
+  // the exact form)
   mutable double* adc64 = nullptr;
   mutable int adc_valid = 0;
   // device staging boxes of xf_solve_host, kept between calls

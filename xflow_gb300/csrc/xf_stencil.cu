@@ -169,16 +169,65 @@ static void set_ad_fields(StencilGrid<T>& s, const xf_op* op) {
   s.adc_n = op->g->ncell;
 }
 
-// The FP64 coefficient table of the Actual rows (the operator's own
-// expressions, so the rows read from it are the same doubles).
-__global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, double* __restrict__ out) {
+// Per-axis factors of the fast coefficients, 5 per node m of each axis (the
+// halves folded in): 0.5/hx2, 0.5/h, 0.5 h/hxhxh, 0.5 hx2/hxhxh, 0.5 h_1/hxhxh
+// with h_1 = h[m-1], h = h[m], hx2 = h_1 + h, hxhxh = h_1 h hx2 / 2 (the exact
+// rows' quantities; nodes 0 and n-1, which carry no Actual row, get 0).
+__global__ void k_ad_axis(const double* __restrict__ h, int n, double* __restrict__ t) {
+  for (int m = threadIdx.x; m < n; m += blockDim.x) {
+    double r2 = 0, rh = 0, dA = 0, dB = 0, dC = 0;
+    if (m >= 1 && m <= n - 2) {
+      const double h_1 = h[m - 1], hh = h[m], hx2 = h_1 + hh, hxhxh = h_1 * hh * hx2 / 2;
+      r2 = 0.5 / hx2;
+      rh = 0.5 / hh;
+      dA = 0.5 * hh / hxhxh;
+      dB = 0.5 * hx2 / hxhxh;
+      dC = 0.5 * h_1 / hxhxh;
+    }
+    t[5 * m] = r2; t[5 * m + 1] = rh; t[5 * m + 2] = dA; t[5 * m + 3] = dB; t[5 * m + 4] = dC;
+  }
+}
+
+// A, B, C of one direction from the axis factors (central or upwind), as the
+// exact rows define them but with products for the divisions.
+__device__ __forceinline__ void ad_coef_fast(const double* __restrict__ t, double vd, double D, double conv,
+                                             double diff, bool upwind, double& A, double& B, double& C) {
+  const double dA = diff * (-D * t[2]), dB = diff * (D * t[3]), dC = diff * (-D * t[4]);
+  if (!upwind) {
+    A = conv * (-vd * t[0]) + dA;
+    B = dB;
+    C = conv * (vd * t[0]) + dC;
+  } else if (vd < 0) {
+    A = dA;
+    B = conv * (-vd * t[1]) + dB;
+    C = conv * (vd * t[1]) + dC;
+  } else {
+    A = conv * (-vd * t[1]) + dA;
+    B = conv * (vd * t[1]) + dB;
+    C = dC;
+  }
+}
+
+// The FP64 coefficient table of the fast Actual rows: a centre coefficient
+// 1/tau + B_x + B_y + B_z and the six neighbour coefficients.
+__global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, const double* __restrict__ tx,
+                            const double* __restrict__ ty, const double* __restrict__ tz, double* __restrict__ out) {
+  const bool up = g.ad_upwind != 0;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     if (row_of(g.kind[c]) != ROW_ACTUAL) continue;
     const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
-    double q[9];
-    ad_coefs<double>(g, i, j, k, (int)c, q);
-#pragma unroll
-    for (int t = 0; t < 9; t++) out[t * n + c] = q[t];
+    const double D = g.adDf ? g.adDf[c] : g.ad_D;
+    double Ax, Bx, Cx, Ay, By, Cy, Az, Bz, Cz;
+    ad_coef_fast(tx + 5 * i, g.adv0[c], D, g.ad_conv, g.ad_diff, up, Ax, Bx, Cx);
+    ad_coef_fast(ty + 5 * j, g.adv1[c], D, g.ad_conv, g.ad_diff, up, Ay, By, Cy);
+    ad_coef_fast(tz + 5 * k, g.adv2[c], D, g.ad_conv, g.ad_diff, up, Az, Bz, Cz);
+    out[c] = g.ad_itau + Bx + By + Bz;
+    out[n + c] = Ax;
+    out[2 * n + c] = Cx;
+    out[3 * n + c] = Ay;
+    out[4 * n + c] = Cy;
+    out[5 * n + c] = Az;
+    out[6 * n + c] = Cz;
   }
 }
 
@@ -204,7 +253,8 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   const bool use_d = std::is_same<T, double>::value && op->kind == XF_OP_LAPLACE && !q.exact;
   if (op->kind == XF_OP_ADVDIFF) {
     set_ad_fields<T>(a.g, op);
-    k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    if (q.exact) k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
+    else k_matvec<T, XF_OP_ADVDIFF, false, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     return;
   }
   if (op->kind == XF_OP_LAPLACE) {
@@ -325,7 +375,8 @@ extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, 
   XF_CUDA(ctx, cudaSetDevice(ctx->device));
   const int64_t n = op->g->ncell;
   op->adc_valid = 0;
-  if (!op->adc64 && cudaMalloc(&op->adc64, 9 * n * 8) != cudaSuccess) {
+  const int64_t nax = 5 * ((int64_t)op->g->n1 + op->g->n2 + op->g->n3);   // per-axis factors after the table
+  if (!op->adc64 && cudaMalloc(&op->adc64, (7 * n + nax) * 8) != cudaSuccess) {
     cudaGetLastError();
     return xf_fail(ctx, XF_ERR_NOMEM, "xf_op_set_advection: allocation");
   }
@@ -378,11 +429,18 @@ int xf_op_ready(const xf_op* op) {
   if (op->kind == XF_OP_ADVDIFF && !op->adc_valid && op->adc64) {   // refresh the coefficient table
     xf_ctx* ctx = op->g->ctx;
     XF_CUDA(ctx, cudaSetDevice(ctx->device));
-    StencilGrid<double> s = make_stencil_grid<double>(op->g, nullptr);
+    const xf_grid* g = op->g;
+    StencilGrid<double> s = make_stencil_grid<double>(g, nullptr);
     op->adc_valid = 0;
     set_ad_fields<double>(s, op);
-    const int64_t n = op->g->ncell;
-    k_ad_coeffs<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, op->adc64);
+    const int64_t n = g->ncell;
+    double* tx = op->adc64 + 7 * n;   // the axis factors sit after the table
+    double* ty = tx + 5 * g->n1;
+    double* tz = ty + 5 * g->n2;
+    k_ad_axis<<<1, 256, 0, ctx->stream>>>(g->hx, g->n1, tx);
+    k_ad_axis<<<1, 256, 0, ctx->stream>>>(g->hy, g->n2, ty);
+    k_ad_axis<<<1, 256, 0, ctx->stream>>>(g->hz, g->n3, tz);
+    k_ad_coeffs<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, tx, ty, tz, op->adc64);
     XF_CUDA(ctx, cudaGetLastError());
     op->adc_valid = 1;
   }

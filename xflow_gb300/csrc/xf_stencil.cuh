@@ -27,8 +27,9 @@ struct StencilGrid {
   // ADVDIFF: advecting velocity per direction, 1/tau, D and the two flags as 0/1
   const T* __restrict__ adv0; const T* __restrict__ adv1; const T* __restrict__ adv2;
   const T* __restrict__ adDf;   // per-cell D of the variable-viscosity form, or null
-  // the Actual rows' nine coefficients (A, B, C per direction, SoA with
-  // stride adc_n), precomputed from the fields above, or null
+  // the Actual rows' seven coefficients of the fast form (centre, then the
+  // x-, x+, y-, y+, z-, z+ neighbours; SoA with stride adc_n), precomputed
+  // from the fields above, or null
   const T* __restrict__ adc;
   int64_t adc_n;
   T ad_itau, ad_D, ad_conv, ad_diff;
@@ -244,20 +245,29 @@ __device__ __forceinline__ void ad_coefs(const StencilGrid<T>& g, int i, int j, 
   }
 }
 
-// (1/tau) f_c, then per direction A f[m-1] + B f_c + C f[m+1] in that order;
-// from the precomputed table when there is one (the same doubles: the FP64
-// divisions of the coefficients are paid once per set-up, not per apply).
-template <typename T>
+// EXACT: (1/tau) f_c, then per direction A f[m-1] + B f_c + C f[m+1], the
+// reference's operation order (19 FP64 operations and 15 divisions a row).
+// Otherwise, from the table when there is one: the centre coefficient
+// 1/tau + B_x + B_y + B_z and six FMAs (7 FP64 operations: GB300's FP64 rate
+// bounds this row, not its bytes).
+template <typename T, bool EXACT>
 __device__ __forceinline__ T ad_actual(const StencilGrid<T>& g, const T* __restrict__ f, int i, int j, int k, int c) {
   const int s1 = g.s1, s2 = g.s2;
   const T fc = f[c];
-  T q[9];
-  if (g.adc) {
-#pragma unroll
-    for (int t = 0; t < 9; t++) q[t] = g.adc[t * g.adc_n + c];
-  } else {
-    ad_coefs<T>(g, i, j, k, c, q);
+  if (!EXACT && g.adc) {
+    const T* __restrict__ q = g.adc + c;
+    const int64_t n = g.adc_n;
+    T res = q[0] * fc;
+    res = fma(q[n], f[c - s1], res);
+    res = fma(q[2 * n], f[c + s1], res);
+    res = fma(q[3 * n], f[c - s2], res);
+    res = fma(q[4 * n], f[c + s2], res);
+    res = fma(q[5 * n], f[c - 1], res);
+    res = fma(q[6 * n], f[c + 1], res);
+    return res;
   }
+  T q[9];
+  ad_coefs<T>(g, i, j, k, c, q);
   T res = g.ad_itau * fc;
   res = res + (q[0] * f[c - s1] + q[1] * fc + q[2] * f[c + s1]);
   res = res + (q[3] * f[c - s2] + q[4] * fc + q[5] * f[c + s2]);
@@ -271,7 +281,7 @@ __device__ __forceinline__ T apply_row(const StencilGrid<T>& g, const T* __restr
                                        uint8_t kb) {
   const int row = row_of(kb);
   if (row == ROW_ACTUAL) {
-    if (OP == XF_OP_ADVDIFF) return ad_actual<T>(g, f, i, j, k, c);
+    if (OP == XF_OP_ADVDIFF) return ad_actual<T, EXACT>(g, f, i, j, k, c);
     if (OP == XF_OP_LAPLACE) return EXACT ? exact_lap_actual<T>(g, f, i, j, k, c, kb) : fast_lap_actual<T>(g, f, i, j, k, c, kb);
     return EXACT ? exact_vd_actual<T>(g, f, i, j, k, c, kb) : fast_vd_actual<T>(g, f, i, j, k, c, kb);
   }
