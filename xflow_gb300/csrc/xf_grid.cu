@@ -50,6 +50,14 @@ extern "C" int xf_create(int device, xf_ctx** out) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete ctx; return XF_ERR_CUDA; }
   ctx->sm_count = prop.multiProcessorCount;
+  // Solver work vectors come from the device's default pool (cudaMallocAsync):
+  // keep what one solve frees for the next instead of unmapping it at every
+  // synchronisation (an attribute of this process's pool).
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return XF_ERR_CUDA; }
   if (cudaMalloc(&ctx->scratch, sizeof(DevScratch)) != cudaSuccess) { delete ctx; return XF_ERR_NOMEM; }
   cudaMemsetAsync(ctx->scratch, 0, sizeof(DevScratch), ctx->stream);

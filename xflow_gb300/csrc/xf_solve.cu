@@ -250,8 +250,9 @@ __device__ double block_max(double v, double* sh) {
   return v;
 }
 
-// XSLAE.cpp:738-749: Un += an*Pn1 + wn*Sn; Rn = Sn - wn*Tn; Pn = Pn1; then
-// ||Rn||_inf (NaN never wins, XSpace.cpp:3455-3463) with control `ctl`.
+// XSLAE.cpp:738-749: Un += an*Pn1 + wn*Sn; Rn = Sn - wn*Tn; Pn = Pn1 (no
+// copy when Pn is null: the caller alternates the two direction buffers);
+// then ||Rn||_inf (NaN never wins, XSpace.cpp:3455-3463) with control `ctl`.
 __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ Un, double* __restrict__ Rn,
                                                           double* __restrict__ Pn, const double* __restrict__ Pn1,
                                                           const double* __restrict__ Sn, const double* __restrict__ Tn,
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ U
       double t = wn * Tn[i];
       r = Sn[i] - t;
       Rn[i] = r;
-      Pn[i] = Pn1[i];
+      if (Pn) Pn[i] = Pn1[i];
     } else {
       r = Rn[i];
     }
@@ -714,6 +715,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
   Bufs B(ctx);
   const int rb = red_blocks(ctx, n), eb = grid_blocks(ctx, n, 256);
   std::function<void(int)> iter;
+  bool even_chunks = false;   // the iteration alternates buffers by parity
   HostState hs = {0, 0, 0, 0, 0};
   double eps = o.atol;
   if (o.method == XF_CG_REFERENCE) {
@@ -758,17 +760,22 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     xf_mv64(op, q0);
     XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
-    iter = [=](int) {
+    // the previous direction and the new one alternate between Pn and Pn1 with
+    // the iteration's parity (chunks of an even number of iterations)
+    even_chunks = true;
+    iter = [=](int it) {
+      double* Pold = (it & 1) ? Pn1 : Pn;
+      double* Pnew = (it & 1) ? Pn : Pn1;
       k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(sRn, Rn, m, n, S, SL_A, CTL_BCGS_PN1, 1);
-      k_bcgs_p<<<eb, 256, 0, ctx->stream>>>(Pn1, Rn, Pn, Vn, m, n, S);
+      k_bcgs_p<<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
       MvReq<double> a;
-      a.x = Pn1; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
+      a.x = Pnew; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
       xf_mv64(op, a);
       k_bcgs_s<<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
       MvReq<double> c;
       c.x = Sn; c.y = Tn; c.w = Sn; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_BCGS_WN;
       xf_mv64(op, c);
-      k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 1, CTL_BCGS_END);
+      k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1, CTL_BCGS_END);
     };
   } else if (o.method == XF_MINRES) {
     if (eps <= 0) eps = 1e-7;   // XSLAE.cpp:358
@@ -815,6 +822,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
   }
   XF_CUDA(ctx, cudaGetLastError());
   int chunk = o.check_every > 0 ? o.check_every : 16;
+  if (even_chunks) chunk += chunk & 1;
   int rc = run_loop(ctx, iter, chunk, o.maxit, &hs);
   if (rc) return rc;
   double* tmp = B.get<double>(n, false);
