@@ -162,7 +162,7 @@ def test_momentum_rhs_normal_cells_and_throws(ctx):
 
 def test_momentum_equation_variable_viscosity(ctx):
     """The u equation end to end: rp from xf_momentum_rhs, the variable-viscosity advection-diffusion rows
-    (diffCoefVar = visTr) bit-exact against the oracle, and the implicit system (1/tau) u + ... = u_prev/tau + rp
+    (diffCoefVar = visTr) bit-exact against the oracle (XF_EXACT; the fast rows within 1e-13), and the implicit system (1/tau) u + ... = u_prev/tau + rp
     solved by BiCGStab to its stop rule (max-norm of the true residual <= 1e-5, XSLAE.cpp:712)."""
     cs = wl_step.staggered_channel()
     gp, gu0, gv, gw = grids(ctx, cs)
@@ -181,14 +181,16 @@ def test_momentum_equation_variable_viscosity(ctx):
     rng = np.random.Generator(np.random.PCG64(4))
     x = rng.standard_normal(gu.shape)
     y = gu.vec(None)
-    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE | xf.XF_EXACT)
     want = O.apply_advdiff(og, x, uTr.download(), vTr.download(), wTr.download(), tau, 0.0, 3,
                            Dfield=visTr.download())
     sm = og.smask.astype(bool)
     np.testing.assert_array_equal(y.download()[sm], want[sm])
+    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE)   # the fast rows (the solver's)
+    assert np.abs(y.download()[sm] - want[sm]).max() <= 1e-13 * np.abs(want[sm]).max()
     # the constant form differs once the field is set, and returns when it is cleared
     A.set_diffusion_field(None)
-    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE)
+    A.apply(gu.vec(x), y, flags=xf.XF_ZERO_INACTIVE | xf.XF_EXACT)
     np.testing.assert_array_equal(y.download()[sm], O.apply_advdiff(og, x, uTr.download(), vTr.download(),
                                                                      wTr.download(), tau, 0.0, 3)[sm])
     A.set_diffusion_field(visTr)
