@@ -211,27 +211,36 @@ __global__ void k_rcg_update(double* __restrict__ xk, double* __restrict__ xk_1,
   }
 }
 
-// XSLAE.cpp:723-727: Pn1 = Rn + bn*(Pn - wn*Vn), in the reference's steps.
+// BiCGStab's vector steps come in two forms: the reference's steps (EXACT,
+// for XF_EXACT solves) and FMA forms with fewer FP64 operations (GB300's FP64
+// rate, not memory, bounds these passes).
+// XSLAE.cpp:723-727: Pn1 = Rn + bn*(Pn - wn*Vn).
+template <bool EXACT>
 __global__ void k_bcgs_p(double* __restrict__ Pn1, const double* __restrict__ Rn, const double* __restrict__ Pn,
                          const double* __restrict__ Vn, const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
   GUARD_DONE(S);
   const double wn = S->scalars[D_WN], bn = S->scalars[D_BN];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (!m[i]) continue;
-    double t = wn * Vn[i];
-    t = Pn[i] - t;
-    t = bn * t;
-    Pn1[i] = Rn[i] + t;
+    if (EXACT) {
+      double t = wn * Vn[i];
+      t = Pn[i] - t;
+      t = bn * t;
+      Pn1[i] = Rn[i] + t;
+    } else {
+      Pn1[i] = fma(bn, fma(-wn, Vn[i], Pn[i]), Rn[i]);
+    }
   }
 }
 
 // XSLAE.cpp:732-733: Sn = Rn - an*Vn.
+template <bool EXACT>
 __global__ void k_bcgs_s(double* __restrict__ Sn, const double* __restrict__ Rn, const double* __restrict__ Vn,
                          const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
   GUARD_DONE(S);
   const double an = S->scalars[D_AN];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    if (m[i]) Sn[i] = Rn[i] - an * Vn[i];
+    if (m[i]) Sn[i] = EXACT ? Rn[i] - an * Vn[i] : fma(-an, Vn[i], Rn[i]);
 }
 
 __device__ __forceinline__ double max_nan_skip(double a, double b) { return b > a ? b : a; }
@@ -253,6 +262,7 @@ __device__ double block_max(double v, double* sh) {
 // XSLAE.cpp:738-749: Un += an*Pn1 + wn*Sn; Rn = Sn - wn*Tn; Pn = Pn1 (no
 // copy when Pn is null: the caller alternates the two direction buffers);
 // then ||Rn||_inf (NaN never wins, XSpace.cpp:3455-3463) with control `ctl`.
+template <bool EXACT>
 __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ Un, double* __restrict__ Rn,
                                                           double* __restrict__ Pn, const double* __restrict__ Pn1,
                                                           const double* __restrict__ Sn, const double* __restrict__ Tn,
@@ -266,12 +276,18 @@ __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ U
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (!m[i]) continue;
     double r;
-    if (update) {
+    if (update && EXACT) {
       double tmp1 = an * Pn1[i];
       double tmp2 = tmp1 + wn * Sn[i];
       Un[i] = Un[i] + tmp2;
       double t = wn * Tn[i];
       r = Sn[i] - t;
+      Rn[i] = r;
+      if (Pn) Pn[i] = Pn1[i];
+    } else if (update) {
+      const double sn = Sn[i];
+      Un[i] = Un[i] + fma(an, Pn1[i], wn * sn);
+      r = fma(-wn, Tn[i], sn);
       Rn[i] = r;
       if (Pn) Pn[i] = Pn1[i];
     } else {
@@ -759,7 +775,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     q0.x = x; q0.y = Rn; q0.s = b; q0.sign = -1; q0.neg = 1; q0.exact = exact;
     xf_mv64(op, q0);
     XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
+    k_bcgs_end<true><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
     // the previous direction and the new one alternate between Pn and Pn1 with
     // the iteration's parity (chunks of an even number of iterations)
     even_chunks = true;
@@ -767,15 +783,20 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
       double* Pold = (it & 1) ? Pn1 : Pn;
       double* Pnew = (it & 1) ? Pn : Pn1;
       k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(sRn, Rn, m, n, S, SL_A, CTL_BCGS_PN1, 1);
-      k_bcgs_p<<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
+      if (exact) k_bcgs_p<true><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
+      else k_bcgs_p<false><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
       MvReq<double> a;
       a.x = Pnew; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
       xf_mv64(op, a);
-      k_bcgs_s<<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
+      if (exact) k_bcgs_s<true><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
+      else k_bcgs_s<false><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
       MvReq<double> c;
       c.x = Sn; c.y = Tn; c.w = Sn; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_BCGS_WN;
       xf_mv64(op, c);
-      k_bcgs_end<<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1, CTL_BCGS_END);
+      if (exact) k_bcgs_end<true><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1,
+                                                                        CTL_BCGS_END);
+      else k_bcgs_end<false><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1,
+                                                                  CTL_BCGS_END);
     };
   } else if (o.method == XF_MINRES) {
     if (eps <= 0) eps = 1e-7;   // XSLAE.cpp:358

@@ -85,8 +85,10 @@ __device__ __forceinline__ T march_lap(const StencilGrid<T>& g, const MatvecArgs
   }
 }
 
+// The fast FP64 advection-diffusion rows stream ten arrays a cell: four
+// blocks an SM (at most 64 registers) keep enough loads in flight.
 template <typename T, int OP, bool EXACT, bool USE_D>
-__global__ void __launch_bounds__(MV_THREADS) k_matvec(MatvecArgs<T> a) {
+__global__ void __launch_bounds__(MV_THREADS, (OP == XF_OP_ADVDIFF && !EXACT) ? 4 : 1) k_matvec(MatvecArgs<T> a) {
   __shared__ double sh[32];
   __shared__ bool last;
   // Solver kernels turn into no-ops once the solve is done (or, when gated,
