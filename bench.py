@@ -765,7 +765,17 @@ def full_loop(ctx, steps, solver_choice="compare"):
         st = tl.with_scalar(base, tl.gaussian_inlet(base["p"][0].shape, base["h"], sigma=0.05))
         loop = tl.SplittingLoop(ctx, st, markers=mk, pressure_solver=solver,
                                 net_params=params if solver == "learned" else None)
-        recs = [loop.step() for _ in range(steps)]
+        recs = []
+        for _ in range(steps):
+            try:
+                recs.append(loop.step())
+            except xf.XFError as e:   # report how far the run got, then fail
+                print(json.dumps({"mode": "full loop", "pressure": solver, "failed_at_step": len(recs) + 1,
+                                  "error": str(e), "last": recs[-1] if recs else None}), flush=True)
+                raise
+            r = recs[-1]
+            print(f"[{solver}] step {r['step']}: {r['ms']:.1f} ms, pressure {r['pressure_iterations']} it, "
+                  f"|u|max {max(r['velocity_max']):.4g}, div {r['divergence_max']:.3g}", file=sys.stderr, flush=True)
         runs[solver] = (recs, loop.fields())
         del loop
 

@@ -367,7 +367,8 @@ class SplittingLoop:
         self.ctx.synchronize()
         self.steps += 1
         rec.update({"step": self.steps, "ms": (time.perf_counter() - t0) * 1e3, "momentum_iterations": its[:3],
-                    "divergence_max": div, "divergence_cell": ijk, "phase_ms": phase})
+                    "divergence_max": div, "divergence_cell": ijk, "phase_ms": phase,
+                    "velocity_max": [v.absmax()[0] for v in self.vel]})
         return rec
 
     def fields(self):
