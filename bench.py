@@ -744,7 +744,9 @@ def timeloop(args):
 def full_loop(ctx, steps, solver_choice="compare"):
     """The full loop: the 512x128x128 channel on [0,4]x[0,1]^2 (8,388,608
     cells, h = 1/128), inflow u = 1, convective flux-balanced outflow,
-    free-slip walls (lagged zero-gradient tangential values), Re = 200,
+    no-slip walls (free-slip ones let the momentum right-hand side's
+    near-wall viscosity-gradient term, the reference's, accelerate the flow
+    without bound: no wall friction balances it), Re = 200,
     dt = 2e-3, the icosphere of radius 0.15 at (1, 0.5, 0.5) as 2,562 target
     markers, and a passive scalar (Schmidt 1) entering as a Gaussian blob of
     sigma 0.05 on the inlet, transported by the upwind operator under
@@ -758,7 +760,7 @@ def full_loop(ctx, steps, solver_choice="compare"):
 
     solvers = ("learned", "fp64") if solver_choice == "compare" else (solver_choice,)
     params, train = train_unet(ctx) if "learned" in solvers else (None, None)
-    base = tl.channel(512, 128, 128, re=200.0, tau=2e-3, outflow="convective", walls="free_slip")
+    base = tl.channel(512, 128, 128, re=200.0, tau=2e-3, outflow="convective", walls="no_slip")
     mk = tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4)
     runs = {}
     for solver in solvers:

@@ -161,7 +161,12 @@ def channel(nx, ny, nz, length=4.0, u_in=1.0, re=200.0, tau=2e-3, outflow="zero_
         the interior; the pressure is all-Neumann.
       walls="no_slip": zero tangential border values; "free_slip": the
         tangential components' border values follow the interior (a lagged
-        zero normal gradient)."""
+        zero normal gradient).  With free-slip walls the flow accelerates
+        without bound: the momentum right-hand side's viscous term
+        dVis . (dVel + dU) (XProblem.cpp:5352-5419) sees the face viscosity
+        drop to 0 on the border points, a forcing of the wall layer that no
+        wall friction balances (a property of the reference's
+        discretisation, reproduced by the CPU restatement)."""
     if outflow not in ("zero_gradient", "convective") or walls not in ("no_slip", "free_slip"):
         raise ValueError("outflow: zero_gradient | convective; walls: no_slip | free_slip")
     pshape = (nx + 2, ny + 2, nz + 2)
