@@ -104,6 +104,33 @@ def test_upwind_transport_solves(ctx):
         assert np.abs(x.download()[sm] - xt[sm]).max() <= 1e-6 * np.abs(xt[sm]).max()
 
 
+def test_jacobi_bicgstab_on_the_transport_operator(ctx):
+    """Right Jacobi preconditioning of BiCGStab: the same stop rule on the true residual, the manufactured
+    solution recovered, and fewer iterations than plain BiCGStab on a system whose border rows (semi-sums,
+    normal differences) are far from the Actual rows' scale."""
+    g, A, og, vel, rng = case(ctx, shape=(26, 22, 24), seed=13, tau=1e-3, D=0.02, flags=7)
+    sm = og.smask.astype(bool)
+    xt = np.where(sm, rng.standard_normal(g.shape), 0.0)
+    b = O.apply_advdiff(og, xt, *vel, 1e-3, 0.02, 7)
+    bv = g.vec(b)
+    its = {}
+    for pre in (capi.XF_PRECOND_NONE, capi.XF_PRECOND_JACOBI):
+        x = g.vec(np.zeros(g.shape))
+        st = xf.solve(A, x, bv, method=xf.XF_BICGSTAB, precond=pre, atol=1e-9 * np.abs(b).max())
+        assert st.status == capi.XF_OK, (pre, st.status)
+        got = x.download()
+        r = O.apply_advdiff(og, got, *vel, 1e-3, 0.02, 7) - b
+        assert np.abs(r[sm]).max() <= 1e-9 * np.abs(b).max() * 1.0001
+        assert np.abs(got[sm] - xt[sm]).max() <= 1e-5 * np.abs(xt[sm]).max()
+        its[pre] = st.iterations
+    assert its[capi.XF_PRECOND_JACOBI] < its[capi.XF_PRECOND_NONE], its
+    # the Laplace operator has no such table: refused
+    L = xf.Operator(g, xf.XF_OP_LAPLACE)
+    with pytest.raises(xf.XFError) as e:
+        xf.solve(L, g.vec(np.zeros(g.shape)), bv, method=xf.XF_BICGSTAB, precond=capi.XF_PRECOND_JACOBI)
+    assert e.value.status == capi.XF_ERR_UNSUPPORTED
+
+
 def test_advdiff_needs_coefficients(ctx):
     codes, nrm = wl.poisson_cube(8, 8, 8)
     sep = np.full(7, 1 / 7)

@@ -103,6 +103,9 @@ struct xf_op {
   // the exact form)
   mutable double* adc64 = nullptr;
   mutable int adc_valid = 0;
+  // and the inverse row diagonals (0 off the active set), for the Jacobi
+  // preconditioner of BiCGStab, refreshed with the table
+  mutable double* adj64 = nullptr;
   // device staging boxes of xf_solve_host, kept between calls
   xf_vec* host_x = nullptr;
   xf_vec* host_b = nullptr;

@@ -214,33 +214,43 @@ __global__ void k_rcg_update(double* __restrict__ xk, double* __restrict__ xk_1,
 // BiCGStab's vector steps come in two forms: the reference's steps (EXACT,
 // for XF_EXACT solves) and FMA forms with fewer FP64 operations (GB300's FP64
 // rate, not memory, bounds these passes).
-// XSLAE.cpp:723-727: Pn1 = Rn + bn*(Pn - wn*Vn).
+// XSLAE.cpp:723-727: Pn1 = Rn + bn*(Pn - wn*Vn).  With a Jacobi
+// preconditioner (dinv non-null) also Ph = dinv Pn1, the vector A sees.
 template <bool EXACT>
 __global__ void k_bcgs_p(double* __restrict__ Pn1, const double* __restrict__ Rn, const double* __restrict__ Pn,
-                         const double* __restrict__ Vn, const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+                         const double* __restrict__ Vn, const uint8_t* __restrict__ m, int64_t n, DevScratch* S,
+                         const double* __restrict__ dinv, double* __restrict__ Ph) {
   GUARD_DONE(S);
   const double wn = S->scalars[D_WN], bn = S->scalars[D_BN];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (!m[i]) continue;
+    double p;
     if (EXACT) {
       double t = wn * Vn[i];
       t = Pn[i] - t;
       t = bn * t;
-      Pn1[i] = Rn[i] + t;
+      p = Rn[i] + t;
     } else {
-      Pn1[i] = fma(bn, fma(-wn, Vn[i], Pn[i]), Rn[i]);
+      p = fma(bn, fma(-wn, Vn[i], Pn[i]), Rn[i]);
     }
+    Pn1[i] = p;
+    if (dinv) Ph[i] = dinv[i] * p;
   }
 }
 
-// XSLAE.cpp:732-733: Sn = Rn - an*Vn.
+// XSLAE.cpp:732-733: Sn = Rn - an*Vn (and Sh = dinv Sn).
 template <bool EXACT>
 __global__ void k_bcgs_s(double* __restrict__ Sn, const double* __restrict__ Rn, const double* __restrict__ Vn,
-                         const uint8_t* __restrict__ m, int64_t n, DevScratch* S) {
+                         const uint8_t* __restrict__ m, int64_t n, DevScratch* S, const double* __restrict__ dinv,
+                         double* __restrict__ Sh) {
   GUARD_DONE(S);
   const double an = S->scalars[D_AN];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    if (m[i]) Sn[i] = EXACT ? Rn[i] - an * Vn[i] : fma(-an, Vn[i], Rn[i]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!m[i]) continue;
+    const double s = EXACT ? Rn[i] - an * Vn[i] : fma(-an, Vn[i], Rn[i]);
+    Sn[i] = s;
+    if (dinv) Sh[i] = dinv[i] * s;
+  }
 }
 
 __device__ __forceinline__ double max_nan_skip(double a, double b) { return b > a ? b : a; }
@@ -262,12 +272,15 @@ __device__ double block_max(double v, double* sh) {
 // XSLAE.cpp:738-749: Un += an*Pn1 + wn*Sn; Rn = Sn - wn*Tn; Pn = Pn1 (no
 // copy when Pn is null: the caller alternates the two direction buffers);
 // then ||Rn||_inf (NaN never wins, XSpace.cpp:3455-3463) with control `ctl`.
+// With a Jacobi preconditioner Un moves along the preconditioned vectors:
+// Un += an*Ph + wn*Sh (Xp, Xs; otherwise Pn1 and Sn).
 template <bool EXACT>
 __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ Un, double* __restrict__ Rn,
                                                           double* __restrict__ Pn, const double* __restrict__ Pn1,
                                                           const double* __restrict__ Sn, const double* __restrict__ Tn,
                                                           const uint8_t* __restrict__ m, int64_t n, DevScratch* S,
-                                                          int update, int ctl) {
+                                                          int update, int ctl, const double* __restrict__ Xp = nullptr,
+                                                          const double* __restrict__ Xs = nullptr) {
   __shared__ double sh[32];
   __shared__ bool last;
   if (update) GUARD_DONE(S);
@@ -277,8 +290,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ U
     if (!m[i]) continue;
     double r;
     if (update && EXACT) {
-      double tmp1 = an * Pn1[i];
-      double tmp2 = tmp1 + wn * Sn[i];
+      double tmp1 = an * (Xp ? Xp[i] : Pn1[i]);
+      double tmp2 = tmp1 + wn * (Xs ? Xs[i] : Sn[i]);
       Un[i] = Un[i] + tmp2;
       double t = wn * Tn[i];
       r = Sn[i] - t;
@@ -286,7 +299,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_bcgs_end(double* __restrict__ U
       if (Pn) Pn[i] = Pn1[i];
     } else if (update) {
       const double sn = Sn[i];
-      Un[i] = Un[i] + fma(an, Pn1[i], wn * sn);
+      Un[i] = Un[i] + fma(an, Xp ? Xp[i] : Pn1[i], wn * (Xs ? Xs[i] : sn));
       r = fma(-wn, Tn[i], sn);
       Rn[i] = r;
       if (Pn) Pn[i] = Pn1[i];
@@ -776,6 +789,23 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     xf_mv64(op, q0);
     XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     k_bcgs_end<true><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
+    // Jacobi (XF_PRECOND_JACOBI, advection-diffusion operators): right
+    // preconditioning by the inverse row diagonals, so A sees dinv p and
+    // dinv s, x moves along them, and the residual stays b - A x.  It evens
+    // out rows of very different scales (semi-sums of 1/2, normal differences
+    // of 1/h, Actual rows of 1/tau and more).
+    const double* dinv = nullptr;
+    double *Ph = nullptr, *Sh = nullptr;
+    if (o.precond == XF_PRECOND_JACOBI) {
+      if (op->kind != XF_OP_ADVDIFF || !op->adc_valid || !op->adj64)
+        return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: Jacobi BiCGStab takes an advection-diffusion operator");
+      dinv = op->adj64;
+      Ph = B.get<double>(n);
+      Sh = B.get<double>(n);
+      if (!Ph || !Sh) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    } else if (o.precond != XF_PRECOND_NONE) {
+      return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: BiCGStab takes XF_PRECOND_JACOBI or none");
+    }
     // the previous direction and the new one alternate between Pn and Pn1 with
     // the iteration's parity (chunks of an even number of iterations)
     even_chunks = true;
@@ -783,20 +813,20 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
       double* Pold = (it & 1) ? Pn1 : Pn;
       double* Pnew = (it & 1) ? Pn : Pn1;
       k_dot_ctl<double><<<rb, RED_THREADS, 0, ctx->stream>>>(sRn, Rn, m, n, S, SL_A, CTL_BCGS_PN1, 1);
-      if (exact) k_bcgs_p<true><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
-      else k_bcgs_p<false><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S);
+      if (exact) k_bcgs_p<true><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S, dinv, Ph);
+      else k_bcgs_p<false><<<eb, 256, 0, ctx->stream>>>(Pnew, Rn, Pold, Vn, m, n, S, dinv, Ph);
       MvReq<double> a;
-      a.x = Pnew; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
+      a.x = dinv ? Ph : Pnew; a.y = Vn; a.w = sRn; a.exact = exact; a.slot = SL_A; a.ctl = CTL_BCGS_AN;
       xf_mv64(op, a);
-      if (exact) k_bcgs_s<true><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
-      else k_bcgs_s<false><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S);
+      if (exact) k_bcgs_s<true><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S, dinv, Sh);
+      else k_bcgs_s<false><<<eb, 256, 0, ctx->stream>>>(Sn, Rn, Vn, m, n, S, dinv, Sh);
       MvReq<double> c;
-      c.x = Sn; c.y = Tn; c.w = Sn; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_BCGS_WN;
+      c.x = dinv ? Sh : Sn; c.y = Tn; c.w = Sn; c.dot_self = 1; c.exact = exact; c.slot = SL_A; c.ctl = CTL_BCGS_WN;
       xf_mv64(op, c);
       if (exact) k_bcgs_end<true><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1,
-                                                                        CTL_BCGS_END);
+                                                                        CTL_BCGS_END, Ph, Sh);
       else k_bcgs_end<false><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, nullptr, Pnew, Sn, Tn, m, n, S, 1,
-                                                                  CTL_BCGS_END);
+                                                                  CTL_BCGS_END, Ph, Sh);
     };
   } else if (o.method == XF_MINRES) {
     if (eps <= 0) eps = 1e-7;   // XSLAE.cpp:358

@@ -233,6 +233,30 @@ __global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, const double* __re
   }
 }
 
+// A unit probe at the row's own cell: a border row evaluated on it is the
+// row's diagonal coefficient.
+struct UnitProbe {
+  __device__ __forceinline__ double operator()(int a, int b, int d) const { return (a | b | d) == 0 ? 1.0 : 0.0; }
+};
+
+// Inverse row diagonals of the fast rows (Actual: the table's centre; border
+// rows: the row on a unit probe), 0 off the active set and where a diagonal
+// is 0.
+__global__ void k_ad_jacobi(StencilGrid<double> g, int64_t n, const double* __restrict__ table,
+                            double* __restrict__ dinv) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int row = row_of(g.kind[c]);
+    double d = 0;
+    if (row == ROW_ACTUAL) {
+      d = table[c];
+    } else if (row != ROW_NONE) {
+      const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
+      d = boundary_row_acc<double, false>(g, UnitProbe{}, i, j, k, (int)c, row);
+    }
+    dinv[c] = d != 0 ? 1.0 / d : 0.0;
+  }
+}
+
 template <typename T>
 static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   const xf_grid* g = op->g;
@@ -339,6 +363,7 @@ extern "C" int xf_op_destroy(xf_op* op) {
   if (op->adD64) cudaFree(op->adD64);
   if (op->adD32) cudaFree(op->adD32);
   if (op->adc64) cudaFree(op->adc64);
+  if (op->adj64) cudaFree(op->adj64);
   if (op->pack) xf_pack_free(op->pack);
   if (op->host_x) xf_vec_destroy(op->host_x);
   if (op->host_b) xf_vec_destroy(op->host_b);
@@ -378,7 +403,8 @@ extern "C" int xf_op_set_advection(xf_op* op, const xf_vec* u, const xf_vec* v, 
   const int64_t n = op->g->ncell;
   op->adc_valid = 0;
   const int64_t nax = 5 * ((int64_t)op->g->n1 + op->g->n2 + op->g->n3);   // per-axis factors after the table
-  if (!op->adc64 && cudaMalloc(&op->adc64, (7 * n + nax) * 8) != cudaSuccess) {
+  if ((!op->adc64 && cudaMalloc(&op->adc64, (7 * n + nax) * 8) != cudaSuccess) ||
+      (!op->adj64 && cudaMalloc(&op->adj64, n * 8) != cudaSuccess)) {
     cudaGetLastError();
     return xf_fail(ctx, XF_ERR_NOMEM, "xf_op_set_advection: allocation");
   }
@@ -443,6 +469,7 @@ int xf_op_ready(const xf_op* op) {
     k_ad_axis<<<1, 256, 0, ctx->stream>>>(g->hy, g->n2, ty);
     k_ad_axis<<<1, 256, 0, ctx->stream>>>(g->hz, g->n3, tz);
     k_ad_coeffs<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, tx, ty, tz, op->adc64);
+    k_ad_jacobi<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, op->adc64, op->adj64);
     XF_CUDA(ctx, cudaGetLastError());
     op->adc_valid = 1;
   }
