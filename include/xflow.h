@@ -230,11 +230,12 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
  * lambda s p(lambda) is closest to 1 on its interval.  Uniform Laplace grids
  * without boundary rows. */
 /* XF_PRECOND_JACOBI: with xf_solve_fcg, the Laplace diagonal; with
- * XF_BICGSTAB on an XF_OP_ADVDIFF operator, right preconditioning by the
- * inverse row diagonals (the fast rows' centre coefficients, the border rows'
- * own diagonals): the residual and the stop rule stay those of A x = b, and
- * rows of very different scales (semi-sums, normal differences, Actual rows of
- * 1/tau and more) no longer slow the iteration down. */
+ * XF_BICGSTAB on an XF_OP_LAPLACE or XF_OP_ADVDIFF operator, right
+ * preconditioning by the inverse row diagonals (the Actual rows' diagonals,
+ * the border rows' own): the residual and the stop rule stay those of
+ * A x = b, and rows of very different scales (semi-sums of 1/2, normal
+ * differences of 1/h, Actual rows of 1/h^2 or 1/tau) no longer slow the
+ * iteration down. */
 enum { XF_PRECOND_NONE = 0, XF_PRECOND_JACOBI = 1, XF_PRECOND_UNET = 2, XF_PRECOND_CHEB = 3, XF_PRECOND_UNET2 = 4 };
 /* Host only (no device work): the XF_PRECOND_CHEB polynomial as the solver
  * builds it, in powers of A.  degree 2 writes its three Horner coefficients

@@ -124,10 +124,23 @@ def test_jacobi_bicgstab_on_the_transport_operator(ctx):
         assert np.abs(got[sm] - xt[sm]).max() <= 1e-5 * np.abs(xt[sm]).max()
         its[pre] = st.iterations
     assert its[capi.XF_PRECOND_JACOBI] < its[capi.XF_PRECOND_NONE], its
-    # the Laplace operator has no such table: refused
+    # the Laplace operator of the same grid (Dirichlet faces: semi-sum rows beside rows of 1/h^2)
     L = xf.Operator(g, xf.XF_OP_LAPLACE)
+    bl = O.apply(O.LAPLACE, og, xt)
+    blv = g.vec(bl)
+    its = {}
+    for pre in (capi.XF_PRECOND_NONE, capi.XF_PRECOND_JACOBI):
+        x = g.vec(np.zeros(g.shape))
+        st = xf.solve(L, x, blv, method=xf.XF_BICGSTAB, precond=pre, atol=1e-9 * np.abs(bl).max())
+        assert st.status == capi.XF_OK, (pre, st.status)
+        assert np.abs(x.download()[sm] - xt[sm]).max() <= 1e-4 * np.abs(xt[sm]).max()
+        its[pre] = st.iterations
+    assert its[capi.XF_PRECOND_JACOBI] < its[capi.XF_PRECOND_NONE], its
+    # the variable-density operator has no diagonal table: refused
+    V = xf.Operator(g, xf.XF_OP_VARDIV)
+    V.set_density(np.ones(g.shape))
     with pytest.raises(xf.XFError) as e:
-        xf.solve(L, g.vec(np.zeros(g.shape)), bv, method=xf.XF_BICGSTAB, precond=capi.XF_PRECOND_JACOBI)
+        xf.solve(V, g.vec(np.zeros(g.shape)), blv, method=xf.XF_BICGSTAB, precond=capi.XF_PRECOND_JACOBI)
     assert e.value.status == capi.XF_ERR_UNSUPPORTED
 
 

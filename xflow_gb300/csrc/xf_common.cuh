@@ -106,6 +106,7 @@ struct xf_op {
   // and the inverse row diagonals (0 off the active set), for the Jacobi
   // preconditioner of BiCGStab, refreshed with the table
   mutable double* adj64 = nullptr;
+  mutable int lap_jac_valid = 0;   // XF_OP_LAPLACE: adj64 holds its inverse diagonals (built on first use)
   // device staging boxes of xf_solve_host, kept between calls
   xf_vec* host_x = nullptr;
   xf_vec* host_b = nullptr;

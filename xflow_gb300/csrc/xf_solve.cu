@@ -48,6 +48,7 @@ void xf_cg_poly_second_launch(const xf_op* op, const float* w, const float* r, f
 void xf_cg_pq32_variant(const xf_op* op, const float* r, float* pb0, float* pb1, float* q, int variant);
 bool xf_cg_pqt_supported(const xf_grid* g);
 int xf_op_ready(const xf_op* op);
+int xf_op_jacobi(const xf_op* op, const double** dinv);
 
 #define GUARD_DONE(S) \
   if ((S)->iscalars[I_DONE]) return;
@@ -789,7 +790,7 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     xf_mv64(op, q0);
     XF_CUDA(ctx, cudaMemcpyAsync(sRn, Rn, n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     k_bcgs_end<true><<<rb, RED_THREADS, 0, ctx->stream>>>(x, Rn, Pn, Pn1, Sn, Tn, m, n, S, 0, CTL_BCGS_NORM0);
-    // Jacobi (XF_PRECOND_JACOBI, advection-diffusion operators): right
+    // Jacobi (XF_PRECOND_JACOBI; Laplace and advection-diffusion operators): right
     // preconditioning by the inverse row diagonals, so A sees dinv p and
     // dinv s, x moves along them, and the residual stays b - A x.  It evens
     // out rows of very different scales (semi-sums of 1/2, normal differences
@@ -797,9 +798,8 @@ static int solve_reference(xf_op* op, const xf_solve_opts& o, xf_vec* xv, const 
     const double* dinv = nullptr;
     double *Ph = nullptr, *Sh = nullptr;
     if (o.precond == XF_PRECOND_JACOBI) {
-      if (op->kind != XF_OP_ADVDIFF || !op->adc_valid || !op->adj64)
-        return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: Jacobi BiCGStab takes an advection-diffusion operator");
-      dinv = op->adj64;
+      int js = xf_op_jacobi(op, &dinv);
+      if (js) return js;
       Ph = B.get<double>(n);
       Sh = B.get<double>(n);
       if (!Ph || !Sh) return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");

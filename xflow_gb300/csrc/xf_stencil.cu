@@ -257,6 +257,48 @@ __global__ void k_ad_jacobi(StencilGrid<double> g, int64_t n, const double* __re
   }
 }
 
+// The Laplace operator's inverse row diagonals (Actual: the fast row's
+// diagonal; border rows: the row on a unit probe), 0 off the active set.
+__global__ void k_lap_jacobi(StencilGrid<double> g, int64_t n, const double* __restrict__ diag,
+                             double* __restrict__ dinv) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int row = row_of(g.kind[c]);
+    double d = 0;
+    if (row == ROW_ACTUAL) {
+      d = diag[c];
+    } else if (row != ROW_NONE) {
+      const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
+      d = boundary_row_acc<double, false>(g, UnitProbe{}, i, j, k, (int)c, row);
+    }
+    dinv[c] = d != 0 ? 1.0 / d : 0.0;
+  }
+}
+
+// The inverse row diagonals of a Laplace or advection-diffusion operator
+// (the latter refreshed by xf_op_ready), for Jacobi-preconditioned BiCGStab.
+int xf_op_jacobi(const xf_op* op, const double** dinv) {
+  xf_ctx* ctx = op->g->ctx;
+  if (op->kind == XF_OP_ADVDIFF && op->adc_valid && op->adj64) {
+    *dinv = op->adj64;
+    return XF_OK;
+  }
+  if (op->kind != XF_OP_LAPLACE)
+    return xf_fail(ctx, XF_ERR_UNSUPPORTED, "xf_solve: Jacobi BiCGStab takes a Laplace or advection-diffusion operator");
+  const int64_t n = op->g->ncell;
+  if (!op->lap_jac_valid) {
+    if (!op->adj64 && cudaMalloc(&op->adj64, n * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return xf_fail(ctx, XF_ERR_NOMEM, "xf_solve: allocation");
+    }
+    StencilGrid<double> s = make_stencil_grid<double>(op->g, nullptr);
+    k_lap_jacobi<<<grid_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(s, n, op->g->diag, op->adj64);
+    XF_CUDA(ctx, cudaGetLastError());
+    op->lap_jac_valid = 1;
+  }
+  *dinv = op->adj64;
+  return XF_OK;
+}
+
 template <typename T>
 static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   const xf_grid* g = op->g;
