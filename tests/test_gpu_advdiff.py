@@ -136,11 +136,10 @@ def test_jacobi_bicgstab_on_the_transport_operator(ctx):
         assert np.abs(x.download()[sm] - xt[sm]).max() <= 1e-4 * np.abs(xt[sm]).max()
         its[pre] = st.iterations
     assert its[capi.XF_PRECOND_JACOBI] < its[capi.XF_PRECOND_NONE], its
-    # the variable-density operator has no diagonal table: refused
-    V = xf.Operator(g, xf.XF_OP_VARDIV)
-    V.set_density(np.ones(g.shape))
+    # a packed operator has no diagonal table: refused
+    P = xf.PackedOperator(L)
     with pytest.raises(xf.XFError) as e:
-        xf.solve(V, g.vec(np.zeros(g.shape)), blv, method=xf.XF_BICGSTAB, precond=capi.XF_PRECOND_JACOBI)
+        xf.solve(P, g.vec(np.zeros(g.shape)), blv, method=xf.XF_BICGSTAB, precond=capi.XF_PRECOND_JACOBI)
     assert e.value.status == capi.XF_ERR_UNSUPPORTED
 
 
