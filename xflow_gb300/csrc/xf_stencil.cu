@@ -233,6 +233,73 @@ __global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, const double* __re
   }
 }
 
+// The fast FP64 advection-diffusion apply as a flat grid-stride kernel: a
+// thread takes cell after cell (the row reads its seven coefficients and its
+// neighbours directly, so the plane march buys nothing), at full occupancy.
+// Same results, dots and control step as k_matvec's fast rows.
+constexpr int AD_THREADS = 256;
+// The border rows, out of line: they are few, and inlined they would set the
+// register budget of the whole loop.
+__device__ __noinline__ double ad_border_row(const StencilGrid<double>& g, const double* __restrict__ x, int64_t c,
+                                             int row) {
+  const int64_t s1 = g.s1, s2 = g.s2;
+  const int i = (int)(c / s1), j = (int)((c - (int64_t)i * s1) / s2), k = (int)(c % s2);
+  return boundary_row<double, false>(g, x, i, j, k, (int)c, row);
+}
+
+__global__ void __launch_bounds__(AD_THREADS, 4) k_ad_fast(MatvecArgs<double> a) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (a.ctl != CTL_NONE && (a.S->iscalars[I_DONE] || (a.gate && !a.S->iscalars[I_NEEDREP]))) return;
+  const StencilGrid<double>& g = a.g;
+  const int64_t s1 = g.s1, s2 = g.s2, n = (int64_t)g.n1 * s1, nn = g.adc_n;
+  const double* __restrict__ x = a.x;
+  DotAcc<double> dw, ds;
+  for (int64_t c = blockIdx.x * (int64_t)AD_THREADS + threadIdx.x; c < n; c += (int64_t)gridDim.x * AD_THREADS) {
+    const int row = row_of(g.kind[c]);
+    if (row == ROW_NONE) {
+      if (a.zero_inactive) {
+        if (a.y) a.y[c] = 0.0;
+        if (a.y32) a.y32[c] = 0.f;
+      }
+      continue;
+    }
+    double v;
+    if (row == ROW_ACTUAL) {
+      const double* __restrict__ q = g.adc + c;
+      v = q[0] * x[c];
+      v = fma(q[nn], x[c - s1], v);
+      v = fma(q[2 * nn], x[c + s1], v);
+      v = fma(q[3 * nn], x[c - s2], v);
+      v = fma(q[4 * nn], x[c + s2], v);
+      v = fma(q[5 * nn], x[c - 1], v);
+      v = fma(q[6 * nn], x[c + 1], v);
+    } else {
+      v = ad_border_row(g, x, c, row);
+    }
+    if (a.sign > 0) v = v + a.s[c];
+    else if (a.sign < 0) v = v - a.s[c];
+    if (a.neg) v = -v;
+    if (a.dot_w) dw.add(a.w[c], v);
+    if (a.dot_self) ds.add(v, v);
+    if (a.y) a.y[c] = v;
+    if (a.y32) a.y32[c] = (float)v;
+  }
+  if (a.dot_w || a.dot_self || a.ctl != CTL_NONE) {
+    double vals[2] = {dw.value(), ds.value()};
+    if (publish_partials<2>(a.S, a.slot_w, vals, sh, &last)) {
+      double tw = finish_partials(a.S, a.slot_w, sh);
+      double ts = finish_partials(a.S, a.slot_w + 1, sh);
+      if (threadIdx.x == 0) {
+        if (a.dot_w) a.S->scalars[a.slot_w] = tw;
+        if (a.dot_self) a.S->scalars[a.slot_w + 1] = ts;
+        a.S->tickets[a.slot_w] = 0;
+        control_step(a.S, a.ctl);
+      }
+    }
+  }
+}
+
 // A unit probe at the row's own cell: a border row evaluated on it is the
 // row's diagonal coefficient.
 struct UnitProbe {
@@ -321,6 +388,12 @@ static void launch_matvec(const xf_op* op, const T* rho, const MvReq<T>& q) {
   const bool use_d = std::is_same<T, double>::value && op->kind == XF_OP_LAPLACE && !q.exact;
   if (op->kind == XF_OP_ADVDIFF) {
     set_ad_fields<T>(a.g, op);
+    if constexpr (std::is_same<T, double>::value) {
+      if (!q.exact && a.g.adc) {
+        k_ad_fast<<<grid_blocks(ctx, g->ncell, AD_THREADS), AD_THREADS, 0, ctx->stream>>>(a);
+        return;
+      }
+    }
     if (q.exact) k_matvec<T, XF_OP_ADVDIFF, true, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     else k_matvec<T, XF_OP_ADVDIFF, false, false><<<grid, MV_THREADS, 0, ctx->stream>>>(a);
     return;
