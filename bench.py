@@ -421,6 +421,11 @@ def main(argv=None):
     st_plain = one(xf.XF_PREC_MIXED)
     one(xf.XF_PREC_MIXED, **cheb)
     cheb_sts = [one(xf.XF_PREC_MIXED, **cheb) for _ in range(3)]
+    # Jacobi-preconditioned FP64 CG (flexible CG with the Laplace diagonal, FCG(1)), the other comparator
+    jac = family_solvers(A, x, bv, None, ("jacobi_cg_fp64",))["jacobi_cg_fp64"]
+    # the learned solver with the same parameters on a fresh 128^3 geometry of the family, beside
+    # plain FP64 CG and Jacobi CG there
+    family128 = family_check(ctx, params, 128, SEED + 11)
 
     # one coarse network application, CUDA events on the context stream
     stream = torch.cuda.ExternalStream(capi_stream(ctx))
@@ -531,6 +536,8 @@ def main(argv=None):
         "mixed_cg_chebyshev": {"ms": float(np.mean([c.ms for c in cheb_sts])), "iterations": cheb_sts[-1].iterations,
                                "rel_resid": cheb_sts[-1].rel_resid,
                                "preconditioner": f"degree-{CHEB_DEGREE} Chebyshev, ratio {CHEB_RATIO}, no network"},
+        "jacobi_cg_fp64": jac,
+        "family_128": family128,
         "train": train,
         "coarse_unet": {"grid": f"{gc.shape[0] - 2}^3 (+ ghost layer)", "ms_per_apply": unet_ms,
                         "tflops_executed": unet_ex / (unet_ms * 1e-3) / 1e12},
@@ -818,6 +825,47 @@ UNET_TRAIN = dict(n=64, spheres=16, seed=5, rhs_seeds=tuple(range(200, 208)),
                   # `check_from` on are scored by the timed solver's iterations on a held-out
                   # system of the bench's family (another geometry and right-hand side)
                   check_from=1000, check_every=250, val_seed=7)
+
+
+def family_solvers(A, x, bv, net, which):
+    """Each solver of `which` once untimed, once timed, from x = 0 to RTOL on A x = b: "learned" (the
+    timed solver, with `net` on the coarse grid), "fp64_cg", "jacobi_cg_fp64"."""
+    import xflow_gb300 as xf
+    from xflow_gb300 import capi
+
+    calls = {
+        "learned": lambda: xf.solve_fcg(A, x, bv, unet=net, precond=capi.XF_PRECOND_UNET2, rtol=RTOL,
+                                        window=TL_WINDOW, degree=TL_DEGREE, ratio=TL_RATIO,
+                                        precision=xf.XF_PREC_MIXED),
+        "fp64_cg": lambda: xf.solve(A, x, bv, method=xf.XF_CG, precision=xf.XF_PREC_FP64, rtol=RTOL),
+        "jacobi_cg_fp64": lambda: xf.solve_fcg(A, x, bv, precond=capi.XF_PRECOND_JACOBI, rtol=RTOL, window=1),
+    }
+    out = {}
+    for k in which:
+        for _ in range(2):
+            x.fill(0.0)
+            st = calls[k]()
+        out[k] = {"ms": st.ms, "iterations": st.iterations, "rel_resid": st.rel_resid, "status": int(st.status)}
+        if k == "learned":
+            out[k]["fallbacks"] = st.fallbacks
+    return out
+
+
+def family_check(ctx, params, n, seed):
+    """The trained network on another system of the sphere family (n^3, a fresh geometry and right-hand
+    side): the learned solver beside plain FP64 CG and Jacobi CG."""
+    import xflow_gb300 as xf
+    from xflow_gb300 import workloads as wl
+
+    codes, _, _, sep, _ = wl.spheres_grid(n, N_SPHERES, 0.02, 0.06, seed)
+    b = wl.divergence_rhs(codes, (sep, sep, sep), seed + 1)
+    g = xf.Grid(ctx, codes, sep, sep, sep, None)
+    A = xf.Operator(g, xf.XF_OP_LAPLACE)
+    cc, c1, c2, c3 = wl.coarse_grid(codes, sep, TL_BLOCK)
+    net = xf.UNet(xf.Grid(ctx, cc, c1, c2, c3, None), params)
+    res = family_solvers(A, g.vec(np.zeros(g.shape)), g.vec(b), net, ("learned", "fp64_cg", "jacobi_cg_fp64"))
+    res["system"] = f"{n}^3, {N_SPHERES} spheres, seed {seed}"
+    return res
 
 
 def unet_flops(shape):
