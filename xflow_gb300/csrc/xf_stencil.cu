@@ -210,13 +210,62 @@ __device__ __forceinline__ void ad_coef_fast(const double* __restrict__ t, doubl
   }
 }
 
-// The FP64 coefficient table of the fast Actual rows: a centre coefficient
-// 1/tau + B_x + B_y + B_z and the six neighbour coefficients.
+// The border rows in the same seven-coefficient form (centre, x-, x+, y-,
+// y+, z-, z+): a semi-sum row takes 1/2 of itself and of its neighbour
+// against the normal (the last nonzero normal component decides, as the row
+// does); a normal-difference row with an axis-aligned normal is
+// n_a (f_c - f_{c-1}) / h (normal +) or n_a (f_{c+1} - f_c) / h (normal -),
+// its 4-point face averages collapsing to single cells.  A normal-difference
+// row with an oblique normal reaches beyond the seven points: NaN in the
+// centre sends it to the general row.
+__device__ void ad_border_coeffs(const StencilGrid<double>& g, int64_t c, int row, double q[7]) {
+  for (int t = 0; t < 7; t++) q[t] = 0.0;
+  const int b = g.brow_of[c];
+  const double nrm[3] = {g.brow_nrm[3 * b], g.brow_nrm[3 * b + 1], g.brow_nrm[3 * b + 2]};
+  if (row == ROW_PREDEF) {
+    int ax = -1;
+    for (int a = 0; a < 3; a++)
+      if (nrm[a] != 0) ax = a;
+    if (ax < 0) return;   // no normal: the row is 0
+    q[0] = 0.5;
+    q[1 + 2 * ax + (nrm[ax] > 0 ? 0 : 1)] = 0.5;
+    return;
+  }
+  int ax = -1, cnt = 0;
+  for (int a = 0; a < 3; a++)
+    if (nrm[a] != 0) { ax = a; cnt++; }
+  if (cnt == 0) return;   // the row is 0
+  if (cnt > 1) { q[0] = __longlong_as_double(0x7ff8000000000000ll); return; }
+  const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
+  const int m = ax == 0 ? i : ax == 1 ? j : k;
+  const double* h = ax == 0 ? g.hx : ax == 1 ? g.hy : g.hz;
+  const double na = nrm[ax];
+  if (na > 0) {
+    const double r = na / h[m - 1];
+    q[0] = r;
+    q[1 + 2 * ax] = -r;
+  } else {
+    const double r = na / h[m];
+    q[0] = -r;
+    q[2 + 2 * ax] = r;
+  }
+}
+
+// The FP64 coefficient table of the fast rows: for Actual rows a centre
+// coefficient 1/tau + B_x + B_y + B_z and the six neighbour coefficients;
+// border rows as ad_border_coeffs.
 __global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, const double* __restrict__ tx,
                             const double* __restrict__ ty, const double* __restrict__ tz, double* __restrict__ out) {
   const bool up = g.ad_upwind != 0;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-    if (row_of(g.kind[c]) != ROW_ACTUAL) continue;
+    const int row = row_of(g.kind[c]);
+    if (row == ROW_NONE) continue;
+    if (row != ROW_ACTUAL) {
+      double q[7];
+      ad_border_coeffs(g, c, row, q);
+      for (int t = 0; t < 7; t++) out[t * n + c] = q[t];
+      continue;
+    }
     const int i = (int)(c / g.s1), j = (int)((c - (int64_t)i * g.s1) / g.s2), k = (int)(c % g.s2);
     const double D = g.adDf ? g.adDf[c] : g.ad_D;
     double Ax, Bx, Cx, Ay, By, Cy, Az, Bz, Cz;
@@ -236,7 +285,10 @@ __global__ void k_ad_coeffs(StencilGrid<double> g, int64_t n, const double* __re
 // The fast FP64 advection-diffusion apply as a flat grid-stride kernel: a
 // thread takes cell after cell (the row reads its seven coefficients and its
 // neighbours directly, so the plane march buys nothing), at full occupancy.
-// Same results, dots and control step as k_matvec's fast rows.
+// Border rows read the table too (their semi-sums and axis-aligned normal
+// differences are seven-point rows), so a warp that holds a face cell does
+// not wait on the general border row; only oblique normal differences take
+// it.  Same dots and control step as k_matvec.
 constexpr int AD_THREADS = 256;
 // The border rows, out of line: they are few, and inlined they would set the
 // register budget of the whole loop.
@@ -265,16 +317,25 @@ __global__ void __launch_bounds__(AD_THREADS, 4) k_ad_fast(MatvecArgs<double> a)
       continue;
     }
     double v;
-    if (row == ROW_ACTUAL) {
-      const double* __restrict__ q = g.adc + c;
-      v = q[0] * x[c];
+    const double* __restrict__ q = g.adc + c;
+    const double q0 = q[0];
+    if (row == ROW_ACTUAL) {   // interior: all six neighbours are inside the box
+      v = q0 * x[c];
       v = fma(q[nn], x[c - s1], v);
       v = fma(q[2 * nn], x[c + s1], v);
       v = fma(q[3 * nn], x[c - s2], v);
       v = fma(q[4 * nn], x[c + s2], v);
       v = fma(q[5 * nn], x[c - 1], v);
       v = fma(q[6 * nn], x[c + 1], v);
-    } else {
+    } else if (q0 == q0) {   // a border row from the table: it reads only its nonzero neighbours
+      const int64_t off[6] = {-s1, s1, -s2, s2, -1, 1};
+      v = q0 * x[c];
+#pragma unroll
+      for (int t = 0; t < 6; t++) {
+        const double qt = q[(t + 1) * nn];
+        if (qt != 0) v = fma(qt, x[c + off[t]], v);
+      }
+    } else {   // an oblique normal difference
       v = ad_border_row(g, x, c, row);
     }
     if (a.sign > 0) v = v + a.s[c];
