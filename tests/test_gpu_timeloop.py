@@ -138,3 +138,33 @@ def test_learned_and_mixed_pressure_solves_stay_on_the_fp64_trajectory():
             assert np.abs(runs[solver][4] - ref[4]).max() <= 1e-6, solver
     finally:
         ctx.close()
+
+
+def test_outflow_pass_matches_its_cpu_restatement():
+    """xf_outflow_convective against tests/timeloop_cpu.py's restatement on a non-uniform state: the upwind
+    step and the common shift agree to rounding (the device sums in a fixed tree, numpy in its own order), and
+    the outlet's area-weighted flux equals the inlet's."""
+    import timeloop_cpu
+
+    ctx = xf.Context(0)
+    try:
+        st = tl.channel(24, 10, 12, outflow="convective")
+        codes, nrm, bc = st["comps"][0]
+        hp = st["p"][3]
+        h = [0.5 * (hp[0][:-1] + hp[0][1:]), hp[1], hp[2]]
+        g = xf.Grid(ctx, codes, *h, nrm)
+        rng = np.random.Generator(np.random.PCG64(21))
+        vel = np.where(codes == tl.ACTUAL, 1 + 0.3 * rng.standard_normal(codes.shape), 0.0)
+        bc = bc.copy()
+        bc[0, 1:-1, 1:-1] = 1 + 0.2 * rng.standard_normal(bc[0, 1:-1, 1:-1].shape)
+        bc[-1, 1:-1, 1:-1] = 1 + 0.2 * rng.standard_normal(bc[-1, 1:-1, 1:-1].shape)
+        bv = g.vec(bc)
+        xf.outflow_convective(g.vec(vel), bv, 1, 1.0, st["tau"])
+        got = bv.download()
+        want = bc.copy()
+        timeloop_cpu.outflow_convective(codes, vel, want, h, 1, 1.0, st["tau"])
+        assert np.abs(got - want).max() <= 1e-14 * np.abs(want).max()
+        np.testing.assert_array_equal(got[:-1], bc[:-1])   # only the outlet face changes
+        assert abs(got[-1, 1:-1, 1:-1].sum() - got[0, 1:-1, 1:-1].sum()) <= 1e-12 * got[0].sum()
+    finally:
+        ctx.close()
