@@ -720,23 +720,26 @@ def rows(args):
 # 3000 Adam steps with the learning rate halved every 1000 steps
 def timeloop(args):
     """The time step of TVPProblem::SolveBySplitting on the GPU
-    (xflow_gb300.timeloop): momentum by the implicit transfer operator under
-    BiCGStab, pressure by mixed-precision CG (the cavity's all-Neumann system)
-    or BiCGStab (the channel's outlet rows), correction and control balance,
-    all FP64 but the cavity's pressure solve.  One JSON line per statement:
-    per-step ms (wall, synchronised; the first step, which builds the solver
-    graphs, apart), iterations and the control balance of the last step."""
+    (xflow_gb300.timeloop), configs 1 and 2 all in FP64: momentum by the
+    implicit transfer operator under Jacobi BiCGStab, pressure by plain FP64
+    CG (both statements are all-Neumann: the cavity's walls, the channel's
+    Defined inflow and convective, flux-balanced outflow), correction and
+    control balance.  One JSON line per statement: per-step ms (wall,
+    synchronised; the first step, which builds the solver graphs, apart),
+    iterations and the control balance of the last step.  Then the full loop
+    (config 5, full_loop)."""
     import xflow_gb300 as xf
     from xflow_gb300 import timeloop as tl
 
     ctx = xf.Context(0)
     cases = (("lid-driven cavity", tl.cavity(64, re=100.0, tau=1e-3), None, 10),
-             ("channel with an immersed sphere", tl.channel(256, 64, 64, re=200.0, tau=2e-3),
+             ("channel with an immersed sphere",
+              tl.channel(256, 64, 64, re=200.0, tau=2e-3, outflow="convective", walls="no_slip"),
               tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4), 100))
     for label, st, mk, steps in (() if args.loop_only else cases):
-        loop = tl.SplittingLoop(ctx, st, markers=mk)
+        loop = tl.SplittingLoop(ctx, st, markers=mk, pressure_solver="fp64")
         recs = [loop.step() for _ in range(steps)]
-        line = {"mode": "time loop", "statement": st["name"], "steps": steps,
+        line = {"mode": "time loop", "statement": st["name"], "steps": steps, "pressure": "FP64 CG",
                 "markers": None if mk is None else int(len(mk["pos"])),
                 "first_step_ms": recs[0]["ms"], "ms_per_step": float(np.mean([r["ms"] for r in recs[1:]])),
                 "momentum_iterations_mean": float(np.mean([r["momentum_iterations"] for r in recs])),
