@@ -769,7 +769,8 @@ def full_loop(ctx, steps, solver_choice="compare"):
     from xflow_gb300 import timeloop as tl
 
     solvers = ("learned", "fp64") if solver_choice == "compare" else (solver_choice,)
-    params, train = train_unet(ctx) if "learned" in solvers else (None, None)
+    # the network trained on the channel family (its pressure box at 128x32x32, the coarse grid's own shape)
+    params, train = train_unet(ctx, family="channel") if "learned" in solvers else (None, None)
     base = tl.channel(512, 128, 128, re=200.0, tau=2e-3, outflow="convective", walls="no_slip")
     mk = tl.sphere_markers((1.0, 0.5, 0.5), 0.15, 4)
     runs = {}
@@ -890,27 +891,44 @@ def unet_flops(shape):
     return ex, us
 
 
-def train_unet(ctx):
+def channel_codes(nx, ny, nz):
+    """Point codes and separations (hx, hy, hz) of the channel's all-Neumann pressure box (the
+    convective-outflow statement of the time loop: Actual interior, Fictive walls, inflow and outlet)."""
+    from xflow_gb300 import timeloop as tl
+
+    st = tl.channel(nx, ny, nz, outflow="convective", walls="no_slip")
+    return st["p"][0], tuple(st["p"][3])
+
+
+def train_unet(ctx, family="spheres"):
     """Trains the U-Net on the GPU (this library's forward/backward kernels,
     Adam, the A-norm loss) on (residual, error) pairs harvested from plain
-    CG's own iterates on a 64^3 system of the bench's sphere family (16
-    spheres, another seed).  The training loss is a poor predictor of the
-    two-level solver's iterations, so checkpoints are scored by the solver
-    itself on a held-out 256^3 system of the family (another geometry and
-    right-hand side; never the timed one) and the best is kept.  Returns the
-    parameters and a description."""
+    CG's own iterates on a small system of a family: "spheres" (the bench's,
+    a 64^3 cube with 16 spheres, another seed) or "channel" (the time loop's
+    channel pressure box at 128x32x32, divergence right-hand sides).  The
+    training loss is a poor predictor of the two-level solver's iterations,
+    so checkpoints are scored by the solver itself on a held-out larger
+    system of the family (spheres: 256^3, another geometry and right-hand
+    side, never the timed one; channel: 256x64x64) and the best is kept.
+    Returns the parameters and a description."""
     import xflow_gb300 as xf
     from xflow_gb300 import capi
     from xflow_gb300 import workloads as wl
 
     T = UNET_TRAIN
     # the held-out system and its coarse grid
-    vcodes, _, _, vsep, _ = wl.spheres_grid(N_CELLS, N_SPHERES, 0.02, 0.06, SEED + T["val_seed"])
-    vb = wl.divergence_rhs(vcodes, (vsep, vsep, vsep), SEED + T["val_seed"] + 1)
-    vg = xf.Grid(ctx, vcodes, vsep, vsep, vsep, None)
+    if family == "channel":
+        vcodes, vseps = channel_codes(256, 64, 64)
+        held_out = "channel 256x64x64 pressure box, divergence right-hand side"
+    else:
+        vcodes, _, _, vsep, _ = wl.spheres_grid(N_CELLS, N_SPHERES, 0.02, 0.06, SEED + T["val_seed"])
+        vseps = (vsep, vsep, vsep)
+        held_out = f"{N_CELLS}^3, {N_SPHERES} spheres, seed {SEED + T['val_seed']}"
+    vb = wl.divergence_rhs(vcodes, vseps, SEED + T["val_seed"] + 1)
+    vg = xf.Grid(ctx, vcodes, *vseps, None)
     vA = xf.Operator(vg, xf.XF_OP_LAPLACE)
     vbv, vx = vg.vec(vb), vg.vec(np.zeros(vg.shape))
-    vcc, v1, v2, v3 = wl.coarse_grid(vcodes, vsep, TL_BLOCK)
+    vcc, v1, v2, v3 = wl.coarse_grid(vcodes, vseps[0], TL_BLOCK)
     vnet = xf.UNet(xf.Grid(ctx, vcc, v1, v2, v3, None), seed=1)
 
     def val_iters(params):
@@ -920,14 +938,21 @@ def train_unet(ctx):
                           degree=TL_DEGREE, ratio=TL_RATIO, precision=xf.XF_PREC_MIXED, maxit=2000)
         return st.iterations if st.status == capi.XF_OK and st.fallbacks == 0 else 10 ** 6
 
-    codes, nrm, _, sep, _ = wl.spheres_grid(T["n"], T["spheres"], 0.02, 0.06, T["seed"])
-    g = xf.Grid(ctx, codes, sep, sep, sep, nrm)
+    if family == "channel":
+        codes, seps = channel_codes(128, 32, 32)
+        nrm = None
+        grid_name = "channel 128x32x32 pressure box"
+    else:
+        codes, nrm, _, sep, _ = wl.spheres_grid(T["n"], T["spheres"], 0.02, 0.06, T["seed"])
+        seps = (sep, sep, sep)
+        grid_name = f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}"
+    g = xf.Grid(ctx, codes, *seps, nrm)
     A = xf.Operator(g)
     net = xf.UNet(g, seed=1)
     t0 = time.perf_counter()
     rs, es = [], []
     for s in T["rhs_seeds"]:
-        b = wl.divergence_rhs(codes, (sep,) * 3, s)
+        b = wl.divergence_rhs(codes, seps, s)
         r_, e_ = xf.harvest_pairs(A, g.vec(b), iters=T["iters"])
         rs += r_
         es += e_
@@ -948,11 +973,11 @@ def train_unet(ctx):
     t2 = time.perf_counter()
     net.set_params(best[2])
     last = float(np.mean([net.train_step(r, e, update=False, op=A) for r, e in zip(rs, es)]))
-    return best[2], {"grid": f"{T['n']}^3, {T['spheres']} spheres, seed {T['seed']}", "pairs": len(rs),
+    return best[2], {"grid": grid_name, "pairs": len(rs),
                      "steps": T["steps"], "lr": T["lr"], "lr_halvings": T["halvings"], "s": t2 - t1,
                      "harvest_s": t1 - t0, "anorm_loss_before": first, "anorm_loss_after": last,
-                     "selection": {"held_out": f"{N_CELLS}^3, {N_SPHERES} spheres, seed {SEED + T['val_seed']}",
-                                   "checkpoints": checks, "chosen_step": best[0], "held_out_iterations": best[1]}}
+                     "selection": {"held_out": held_out, "checkpoints": checks, "chosen_step": best[0],
+                                   "held_out_iterations": best[1]}}
 
 
 def learned(args):
